@@ -1,0 +1,295 @@
+"""Benchmark of the DE path on GB300: DE-traced Mrays/s of the Mandelbox
+wavefront path trace (1280x720, 64 spp, 4 bounces, 512 steps).
+
+  python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
+
+A step is one progressive pass of 8 samples per pixel over the whole frame
+(7,372,800 paths); the default K = 8 covers the full 64-spp image. `value` is
+device-timed (CUDA events on the library stream, max over ranks); `e2e` is the
+same metric through the public API with host buffers: a full render via
+Renderer.render (scene and graph uploaded from the host, film read back).
+With N > 1 (torchrun) every rank renders its own replica (the path has no
+exchange step; see the scaling note in the JSON line).
+"""
+from __future__ import annotations
+
+import argparse
+import json
+import os
+import statistics
+import subprocess
+import sys
+import threading
+import time
+
+ROOT = os.path.dirname(os.path.abspath(__file__))
+sys.path.insert(0, ROOT)
+
+METRIC = "DE-traced Mrays/s"
+UNIT = "Mrays/s"
+WORKLOAD = "mandelbox_pathtrace_1280x720_64spp_4bounce"
+SPP_PER_STEP = 8
+# Algorithmic FP32 flops (FMA = 2) of the Mandelbox form: per Iterate iteration
+# (box fold 6, |p| 5 + sqrt 1, trap |p| 5 + sqrt 1 + min, sphere fold 1 div + 4,
+# scale 4, add origin 4 = 31) and per DE evaluation outside the loop (query point
+# 6, NormFence 7 + sqrt 1, march update 15 = 29).
+FLOPS_PER_ITER = 31
+FLOPS_PER_EVAL = 29
+
+
+def dist_env():
+    n = int(os.environ.get("WORLD_SIZE", "1"))
+    r = int(os.environ.get("RANK", "0"))
+    lr = int(os.environ.get("LOCAL_RANK", "0"))
+    return n, r, lr
+
+
+class ClockSampler:
+    """nvidia-smi clock/throttle samples during the timed region."""
+
+    def __init__(self, index: int):
+        self.index = index
+        self.samples = []
+        self.proc = None
+
+    def __enter__(self):
+        q = ("clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.hw_slowdown,"
+             "clocks_event_reasons.hw_thermal_slowdown,clocks_event_reasons.sw_thermal_slowdown,"
+             "clocks_event_reasons.sw_power_cap")
+        try:
+            self.proc = subprocess.Popen(["nvidia-smi", "-i", str(self.index), f"--query-gpu={q}",
+                                          "--format=csv,noheader,nounits", "-lms", "200"],
+                                         stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (OSError, FileNotFoundError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) >= 7:
+                self.samples.append(parts)
+
+    def __exit__(self, *a):
+        if self.proc:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=2)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        if not self.samples:
+            return {"sm_mhz": None, "sm_max_mhz": None, "reasons": ["unavailable"]}
+        sm = [float(s[0]) for s in self.samples if s[0].replace(".", "").isdigit()]
+        mx = [float(s[1]) for s in self.samples if s[1].replace(".", "").isdigit()]
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        reasons = sorted({names[i] for s in self.samples for i in range(4) if s[3 + i].lower() == "active"})
+        return {"sm_mhz": statistics.median(sm) if sm else None, "sm_max_mhz": max(mx) if mx else None,
+                "reasons": reasons, "samples": len(self.samples)}
+
+
+def cpu_port_rate(seconds_target: float = 12.0):
+    """The oracle (FP32 restatement of the reference, all host cores) on a bounded
+    sample of the same frame: pixels on a stride, 8 spp. Returns (Mrays/s, sample)."""
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import numpy as np
+    import oracle  # the CPU restatement; used only as the baseline here
+
+    from syfrack_gb300 import workloads
+
+    scene = workloads.mandelbox_scene()
+    cfg = workloads.mandelbox_pathtrace_config()
+    og = oracle.OracleGraph(scene.graph)
+    threads = os.cpu_count() or 1
+    rng = np.random.default_rng(3)
+    n = 64
+    total_seg, total_t, used = 0, 0.0, 0
+    while total_t < seconds_target and n <= 65536:
+        pix = np.stack([rng.integers(0, cfg.width, n), rng.integers(0, cfg.height, n)], 1).astype(np.uint32)
+        t0 = time.perf_counter()
+        r = og.render(scene.desc(cfg.width, cfg.height), cfg.desc(), pix, 0, SPP_PER_STEP, precision=32,
+                      threads=threads)
+        dt = time.perf_counter() - t0
+        total_seg += r["segments"]
+        total_t += dt
+        used += n
+        n *= 2
+    return total_seg / total_t / 1e6, threads, f"{used} random pixels x {SPP_PER_STEP} spp of the frame, FP32"
+
+
+def run_reference(args):
+    n, rank, _ = dist_env()
+    if rank != 0:
+        return
+    rates = []
+    # warm-up then K bounded samples of the workload, each a separate measurement
+    cpu_port_rate(2.0)
+    for _ in range(args.steps):
+        rate, threads, sample = cpu_port_rate(max(3.0, 20.0 / max(args.steps, 1)))
+        rates.append(rate)
+    value = statistics.median(rates)
+    line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": n,
+            "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Mandelbox scene)",
+            "config": {"workload": WORKLOAD, "host_threads": threads},
+            "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                             "sample": sample + " (the reference is Rust/WGSL and cannot be built here; "
+                                                "timed: its C++ restatement in oracle/)"},
+            "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0, "d2h_bytes_per_step": 0}}
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args):
+    import ctypes as C
+
+    n_ranks, rank, local_rank = dist_env()
+    dist = None
+    if n_ranks > 1:
+        import torch
+        import torch.distributed as dist
+
+        torch.cuda.set_device(local_rank)
+        dist.init_process_group("nccl")
+
+    from syfrack_gb300 import GpuContext, Renderer, RenderSession, workloads
+    from syfrack_gb300._lib import check
+
+    ctx = GpuContext(device=local_rank if n_ranks > 1 else 0)
+    renderer = Renderer(ctx)
+    scene = workloads.mandelbox_scene()
+    spp_total = SPP_PER_STEP * (args.warmup + args.steps)
+    cfg = workloads.mandelbox_pathtrace_config(spp=spp_total, samples_per_dispatch=SPP_PER_STEP)
+    sess = RenderSession(renderer, scene, cfg)
+    if args.blocks_per_sm:
+        sess.set_launch(args.blocks_per_sm, args.threads)
+    tile = (0, 0, cfg.width, cfg.height)
+    peak = C.c_double()
+    check(ctx.lib.sf_device_fp32_peak(ctx.h, C.byref(peak)))
+
+    def step(k):
+        sess.dispatch((*tile, k * SPP_PER_STEP), SPP_PER_STEP)
+
+    for k in range(args.warmup):
+        step(k)
+    sess.sync(600000)
+    ctx.set_profiling(True)
+    ctx.reset_stats()
+    if dist:
+        dist.barrier()
+    # timed region: events on the library stream bracket the K steps
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    with ClockSampler(local_rank) as clocks:
+        torch.cuda.synchronize()
+        ev0.record(stream)
+        for k in range(args.warmup, args.warmup + args.steps):
+            step(k)
+        ev1.record(stream)
+        ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    status = sess.sync(600000)
+    st = ctx.stats()
+    segs = st["segments"]
+    if dist:
+        import torch
+
+        t = torch.tensor([ms, float(segs)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        ms_max, segs_all = float(mx[0]), float(t[1])
+    else:
+        ms_max, segs_all = ms, float(segs)
+    value = segs_all / (ms_max * 1e-3) / 1e6
+    # dominant kernel: the persistent trace kernel (CUDA events around each launch)
+    trace_ms = st["trace_ms"]
+    trace_launches = max(st["trace_launches"], 1)
+    flops = FLOPS_PER_ITER * st["de_iterations"] + FLOPS_PER_EVAL * st["de_evals"]
+    per_launch_flops = flops / trace_launches
+    avg_launch_s = trace_ms * 1e-3 / trace_launches
+    achieved = per_launch_flops / avg_launch_s / 1e12 if avg_launch_s > 0 else 0.0
+    ctx.set_profiling(False)
+    sess.close()
+
+    # end to end through the public API: a full 64-spp render from host descriptions
+    e2e_cfg = workloads.mandelbox_pathtrace_config(spp=SPP_PER_STEP * args.steps,
+                                                   samples_per_dispatch=SPP_PER_STEP)
+    ctx.reset_stats()
+    if dist:
+        dist.barrier()
+    t0 = time.perf_counter()
+    out = renderer.render(scene, e2e_cfg)
+    e2e_s = time.perf_counter() - t0
+    e2e_segs = ctx.stats()["segments"]
+    if dist:
+        t = torch.tensor([e2e_s, float(e2e_segs)], dtype=torch.float64, device="cuda")
+        mx = t.clone()
+        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+        dist.all_reduce(t, op=dist.ReduceOp.SUM)
+        e2e_s, e2e_segs = float(mx[0]), float(t[1])
+    e2e = e2e_segs / e2e_s / 1e6
+    px = e2e_cfg.width * e2e_cfg.height
+    d2h = px * (16 + 4 + 16)
+    h2d = C.sizeof(__import__("syfrack_gb300").abi.sf_scene_desc) + 4096
+
+    if rank == 0:
+        cpu = None
+        if n_ranks == 1 and not args.no_cpu_baseline:
+            rate, threads, sample = cpu_port_rate(12.0)
+            cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port", "sample": sample}
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": n_ranks, "steps": args.steps,
+            "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32",
+            "data": "synthetic (seeded Mandelbox scene; no dataset)",
+            "config": {"workload": WORKLOAD, "width": cfg.width, "height": cfg.height, "spp_per_step": SPP_PER_STEP,
+                       "paths_per_step": cfg.width * cfg.height * SPP_PER_STEP, "max_bounces": cfg.max_bounces,
+                       "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
+                       "l2": "inputs larger than L2 (path state 1.4 GB per step)",
+                       "segments_per_step": segs_all / args.steps,
+                       "pixel_samples_per_s": cfg.width * cfg.height * SPP_PER_STEP * args.steps * n_ranks
+                       / (ms_max * 1e-3)},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
+                    "d2h_bytes_per_step": d2h // args.steps, "call": "Renderer.render (full 64-spp frame)"},
+            "roofline": {"bound": "fp32", "kernel": "k_trace_path", "achieved": achieved, "peak": peak.value,
+                         "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
+                         "traffic": None, "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
+                         "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
+                         "de_evals_per_step": st["de_evals"] / args.steps,
+                         "de_iterations_per_step": st["de_iterations"] / args.steps},
+            "gpu_launches": st["launches"],
+            "status_word": status,
+            "clocks": clocks.summary(),
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+    if dist:
+        dist.barrier()
+        dist.destroy_process_group()
+    renderer = None
+    ctx.close()
+
+
+def main():
+    ap = argparse.ArgumentParser()
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=8)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
+    ap.add_argument("--blocks-per-sm", type=int, default=0)
+    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    args = ap.parse_args()
+    if args.impl == "reference":
+        run_reference(args)
+    else:
+        run_ours(args)
+
+
+if __name__ == "__main__":
+    main()

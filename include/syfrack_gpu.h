@@ -1,0 +1,339 @@
+/*
+ * syfrack_gpu.h -- C ABI of the GB300 (sm_103a) distance-estimator path.
+ *
+ * This header is the drop-in boundary for SyFrack's DE / sphere-trace /
+ * escape-time hot path. Each entry point names the reference interface it
+ * replaces (paths are relative to the SyFrack source tree). All functions
+ * return sf_status (SF_OK == 0); handles are opaque; buffers passed as plain
+ * pointers are caller-owned host memory unless the name says "device".
+ * No C++ exception crosses this boundary. One thread drives one handle.
+ *
+ * Arithmetic is IEEE binary32 on the device, like the reference's glam Vec3
+ * and WGSL f32 (crates/syfrack-core/src/scene/graph/eval.rs, shaders/*.wgsl).
+ */
+#ifndef SYFRACK_GPU_H
+#define SYFRACK_GPU_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+typedef int32_t sf_status;
+enum {
+    SF_OK = 0,
+    SF_ERR_INVALID = 1,      /* bad argument (null pointer, size, range)            */
+    SF_ERR_GRAPH = 2,        /* graph fails validation (cycle, ports, bounds)       */
+    SF_ERR_UNSUPPORTED = 3,  /* valid graph/scene using a feature not built on GPU  */
+    SF_ERR_CUDA = 4,         /* CUDA runtime error (message in sf_last_error)       */
+    SF_ERR_OOM = 5,          /* device allocation failed                            */
+    SF_ERR_TIMEOUT = 6,      /* bounded wait expired (renderer.rs:236 DISPATCH_TIMEOUT) */
+    SF_ERR_BUDGET = 7,       /* HBM admission budget exceeded                       */
+    SF_ERR_IO = 8,           /* checkpoint file could not be read or written        */
+    SF_ERR_CHECKPOINT = 9,   /* checkpoint corrupt or from another producer         */
+    SF_ERR_WAVEFRONT = 10,   /* wavefront invariant word non-zero (wavefront.rs:414-417) */
+    SF_ERR_NO_DEVICE = 11,   /* no CUDA device / extension not usable               */
+};
+
+/* Human-readable name of a status code. Never NULL. */
+const char* sf_status_string(sf_status status);
+/* Message of the last error on the calling thread ("" if none). */
+const char* sf_last_error(void);
+/* ABI version: (major << 16) | minor. */
+uint32_t sf_abi_version(void);
+
+/* ------------------------------------------------------------------ graph
+ * The form graph of crates/syfrack-core/src/scene/graph/mod.rs:444-451
+ * (Graph{nodes, links, safety, bounding_radius_hint}) passed flat.
+ * Node kinds keep the order of NodeKind (graph/mod.rs:105-257).
+ */
+enum sf_node_kind {
+    SF_NODE_INPUT = 0, SF_NODE_OUTPUT, SF_NODE_TRANSLATE, SF_NODE_ROTATE,
+    SF_NODE_SCALE, SF_NODE_SCALE_AXES, SF_NODE_MIRROR, SF_NODE_BOX_FOLD,
+    SF_NODE_BOX_FOLD_AXES, SF_NODE_SPHERE_INVERSION, SF_NODE_SPHERE_FOLD,
+    SF_NODE_ABS, SF_NODE_MENGER_FOLD, SF_NODE_KALEIDO, SF_NODE_POWER,
+    SF_NODE_ADD_ORIGIN, SF_NODE_ADD_SEED, SF_NODE_ADD_CONSTANT, SF_NODE_TWIST,
+    SF_NODE_BEND, SF_NODE_TILE, SF_NODE_REPEAT_FINITE, SF_NODE_ITERATE,
+    SF_NODE_TRAP, SF_NODE_SPHERE, SF_NODE_TORUS, SF_NODE_CYLINDER, SF_NODE_BOX,
+    SF_NODE_ROUND_BOX, SF_NODE_ROCK, SF_NODE_PLANE, SF_NODE_NORM_FENCE,
+    SF_NODE_BULB_FENCE, SF_NODE_MATERIAL_TAG, SF_NODE_BOUNDED,
+    SF_NODE_INSTANCES, SF_NODE_UNION, SF_NODE_INTERSECTION,
+    SF_NODE_SUBTRACTION, SF_NODE_SMOOTH_UNION, SF_NODE_SMOOTH_INTERSECTION,
+    SF_NODE_KIND_COUNT
+};
+/* Trap measures and modes: graph/mod.rs:82-101 (Measure, TrapMode). */
+enum sf_measure { SF_MEASURE_NORM = 0, SF_MEASURE_AXIS_X, SF_MEASURE_AXIS_Y,
+    SF_MEASURE_AXIS_Z, SF_MEASURE_PLANE_Y, SF_MEASURE_ANGLE_XY,
+    SF_MEASURE_ANGLE_XZ, SF_MEASURE_ANGLE_YZ, SF_MEASURE_LOG_NORM };
+enum sf_trap_mode { SF_TRAP_MINIMUM = 0, SF_TRAP_MAXIMUM, SF_TRAP_LAST };
+
+/*
+ * One node. Parameters per kind (f = floats, u = unsigned):
+ *   Translate f0..2 offset | Rotate f0..2 angles (deg) | Scale f0 factor
+ *   ScaleAxes f0..2 | Mirror f0..2 normal, f3 offset | BoxFold f0 limit
+ *   BoxFoldAxes f0..2 limit, u0..2 x/y/z | SphereInversion f0 radius f1 min_radius
+ *   SphereFold f0 min_radius f1 fixed_radius | Abs u0..2 | MengerFold f0 scale f1..3 offset
+ *   Kaleido u0 planes f0 phase (deg) | Power f0 power | AddSeed f0..2 multiplier
+ *   AddConstant f0..2 multiplier f3..5 julia | Twist/Bend f0 rate | Tile f0..2 period
+ *   RepeatFinite f0..2 period u0..2 count | Iterate u0 iterations f0 bailout,
+ *     body = body_ids[body_offset .. body_offset+body_len]
+ *   Trap u0 slot u1 measure u2 mode f0 scale | Sphere f0 radius | Torus f0 radius f1 tube
+ *   Cylinder f0 radius f1 half_height | Box f0..2 half | RoundBox f0..2 half f3 radius
+ *   Rock f0..2 half f3 erosion u0 seed | Plane f0..2 normal f3 offset | NormFence f0 inset
+ *   MaterialTag u0 index | Bounded f0..2 half f3 margin | SmoothUnion/Intersection f0 k
+ */
+typedef struct sf_node {
+    uint32_t id;
+    uint32_t kind;      /* enum sf_node_kind */
+    uint32_t enabled;   /* 0 = disabled (Node.enabled) */
+    uint32_t body_offset;
+    uint32_t body_len;
+    uint32_t u[3];
+    float f[8];
+} sf_node;
+
+typedef struct sf_link {           /* Link{from:(node,port), to:(node,port)} */
+    uint32_t from_node, from_port, to_node, to_port;
+} sf_link;
+
+typedef struct sf_graph_desc {
+    const sf_node* nodes;
+    uint32_t node_count;
+    const sf_link* links;
+    uint32_t link_count;
+    const uint32_t* body_ids;      /* concatenated Iterate bodies */
+    uint32_t body_id_count;
+    float safety;
+    float bounding_radius_hint;
+} sf_graph_desc;
+
+/* DeSample (crates/syfrack-core/src/scene/fractal.rs:18-27). */
+typedef struct sf_de_sample {
+    float distance;
+    float traps[4];      /* normalised min(trap/scale, 1); 1 when unwritten */
+    uint32_t iterations; /* clamped to the iteration product */
+    uint32_t material;
+} sf_de_sample;
+
+/* Constants derived on the host, as Uniforms::from_fractal (uniforms.rs:183-189). */
+typedef struct sf_graph_info {
+    float step_scale;            /* safety / lipschitz(hint): eval.rs:879-881 */
+    float lipschitz;             /* eval.rs:828-849 */
+    float trap_scales[4];        /* eval.rs:853-877 */
+    uint32_t iteration_product;  /* validate.rs:112-141 */
+    uint32_t form;               /* SF_FORM_*: specialised device code path */
+    uint32_t op_count;           /* length of the lowered device program */
+    float bounding_radius_hint;
+} sf_graph_info;
+enum { SF_FORM_GENERIC = 0, SF_FORM_BULB = 1, SF_FORM_BOX = 2, SF_FORM_MENGER = 3 };
+
+typedef struct sf_context sf_context;
+typedef struct sf_graph sf_graph;
+
+/* Device context: owns the CUDA stream, the module and the HBM admission
+ * budget (0 = 90% of free memory). Replaces GpuContext::new (gpu.rs:15-36)
+ * and Renderer::new (renderer.rs:328). */
+sf_status sf_context_create(int device, uint64_t hbm_budget_bytes, sf_context** out);
+sf_status sf_context_destroy(sf_context* ctx);
+/* The cudaStream_t every call of this context is ordered on. */
+sf_status sf_context_stream(sf_context* ctx, void** stream_out);
+/* Bytes currently admitted against the budget, and the budget. */
+sf_status sf_context_memory(sf_context* ctx, uint64_t* used, uint64_t* budget);
+
+/* Validates and lowers a graph. Replaces graph_wgsl::compile (graph_wgsl.rs:949-952)
+ * + ParamLayout::pack; the lowered program lives in device memory. */
+sf_status sf_graph_compile(sf_context* ctx, const sf_graph_desc* desc, sf_graph** out);
+sf_status sf_graph_info_get(const sf_graph* graph, sf_graph_info* out);
+/* Value edits without re-lowering: same topology, new floats (topology_key semantics,
+ * graph/mod.rs:397-425). Fails with SF_ERR_GRAPH if the topology changed. */
+sf_status sf_graph_update(sf_graph* graph, const sf_graph_desc* desc);
+sf_status sf_graph_destroy(sf_graph* graph);
+
+/* Batched DE evaluation at n points (xyz interleaved, host memory) -> n samples.
+ * Replaces Renderer::probe_distances (renderer.rs:645-648) / de_probe.wgsl:9-17. */
+sf_status sf_de_probe(sf_graph* graph, const float* xyz, size_t n, sf_de_sample* out);
+/* Same on device buffers, asynchronous on the context stream: SoA x,y,z in;
+ * distance[n], traps[4n] (slot-major: traps[k*n+i]), iterations[n], material[n] out. */
+sf_status sf_de_probe_device(sf_graph* graph, const float* x, const float* y, const float* z,
+                             size_t n, float* distance, float* traps, uint32_t* iterations,
+                             uint32_t* material);
+
+/* ------------------------------------------------------------------ scene */
+/* CameraBasis (crates/syfrack-core/src/scene/camera.rs:44-56), as packed in
+ * Uniforms.camera (uniforms.rs:754-766). */
+typedef struct sf_camera {
+    float origin[3], forward[3], right[3], up[3];
+    float tan_half_fov, aspect, lens_radius, focus_distance;
+} sf_camera;
+/* Material / Finish (material.rs:136-170). */
+typedef struct sf_material {
+    float albedo[3];
+    float roughness, metallic, specular;
+    float emission[3];
+} sf_material;
+/* Light::Area packed as GpuLight (uniforms.rs:671-713): a = centre, b = full
+ * width edge, c = full height edge, radiance = color * intensity. */
+typedef struct sf_area_light {
+    float center[3], edge_u[3], edge_v[3], radiance[3];
+} sf_area_light;
+#define SF_MAX_LIGHTS 8
+#define SF_MAX_FINISHES 8
+typedef struct sf_scene_desc {
+    sf_camera camera;
+    sf_material material;                 /* index 0: the global surface */
+    sf_material finishes[SF_MAX_FINISHES];/* MaterialTag 1..8 */
+    uint32_t finish_count;
+    sf_area_light lights[SF_MAX_LIGHTS];
+    uint32_t light_count;
+    /* SurfaceVariation (uniforms.rs:485-495): trap slot drives roughness/metallic. */
+    uint32_t variation_slot, variation_enabled;
+    float variation_roughness[2], variation_metallic[2];
+    float cavity_darkness;                /* atmosphere.b.w, 0 = off */
+    uint64_t seed;                        /* Scene.seed; the device uses lo ^ hi */
+} sf_scene_desc;
+
+/* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138). */
+enum { SF_INTEGRATOR_MEGAKERNEL = 0, SF_INTEGRATOR_WAVEFRONT = 1 };
+typedef struct sf_render_config {
+    uint32_t integrator;
+    uint32_t width, height, samples_per_pixel, max_bounces, max_steps;
+    float pixel_tolerance;
+    uint32_t tile_size, samples_per_dispatch;
+} sf_render_config;
+
+/* Tile{x,y,w,h,done} (crates/syfrack-render/src/tiles.rs:4-11). */
+typedef struct sf_tile { uint32_t x, y, w, h, done; } sf_tile;
+
+
+/* ------------------------------------------------------------------ primary rays
+ * Primary-ray sphere trace through pixel centres (control.wgsl:266-291 ray set-up,
+ * pathtrace.wgsl:78-145 march). rule 0: the reference's cone-relative hit test
+ * radius/t < pixel_cone*tolerance; rule 1: fixed epsilon radius <= eps. normal_mode
+ * 0: 6-tap central difference, 1: 4-tap tetrahedral (common.wgsl:376-387), both with
+ * h = max(t*pixel_cone*0.5, 1e-4)*tolerance. Outputs (host, width*height each):
+ * t (-1 on a miss), steps, normal (3 planes: x[], y[], z[]). */
+typedef struct sf_primary_desc {
+    sf_camera camera;
+    uint32_t width, height, max_steps;
+    int32_t rule;          /* 0 cone-relative, 1 absolute epsilon */
+    int32_t normal_mode;   /* 0 central (6 taps), 1 tetrahedral (4 taps) */
+    float eps, t_far, pixel_tolerance;
+} sf_primary_desc;
+sf_status sf_primary_trace(sf_graph* graph, const sf_primary_desc* desc, float* t_out, uint32_t* steps_out,
+                           float* normal_out);
+
+/* ------------------------------------------------------------------ statistics & timing */
+typedef struct sf_stats {
+    uint64_t de_evals;         /* distance-estimator evaluations */
+    uint64_t de_iterations;    /* Iterate loop iterations executed inside them */
+    uint64_t segments;         /* march_segment runs: camera, continuation and shadow */
+    uint64_t shadow_segments;
+    uint64_t steps;            /* primary kernel: march steps; deep zoom: rebases */
+    uint64_t launches;         /* kernels launched by this handle */
+    double kernel_ms;          /* device time of the timed kernels (profiling on) */
+    double trace_ms;           /* of which the trace (march) kernels */
+    uint64_t trace_launches;
+} sf_stats;
+/* Per-kernel CUDA-event timing on the context stream (off by default). */
+sf_status sf_context_set_profiling(sf_context* ctx, int enable);
+sf_status sf_context_stats(sf_context* ctx, sf_stats* out);
+sf_status sf_context_reset_stats(sf_context* ctx);
+/* Measured FP32 FMA throughput of the device (TFLOP/s, FMA = 2 flops): the
+ * roofline denominator of the FP32-bound DE kernels. No counterpart in the
+ * reference (a diagnostic like its adapter probe, shaders/probe.wgsl). */
+sf_status sf_device_fp32_peak(sf_context* ctx, double* tflops);
+/* Blocks until the context stream is idle or timeout_ms passes (SF_ERR_TIMEOUT). */
+sf_status sf_context_sync(sf_context* ctx, uint32_t timeout_ms);
+
+/* ------------------------------------------------------------------ render sessions
+ * RenderSession (crates/syfrack-render/src/session.rs:113-162): progressive
+ * accumulation over a TileGrid (tiles.rs:14-90) with samples_per_dispatch samples
+ * per dispatch. Film planes follow RenderOutput (renderer.rs:151-164): accum
+ * holds sample sums (accum += (L,1) per sample in ascending sample order,
+ * pathtrace.wgsl:1243-1245); depth/aux come from sample 0. */
+typedef struct sf_session sf_session;
+typedef struct sf_progress {
+    uint32_t tiles, dispatches, samples_min, samples_max, target;
+    uint64_t pixel_samples_done, pixel_samples_total;
+    uint32_t status_word;   /* wavefront invariant bits 1/2/4 (wavefront.wgsl:183,:220,:236) */
+} sf_progress;
+typedef struct sf_film_planes {
+    float* accum;   /* 4*width*height: rgb sums and sample count */
+    float* depth;   /* width*height */
+    float* aux;     /* 4*width*height: normal xyz, steps (-1 on a miss) */
+} sf_film_planes;
+
+/* Session::new (session.rs:165). The integrator field selects the per-pixel
+ * megakernel (pathtrace.wgsl main) or the wavefront stages (wavefront.rs:310-419). */
+sf_status sf_session_create(sf_context* ctx, sf_graph* graph, const sf_scene_desc* scene,
+                            const sf_render_config* cfg, sf_session** out);
+/* Wavefront::dispatch / Renderer::dispatch: `samples` samples of one tile,
+ * asynchronous on the context stream (no host wait). */
+sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t samples);
+/* RenderSession::step (session.rs:694-877): dispatches least-advanced tiles
+ * (TileGrid::next_pending) until budget_ms of wall time is spent or the image
+ * reached samples_per_pixel; *done = 1 when complete. Waits for the device. */
+sf_status sf_session_step(sf_session* s, uint32_t budget_ms, int* done);
+/* Bounded wait for the session's work; returns the invariant word. */
+sf_status sf_session_sync(sf_session* s, uint32_t timeout_ms, uint32_t* status_word);
+sf_status sf_session_progress(sf_session* s, sf_progress* out);
+sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t capacity, uint32_t* count);
+/* Copies the film planes to host buffers (RenderSession::readback, session.rs:879). */
+sf_status sf_session_readback(sf_session* s, sf_film_planes* out);
+sf_status sf_session_stats(sf_session* s, sf_stats* out);
+/* Checkpoint (session.rs:1194-1346): state + film planes + FNV-1a hash + producer
+ * identity, written to a sibling directory and swapped in. Resume refuses a
+ * corrupt state or another producer with SF_ERR_CHECKPOINT. */
+sf_status sf_session_save(sf_session* s, const char* dir);
+sf_status sf_session_resume(sf_context* ctx, sf_graph* graph, const char* dir, sf_session** out);
+sf_status sf_session_destroy(sf_session* s);
+/* Autotuning knobs of the wavefront trace kernel (blocks per SM, threads per block). */
+sf_status sf_session_set_launch(sf_session* s, uint32_t blocks_per_sm, uint32_t threads);
+
+/* ------------------------------------------------------------------ escape time
+ * PlanarFractal (crates/syfrack-core/src/scene/planar.rs:20-39); family:
+ * 0 Julia, 1 Mandelbrot, 2 BurningShip, 3 Newton, 4 Nova, 5 Phoenix. Angles in
+ * degrees. Iterations are not capped at the reference's 512 (planar.rs:205-210). */
+typedef struct sf_planar_desc {
+    uint32_t family, power, iterations;
+    float julia[2], center[2];
+    float zoom, angle, inversion, twist, relaxation, memory, bailout, trap_radius, stripes;
+} sf_planar_desc;
+/* Flat canvas mapping of the 2D branch (pathtrace.wgsl:1226-1239, uniforms.rs:760-764). */
+typedef struct sf_canvas {
+    float center[2];
+    float zoom, rotation_deg;
+    uint32_t width, height;
+    uint64_t seed;
+} sf_canvas;
+/* PlanarFractal::sample at n points (xy interleaved, host): distance[n],
+ * traps[4n] (slot-major), iterations[n]. Orbit arithmetic is unfused binary32,
+ * so iteration counts equal the reference's f32 evaluation exactly. */
+sf_status sf_planar_probe(sf_context* ctx, const sf_planar_desc* f, const float* xy, size_t n, float* distance,
+                          float* traps, uint32_t* iterations);
+/* One sample per pixel of a tile of the canvas; sample = 0xffffffff for pixel
+ * centres, else the jitter of rng_init(px, sample, seed). Host outputs sized tile w*h. */
+sf_status sf_escape2d(sf_context* ctx, const sf_planar_desc* f, const sf_canvas* canvas, sf_tile tile,
+                      uint32_t sample, float* distance, float* traps, uint32_t* iterations);
+
+/* Deep zoom (no counterpart in the reference, which caps zoom at 1e4): Mandelbrot
+ * z <- z^2 + c around centre (hi + lo), pixel pitch = width_units / image width.
+ * FP64 reference orbit on the GPU, FP32 perturbation deltas with rebasing.
+ * Outputs per pixel: iteration count (first n with |z_n| > bailout, else max_iter)
+ * and smooth value n + 1 - log2(ln|z_n|). reference_f64 != 0 also runs the
+ * full-FP64 direct iteration into iters_f64/smooth_f64 (may be NULL otherwise). */
+typedef struct sf_deep_zoom_desc {
+    double center_hi[2], center_lo[2];
+    double width_units;
+    uint32_t width, height, max_iter;
+    float bailout;
+} sf_deep_zoom_desc;
+sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth,
+                       int reference_f64, uint32_t* iters_f64, float* smooth_f64, uint64_t* rebases);
+
+#ifdef __cplusplus
+}
+#endif
+#endif /* SYFRACK_GPU_H */

@@ -1,0 +1,1102 @@
+// TEST INFRASTRUCTURE -- NOT THE PRODUCT. See oracle_core.hpp.
+#include "oracle_core.hpp"
+
+#include <algorithm>
+#include <map>
+#include <set>
+#include <unordered_map>
+
+namespace orc {
+
+static constexpr uint32_t MAX_DEPTH = 3;  // graph/mod.rs:41
+
+// active_nodes (validate.rs:24-43): everything reachable backwards from the Output.
+static std::vector<uint32_t> active_nodes(const Graph& g) {
+    const sf_node* out = nullptr;
+    for (auto& n : g.nodes) if (n.kind == SF_NODE_OUTPUT) { out = &n; break; }
+    if (!out) return {};
+    std::set<uint32_t> seen;
+    std::vector<uint32_t> stack{out->id};
+    while (!stack.empty()) {
+        uint32_t id = stack.back();
+        stack.pop_back();
+        if (!seen.insert(id).second) continue;
+        for (auto& l : g.links) if (l.to_node == id) stack.push_back(l.from_node);
+    }
+    return std::vector<uint32_t>(seen.begin(), seen.end());  // sorted ascending
+}
+
+static std::map<uint32_t, uint32_t> body_owners(const Graph& g) {
+    std::map<uint32_t, uint32_t> owners;
+    for (auto& n : g.nodes)
+        for (uint32_t b : g.body_of(n)) owners[b] = n.id;
+    return owners;
+}
+
+// topo_order (validate.rs:45-85): Kahn's algorithm, smallest ready id first.
+static bool topo_order(const Graph& g, std::vector<uint32_t>& order) {
+    auto act = active_nodes(g);
+    std::set<uint32_t> active(act.begin(), act.end());
+    auto owners = body_owners(g);
+    std::map<uint32_t, size_t> indeg;
+    for (uint32_t id : active) if (!owners.count(id)) indeg[id] = 0;
+    for (auto& l : g.links)
+        if (indeg.count(l.to_node) && active.count(l.from_node)) indeg[l.to_node] += 1;
+    std::vector<uint32_t> ready;
+    for (auto& [id, d] : indeg) if (d == 0) ready.push_back(id);
+    auto desc = [](uint32_t a, uint32_t b) { return a > b; };
+    std::sort(ready.begin(), ready.end(), desc);
+    order.clear();
+    while (!ready.empty()) {
+        uint32_t id = ready.back();
+        ready.pop_back();
+        order.push_back(id);
+        std::vector<uint32_t> next;
+        for (auto& l : g.links) {
+            if (l.from_node != id) continue;
+            auto it = indeg.find(l.to_node);
+            if (it != indeg.end()) {
+                it->second -= 1;
+                if (it->second == 0) next.push_back(l.to_node);
+            }
+        }
+        std::sort(next.begin(), next.end(), desc);
+        ready.insert(ready.end(), next.begin(), next.end());
+        std::sort(ready.begin(), ready.end(), desc);
+    }
+    return order.size() == indeg.size();
+}
+
+static uint32_t sat_mul(uint32_t a, uint32_t b) {
+    uint64_t r = uint64_t(a) * uint64_t(b);
+    return r > 0xffffffffull ? 0xffffffffu : uint32_t(r);
+}
+
+// iteration_product (validate.rs:112-141).
+static uint32_t product(const Graph& g, uint32_t id, std::vector<uint32_t>& seen) {
+    if (std::find(seen.begin(), seen.end(), id) != seen.end()) return 0xffffffffu;
+    seen.push_back(id);
+    uint32_t p = 1;
+    const sf_node* n = g.node(id);
+    if (n && n->kind == SF_NODE_ITERATE) {
+        uint32_t m = 0;
+        bool any = false;
+        for (uint32_t b : g.body_of(*n)) { m = std::max(m, product(g, b, seen)); any = true; }
+        p = sat_mul(n->u[0], any ? m : 1);
+    }
+    seen.pop_back();
+    return p;
+}
+
+// trap_scales walk (eval.rs:853-877).
+static void trap_walk(const Graph& g, uint32_t id, uint32_t depth, float* scales) {
+    if (depth > MAX_DEPTH + 1) return;
+    const sf_node* n = g.node(id);
+    if (!n || !n->enabled) return;
+    if (n->kind == SF_NODE_TRAP) scales[std::min<uint32_t>(n->u[0], 3)] = n->f[0];
+    else if (n->kind == SF_NODE_ITERATE)
+        for (uint32_t b : g.body_of(*n)) trap_walk(g, b, depth + 1, scales);
+}
+
+// lipschitz visit (eval.rs:828-849).
+static void lip_visit(const Graph& g, uint32_t id, float radius, uint32_t depth, float* l) {
+    if (depth > MAX_DEPTH + 1) return;
+    const sf_node* n = g.node(id);
+    if (!n || !n->enabled) return;
+    if (n->kind == SF_NODE_TWIST || n->kind == SF_NODE_BEND) {
+        float x = n->f[0] * radius;
+        *l *= sqrtf(1.0f + x * x);
+    }
+    for (uint32_t b : g.body_of(*n)) lip_visit(g, b, radius, depth + 1, l);
+}
+
+// needed (eval.rs:35-47).
+static void needed(const Graph& g, uint32_t id, std::set<uint32_t>& set) {
+    if (!set.insert(id).second) return;
+    const sf_node* n = g.node(id);
+    if (!n) return;
+    if (n->enabled && n->kind == SF_NODE_INSTANCES) return;
+    for (uint32_t port = 0; port < input_count(n->kind); ++port) {
+        uint32_t src;
+        if (g.input_of(id, port, &src)) needed(g, src, set);
+    }
+}
+
+bool prepare(Graph& g) {
+    g.ok = false;
+    if (!topo_order(g, g.order)) { g.error = "cycle"; return false; }
+    g.output = 0;
+    for (auto& n : g.nodes) if (n.kind == SF_NODE_OUTPUT) { g.output = n.id; break; }
+    std::set<uint32_t> set;
+    needed(g, g.output, set);
+    g.plan.clear();
+    for (uint32_t id : g.order) if (set.count(id)) g.plan.push_back(id);
+    for (int i = 0; i < 4; ++i) g.trap_scales[i] = 1.f;
+    for (uint32_t id : g.order) trap_walk(g, id, 0, g.trap_scales);
+    auto owners = body_owners(g);
+    uint32_t best = 0;
+    bool any = false;
+    for (uint32_t id : active_nodes(g)) {
+        if (owners.count(id)) continue;
+        std::vector<uint32_t> seen;
+        best = std::max(best, product(g, id, seen));
+        any = true;
+    }
+    g.iteration_product = any ? best : 1;
+    float l = 1.f;
+    for (uint32_t id : active_nodes(g)) lip_visit(g, id, g.hint, 0, &l);
+    g.lipschitz = l;
+    g.step_scale = g.safety / l;
+    g.ok = true;
+    return true;
+}
+
+// ---------------------------------------------------------------- DE
+// integral_spherical_power (eval.rs:129-178).
+template <class R> static void spherical_power(V3<R> p, R r, uint32_t n, V3<R>* out, R* deriv) {
+    if (n == 1) { *out = p; *deriv = R(1); return; }
+    auto mul = [](V2<R> a, V2<R> b) { return V2<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+    R rho = V2<R>(p.x, p.y).length();
+    V2<R> theta(r_clamp(p.z / r, R(-1), R(1)), rho / r);
+    V2<R> phi = rho > R(0) ? V2<R>(p.x, p.y) / rho : V2<R>(1, 0);
+    if (n == 6 || n == 8) {
+        auto square = [](V2<R> a) { return V2<R>(a.x * a.x - a.y * a.y, R(2) * a.x * a.y); };
+        V2<R> t2 = square(theta), f2 = square(phi);
+        V2<R> t4 = square(t2), f4 = square(f2);
+        R r2 = r * r;
+        R r4 = r2 * r2;
+        V2<R> t, f;
+        R previous;
+        if (n == 6) { t = mul(t2, t4); f = mul(f2, f4); previous = r4 * r; }
+        else { t = square(t4); f = square(f4); previous = r4 * r2 * r; }
+        *out = V3<R>(t.y * f.x, t.y * f.y, t.x) * (previous * r);
+        *deriv = R(n) * previous;
+        return;
+    }
+    V2<R> t(1, 0), f(1, 0);
+    uint32_t e = n;
+    while (e != 0) {
+        if (e & 1) { t = mul(t, theta); f = mul(f, phi); }
+        e >>= 1;
+        if (e != 0) { theta = mul(theta, theta); phi = mul(phi, phi); }
+    }
+    R radial_previous = 1;
+    for (uint32_t i = 1; i < n; ++i) radial_previous *= r;
+    *out = V3<R>(t.y * f.x, t.y * f.y, t.x) * (radial_previous * r);
+    *deriv = R(n) * radial_previous;
+}
+
+static inline uint32_t u32_of_f(float v) { return uint32_t(v); }
+
+// terrain noise / rock distance (eval.rs:232-263).
+static float terrain_hash(int32_t cx, int32_t cy, int32_t cz, uint32_t seed) {
+    uint32_t h = (uint32_t(cx) * 0x8da6b343u) ^ (uint32_t(cy) * 0xd8163841u) ^ (uint32_t(cz) * 0xcb1ab31fu) ^ seed;
+    h = (h ^ (h >> 16)) * 0x7feb352du;
+    h = (h ^ (h >> 15)) * 0x846ca68bu;
+    h ^= h >> 16;
+    return float(h >> 8) / 16777216.0f;
+}
+template <class R> static R terrain_noise(V3<R> p, uint32_t seed) {
+    V3<R> base(r_floor(p.x), r_floor(p.y), r_floor(p.z));
+    V3<R> f = p - base;
+    V3<R> t = f * f * (V3<R>::splat(3) - f * R(2));
+    int32_t c0 = int32_t(base.x), c1 = int32_t(base.y), c2 = int32_t(base.z);
+    auto mix = [](R a, R b, R t) { return a + (b - a) * t; };
+    auto hash = [&](int x, int y, int z) { return R(terrain_hash(c0 + x, c1 + y, c2 + z, seed)); };
+    R a = mix(hash(0, 0, 0), hash(1, 0, 0), t.x);
+    R b = mix(hash(0, 1, 0), hash(1, 1, 0), t.x);
+    R d = mix(hash(0, 0, 1), hash(1, 0, 1), t.x);
+    R e = mix(hash(0, 1, 1), hash(1, 1, 1), t.x);
+    return mix(mix(a, b, t.y), mix(d, e, t.y), t.z);
+}
+template <class R> static R rock_distance(V3<R> p, V3<R> half, R erosion, uint32_t seed) {
+    R h = half.min_element();
+    V3<R> q = p * (R(1.15) / h);
+    R relief = R(0.57) * terrain_noise(q, seed) + R(0.29) * terrain_noise(q * R(2.03), seed + 97) +
+               R(0.14) * terrain_noise(q * R(4.17), seed + 193) - R(0.5);
+    return ((p / half).length() - R(1) - erosion * relief) * h / (R(1) + R(5.22) * erosion);
+}
+
+// measure (eval.rs:299-331).
+template <class R> static R measure(uint32_t m, V3<R> p) {
+    const R TAU = R(6.28318530717958647692);
+    switch (m) {
+    case SF_MEASURE_NORM: return p.length();
+    case SF_MEASURE_AXIS_X: return V2<R>(p.y, p.z).length();
+    case SF_MEASURE_AXIS_Y: return V2<R>(p.x, p.z).length();
+    case SF_MEASURE_AXIS_Z: return V2<R>(p.x, p.y).length();
+    case SF_MEASURE_PLANE_Y: return r_abs(p.y);
+    case SF_MEASURE_ANGLE_XY: return (p.x == R(0) && p.y == R(0)) ? R(0.5) : r_atan2(p.y, p.x) / TAU + R(0.5);
+    case SF_MEASURE_ANGLE_XZ: return (p.x == R(0) && p.z == R(0)) ? R(0.5) : r_atan2(p.z, p.x) / TAU + R(0.5);
+    case SF_MEASURE_ANGLE_YZ: return (p.y == R(0) && p.z == R(0)) ? R(0.5) : r_atan2(p.z, p.y) / TAU + R(0.5);
+    case SF_MEASURE_LOG_NORM: return r_log1p(p.length());
+    default: return p.length();
+    }
+}
+
+template <class R> static V3<R> f3(const sf_node& n, int i) { return V3<R>(R(n.f[i]), R(n.f[i + 1]), R(n.f[i + 2])); }
+
+// glam Quat::from_euler(XYZ) * p (common.wgsl:258-265 restates it as Rx(Ry(Rz p))).
+template <class R> static V3<R> rotate_euler_xyz(V3<R> p, V3<R> a) {
+    V3<R> q = p;
+    q = V3<R>(r_cos(a.z) * q.x - r_sin(a.z) * q.y, r_sin(a.z) * q.x + r_cos(a.z) * q.y, q.z);
+    q = V3<R>(r_cos(a.y) * q.x + r_sin(a.y) * q.z, q.y, -r_sin(a.y) * q.x + r_cos(a.y) * q.z);
+    q = V3<R>(q.x, r_cos(a.x) * q.y - r_sin(a.x) * q.z, r_sin(a.x) * q.y + r_cos(a.x) * q.z);
+    return q;
+}
+
+// apply_seeded (eval.rs:346-556).
+template <class R>
+static PointState<R> apply_seeded(const Graph& g, uint32_t id, PointState<R> s, V3<R> c, V3<R> seed_p, R seed_dr) {
+    const sf_node* np = g.node(id);
+    if (!np || !np->enabled) return s;
+    const sf_node& n = *np;
+    switch (n.kind) {
+    case SF_NODE_TRANSLATE: s.p = s.p + f3<R>(n, 0); break;
+    case SF_NODE_ROTATE: {
+        V3<R> a = f3<R>(n, 0);
+        s.p = rotate_euler_xyz(s.p, V3<R>(to_radians(a.x), to_radians(a.y), to_radians(a.z)));
+        break;
+    }
+    case SF_NODE_SCALE: s.p = s.p * R(n.f[0]); s.dr *= r_abs(R(n.f[0])); break;
+    case SF_NODE_SCALE_AXES: { V3<R> f = f3<R>(n, 0); s.p = s.p * f; s.dr *= f.max_element(); break; }
+    case SF_NODE_MIRROR: {
+        V3<R> nn = safe_normalize(f3<R>(n, 0));
+        R h = s.p.dot(nn) - R(n.f[3]);
+        if (h < R(0)) s.p = s.p - nn * (R(2) * h);
+        break;
+    }
+    case SF_NODE_BOX_FOLD: {
+        R l = R(n.f[0]);
+        s.p = vclamp(s.p, V3<R>::splat(-l), V3<R>::splat(l)) * R(2) - s.p;
+        break;
+    }
+    case SF_NODE_BOX_FOLD_AXES: {
+        V3<R> l = f3<R>(n, 0);
+        V3<R> folded = vclamp(s.p, -l, l) * R(2) - s.p;
+        for (int a = 0; a < 3; ++a) if (n.u[a]) s.p[a] = folded[a];
+        break;
+    }
+    case SF_NODE_SPHERE_INVERSION: {
+        R rad = R(n.f[0]), mr = R(n.f[1]);
+        R k = rad * rad / r_max(s.p.length_squared(), mr * mr);
+        s.p = s.p * k;
+        s.dr *= k;
+        break;
+    }
+    case SF_NODE_SPHERE_FOLD: {
+        R r2 = s.p.dot(s.p);
+        R mr = R(n.f[0]), fr = R(n.f[1]);
+        R mr2 = mr * mr, fr2 = fr * fr;
+        R k = r2 < mr2 ? fr2 / mr2 : (r2 < fr2 ? fr2 / r2 : R(1));
+        s.p = s.p * k;
+        s.dr *= k;
+        break;
+    }
+    case SF_NODE_ABS:
+        if (n.u[0]) s.p.x = r_abs(s.p.x);
+        if (n.u[1]) s.p.y = r_abs(s.p.y);
+        if (n.u[2]) s.p.z = r_abs(s.p.z);
+        break;
+    case SF_NODE_MENGER_FOLD: {
+        R scale = R(n.f[0]);
+        V3<R> off = f3<R>(n, 1);
+        V3<R> z = s.p.abs();
+        if (z.x < z.y) z = V3<R>(z.y, z.x, z.z);
+        if (z.x < z.z) z = V3<R>(z.z, z.y, z.x);
+        if (z.y < z.z) z = V3<R>(z.x, z.z, z.y);
+        z = z * scale - off * (scale - R(1));
+        if (z.z < R(-0.5) * off.z * (scale - R(1))) z.z += off.z * (scale - R(1));
+        s.p = z;
+        s.dr *= scale;
+        break;
+    }
+    case SF_NODE_KALEIDO: {
+        const R TAU = R(6.28318530717958647692);
+        R sector = TAU / R(std::max<uint32_t>(n.u[0], 1));
+        R a = r_atan2(s.p.z, s.p.x) + to_radians(R(n.f[0]));
+        a = r_abs(r_rem_euclid(a + sector * R(0.5), sector) - sector * R(0.5));
+        R r = V2<R>(s.p.x, s.p.z).length();
+        s.p.x = r * r_cos(a);
+        s.p.z = r * r_sin(a);
+        break;
+    }
+    case SF_NODE_POWER: {
+        R power = R(n.f[0]);
+        R radius = s.p.length();
+        float pf = n.f[0];
+        if (radius >= R(1e-12) && pf >= 1.0f && pf <= 16.0f && pf == floorf(pf)) {
+            V3<R> point;
+            R deriv;
+            spherical_power(s.p, radius, u32_of_f(pf), &point, &deriv);
+            s.p = point;
+            s.dr *= deriv;
+        } else {
+            R r = r_max(radius, R(1e-12));
+            R theta = radius >= R(1e-12) ? r_atan2(V2<R>(s.p.x, s.p.y).length(), s.p.z)
+                                         : r_acos(r_clamp(s.p.z / r, R(-1), R(1)));
+            R phi = r_atan2(s.p.y, s.p.x);
+            s.dr *= r_pow(r, power - R(1)) * power;
+            R zr = r_pow(r, power);
+            R st = r_sin(theta * power), ct = r_cos(theta * power);
+            R sp = r_sin(phi * power), cp = r_cos(phi * power);
+            s.p = V3<R>(st * cp, st * sp, ct) * zr;
+        }
+        break;
+    }
+    case SF_NODE_ADD_ORIGIN: s.p = s.p + c; s.dr += R(1); break;
+    case SF_NODE_ADD_SEED: {
+        V3<R> m = f3<R>(n, 0);
+        s.p = s.p + seed_p * m;
+        s.dr += seed_dr * m.abs().max_element();
+        break;
+    }
+    case SF_NODE_ADD_CONSTANT: {
+        V3<R> m = f3<R>(n, 0), j = f3<R>(n, 3);
+        s.p = s.p + (c * m + j);
+        s.dr += m.abs().max_element();
+        break;
+    }
+    case SF_NODE_TWIST: {
+        R a = R(n.f[0]) * s.p.y;
+        R sn = r_sin(a), cs = r_cos(a);
+        V2<R> v(cs * s.p.x - sn * s.p.z, sn * s.p.x + cs * s.p.z);
+        s.p.x = v.x;
+        s.p.z = v.y;
+        break;
+    }
+    case SF_NODE_BEND: {
+        R a = R(n.f[0]) * s.p.x;
+        R sn = r_sin(a), cs = r_cos(a);
+        V2<R> v(cs * s.p.x - sn * s.p.y, sn * s.p.x + cs * s.p.y);
+        s.p.x = v.x;
+        s.p.y = v.y;
+        break;
+    }
+    case SF_NODE_TILE: {
+        V3<R> per = f3<R>(n, 0);
+        V3<R> half = per * R(0.5);
+        s.p = V3<R>(r_rem_euclid(s.p.x + half.x, per.x) - half.x, r_rem_euclid(s.p.y + half.y, per.y) - half.y,
+                    r_rem_euclid(s.p.z + half.z, per.z) - half.z);
+        break;
+    }
+    case SF_NODE_REPEAT_FINITE: {
+        V3<R> per = f3<R>(n, 0);
+        V3<R> last = V3<R>(R(n.u[0]), R(n.u[1]), R(n.u[2])) - V3<R>::splat(1);
+        V3<R> half = last * R(0.5);
+        V3<R> q = s.p / per + half + V3<R>::splat(R(0.5));
+        V3<R> cell = vclamp(V3<R>(r_floor(q.x), r_floor(q.y), r_floor(q.z)), V3<R>::splat(0), last) - half;
+        s.p = s.p - cell * per;
+        break;
+    }
+    case SF_NODE_ITERATE: {
+        V3<R> lp = s.p;
+        R ldr = s.dr;
+        uint32_t iterations = n.u[0];
+        R bailout = R(n.f[0]);
+        auto b = g.body_of(n);
+        for (uint32_t i = 0; i < iterations; ++i) {
+            if (s.p.length() > bailout) break;
+            for (uint32_t bid : b) s = apply_seeded(g, bid, s, c, lp, ldr);
+            s.iter += 1;
+        }
+        break;
+    }
+    case SF_NODE_TRAP: {
+        uint32_t i = std::min<uint32_t>(n.u[0], 3);
+        R v = measure(n.u[1], s.p);
+        switch (n.u[2]) {
+        case SF_TRAP_MAXIMUM: s.traps[i] = s.traps[i] >= R(1e30) ? v : r_max(s.traps[i], v); break;
+        case SF_TRAP_LAST: s.traps[i] = v; break;
+        default: s.traps[i] = r_min(s.traps[i], v); break;
+        }
+        break;
+    }
+    default: break;
+    }
+    return s;
+}
+
+// fence (eval.rs:558-599).
+template <class R> static R fence(const sf_node& n, const PointState<R>& s) {
+    switch (n.kind) {
+    case SF_NODE_SPHERE: return (s.p.length() - R(n.f[0])) / s.dr;
+    case SF_NODE_TORUS:
+        return (V2<R>(V2<R>(s.p.x, s.p.z).length() - R(n.f[0]), s.p.y).length() - R(n.f[1])) / s.dr;
+    case SF_NODE_CYLINDER: {
+        V2<R> q(V2<R>(s.p.x, s.p.z).length() - R(n.f[0]), r_abs(s.p.y) - R(n.f[1]));
+        V2<R> qm(r_max(q.x, R(0)), r_max(q.y, R(0)));
+        return (qm.length() + r_min(r_max(q.x, q.y), R(0))) / s.dr;
+    }
+    case SF_NODE_BOX: {
+        V3<R> q = s.p.abs() - f3<R>(n, 0);
+        return (vmax(q, V3<R>::splat(0)).length() + r_min(r_max(q.x, r_max(q.y, q.z)), R(0))) / s.dr;
+    }
+    case SF_NODE_ROUND_BOX: {
+        V3<R> half = f3<R>(n, 0);
+        R r = r_min(R(n.f[3]), half.min_element());
+        V3<R> q = s.p.abs() - (half - V3<R>::splat(r));
+        return (vmax(q, V3<R>::splat(0)).length() + r_min(q.max_element(), R(0)) - r) / s.dr;
+    }
+    case SF_NODE_ROCK: return rock_distance(s.p, f3<R>(n, 0), R(n.f[3]), n.u[0]) / s.dr;
+    case SF_NODE_PLANE: return (s.p.dot(safe_normalize(f3<R>(n, 0))) - R(n.f[3])) / s.dr;
+    case SF_NODE_NORM_FENCE: return (s.p.length() - R(n.f[0])) / r_abs(s.dr);
+    case SF_NODE_BULB_FENCE: {
+        R r = r_max(s.p.length(), R(1e-12));
+        return R(0.5) * r_log(r) * r / s.dr;
+    }
+    default: return std::numeric_limits<R>::infinity();
+    }
+}
+
+template <class R> static bool is_empty(R d) { return d >= R(1e30); }
+
+// combine (eval.rs:601-657).
+template <class R> static DistState<R> combine(const sf_node& n, DistState<R> a, DistState<R> b) {
+    const R INF = std::numeric_limits<R>::infinity();
+    auto blend = [&](R h, R d) {
+        DistState<R> r;
+        for (int i = 0; i < 4; ++i) {
+            bool fa = r_finite(a.traps[i]), fb = r_finite(b.traps[i]);
+            r.traps[i] = (fa && fb) ? b.traps[i] + (a.traps[i] - b.traps[i]) * h : fa ? a.traps[i] : fb ? b.traps[i] : INF;
+        }
+        r.d = d;
+        r.material = h >= R(0.5) ? a.material : b.material;
+        r.iter = h >= R(0.5) ? a.iter : b.iter;
+        return r;
+    };
+    switch (n.kind) {
+    case SF_NODE_UNION: { DistState<R> r = a.d <= b.d ? a : b; r.d = r_min(a.d, b.d); return r; }
+    case SF_NODE_INTERSECTION: { DistState<R> r = a.d >= b.d ? a : b; r.d = r_max(a.d, b.d); return r; }
+    case SF_NODE_SUBTRACTION: { DistState<R> r = a; r.d = r_max(a.d, -b.d); return r; }
+    case SF_NODE_SMOOTH_UNION: {
+        if (is_empty(a.d)) return b;
+        if (is_empty(b.d)) return a;
+        R k = R(n.f[0]);
+        R h = r_clamp(R(0.5) + R(0.5) * (b.d - a.d) / k, R(0), R(1));
+        return blend(h, b.d + (a.d - b.d) * h - k * h * (R(1) - h));
+    }
+    case SF_NODE_SMOOTH_INTERSECTION: {
+        if (is_empty(a.d)) { DistState<R> r = b; r.d = INF; return r; }
+        if (is_empty(b.d)) { DistState<R> r = a; r.d = INF; return r; }
+        R k = R(n.f[0]);
+        R h = r_clamp(R(0.5) - R(0.5) * (b.d - a.d) / k, R(0), R(1));
+        return blend(h, b.d + (a.d - b.d) * h + k * h * (R(1) - h));
+    }
+    default: return a;
+    }
+}
+
+// evaluate_raw (eval.rs:671-826) + PreparedGraph::evaluate (eval.rs:98-114).
+template <class R> Sample<R> evaluate(const Graph& g, V3<R> p) {
+    const R INF = std::numeric_limits<R>::infinity();
+    DistState<R> empty{INF, 0, 0, {INF, INF, INF, INF}};
+    PointState<R> start{p, R(1), 0, {INF, INF, INF, INF}};
+    struct Val { bool point; PointState<R> ps; DistState<R> ds; };
+    std::unordered_map<uint32_t, Val> values;
+    values.reserve(g.plan.size() * 2);
+    auto get_point = [&](uint32_t id, uint32_t port) {
+        uint32_t from;
+        if (g.input_of(id, port, &from)) {
+            auto it = values.find(from);
+            if (it != values.end() && it->second.point) return it->second.ps;
+        }
+        return start;
+    };
+    auto get_dist = [&](uint32_t id, uint32_t port) {
+        uint32_t from;
+        if (g.input_of(id, port, &from)) {
+            auto it = values.find(from);
+            if (it != values.end() && !it->second.point) return it->second.ds;
+        }
+        return empty;
+    };
+    for (uint32_t id : g.plan) {
+        const sf_node& n = *g.node(id);
+        Val v{};
+        uint32_t k = n.kind;
+        if (k == SF_NODE_INPUT) { v.point = true; v.ps = start; }
+        else if (k == SF_NODE_OUTPUT) { v.point = false; v.ds = get_dist(id, 0); }
+        else if (is_point_to_point(k)) {
+            PointState<R> s = get_point(id, 0);
+            v.point = true;
+            v.ps = apply_seeded(g, id, s, p, s.p, s.dr);
+        } else if (is_fence(k)) {
+            PointState<R> s = get_point(id, 0);
+            v.point = false;
+            v.ds.d = n.enabled ? fence(n, s) : INF;
+            v.ds.material = 0;
+            v.ds.iter = s.iter;
+            for (int i = 0; i < 4; ++i) v.ds.traps[i] = s.traps[i];
+        } else if (k == SF_NODE_MATERIAL_TAG) {
+            v.point = false;
+            v.ds = get_dist(id, 0);
+            if (n.enabled) v.ds.material = n.u[0];
+        } else if (k == SF_NODE_BOUNDED) {
+            v.point = false;
+            v.ds = get_dist(id, 1);
+            if (n.enabled) {
+                sf_node box = n;
+                box.kind = SF_NODE_BOX;
+                v.ds.d = r_max(v.ds.d, fence(box, get_point(id, 0)));
+            }
+        } else if (!n.enabled) {
+            v.point = false;
+            v.ds = get_dist(id, 0);
+        } else {
+            v.point = false;
+            v.ds = combine(n, get_dist(id, 0), get_dist(id, 1));
+        }
+        values[id] = v;
+    }
+    DistState<R> r = empty;
+    auto it = values.find(g.output);
+    if (it != values.end() && !it->second.point) r = it->second.ds;
+    Sample<R> out;
+    out.distance = r.d;
+    out.material = r.material;
+    for (int i = 0; i < 4; ++i)
+        out.traps[i] = r_finite(r.traps[i]) ? r_min(r.traps[i] / R(g.trap_scales[i]), R(1)) : R(1);
+    out.iterations = std::min(r.iter, g.iteration_product);
+    return out;
+}
+
+// ---------------------------------------------------------------- transport
+template <class R> static V3<R> v3(const float* f) { return V3<R>(R(f[0]), R(f[1]), R(f[2])); }
+
+template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, const sf_render_config& c) {
+    Scene<R> s;
+    s.cam.origin = v3<R>(d.camera.origin);
+    s.cam.forward = v3<R>(d.camera.forward);
+    s.cam.right = v3<R>(d.camera.right);
+    s.cam.up = v3<R>(d.camera.up);
+    s.cam.tan_half = R(d.camera.tan_half_fov);
+    s.cam.aspect = R(d.camera.aspect);
+    s.cam.lens_radius = R(d.camera.lens_radius);
+    s.cam.focus_distance = R(d.camera.focus_distance);
+    auto mat = [](const sf_material& m) {
+        Mat<R> o;
+        o.albedo = v3<R>(m.albedo);
+        o.roughness = R(m.roughness);
+        o.metallic = R(m.metallic);
+        o.specular = R(m.specular);
+        o.emission = v3<R>(m.emission);
+        return o;
+    };
+    s.material = mat(d.material);
+    s.finish_count = std::min<uint32_t>(d.finish_count, SF_MAX_FINISHES);
+    for (uint32_t i = 0; i < s.finish_count; ++i) s.finishes[i] = mat(d.finishes[i]);
+    s.light_count = std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
+    for (uint32_t i = 0; i < s.light_count; ++i) {
+        s.lights[i].a = v3<R>(d.lights[i].center);
+        s.lights[i].b = v3<R>(d.lights[i].edge_u);
+        s.lights[i].c = v3<R>(d.lights[i].edge_v);
+        s.lights[i].color = v3<R>(d.lights[i].radiance);
+    }
+    s.variation_slot = d.variation_slot;
+    s.variation_enabled = d.variation_enabled;
+    s.var_rough[0] = R(d.variation_roughness[0]);
+    s.var_rough[1] = R(d.variation_roughness[1]);
+    s.var_metal[0] = R(d.variation_metallic[0]);
+    s.var_metal[1] = R(d.variation_metallic[1]);
+    s.cavity = R(d.cavity_darkness);
+    s.seed = uint32_t(d.seed) ^ uint32_t(d.seed >> 32);
+    s.pixel_tolerance = R(c.pixel_tolerance);
+    // uniforms.rs:781-782: far = max(2*hint + |origin|, 200), computed in f32.
+    float origin_len = sqrtf(d.camera.origin[0] * d.camera.origin[0] + d.camera.origin[1] * d.camera.origin[1] +
+                             d.camera.origin[2] * d.camera.origin[2]);
+    float far = std::max(2.0f * g.hint + origin_len, 200.0f);
+    s.far = R(far);
+    s.step_scale = R(g.step_scale);
+    s.iteration_product = g.iteration_product;
+    s.width = c.width;
+    s.height = c.height;
+    s.max_bounces = c.max_bounces;
+    s.max_steps = c.max_steps;
+    return s;
+}
+
+// march_segment (pathtrace.wgsl:78-145). absolute_rule selects the fixed-epsilon
+// hit test (radius <= eps) used by the primary-ray configuration; otherwise the
+// reference's cone-relative test (radius / t < hit_cone).
+template <class R>
+Hit<R> march_segment(const Graph& g, V3<R> ro, V3<R> rd, R safety, R hit_cone, R t_end, uint32_t max_steps,
+                     bool absolute_rule, R eps, uint64_t* de_evals) {
+    const R T_MAX = R(200);
+    R t = 0, omega = R(1.2), prev_radius = 0, step_len = 0, cand_t = 0, cand_err = R(1e30);
+    Sample<R> blank{T_MAX, {1, 1, 1, 1}, 0, 0};
+    Sample<R> cand = blank;
+    Hit<R> out{false, t_end, 0, blank, false, 0xffffffffu};
+    R accept = absolute_rule ? eps : hit_cone;
+    for (uint32_t i = 0; i < max_steps; ++i) {
+        if (t >= t_end) return out;
+        out.steps = i + 1;
+        Sample<R> s = evaluate(g, ro + rd * t);
+        if (de_evals) ++*de_evals;
+        R radius = r_abs(s.distance) * safety;
+        bool sor_fail = omega > R(1) && (radius + prev_radius) < step_len * R(1.0001);
+        if (sor_fail) { step_len = step_len - omega * step_len; omega = 1; }
+        else step_len = radius * omega;
+        prev_radius = radius;
+        R err = absolute_rule ? radius : radius / r_max(t, R(1e-6));
+        if (!sor_fail && err < cand_err) { cand_t = t; cand = s; cand_err = err; }
+        if (!sor_fail && (absolute_rule ? err <= accept : err < accept)) {
+            out.hit = true;
+            out.t = t;
+            out.sample = s;
+            return out;
+        }
+        if (!sor_fail && t + step_len >= t_end) {
+            if (radius >= t_end - t) return out;
+            omega = 1;
+            step_len = radius;
+        }
+        t += step_len;
+    }
+    if (cand_err < accept * R(4)) { out.hit = true; out.t = cand_t; out.sample = cand; }
+    else out.exhausted = true;
+    return out;
+}
+
+// normal_at: tetrahedral 4-tap stencil (common.wgsl:376-387).
+template <class R> V3<R> normal_tetra(const Graph& g, V3<R> p, R h) {
+    const V3<R> k[4] = {V3<R>(1, -1, -1), V3<R>(-1, -1, 1), V3<R>(-1, 1, -1), V3<R>(1, 1, 1)};
+    V3<R> grad(0, 0, 0);
+    for (int i = 0; i < 4; ++i) grad = grad + k[i] * evaluate(g, p + k[i] * h).distance;
+    return normalize(grad);
+}
+// Central difference, 6 taps (the primary-ray configuration's normal).
+template <class R> V3<R> normal_central(const Graph& g, V3<R> p, R h) {
+    V3<R> grad(evaluate(g, p + V3<R>(h, 0, 0)).distance - evaluate(g, p - V3<R>(h, 0, 0)).distance,
+               evaluate(g, p + V3<R>(0, h, 0)).distance - evaluate(g, p - V3<R>(0, h, 0)).distance,
+               evaluate(g, p + V3<R>(0, 0, h)).distance - evaluate(g, p - V3<R>(0, 0, h)).distance);
+    return normalize(grad);
+}
+
+// Lights (lights.wgsl:150-356), area emitters only.
+template <class R> static V3<R> area_normal(const Light<R>& l) { return safe_normalize(l.b.cross(l.c)); }
+template <class R> static R luminance(V3<R> c) { return c.x * R(0.2126) + c.y * R(0.7152) + c.z * R(0.0722); }
+template <class R> static R area_intersection(V3<R> ro, V3<R> rd, const Light<R>& l) {
+    V3<R> n = area_normal(l);
+    R den = n.dot(rd);
+    if (r_abs(den) < R(1e-7)) return R(1e30);
+    R t = (l.a - ro).dot(n) / den;
+    if (t <= R(1e-6)) return R(1e30);
+    V3<R> q = ro + rd * t - l.a;
+    R x = q.dot(l.b) / l.b.dot(l.b);
+    R y = q.dot(l.c) / l.c.dot(l.c);
+    if (r_abs(x) > R(0.5) || r_abs(y) > R(0.5)) return R(1e30);
+    return t;
+}
+template <class R> static R emitter_area(const Light<R>& l) { return l.b.cross(l.c).length(); }
+template <class R> static R area_weight(V3<R> p, V3<R> n, const Light<R>& l) {
+    R area = emitter_area(l);
+    V3<R> to_light = l.a - p;
+    R dist2 = r_max(to_light.dot(to_light), R(1e-6));
+    V3<R> dir = to_light / r_sqrt(dist2);
+    R facing = r_max(area_normal(l).dot(-dir), R(0));
+    return luminance(l.color) * area * facing * r_max(n.dot(dir), R(0.15)) / dist2;
+}
+template <class R> static R area_total_weight(const Scene<R>& sc, V3<R> p, V3<R> n) {
+    R total = 0;
+    for (uint32_t i = 0; i < sc.light_count; ++i) total += area_weight(p, n, sc.lights[i]);
+    return total;
+}
+template <class R> static R area_direction_pdf(const Light<R>& l, R dist2, R cos_l) {
+    return dist2 / r_max(emitter_area(l) * cos_l, R(1e-20));
+}
+template <class R> static R mis_power(R a, R b) {
+    R scale = r_max(a, b);
+    if (scale <= R(0)) return 0;
+    R pa = a / scale, pb = b / scale;
+    return pa * pa / (pa * pa + pb * pb);
+}
+template <class R> static V3<R> area_emission(const Scene<R>& sc, V3<R> ro, V3<R> rd, R distance, R prev_pdf,
+                                              bool use_mis, V3<R> prev_normal, R prev_total) {
+    V3<R> L(0, 0, 0);
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        const Light<R>& l = sc.lights[i];
+        R cos_l = area_normal(l).dot(-rd);
+        if (cos_l <= R(0)) continue;
+        R t = area_intersection(ro, rd, l);
+        if (r_abs(t - distance) > r_max(R(1e-6), distance * R(1e-6))) continue;
+        R w = 1;
+        if (use_mis) {
+            R pl = area_direction_pdf(l, distance * distance, cos_l);
+            R selection = 0;
+            if (prev_total > R(0)) selection = area_weight(ro, prev_normal, l) / prev_total;
+            pl = pl * selection;
+            w = mis_power(prev_pdf, pl);
+        }
+        L = L + l.color * w;
+    }
+    return L;
+}
+
+// BRDF (pathtrace.wgsl:195-249, :394-463).
+template <class R> struct Surface { V3<R> n, diffuse, f0; R alpha; V3<R> emission; };
+static const double PI_W = 3.14159265358979;  // common.wgsl:6
+template <class R> static void tangent_frame(V3<R> n, V3<R>* t, V3<R>* bt) {
+    R s = n.z >= R(0) ? R(1) : R(-1);
+    R a = R(-1) / (s + n.z);
+    R b = n.x * n.y * a;
+    *t = V3<R>(R(1) + s * n.x * n.x * a, s * b, -s * n.x);
+    *bt = V3<R>(b, s + n.y * n.y * a, -n.y);
+}
+template <class R> static V3<R> frame_mul(V3<R> t, V3<R> bt, V3<R> n, V3<R> v) { return t * v.x + bt * v.y + n * v.z; }
+template <class R> static V3<R> cosine_sample(V3<R> n, R r1, R r2) {
+    R phi = R(2) * R(PI_W) * r1;
+    R r = r_sqrt(r2);
+    V3<R> t, bt;
+    tangent_frame(n, &t, &bt);
+    return frame_mul(t, bt, n, V3<R>(r * r_cos(phi), r * r_sin(phi), r_sqrt(r_max(R(0), R(1) - r2))));
+}
+template <class R> static R ggx_d(R nh, R a2) { R d = nh * nh * (a2 - R(1)) + R(1); return a2 / (R(PI_W) * d * d); }
+template <class R> static R smith_g1(R nv, R a2) { return R(2) * nv / (nv + r_sqrt(a2 + (R(1) - a2) * nv * nv)); }
+template <class R> static V3<R> fresnel(V3<R> f0, R vh) { return f0 + (V3<R>::splat(1) - f0) * r_pow(R(1) - vh, R(5)); }
+template <class R> static V3<R> sample_ggx_h(V3<R> n, V3<R> v, R alpha, R r1, R r2) {
+    V3<R> t, bt;
+    tangent_frame(n, &t, &bt);
+    V3<R> lv(t.dot(v), bt.dot(v), n.dot(v));
+    V3<R> vh = safe_normalize(V3<R>(alpha * lv.x, alpha * lv.y, r_max(lv.z, R(1e-5))));
+    R lensq = vh.x * vh.x + vh.y * vh.y;
+    V3<R> t1(1, 0, 0);
+    if (lensq > R(0)) t1 = V3<R>(-vh.y, vh.x, 0) / r_sqrt(lensq);
+    V3<R> t2 = vh.cross(t1);
+    R r = r_sqrt(r1);
+    R phi = R(2) * R(PI_W) * r2;
+    R x = r * r_cos(phi);
+    R blend = R(0.5) * (R(1) + vh.z);
+    R y = mixs(r_sqrt(r_max(R(0), R(1) - x * x)), r * r_sin(phi), blend);
+    V3<R> nh = t1 * x + t2 * y + vh * r_sqrt(r_max(R(0), R(1) - x * x - y * y));
+    return frame_mul(t, bt, n, safe_normalize(V3<R>(alpha * nh.x, alpha * nh.y, r_max(nh.z, R(0)))));
+}
+template <class R> static V3<R> brdf_eval(const Surface<R>& s, V3<R> v, V3<R> l) {
+    R nl = s.n.dot(l), nv = s.n.dot(v);
+    if (nl <= R(0) || nv <= R(0)) return V3<R>(0, 0, 0);
+    V3<R> h = normalize(v + l);
+    R nh = r_max(s.n.dot(h), R(0));
+    R vh = r_max(v.dot(h), R(0));
+    R a2 = s.alpha * s.alpha;
+    V3<R> f = fresnel(s.f0, vh);
+    V3<R> spec = f * (ggx_d(nh, a2) * smith_g1(nv, a2) * smith_g1(nl, a2)) / r_max(R(4) * nv * nl, R(1e-4));
+    return s.diffuse * (V3<R>::splat(1) - f) * R(1) / R(PI_W) + spec;
+}
+template <class R> static R spec_probability(const Surface<R>& s, R nv) {
+    V3<R> f = fresnel(s.f0, nv);
+    return r_clamp(luminance(f) / r_max(luminance(f) + luminance(s.diffuse), R(1e-4)), R(0.05), R(0.95));
+}
+template <class R> static R bsdf_pdf(const Surface<R>& s, V3<R> v, V3<R> l, R p_spec) {
+    R nl = s.n.dot(l);
+    if (nl <= R(0)) return 0;
+    V3<R> hh = normalize(v + l);
+    R nh = r_max(s.n.dot(hh), R(0));
+    R a2 = s.alpha * s.alpha;
+    R nv = r_max(s.n.dot(v), R(1e-4));
+    R pdf_spec = ggx_d(nh, a2) * smith_g1(nv, a2) / (R(4) * nv);
+    return p_spec * pdf_spec + (R(1) - p_spec) * nl / R(PI_W);
+}
+
+// make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
+template <class R> static Surface<R> make_surface(const Scene<R>& sc, V3<R> n, const Sample<R>& smp) {
+    V3<R> albedo = sc.material.albedo;
+    bool assigned = smp.material > 0 && smp.material <= sc.finish_count;
+    R rough = sc.material.roughness, metallic = sc.material.metallic, spec = sc.material.specular;
+    V3<R> emission(0, 0, 0);
+    if (assigned) {
+        const Mat<R>& f = sc.finishes[smp.material - 1];
+        albedo = f.albedo;
+        rough = f.roughness;
+        metallic = f.metallic;
+        spec = f.specular;
+        emission = f.emission;
+    }
+    if (!assigned && sc.variation_enabled) {
+        R value;
+        uint32_t slot = sc.variation_slot;
+        if (slot < 4) value = smp.traps[slot];
+        else if (slot == 5) value = n.y * R(0.5) + R(0.5);
+        else value = R(smp.iterations) / r_max(R(sc.iteration_product), R(1));
+        R t = r_clamp(value, R(0), R(1));
+        rough = sc.var_rough[0] + (sc.var_rough[1] - sc.var_rough[0]) * t;
+        metallic = sc.var_metal[0] + (sc.var_metal[1] - sc.var_metal[0]) * t;
+    }
+    rough = r_clamp(rough, R(0.02), R(1));
+    Surface<R> s;
+    s.n = n;
+    s.diffuse = albedo * (R(1) - metallic);
+    s.f0 = mixv(V3<R>::splat(spec), albedo, metallic);
+    s.alpha = rough * rough;
+    s.emission = emission;
+    return s;
+}
+
+// trace_geometry_lights (lights.wgsl:183-209) around march_segment.
+template <class R>
+static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd, R pixel_cone, R t_end, uint64_t* evals) {
+    R nearest = t_end;
+    uint32_t light_index = 0xffffffffu;
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        R t = area_intersection(ro, rd, sc.lights[i]);
+        if (t < nearest) { nearest = t; light_index = i; }
+    }
+    Hit<R> h = march_segment(g, ro, rd, sc.step_scale, pixel_cone * sc.pixel_tolerance, nearest, sc.max_steps, false,
+                             R(0), evals);
+    if (!h.hit && !h.exhausted && light_index != 0xffffffffu) {
+        h.hit = true;
+        h.t = nearest;
+        h.light_index = light_index;
+    }
+    return h;
+}
+
+// radiance (pathtrace.wgsl:802-1201) with fog, optics, ocean, portals, guiding,
+// textures, sun and environment disabled (those branches are identities when off),
+// camera_ray (:781-800) and the per-sample film terms of main (:1203-1276).
+template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint32_t px, uint32_t py, uint32_t sample) {
+    PixelResult res{};
+    uint32_t rng = rng_init(px, py, sample, sc.seed);
+    R pixel_cone = sc.cam.tan_half * R(2) / R(float(sc.width));
+    // camera_ray
+    R jx = rnd<R>(&rng);
+    R jy = rnd<R>(&rng);
+    R ndcx = ((R(float(px)) + jx) / R(float(sc.width))) * R(2) - R(1);
+    R ndcy = ((R(float(py)) + jy) / R(float(sc.height))) * R(2) - R(1);
+    V3<R> dir = normalize(sc.cam.forward + sc.cam.right * (ndcx * sc.cam.tan_half) +
+                          sc.cam.up * (-ndcy * sc.cam.tan_half / sc.cam.aspect));
+    V3<R> origin = sc.cam.origin;
+    if (sc.cam.lens_radius > R(0)) {
+        V3<R> focus = origin + dir * (sc.cam.focus_distance / r_max(dir.dot(sc.cam.forward), R(1e-4)));
+        R r = sc.cam.lens_radius * r_sqrt(rnd<R>(&rng));
+        R phi = R(2) * R(PI_W) * rnd<R>(&rng);
+        origin = origin + sc.cam.right * (r * r_cos(phi)) + sc.cam.up * (r * r_sin(phi));
+        dir = normalize(focus - origin);
+    }
+    V3<R> ro = origin, rd = dir;
+    V3<R> throughput(1, 1, 1), L(0, 0, 0);
+    R prev_pdf = 0, prev_area_total = 0;
+    bool prev_from_bsdf = false;
+    V3<R> prev_normal(0, 0, 0);
+    R first_depth = -1;
+    R aux[4] = {0, 0, 0, -1};
+    R extent = r_max(R(200), sc.far);
+    for (uint32_t bounce = 0; bounce <= sc.max_bounces;) {
+        Hit<R> h = trace_scene(g, sc, ro, rd, pixel_cone, extent, &res.de_evals);
+        res.segments++;
+        V3<R> gn(0, 0, 0);
+        if (h.hit) {
+            if (h.light_index != 0xffffffffu) gn = area_normal(sc.lights[h.light_index]);
+            else {
+                gn = normal_tetra(g, ro + rd * h.t, r_max(h.t * pixel_cone * R(0.5), R(1e-4)) * sc.pixel_tolerance);
+                res.de_evals += 4;
+            }
+            if (bounce == 0) { first_depth = h.t; aux[0] = gn.x; aux[1] = gn.y; aux[2] = gn.z; aux[3] = R(h.steps); }
+        }
+        if (!h.hit) break;  // no environment: a miss adds nothing
+        V3<R> p = ro + rd * h.t;
+        if (h.light_index != 0xffffffffu) {
+            if (bounce == 0) {
+                first_depth = h.t;
+                V3<R> en = area_normal(sc.lights[h.light_index]);
+                aux[0] = en.x; aux[1] = en.y; aux[2] = en.z; aux[3] = R(h.steps);
+            }
+            L = L + throughput * area_emission(sc, ro, rd, h.t, prev_pdf, prev_from_bsdf, prev_normal, prev_area_total);
+            break;
+        }
+        V3<R> n = gn;
+        if (bounce == 0) {
+            first_depth = h.t;
+            aux[0] = n.x; aux[1] = n.y; aux[2] = n.z; aux[3] = R(h.steps);
+            R x = r_clamp(R(float(h.steps)) / R(96), R(0), R(1));
+            throughput = throughput * (R(1) - sc.cavity * (x * x * (R(3) - R(2) * x)));
+        }
+        V3<R> v = -rd;
+        Surface<R> s = make_surface(sc, n, h.sample);
+        L = L + throughput * s.emission;
+        R offset = r_max(h.t * pixel_cone * R(2), R(1e-3)) * sc.pixel_tolerance;
+        V3<R> p_off = p + n * offset;
+        R nv = r_max(s.n.dot(v), R(1e-4));
+        R p_spec = spec_probability(s, nv);
+        R area_total = area_total_weight(sc, p_off, s.n);
+        bool last = bounce == sc.max_bounces;
+        // direct_light (pathtrace.wgsl:471-558), area emitters.
+        {
+            uint32_t selected = 0xffffffffu;
+            R selected_weight = 0;
+            if (area_total > R(0)) {
+                R threshold = rnd<R>(&rng) * area_total;
+                R sum = 0;
+                for (uint32_t i = 0; i < sc.light_count; ++i) {
+                    R w = area_weight(p_off, s.n, sc.lights[i]);
+                    sum += w;
+                    if (w > R(0)) {
+                        selected = i;
+                        selected_weight = w;
+                        if (threshold < sum) break;
+                    }
+                }
+            }
+            V3<R> Ld(0, 0, 0);
+            if (selected != 0xffffffffu) {
+                const Light<R>& l = sc.lights[selected];
+                R u1 = rnd<R>(&rng);
+                R u2 = rnd<R>(&rng);
+                V3<R> q = l.a + l.b * (u1 - R(0.5)) + l.c * (u2 - R(0.5));
+                V3<R> ln = area_normal(l);
+                V3<R> to_q = q - p_off;
+                R dist2 = to_q.dot(to_q);
+                if (dist2 >= R(1e-8)) {
+                    R dist = r_sqrt(dist2);
+                    V3<R> ldir = to_q / dist;
+                    R nl = s.n.dot(ldir);
+                    R cos_l = ln.dot(-ldir);
+                    if (!(nl <= R(0) || cos_l <= R(0) || n.dot(ldir) <= R(0))) {
+                        R endpoint = r_max(R(0), dist - r_max(R(1e-5), dist * R(1e-6)));
+                        Hit<R> sh = trace_scene(g, sc, p_off, ldir, pixel_cone, endpoint, &res.de_evals);
+                        res.segments++;
+                        if (!sh.hit && !sh.exhausted) {
+                            R pl = (selected_weight / area_total) * area_direction_pdf(l, dist2, cos_l);
+                            R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
+                            R w = last ? R(1) : mis_power(pl, pb);
+                            Ld = brdf_eval(s, v, ldir) * nl * l.color * R(1) * w / pl;
+                        }
+                    }
+                }
+            }
+            L = L + throughput * Ld;
+        }
+        if (last) break;
+        R r0 = rnd<R>(&rng), r1 = rnd<R>(&rng), r2 = rnd<R>(&rng);
+        V3<R> ldir;
+        if (r0 < p_spec) {
+            V3<R> hh = sample_ggx_h(s.n, v, s.alpha, r1, r2);
+            V3<R> i = -v;
+            ldir = i - hh * (R(2) * hh.dot(i));
+        } else ldir = cosine_sample(s.n, r1, r2);
+        R nl = s.n.dot(ldir);
+        if (nl <= R(0) || n.dot(ldir) <= R(0)) break;
+        R pdf = bsdf_pdf(s, v, ldir, p_spec);
+        if (pdf <= R(1e-6)) break;
+        throughput = throughput * (brdf_eval(s, v, ldir) * nl / pdf);
+        prev_pdf = pdf;
+        prev_from_bsdf = true;
+        prev_normal = s.n;
+        prev_area_total = area_total;
+        if (bounce >= 2) {
+            R q = r_clamp(r_max(throughput.x, r_max(throughput.y, throughput.z)), R(0.05), R(0.95));
+            if (rnd<R>(&rng) > q) break;
+            throughput = throughput / q;
+        }
+        ro = p_off;
+        rd = ldir;
+        bounce++;
+    }
+    bool ok = L.x == L.x && L.y == L.y && L.z == L.z && r_abs(L.x) < R(1e30) && r_abs(L.y) < R(1e30) &&
+              r_abs(L.z) < R(1e30);
+    res.L[0] = ok ? double(L.x) : 0.0;
+    res.L[1] = ok ? double(L.y) : 0.0;
+    res.L[2] = ok ? double(L.z) : 0.0;
+    res.depth = double(first_depth);
+    for (int i = 0; i < 4; ++i) res.aux[i] = double(aux[i]);
+    return res;
+}
+
+// ---------------------------------------------------------------- planar
+// PlanarFractal::sample (crates/syfrack-core/src/scene/planar.rs:77-194).
+template <class R> Sample<R> planar_sample(const PlanarParams& f, V2<R> input) {
+    auto cmul = [](V2<R> a, V2<R> b) { return V2<R>(a.x * b.x - a.y * b.y, a.x * b.y + a.y * b.x); };
+    auto cpow = [&](V2<R> z, uint32_t n) { V2<R> r(1, 0); for (uint32_t i = 0; i < n; ++i) r = cmul(r, z); return r; };
+    auto cdiv = [&](V2<R> a, V2<R> b) { return cmul(a, V2<R>(b.x, -b.y)) / r_max(b.length_squared(), R(1e-24)); };
+    R a = to_radians(R(f.angle));
+    R sn = r_sin(a), cs = r_cos(a);
+    V2<R> point = V2<R>(cs * input.x - sn * input.y, sn * input.x + cs * input.y) / R(f.zoom);
+    if (R(f.inversion) != R(0)) point = point * (R(f.inversion) / r_max(point.length_squared(), R(1e-8)));
+    point = point + V2<R>(R(f.center[0]), R(f.center[1]));
+    bool parameter_plane = f.family == 1 || f.family == 2;
+    bool root = f.family == 3 || f.family == 4;
+    V2<R> c = parameter_plane ? point : V2<R>(R(f.julia[0]), R(f.julia[1]));
+    V2<R> z = parameter_plane ? V2<R>(0, 0) : point;
+    V2<R> previous(0, 0);
+    R tw = to_radians(R(f.twist));
+    V2<R> rotation(r_cos(tw), r_sin(tw));
+    V2<R> lambda = rotation * R(f.relaxation);
+    R ring = R(1e20), stripe = 0, previous_error = 1;
+    uint32_t count = 0, measured = 0;
+    R smooth = R(float(f.iterations));
+    bool escaped = false;
+    const R bail = R(f.bailout), stripes = R(f.stripes);
+    for (uint32_t it = 0; it < f.iterations; ++it) {
+        R radius = z.length();
+        if (radius > bail) { escaped = true; break; }
+        ring = r_min(ring, r_abs(radius - R(f.trap_radius)));
+        R angle = radius == R(0) ? R(0) : r_atan2(z.y, z.x);
+        stripe += R(0.5) + R(0.5) * r_sin(stripes * angle);
+        measured += 1;
+        if (root) {
+            V2<R> residual = cpow(z, f.power) - V2<R>(1, 0);
+            if (f.family == 3 && residual.length_squared() < R(1e-12)) {
+                R error = r_max(residual.length(), R(1e-20));
+                R fraction = r_clamp(r_log(R(1e-6) / previous_error) / r_log(error / previous_error), R(0), R(1));
+                smooth = count == 0 ? R(0) : R(float(count)) - R(1) + fraction;
+                break;
+            }
+            previous_error = r_max(residual.length(), R(1e-20));
+            V2<R> old = z;
+            V2<R> derivative = cpow(z, f.power - 1) * R(float(f.power));
+            z = z - cmul(lambda, cdiv(residual, derivative));
+            if (f.family == 4) {
+                z = z + c;
+                if ((z - old).length_squared() < R(1e-12)) { count += 1; smooth = R(float(count)); break; }
+            }
+        } else {
+            V2<R> base = f.family == 2 ? V2<R>(r_abs(z.x), r_abs(z.y)) : z;
+            V2<R> next = cmul(rotation, cpow(base, f.power)) + c;
+            if (f.family == 5) next = next + previous * R(f.memory);
+            previous = z;
+            z = next;
+        }
+        count += 1;
+    }
+    R radius = r_min(z.length(), R(1e20));
+    escaped = escaped || radius > bail;
+    R lnp = r_log(R(float(f.power)));
+    if (escaped && !root) smooth = R(float(count)) + R(1) - r_log(r_log(r_max(radius, R(1.0001)))) / lnp;
+    else if (escaped) smooth = R(float(count));
+    const R TAU = R(6.28318530717958647692);
+    R final_angle = radius == R(0) ? R(0.5) : r_atan2(z.y, z.x) / TAU + R(0.5);
+    R bands = stripe / R(float(std::max<uint32_t>(measured, 1)));
+    if (escaped && !root && measured > 0) {
+        R angle = radius == R(0) ? R(0) : r_atan2(z.y, z.x);
+        R last = R(0.5) + R(0.5) * r_sin(stripes * angle);
+        R full = (stripe + last) / R(float(measured + 1));
+        R t = r_clamp(R(1) + (r_log(r_log(bail)) - r_log(r_log(r_max(radius, R(1.0001))))) / lnp, R(0), R(1));
+        bands += (full - bands) * t;
+    }
+    Sample<R> out;
+    out.material = 0;
+    out.distance = radius / (R(1) + radius);
+    out.iterations = count;
+    out.traps[0] = r_clamp(smooth / R(float(f.iterations)), R(0), R(1));
+    out.traps[1] = ring / (R(1) + ring);
+    out.traps[2] = bands;
+    out.traps[3] = final_angle;
+    return out;
+}
+
+// explicit instantiations
+template Sample<float> evaluate<float>(const Graph&, V3<float>);
+template Sample<double> evaluate<double>(const Graph&, V3<double>);
+template Scene<float> make_scene<float>(const Graph&, const sf_scene_desc&, const sf_render_config&);
+template Scene<double> make_scene<double>(const Graph&, const sf_scene_desc&, const sf_render_config&);
+template PixelResult radiance<float>(const Graph&, const Scene<float>&, uint32_t, uint32_t, uint32_t);
+template PixelResult radiance<double>(const Graph&, const Scene<double>&, uint32_t, uint32_t, uint32_t);
+template Hit<float> march_segment<float>(const Graph&, V3<float>, V3<float>, float, float, float, uint32_t, bool, float, uint64_t*);
+template Hit<double> march_segment<double>(const Graph&, V3<double>, V3<double>, double, double, double, uint32_t, bool, double, uint64_t*);
+template V3<float> normal_tetra<float>(const Graph&, V3<float>, float);
+template V3<double> normal_tetra<double>(const Graph&, V3<double>, double);
+template V3<float> normal_central<float>(const Graph&, V3<float>, float);
+template V3<double> normal_central<double>(const Graph&, V3<double>, double);
+template Sample<float> planar_sample<float>(const PlanarParams&, V2<float>);
+template Sample<double> planar_sample<double>(const PlanarParams&, V2<double>);
+
+}  // namespace orc

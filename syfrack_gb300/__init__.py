@@ -1,0 +1,15 @@
+"""syfrack_gb300: SyFrack's distance-estimator hot path on GB300 (sm_103a).
+
+The compute lives in libsyfrack_gpu.so (C ABI: include/syfrack_gpu.h); this
+package is its ctypes binding with the reference's Rust API names.
+"""
+from . import abi, ron
+from .graph import Graph, Kind, Link, Node
+from .render import (Canvas, CompiledGraph, DeSample, GpuContext, PlanarFractal, RenderOutput, Renderer,
+                     RenderSession, deep_zoom, escape2d)
+from .scene import AreaLight, Camera, Finish, Material, RenderConfig, Scene, SurfaceVariation
+from ._lib import SyfrackError
+
+__all__ = ["abi", "ron", "Graph", "Kind", "Link", "Node", "Canvas", "CompiledGraph", "DeSample", "GpuContext",
+           "PlanarFractal", "RenderOutput", "Renderer", "RenderSession", "deep_zoom", "escape2d", "AreaLight",
+           "Camera", "Finish", "Material", "RenderConfig", "Scene", "SurfaceVariation", "SyfrackError"]

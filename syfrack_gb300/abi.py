@@ -1,0 +1,96 @@
+"""ctypes mirror of include/syfrack_gpu.h (the C ABI of libsyfrack_gpu.so)."""
+from __future__ import annotations
+
+import ctypes as C
+
+SF_OK = 0
+STATUS_NAMES = {
+    0: "SF_OK", 1: "SF_ERR_INVALID", 2: "SF_ERR_GRAPH", 3: "SF_ERR_UNSUPPORTED",
+    4: "SF_ERR_CUDA", 5: "SF_ERR_OOM", 6: "SF_ERR_TIMEOUT", 7: "SF_ERR_BUDGET",
+    8: "SF_ERR_IO", 9: "SF_ERR_CHECKPOINT", 10: "SF_ERR_WAVEFRONT", 11: "SF_ERR_NO_DEVICE",
+}
+
+# enum sf_node_kind: the order of NodeKind (crates/syfrack-core/src/scene/graph/mod.rs:105-257)
+NODE_KINDS = [
+    "Input", "Output", "Translate", "Rotate", "Scale", "ScaleAxes", "Mirror", "BoxFold",
+    "BoxFoldAxes", "SphereInversion", "SphereFold", "Abs", "MengerFold", "Kaleido", "Power",
+    "AddOrigin", "AddSeed", "AddConstant", "Twist", "Bend", "Tile", "RepeatFinite", "Iterate",
+    "Trap", "Sphere", "Torus", "Cylinder", "Box", "RoundBox", "Rock", "Plane", "NormFence",
+    "BulbFence", "MaterialTag", "Bounded", "Instances", "Union", "Intersection", "Subtraction",
+    "SmoothUnion", "SmoothIntersection",
+]
+KIND_ID = {k: i for i, k in enumerate(NODE_KINDS)}
+MEASURES = ["Norm", "AxisX", "AxisY", "AxisZ", "PlaneY", "AngleXY", "AngleXZ", "AngleYZ", "LogNorm"]
+TRAP_MODES = ["Minimum", "Maximum", "Last"]
+FORMS = {0: "generic", 1: "bulb", 2: "box", 3: "menger"}
+
+SF_MAX_LIGHTS = 8
+SF_MAX_FINISHES = 8
+INTEGRATOR_MEGAKERNEL = 0
+INTEGRATOR_WAVEFRONT = 1
+
+
+class sf_node(C.Structure):
+    _fields_ = [("id", C.c_uint32), ("kind", C.c_uint32), ("enabled", C.c_uint32),
+                ("body_offset", C.c_uint32), ("body_len", C.c_uint32),
+                ("u", C.c_uint32 * 3), ("f", C.c_float * 8)]
+
+
+class sf_link(C.Structure):
+    _fields_ = [("from_node", C.c_uint32), ("from_port", C.c_uint32),
+                ("to_node", C.c_uint32), ("to_port", C.c_uint32)]
+
+
+class sf_graph_desc(C.Structure):
+    _fields_ = [("nodes", C.POINTER(sf_node)), ("node_count", C.c_uint32),
+                ("links", C.POINTER(sf_link)), ("link_count", C.c_uint32),
+                ("body_ids", C.POINTER(C.c_uint32)), ("body_id_count", C.c_uint32),
+                ("safety", C.c_float), ("bounding_radius_hint", C.c_float)]
+
+
+class sf_de_sample(C.Structure):
+    _fields_ = [("distance", C.c_float), ("traps", C.c_float * 4),
+                ("iterations", C.c_uint32), ("material", C.c_uint32)]
+
+
+class sf_graph_info(C.Structure):
+    _fields_ = [("step_scale", C.c_float), ("lipschitz", C.c_float), ("trap_scales", C.c_float * 4),
+                ("iteration_product", C.c_uint32), ("form", C.c_uint32), ("op_count", C.c_uint32),
+                ("bounding_radius_hint", C.c_float)]
+
+
+class sf_camera(C.Structure):
+    _fields_ = [("origin", C.c_float * 3), ("forward", C.c_float * 3), ("right", C.c_float * 3),
+                ("up", C.c_float * 3), ("tan_half_fov", C.c_float), ("aspect", C.c_float),
+                ("lens_radius", C.c_float), ("focus_distance", C.c_float)]
+
+
+class sf_material(C.Structure):
+    _fields_ = [("albedo", C.c_float * 3), ("roughness", C.c_float), ("metallic", C.c_float),
+                ("specular", C.c_float), ("emission", C.c_float * 3)]
+
+
+class sf_area_light(C.Structure):
+    _fields_ = [("center", C.c_float * 3), ("edge_u", C.c_float * 3), ("edge_v", C.c_float * 3),
+                ("radiance", C.c_float * 3)]
+
+
+class sf_scene_desc(C.Structure):
+    _fields_ = [("camera", sf_camera), ("material", sf_material),
+                ("finishes", sf_material * SF_MAX_FINISHES), ("finish_count", C.c_uint32),
+                ("lights", sf_area_light * SF_MAX_LIGHTS), ("light_count", C.c_uint32),
+                ("variation_slot", C.c_uint32), ("variation_enabled", C.c_uint32),
+                ("variation_roughness", C.c_float * 2), ("variation_metallic", C.c_float * 2),
+                ("cavity_darkness", C.c_float), ("seed", C.c_uint64)]
+
+
+class sf_render_config(C.Structure):
+    _fields_ = [("integrator", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
+                ("samples_per_pixel", C.c_uint32), ("max_bounces", C.c_uint32),
+                ("max_steps", C.c_uint32), ("pixel_tolerance", C.c_float),
+                ("tile_size", C.c_uint32), ("samples_per_dispatch", C.c_uint32)]
+
+
+class sf_tile(C.Structure):
+    _fields_ = [("x", C.c_uint32), ("y", C.c_uint32), ("w", C.c_uint32), ("h", C.c_uint32),
+                ("done", C.c_uint32)]

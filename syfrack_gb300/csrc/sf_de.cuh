@@ -1,0 +1,581 @@
+// Distance-estimator evaluation on sm_103a.
+//
+// Device twin of the reference's CPU interpreter (crates/syfrack-core/src/
+// scene/graph/eval.rs:346-826) and of the generated WGSL `de_sample`
+// (crates/syfrack-render/src/graph_wgsl.rs:385-681). FP32 throughout.
+// Three iterated forms have straight-line routines selected on the host; every
+// other supported graph runs through the postfix interpreter at the end.
+#pragma once
+#include <math.h>
+#include <stdint.h>
+
+#include "../../include/syfrack_gpu.h"
+#include "sf_program.h"
+
+#define SF_INF __int_as_float(0x7f800000)
+
+// ------------------------------------------------------------------ float3 helpers
+__device__ __forceinline__ float3 mk3(float x, float y, float z) { return make_float3(x, y, z); }
+__device__ __forceinline__ float3 operator+(float3 a, float3 b) { return mk3(a.x + b.x, a.y + b.y, a.z + b.z); }
+__device__ __forceinline__ float3 operator-(float3 a, float3 b) { return mk3(a.x - b.x, a.y - b.y, a.z - b.z); }
+__device__ __forceinline__ float3 operator-(float3 a) { return mk3(-a.x, -a.y, -a.z); }
+__device__ __forceinline__ float3 operator*(float3 a, float s) { return mk3(a.x * s, a.y * s, a.z * s); }
+__device__ __forceinline__ float3 operator*(float3 a, float3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
+__device__ __forceinline__ float3 operator/(float3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
+__device__ __forceinline__ float3 operator/(float3 a, float3 b) { return mk3(a.x / b.x, a.y / b.y, a.z / b.z); }
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+__device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
+__device__ __forceinline__ float3 abs3(float3 a) { return mk3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
+__device__ __forceinline__ float3 cross3(float3 a, float3 b) {
+    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+}
+__device__ __forceinline__ float3 ld3(const float* f) { return mk3(f[0], f[1], f[2]); }
+__device__ __forceinline__ float max3(float3 a) { return fmaxf(fmaxf(a.x, a.y), a.z); }
+__device__ __forceinline__ float min3(float3 a) { return fminf(fminf(a.x, a.y), a.z); }
+__device__ __forceinline__ float3 clamp3(float3 v, float lo, float hi) {
+    return mk3(fminf(fmaxf(v.x, lo), hi), fminf(fmaxf(v.y, lo), hi), fminf(fmaxf(v.z, lo), hi));
+}
+__device__ __forceinline__ float3 normalize3(float3 v) { return v / len3(v); }
+// glam try_normalize().unwrap_or(Y) (common.wgsl:241-246).
+__device__ __forceinline__ float3 safe_normalize3(float3 v) {
+    float l = len3(v);
+    float rcp = 1.0f / l;
+    if (!(l > 0.0f) || !(rcp > 0.0f) || !(rcp <= 3.4028235e38f)) return mk3(0.f, 1.f, 0.f);
+    return v * rcp;
+}
+__device__ __forceinline__ float rem_euclid(float x, float m) {
+    float r = fmodf(x, m);
+    return r < 0.0f ? r + fabsf(m) : r;
+}
+
+// Raw DE state before normalisation (eval.rs DistState :14-19).
+struct DeRaw {
+    float d;
+    float t0, t1, t2, t3;  // raw trap slots (+inf = unwritten)
+    uint32_t iter;
+    uint32_t material;
+};
+
+// Normalised sample (PreparedGraph::evaluate, eval.rs:98-114).
+struct DeSampleF {
+    float d;
+    float traps[4];
+    uint32_t iter;
+    uint32_t material;
+};
+
+__device__ __forceinline__ float trap_norm(float t, float scale) {
+    return isfinite(t) ? fminf(t / scale, 1.0f) : 1.0f;
+}
+__device__ __forceinline__ DeSampleF de_finalize(const DeProgram& P, const DeRaw& r) {
+    DeSampleF s;
+    s.d = r.d;
+    s.traps[0] = trap_norm(r.t0, P.trap_scales[0]);
+    s.traps[1] = trap_norm(r.t1, P.trap_scales[1]);
+    s.traps[2] = trap_norm(r.t2, P.trap_scales[2]);
+    s.traps[3] = trap_norm(r.t3, P.trap_scales[3]);
+    s.iter = min(r.iter, P.iteration_product);
+    s.material = r.material;
+    return s;
+}
+
+// measure (eval.rs:299-331).
+__device__ __forceinline__ float trap_measure(uint32_t m, float3 p) {
+    const float TAU = 6.2831855f;
+    switch (m) {
+    case SF_MEASURE_AXIS_X: return sqrtf(p.y * p.y + p.z * p.z);
+    case SF_MEASURE_AXIS_Y: return sqrtf(p.x * p.x + p.z * p.z);
+    case SF_MEASURE_AXIS_Z: return sqrtf(p.x * p.x + p.y * p.y);
+    case SF_MEASURE_PLANE_Y: return fabsf(p.y);
+    case SF_MEASURE_ANGLE_XY: return (p.x == 0.f && p.y == 0.f) ? 0.5f : atan2f(p.y, p.x) / TAU + 0.5f;
+    case SF_MEASURE_ANGLE_XZ: return (p.x == 0.f && p.z == 0.f) ? 0.5f : atan2f(p.z, p.x) / TAU + 0.5f;
+    case SF_MEASURE_ANGLE_YZ: return (p.y == 0.f && p.z == 0.f) ? 0.5f : atan2f(p.z, p.y) / TAU + 0.5f;
+    case SF_MEASURE_LOG_NORM: return log1pf(len3(p));
+    default: return len3(p);
+    }
+}
+// Trap slot update (eval.rs:533-552) on four named registers (no local memory).
+__device__ __forceinline__ float trap_mode_apply(uint32_t mode, float old, float v) {
+    if (mode == SF_TRAP_LAST) return v;
+    if (mode == SF_TRAP_MAXIMUM) return old >= 1e30f ? v : fmaxf(old, v);
+    return fminf(old, v);
+}
+__device__ __forceinline__ void trap_update(DeRaw& s, uint32_t slot, uint32_t mode, float v) {
+    if (slot == 0) s.t0 = trap_mode_apply(mode, s.t0, v);
+    else if (slot == 1) s.t1 = trap_mode_apply(mode, s.t1, v);
+    else if (slot == 2) s.t2 = trap_mode_apply(mode, s.t2, v);
+    else s.t3 = trap_mode_apply(mode, s.t3, v);
+}
+
+// integral_spherical_power (eval.rs:129-178): complex powers of the polar and
+// azimuthal unit vectors; n = 6, 8 by repeated squaring, other n by binary powers.
+__device__ __forceinline__ void spherical_power(float3 p, float r, uint32_t n, float3& out, float& deriv) {
+    if (n == 1) { out = p; deriv = 1.0f; return; }
+    float rho = sqrtf(p.x * p.x + p.y * p.y);
+    float tx = fminf(fmaxf(p.z / r, -1.0f), 1.0f), ty = rho / r;
+    float fx = 1.0f, fy = 0.0f;
+    if (rho > 0.0f) { fx = p.x / rho; fy = p.y / rho; }
+    if (n == 8 || n == 6) {
+        float t2x = tx * tx - ty * ty, t2y = 2.0f * tx * ty;
+        float f2x = fx * fx - fy * fy, f2y = 2.0f * fx * fy;
+        float t4x = t2x * t2x - t2y * t2y, t4y = 2.0f * t2x * t2y;
+        float f4x = f2x * f2x - f2y * f2y, f4y = 2.0f * f2x * f2y;
+        float r2 = r * r, r4 = r2 * r2;
+        float ax, ay, bx, by, prev;
+        if (n == 6) {
+            ax = t2x * t4x - t2y * t4y; ay = t2x * t4y + t2y * t4x;
+            bx = f2x * f4x - f2y * f4y; by = f2x * f4y + f2y * f4x;
+            prev = r4 * r;
+        } else {
+            ax = t4x * t4x - t4y * t4y; ay = 2.0f * t4x * t4y;
+            bx = f4x * f4x - f4y * f4y; by = 2.0f * f4x * f4y;
+            prev = r4 * r2 * r;
+        }
+        float m = prev * r;
+        out = mk3(ay * bx * m, ay * by * m, ax * m);
+        deriv = float(n) * prev;
+        return;
+    }
+    float ax = 1.f, ay = 0.f, bx = 1.f, by = 0.f;
+    uint32_t e = n;
+    while (e != 0) {
+        if (e & 1u) {
+            float nx = ax * tx - ay * ty, ny = ax * ty + ay * tx; ax = nx; ay = ny;
+            nx = bx * fx - by * fy; ny = bx * fy + by * fx; bx = nx; by = ny;
+        }
+        e >>= 1;
+        if (e != 0) {
+            float nx = tx * tx - ty * ty, ny = tx * ty + ty * tx; tx = nx; ty = ny;
+            nx = fx * fx - fy * fy; ny = fx * fy + fy * fx; fx = nx; fy = ny;
+        }
+    }
+    float prev = 1.0f;
+    for (uint32_t i = 1; i < n; ++i) prev *= r;
+    float m = prev * r;
+    out = mk3(ay * bx * m, ay * by * m, ax * m);
+    deriv = float(n) * prev;
+}
+
+// Power node (eval.rs:456-476), including the trigonometric path for
+// non-integer exponents and radii below 1e-12.
+__device__ __forceinline__ void power_op(float3& p, float& dr, float radius, float power, uint32_t power_int) {
+    if (radius >= 1e-12f && power_int != 0) {
+        float3 q;
+        float dv;
+        spherical_power(p, radius, power_int, q, dv);
+        p = q;
+        dr *= dv;
+        return;
+    }
+    float r = fmaxf(radius, 1e-12f);
+    float theta = radius >= 1e-12f ? atan2f(sqrtf(p.x * p.x + p.y * p.y), p.z)
+                                   : acosf(fminf(fmaxf(p.z / r, -1.0f), 1.0f));
+    float phi = atan2f(p.y, p.x);
+    dr *= powf(r, power - 1.0f) * power;
+    float zr = powf(r, power);
+    float st, ct, sp, cp;
+    sincosf(theta * power, &st, &ct);
+    sincosf(phi * power, &sp, &cp);
+    p = mk3(st * cp, st * sp, ct) * zr;
+}
+
+__device__ __forceinline__ float bulb_fence(float3 p, float dr) {
+    float r = fmaxf(len3(p), 1e-12f);
+    return 0.5f * logf(r) * r / dr;
+}
+__device__ __forceinline__ float box_fence(float3 p, float3 half, float dr) {
+    float3 q = abs3(p) - half;
+    float3 qm = mk3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
+    return (len3(qm) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f)) / dr;
+}
+
+__device__ __forceinline__ DeRaw raw_empty() {
+    DeRaw r;
+    r.d = SF_INF; r.t0 = r.t1 = r.t2 = r.t3 = SF_INF; r.iter = 0; r.material = 0;
+    return r;
+}
+
+// ------------------------------------------------------------------ specialised forms
+// Mandelbulb: Iterate{Trap, Power, AddOrigin} -> BulbFence (graphs/mandelbulb.ron).
+__device__ __forceinline__ DeRaw de_bulb(const FormParams& f, float3 p) {
+    DeRaw s = raw_empty();
+    const float3 c = p;
+    float dr = 1.0f;
+    const uint32_t n = f.iterations;
+    for (uint32_t i = 0; i < n; ++i) {
+        float r = len3(p);
+        if (r > f.bailout) break;
+        float v = f.trap_measure == SF_MEASURE_NORM ? r : trap_measure(f.trap_measure, p);
+        trap_update(s, f.trap_slot, f.trap_mode, v);
+        power_op(p, dr, r, f.power, f.power_int);
+        p = p + c;
+        dr += 1.0f;
+        s.iter++;
+    }
+    s.d = bulb_fence(p, dr);
+    s.material = f.material;
+    return s;
+}
+
+// Mandelbox: Iterate{BoxFold, Trap, SphereFold, Scale, AddOrigin} -> NormFence.
+__device__ __forceinline__ DeRaw de_box(const FormParams& f, float3 p) {
+    DeRaw s = raw_empty();
+    const float3 c = p;
+    float dr = 1.0f;
+    const uint32_t n = f.iterations;
+    const float l = f.limit;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (len3(p) > f.bailout) break;
+        p = clamp3(p, -l, l) * 2.0f - p;
+        float r2 = dot3(p, p);
+        float v = f.trap_measure == SF_MEASURE_NORM ? sqrtf(r2) : trap_measure(f.trap_measure, p);
+        trap_update(s, f.trap_slot, f.trap_mode, v);
+        float k = r2 < f.min_radius2 ? f.fold_k_min : (r2 < f.fixed_radius2 ? f.fixed_radius2 / r2 : 1.0f);
+        p = p * k;
+        dr *= k;
+        p = p * f.scale;
+        dr *= f.abs_scale;
+        p = p + c;
+        dr += 1.0f;
+        s.iter++;
+    }
+    s.d = (len3(p) - f.fence[0]) / fabsf(dr);
+    s.material = f.material;
+    return s;
+}
+
+// Menger: Iterate{MengerFold, Trap} -> Box (graphs/menger.ron).
+__device__ __forceinline__ DeRaw de_menger(const FormParams& f, float3 p) {
+    DeRaw s = raw_empty();
+    float dr = 1.0f;
+    const uint32_t n = f.iterations;
+    const float sc = f.scale;
+    const float3 off = mk3(f.offset[0], f.offset[1], f.offset[2]);
+    for (uint32_t i = 0; i < n; ++i) {
+        if (len3(p) > f.bailout) break;
+        float3 z = abs3(p);
+        if (z.x < z.y) z = mk3(z.y, z.x, z.z);
+        if (z.x < z.z) z = mk3(z.z, z.y, z.x);
+        if (z.y < z.z) z = mk3(z.x, z.z, z.y);
+        z = z * sc - off * (sc - 1.0f);
+        if (z.z < -0.5f * off.z * (sc - 1.0f)) z.z += off.z * (sc - 1.0f);
+        p = z;
+        dr *= sc;
+        float v = trap_measure(f.trap_measure, p);
+        trap_update(s, f.trap_slot, f.trap_mode, v);
+        s.iter++;
+    }
+    s.d = box_fence(p, mk3(f.fence[0], f.fence[1], f.fence[2]), dr);
+    s.material = f.material;
+    return s;
+}
+
+// ------------------------------------------------------------------ generic interpreter
+struct PState {
+    float3 p;
+    float dr;
+    uint32_t iter;
+    float t0, t1, t2, t3;
+};
+
+__device__ __forceinline__ float3 rotate_euler_xyz(float3 p, float3 a) {
+    float3 q = p;
+    q = mk3(cosf(a.z) * q.x - sinf(a.z) * q.y, sinf(a.z) * q.x + cosf(a.z) * q.y, q.z);
+    q = mk3(cosf(a.y) * q.x + sinf(a.y) * q.z, q.y, -sinf(a.y) * q.x + cosf(a.y) * q.z);
+    q = mk3(q.x, cosf(a.x) * q.y - sinf(a.x) * q.z, sinf(a.x) * q.y + cosf(a.x) * q.z);
+    return q;
+}
+__device__ __forceinline__ float to_rad(float d) { return d * (3.14159265358979323846f / 180.0f); }
+
+__device__ __forceinline__ float terrain_hash(int cx, int cy, int cz, uint32_t seed) {
+    uint32_t h = (uint32_t(cx) * 0x8da6b343u) ^ (uint32_t(cy) * 0xd8163841u) ^ (uint32_t(cz) * 0xcb1ab31fu) ^ seed;
+    h = (h ^ (h >> 16)) * 0x7feb352du;
+    h = (h ^ (h >> 15)) * 0x846ca68bu;
+    h ^= h >> 16;
+    return float(h >> 8) / 16777216.0f;
+}
+__device__ float terrain_noise(float3 p, uint32_t seed) {
+    float3 base = mk3(floorf(p.x), floorf(p.y), floorf(p.z));
+    float3 f = p - base;
+    float3 t = f * f * (mk3(3.f, 3.f, 3.f) - f * 2.0f);
+    int c0 = int(base.x), c1 = int(base.y), c2 = int(base.z);
+#define SF_MIX(a, b, t) ((a) + ((b) - (a)) * (t))
+    float a = SF_MIX(terrain_hash(c0, c1, c2, seed), terrain_hash(c0 + 1, c1, c2, seed), t.x);
+    float b = SF_MIX(terrain_hash(c0, c1 + 1, c2, seed), terrain_hash(c0 + 1, c1 + 1, c2, seed), t.x);
+    float d = SF_MIX(terrain_hash(c0, c1, c2 + 1, seed), terrain_hash(c0 + 1, c1, c2 + 1, seed), t.x);
+    float e = SF_MIX(terrain_hash(c0, c1 + 1, c2 + 1, seed), terrain_hash(c0 + 1, c1 + 1, c2 + 1, seed), t.x);
+    float r = SF_MIX(SF_MIX(a, b, t.y), SF_MIX(d, e, t.y), t.z);
+#undef SF_MIX
+    return r;
+}
+
+__device__ void apply_point_op(const DeOp& op, PState& s, float3 c, float3 seed_p, float seed_dr) {
+    switch (op.code) {
+    case SF_NODE_TRANSLATE: s.p = s.p + ld3(op.f); break;
+    case SF_NODE_ROTATE: s.p = rotate_euler_xyz(s.p, mk3(to_rad(op.f[0]), to_rad(op.f[1]), to_rad(op.f[2]))); break;
+    case SF_NODE_SCALE: s.p = s.p * op.f[0]; s.dr *= fabsf(op.f[0]); break;
+    case SF_NODE_SCALE_AXES: { float3 f = ld3(op.f); s.p = s.p * f; s.dr *= max3(f); break; }
+    case SF_NODE_MIRROR: {
+        float3 nn = safe_normalize3(ld3(op.f));
+        float h = dot3(s.p, nn) - op.f[3];
+        if (h < 0.0f) s.p = s.p - nn * (2.0f * h);
+        break;
+    }
+    case SF_NODE_BOX_FOLD: s.p = clamp3(s.p, -op.f[0], op.f[0]) * 2.0f - s.p; break;
+    case SF_NODE_BOX_FOLD_AXES: {
+        float3 l = ld3(op.f);
+        float3 fo = mk3(fminf(fmaxf(s.p.x, -l.x), l.x), fminf(fmaxf(s.p.y, -l.y), l.y), fminf(fmaxf(s.p.z, -l.z), l.z)) * 2.0f - s.p;
+        if (op.a & 1u) s.p.x = fo.x;
+        if (op.a & 2u) s.p.y = fo.y;
+        if (op.a & 4u) s.p.z = fo.z;
+        break;
+    }
+    case SF_NODE_SPHERE_INVERSION: {
+        float k = op.f[0] * op.f[0] / fmaxf(dot3(s.p, s.p), op.f[1] * op.f[1]);
+        s.p = s.p * k; s.dr *= k;
+        break;
+    }
+    case SF_NODE_SPHERE_FOLD: {
+        float r2 = dot3(s.p, s.p);
+        float mr2 = op.f[0] * op.f[0], fr2 = op.f[1] * op.f[1];
+        float k = r2 < mr2 ? fr2 / mr2 : (r2 < fr2 ? fr2 / r2 : 1.0f);
+        s.p = s.p * k; s.dr *= k;
+        break;
+    }
+    case SF_NODE_ABS:
+        if (op.a & 1u) s.p.x = fabsf(s.p.x);
+        if (op.a & 2u) s.p.y = fabsf(s.p.y);
+        if (op.a & 4u) s.p.z = fabsf(s.p.z);
+        break;
+    case SF_NODE_MENGER_FOLD: {
+        float sc = op.f[0];
+        float3 off = mk3(op.f[1], op.f[2], op.f[3]);
+        float3 z = abs3(s.p);
+        if (z.x < z.y) z = mk3(z.y, z.x, z.z);
+        if (z.x < z.z) z = mk3(z.z, z.y, z.x);
+        if (z.y < z.z) z = mk3(z.x, z.z, z.y);
+        z = z * sc - off * (sc - 1.0f);
+        if (z.z < -0.5f * off.z * (sc - 1.0f)) z.z += off.z * (sc - 1.0f);
+        s.p = z; s.dr *= sc;
+        break;
+    }
+    case SF_NODE_KALEIDO: {
+        float sector = 6.2831855f / float(op.a > 0 ? op.a : 1u);
+        float a = atan2f(s.p.z, s.p.x) + to_rad(op.f[0]);
+        a = fabsf(rem_euclid(a + sector * 0.5f, sector) - sector * 0.5f);
+        float r = sqrtf(s.p.x * s.p.x + s.p.z * s.p.z);
+        float sn, cs;
+        sincosf(a, &sn, &cs);
+        s.p.x = r * cs; s.p.z = r * sn;
+        break;
+    }
+    case SF_NODE_POWER: power_op(s.p, s.dr, len3(s.p), op.f[0], op.a); break;
+    case SF_NODE_ADD_ORIGIN: s.p = s.p + c; s.dr += 1.0f; break;
+    case SF_NODE_ADD_SEED: { float3 m = ld3(op.f); s.p = s.p + seed_p * m; s.dr += seed_dr * max3(abs3(m)); break; }
+    case SF_NODE_ADD_CONSTANT: {
+        float3 m = ld3(op.f);
+        s.p = s.p + (c * m + ld3(op.f + 3));
+        s.dr += max3(abs3(m));
+        break;
+    }
+    case SF_NODE_TWIST: {
+        float sn, cs; sincosf(op.f[0] * s.p.y, &sn, &cs);
+        float x = cs * s.p.x - sn * s.p.z, z = sn * s.p.x + cs * s.p.z;
+        s.p.x = x; s.p.z = z;
+        break;
+    }
+    case SF_NODE_BEND: {
+        float sn, cs; sincosf(op.f[0] * s.p.x, &sn, &cs);
+        float x = cs * s.p.x - sn * s.p.y, y = sn * s.p.x + cs * s.p.y;
+        s.p.x = x; s.p.y = y;
+        break;
+    }
+    case SF_NODE_TILE: {
+        float3 per = ld3(op.f), h = per * 0.5f;
+        s.p = mk3(rem_euclid(s.p.x + h.x, per.x) - h.x, rem_euclid(s.p.y + h.y, per.y) - h.y,
+                  rem_euclid(s.p.z + h.z, per.z) - h.z);
+        break;
+    }
+    case SF_NODE_REPEAT_FINITE: {
+        float3 per = ld3(op.f);
+        float3 last = mk3(float(op.a) - 1.0f, float(op.b) - 1.0f, float(op.c) - 1.0f);
+        float3 h = last * 0.5f;
+        float3 q = s.p / per + h + mk3(0.5f, 0.5f, 0.5f);
+        float3 cell = mk3(fminf(fmaxf(floorf(q.x), 0.f), last.x), fminf(fmaxf(floorf(q.y), 0.f), last.y),
+                          fminf(fmaxf(floorf(q.z), 0.f), last.z)) - h;
+        s.p = s.p - cell * per;
+        break;
+    }
+    case SF_NODE_TRAP: {
+        float v = trap_measure(op.b, s.p);
+        DeRaw tmp;
+        tmp.t0 = s.t0; tmp.t1 = s.t1; tmp.t2 = s.t2; tmp.t3 = s.t3;
+        trap_update(tmp, op.a, op.c, v);
+        s.t0 = tmp.t0; s.t1 = tmp.t1; s.t2 = tmp.t2; s.t3 = tmp.t3;
+        break;
+    }
+    default: break;
+    }
+}
+
+// fence (eval.rs:558-599).
+__device__ float fence_op(const DeOp& op, const PState& s) {
+    switch (op.code) {
+    case SF_NODE_SPHERE: return (len3(s.p) - op.f[0]) / s.dr;
+    case SF_NODE_TORUS: {
+        float q = sqrtf(s.p.x * s.p.x + s.p.z * s.p.z) - op.f[0];
+        return (sqrtf(q * q + s.p.y * s.p.y) - op.f[1]) / s.dr;
+    }
+    case SF_NODE_CYLINDER: {
+        float qx = sqrtf(s.p.x * s.p.x + s.p.z * s.p.z) - op.f[0], qy = fabsf(s.p.y) - op.f[1];
+        float mx = fmaxf(qx, 0.f), my = fmaxf(qy, 0.f);
+        return (sqrtf(mx * mx + my * my) + fminf(fmaxf(qx, qy), 0.0f)) / s.dr;
+    }
+    case SF_NODE_BOX: return box_fence(s.p, ld3(op.f), s.dr);
+    case SF_NODE_ROUND_BOX: {
+        float3 half = ld3(op.f);
+        float r = fminf(op.f[3], min3(half));
+        float3 q = abs3(s.p) - (half - mk3(r, r, r));
+        float3 qm = mk3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
+        return (len3(qm) + fminf(max3(q), 0.0f) - r) / s.dr;
+    }
+    case SF_NODE_ROCK: {
+        float3 half = ld3(op.f);
+        float e = op.f[3];
+        float h = min3(half);
+        float3 q = s.p * (1.15f / h);
+        float relief = 0.57f * terrain_noise(q, op.a) + 0.29f * terrain_noise(q * 2.03f, op.a + 97u) +
+                       0.14f * terrain_noise(q * 4.17f, op.a + 193u) - 0.5f;
+        return ((len3(s.p / half) - 1.0f - e * relief) * h / (1.0f + 5.22f * e)) / s.dr;
+    }
+    case SF_NODE_PLANE: return (dot3(s.p, safe_normalize3(ld3(op.f))) - op.f[3]) / s.dr;
+    case SF_NODE_NORM_FENCE: return (len3(s.p) - op.f[0]) / fabsf(s.dr);
+    case SF_NODE_BULB_FENCE: return bulb_fence(s.p, s.dr);
+    default: return SF_INF;
+    }
+}
+
+__device__ __forceinline__ DeRaw dist_from(const PState& s, float d) {
+    DeRaw r;
+    r.d = d; r.material = 0; r.iter = s.iter;
+    r.t0 = s.t0; r.t1 = s.t1; r.t2 = s.t2; r.t3 = s.t3;
+    return r;
+}
+
+// combine (eval.rs:601-657).
+__device__ DeRaw combine_op(uint32_t kind, float k, DeRaw a, DeRaw b) {
+    auto blend = [&](float h, float d) {
+        DeRaw r;
+        float ta[4] = {a.t0, a.t1, a.t2, a.t3}, tb[4] = {b.t0, b.t1, b.t2, b.t3}, tr[4];
+#pragma unroll
+        for (int i = 0; i < 4; ++i) {
+            bool fa = isfinite(ta[i]), fb = isfinite(tb[i]);
+            tr[i] = (fa && fb) ? tb[i] + (ta[i] - tb[i]) * h : (fa ? ta[i] : (fb ? tb[i] : SF_INF));
+        }
+        r.t0 = tr[0]; r.t1 = tr[1]; r.t2 = tr[2]; r.t3 = tr[3];
+        r.d = d;
+        r.material = h >= 0.5f ? a.material : b.material;
+        r.iter = h >= 0.5f ? a.iter : b.iter;
+        return r;
+    };
+    switch (kind) {
+    case SF_NODE_UNION: { DeRaw r = a.d <= b.d ? a : b; r.d = fminf(a.d, b.d); return r; }
+    case SF_NODE_INTERSECTION: { DeRaw r = a.d >= b.d ? a : b; r.d = fmaxf(a.d, b.d); return r; }
+    case SF_NODE_SUBTRACTION: { DeRaw r = a; r.d = fmaxf(a.d, -b.d); return r; }
+    case SF_NODE_SMOOTH_UNION: {
+        if (a.d >= 1e30f) return b;
+        if (b.d >= 1e30f) return a;
+        float h = fminf(fmaxf(0.5f + 0.5f * (b.d - a.d) / k, 0.0f), 1.0f);
+        return blend(h, b.d + (a.d - b.d) * h - k * h * (1.0f - h));
+    }
+    case SF_NODE_SMOOTH_INTERSECTION: {
+        if (a.d >= 1e30f) { DeRaw r = b; r.d = SF_INF; return r; }
+        if (b.d >= 1e30f) { DeRaw r = a; r.d = SF_INF; return r; }
+        float h = fminf(fmaxf(0.5f - 0.5f * (b.d - a.d) / k, 0.0f), 1.0f);
+        return blend(h, b.d + (a.d - b.d) * h + k * h * (1.0f - h));
+    }
+    default: return a;
+    }
+}
+
+// Postfix interpreter over DeProgram.ops (generic graphs).
+__device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
+    PState s;
+    s.p = c; s.dr = 1.0f; s.iter = 0; s.t0 = s.t1 = s.t2 = s.t3 = SF_INF;
+    uint32_t loop_count[SF_MAX_LOOP_DEPTH];
+    float3 loop_seed[SF_MAX_LOOP_DEPTH];
+    float loop_seed_dr[SF_MAX_LOOP_DEPTH];
+    int depth = 0;
+    DeRaw stack[SF_MAX_DIST_STACK];
+    int sp = 0;
+    float3 seed_p = c;
+    float seed_dr = 1.0f;
+    const uint32_t n = P.n_ops;
+    for (uint32_t pc = 0; pc < n; ++pc) {
+        const DeOp& op = P.ops[pc];
+        switch (op.code) {
+        case SF_OP_BEGIN:
+            s.p = c; s.dr = 1.0f; s.iter = 0; s.t0 = s.t1 = s.t2 = s.t3 = SF_INF;
+            seed_p = c; seed_dr = 1.0f; depth = 0;
+            break;
+        case SF_OP_ITER_BEGIN:
+            if (op.a == 0 || len3(s.p) > op.f[0] || depth >= SF_MAX_LOOP_DEPTH) { pc = op.b; break; }
+            loop_count[depth] = 0;
+            loop_seed[depth] = s.p;
+            loop_seed_dr[depth] = s.dr;
+            seed_p = s.p; seed_dr = s.dr;
+            depth++;
+            break;
+        case SF_OP_ITER_END: {
+            const DeOp& b = P.ops[op.a];
+            s.iter += 1;
+            uint32_t cnt = ++loop_count[depth - 1];
+            if (cnt < b.a && !(len3(s.p) > b.f[0])) {
+                pc = op.a;  // continue at the first body op (pc++ follows)
+                seed_p = loop_seed[depth - 1];
+                seed_dr = loop_seed_dr[depth - 1];
+            } else {
+                depth--;
+                if (depth > 0) { seed_p = loop_seed[depth - 1]; seed_dr = loop_seed_dr[depth - 1]; }
+                else { seed_p = s.p; seed_dr = s.dr; }
+            }
+            break;
+        }
+        case SF_OP_FENCE_OFF:
+            if (sp < SF_MAX_DIST_STACK) stack[sp++] = dist_from(s, SF_INF);
+            break;
+        case SF_OP_EMPTY:
+            if (sp < SF_MAX_DIST_STACK) stack[sp++] = raw_empty();
+            break;
+        case SF_OP_TAG:
+            if (sp > 0) stack[sp - 1].material = op.a;
+            break;
+        case SF_OP_BOUND:
+            if (sp > 0) stack[sp - 1].d = fmaxf(stack[sp - 1].d, box_fence(s.p, ld3(op.f), s.dr));
+            break;
+        case SF_OP_COMBINE:
+            if (sp >= 2) { stack[sp - 2] = combine_op(op.a, op.f[0], stack[sp - 2], stack[sp - 1]); sp--; }
+            break;
+        default:
+            if (op.code >= SF_NODE_SPHERE && op.code <= SF_NODE_BULB_FENCE) {
+                if (sp < SF_MAX_DIST_STACK) stack[sp++] = dist_from(s, fence_op(op, s));
+            } else {
+                // outside any Iterate, AddSeed reinjects the point entering this node
+                if (depth == 0) { seed_p = s.p; seed_dr = s.dr; }
+                apply_point_op(op, s, c, seed_p, seed_dr);
+            }
+            break;
+        }
+    }
+    return sp > 0 ? stack[sp - 1] : raw_empty();
+}
+
+// Entry point: raw DE at p for the program's form.
+__device__ __forceinline__ DeRaw de_raw(const DeProgram& P, float3 p) {
+    switch (P.form) {
+    case SF_FORM_BULB: return de_bulb(P.fp, p);
+    case SF_FORM_BOX: return de_box(P.fp, p);
+    case SF_FORM_MENGER: return de_menger(P.fp, p);
+    default: return de_generic(P, p);
+    }
+}

@@ -1,0 +1,1648 @@
+// Host side of the C ABI (include/syfrack_gpu.h): graph validation and
+// lowering, device context with HBM admission, DE probe, primary rays, render
+// sessions with tile scheduling and checkpoints, escape time and deep zoom.
+#include <cuda_runtime.h>
+
+#include <algorithm>
+#include <chrono>
+#include <cmath>
+#include <cstdio>
+#include <cstring>
+#include <fstream>
+#include <functional>
+#include <map>
+#include <mutex>
+#include <set>
+#include <string>
+#include <thread>
+#include <vector>
+
+#include <sys/stat.h>
+#include <unistd.h>
+
+#include "../../include/syfrack_gpu.h"
+#include "sf_kernels.cuh"
+#include "sf_program.h"
+
+namespace {
+
+thread_local std::string g_error;
+
+sf_status fail(sf_status s, const std::string& msg) {
+    g_error = msg;
+    return s;
+}
+sf_status cuda_fail(cudaError_t e, const char* what) {
+    g_error = std::string(what) + ": " + cudaGetErrorString(e);
+    return e == cudaErrorMemoryAllocation ? SF_ERR_OOM : SF_ERR_CUDA;
+}
+#define CU(expr)                                               \
+    do {                                                       \
+        cudaError_t _e = (expr);                               \
+        if (_e != cudaSuccess) return cuda_fail(_e, #expr);    \
+    } while (0)
+
+constexpr uint32_t MAX_DEPTH = 3;          // graph/mod.rs:41
+constexpr uint32_t ABI_VERSION = (1u << 16) | 0u;
+
+// ------------------------------------------------------------------ graph preparation
+struct HostGraph {
+    std::vector<sf_node> nodes;
+    std::vector<sf_link> links;
+    std::vector<uint32_t> body;
+    float safety = 1.f, hint = 1.f;
+
+    const sf_node* node(uint32_t id) const {
+        for (auto& n : nodes)
+            if (n.id == id) return &n;
+        return nullptr;
+    }
+    bool input_of(uint32_t to, uint32_t port, uint32_t* from) const {
+        for (auto& l : links)
+            if (l.to_node == to && l.to_port == port) { *from = l.from_node; return true; }
+        return false;
+    }
+    std::vector<uint32_t> body_of(const sf_node& n) const {
+        std::vector<uint32_t> b;
+        if (n.kind == SF_NODE_ITERATE)
+            for (uint32_t i = 0; i < n.body_len; ++i) b.push_back(body[n.body_offset + i]);
+        return b;
+    }
+};
+
+bool is_point_kind(uint32_t k) {
+    switch (k) {
+    case SF_NODE_TRANSLATE: case SF_NODE_ROTATE: case SF_NODE_SCALE: case SF_NODE_SCALE_AXES:
+    case SF_NODE_MIRROR: case SF_NODE_BOX_FOLD: case SF_NODE_BOX_FOLD_AXES: case SF_NODE_SPHERE_INVERSION:
+    case SF_NODE_SPHERE_FOLD: case SF_NODE_ABS: case SF_NODE_MENGER_FOLD: case SF_NODE_KALEIDO:
+    case SF_NODE_POWER: case SF_NODE_ADD_ORIGIN: case SF_NODE_ADD_SEED: case SF_NODE_ADD_CONSTANT:
+    case SF_NODE_TWIST: case SF_NODE_BEND: case SF_NODE_TILE: case SF_NODE_REPEAT_FINITE:
+    case SF_NODE_ITERATE: case SF_NODE_TRAP:
+        return true;
+    default: return false;
+    }
+}
+bool is_fence_kind(uint32_t k) { return k >= SF_NODE_SPHERE && k <= SF_NODE_BULB_FENCE; }
+bool is_combine_kind(uint32_t k) { return k >= SF_NODE_UNION && k <= SF_NODE_SMOOTH_INTERSECTION; }
+// Port types (NodeKind::inputs/outputs, graph/mod.rs:366-396): 0 point, 1 distance.
+std::vector<int> in_ports(uint32_t k) {
+    if (k == SF_NODE_INPUT) return {};
+    if (k == SF_NODE_OUTPUT || k == SF_NODE_MATERIAL_TAG || k == SF_NODE_INSTANCES) return {1};
+    if (k == SF_NODE_BOUNDED) return {0, 1};
+    if (is_combine_kind(k)) return {1, 1};
+    return {0};
+}
+std::vector<int> out_ports(uint32_t k) {
+    if (k == SF_NODE_OUTPUT) return {};
+    if (k == SF_NODE_MATERIAL_TAG || k == SF_NODE_BOUNDED || k == SF_NODE_INSTANCES || is_fence_kind(k) ||
+        is_combine_kind(k))
+        return {1};
+    return {0};
+}
+
+std::vector<uint32_t> active_nodes(const HostGraph& g) {
+    const sf_node* out = nullptr;
+    for (auto& n : g.nodes)
+        if (n.kind == SF_NODE_OUTPUT) { out = &n; break; }
+    if (!out) return {};
+    std::set<uint32_t> seen;
+    std::vector<uint32_t> stack{out->id};
+    while (!stack.empty()) {
+        uint32_t id = stack.back();
+        stack.pop_back();
+        if (!seen.insert(id).second) continue;
+        for (auto& l : g.links)
+            if (l.to_node == id) stack.push_back(l.from_node);
+    }
+    return std::vector<uint32_t>(seen.begin(), seen.end());
+}
+
+// validate_structure (validate.rs:146-330) for the checks the device path relies on.
+std::string validate(const HostGraph& g) {
+    std::set<uint32_t> ids;
+    int inputs = 0, outputs = 0;
+    for (auto& n : g.nodes) {
+        if (n.kind >= SF_NODE_KIND_COUNT) return "unknown node kind on node " + std::to_string(n.id);
+        if (!ids.insert(n.id).second) return "duplicate node id " + std::to_string(n.id);
+        inputs += n.kind == SF_NODE_INPUT;
+        outputs += n.kind == SF_NODE_OUTPUT;
+        if (n.kind == SF_NODE_SCALE && std::fabs(n.f[0]) < 1e-3f) return "Scale factor cannot be zero";
+        if (n.kind == SF_NODE_ITERATE && size_t(n.body_offset) + n.body_len > g.body.size())
+            return "Iterate body out of range on node " + std::to_string(n.id);
+    }
+    if (inputs != 1) return "the graph must have exactly one Input";
+    if (outputs != 1) return "the graph must have exactly one Output";
+    std::map<uint32_t, uint32_t> member;
+    for (auto& n : g.nodes)
+        for (uint32_t b : g.body_of(n)) {
+            if (member.count(b)) return "node " + std::to_string(b) + " is in two Iterate bodies";
+            member[b] = n.id;
+            const sf_node* bn = g.node(b);
+            if (!bn) return "Iterate body cites unknown node " + std::to_string(b);
+            if (!is_point_kind(bn->kind)) return "Iterate body node " + std::to_string(b) + " is not Point -> Point";
+            for (auto& l : g.links)
+                if (l.from_node == b || l.to_node == b)
+                    return "Iterate body node " + std::to_string(b) + " cannot be wired";
+        }
+    std::set<std::pair<uint32_t, uint32_t>> wired;
+    for (auto& l : g.links) {
+        const sf_node* from = g.node(l.from_node);
+        const sf_node* to = g.node(l.to_node);
+        if (!from) return "link from unknown node " + std::to_string(l.from_node);
+        if (!to) return "link to unknown node " + std::to_string(l.to_node);
+        auto op = out_ports(from->kind);
+        auto ip = in_ports(to->kind);
+        if (l.from_port >= op.size()) return "missing output port on node " + std::to_string(from->id);
+        if (l.to_port >= ip.size()) return "missing input port on node " + std::to_string(to->id);
+        if (op[l.from_port] != ip[l.to_port]) return "port type mismatch into node " + std::to_string(to->id);
+        if (!wired.insert({l.to_node, l.to_port}).second)
+            return "two wires into one input of node " + std::to_string(to->id);
+    }
+    // iterate nesting depth (validate.rs:87-110)
+    std::function<uint32_t(uint32_t, std::vector<uint32_t>&)> depth = [&](uint32_t id, std::vector<uint32_t>& seen) -> uint32_t {
+        if (std::find(seen.begin(), seen.end(), id) != seen.end()) return 99;
+        seen.push_back(id);
+        const sf_node* n = g.node(id);
+        uint32_t d = 0;
+        if (n && n->kind == SF_NODE_ITERATE) {
+            uint32_t m = 0;
+            for (uint32_t b : g.body_of(*n)) m = std::max(m, depth(b, seen));
+            d = 1 + m;
+        }
+        seen.pop_back();
+        return d;
+    };
+    for (auto& n : g.nodes) {
+        std::vector<uint32_t> seen;
+        if (depth(n.id, seen) > MAX_DEPTH) return "Iterate nesting deeper than 3";
+    }
+    return "";
+}
+
+bool topo_order(const HostGraph& g, std::vector<uint32_t>& order) {
+    auto act = active_nodes(g);
+    std::set<uint32_t> active(act.begin(), act.end());
+    std::set<uint32_t> owned;
+    for (auto& n : g.nodes)
+        for (uint32_t b : g.body_of(n)) owned.insert(b);
+    std::map<uint32_t, size_t> indeg;
+    for (uint32_t id : active)
+        if (!owned.count(id)) indeg[id] = 0;
+    for (auto& l : g.links)
+        if (indeg.count(l.to_node) && active.count(l.from_node)) indeg[l.to_node] += 1;
+    std::vector<uint32_t> ready;
+    for (auto& kv : indeg)
+        if (kv.second == 0) ready.push_back(kv.first);
+    auto desc = [](uint32_t a, uint32_t b) { return a > b; };
+    std::sort(ready.begin(), ready.end(), desc);
+    order.clear();
+    while (!ready.empty()) {
+        uint32_t id = ready.back();
+        ready.pop_back();
+        order.push_back(id);
+        for (auto& l : g.links) {
+            if (l.from_node != id) continue;
+            auto it = indeg.find(l.to_node);
+            if (it != indeg.end() && --it->second == 0) ready.push_back(l.to_node);
+        }
+        std::sort(ready.begin(), ready.end(), desc);
+    }
+    return order.size() == indeg.size();
+}
+
+uint32_t iter_product(const HostGraph& g, uint32_t id, std::vector<uint32_t>& seen) {
+    if (std::find(seen.begin(), seen.end(), id) != seen.end()) return 0xffffffffu;
+    seen.push_back(id);
+    uint32_t p = 1;
+    const sf_node* n = g.node(id);
+    if (n && n->kind == SF_NODE_ITERATE) {
+        uint32_t m = 0;
+        bool any = false;
+        for (uint32_t b : g.body_of(*n)) { m = std::max(m, iter_product(g, b, seen)); any = true; }
+        uint64_t r = uint64_t(n->u[0]) * (any ? m : 1);
+        p = r > 0xffffffffull ? 0xffffffffu : uint32_t(r);
+    }
+    seen.pop_back();
+    return p;
+}
+
+void trap_walk(const HostGraph& g, uint32_t id, uint32_t depth, float* scales) {
+    if (depth > MAX_DEPTH + 1) return;
+    const sf_node* n = g.node(id);
+    if (!n || !n->enabled) return;
+    if (n->kind == SF_NODE_TRAP) scales[std::min<uint32_t>(n->u[0], 3)] = n->f[0];
+    else if (n->kind == SF_NODE_ITERATE)
+        for (uint32_t b : g.body_of(*n)) trap_walk(g, b, depth + 1, scales);
+}
+
+void lip_visit(const HostGraph& g, uint32_t id, float radius, uint32_t depth, float* l) {
+    if (depth > MAX_DEPTH + 1) return;
+    const sf_node* n = g.node(id);
+    if (!n || !n->enabled) return;
+    if (n->kind == SF_NODE_TWIST || n->kind == SF_NODE_BEND) {
+        float x = n->f[0] * radius;
+        *l *= sqrtf(1.0f + x * x);
+    }
+    for (uint32_t b : g.body_of(*n)) lip_visit(g, b, radius, depth + 1, l);
+}
+
+// ------------------------------------------------------------------ lowering
+struct Lowerer {
+    const HostGraph& g;
+    DeProgram& P;
+    std::string err;
+    int stack_depth = 0, max_stack = 0;
+
+    bool push(const DeOp& op) {
+        if (P.n_ops >= SF_MAX_OPS) { err = "graph too large for the device program"; return false; }
+        P.ops[P.n_ops++] = op;
+        return true;
+    }
+    static DeOp mk(uint32_t code) { DeOp o; std::memset(&o, 0, sizeof o); o.code = code; return o; }
+
+    bool point_op(uint32_t id) {
+        const sf_node* n = g.node(id);
+        if (!n || !n->enabled || !is_point_kind(n->kind)) return true;  // no-op (eval.rs:351-353, :555)
+        if (n->kind == SF_NODE_ITERATE) {
+            uint32_t begin = P.n_ops;
+            DeOp b = mk(SF_OP_ITER_BEGIN);
+            b.a = n->u[0];
+            b.f[0] = n->f[0];
+            if (!push(b)) return false;
+            for (uint32_t c : g.body_of(*n))
+                if (!point_op(c)) return false;
+            DeOp e = mk(SF_OP_ITER_END);
+            e.a = begin;
+            if (!push(e)) return false;
+            P.ops[begin].b = P.n_ops - 1;
+            return true;
+        }
+        DeOp o = mk(n->kind);
+        std::memcpy(o.f, n->f, sizeof o.f);
+        switch (n->kind) {
+        case SF_NODE_POWER: {
+            float pw = n->f[0];
+            o.a = (pw >= 1.f && pw <= 16.f && pw == std::floor(pw)) ? uint32_t(pw) : 0u;
+            break;
+        }
+        case SF_NODE_BOX_FOLD_AXES: case SF_NODE_ABS:
+            o.a = (n->u[0] ? 1u : 0u) | (n->u[1] ? 2u : 0u) | (n->u[2] ? 4u : 0u);
+            break;
+        case SF_NODE_KALEIDO: o.a = n->u[0]; break;
+        case SF_NODE_REPEAT_FINITE: o.a = n->u[0]; o.b = n->u[1]; o.c = n->u[2]; break;
+        case SF_NODE_TRAP: o.a = std::min<uint32_t>(n->u[0], 3); o.b = n->u[1]; o.c = n->u[2]; break;
+        default: break;
+        }
+        return push(o);
+    }
+    // The point state feeding a port: a chain of point ops from the Input.
+    bool chain(bool has_src, uint32_t src, int guard = 0) {
+        if (guard > 256) { err = "point chain too deep"; return false; }
+        if (!has_src) return push(mk(SF_OP_BEGIN));
+        const sf_node* n = g.node(src);
+        if (!n) return push(mk(SF_OP_BEGIN));
+        if (n->kind == SF_NODE_INPUT) return push(mk(SF_OP_BEGIN));
+        if (!is_point_kind(n->kind)) { err = "distance value wired into a point port"; return false; }
+        uint32_t up;
+        bool has = g.input_of(src, 0, &up);
+        if (!chain(has, up, guard + 1)) return false;
+        return point_op(src);
+    }
+    bool dist(bool has_src, uint32_t src, int guard = 0) {
+        if (guard > 256) { err = "distance tree too deep"; return false; }
+        if (!has_src || !g.node(src)) {
+            stack_depth++;
+            max_stack = std::max(max_stack, stack_depth);
+            return push(mk(SF_OP_EMPTY));
+        }
+        const sf_node& n = *g.node(src);
+        uint32_t a, b;
+        bool ha = g.input_of(src, 0, &a), hb = g.input_of(src, 1, &b);
+        if (is_fence_kind(n.kind)) {
+            if (!chain(ha, a)) return false;
+            DeOp o = mk(n.enabled ? n.kind : (uint32_t)SF_OP_FENCE_OFF);
+            std::memcpy(o.f, n.f, sizeof o.f);
+            if (n.kind == SF_NODE_ROCK) o.a = n.u[0];
+            stack_depth++;
+            max_stack = std::max(max_stack, stack_depth);
+            return push(o);
+        }
+        if (n.kind == SF_NODE_MATERIAL_TAG) {
+            if (!dist(ha, a, guard + 1)) return false;
+            if (!n.enabled) return true;
+            DeOp o = mk(SF_OP_TAG);
+            o.a = n.u[0];
+            return push(o);
+        }
+        if (n.kind == SF_NODE_BOUNDED) {
+            if (!dist(hb, b, guard + 1)) return false;
+            if (!n.enabled) return true;
+            if (!chain(ha, a)) return false;
+            DeOp o = mk(SF_OP_BOUND);
+            std::memcpy(o.f, n.f, sizeof o.f);
+            return push(o);
+        }
+        if (n.kind == SF_NODE_INSTANCES) { err = "Instances nodes are not supported on the device"; return false; }
+        if (is_combine_kind(n.kind)) {
+            if (!dist(ha, a, guard + 1)) return false;
+            if (!n.enabled) return true;  // disabled: port 0 passes through (eval.rs:822)
+            if (!dist(hb, b, guard + 1)) return false;
+            DeOp o = mk(SF_OP_COMBINE);
+            o.a = n.kind;
+            o.f[0] = n.f[0];
+            stack_depth--;
+            return push(o);
+        }
+        err = "point value wired into a distance port";
+        return false;
+    }
+};
+
+// Recognises the iterated forms of graphs/{mandelbulb,mandelbox,menger}.ron.
+void detect_form(const HostGraph& g, DeProgram& P) {
+    P.form = SF_FORM_GENERIC;
+    const sf_node* out = nullptr;
+    for (auto& n : g.nodes)
+        if (n.kind == SF_NODE_OUTPUT) out = &n;
+    uint32_t fid;
+    if (!out || !g.input_of(out->id, 0, &fid)) return;
+    const sf_node* fence = g.node(fid);
+    uint32_t material = 0;
+    if (fence && fence->kind == SF_NODE_MATERIAL_TAG) {
+        if (!fence->enabled) return;
+        material = fence->u[0];
+        if (!g.input_of(fence->id, 0, &fid)) return;
+        fence = g.node(fid);
+    }
+    if (!fence || !fence->enabled || !is_fence_kind(fence->kind)) return;
+    uint32_t iid;
+    if (!g.input_of(fence->id, 0, &iid)) return;
+    const sf_node* it = g.node(iid);
+    if (!it || !it->enabled || it->kind != SF_NODE_ITERATE) return;
+    uint32_t src;
+    if (!g.input_of(it->id, 0, &src)) return;
+    const sf_node* in = g.node(src);
+    if (!in || in->kind != SF_NODE_INPUT) return;
+    std::vector<const sf_node*> body;
+    for (uint32_t b : g.body_of(*it)) {
+        const sf_node* bn = g.node(b);
+        if (!bn || !bn->enabled) return;
+        body.push_back(bn);
+    }
+    auto kinds = [&](std::initializer_list<uint32_t> want) {
+        if (body.size() != want.size()) return false;
+        size_t i = 0;
+        for (uint32_t k : want)
+            if (body[i++]->kind != k) return false;
+        return true;
+    };
+    FormParams& f = P.fp;
+    std::memset(&f, 0, sizeof f);
+    f.iterations = it->u[0];
+    f.bailout = it->f[0];
+    f.material = material;
+    auto set_trap = [&](const sf_node* t) {
+        f.trap_slot = std::min<uint32_t>(t->u[0], 3);
+        f.trap_measure = t->u[1];
+        f.trap_mode = t->u[2];
+    };
+    if (fence->kind == SF_NODE_BULB_FENCE && kinds({SF_NODE_TRAP, SF_NODE_POWER, SF_NODE_ADD_ORIGIN})) {
+        set_trap(body[0]);
+        f.power = body[1]->f[0];
+        float pw = f.power;
+        f.power_int = (pw >= 1.f && pw <= 16.f && pw == std::floor(pw)) ? uint32_t(pw) : 0u;
+        P.form = SF_FORM_BULB;
+    } else if (fence->kind == SF_NODE_NORM_FENCE &&
+               kinds({SF_NODE_BOX_FOLD, SF_NODE_TRAP, SF_NODE_SPHERE_FOLD, SF_NODE_SCALE, SF_NODE_ADD_ORIGIN})) {
+        f.limit = body[0]->f[0];
+        set_trap(body[1]);
+        float mr = body[2]->f[0], fr = body[2]->f[1];
+        f.min_radius2 = mr * mr;
+        f.fixed_radius2 = fr * fr;
+        f.fold_k_min = f.fixed_radius2 / f.min_radius2;
+        f.scale = body[3]->f[0];
+        f.abs_scale = std::fabs(f.scale);
+        f.fence[0] = fence->f[0];
+        P.form = SF_FORM_BOX;
+    } else if (fence->kind == SF_NODE_BOX && kinds({SF_NODE_MENGER_FOLD, SF_NODE_TRAP})) {
+        f.scale = body[0]->f[0];
+        f.offset[0] = body[0]->f[1];
+        f.offset[1] = body[0]->f[2];
+        f.offset[2] = body[0]->f[3];
+        set_trap(body[1]);
+        f.fence[0] = fence->f[0];
+        f.fence[1] = fence->f[1];
+        f.fence[2] = fence->f[2];
+        P.form = SF_FORM_MENGER;
+    }
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ context
+struct sf_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0, used = 0;
+    std::string device_name;
+    int cc_major = 0, cc_minor = 0, sm_count = 0;
+    bool profiling = false;
+    struct Timed { cudaEvent_t a, b; bool trace; };
+    std::vector<Timed> timed;
+    std::vector<cudaEvent_t> spare;
+    double kernel_ms = 0, trace_ms = 0;
+    uint64_t launches = 0, trace_launches = 0;
+    unsigned long long* d_stats = nullptr;  // SF_STAT_COUNT counters
+    uint32_t* d_work = nullptr;             // scratch work counters
+    std::mutex mu;
+};
+
+struct sf_graph {
+    sf_context* ctx = nullptr;
+    HostGraph host;
+    DeProgram prog;
+    DeProgram* d_prog = nullptr;
+    sf_graph_info info;
+    std::string topology;
+};
+
+namespace {
+
+sf_status ctx_alloc(sf_context* c, size_t bytes, void** p) {
+    *p = nullptr;
+    if (bytes == 0) return SF_OK;
+    if (c->used + bytes > c->budget)
+        return fail(SF_ERR_BUDGET, "HBM admission budget exceeded: " + std::to_string(c->used + bytes) + " > " +
+                                       std::to_string(c->budget) + " bytes");
+    cudaError_t e = cudaMalloc(p, bytes);
+    if (e != cudaSuccess) {
+        *p = nullptr;
+        return cuda_fail(e, "cudaMalloc");
+    }
+    c->used += bytes;
+    return SF_OK;
+}
+void ctx_free(sf_context* c, void* p, size_t bytes) {
+    if (!p) return;
+    cudaFree(p);
+    c->used -= std::min<uint64_t>(c->used, bytes);
+}
+
+cudaEvent_t get_event(sf_context* c) {
+    if (!c->spare.empty()) {
+        cudaEvent_t e = c->spare.back();
+        c->spare.pop_back();
+        return e;
+    }
+    cudaEvent_t e;
+    cudaEventCreate(&e);
+    return e;
+}
+// Scoped CUDA-event timing of one launch on the context stream.
+struct LaunchTimer {
+    sf_context* c;
+    cudaEvent_t a = nullptr;
+    bool trace;
+    LaunchTimer(sf_context* ctx, bool is_trace) : c(ctx), trace(is_trace) {
+        c->launches++;
+        if (is_trace) c->trace_launches++;
+        if (c->profiling) {
+            a = get_event(c);
+            cudaEventRecord(a, c->stream);
+        }
+    }
+    ~LaunchTimer() {
+        if (a) {
+            cudaEvent_t b = get_event(c);
+            cudaEventRecord(b, c->stream);
+            c->timed.push_back({a, b, trace});
+        }
+    }
+};
+void collect_timing(sf_context* c) {
+    if (c->timed.empty()) return;
+    cudaStreamSynchronize(c->stream);
+    for (auto& t : c->timed) {
+        float ms = 0;
+        if (cudaEventElapsedTime(&ms, t.a, t.b) == cudaSuccess) {
+            c->kernel_ms += ms;
+            if (t.trace) c->trace_ms += ms;
+        }
+        c->spare.push_back(t.a);
+        c->spare.push_back(t.b);
+    }
+    c->timed.clear();
+}
+
+sf_status wait_stream(cudaStream_t st, uint32_t timeout_ms) {
+    auto t0 = std::chrono::steady_clock::now();
+    for (;;) {
+        cudaError_t e = cudaStreamQuery(st);
+        if (e == cudaSuccess) return SF_OK;
+        if (e != cudaErrorNotReady) return cuda_fail(e, "stream");
+        double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (timeout_ms && el > timeout_ms) return fail(SF_ERR_TIMEOUT, "dispatch exceeded its time limit");
+        std::this_thread::sleep_for(std::chrono::microseconds(200));
+    }
+}
+
+std::string topology_of(const HostGraph& g) {
+    // Everything but the float parameters (topology_key, graph/mod.rs:397-425).
+    std::string s;
+    char buf[96];
+    for (auto& n : g.nodes) {
+        float pw = n.kind == SF_NODE_POWER ? n.f[0] : 0.f;
+        bool even68 = pw == 6.f || pw == 8.f;
+        std::snprintf(buf, sizeof buf, "%u:%u:%u:%u:%u:%u:%u:%u;", n.id, n.kind, n.enabled, n.body_offset, n.body_len,
+                      n.u[0], n.u[1], n.u[2]);
+        s += buf;
+        if (n.kind == SF_NODE_POWER && !even68) { std::snprintf(buf, sizeof buf, "p%g;", pw); s += buf; }
+    }
+    for (auto& l : g.links) {
+        std::snprintf(buf, sizeof buf, "%u.%u>%u.%u;", l.from_node, l.from_port, l.to_node, l.to_port);
+        s += buf;
+    }
+    for (uint32_t b : g.body) s += std::to_string(b) + ",";
+    return s;
+}
+
+sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_graph_info& info) {
+    if (!d || (!d->nodes && d->node_count)) return fail(SF_ERR_INVALID, "null graph descriptor");
+    g.nodes.assign(d->nodes, d->nodes + d->node_count);
+    g.links.assign(d->links ? d->links : nullptr, d->links ? d->links + d->link_count : nullptr);
+    g.body.assign(d->body_ids ? d->body_ids : nullptr, d->body_ids ? d->body_ids + d->body_id_count : nullptr);
+    g.safety = d->safety;
+    g.hint = d->bounding_radius_hint;
+    std::string e = validate(g);
+    if (!e.empty()) return fail(SF_ERR_GRAPH, e);
+    std::vector<uint32_t> order;
+    if (!topo_order(g, order)) return fail(SF_ERR_GRAPH, "cycle in the graph");
+    std::memset(&P, 0, sizeof P);
+    for (int i = 0; i < 4; ++i) P.trap_scales[i] = 1.f;
+    for (uint32_t id : order) trap_walk(g, id, 0, P.trap_scales);
+    std::set<uint32_t> owned;
+    for (auto& n : g.nodes)
+        for (uint32_t b : g.body_of(n)) owned.insert(b);
+    uint32_t best = 0;
+    bool any = false;
+    for (uint32_t id : active_nodes(g)) {
+        if (owned.count(id)) continue;
+        std::vector<uint32_t> seen;
+        best = std::max(best, iter_product(g, id, seen));
+        any = true;
+    }
+    P.iteration_product = any ? best : 1;
+    float lip = 1.f;
+    for (uint32_t id : active_nodes(g)) lip_visit(g, id, g.hint, 0, &lip);
+    Lowerer L{g, P};
+    const sf_node* out = nullptr;
+    for (auto& n : g.nodes)
+        if (n.kind == SF_NODE_OUTPUT) out = &n;
+    uint32_t src;
+    bool has = g.input_of(out->id, 0, &src);
+    if (!L.dist(has, src)) return fail(L.err.find("not supported") != std::string::npos ? SF_ERR_UNSUPPORTED : SF_ERR_GRAPH, L.err);
+    if (L.max_stack > SF_MAX_DIST_STACK) return fail(SF_ERR_UNSUPPORTED, "distance tree wider than the device stack");
+    P.max_stack = L.max_stack;
+    detect_form(g, P);
+    std::memset(&info, 0, sizeof info);
+    info.step_scale = g.safety / lip;
+    info.lipschitz = lip;
+    for (int i = 0; i < 4; ++i) info.trap_scales[i] = P.trap_scales[i];
+    info.iteration_product = P.iteration_product;
+    info.form = P.form;
+    info.op_count = P.n_ops;
+    info.bounding_radius_hint = g.hint;
+    return SF_OK;
+}
+
+void light_dev(const sf_area_light& l, DevLight& o) {
+    std::memcpy(o.a, l.center, 12);
+    std::memcpy(o.b, l.edge_u, 12);
+    std::memcpy(o.c, l.edge_v, 12);
+    std::memcpy(o.color, l.radiance, 12);
+    float cx = l.edge_u[1] * l.edge_v[2] - l.edge_u[2] * l.edge_v[1];
+    float cy = l.edge_u[2] * l.edge_v[0] - l.edge_u[0] * l.edge_v[2];
+    float cz = l.edge_u[0] * l.edge_v[1] - l.edge_u[1] * l.edge_v[0];
+    float len = sqrtf(cx * cx + cy * cy + cz * cz);
+    float rcp = 1.0f / len;
+    if (!(len > 0.f) || !(rcp > 0.f) || !(rcp <= 3.4028235e38f)) { o.n[0] = 0; o.n[1] = 1; o.n[2] = 0; }
+    else { o.n[0] = cx * rcp; o.n[1] = cy * rcp; o.n[2] = cz * rcp; }
+    o.area = len;
+    float bb = l.edge_u[0] * l.edge_u[0] + l.edge_u[1] * l.edge_u[1] + l.edge_u[2] * l.edge_u[2];
+    float cc = l.edge_v[0] * l.edge_v[0] + l.edge_v[1] * l.edge_v[1] + l.edge_v[2] * l.edge_v[2];
+    o.inv_bb = 1.0f / bb;
+    o.inv_cc = 1.0f / cc;
+    o.lum = l.radiance[0] * 0.2126f + l.radiance[1] * 0.7152f + l.radiance[2] * 0.0722f;
+}
+void material_dev(const sf_material& m, DevMaterial& o) {
+    std::memcpy(o.albedo, m.albedo, 12);
+    o.roughness = m.roughness;
+    o.metallic = m.metallic;
+    o.specular = m.specular;
+    std::memcpy(o.emission, m.emission, 12);
+}
+// Uniforms::from_scene (uniforms.rs:748-830) for the DE path.
+void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph_info& gi, DevScene& S) {
+    std::memset(&S, 0, sizeof S);
+    std::memcpy(S.origin, d.camera.origin, 12);
+    std::memcpy(S.forward, d.camera.forward, 12);
+    std::memcpy(S.right, d.camera.right, 12);
+    std::memcpy(S.up, d.camera.up, 12);
+    S.tan_half = d.camera.tan_half_fov;
+    S.aspect = d.camera.aspect;
+    S.lens_radius = d.camera.lens_radius;
+    S.focus_distance = d.camera.focus_distance;
+    S.width = c.width;
+    S.height = c.height;
+    S.max_bounces = c.max_bounces;
+    S.max_steps = c.max_steps;
+    S.seed = uint32_t(d.seed) ^ uint32_t(d.seed >> 32);
+    S.light_count = std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
+    S.finish_count = std::min<uint32_t>(d.finish_count, SF_MAX_FINISHES);
+    S.variation_slot = d.variation_slot;
+    S.variation_enabled = d.variation_enabled;
+    S.var_rough[0] = d.variation_roughness[0];
+    S.var_rough[1] = d.variation_roughness[1];
+    S.var_metal[0] = d.variation_metallic[0];
+    S.var_metal[1] = d.variation_metallic[1];
+    S.cavity = d.cavity_darkness;
+    S.pixel_tolerance = c.pixel_tolerance;
+    S.step_scale = gi.step_scale;
+    float ol = sqrtf(d.camera.origin[0] * d.camera.origin[0] + d.camera.origin[1] * d.camera.origin[1] +
+                     d.camera.origin[2] * d.camera.origin[2]);
+    float far = std::max(2.0f * gi.bounding_radius_hint + ol, 200.0f);  // uniforms.rs:781-782
+    S.extent = std::max(200.0f, far);                                   // ray_extent, common.wgsl:206-208
+    S.pixel_cone = d.camera.tan_half_fov * 2.0f / float(c.width);
+    S.iteration_product = gi.iteration_product;
+    material_dev(d.material, S.material);
+    for (uint32_t i = 0; i < S.finish_count; ++i) material_dev(d.finishes[i], S.finishes[i]);
+    for (uint32_t i = 0; i < S.light_count; ++i) light_dev(d.lights[i], S.lights[i]);
+}
+
+}  // namespace
+
+// ------------------------------------------------------------------ ABI: basics
+extern "C" const char* sf_status_string(sf_status s) {
+    static const char* names[] = {"SF_OK", "SF_ERR_INVALID", "SF_ERR_GRAPH", "SF_ERR_UNSUPPORTED", "SF_ERR_CUDA",
+                                  "SF_ERR_OOM", "SF_ERR_TIMEOUT", "SF_ERR_BUDGET", "SF_ERR_IO", "SF_ERR_CHECKPOINT",
+                                  "SF_ERR_WAVEFRONT", "SF_ERR_NO_DEVICE"};
+    if (s < 0 || s > 11) return "SF_ERR_UNKNOWN";
+    return names[s];
+}
+extern "C" const char* sf_last_error(void) { return g_error.c_str(); }
+extern "C" uint32_t sf_abi_version(void) { return ABI_VERSION; }
+
+extern "C" sf_status sf_context_create(int device, uint64_t budget, sf_context** out) {
+    if (!out) return fail(SF_ERR_INVALID, "null output");
+    *out = nullptr;
+    int count = 0;
+    cudaError_t e = cudaGetDeviceCount(&count);
+    if (e != cudaSuccess || count == 0) return fail(SF_ERR_NO_DEVICE, "no CUDA device available");
+    if (device < 0 || device >= count) return fail(SF_ERR_INVALID, "device index out of range");
+    CU(cudaSetDevice(device));
+    cudaDeviceProp prop;
+    CU(cudaGetDeviceProperties(&prop, device));
+    auto* c = new sf_context();
+    c->device = device;
+    c->device_name = prop.name;
+    c->cc_major = prop.major;
+    c->cc_minor = prop.minor;
+    c->sm_count = prop.multiProcessorCount;
+    size_t free_b = 0, total_b = 0;
+    cudaMemGetInfo(&free_b, &total_b);
+    c->budget = budget ? budget : uint64_t(double(free_b) * 0.9);
+    e = cudaStreamCreateWithFlags(&c->stream, cudaStreamNonBlocking);
+    if (e != cudaSuccess) { delete c; return cuda_fail(e, "cudaStreamCreate"); }
+    void* p = nullptr;
+    sf_status s = ctx_alloc(c, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t), &p);
+    if (s != SF_OK) { cudaStreamDestroy(c->stream); delete c; return s; }
+    c->d_stats = static_cast<unsigned long long*>(p);
+    c->d_work = reinterpret_cast<uint32_t*>(c->d_stats + SF_STAT_COUNT);
+    cudaMemsetAsync(p, 0, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t), c->stream);
+    *out = c;
+    return SF_OK;
+}
+extern "C" sf_status sf_context_destroy(sf_context* c) {
+    if (!c) return SF_OK;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    collect_timing(c);
+    for (auto e : c->spare) cudaEventDestroy(e);
+    ctx_free(c, c->d_stats, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t));
+    cudaStreamDestroy(c->stream);
+    delete c;
+    return SF_OK;
+}
+extern "C" sf_status sf_context_stream(sf_context* c, void** s) {
+    if (!c || !s) return fail(SF_ERR_INVALID, "null argument");
+    *s = c->stream;
+    return SF_OK;
+}
+extern "C" sf_status sf_context_memory(sf_context* c, uint64_t* used, uint64_t* budget) {
+    if (!c) return fail(SF_ERR_INVALID, "null context");
+    if (used) *used = c->used;
+    if (budget) *budget = c->budget;
+    return SF_OK;
+}
+extern "C" sf_status sf_context_set_profiling(sf_context* c, int enable) {
+    if (!c) return fail(SF_ERR_INVALID, "null context");
+    collect_timing(c);
+    c->profiling = enable != 0;
+    return SF_OK;
+}
+extern "C" sf_status sf_context_reset_stats(sf_context* c) {
+    if (!c) return fail(SF_ERR_INVALID, "null context");
+    cudaSetDevice(c->device);
+    collect_timing(c);
+    c->kernel_ms = c->trace_ms = 0;
+    c->launches = c->trace_launches = 0;
+    CU(cudaMemsetAsync(c->d_stats, 0, SF_STAT_COUNT * sizeof(unsigned long long), c->stream));
+    return SF_OK;
+}
+extern "C" sf_status sf_context_stats(sf_context* c, sf_stats* out) {
+    if (!c || !out) return fail(SF_ERR_INVALID, "null argument");
+    cudaSetDevice(c->device);
+    collect_timing(c);
+    unsigned long long h[SF_STAT_COUNT];
+    CU(cudaMemcpyAsync(h, c->d_stats, sizeof h, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    std::memset(out, 0, sizeof *out);
+    out->de_evals = h[SF_STAT_DE_EVALS];
+    out->de_iterations = h[SF_STAT_DE_ITERS];
+    out->segments = h[SF_STAT_SEGMENTS];
+    out->shadow_segments = h[SF_STAT_SHADOW_SEGMENTS];
+    out->steps = h[SF_STAT_STEPS];
+    out->launches = c->launches;
+    out->kernel_ms = c->kernel_ms;
+    out->trace_ms = c->trace_ms;
+    out->trace_launches = c->trace_launches;
+    return SF_OK;
+}
+extern "C" sf_status sf_context_sync(sf_context* c, uint32_t timeout_ms) {
+    if (!c) return fail(SF_ERR_INVALID, "null context");
+    cudaSetDevice(c->device);
+    return wait_stream(c->stream, timeout_ms);
+}
+
+// ------------------------------------------------------------------ ABI: graph
+extern "C" sf_status sf_graph_compile(sf_context* c, const sf_graph_desc* d, sf_graph** out) {
+    if (!c || !out) return fail(SF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    auto* g = new sf_graph();
+    g->ctx = c;
+    sf_status s = build_graph(d, g->host, g->prog, g->info);
+    if (s != SF_OK) { delete g; return s; }
+    g->topology = topology_of(g->host);
+    cudaSetDevice(c->device);
+    void* p = nullptr;
+    s = ctx_alloc(c, sizeof(DeProgram), &p);
+    if (s != SF_OK) { delete g; return s; }
+    g->d_prog = static_cast<DeProgram*>(p);
+    cudaError_t e = cudaMemcpyAsync(g->d_prog, &g->prog, sizeof(DeProgram), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess) {
+        ctx_free(c, g->d_prog, sizeof(DeProgram));
+        delete g;
+        return cuda_fail(e, "graph upload");
+    }
+    *out = g;
+    return SF_OK;
+}
+extern "C" sf_status sf_graph_info_get(const sf_graph* g, sf_graph_info* out) {
+    if (!g || !out) return fail(SF_ERR_INVALID, "null argument");
+    *out = g->info;
+    return SF_OK;
+}
+extern "C" sf_status sf_graph_update(sf_graph* g, const sf_graph_desc* d) {
+    if (!g) return fail(SF_ERR_INVALID, "null graph");
+    HostGraph h;
+    DeProgram P;
+    sf_graph_info info;
+    sf_status s = build_graph(d, h, P, info);
+    if (s != SF_OK) return s;
+    if (topology_of(h) != g->topology) return fail(SF_ERR_GRAPH, "topology changed: compile a new graph");
+    cudaSetDevice(g->ctx->device);
+    CU(cudaMemcpyAsync(g->d_prog, &P, sizeof P, cudaMemcpyHostToDevice, g->ctx->stream));
+    CU(cudaStreamSynchronize(g->ctx->stream));
+    g->host = h;
+    g->prog = P;
+    g->info = info;
+    return SF_OK;
+}
+extern "C" sf_status sf_graph_destroy(sf_graph* g) {
+    if (!g) return SF_OK;
+    cudaSetDevice(g->ctx->device);
+    cudaStreamSynchronize(g->ctx->stream);
+    ctx_free(g->ctx, g->d_prog, sizeof(DeProgram));
+    delete g;
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ ABI: DE probe
+extern "C" sf_status sf_de_probe_device(sf_graph* g, const float* x, const float* y, const float* z, size_t n,
+                                        float* dist, float* traps, uint32_t* iters, uint32_t* mats) {
+    if (!g) return fail(SF_ERR_INVALID, "null graph");
+    if (n && (!x || !y || !z || !dist || !traps || !iters || !mats)) return fail(SF_ERR_INVALID, "null buffer");
+    sf_context* c = g->ctx;
+    cudaSetDevice(c->device);
+    LaunchTimer t(c, true);
+    CU(sf_launch_de_probe(g->d_prog, x, y, z, n, dist, traps, iters, mats, c->stream));
+    return SF_OK;
+}
+
+extern "C" sf_status sf_de_probe(sf_graph* g, const float* xyz, size_t n, sf_de_sample* out) {
+    if (!g) return fail(SF_ERR_INVALID, "null graph");
+    if (n == 0) return SF_OK;
+    if (!xyz || !out) return fail(SF_ERR_INVALID, "null buffer");
+    sf_context* c = g->ctx;
+    cudaSetDevice(c->device);
+    std::vector<float> soa(3 * n);
+    for (size_t i = 0; i < n; ++i) {
+        soa[i] = xyz[3 * i];
+        soa[n + i] = xyz[3 * i + 1];
+        soa[2 * n + i] = xyz[3 * i + 2];
+    }
+    size_t bytes = n * (3 + 1 + 4) * sizeof(float) + 2 * n * sizeof(uint32_t);
+    void* buf = nullptr;
+    sf_status s = ctx_alloc(c, bytes, &buf);
+    if (s != SF_OK) return s;
+    float* d_in = static_cast<float*>(buf);
+    float* d_dist = d_in + 3 * n;
+    float* d_traps = d_dist + n;
+    uint32_t* d_iter = reinterpret_cast<uint32_t*>(d_traps + 4 * n);
+    uint32_t* d_mat = d_iter + n;
+    std::vector<float> h_dist(n), h_traps(4 * n);
+    std::vector<uint32_t> h_iter(n), h_mat(n);
+    cudaError_t e = cudaMemcpyAsync(d_in, soa.data(), 3 * n * sizeof(float), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        LaunchTimer t(c, true);
+        e = sf_launch_de_probe(g->d_prog, d_in, d_in + n, d_in + 2 * n, n, d_dist, d_traps, d_iter, d_mat, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_dist.data(), d_dist, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_traps.data(), d_traps, 4 * n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_iter.data(), d_iter, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(h_mat.data(), d_mat, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    ctx_free(c, buf, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "sf_de_probe");
+    for (size_t i = 0; i < n; ++i) {
+        out[i].distance = h_dist[i];
+        for (int k = 0; k < 4; ++k) out[i].traps[k] = h_traps[k * n + i];
+        out[i].iterations = h_iter[i];
+        out[i].material = h_mat[i];
+    }
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ ABI: primary rays
+extern "C" sf_status sf_primary_trace(sf_graph* g, const sf_primary_desc* d, float* t_out, uint32_t* steps_out,
+                                      float* normal_out) {
+    if (!g || !d) return fail(SF_ERR_INVALID, "null argument");
+    if (!d->width || !d->height) return fail(SF_ERR_INVALID, "empty image");
+    if (!t_out || !steps_out || !normal_out) return fail(SF_ERR_INVALID, "null output");
+    sf_context* c = g->ctx;
+    cudaSetDevice(c->device);
+    size_t n = size_t(d->width) * d->height;
+    sf_scene_desc sd;
+    std::memset(&sd, 0, sizeof sd);
+    sd.camera = d->camera;
+    sf_render_config rc;
+    std::memset(&rc, 0, sizeof rc);
+    rc.width = d->width;
+    rc.height = d->height;
+    rc.max_steps = d->max_steps;
+    rc.pixel_tolerance = d->pixel_tolerance > 0 ? d->pixel_tolerance : 1.0f;
+    DevScene S;
+    scene_dev(sd, rc, g->info, S);
+    size_t bytes = sizeof(DevScene) + n * (1 + 1 + 3) * 4;
+    void* buf = nullptr;
+    sf_status s = ctx_alloc(c, bytes, &buf);
+    if (s != SF_OK) return s;
+    DevScene* dS = static_cast<DevScene*>(buf);
+    float* dt = reinterpret_cast<float*>(reinterpret_cast<char*>(buf) + sizeof(DevScene));
+    uint32_t* ds = reinterpret_cast<uint32_t*>(dt + n);
+    float* dn = reinterpret_cast<float*>(ds + n);
+    cudaError_t e = cudaMemcpyAsync(dS, &S, sizeof S, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(c->d_work, 0, 4, c->stream);
+    if (e == cudaSuccess) {
+        LaunchTimer t(c, true);
+        e = sf_launch_primary(g->d_prog, dS, d->width, d->height, d->max_steps, d->rule, d->eps, d->t_far,
+                              d->normal_mode, dt, ds, dn, c->d_work, c->d_stats, 1, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, dt, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(steps_out, ds, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(normal_out, dn, 3 * n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    ctx_free(c, buf, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "sf_primary_trace");
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ sessions
+struct sf_session {
+    sf_context* ctx = nullptr;
+    sf_graph* graph = nullptr;
+    sf_scene_desc scene;
+    sf_render_config cfg;
+    DevScene* d_scene = nullptr;
+    FilmPlanes film{};
+    PathSoA soa{};
+    uint32_t capacity = 0;
+    uint32_t* lists = nullptr;     // 2 x {active, cont, shadow} x capacity
+    uint32_t* counts = nullptr;    // per round: {active, cont, shadow, work}
+    uint32_t* status = nullptr;
+    void* mem = nullptr;
+    size_t mem_bytes = 0;
+    std::vector<sf_tile> tiles;
+    uint32_t tile_size = 0, dispatches = 0;
+    uint32_t blocks_per_sm = 8, threads = 256;
+    uint32_t status_host = 0;
+};
+
+namespace {
+
+uint32_t rounds_of(const sf_render_config& c) { return c.max_bounces + 2; }
+
+void tile_grid(sf_session* s) {
+    s->tiles.clear();
+    uint32_t ts = std::max<uint32_t>(s->tile_size, 8);  // MIN_TILE_SIZE, tiles.rs:1
+    for (uint32_t y = 0; y < s->cfg.height; y += std::min(ts, s->cfg.height - y)) {
+        uint32_t h = std::min(ts, s->cfg.height - y);
+        for (uint32_t x = 0; x < s->cfg.width; x += std::min(ts, s->cfg.width - x)) {
+            uint32_t w = std::min(ts, s->cfg.width - x);
+            s->tiles.push_back({x, y, w, h, 0});
+        }
+    }
+}
+
+sf_status validate_config(const sf_render_config& c) {
+    // RenderConfig::validate (renderer.rs:81-138)
+    if (c.width < 1 || c.height < 1) return fail(SF_ERR_INVALID, "width and height must be at least 1");
+    if (c.samples_per_pixel < 1) return fail(SF_ERR_INVALID, "samples_per_pixel must be at least 1");
+    if (c.max_bounces > 32) return fail(SF_ERR_INVALID, "max_bounces must be at most 32");
+    if (c.max_steps < 1) return fail(SF_ERR_INVALID, "max_steps must be at least 1");
+    if (!(c.pixel_tolerance >= 0.125f && c.pixel_tolerance <= 1.0f))
+        return fail(SF_ERR_INVALID, "pixel_tolerance must be between 0.125 and 1.0");
+    if (c.integrator > SF_INTEGRATOR_WAVEFRONT) return fail(SF_ERR_INVALID, "unknown integrator");
+    return SF_OK;
+}
+
+sf_status session_alloc(sf_session* s) {
+    sf_context* c = s->ctx;
+    const sf_render_config& cfg = s->cfg;
+    uint32_t ts = std::max<uint32_t>(cfg.tile_size ? cfg.tile_size : 256, 8);
+    s->tile_size = ts;
+    uint32_t tw = std::min(ts, cfg.width), th = std::min(ts, cfg.height);
+    uint32_t spd = std::max<uint32_t>(std::min(cfg.samples_per_dispatch ? cfg.samples_per_dispatch : 1,
+                                               cfg.samples_per_pixel), 1);
+    s->cfg.samples_per_dispatch = spd;
+    uint64_t cap64 = uint64_t(tw) * th * spd;
+    if (cap64 > 0x7fffffffull) return fail(SF_ERR_INVALID, "tile_size^2 * samples_per_dispatch too large");
+    s->capacity = uint32_t(cap64);
+    const size_t N = s->capacity;
+    const size_t px = size_t(cfg.width) * cfg.height;
+    const bool wf = cfg.integrator == SF_INTEGRATOR_WAVEFRONT;
+    const uint32_t R = rounds_of(cfg);
+    // layout
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+    size_t o_scene = take(sizeof(DevScene));
+    size_t o_acc = take(px * 16), o_depth = take(px * 4), o_aux = take(px * 16);
+    size_t o_Ls = take(N * 16);
+    size_t o_soa = 0, o_lists = 0;
+    if (wf) {
+        o_soa = take(N * 16 * 11 + N * 16);  // 11 float4/uint4 planes + vis (padded)
+        o_lists = take(N * 4 * 6);
+    }
+    size_t o_counts = take(size_t(R + 1) * 4 * 4);
+    size_t o_status = take(16);
+    s->mem_bytes = off;
+    sf_status st = ctx_alloc(c, off, &s->mem);
+    if (st != SF_OK) return st;
+    char* base = static_cast<char*>(s->mem);
+    s->d_scene = reinterpret_cast<DevScene*>(base + o_scene);
+    s->film.accum = reinterpret_cast<float4*>(base + o_acc);
+    s->film.depth = reinterpret_cast<float*>(base + o_depth);
+    s->film.aux = reinterpret_cast<float4*>(base + o_aux);
+    s->film.width = cfg.width;
+    s->film.height = cfg.height;
+    std::memset(&s->soa, 0, sizeof s->soa);
+    s->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
+    s->soa.capacity = s->capacity;
+    if (wf) {
+        float4* p = reinterpret_cast<float4*>(base + o_soa);
+        s->soa.o = p; p += N;
+        s->soa.d = p; p += N;
+        s->soa.tp = p; p += N;
+        s->soa.L = p; p += N;
+        s->soa.pn = p; p += N;
+        s->soa.sh_o = p; p += N;
+        s->soa.sh_d = p; p += N;
+        s->soa.sh_c = p; p += N;
+        s->soa.hit = reinterpret_cast<uint4*>(p); p += N;
+        s->soa.hit_tr = p; p += N;
+        s->soa.hit_n = p; p += N;
+        s->soa.vis = reinterpret_cast<uint32_t*>(p);
+        s->lists = reinterpret_cast<uint32_t*>(base + o_lists);
+    }
+    s->counts = reinterpret_cast<uint32_t*>(base + o_counts);
+    s->status = reinterpret_cast<uint32_t*>(base + o_status);
+    DevScene S;
+    scene_dev(s->scene, cfg, s->graph->info, S);
+    CU(cudaMemcpyAsync(s->d_scene, &S, sizeof S, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemsetAsync(s->film.accum, 0, px * 16, c->stream));
+    // depth = -1 and aux = (0,0,0,-1) until sample 0 lands (RenderOutput conventions)
+    std::vector<float> init(px * 4);
+    for (size_t i = 0; i < px; ++i) { init[4 * i] = 0; init[4 * i + 1] = 0; init[4 * i + 2] = 0; init[4 * i + 3] = -1; }
+    CU(cudaMemcpyAsync(s->film.aux, init.data(), px * 16, cudaMemcpyHostToDevice, c->stream));
+    std::vector<float> dinit(px, -1.0f);
+    CU(cudaMemcpyAsync(s->film.depth, dinit.data(), px * 4, cudaMemcpyHostToDevice, c->stream));
+    CU(cudaMemsetAsync(s->status, 0, 16, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    tile_grid(s);
+    return SF_OK;
+}
+
+}  // namespace
+
+extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scene_desc* scene,
+                                       const sf_render_config* cfg, sf_session** out) {
+    if (!c || !g || !scene || !cfg || !out) return fail(SF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    sf_status st = validate_config(*cfg);
+    if (st != SF_OK) return st;
+    if (scene->light_count > SF_MAX_LIGHTS || scene->finish_count > SF_MAX_FINISHES)
+        return fail(SF_ERR_INVALID, "too many lights or finishes");
+    cudaSetDevice(c->device);
+    auto* s = new sf_session();
+    s->ctx = c;
+    s->graph = g;
+    s->scene = *scene;
+    s->cfg = *cfg;
+    st = session_alloc(s);
+    if (st != SF_OK) {
+        if (s->mem) ctx_free(c, s->mem, s->mem_bytes);
+        delete s;
+        return st;
+    }
+    *out = s;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t blocks_per_sm, uint32_t threads) {
+    if (!s) return fail(SF_ERR_INVALID, "null session");
+    if (threads % 32 || threads == 0 || threads > 1024 || blocks_per_sm == 0 || blocks_per_sm > 64)
+        return fail(SF_ERR_INVALID, "invalid launch shape");
+    s->blocks_per_sm = blocks_per_sm;
+    s->threads = threads;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t samples) {
+    if (!s) return fail(SF_ERR_INVALID, "null session");
+    if (tile.w == 0 || tile.h == 0 || samples == 0) return SF_OK;
+    if (tile.x + tile.w > s->cfg.width || tile.y + tile.h > s->cfg.height)
+        return fail(SF_ERR_INVALID, "tile outside the image");
+    uint64_t paths = uint64_t(tile.w) * tile.h * samples;
+    if (paths > s->capacity) return fail(SF_ERR_INVALID, "tile * samples exceeds the session capacity");
+    sf_context* c = s->ctx;
+    cudaSetDevice(c->device);
+    DispatchGeom g{tile.x, tile.y, tile.w, tile.h, tile.done, samples, uint32_t(paths)};
+    cudaStream_t st = c->stream;
+    if (s->cfg.integrator == SF_INTEGRATOR_MEGAKERNEL) {
+        {
+            LaunchTimer t(c, true);
+            CU(sf_launch_megakernel(s->graph->d_prog, s->d_scene, s->soa, g, s->film, c->d_stats, st));
+        }
+        LaunchTimer t2(c, false);
+        CU(sf_launch_commit(s->soa, g, s->film, st));
+        s->dispatches++;
+        return SF_OK;
+    }
+    const uint32_t R = rounds_of(s->cfg);
+    const size_t N = s->capacity;
+    CU(cudaMemsetAsync(s->counts, 0, size_t(R + 1) * 16, st));
+    {
+        LaunchTimer t(c, false);
+        CU(sf_launch_generate(s->d_scene, s->soa, g, s->counts, st));
+    }
+    for (uint32_t r = 0; r < R; ++r) {
+        uint32_t cur = r & 1, nxt = cur ^ 1;
+        RoundQueues q;
+        q.active = r == 0 ? nullptr : s->lists + (cur * 3 + 0) * N;
+        q.cont = r == 0 ? nullptr : s->lists + (cur * 3 + 1) * N;
+        q.shadow = s->lists + (cur * 3 + 2) * N;
+        q.counts = s->counts + 4 * r;
+        q.next_active = s->lists + (nxt * 3 + 0) * N;
+        q.next_cont = s->lists + (nxt * 3 + 1) * N;
+        q.next_shadow = s->lists + (nxt * 3 + 2) * N;
+        q.next_counts = s->counts + 4 * (r + 1);
+        q.work_counter = s->counts + 4 * r + 3;
+        {
+            LaunchTimer t(c, true);
+            CU(sf_launch_trace(s->graph->d_prog, s->d_scene, s->soa, q, c->d_stats,
+                               int(s->blocks_per_sm) * c->sm_count, int(s->threads), st));
+        }
+        LaunchTimer t(c, false);
+        CU(sf_launch_shade(s->d_scene, s->soa, q, g, s->film, s->status, r + 1 == R ? 1 : 0, st));
+    }
+    LaunchTimer t(c, false);
+    CU(sf_launch_commit(s->soa, g, s->film, st));
+    s->dispatches++;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_sync(sf_session* s, uint32_t timeout_ms, uint32_t* status_word) {
+    if (!s) return fail(SF_ERR_INVALID, "null session");
+    sf_context* c = s->ctx;
+    cudaSetDevice(c->device);
+    sf_status st = wait_stream(c->stream, timeout_ms);
+    if (st != SF_OK) return st;
+    uint32_t w = 0;
+    CU(cudaMemcpy(&w, s->status, 4, cudaMemcpyDeviceToHost));
+    s->status_host |= w;
+    if (status_word) *status_word = s->status_host;
+    if (s->status_host) return fail(SF_ERR_WAVEFRONT, "wavefront invariant word " + std::to_string(s->status_host));
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_step(sf_session* s, uint32_t budget_ms, int* done) {
+    if (!s) return fail(SF_ERR_INVALID, "null session");
+    auto t0 = std::chrono::steady_clock::now();
+    const uint32_t target = s->cfg.samples_per_pixel;
+    for (;;) {
+        // TileGrid::next_pending (tiles.rs:52-59): least-advanced tile below target, lowest index.
+        int best = -1;
+        for (size_t i = 0; i < s->tiles.size(); ++i)
+            if (s->tiles[i].done < target && (best < 0 || s->tiles[i].done < s->tiles[best].done)) best = int(i);
+        if (best < 0) break;
+        sf_tile& t = s->tiles[best];
+        uint32_t n = std::min(s->cfg.samples_per_dispatch, target - t.done);
+        sf_status st = sf_session_dispatch(s, t, n);
+        if (st != SF_OK) return st;
+        st = sf_session_sync(s, 10000, nullptr);  // DISPATCH_TIMEOUT, renderer.rs:236
+        if (st != SF_OK) return st;
+        t.done += n;
+        double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+        if (budget_ms && el >= budget_ms) break;
+    }
+    bool complete = true;
+    for (auto& t : s->tiles)
+        if (t.done < target) complete = false;
+    if (done) *done = complete ? 1 : 0;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_progress(sf_session* s, sf_progress* out) {
+    if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
+    std::memset(out, 0, sizeof *out);
+    out->tiles = uint32_t(s->tiles.size());
+    out->dispatches = s->dispatches;
+    out->target = s->cfg.samples_per_pixel;
+    uint32_t mn = 0xffffffffu, mx = 0;
+    for (auto& t : s->tiles) {
+        mn = std::min(mn, t.done);
+        mx = std::max(mx, t.done);
+        out->pixel_samples_done += uint64_t(t.w) * t.h * t.done;
+    }
+    out->samples_min = s->tiles.empty() ? 0 : mn;
+    out->samples_max = mx;
+    out->pixel_samples_total = uint64_t(s->cfg.width) * s->cfg.height * s->cfg.samples_per_pixel;
+    out->status_word = s->status_host;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t capacity, uint32_t* count) {
+    if (!s || !count) return fail(SF_ERR_INVALID, "null argument");
+    *count = uint32_t(s->tiles.size());
+    if (tiles)
+        for (uint32_t i = 0; i < std::min<uint32_t>(capacity, *count); ++i) tiles[i] = s->tiles[i];
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
+    if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
+    sf_context* c = s->ctx;
+    cudaSetDevice(c->device);
+    size_t px = size_t(s->cfg.width) * s->cfg.height;
+    if (out->accum) CU(cudaMemcpyAsync(out->accum, s->film.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
+    if (out->depth) CU(cudaMemcpyAsync(out->depth, s->film.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (out->aux) CU(cudaMemcpyAsync(out->aux, s->film.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_stats(sf_session* s, sf_stats* out) {
+    if (!s) return fail(SF_ERR_INVALID, "null session");
+    return sf_context_stats(s->ctx, out);
+}
+
+extern "C" sf_status sf_session_destroy(sf_session* s) {
+    if (!s) return SF_OK;
+    cudaSetDevice(s->ctx->device);
+    cudaStreamSynchronize(s->ctx->stream);
+    ctx_free(s->ctx, s->mem, s->mem_bytes);
+    delete s;
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ checkpoints
+namespace {
+
+uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+    const uint8_t* p = static_cast<const uint8_t*>(data);
+    for (size_t i = 0; i < n; ++i) {
+        h ^= p[i];
+        h *= 0x100000001b3ull;
+    }
+    return h;
+}
+
+struct Writer {
+    std::vector<uint8_t> buf;
+    template <class T> void put(const T& v) {
+        const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+        buf.insert(buf.end(), p, p + sizeof(T));
+    }
+    void put_bytes(const void* p, size_t n) {
+        const uint8_t* q = static_cast<const uint8_t*>(p);
+        buf.insert(buf.end(), q, q + n);
+    }
+    void put_str(const std::string& s) { put(uint32_t(s.size())); put_bytes(s.data(), s.size()); }
+};
+struct Reader {
+    const std::vector<uint8_t>& buf;
+    size_t pos = 0;
+    bool ok = true;
+    template <class T> T get() {
+        T v{};
+        if (pos + sizeof(T) > buf.size()) { ok = false; return v; }
+        std::memcpy(&v, buf.data() + pos, sizeof(T));
+        pos += sizeof(T);
+        return v;
+    }
+    void get_bytes(void* p, size_t n) {
+        if (pos + n > buf.size()) { ok = false; return; }
+        std::memcpy(p, buf.data() + pos, n);
+        pos += n;
+    }
+    std::string get_str() {
+        uint32_t n = get<uint32_t>();
+        if (!ok || pos + n > buf.size()) { ok = false; return ""; }
+        std::string s(reinterpret_cast<const char*>(buf.data() + pos), n);
+        pos += n;
+        return s;
+    }
+};
+
+const uint32_t CK_MAGIC = 0x4b434653u;  // "SFCK"
+const uint32_t CK_VERSION = 1;
+
+std::string producer_of(const sf_context* c) {
+    return c->device_name + "|sm_" + std::to_string(c->cc_major) + std::to_string(c->cc_minor) + "|abi " +
+           std::to_string(ABI_VERSION);
+}
+
+bool write_file(const std::string& path, const std::vector<uint8_t>& data) {
+    std::ofstream f(path, std::ios::binary | std::ios::trunc);
+    if (!f) return false;
+    f.write(reinterpret_cast<const char*>(data.data()), std::streamsize(data.size()));
+    return bool(f);
+}
+bool read_file(const std::string& path, std::vector<uint8_t>& data) {
+    std::ifstream f(path, std::ios::binary);
+    if (!f) return false;
+    f.seekg(0, std::ios::end);
+    std::streamoff n = f.tellg();
+    if (n < 0) return false;
+    f.seekg(0);
+    data.resize(size_t(n));
+    f.read(reinterpret_cast<char*>(data.data()), n);
+    return bool(f) || f.eof();
+}
+void remove_tree(const std::string& dir) {
+    for (const char* name : {"state.bin", "film.bin"}) unlink((dir + "/" + name).c_str());
+    rmdir(dir.c_str());
+}
+
+}  // namespace
+
+extern "C" sf_status sf_session_save(sf_session* s, const char* dir) {
+    if (!s || !dir || !*dir) return fail(SF_ERR_INVALID, "null argument");
+    sf_context* c = s->ctx;
+    cudaSetDevice(c->device);
+    CU(cudaStreamSynchronize(c->stream));
+    size_t px = size_t(s->cfg.width) * s->cfg.height;
+    Writer film;
+    film.buf.resize(px * 36);
+    CU(cudaMemcpy(film.buf.data(), s->film.accum, px * 16, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(film.buf.data() + px * 16, s->film.depth, px * 4, cudaMemcpyDeviceToHost));
+    CU(cudaMemcpy(film.buf.data() + px * 20, s->film.aux, px * 16, cudaMemcpyDeviceToHost));
+    Writer w;
+    w.put(CK_MAGIC);
+    w.put(CK_VERSION);
+    w.put_str(producer_of(c));
+    w.put(s->cfg);
+    w.put(s->scene);
+    w.put_str(s->graph->topology);
+    w.put(uint32_t(s->graph->host.nodes.size()));
+    w.put_bytes(s->graph->host.nodes.data(), s->graph->host.nodes.size() * sizeof(sf_node));
+    w.put(s->dispatches);
+    w.put(s->tile_size);
+    w.put(uint32_t(s->tiles.size()));
+    for (auto& t : s->tiles) w.put(t);
+    w.put(uint64_t(film.buf.size()));
+    w.put(fnv1a(film.buf.data(), film.buf.size()));
+    uint64_t h = fnv1a(w.buf.data(), w.buf.size());
+    w.put(h);
+    // write a sibling directory, then swap it in (session.rs:33-45)
+    std::string final_dir(dir), tmp = final_dir + ".tmp-" + std::to_string(getpid()), old = final_dir + ".old";
+    remove_tree(tmp);
+    if (mkdir(tmp.c_str(), 0755) != 0) return fail(SF_ERR_IO, "cannot create " + tmp);
+    if (!write_file(tmp + "/film.bin", film.buf) || !write_file(tmp + "/state.bin", w.buf)) {
+        remove_tree(tmp);
+        return fail(SF_ERR_IO, "cannot write checkpoint files");
+    }
+    struct stat st;
+    bool existed = stat(final_dir.c_str(), &st) == 0;
+    if (existed) {
+        remove_tree(old);
+        if (rename(final_dir.c_str(), old.c_str()) != 0) { remove_tree(tmp); return fail(SF_ERR_IO, "cannot move old checkpoint"); }
+    }
+    if (rename(tmp.c_str(), final_dir.c_str()) != 0) return fail(SF_ERR_IO, "cannot install checkpoint");
+    if (existed) remove_tree(old);
+    return SF_OK;
+}
+
+extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* dir, sf_session** out) {
+    if (!c || !g || !dir || !out) return fail(SF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    std::string d(dir);
+    std::vector<uint8_t> state, filmb;
+    if (!read_file(d + "/state.bin", state) || !read_file(d + "/film.bin", filmb))
+        return fail(SF_ERR_IO, "cannot read checkpoint in " + d);
+    if (state.size() < 16) return fail(SF_ERR_CHECKPOINT, "checkpoint state truncated");
+    uint64_t stored;
+    std::memcpy(&stored, state.data() + state.size() - 8, 8);
+    if (fnv1a(state.data(), state.size() - 8) != stored) return fail(SF_ERR_CHECKPOINT, "checkpoint state hash mismatch");
+    Reader r{state};
+    if (r.get<uint32_t>() != CK_MAGIC || r.get<uint32_t>() != CK_VERSION)
+        return fail(SF_ERR_CHECKPOINT, "not a checkpoint of this version");
+    std::string producer = r.get_str();
+    if (producer != producer_of(c))
+        return fail(SF_ERR_CHECKPOINT, "checkpoint from another producer: " + producer);
+    sf_render_config cfg = r.get<sf_render_config>();
+    sf_scene_desc scene = r.get<sf_scene_desc>();
+    std::string topo = r.get_str();
+    uint32_t nn = r.get<uint32_t>();
+    std::vector<sf_node> nodes(nn);
+    if (nn > 4096) return fail(SF_ERR_CHECKPOINT, "checkpoint graph too large");
+    r.get_bytes(nodes.data(), nn * sizeof(sf_node));
+    uint32_t dispatches = r.get<uint32_t>();
+    uint32_t tile_size = r.get<uint32_t>();
+    uint32_t nt = r.get<uint32_t>();
+    if (!r.ok || nt > (1u << 24)) return fail(SF_ERR_CHECKPOINT, "checkpoint state truncated");
+    std::vector<sf_tile> tiles(nt);
+    for (auto& t : tiles) t = r.get<sf_tile>();
+    uint64_t film_bytes = r.get<uint64_t>();
+    uint64_t film_hash = r.get<uint64_t>();
+    if (!r.ok) return fail(SF_ERR_CHECKPOINT, "checkpoint state truncated");
+    if (film_bytes != filmb.size() || fnv1a(filmb.data(), filmb.size()) != film_hash)
+        return fail(SF_ERR_CHECKPOINT, "checkpoint film hash mismatch");
+    if (topo != g->topology || nn != g->host.nodes.size() ||
+        std::memcmp(nodes.data(), g->host.nodes.data(), nn * sizeof(sf_node)) != 0)
+        return fail(SF_ERR_CHECKPOINT, "checkpoint was made with another graph");
+    size_t px = size_t(cfg.width) * cfg.height;
+    if (filmb.size() != px * 36) return fail(SF_ERR_CHECKPOINT, "checkpoint film size mismatch");
+    sf_session* s = nullptr;
+    sf_status st = sf_session_create(c, g, &scene, &cfg, &s);
+    if (st != SF_OK) return st;
+    if (s->tile_size != tile_size || s->tiles.size() != tiles.size()) {
+        sf_session_destroy(s);
+        return fail(SF_ERR_CHECKPOINT, "checkpoint tile layout mismatch");
+    }
+    for (size_t i = 0; i < tiles.size(); ++i) {
+        const sf_tile& a = tiles[i];
+        const sf_tile& b = s->tiles[i];
+        if (a.x != b.x || a.y != b.y || a.w != b.w || a.h != b.h || a.done > cfg.samples_per_pixel) {
+            sf_session_destroy(s);
+            return fail(SF_ERR_CHECKPOINT, "checkpoint tile layout mismatch");
+        }
+    }
+    s->tiles = tiles;
+    s->dispatches = dispatches;
+    cudaError_t e = cudaMemcpy(s->film.accum, filmb.data(), px * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->film.depth, filmb.data() + px * 16, px * 4, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess) e = cudaMemcpy(s->film.aux, filmb.data() + px * 20, px * 16, cudaMemcpyHostToDevice);
+    if (e != cudaSuccess) {
+        sf_session_destroy(s);
+        return cuda_fail(e, "checkpoint upload");
+    }
+    *out = s;
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ escape time
+namespace {
+void planar_dev(const sf_planar_desc& f, PlanarDev& o) {
+    std::memset(&o, 0, sizeof o);
+    o.family = f.family;
+    o.power = f.power;
+    o.iterations = f.iterations;
+    o.julia[0] = f.julia[0];
+    o.julia[1] = f.julia[1];
+    o.center[0] = f.center[0];
+    o.center[1] = f.center[1];
+    o.zoom = f.zoom;
+    o.inversion = f.inversion;
+    o.relaxation = f.relaxation;
+    o.memory = f.memory;
+    o.bailout = f.bailout;
+    o.trap_radius = f.trap_radius;
+    o.stripes = f.stripes;
+    // f32::to_radians then sin_cos, evaluated on the host in binary32 (planar.rs:79-80, :97)
+    const float k = 3.14159265358979323846f / 180.0f;
+    float a = f.angle * k, t = f.twist * k;
+    o.angle_sin = sinf(a);
+    o.angle_cos = cosf(a);
+    o.twist_sin = sinf(t);
+    o.twist_cos = cosf(t);
+}
+sf_status planar_check(const sf_planar_desc* f) {
+    if (!f) return fail(SF_ERR_INVALID, "null planar descriptor");
+    if (f->family > 5) return fail(SF_ERR_INVALID, "unknown planar family");
+    if (f->power < 1 || f->power > 8) return fail(SF_ERR_INVALID, "power must be between 1 and 8");
+    if (!(f->zoom != 0.0f)) return fail(SF_ERR_INVALID, "zoom must be non-zero");
+    return SF_OK;
+}
+}  // namespace
+
+extern "C" sf_status sf_planar_probe(sf_context* c, const sf_planar_desc* f, const float* xy, size_t n, float* dist,
+                                     float* traps, uint32_t* iters) {
+    if (!c) return fail(SF_ERR_INVALID, "null context");
+    sf_status st = planar_check(f);
+    if (st != SF_OK) return st;
+    if (n == 0) return SF_OK;
+    if (!xy || !dist || !traps || !iters) return fail(SF_ERR_INVALID, "null buffer");
+    cudaSetDevice(c->device);
+    PlanarDev F;
+    planar_dev(*f, F);
+    std::vector<float> soa(2 * n);
+    for (size_t i = 0; i < n; ++i) { soa[i] = xy[2 * i]; soa[n + i] = xy[2 * i + 1]; }
+    size_t bytes = 256 + n * 4 * (2 + 1 + 4 + 1);
+    void* buf = nullptr;
+    st = ctx_alloc(c, bytes, &buf);
+    if (st != SF_OK) return st;
+    PlanarDev* dF = static_cast<PlanarDev*>(buf);
+    float* din = reinterpret_cast<float*>(static_cast<char*>(buf) + 256);
+    float* dd = din + 2 * n;
+    float* dt = dd + n;
+    uint32_t* di = reinterpret_cast<uint32_t*>(dt + 4 * n);
+    cudaError_t e = cudaMemcpyAsync(dF, &F, sizeof F, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(din, soa.data(), 2 * n * 4, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        LaunchTimer t(c, true);
+        e = sf_launch_planar(dF, din, din + n, n, dd, dt, di, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dist, dd, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(traps, dt, 4 * n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(iters, di, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    ctx_free(c, buf, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "sf_planar_probe");
+    return SF_OK;
+}
+
+extern "C" sf_status sf_escape2d(sf_context* c, const sf_planar_desc* f, const sf_canvas* canvas, sf_tile tile,
+                                 uint32_t sample, float* dist, float* traps, uint32_t* iters) {
+    if (!c || !canvas) return fail(SF_ERR_INVALID, "null argument");
+    sf_status st = planar_check(f);
+    if (st != SF_OK) return st;
+    if (!canvas->width || !canvas->height || tile.x + tile.w > canvas->width || tile.y + tile.h > canvas->height)
+        return fail(SF_ERR_INVALID, "tile outside the canvas");
+    size_t n = size_t(tile.w) * tile.h;
+    if (n == 0) return SF_OK;
+    if (!dist || !traps || !iters) return fail(SF_ERR_INVALID, "null buffer");
+    cudaSetDevice(c->device);
+    PlanarDev F;
+    planar_dev(*f, F);
+    CanvasDev K;
+    std::memset(&K, 0, sizeof K);
+    K.center[0] = canvas->center[0];
+    K.center[1] = canvas->center[1];
+    K.zoom = canvas->zoom;
+    K.aspect = float(canvas->width) / float(canvas->height);
+    float r = canvas->rotation_deg * (3.14159265358979323846f / 180.0f);
+    K.rot_sin = sinf(r);
+    K.rot_cos = cosf(r);
+    K.width = canvas->width;
+    K.height = canvas->height;
+    K.seed = uint32_t(canvas->seed) ^ uint32_t(canvas->seed >> 32);
+    size_t bytes = 512 + n * 4 * 6;
+    void* buf = nullptr;
+    st = ctx_alloc(c, bytes, &buf);
+    if (st != SF_OK) return st;
+    PlanarDev* dF = static_cast<PlanarDev*>(buf);
+    CanvasDev* dK = reinterpret_cast<CanvasDev*>(static_cast<char*>(buf) + 256);
+    float* dd = reinterpret_cast<float*>(static_cast<char*>(buf) + 512);
+    float* dt = dd + n;
+    uint32_t* di = reinterpret_cast<uint32_t*>(dt + 4 * n);
+    cudaError_t e = cudaMemcpyAsync(dF, &F, sizeof F, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dK, &K, sizeof K, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) {
+        LaunchTimer t(c, true);
+        e = sf_launch_escape2d(dF, dK, tile.x, tile.y, tile.w, tile.h, sample, dd, dt, di, c->d_stats, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(dist, dd, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(traps, dt, 4 * n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(iters, di, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    ctx_free(c, buf, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "sf_escape2d");
+    return SF_OK;
+}
+
+extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uint32_t* iters, float* smooth,
+                                  int reference_f64, uint32_t* iters64, float* smooth64, uint64_t* rebases) {
+    if (!c || !d) return fail(SF_ERR_INVALID, "null argument");
+    if (!d->width || !d->height || !d->max_iter) return fail(SF_ERR_INVALID, "empty deep-zoom request");
+    if (!iters || !smooth) return fail(SF_ERR_INVALID, "null output");
+    if (reference_f64 && (!iters64 || !smooth64)) return fail(SF_ERR_INVALID, "null FP64 output");
+    if (!(d->bailout >= 2.0f)) return fail(SF_ERR_INVALID, "bailout must be at least 2");
+    cudaSetDevice(c->device);
+    size_t n = size_t(d->width) * d->height;
+    size_t M = size_t(d->max_iter) + 2;
+    size_t bytes = M * 16 + M * 8 + 256 + n * 8 * (reference_f64 ? 2 : 1);
+    void* buf = nullptr;
+    sf_status st = ctx_alloc(c, bytes, &buf);
+    if (st != SF_OK) return st;
+    char* b = static_cast<char*>(buf);
+    double2* od = reinterpret_cast<double2*>(b);
+    float2* of = reinterpret_cast<float2*>(b + M * 16);
+    uint32_t* olen = reinterpret_cast<uint32_t*>(b + M * 24);
+    uint32_t* di = reinterpret_cast<uint32_t*>(b + M * 24 + 256);
+    float* ds = reinterpret_cast<float*>(di + n);
+    uint32_t* di64 = reinterpret_cast<uint32_t*>(ds + n);
+    float* ds64 = reinterpret_cast<float*>(di64 + n);
+    double cx = d->center_hi[0] + d->center_lo[0], cy = d->center_hi[1] + d->center_lo[1];
+    double pitch = d->width_units / double(d->width);
+    cudaError_t e = cudaSuccess;
+    unsigned long long before[SF_STAT_COUNT];
+    e = cudaMemcpyAsync(before, c->d_stats, sizeof before, cudaMemcpyDeviceToHost, c->stream);
+    {
+        LaunchTimer t(c, false);
+        if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, od, of, olen, c->stream);
+    }
+    if (e == cudaSuccess) {
+        LaunchTimer t(c, true);
+        e = sf_launch_perturb(of, olen, d->width, d->height, float(pitch), 1.0f, d->max_iter, d->bailout, di, ds,
+                              c->d_stats, c->stream);
+    }
+    if (e == cudaSuccess && reference_f64) {
+        LaunchTimer t(c, false);
+        e = sf_launch_direct_f64(cx, cy, d->width, d->height, pitch, d->max_iter, d->bailout, di64, ds64, c->stream);
+    }
+    if (e == cudaSuccess) e = cudaMemcpyAsync(iters, di, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(smooth, ds, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && reference_f64) e = cudaMemcpyAsync(iters64, di64, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess && reference_f64) e = cudaMemcpyAsync(smooth64, ds64, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    unsigned long long after[SF_STAT_COUNT];
+    if (e == cudaSuccess) e = cudaMemcpyAsync(after, c->d_stats, sizeof after, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
+    ctx_free(c, buf, bytes);
+    if (e != cudaSuccess) return cuda_fail(e, "sf_deep_zoom");
+    if (rebases) *rebases = after[SF_STAT_STEPS] - before[SF_STAT_STEPS];
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ FP32 peak
+extern "C" sf_status sf_device_fp32_peak(sf_context* c, double* tflops) {
+    if (!c || !tflops) return fail(SF_ERR_INVALID, "null argument");
+    cudaSetDevice(c->device);
+    void* buf = nullptr;
+    sf_status s = ctx_alloc(c, 256, &buf);
+    if (s != SF_OK) return s;
+    const int blocks = c->sm_count * 8;
+    const uint32_t iters = 4096;
+    cudaEvent_t a, b;
+    cudaEventCreate(&a);
+    cudaEventCreate(&b);
+    cudaError_t e = sf_launch_ffma_peak(static_cast<float*>(buf), 64, blocks, c->stream);  // warm-up
+    float best = 1e30f;
+    for (int rep = 0; rep < 5 && e == cudaSuccess; ++rep) {
+        cudaEventRecord(a, c->stream);
+        e = sf_launch_ffma_peak(static_cast<float*>(buf), iters, blocks, c->stream);
+        cudaEventRecord(b, c->stream);
+        if (e == cudaSuccess) e = cudaEventSynchronize(b);
+        float ms = 0;
+        if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
+        if (ms > 0 && ms < best) best = ms;
+    }
+    cudaEventDestroy(a);
+    cudaEventDestroy(b);
+    ctx_free(c, buf, 256);
+    if (e != cudaSuccess) return cuda_fail(e, "fp32 peak probe");
+    double flops = double(blocks) * 256.0 * iters * 16.0 * 8.0 * 2.0;
+    *tflops = flops / (best * 1e-3) / 1e12;
+    return SF_OK;
+}

@@ -1,0 +1,104 @@
+// Launch parameter blocks and host-callable launchers of sf_kernels.cu.
+#pragma once
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "sf_program.h"
+
+// Path flags kept in the path state.
+enum { SF_PF_CONT = 1u, SF_PF_SHADOW = 2u, SF_PF_FROM_BSDF = 4u };
+// Hit record flags.
+enum { SF_HF_HIT = 1u, SF_HF_EXHAUSTED = 2u };
+// Wavefront invariant word (wavefront.wgsl:183/:220/:236 bits 1, 2, 4).
+enum { SF_WF_QUEUE_OVERFLOW = 1u, SF_WF_COMPACT_OVERFLOW = 2u, SF_WF_ALIVE_AT_COMMIT = 4u };
+
+// Statistics accumulated by the trace kernels (64-bit device counters).
+enum { SF_STAT_DE_EVALS = 0, SF_STAT_DE_ITERS, SF_STAT_SEGMENTS, SF_STAT_STEPS, SF_STAT_SHADOW_SEGMENTS,
+       SF_STAT_COUNT = 8 };
+
+// Structure-of-arrays path storage for one dispatch of `capacity` paths.
+struct PathSoA {
+    float4* o;       // ray origin, w = prev_pdf
+    float4* d;       // ray direction, w = prev_area_total
+    float4* tp;      // throughput, w = bits(rng)
+    float4* L;       // radiance, w = bits(bounce | flags << 16)
+    float4* pn;      // prev normal, w unused
+    float4* sh_o;    // shadow origin, w = t_end
+    float4* sh_d;    // shadow direction
+    float4* sh_c;    // radiance carried by the shadow segment if clear
+    uint4* hit;      // (bits(t), steps, light_index, flags)
+    float4* hit_tr;  // normalised traps
+    float4* hit_n;   // normal, w = bits(iterations | material << 16)
+    uint32_t* vis;   // shadow visibility (1 = clear)
+    float4* Ls;      // per-path final radiance (committed in ascending sample order)
+    uint32_t capacity;
+};
+
+// Queues of one round: active paths, continuation rays, shadow rays (ids),
+// with their counts in `counts[0..2]`; next round's lists are written by shade.
+struct RoundQueues {
+    const uint32_t* active;   // null: identity (round 0)
+    const uint32_t* cont;     // null: identity (round 0)
+    const uint32_t* shadow;
+    const uint32_t* counts;   // [active, cont, shadow]
+    uint32_t* next_active;
+    uint32_t* next_cont;
+    uint32_t* next_shadow;
+    uint32_t* next_counts;    // [active, cont, shadow]
+    uint32_t* work_counter;   // trace kernel fetch counter (zeroed per round)
+};
+
+struct FilmPlanes {
+    float4* accum;  // sum of (L, 1) per sample
+    float* depth;   // first-hit distance, -1 for a miss (sample 0)
+    float4* aux;    // first-hit normal and steps (sample 0)
+    uint32_t width, height;
+};
+
+struct DispatchGeom {
+    uint32_t tile_x, tile_y, tile_w, tile_h;
+    uint32_t sample_start, samples;
+    uint32_t paths;  // tile_w * tile_h * samples
+};
+
+struct PlanarDev {
+    uint32_t family, power, iterations, pad;
+    float julia[2], center[2];
+    float zoom, inversion, relaxation, memory, bailout, trap_radius, stripes;
+    float angle_cos, angle_sin, twist_cos, twist_sin;
+};
+
+struct CanvasDev {
+    float center[2], zoom, aspect, rot_cos, rot_sin;
+    uint32_t width, height, seed;
+};
+
+// ---- launchers (return cudaError_t of the launch) ----
+cudaError_t sf_launch_de_probe(const DeProgram* prog, const float* x, const float* y, const float* z, size_t n,
+                               float* dist, float* traps, uint32_t* iters, uint32_t* mats, cudaStream_t st);
+cudaError_t sf_launch_primary(const DeProgram* prog, const DevScene* scene, uint32_t width, uint32_t height,
+                              uint32_t max_steps, int rule, float eps, float t_far, int normal_mode, float* t_out,
+                              uint32_t* steps_out, float* normal_out, uint32_t* work_counter,
+                              unsigned long long* stats, int persistent, cudaStream_t st);
+cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom g, uint32_t* counts, cudaStream_t st);
+cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, RoundQueues q,
+                            unsigned long long* stats, int blocks, int threads, cudaStream_t st);
+cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
+                            uint32_t* status, int final_round, cudaStream_t st);
+cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st);
+cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, PathSoA soa, DispatchGeom g,
+                                 FilmPlanes film, unsigned long long* stats, cudaStream_t st);
+cudaError_t sf_launch_planar(const PlanarDev* f, const float* x, const float* y, size_t n, float* dist, float* traps,
+                             uint32_t* iters, cudaStream_t st);
+cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint32_t tile_x, uint32_t tile_y,
+                               uint32_t tile_w, uint32_t tile_h, uint32_t sample, float* dist, float* traps,
+                               uint32_t* iters, unsigned long long* stats, cudaStream_t st);
+cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d,
+                                float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
+cudaError_t sf_launch_perturb(const float2* orbit_f, const uint32_t* orbit_len, uint32_t width, uint32_t height,
+                              float pitch, float aspect_unused, uint32_t max_iter, float bailout, uint32_t* iters,
+                              float* smooth, unsigned long long* stats, cudaStream_t st);
+cudaError_t sf_launch_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch, uint32_t max_iter,
+                                 double bailout, uint32_t* iters, float* smooth, cudaStream_t st);
+int sf_device_sm_count();
+cudaError_t sf_launch_ffma_peak(float* out, uint32_t iters, int blocks, cudaStream_t st);

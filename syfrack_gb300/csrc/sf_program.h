@@ -1,0 +1,99 @@
+// Lowered form graph and per-launch parameter blocks shared by the host
+// library (sf_host.cpp) and the sm_103a kernels (sf_kernels.cu). Plain data only.
+//
+// The reference compiles a Graph into a WGSL `de_sample` function and packs its
+// scalars into a uniform array (graph_wgsl.rs:949-1179, ParamLayout :30-184).
+// Here a graph is lowered once on the host into a `DeProgram`:
+//   * `form` names a specialised device routine when the graph is one of the
+//     iterated forms (Mandelbulb, Mandelbox, Menger body orders of graphs/*.ron),
+//     whose constants are read from `fp`;
+//   * otherwise `ops` is a postfix program run by the generic interpreter: every
+//     distance leaf re-evaluates its point chain from the input point (leaves
+//     that share a prefix recompute it; the result is identical), fences push a
+//     distance state, combinations pop two.
+#pragma once
+#include <stdint.h>
+
+#define SF_MAX_OPS 96
+#define SF_MAX_LOOP_DEPTH 4
+#define SF_MAX_DIST_STACK 6
+
+// Opcodes of the generic interpreter. Point and fence operations use the node
+// kind (enum sf_node_kind) as their code; control codes start at 100.
+enum {
+    SF_OP_BEGIN = 100,      // point state := input point
+    SF_OP_ITER_BEGIN = 101, // a = iterations, b = index of the matching ITER_END, f0 = bailout
+    SF_OP_ITER_END = 102,   // a = index of the matching ITER_BEGIN
+    SF_OP_FENCE_OFF = 103,  // disabled fence: push +inf with the point's iter/traps
+    SF_OP_EMPTY = 104,      // unconnected distance input: push the empty state
+    SF_OP_TAG = 105,        // a = material index
+    SF_OP_BOUND = 106,      // top.d = max(top.d, box(point)); f0..2 = half
+    SF_OP_COMBINE = 107,    // a = node kind of the combination, f0 = k
+    SF_OP_END = 108
+};
+
+struct DeOp {
+    uint32_t code;
+    uint32_t a, b, c;
+    float f[8];
+};
+
+// Constants of the specialised forms.
+struct FormParams {
+    uint32_t iterations;
+    uint32_t trap_slot, trap_measure, trap_mode;  // the body's Trap node
+    float bailout;
+    float power;         // Bulb
+    uint32_t power_int;  // Bulb: 0 = trigonometric path, else the integer exponent 1..16
+    float limit;         // Box: fold limit
+    float min_radius2, fixed_radius2, fold_k_min;  // Box: mr^2, fr^2, fr^2/mr^2
+    float scale;         // Box: Scale factor; Menger: fold scale
+    float abs_scale;     // Box: |scale|
+    float offset[3];     // Menger: fold offset
+    float fence[3];      // NormFence inset / Box half
+    uint32_t material;   // MaterialTag index applied to the root (0 = none)
+};
+
+struct DeProgram {
+    uint32_t form;  // SF_FORM_*
+    uint32_t n_ops;
+    uint32_t iteration_product;
+    uint32_t max_stack;
+    float trap_scales[4];
+    FormParams fp;
+    DeOp ops[SF_MAX_OPS];
+};
+
+// One area light in device form (GpuLight of uniforms.rs:671-713 with the
+// derived quantities the shading code needs every bounce).
+struct DevLight {
+    float a[3], b[3], c[3], color[3];
+    float n[3];          // safe_normalize(cross(b, c))
+    float area;          // |cross(b, c)|
+    float inv_bb, inv_cc;// 1 / dot(b,b), 1 / dot(c,c)
+    float lum;           // luminance(color)
+};
+
+struct DevMaterial {
+    float albedo[3], roughness, metallic, specular, emission[3];
+};
+
+// Scene constants of one render (the Uniforms subset of common.wgsl:163-191
+// that the DE path reads).
+struct DevScene {
+    float origin[3], forward[3], right[3], up[3];
+    float tan_half, aspect, lens_radius, focus_distance;
+    uint32_t width, height;
+    uint32_t max_bounces, max_steps;
+    uint32_t seed;
+    uint32_t light_count, finish_count;
+    uint32_t variation_slot, variation_enabled;
+    float var_rough[2], var_metal[2];
+    float cavity;
+    float pixel_tolerance, step_scale, extent;  // extent = max(200, far)
+    float pixel_cone;                           // tan_half * 2 / width
+    uint32_t iteration_product;
+    DevMaterial material;
+    DevMaterial finishes[8];
+    DevLight lights[8];
+};

@@ -1,0 +1,417 @@
+// Sphere tracing and path transport on sm_103a.
+//
+// Device twins of pathtrace.wgsl (PCG :20-37, march_segment :78-145, BRDF
+// :195-463, direct_light :471-558, camera_ray :781-800, radiance :802-1201)
+// and lights.wgsl (:150-356), restricted to area emitters with fog, optics,
+// ocean, portals, guiding, textures, sun and environment off. The bounce body
+// is one function (bounce_body) used by both the per-pixel megakernel and the
+// wavefront shade stage, so both integrators perform identical arithmetic.
+#pragma once
+#include "sf_de.cuh"
+
+#define SF_NO_LIGHT 0xffffffffu
+#define SF_PI 3.14159265358979f  // common.wgsl:6
+
+// ------------------------------------------------------------------ RNG
+__device__ __forceinline__ uint32_t pcg(uint32_t v) {
+    uint32_t state = v * 747796405u + 2891336453u;
+    uint32_t word = ((state >> ((state >> 28u) + 4u)) ^ state) * 277803737u;
+    return (word >> 22u) ^ word;
+}
+__device__ __forceinline__ uint32_t rng_init(uint32_t px, uint32_t py, uint32_t sample, uint32_t seed) {
+    uint32_t h = pcg(seed);
+    h = pcg(h ^ px);
+    h = pcg(h ^ py);
+    h = pcg(h ^ sample);
+    return h;
+}
+__device__ __forceinline__ float rnd(uint32_t& state) {
+    state = pcg(state);
+    return float(state >> 8u) * (1.0f / 16777216.0f);
+}
+
+// ------------------------------------------------------------------ camera
+__device__ __forceinline__ void camera_ray(const DevScene& S, uint32_t px, uint32_t py, uint32_t& rng, float3& o,
+                                           float3& d) {
+    float jx = rnd(rng);
+    float jy = rnd(rng);
+    float ndcx = ((float(px) + jx) / float(S.width)) * 2.0f - 1.0f;
+    float ndcy = ((float(py) + jy) / float(S.height)) * 2.0f - 1.0f;
+    float3 dir = normalize3(ld3(S.forward) + ld3(S.right) * (ndcx * S.tan_half) +
+                            ld3(S.up) * (-ndcy * S.tan_half / S.aspect));
+    float3 origin = ld3(S.origin);
+    if (S.lens_radius > 0.0f) {
+        float3 focus = origin + dir * (S.focus_distance / fmaxf(dot3(dir, ld3(S.forward)), 1e-4f));
+        float r = S.lens_radius * sqrtf(rnd(rng));
+        float phi = 2.0f * SF_PI * rnd(rng);
+        origin = origin + ld3(S.right) * (r * cosf(phi)) + ld3(S.up) * (r * sinf(phi));
+        dir = normalize3(focus - origin);
+    }
+    o = origin;
+    d = dir;
+}
+
+// ------------------------------------------------------------------ march state machine
+// march_segment (pathtrace.wgsl:78-145) split into resumable steps so that a
+// persistent kernel can interleave lanes: march_query() gives the point to
+// evaluate, march_update() consumes its DE. absolute = fixed-epsilon hit test.
+enum { MARCH_CONTINUE = 0, MARCH_HIT = 1, MARCH_MISS = 2, MARCH_EXHAUSTED = 3 };
+struct March {
+    float3 ro, rd;
+    float t, omega, prev_radius, step_len, t_end;
+    float cand_t, cand_err;
+    DeRaw cand;
+    uint32_t i;  // steps taken
+};
+__device__ __forceinline__ void march_begin(March& m, float3 ro, float3 rd, float t_end) {
+    m.ro = ro; m.rd = rd; m.t = 0.0f; m.omega = 1.2f; m.prev_radius = 0.0f; m.step_len = 0.0f;
+    m.t_end = t_end; m.cand_t = 0.0f; m.cand_err = 1e30f; m.i = 0;
+    m.cand.d = 200.0f; m.cand.t0 = m.cand.t1 = m.cand.t2 = m.cand.t3 = SF_INF;
+    m.cand.iter = 0; m.cand.material = 0;
+}
+// Before a step: decide whether the march continues; returns MARCH_CONTINUE when a
+// DE evaluation at m.ro + m.rd * m.t is needed.
+__device__ __forceinline__ int march_check(March& m, uint32_t max_steps, float accept) {
+    if (m.i >= max_steps) return m.cand_err < accept * 4.0f ? MARCH_HIT : MARCH_EXHAUSTED;
+    if (m.t >= m.t_end) return MARCH_MISS;
+    return MARCH_CONTINUE;
+}
+// After the DE at the current t: MARCH_HIT (hit at m.t, sample s), MARCH_MISS
+// (proven clear) or MARCH_CONTINUE (t advanced).
+__device__ __forceinline__ int march_update(March& m, const DeRaw& s, float safety, float accept, bool absolute) {
+    m.i += 1;
+    float radius = fabsf(s.d) * safety;
+    bool sor_fail = m.omega > 1.0f && (radius + m.prev_radius) < m.step_len * 1.0001f;
+    if (sor_fail) { m.step_len = m.step_len - m.omega * m.step_len; m.omega = 1.0f; }
+    else m.step_len = radius * m.omega;
+    m.prev_radius = radius;
+    float err = absolute ? radius : radius / fmaxf(m.t, 1e-6f);
+    if (!sor_fail && err < m.cand_err) { m.cand_t = m.t; m.cand = s; m.cand_err = err; }
+    if (!sor_fail && (absolute ? err <= accept : err < accept)) return MARCH_HIT;
+    if (!sor_fail && m.t + m.step_len >= m.t_end) {
+        if (radius >= m.t_end - m.t) return MARCH_MISS;
+        m.omega = 1.0f;
+        m.step_len = radius;
+    }
+    m.t += m.step_len;
+    return MARCH_CONTINUE;
+}
+
+// ------------------------------------------------------------------ lights (lights.wgsl)
+__device__ __forceinline__ float area_intersection(float3 ro, float3 rd, const DevLight& l) {
+    float3 n = ld3(l.n);
+    float den = dot3(n, rd);
+    if (fabsf(den) < 1e-7f) return 1e30f;
+    float t = dot3(ld3(l.a) - ro, n) / den;
+    if (t <= 1e-6f) return 1e30f;
+    float3 q = ro + rd * t - ld3(l.a);
+    float x = dot3(q, ld3(l.b)) * l.inv_bb;
+    float y = dot3(q, ld3(l.c)) * l.inv_cc;
+    if (fabsf(x) > 0.5f || fabsf(y) > 0.5f) return 1e30f;
+    return t;
+}
+__device__ __forceinline__ float area_weight(float3 p, float3 n, const DevLight& l) {
+    float3 to_light = ld3(l.a) - p;
+    float dist2 = fmaxf(dot3(to_light, to_light), 1e-6f);
+    float3 dir = to_light / sqrtf(dist2);
+    float facing = fmaxf(dot3(ld3(l.n), -dir), 0.0f);
+    return l.lum * l.area * facing * fmaxf(dot3(n, dir), 0.15f) / dist2;
+}
+__device__ __forceinline__ float area_total_weight(const DevScene& S, float3 p, float3 n) {
+    float total = 0.0f;
+    for (uint32_t i = 0; i < S.light_count; ++i) total += area_weight(p, n, S.lights[i]);
+    return total;
+}
+__device__ __forceinline__ float mis_power(float a, float b) {
+    float scale = fmaxf(a, b);
+    if (scale <= 0.0f) return 0.0f;
+    float pa = a / scale, pb = b / scale;
+    return pa * pa / (pa * pa + pb * pb);
+}
+// Emitter hit by a continuation ray (area_emission, lights.wgsl:330-356).
+__device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, float distance, float prev_pdf, bool use_mis,
+                                float3 prev_normal, float prev_total) {
+    float3 L = mk3(0.f, 0.f, 0.f);
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        float cos_l = dot3(ld3(l.n), -rd);
+        if (cos_l <= 0.0f) continue;
+        float t = area_intersection(ro, rd, l);
+        if (fabsf(t - distance) > fmaxf(1e-6f, distance * 1e-6f)) continue;
+        float w = 1.0f;
+        if (use_mis) {
+            float pl = (distance * distance) / fmaxf(l.area * cos_l, 1e-20f);
+            float selection = 0.0f;
+            if (prev_total > 0.0f) selection = area_weight(ro, prev_normal, l) / prev_total;
+            pl = pl * selection;
+            w = mis_power(prev_pdf, pl);
+        }
+        L = L + ld3(l.color) * w;
+    }
+    return L;
+}
+// Nearest emitter along a ray, before the geometry march (trace_geometry_lights).
+__device__ __forceinline__ float nearest_emitter(const DevScene& S, float3 ro, float3 rd, float t_end, uint32_t& li) {
+    float nearest = t_end;
+    li = SF_NO_LIGHT;
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        float t = area_intersection(ro, rd, S.lights[i]);
+        if (t < nearest) { nearest = t; li = i; }
+    }
+    return nearest;
+}
+
+// ------------------------------------------------------------------ BRDF
+struct Surface {
+    float3 n, diffuse, f0, emission;
+    float alpha;
+};
+__device__ __forceinline__ float luminance(float3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+__device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt) {
+    float s = n.z >= 0.0f ? 1.0f : -1.0f;
+    float a = -1.0f / (s + n.z);
+    float b = n.x * n.y * a;
+    t = mk3(1.0f + s * n.x * n.x * a, s * b, -s * n.x);
+    bt = mk3(b, s + n.y * n.y * a, -n.y);
+}
+__device__ __forceinline__ float3 frame_mul(float3 t, float3 bt, float3 n, float3 v) { return t * v.x + bt * v.y + n * v.z; }
+__device__ __forceinline__ float3 cosine_sample(float3 n, float r1, float r2) {
+    float phi = 2.0f * SF_PI * r1;
+    float r = sqrtf(r2);
+    float3 t, bt;
+    tangent_frame(n, t, bt);
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return frame_mul(t, bt, n, mk3(r * cp, r * sp, sqrtf(fmaxf(0.0f, 1.0f - r2))));
+}
+__device__ __forceinline__ float ggx_d(float nh, float a2) {
+    float d = nh * nh * (a2 - 1.0f) + 1.0f;
+    return a2 / (SF_PI * d * d);
+}
+__device__ __forceinline__ float smith_g1(float nv, float a2) { return 2.0f * nv / (nv + sqrtf(a2 + (1.0f - a2) * nv * nv)); }
+__device__ __forceinline__ float3 fresnel(float3 f0, float vh) {
+    float m = 1.0f - vh;
+    float m2 = m * m;
+    float p5 = m2 * m2 * m;  // pow(1 - vh, 5)
+    return f0 + (mk3(1.f, 1.f, 1.f) - f0) * p5;
+}
+__device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1, float r2) {
+    float3 t, bt;
+    tangent_frame(n, t, bt);
+    float3 lv = mk3(dot3(t, v), dot3(bt, v), dot3(n, v));
+    float3 vh = safe_normalize3(mk3(alpha * lv.x, alpha * lv.y, fmaxf(lv.z, 1e-5f)));
+    float lensq = vh.x * vh.x + vh.y * vh.y;
+    float3 t1 = mk3(1.f, 0.f, 0.f);
+    if (lensq > 0.0f) t1 = mk3(-vh.y, vh.x, 0.0f) / sqrtf(lensq);
+    float3 t2 = cross3(vh, t1);
+    float r = sqrtf(r1);
+    float phi = 2.0f * SF_PI * r2;
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    float x = r * cp;
+    float blend = 0.5f * (1.0f + vh.z);
+    float y0 = sqrtf(fmaxf(0.0f, 1.0f - x * x));
+    float y = y0 * (1.0f - blend) + (r * sp) * blend;
+    float3 nh = t1 * x + t2 * y + vh * sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y));
+    return frame_mul(t, bt, n, safe_normalize3(mk3(alpha * nh.x, alpha * nh.y, fmaxf(nh.z, 0.0f))));
+}
+__device__ float3 brdf_eval(const Surface& s, float3 v, float3 l) {
+    float nl = dot3(s.n, l), nv = dot3(s.n, v);
+    if (nl <= 0.0f || nv <= 0.0f) return mk3(0.f, 0.f, 0.f);
+    float3 h = normalize3(v + l);
+    float nh = fmaxf(dot3(s.n, h), 0.0f);
+    float vh = fmaxf(dot3(v, h), 0.0f);
+    float a2 = s.alpha * s.alpha;
+    float3 f = fresnel(s.f0, vh);
+    float3 spec = f * (ggx_d(nh, a2) * smith_g1(nv, a2) * smith_g1(nl, a2)) / fmaxf(4.0f * nv * nl, 1e-4f);
+    return s.diffuse * (mk3(1.f, 1.f, 1.f) - f) / SF_PI + spec;
+}
+__device__ __forceinline__ float spec_probability(const Surface& s, float nv) {
+    float3 f = fresnel(s.f0, nv);
+    return fminf(fmaxf(luminance(f) / fmaxf(luminance(f) + luminance(s.diffuse), 1e-4f), 0.05f), 0.95f);
+}
+__device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_spec) {
+    float nl = dot3(s.n, l);
+    if (nl <= 0.0f) return 0.0f;
+    float3 hh = normalize3(v + l);
+    float nh = fmaxf(dot3(s.n, hh), 0.0f);
+    float a2 = s.alpha * s.alpha;
+    float nv = fmaxf(dot3(s.n, v), 1e-4f);
+    float pdf_spec = ggx_d(nh, a2) * smith_g1(nv, a2) / (4.0f * nv);
+    return p_spec * pdf_spec + (1.0f - p_spec) * nl / SF_PI;
+}
+// make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
+__device__ Surface make_surface(const DevScene& S, float3 n, const DeSampleF& smp) {
+    const DevMaterial* m = &S.material;
+    bool assigned = smp.material > 0 && smp.material <= S.finish_count;
+    if (assigned) m = &S.finishes[smp.material - 1];
+    float3 albedo = ld3(m->albedo);
+    float rough = m->roughness, metallic = m->metallic, spec = m->specular;
+    float3 emission = assigned ? ld3(m->emission) : mk3(0.f, 0.f, 0.f);
+    if (!assigned && S.variation_enabled) {
+        uint32_t slot = S.variation_slot;
+        float value = slot < 4 ? smp.traps[slot]
+                               : (slot == 5 ? n.y * 0.5f + 0.5f : float(smp.iter) / fmaxf(float(S.iteration_product), 1.0f));
+        float t = fminf(fmaxf(value, 0.0f), 1.0f);
+        rough = S.var_rough[0] + (S.var_rough[1] - S.var_rough[0]) * t;
+        metallic = S.var_metal[0] + (S.var_metal[1] - S.var_metal[0]) * t;
+    }
+    rough = fminf(fmaxf(rough, 0.02f), 1.0f);
+    Surface s;
+    s.n = n;
+    s.diffuse = albedo * (1.0f - metallic);
+    s.f0 = mk3(spec, spec, spec) * (1.0f - metallic) + albedo * metallic;
+    s.alpha = rough * rough;
+    s.emission = emission;
+    return s;
+}
+
+// ------------------------------------------------------------------ path state
+struct PathState {
+    float3 o, d, tp, L, prev_normal;
+    float prev_pdf, prev_area_total;
+    uint32_t rng, bounce;
+    bool prev_from_bsdf;
+};
+// Result of a continuation trace (Hit of pathtrace.wgsl:60-74 plus the normal).
+struct HitInfo {
+    bool hit, exhausted;
+    float t;
+    uint32_t steps, light_index;
+    DeSampleF sample;
+    float3 n;  // geometric normal at a surface hit (tetrahedral, common.wgsl:376-387)
+};
+// Next-event request: a visibility segment and the radiance it carries if clear.
+struct ShadowReq {
+    bool active;
+    float3 o, dir;
+    float t_end;
+    float3 contrib;
+};
+enum { PATH_CONTINUE = 1, PATH_DONE = 0 };
+
+__device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uint32_t px, uint32_t py, uint32_t sample) {
+    ps.rng = rng_init(px, py, sample, S.seed);
+    camera_ray(S, px, py, ps.rng, ps.o, ps.d);
+    ps.tp = mk3(1.f, 1.f, 1.f);
+    ps.L = mk3(0.f, 0.f, 0.f);
+    ps.prev_normal = mk3(0.f, 0.f, 0.f);
+    ps.prev_pdf = 0.0f;
+    ps.prev_area_total = 0.0f;
+    ps.prev_from_bsdf = false;
+    ps.bounce = 0;
+}
+
+// One bounce of `radiance` (pathtrace.wgsl:841-1196) after its trace: hit
+// classification, emitter MIS, surface, next-event sampling (the visibility
+// test is returned in `sh` and its radiance added by the caller if clear) and
+// BSDF continuation with Russian roulette. Writes first-hit depth/aux at bounce 0.
+__device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, ShadowReq& sh, float* first_depth,
+                           float4* first_aux) {
+    sh.active = false;
+    if (!h.hit) return PATH_DONE;  // no environment light: a miss adds nothing
+    float3 p = ps.o + ps.d * h.t;
+    if (h.light_index != SF_NO_LIGHT) {
+        if (ps.bounce == 0 && first_depth) {
+            *first_depth = h.t;
+            float3 en = ld3(S.lights[h.light_index].n);
+            *first_aux = make_float4(en.x, en.y, en.z, float(h.steps));
+        }
+        ps.L = ps.L + ps.tp * area_emission(S, ps.o, ps.d, h.t, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
+                                            ps.prev_area_total);
+        return PATH_DONE;
+    }
+    float3 n = h.n;
+    if (ps.bounce == 0) {
+        if (first_depth) {
+            *first_depth = h.t;
+            *first_aux = make_float4(n.x, n.y, n.z, float(h.steps));
+        }
+        float x = fminf(fmaxf(float(h.steps) / 96.0f, 0.0f), 1.0f);
+        ps.tp = ps.tp * (1.0f - S.cavity * (x * x * (3.0f - 2.0f * x)));
+    }
+    float3 v = -ps.d;
+    Surface s = make_surface(S, n, h.sample);
+    ps.L = ps.L + ps.tp * s.emission;
+    float offset = fmaxf(h.t * S.pixel_cone * 2.0f, 1e-3f) * S.pixel_tolerance;
+    float3 p_off = p + n * offset;
+    float nv = fmaxf(dot3(s.n, v), 1e-4f);
+    float p_spec = spec_probability(s, nv);
+    float area_total = area_total_weight(S, p_off, s.n);
+    bool last = ps.bounce == S.max_bounces;
+    // direct_light (pathtrace.wgsl:471-558), area emitters
+    uint32_t selected = SF_NO_LIGHT;
+    float selected_weight = 0.0f;
+    if (area_total > 0.0f) {
+        float threshold = rnd(ps.rng) * area_total;
+        float sum = 0.0f;
+        for (uint32_t i = 0; i < S.light_count; ++i) {
+            float w = area_weight(p_off, s.n, S.lights[i]);
+            sum += w;
+            if (w > 0.0f) {
+                selected = i;
+                selected_weight = w;
+                if (threshold < sum) break;
+            }
+        }
+    }
+    if (selected != SF_NO_LIGHT) {
+        const DevLight& l = S.lights[selected];
+        float u1 = rnd(ps.rng);
+        float u2 = rnd(ps.rng);
+        float3 q = ld3(l.a) + ld3(l.b) * (u1 - 0.5f) + ld3(l.c) * (u2 - 0.5f);
+        float3 ln = ld3(l.n);
+        float3 to_q = q - p_off;
+        float dist2 = dot3(to_q, to_q);
+        if (dist2 >= 1e-8f) {
+            float dist = sqrtf(dist2);
+            float3 ldir = to_q / dist;
+            float nl = dot3(s.n, ldir);
+            float cos_l = dot3(ln, -ldir);
+            if (!(nl <= 0.0f || cos_l <= 0.0f || dot3(n, ldir) <= 0.0f)) {
+                float pl = (selected_weight / area_total) * (dist2 / fmaxf(l.area * cos_l, 1e-20f));
+                float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
+                float w = last ? 1.0f : mis_power(pl, pb);
+                float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * w / pl;
+                sh.active = true;
+                sh.o = p_off;
+                sh.dir = ldir;
+                sh.t_end = fmaxf(0.0f, dist - fmaxf(1e-5f, dist * 1e-6f));
+                sh.contrib = ps.tp * Ld;
+            }
+        }
+    }
+    if (last) return PATH_DONE;
+    float r0 = rnd(ps.rng), r1 = rnd(ps.rng), r2 = rnd(ps.rng);
+    float3 ldir;
+    if (r0 < p_spec) {
+        float3 hh = sample_ggx_h(s.n, v, s.alpha, r1, r2);
+        float3 i = -v;
+        ldir = i - hh * (2.0f * dot3(hh, i));
+    } else {
+        ldir = cosine_sample(s.n, r1, r2);
+    }
+    float nl = dot3(s.n, ldir);
+    if (nl <= 0.0f || dot3(n, ldir) <= 0.0f) return PATH_DONE;
+    float pdf = bsdf_pdf(s, v, ldir, p_spec);
+    if (pdf <= 1e-6f) return PATH_DONE;
+    ps.tp = ps.tp * (brdf_eval(s, v, ldir) * nl / pdf);
+    ps.prev_pdf = pdf;
+    ps.prev_from_bsdf = true;
+    ps.prev_normal = s.n;
+    ps.prev_area_total = area_total;
+    if (ps.bounce >= 2) {
+        float q = fminf(fmaxf(fmaxf(ps.tp.x, fmaxf(ps.tp.y, ps.tp.z)), 0.05f), 0.95f);
+        if (rnd(ps.rng) > q) return PATH_DONE;
+        ps.tp = ps.tp / q;
+    }
+    ps.o = p_off;
+    ps.d = ldir;
+    ps.bounce += 1;
+    return PATH_CONTINUE;
+}
+
+// Tetrahedral stencil (common.wgsl:376-387).
+__device__ __forceinline__ float3 tetra_offset(uint32_t i) {
+    return i == 0 ? mk3(1.f, -1.f, -1.f) : (i == 1 ? mk3(-1.f, -1.f, 1.f) : (i == 2 ? mk3(-1.f, 1.f, -1.f) : mk3(1.f, 1.f, 1.f)));
+}

@@ -1,0 +1,53 @@
+"""Shared test inputs: the reference's LCG point sets (graph_parity.rs:4-13,
+parity.rs corpus) and golden fixture loading."""
+import json
+import os
+
+import numpy as np
+
+GOLDEN = os.path.join(os.path.dirname(os.path.abspath(__file__)), "golden")
+FORMS = ["sphere", "mandelbulb", "mandelbox", "menger"]
+
+
+def lcg_points(n, extent, seed):
+    """points() of crates/syfrack-core/tests/graph_parity.rs:8-13, in binary32."""
+    s = seed & 0xFFFFFFFF
+    out = np.zeros((n, 3), np.float32)
+    e = np.float32(extent)
+    for i in range(n):
+        v = []
+        for _ in range(3):
+            s = (s * 1664525 + 1013904223) & 0xFFFFFFFF
+            v.append(np.float32(s >> 8) / np.float32(16777216.0))
+        out[i] = np.array(v, np.float32) * (np.float32(2.0) * e) - e
+    return out
+
+
+def golden(name):
+    with open(os.path.join(GOLDEN, f"de_parity_{name}.json")) as f:
+        d = json.load(f)
+    s = d["samples"]
+    return (d["extent"], np.array([r["p"] for r in s], np.float32), np.array([r["distance"] for r in s]),
+            np.array([r["traps"] for r in s]), np.array([r["iterations"] for r in s], np.uint32))
+
+
+def golden_graph(name):
+    from syfrack_gb300.graph import Graph
+
+    with open(os.path.join(GOLDEN, f"graph_{name}.json")) as f:
+        d = json.load(f)
+    return Graph.from_ron_value(_jsonish_to_ron(d["graph"]))
+
+
+def _jsonish_to_ron(g):
+    """The fixture JSON keeps RON's shape; rebuild the few tuple fields."""
+    from syfrack_gb300 import ron
+
+    g = json.loads(json.dumps(g))
+    for n in g["nodes"]:
+        k = n["kind"]
+        if isinstance(k, str):
+            n["kind"] = ron.Unit(k)
+        n["pos"] = ron.Tuple(None, n["pos"])
+    g["links"] = [{"from": ron.Tuple(None, l["from"]), "to": ron.Tuple(None, l["to"])} for l in g["links"]]
+    return g

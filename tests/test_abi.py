@@ -1,0 +1,60 @@
+"""The C-ABI library builds, loads and exports every symbol the headers
+declare; host-side argument checks run without a GPU (CPU)."""
+import ctypes as C
+import os
+import re
+import subprocess
+
+import pytest
+
+ROOT = os.path.dirname(os.path.dirname(os.path.abspath(__file__)))
+
+
+def declared_symbols():
+    names = set()
+    inc = os.path.join(ROOT, "include")
+    for f in os.listdir(inc):
+        if f.endswith(".h"):
+            text = open(os.path.join(inc, f)).read()
+            names |= set(re.findall(r"^\s*(?:const\s+char\s*\*|sf_status|uint32_t|void)\s+(sf_\w+)\s*\(", text, re.M))
+    return sorted(names)
+
+
+@pytest.fixture(scope="module")
+def lib():
+    from syfrack_gb300 import _lib, build
+
+    build.build()
+    return _lib.load()
+
+
+def test_every_declared_symbol_is_exported(lib):
+    names = declared_symbols()
+    assert len(names) >= 30
+    path = os.path.join(ROOT, "syfrack_gb300", "libsyfrack_gpu.so")
+    out = subprocess.run(["nm", "-D", "--defined-only", path], capture_output=True, text=True).stdout
+    exported = set(re.findall(r" T (sf_\w+)$", out, re.M))
+    missing = [n for n in names if n not in exported]
+    assert not missing, missing
+    for n in names:
+        assert hasattr(lib, n)
+
+
+def test_python_binding_covers_the_abi():
+    from syfrack_gb300._lib import SIGNATURES
+
+    assert sorted(SIGNATURES) == declared_symbols()
+
+
+def test_status_strings(lib):
+    assert lib.sf_status_string(0) == b"SF_OK"
+    assert lib.sf_status_string(9) == b"SF_ERR_CHECKPOINT"
+    assert lib.sf_status_string(99) == b"SF_ERR_UNKNOWN"
+    assert lib.sf_abi_version() >> 16 == 1
+
+
+def test_null_arguments_are_rejected(lib):
+    assert lib.sf_context_create(0, 0, None) == 1  # SF_ERR_INVALID
+    assert lib.sf_graph_compile(None, None, None) == 1
+    assert lib.sf_session_dispatch(None, __import__("syfrack_gb300").abi.sf_tile(0, 0, 1, 1, 0), 1) == 1
+    assert lib.sf_last_error() != b""

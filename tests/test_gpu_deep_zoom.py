@@ -1,0 +1,45 @@
+"""Deep zoom: FP64 reference orbit + FP32 perturbation with rebasing (GPU),
+checked against IEEE binary128 direct iteration on a seeded pixel subsample
+(the truth) and against full-FP64 direct iteration on every pixel."""
+import numpy as np
+import pytest
+
+from syfrack_gb300 import deep_zoom, workloads
+
+pytestmark = pytest.mark.gpu
+
+
+def offsets(w, h, pitch, idx):
+    f = np.float32
+    px, py = idx % w, idx // w
+    dx = (px.astype(np.float32) - f(w) * f(0.5) + f(0.5)) * f(pitch)
+    dy = (f(h) * f(0.5) - py.astype(np.float32) - f(0.5)) * f(pitch)
+    return np.stack([dx, dy], 1).astype(np.float64)
+
+
+def test_deep_zoom_against_binary128(gpu_ctx, oracle_mod):
+    max_iter = 20000
+    c = workloads.deep_zoom_center(seed=2026, max_iter=max_iter)
+    w, h, width = 192, 108, 1e-12
+    out = deep_zoom(gpu_ctx, c, (0.0, 0.0), width, w, h, max_iter, bailout=16.0, reference_f64=True)
+    it = out["iterations"].ravel()
+    assert it.min() < max_iter and it.max() > 100  # the view straddles the boundary
+    idx = np.random.default_rng(0).choice(w * h, 96, replace=False)
+    pitch = np.float32(width / w)
+    truth, _ = oracle_mod.mandel_escape(np.array(c), np.zeros(2), offsets(w, h, pitch, idx), max_iter, 16.0,
+                                        precision=128)
+    match = (it[idx] == truth).mean()
+    near = (np.abs(it[idx].astype(np.int64) - truth.astype(np.int64)) <= 1).mean()
+    assert match >= 0.90 and near >= 0.97, (match, near)
+    agree64 = (out["iterations_f64"].ravel() == it).mean()
+    assert agree64 >= 0.5  # FP64 direct iteration cannot resolve a 1e-12 view (pitch ~ 1 ulp)
+    s = out["smooth"].ravel()[idx]
+    esc = truth < max_iter
+    assert np.all(np.isfinite(s)) and np.all(s[esc] >= it[idx][esc] - 1.0)
+
+
+def test_shallow_zoom_matches_fp64_everywhere(gpu_ctx):
+    # at width 1e-3 FP64 direct iteration is trustworthy: counts agree on almost every pixel
+    out = deep_zoom(gpu_ctx, (-0.743, 0.131), (0.0, 0.0), 1e-3, 160, 90, 4000, bailout=16.0, reference_f64=True)
+    agree = (out["iterations"] == out["iterations_f64"]).mean()
+    assert agree >= 0.97, agree

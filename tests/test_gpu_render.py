@@ -1,0 +1,149 @@
+"""Path-traced film on the GPU: wavefront stages against the per-pixel
+megakernel, both against the oracle; session stepping, checkpoints (GPU).
+
+Reference conventions: accum holds sample sums added in ascending sample order
+(pathtrace.wgsl:1243-1245); depth/aux from sample 0; the wavefront result equals
+the tiled megakernel (gpu_export.rs:110-163 uses 1e-4); save/resume is
+bit-for-bit (gpu_render.rs:1120); a corrupt state is refused (:1180)."""
+import os
+
+import numpy as np
+import pytest
+
+from syfrack_gb300 import RenderSession, SyfrackError, workloads
+from syfrack_gb300.graph import Graph
+from syfrack_gb300.scene import AreaLight, Camera, Material, RenderConfig, Scene
+
+pytestmark = pytest.mark.gpu
+
+
+def small_cfg(integrator, w=96, h=54, spp=8, spd=4, tile=64):
+    return RenderConfig(width=w, height=h, samples_per_pixel=spp, max_bounces=4, max_steps=512,
+                        pixel_tolerance=1.0, tile_size=tile, samples_per_dispatch=spd, integrator=integrator)
+
+
+def render(renderer, scene, cfg):
+    s = RenderSession(renderer, scene, cfg)
+    while not s.step(0):
+        pass
+    out = s.readback()
+    assert s.sync() == 0
+    s.close()
+    return out
+
+
+def test_wavefront_equals_megakernel(renderer):
+    scene = workloads.mandelbox_scene()
+    a = render(renderer, scene, small_cfg("wavefront"))
+    b = render(renderer, scene, small_cfg("megakernel"))
+    assert a.accum[..., 3].min() == 8 and b.accum[..., 3].min() == 8
+    diff = np.abs(a.accum[..., :3] - b.accum[..., :3])
+    assert diff.max() <= 1e-4 * max(1.0, float(np.abs(b.accum[..., :3]).max()))
+    np.testing.assert_array_equal(a.depth >= 0, b.depth >= 0)
+    np.testing.assert_allclose(a.depth, b.depth, rtol=1e-6, atol=1e-6)
+    np.testing.assert_allclose(a.normals, b.normals, atol=1e-5)
+    assert a.color[..., :3].mean() > 0.01  # the light reaches the form
+
+
+def test_film_against_oracle(renderer, oracle_mod):
+    scene = workloads.mandelbox_scene()
+    cfg = small_cfg("wavefront", spp=16, spd=8)
+    out = render(renderer, scene, cfg)
+    rng = np.random.default_rng(1)
+    pix = np.stack([rng.integers(0, cfg.width, 96), rng.integers(0, cfg.height, 96)], 1).astype(np.uint32)
+    og = oracle_mod.OracleGraph(scene.graph)
+    for prec, tol in ((32, 2e-2), (64, 2e-2)):
+        ref = og.render(scene.desc(cfg.width, cfg.height), cfg.desc(), pix, 0, cfg.samples_per_pixel, precision=prec)
+        mine = out.accum[pix[:, 1], pix[:, 0], :3] / cfg.samples_per_pixel
+        mean_ref = ref["accum"] / cfg.samples_per_pixel
+        rmse = float(np.sqrt(np.mean((mine - mean_ref) ** 2)))
+        assert rmse <= tol, (prec, rmse)
+        hit = ref["depth"] >= 0
+        np.testing.assert_array_equal(out.depth[pix[:, 1], pix[:, 0]] >= 0, hit)
+        np.testing.assert_allclose(out.depth[pix[:, 1], pix[:, 0]][hit], ref["depth"][hit], rtol=1e-3)
+
+
+def test_step_equals_one_shot(renderer):
+    scene = workloads.mandelbox_scene()
+    cfg = small_cfg("wavefront", spp=8, spd=8, tile=128)
+    a = render(renderer, scene, cfg)
+    cfg2 = small_cfg("wavefront", spp=8, spd=2, tile=32)
+    b = render(renderer, scene, cfg2)
+    np.testing.assert_array_equal(a.accum, b.accum)
+    np.testing.assert_array_equal(a.depth, b.depth)
+
+
+def test_save_resume_bit_for_bit(renderer, tmp_path):
+    scene = workloads.mandelbox_scene()
+    cfg = small_cfg("wavefront", spp=8, spd=4)
+    full = render(renderer, scene, cfg)
+    s = RenderSession(renderer, scene, cfg)
+    s.step(1)  # stops after the first dispatch that exceeds 1 ms
+    d = str(tmp_path / "ck")
+    s.save(d)
+    prog = s.progress()
+    s.close()
+    r = RenderSession.resume(renderer, scene, cfg, d)
+    assert r.progress()["pixel_samples_done"] == prog["pixel_samples_done"]
+    while not r.step(0):
+        pass
+    out = r.readback()
+    np.testing.assert_array_equal(out.accum, full.accum)
+    np.testing.assert_array_equal(out.depth, full.depth)
+    r.close()
+
+
+def test_corrupt_and_foreign_checkpoints_are_refused(renderer, tmp_path):
+    scene = workloads.mandelbox_scene()
+    cfg = small_cfg("wavefront", spp=4, spd=4)
+    s = RenderSession(renderer, scene, cfg)
+    s.step(0)
+    d = str(tmp_path / "ck")
+    s.save(d)
+    s.close()
+    film = os.path.join(d, "film.bin")
+    data = bytearray(open(film, "rb").read())
+    data[100] ^= 0xFF
+    open(film, "wb").write(bytes(data))
+    with pytest.raises(SyfrackError) as e:
+        RenderSession.resume(renderer, scene, cfg, d)
+    assert e.value.status == 9
+    s = RenderSession(renderer, scene, cfg)
+    s.step(0)
+    s.save(d)
+    s.close()
+    other = Scene(graph=Graph.bundled("menger"), camera=scene.camera, lights=scene.lights)
+    with pytest.raises(SyfrackError) as e:
+        RenderSession.resume(renderer, other, cfg, d)
+    assert e.value.status == 9
+
+
+def test_sphere_centre_depth(renderer):
+    # gpu_render.rs:479: centre-pixel depth = camera distance - radius
+    g = Graph.bundled("sphere", ground=-50.0)
+    scene = Scene(graph=g, camera=Camera.look_at((0.0, 0.0, -4.0), (0.0, 0.0, 0.0), 40.0),
+                  lights=[AreaLight(position=(0, 3, -2))])
+    cfg = RenderConfig(width=65, height=65, samples_per_pixel=1, max_bounces=1, integrator="wavefront")
+    out = render(renderer, scene, cfg)
+    assert abs(out.depth[32, 32] - 3.0) < 2e-2
+    n = out.normals[32, 32, :3]
+    assert n[2] < -0.99
+
+
+def test_config_validation(renderer):
+    scene = workloads.mandelbox_scene()
+    with pytest.raises(SyfrackError):
+        RenderSession(renderer, scene, RenderConfig(width=8, height=8, samples_per_pixel=1, max_bounces=33))
+    with pytest.raises(SyfrackError):
+        RenderSession(renderer, scene, RenderConfig(width=8, height=8, samples_per_pixel=1, pixel_tolerance=2.0))
+
+
+def test_budget_admission(gpu_ctx):
+    from syfrack_gb300 import GpuContext, Renderer
+
+    ctx = GpuContext(hbm_budget=8 << 20)
+    r = Renderer(ctx)
+    with pytest.raises(SyfrackError) as e:
+        RenderSession(r, workloads.mandelbox_scene(), workloads.mandelbox_pathtrace_config())
+    assert e.value.status == 7
+    ctx.close()
