@@ -161,7 +161,8 @@ def run_ours(args):
     renderer = Renderer(ctx)
     scene = workloads.mandelbox_scene()
     spp_total = SPP_PER_STEP * (args.warmup + args.steps)
-    cfg = workloads.mandelbox_pathtrace_config(spp=spp_total, samples_per_dispatch=SPP_PER_STEP)
+    cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=spp_total,
+                                               samples_per_dispatch=SPP_PER_STEP)
     sess = RenderSession(renderer, scene, cfg)
     if args.blocks_per_sm:
         sess.set_launch(args.blocks_per_sm, args.threads)
@@ -217,15 +218,17 @@ def run_ours(args):
     sess.close()
 
     # end to end through the public API: a full 64-spp render from host descriptions
-    e2e_cfg = workloads.mandelbox_pathtrace_config(spp=SPP_PER_STEP * args.steps,
-                                                   samples_per_dispatch=SPP_PER_STEP)
+    e2e_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height,
+                                                   spp=SPP_PER_STEP * args.steps, samples_per_dispatch=SPP_PER_STEP)
     ctx.reset_stats()
     if dist:
         dist.barrier()
-    t0 = time.perf_counter()
-    out = renderer.render(scene, e2e_cfg)
-    e2e_s = time.perf_counter() - t0
-    e2e_segs = ctx.stats()["segments"]
+    e2e_s, e2e_segs = 1.0, 0
+    if not args.no_e2e:
+        t0 = time.perf_counter()
+        renderer.render(scene, e2e_cfg)
+        e2e_s = time.perf_counter() - t0
+        e2e_segs = ctx.stats()["segments"]
     if dist:
         t = torch.tensor([e2e_s, float(e2e_segs)], dtype=torch.float64, device="cuda")
         mx = t.clone()
@@ -247,7 +250,8 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Mandelbox scene; no dataset)",
-            "config": {"workload": WORKLOAD, "width": cfg.width, "height": cfg.height, "spp_per_step": SPP_PER_STEP,
+            "config": {"workload": WORKLOAD if (cfg.width, cfg.height) == (1280, 720) else f"profiling case {cfg.width}x{cfg.height}",
+                       "width": cfg.width, "height": cfg.height, "spp_per_step": SPP_PER_STEP,
                        "paths_per_step": cfg.width * cfg.height * SPP_PER_STEP, "max_bounces": cfg.max_bounces,
                        "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
                        "l2": "inputs larger than L2 (path state 1.4 GB per step)",
@@ -284,6 +288,10 @@ def main():
     ap.add_argument("--blocks-per-sm", type=int, default=0)
     ap.add_argument("--threads", type=int, default=256)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    # smaller frames are for profiler captures only; the measured workload is 1280x720
+    ap.add_argument("--width", type=int, default=1280)
+    ap.add_argument("--height", type=int, default=720)
+    ap.add_argument("--no-e2e", action="store_true")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)

@@ -454,11 +454,14 @@ struct sf_context {
     uint64_t launches = 0, trace_launches = 0;
     unsigned long long* d_stats = nullptr;  // SF_STAT_COUNT counters
     uint32_t* d_work = nullptr;             // scratch work counters
+    // Graphs and sessions hold a reference, so handles may be destroyed in any order.
+    int refs = 1;
     std::mutex mu;
 };
 
 struct sf_graph {
     sf_context* ctx = nullptr;
+    int refs = 1;  // sessions hold a reference
     HostGraph host;
     DeProgram prog;
     DeProgram* d_prog = nullptr;
@@ -486,6 +489,25 @@ void ctx_free(sf_context* c, void* p, size_t bytes) {
     if (!p) return;
     cudaFree(p);
     c->used -= std::min<uint64_t>(c->used, bytes);
+}
+
+void ctx_retain(sf_context* c) {
+    std::lock_guard<std::mutex> lk(c->mu);
+    c->refs++;
+}
+void collect_timing(sf_context* c);
+void ctx_release(sf_context* c) {
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        if (--c->refs > 0) return;
+    }
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    collect_timing(c);
+    for (auto e : c->spare) cudaEventDestroy(e);
+    ctx_free(c, c->d_stats, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t));
+    cudaStreamDestroy(c->stream);
+    delete c;
 }
 
 cudaEvent_t get_event(sf_context* c) {
@@ -724,13 +746,7 @@ extern "C" sf_status sf_context_create(int device, uint64_t budget, sf_context**
 }
 extern "C" sf_status sf_context_destroy(sf_context* c) {
     if (!c) return SF_OK;
-    cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    collect_timing(c);
-    for (auto e : c->spare) cudaEventDestroy(e);
-    ctx_free(c, c->d_stats, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t));
-    cudaStreamDestroy(c->stream);
-    delete c;
+    ctx_release(c);
     return SF_OK;
 }
 extern "C" sf_status sf_context_stream(sf_context* c, void** s) {
@@ -805,6 +821,7 @@ extern "C" sf_status sf_graph_compile(sf_context* c, const sf_graph_desc* d, sf_
         delete g;
         return cuda_fail(e, "graph upload");
     }
+    ctx_retain(c);
     *out = g;
     return SF_OK;
 }
@@ -829,12 +846,24 @@ extern "C" sf_status sf_graph_update(sf_graph* g, const sf_graph_desc* d) {
     g->info = info;
     return SF_OK;
 }
+namespace {
+void graph_retain(sf_graph* g) {
+    std::lock_guard<std::mutex> lk(g->ctx->mu);
+    g->refs++;
+}
+}  // namespace
 extern "C" sf_status sf_graph_destroy(sf_graph* g) {
     if (!g) return SF_OK;
-    cudaSetDevice(g->ctx->device);
-    cudaStreamSynchronize(g->ctx->stream);
-    ctx_free(g->ctx, g->d_prog, sizeof(DeProgram));
+    sf_context* c = g->ctx;
+    {
+        std::lock_guard<std::mutex> lk(c->mu);
+        if (--g->refs > 0) return SF_OK;
+    }
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    ctx_free(c, g->d_prog, sizeof(DeProgram));
     delete g;
+    ctx_release(c);
     return SF_OK;
 }
 
@@ -1085,6 +1114,8 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
         delete s;
         return st;
     }
+    ctx_retain(c);
+    graph_retain(g);
     *out = s;
     return SF_OK;
 }
@@ -1239,10 +1270,14 @@ extern "C" sf_status sf_session_stats(sf_session* s, sf_stats* out) {
 
 extern "C" sf_status sf_session_destroy(sf_session* s) {
     if (!s) return SF_OK;
-    cudaSetDevice(s->ctx->device);
-    cudaStreamSynchronize(s->ctx->stream);
-    ctx_free(s->ctx, s->mem, s->mem_bytes);
+    sf_context* c = s->ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    ctx_free(c, s->mem, s->mem_bytes);
+    sf_graph* g = s->graph;
     delete s;
+    sf_graph_destroy(g);  // drops the session's reference
+    ctx_release(c);
     return SF_OK;
 }
 
