@@ -164,8 +164,7 @@ def run_ours(args):
     cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=spp_total,
                                                samples_per_dispatch=SPP_PER_STEP)
     sess = RenderSession(renderer, scene, cfg)
-    if args.blocks_per_sm:
-        sess.set_launch(args.blocks_per_sm, args.threads)
+    sess.set_launch(args.min_blocks, 256, args.quantum)
     tile = (0, 0, cfg.width, cfg.height)
     peak = C.c_double()
     check(ctx.lib.sf_device_fp32_peak(ctx.h, C.byref(peak)))
@@ -285,8 +284,8 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--blocks-per-sm", type=int, default=0)
-    ap.add_argument("--threads", type=int, default=256)
+    ap.add_argument("--min-blocks", type=int, default=2)
+    ap.add_argument("--quantum", type=int, default=64)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     # smaller frames are for profiler captures only; the measured workload is 1280x720
     ap.add_argument("--width", type=int, default=1280)

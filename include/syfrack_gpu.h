@@ -289,8 +289,10 @@ sf_status sf_session_stats(sf_session* s, sf_stats* out);
 sf_status sf_session_save(sf_session* s, const char* dir);
 sf_status sf_session_resume(sf_context* ctx, sf_graph* graph, const char* dir, sf_session** out);
 sf_status sf_session_destroy(sf_session* s);
-/* Autotuning knobs of the wavefront trace kernel (blocks per SM, threads per block). */
-sf_status sf_session_set_launch(sf_session* s, uint32_t blocks_per_sm, uint32_t threads);
+/* Autotuning knobs of the wavefront trace kernel: resident blocks per SM (2..4,
+ * selecting the register budget), threads per block (256) and the march step
+ * quantum after which an open segment is saved and re-queued (0 = unbounded). */
+sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t threads, uint32_t quantum);
 
 /* ------------------------------------------------------------------ escape time
  * PlanarFractal (crates/syfrack-core/src/scene/planar.rs:20-39); family:

@@ -102,7 +102,7 @@ SIGNATURES = {
     "sf_session_save": [vp, C.c_char_p],
     "sf_session_resume": [vp, vp, C.c_char_p, P(vp)],
     "sf_session_destroy": [vp],
-    "sf_session_set_launch": [vp, u32, u32],
+    "sf_session_set_launch": [vp, u32, u32, u32],
     "sf_planar_probe": [vp, P(sf_planar_desc), fp, C.c_size_t, fp, fp, up],
     "sf_escape2d": [vp, P(sf_planar_desc), P(sf_canvas), abi.sf_tile, u32, fp, fp, up],
     "sf_deep_zoom": [vp, P(sf_deep_zoom_desc), up, fp, C.c_int, up, fp, P(u64)],

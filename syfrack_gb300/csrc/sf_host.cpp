@@ -978,13 +978,15 @@ struct sf_session {
     PathSoA soa{};
     uint32_t capacity = 0;
     uint32_t* lists = nullptr;     // 2 x {active, cont, shadow} x capacity
+    uint32_t* resume = nullptr;    // 2 x 2*capacity segments cut at a step quantum
+    uint32_t* qcounts = nullptr;   // per round and launch: {work counter, resumed count}
     uint32_t* counts = nullptr;    // per round: {active, cont, shadow, work}
     uint32_t* status = nullptr;
     void* mem = nullptr;
     size_t mem_bytes = 0;
     std::vector<sf_tile> tiles;
     uint32_t tile_size = 0, dispatches = 0;
-    uint32_t blocks_per_sm = 8, threads = 256;
+    uint32_t min_blocks = 2, threads = 256, quantum = 64;
     uint32_t status_host = 0;
 };
 
@@ -1038,12 +1040,15 @@ sf_status session_alloc(sf_session* s) {
     size_t o_scene = take(sizeof(DevScene));
     size_t o_acc = take(px * 16), o_depth = take(px * 4), o_aux = take(px * 16);
     size_t o_Ls = take(N * 16);
-    size_t o_soa = 0, o_lists = 0;
+    size_t o_soa = 0, o_lists = 0, o_march = 0, o_resume = 0;
     if (wf) {
         o_soa = take(N * 16 * 11 + N * 16);  // 11 float4/uint4 planes + vis (padded)
         o_lists = take(N * 4 * 6);
+        o_march = take(2 * N * 16 * 4);      // m0..m3 for continuation and shadow rows
+        o_resume = take(2 * 2 * N * 4);
     }
     size_t o_counts = take(size_t(R + 1) * 4 * 4);
+    size_t o_qcounts = take(size_t(R) * 64 * 2 * 4);
     size_t o_status = take(16);
     s->mem_bytes = off;
     sf_status st = ctx_alloc(c, off, &s->mem);
@@ -1073,8 +1078,15 @@ sf_status session_alloc(sf_session* s) {
         s->soa.hit_n = p; p += N;
         s->soa.vis = reinterpret_cast<uint32_t*>(p);
         s->lists = reinterpret_cast<uint32_t*>(base + o_lists);
+        float4* m = reinterpret_cast<float4*>(base + o_march);
+        s->soa.m0 = m;
+        s->soa.m1 = m + 2 * N;
+        s->soa.m2 = m + 4 * N;
+        s->soa.m3 = m + 6 * N;
+        s->resume = reinterpret_cast<uint32_t*>(base + o_resume);
     }
     s->counts = reinterpret_cast<uint32_t*>(base + o_counts);
+    s->qcounts = reinterpret_cast<uint32_t*>(base + o_qcounts);
     s->status = reinterpret_cast<uint32_t*>(base + o_status);
     DevScene S;
     scene_dev(s->scene, cfg, s->graph->info, S);
@@ -1120,12 +1132,15 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
     return SF_OK;
 }
 
-extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t blocks_per_sm, uint32_t threads) {
+extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t threads,
+                                           uint32_t quantum) {
     if (!s) return fail(SF_ERR_INVALID, "null session");
-    if (threads % 32 || threads == 0 || threads > 1024 || blocks_per_sm == 0 || blocks_per_sm > 64)
-        return fail(SF_ERR_INVALID, "invalid launch shape");
-    s->blocks_per_sm = blocks_per_sm;
+    if (threads != 256 || min_blocks_per_sm < 2 || min_blocks_per_sm > 4)
+        return fail(SF_ERR_INVALID, "trace launch: 256 threads and 2..4 resident blocks per SM");
+    if (quantum != 0 && quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
+    s->min_blocks = min_blocks_per_sm;
     s->threads = threads;
+    s->quantum = quantum;
     return SF_OK;
 }
 
@@ -1152,11 +1167,15 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
     }
     const uint32_t R = rounds_of(s->cfg);
     const size_t N = s->capacity;
+    // launches per round: the first, then one per step quantum a segment may still need
+    const uint32_t Q = s->quantum ? std::min<uint32_t>((s->cfg.max_steps + s->quantum - 1) / s->quantum + 1, 64) : 1;
     CU(cudaMemsetAsync(s->counts, 0, size_t(R + 1) * 16, st));
+    CU(cudaMemsetAsync(s->qcounts, 0, size_t(R) * 64 * 2 * 4, st));
     {
         LaunchTimer t(c, false);
         CU(sf_launch_generate(s->d_scene, s->soa, g, s->counts, st));
     }
+    const int blocks = int(s->min_blocks) * c->sm_count;
     for (uint32_t r = 0; r < R; ++r) {
         uint32_t cur = r & 1, nxt = cur ^ 1;
         RoundQueues q;
@@ -1169,10 +1188,19 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
         q.next_shadow = s->lists + (nxt * 3 + 2) * N;
         q.next_counts = s->counts + 4 * (r + 1);
         q.work_counter = s->counts + 4 * r + 3;
-        {
+        for (uint32_t j = 0; j < Q; ++j) {
+            TraceLaunch tl;
+            tl.q = q;
+            uint32_t* qc = s->qcounts + (size_t(r) * 64 + j) * 2;
+            tl.work_counter = qc;
+            tl.resume = j == 0 ? nullptr : s->resume + size_t((j - 1) & 1) * 2 * N;
+            tl.resume_count = j == 0 ? nullptr : qc - 2 + 1;  // previous launch's resumed count
+            tl.next_resume = s->resume + size_t(j & 1) * 2 * N;
+            tl.next_resume_count = qc + 1;
+            tl.quantum = j + 1 == Q ? 0u : s->quantum;  // the last launch runs segments to completion
             LaunchTimer t(c, true);
-            CU(sf_launch_trace(s->graph->d_prog, s->d_scene, s->soa, q, c->d_stats,
-                               int(s->blocks_per_sm) * c->sm_count, int(s->threads), st));
+            CU(sf_launch_trace(s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks, int(s->threads),
+                               int(s->min_blocks), st));
         }
         LaunchTimer t(c, false);
         CU(sf_launch_shade(s->d_scene, s->soa, q, g, s->film, s->status, r + 1 == R ? 1 : 0, st));
@@ -1630,7 +1658,7 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     }
     if (e == cudaSuccess) {
         LaunchTimer t(c, true);
-        e = sf_launch_perturb(of, olen, d->width, d->height, float(pitch), 1.0f, d->max_iter, d->bailout, di, ds,
+        e = sf_launch_perturb(od, of, olen, d->width, d->height, float(pitch), 1.0f, d->max_iter, d->bailout, di, ds,
                               c->d_stats, c->stream);
     }
     if (e == cudaSuccess && reference_f64) {

@@ -85,48 +85,69 @@ __global__ void __launch_bounds__(256) k_de_probe(const DeProgram* __restrict__ 
 // continuation rays run the four normal taps through the same DE call.
 enum { LANE_IDLE = 0, LANE_CONT = 1, LANE_SHADOW = 2, LANE_NORMAL = 3, LANE_DONE = 4 };
 
-__global__ void __launch_bounds__(256) k_trace_path(const DeProgram* __restrict__ prog_g,
-                                                    const DevScene* __restrict__ scene_g, PathSoA soa, RoundQueues q,
-                                                    unsigned long long* stats) {
+// Segments are marched in quanta of `tl.quantum` steps: a segment still open at
+// the end of its quantum saves its march state (t, omega, previous radius, step,
+// candidate) and is re-queued for the next launch of the round. The tail of a
+// launch is thus bounded by one quantum instead of the longest ray.
+template <int MIN_BLOCKS>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace_path(const DeProgram* __restrict__ prog_g,
+                                                                const DevScene* __restrict__ scene_g, PathSoA soa,
+                                                                TraceLaunch tl, unsigned long long* stats) {
     __shared__ DeProgram P;
     __shared__ DevScene S;
     stage_program(P, prog_g);
     stage_pod(S, scene_g);
     __syncthreads();
-    const uint32_t n_cont = q.counts[1];
-    const uint32_t total = n_cont + q.counts[2];
+    const bool first = tl.resume == nullptr;
+    const uint32_t n_cont = first ? tl.q.counts[1] : 0u;
+    const uint32_t total = first ? n_cont + tl.q.counts[2] : *tl.resume_count;
+    const uint32_t quantum = tl.quantum ? tl.quantum : 0xffffffffu;
     const float accept = S.pixel_cone * S.pixel_tolerance;
     const float safety = S.step_scale;
     const uint32_t max_steps = S.max_steps;
+    const uint32_t cap = soa.capacity;
 
-    uint32_t state = LANE_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0;
+    uint32_t state = LANE_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
     March m;
     float3 hp = mk3(0.f, 0.f, 0.f), grad = mk3(0.f, 0.f, 0.f);
     float hstep = 0.f;
     unsigned long long n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0;
 
     while (true) {
-        // refill idle lanes
-        uint32_t w = warp_fetch(q.work_counter, state == LANE_IDLE);
+        uint32_t w = warp_fetch(tl.work_counter, state == LANE_IDLE);
         if (state == LANE_IDLE) {
             if (w >= total) {
                 state = LANE_DONE;
-            } else if (w < n_cont) {
-                path = q.cont ? q.cont[w] : w;
-                float4 o = soa.o[path], d = soa.d[path];
-                float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
-                float t_end = nearest_emitter(S, ro, rd, S.extent, li);
-                march_begin(m, ro, rd, t_end);
-                state = LANE_CONT;
-                n_seg++;
             } else {
-                path = q.shadow[w - n_cont];
-                float4 o = soa.sh_o[path], d = soa.sh_d[path];
+                bool shadow, resumed = !first;
+                if (first) {
+                    shadow = w >= n_cont;
+                    path = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
+                } else {
+                    uint32_t item = tl.resume[w];
+                    path = item & 0x7fffffffu;
+                    shadow = (item >> 31) != 0;
+                }
+                float4 o = shadow ? soa.sh_o[path] : soa.o[path];
+                float4 d = shadow ? soa.sh_d[path] : soa.d[path];
                 float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
-                float t_end = nearest_emitter(S, ro, rd, o.w, li);
-                march_begin(m, ro, rd, t_end);
-                state = LANE_SHADOW;
-                n_shseg++;
+                if (!resumed) {
+                    float t_end = nearest_emitter(S, ro, rd, shadow ? o.w : S.extent, li);
+                    march_begin(m, ro, rd, t_end);
+                    if (shadow) n_shseg++;
+                    else n_seg++;
+                } else {
+                    uint32_t row = path + (shadow ? cap : 0u);
+                    float4 a = soa.m0[row], b = soa.m1[row], c = soa.m2[row], e = soa.m3[row];
+                    m.ro = ro; m.rd = rd;
+                    m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
+                    m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
+                    m.cand.d = c.x; m.cand.t0 = c.y; m.cand.t1 = c.z; m.cand.t2 = c.w;
+                    m.cand.t3 = e.x; m.cand.iter = __float_as_uint(e.y); m.cand.material = __float_as_uint(e.z);
+                    li = __float_as_uint(e.w);
+                }
+                state = shadow ? LANE_SHADOW : LANE_CONT;
+                budget = quantum;
             }
         }
         if (__all_sync(FULL_MASK, state == LANE_DONE)) break;
@@ -157,7 +178,18 @@ __global__ void __launch_bounds__(256) k_trace_path(const DeProgram* __restrict_
                     if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept), at_budget = r != MARCH_CONTINUE;
                     if (r == MARCH_HIT && !at_budget) m.cand = s, m.cand_t = m.t;  // hit at this step
                 }
-                if (r != MARCH_CONTINUE) {
+                if (r == MARCH_CONTINUE && --budget == 0) {
+                    // quantum spent: save the march and hand the segment to the next launch
+                    bool shadow = state == LANE_SHADOW;
+                    uint32_t row = path + (shadow ? cap : 0u);
+                    soa.m0[row] = make_float4(m.t, m.omega, m.prev_radius, m.step_len);
+                    soa.m1[row] = make_float4(m.t_end, m.cand_t, m.cand_err, __uint_as_float(m.i));
+                    soa.m2[row] = make_float4(m.cand.d, m.cand.t0, m.cand.t1, m.cand.t2);
+                    soa.m3[row] = make_float4(m.cand.t3, __uint_as_float(m.cand.iter), __uint_as_float(m.cand.material),
+                                              __uint_as_float(li));
+                    warp_append(tl.next_resume_count, tl.next_resume, true, path | (shadow ? 0x80000000u : 0u));
+                    state = LANE_IDLE;
+                } else if (r != MARCH_CONTINUE) {
                     if (state == LANE_SHADOW) {
                         soa.vis[path] = (r == MARCH_MISS && li == SF_NO_LIGHT) ? 1u : 0u;
                         state = LANE_IDLE;
@@ -756,7 +788,8 @@ __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bail
 // FP32 perturbation with rebasing: z_n = Z_m + d, d' = (2 Z_m + d) d + dc;
 // when |z| < |d| or the reference ends, restart from Z_0 with d = z.
 // count = first n with |z_n| > bailout (max_iter if none), as the direct iteration.
-__global__ void __launch_bounds__(256) k_perturb(const float2* __restrict__ orbit, const uint32_t* __restrict__ orbit_len,
+__global__ void __launch_bounds__(256) k_perturb(const double2* __restrict__ orbit_d, const float2* __restrict__ orbit,
+                                                 const uint32_t* __restrict__ orbit_len,
                                                  uint32_t width, uint32_t height, float pitch, uint32_t max_iter,
                                                  float bailout, uint32_t* iters, float* smooth,
                                                  unsigned long long* stats) {
@@ -785,8 +818,11 @@ __global__ void __launch_bounds__(256) k_perturb(const float2* __restrict__ orbi
             mag = zx * zx + zy * zy;
             if (mag > b2) break;
             if (mag < dx * dx + dy * dy || m + 1 >= M) {
-                dx = zx;
-                dy = zy;
+                // z = Z_m + d formed in FP64: |Z_m| >> |z| here, and an FP32 sum would
+                // cancel away the pixel's offset
+                double2 Zd = orbit_d[m];
+                dx = (float)(Zd.x + (double)dx);
+                dy = (float)(Zd.y + (double)dy);
                 m = 0;
                 ++rebases;
             }
@@ -865,11 +901,15 @@ cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom 
     k_generate<<<(g.paths + 255) / 256, 256, 0, st>>>(scene, soa, g, counts);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, RoundQueues q,
-                            unsigned long long* stats, int blocks, int threads, cudaStream_t st) {
-    if (blocks <= 0) blocks = sf_device_sm_count() * 8;
+cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
+                            unsigned long long* stats, int blocks, int threads, int min_blocks, cudaStream_t st) {
     if (threads <= 0) threads = 256;
-    k_trace_path<<<blocks, threads, 0, st>>>(prog, scene, soa, q, stats);
+    if (blocks <= 0) blocks = sf_device_sm_count() * (min_blocks > 0 ? min_blocks : 2);
+    switch (min_blocks) {
+    case 3: k_trace_path<3><<<blocks, threads, 0, st>>>(prog, scene, soa, tl, stats); break;
+    case 4: k_trace_path<4><<<blocks, threads, 0, st>>>(prog, scene, soa, tl, stats); break;
+    default: k_trace_path<2><<<blocks, threads, 0, st>>>(prog, scene, soa, tl, stats); break;
+    }
     return cudaGetLastError();
 }
 cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
@@ -908,11 +948,11 @@ cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double 
     k_ref_orbit<<<1, 32, 0, st>>>(cx, cy, max_iter, bailout, orbit_d, orbit_f, orbit_len);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_perturb(const float2* orbit_f, const uint32_t* orbit_len, uint32_t width, uint32_t height,
-                              float pitch, float, uint32_t max_iter, float bailout, uint32_t* iters, float* smooth,
-                              unsigned long long* stats, cudaStream_t st) {
+cudaError_t sf_launch_perturb(const double2* orbit_d, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,
+                              uint32_t height, float pitch, float, uint32_t max_iter, float bailout, uint32_t* iters,
+                              float* smooth, unsigned long long* stats, cudaStream_t st) {
     size_t n = (size_t)width * height;
-    k_perturb<<<grid_for(n, 256, 8), 256, 0, st>>>(orbit_f, orbit_len, width, height, pitch, max_iter, bailout, iters,
+    k_perturb<<<grid_for(n, 256, 8), 256, 0, st>>>(orbit_d, orbit_f, orbit_len, width, height, pitch, max_iter, bailout, iters,
                                                     smooth, stats);
     return cudaGetLastError();
 }

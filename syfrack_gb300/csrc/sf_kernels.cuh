@@ -31,6 +31,12 @@ struct PathSoA {
     float4* hit_n;   // normal, w = bits(iterations | material << 16)
     uint32_t* vis;   // shadow visibility (1 = clear)
     float4* Ls;      // per-path final radiance (committed in ascending sample order)
+    // resumable march state of a segment cut at the step quantum (one row per path
+    // and segment kind: continuation rows [0, capacity), shadow rows [capacity, 2*capacity))
+    float4* m0;      // t, omega, prev_radius, step_len
+    float4* m1;      // t_end, cand_t, cand_err, bits(steps)
+    float4* m2;      // candidate sample: d, traps 0..2
+    float4* m3;      // trap 3, bits(iterations), bits(material), bits(light index)
     uint32_t capacity;
 };
 
@@ -46,6 +52,19 @@ struct RoundQueues {
     uint32_t* next_shadow;
     uint32_t* next_counts;    // [active, cont, shadow]
     uint32_t* work_counter;   // trace kernel fetch counter (zeroed per round)
+};
+
+// One launch of the persistent trace kernel: the round's fresh segments
+// (continuations then shadows) or the segments resumed after a step quantum.
+// Item encoding in resume lists: path | (shadow ? 1u << 31 : 0).
+struct TraceLaunch {
+    RoundQueues q;
+    const uint32_t* resume;       // null on the first launch of a round
+    const uint32_t* resume_count;
+    uint32_t* next_resume;        // segments cut at this launch's quantum
+    uint32_t* next_resume_count;
+    uint32_t* work_counter;
+    uint32_t quantum;             // march steps per segment per launch (0 = unbounded)
 };
 
 struct FilmPlanes {
@@ -81,8 +100,8 @@ cudaError_t sf_launch_primary(const DeProgram* prog, const DevScene* scene, uint
                               uint32_t* steps_out, float* normal_out, uint32_t* work_counter,
                               unsigned long long* stats, int persistent, cudaStream_t st);
 cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom g, uint32_t* counts, cudaStream_t st);
-cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, RoundQueues q,
-                            unsigned long long* stats, int blocks, int threads, cudaStream_t st);
+cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
+                            unsigned long long* stats, int blocks, int threads, int min_blocks, cudaStream_t st);
 cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
                             uint32_t* status, int final_round, cudaStream_t st);
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st);
@@ -95,7 +114,7 @@ cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint
                                uint32_t* iters, unsigned long long* stats, cudaStream_t st);
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
-cudaError_t sf_launch_perturb(const float2* orbit_f, const uint32_t* orbit_len, uint32_t width, uint32_t height,
+cudaError_t sf_launch_perturb(const double2* orbit_d, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width, uint32_t height,
                               float pitch, float aspect_unused, uint32_t max_iter, float bailout, uint32_t* iters,
                               float* smooth, unsigned long long* stats, cudaStream_t st);
 cudaError_t sf_launch_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch, uint32_t max_iter,

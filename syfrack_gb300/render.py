@@ -229,8 +229,9 @@ class RenderSession:
         except Exception:
             pass
 
-    def set_launch(self, blocks_per_sm: int, threads: int):
-        check(self.ctx.lib.sf_session_set_launch(self.h, blocks_per_sm, threads))
+    def set_launch(self, min_blocks_per_sm: int = 2, threads: int = 256, quantum: int = 64):
+        """Trace-kernel shape: resident blocks per SM (register budget), threads, step quantum."""
+        check(self.ctx.lib.sf_session_set_launch(self.h, min_blocks_per_sm, threads, quantum))
 
     def dispatch(self, tile, samples: int):
         """One tile, `samples` samples starting at tile.done; asynchronous."""

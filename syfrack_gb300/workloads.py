@@ -9,7 +9,8 @@ mandelbox_pathtrace: 1280x720, 64 spp, 4 bounces, 512 steps; Mandelbox scale -1.
                      (box fold 1, min radius 0.5, fixed radius 1, 15 iterations,
                      bailout 1000, NormFence); Lambert albedo 0.7 blending into a
                      metal of roughness 0.2 by orbit trap 0; one 1x1 area light of
-                     radiance 10 above the form facing down.
+                     radiance 10 above the form's front-top edge, facing
+                     down towards its centre.
 mixed_batch        : 64 seeded jobs (Mandelbulb powers 2-12, Mandelbox scales
                      -2.5..2.5, Menger levels 3-7), tiles log-uniform 64..512,
                      1-16 spp, 2 bounces, camera distance 2.5-4, random orientation.
@@ -45,7 +46,8 @@ def mandelbox_graph(scale=-1.5, iterations=15) -> Graph:
 def mandelbox_scene(seed: int = 20261203) -> Scene:
     mat = Material(albedo=(0.7, 0.7, 0.7), roughness=0.2, metallic=0.0, specular=0.04,
                    surface=SurfaceVariation(slot=0, roughness=(0.2, 0.2), metallic=(0.0, 1.0)))
-    light = AreaLight(position=(0.0, 3.0, -1.0), normal=(0.0, -1.0, 0.0), size=(1.0, 1.0),
+    # above the form's front-top edge, facing down towards its centre
+    light = AreaLight(position=(1.0, 3.5, -3.5), normal=(-1.0, -3.5, 3.5), size=(1.0, 1.0),
                       color=(1.0, 1.0, 1.0), intensity=10.0)
     cam = Camera.look_at((3.2, 2.6, -5.5), (0.0, 0.0, 0.0), 45.0)
     return Scene(graph=mandelbox_graph(), camera=cam, material=mat, lights=[light], seed=seed)

@@ -81,8 +81,8 @@ def test_escape2d_canvas_against_oracle(gpu_ctx, oracle_mod):
 
 
 def test_beyond_reference_caps(gpu_ctx, oracle_mod):
-    # 20,000 iterations and zoom 1e5 (the reference caps 512 and 1e4)
-    f = PlanarFractal(family="BurningShip", iterations=20000, zoom=1e5, center=(-1.7619, -0.0285))
+    # 20,000 iterations and zoom 1e5 (the reference caps 512 and 1e4), seahorse valley
+    f = PlanarFractal(family="Mandelbrot", iterations=20000, zoom=1e5, center=(-0.7436, 0.1318))
     pts = np.random.default_rng(8).uniform(-1, 1, (2048, 2)).astype(np.float32)
     gpu = f.sample(gpu_ctx, pts)
     ref = oracle_mod.planar(oracle_params(oracle_mod, f), pts, precision=32)
