@@ -235,6 +235,8 @@ typedef struct sf_stats {
     double kernel_ms;          /* device time of the timed kernels (profiling on) */
     double trace_ms;           /* of which the trace (march) kernels */
     uint64_t trace_launches;
+    uint64_t warp_de_calls;    /* warp-level DE invocations of the trace kernel */
+    uint64_t iteration_slots;  /* per invocation: warp max iterations x active lanes */
 } sf_stats;
 /* Per-kernel CUDA-event timing on the context stream (off by default). */
 sf_status sf_context_set_profiling(sf_context* ctx, int enable);

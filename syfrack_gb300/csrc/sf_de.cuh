@@ -107,6 +107,15 @@ __device__ __forceinline__ void trap_update(DeRaw& s, uint32_t slot, uint32_t mo
     else s.t3 = trap_mode_apply(mode, s.t3, v);
 }
 
+// A Norm trap kept as |p|^2 (Minimum / Last modes): sqrtf is monotonic, so the
+// root of the minimum (or of the last value) equals the reference's minimum of roots.
+__device__ __forceinline__ void trap_sqrt(DeRaw& s, uint32_t slot) {
+    if (slot == 0) s.t0 = sqrtf(s.t0);
+    else if (slot == 1) s.t1 = sqrtf(s.t1);
+    else if (slot == 2) s.t2 = sqrtf(s.t2);
+    else s.t3 = sqrtf(s.t3);
+}
+
 // integral_spherical_power (eval.rs:129-178): complex powers of the polar and
 // azimuthal unit vectors; n = 6, 8 by repeated squaring, other n by binary powers.
 __device__ __forceinline__ void spherical_power(float3 p, float r, uint32_t n, float3& out, float& deriv) {
@@ -224,11 +233,12 @@ __device__ __forceinline__ DeRaw de_box(const FormParams& f, float3 p) {
     float dr = 1.0f;
     const uint32_t n = f.iterations;
     const float l = f.limit;
+    const bool sq = f.trap_squared != 0;
     for (uint32_t i = 0; i < n; ++i) {
-        if (len3(p) > f.bailout) break;
+        if (dot3(p, p) > f.bailout_t) break;
         p = clamp3(p, -l, l) * 2.0f - p;
         float r2 = dot3(p, p);
-        float v = f.trap_measure == SF_MEASURE_NORM ? sqrtf(r2) : trap_measure(f.trap_measure, p);
+        float v = sq ? r2 : trap_measure(f.trap_measure, p);
         trap_update(s, f.trap_slot, f.trap_mode, v);
         float k = r2 < f.min_radius2 ? f.fold_k_min : (r2 < f.fixed_radius2 ? f.fixed_radius2 / r2 : 1.0f);
         p = p * k;
@@ -241,6 +251,7 @@ __device__ __forceinline__ DeRaw de_box(const FormParams& f, float3 p) {
     }
     s.d = (len3(p) - f.fence[0]) / fabsf(dr);
     s.material = f.material;
+    if (sq) trap_sqrt(s, f.trap_slot);
     return s;
 }
 
@@ -251,8 +262,9 @@ __device__ __forceinline__ DeRaw de_menger(const FormParams& f, float3 p) {
     const uint32_t n = f.iterations;
     const float sc = f.scale;
     const float3 off = mk3(f.offset[0], f.offset[1], f.offset[2]);
+    const bool sq = f.trap_squared != 0;
     for (uint32_t i = 0; i < n; ++i) {
-        if (len3(p) > f.bailout) break;
+        if (dot3(p, p) > f.bailout_t) break;
         float3 z = abs3(p);
         if (z.x < z.y) z = mk3(z.y, z.x, z.z);
         if (z.x < z.z) z = mk3(z.z, z.y, z.x);
@@ -261,12 +273,13 @@ __device__ __forceinline__ DeRaw de_menger(const FormParams& f, float3 p) {
         if (z.z < -0.5f * off.z * (sc - 1.0f)) z.z += off.z * (sc - 1.0f);
         p = z;
         dr *= sc;
-        float v = trap_measure(f.trap_measure, p);
+        float v = sq ? dot3(p, p) : trap_measure(f.trap_measure, p);
         trap_update(s, f.trap_slot, f.trap_mode, v);
         s.iter++;
     }
     s.d = box_fence(p, mk3(f.fence[0], f.fence[1], f.fence[2]), dr);
     s.material = f.material;
+    if (sq) trap_sqrt(s, f.trap_slot);
     return s;
 }
 
@@ -519,7 +532,7 @@ __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
             seed_p = c; seed_dr = 1.0f; depth = 0;
             break;
         case SF_OP_ITER_BEGIN:
-            if (op.a == 0 || len3(s.p) > op.f[0] || depth >= SF_MAX_LOOP_DEPTH) { pc = op.b; break; }
+            if (op.a == 0 || dot3(s.p, s.p) > op.f[1] || depth >= SF_MAX_LOOP_DEPTH) { pc = op.b; break; }
             loop_count[depth] = 0;
             loop_seed[depth] = s.p;
             loop_seed_dr[depth] = s.dr;
@@ -530,7 +543,7 @@ __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
             const DeOp& b = P.ops[op.a];
             s.iter += 1;
             uint32_t cnt = ++loop_count[depth - 1];
-            if (cnt < b.a && !(len3(s.p) > b.f[0])) {
+            if (cnt < b.a && !(dot3(s.p, s.p) > b.f[1])) {
                 pc = op.a;  // continue at the first body op (pc++ follows)
                 seed_p = loop_seed[depth - 1];
                 seed_dr = loop_seed_dr[depth - 1];

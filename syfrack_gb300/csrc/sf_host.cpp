@@ -247,6 +247,7 @@ void lip_visit(const HostGraph& g, uint32_t id, float radius, uint32_t depth, fl
 }
 
 // ------------------------------------------------------------------ lowering
+float sqrt_threshold(float b);
 struct Lowerer {
     const HostGraph& g;
     DeProgram& P;
@@ -268,6 +269,7 @@ struct Lowerer {
             DeOp b = mk(SF_OP_ITER_BEGIN);
             b.a = n->u[0];
             b.f[0] = n->f[0];
+            b.f[1] = sqrt_threshold(n->f[0]);
             if (!push(b)) return false;
             for (uint32_t c : g.body_of(*n))
                 if (!point_op(c)) return false;
@@ -358,6 +360,23 @@ struct Lowerer {
     }
 };
 
+// Largest float x with sqrtf(x) <= b. sqrtf is correctly rounded and monotonic,
+// so |p| > b (the reference's `p.length() > bailout`) is exactly dot(p,p) > T.
+float sqrt_threshold(float b) {
+    if (!(b == b)) return b;                  // NaN: no comparison is ever true
+    if (b < 0.f) return -1.0f;                // any x >= 0 exceeds it (sqrt(x) >= 0 > b)
+    if (std::isinf(b)) return b;
+    float t = b * b;
+    if (std::isinf(t)) t = 3.4028235e38f;
+    while (t > 0.f && sqrtf(t) > b) t = std::nextafter(t, 0.0f);
+    for (;;) {
+        float u = std::nextafter(t, INFINITY);
+        if (std::isinf(u) || sqrtf(u) > b) break;
+        t = u;
+    }
+    return t;
+}
+
 // Recognises the iterated forms of graphs/{mandelbulb,mandelbox,menger}.ron.
 void detect_form(const HostGraph& g, DeProgram& P) {
     P.form = SF_FORM_GENERIC;
@@ -400,11 +419,13 @@ void detect_form(const HostGraph& g, DeProgram& P) {
     std::memset(&f, 0, sizeof f);
     f.iterations = it->u[0];
     f.bailout = it->f[0];
+    f.bailout_t = sqrt_threshold(it->f[0]);
     f.material = material;
     auto set_trap = [&](const sf_node* t) {
         f.trap_slot = std::min<uint32_t>(t->u[0], 3);
         f.trap_measure = t->u[1];
         f.trap_mode = t->u[2];
+        f.trap_squared = t->u[1] == SF_MEASURE_NORM && t->u[2] != SF_TRAP_MAXIMUM;
     };
     if (fence->kind == SF_NODE_BULB_FENCE && kinds({SF_NODE_TRAP, SF_NODE_POWER, SF_NODE_ADD_ORIGIN})) {
         set_trap(body[0]);
@@ -788,6 +809,8 @@ extern "C" sf_status sf_context_stats(sf_context* c, sf_stats* out) {
     out->segments = h[SF_STAT_SEGMENTS];
     out->shadow_segments = h[SF_STAT_SHADOW_SEGMENTS];
     out->steps = h[SF_STAT_STEPS];
+    out->warp_de_calls = h[SF_STAT_WARP_DE_CALLS];
+    out->iteration_slots = h[SF_STAT_ITER_SLOTS];
     out->launches = c->launches;
     out->kernel_ms = c->kernel_ms;
     out->trace_ms = c->trace_ms;

@@ -111,7 +111,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace_path(const DeProgram*
     March m;
     float3 hp = mk3(0.f, 0.f, 0.f), grad = mk3(0.f, 0.f, 0.f);
     float hstep = 0.f;
-    unsigned long long n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0;
+    unsigned long long n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0, n_slots = 0;
 
     while (true) {
         uint32_t w = warp_fetch(tl.work_counter, state == LANE_IDLE);
@@ -162,6 +162,12 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace_path(const DeProgram*
                 evaluated = true;
                 n_eval++;
                 n_iter += s.iter;
+                uint32_t act = __activemask();
+                uint32_t mx = __reduce_max_sync(act, s.iter);
+                if (lane_id() == (uint32_t)(__ffs(act) - 1)) {
+                    n_wcall++;
+                    n_slots += (unsigned long long)mx * __popc(act);
+                }
             }
             if (state == LANE_NORMAL) {
                 grad = grad + tetra_offset(tap) * s.d;
@@ -221,6 +227,8 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace_path(const DeProgram*
     warp_stat(&stats[SF_STAT_DE_ITERS], n_iter);
     warp_stat(&stats[SF_STAT_SEGMENTS], n_seg + n_shseg);
     warp_stat(&stats[SF_STAT_SHADOW_SEGMENTS], n_shseg);
+    warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
+    warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
 }
 
 // ------------------------------------------------------------------ primary rays

@@ -13,8 +13,11 @@ enum { SF_HF_HIT = 1u, SF_HF_EXHAUSTED = 2u };
 enum { SF_WF_QUEUE_OVERFLOW = 1u, SF_WF_COMPACT_OVERFLOW = 2u, SF_WF_ALIVE_AT_COMMIT = 4u };
 
 // Statistics accumulated by the trace kernels (64-bit device counters).
+// WARP_DE_CALLS counts warp-level DE invocations; ITER_SLOTS sums, per invocation,
+// the warp's largest iteration count times its active lanes (SIMT efficiency:
+// DE_EVALS / (32 * WARP_DE_CALLS) and DE_ITERS / ITER_SLOTS).
 enum { SF_STAT_DE_EVALS = 0, SF_STAT_DE_ITERS, SF_STAT_SEGMENTS, SF_STAT_STEPS, SF_STAT_SHADOW_SEGMENTS,
-       SF_STAT_COUNT = 8 };
+       SF_STAT_WARP_DE_CALLS, SF_STAT_ITER_SLOTS, SF_STAT_COUNT = 8 };
 
 // Structure-of-arrays path storage for one dispatch of `capacity` paths.
 struct PathSoA {

@@ -22,7 +22,7 @@
 // kind (enum sf_node_kind) as their code; control codes start at 100.
 enum {
     SF_OP_BEGIN = 100,      // point state := input point
-    SF_OP_ITER_BEGIN = 101, // a = iterations, b = index of the matching ITER_END, f0 = bailout
+    SF_OP_ITER_BEGIN = 101, // a = iterations, b = index of the matching ITER_END, f0 = bailout, f1 = bailout_t
     SF_OP_ITER_END = 102,   // a = index of the matching ITER_BEGIN
     SF_OP_FENCE_OFF = 103,  // disabled fence: push +inf with the point's iter/traps
     SF_OP_EMPTY = 104,      // unconnected distance input: push the empty state
@@ -42,7 +42,9 @@ struct DeOp {
 struct FormParams {
     uint32_t iterations;
     uint32_t trap_slot, trap_measure, trap_mode;  // the body's Trap node
+    uint32_t trap_squared;  // Norm trap in Minimum/Last mode: kept as |p|^2, one sqrt at the end
     float bailout;
+    float bailout_t;     // largest float x with sqrtf(x) <= bailout: |p| > bailout <=> dot(p,p) > bailout_t
     float power;         // Bulb
     uint32_t power_int;  // Bulb: 0 = trigonometric path, else the integer exponent 1..16
     float limit;         // Box: fold limit
