@@ -227,32 +227,51 @@ __device__ __forceinline__ DeRaw de_bulb(const FormParams& f, float3 p) {
 }
 
 // Mandelbox: Iterate{BoxFold, Trap, SphereFold, Scale, AddOrigin} -> NormFence.
-__device__ __forceinline__ DeRaw de_box(const FormParams& f, float3 p) {
+// NORM_MIN0: the bundled trap (slot 0, Norm, Minimum) kept as min |p|^2.
+// The sphere fold's fr^2 / r^2 uses the fast reciprocal division (<= 2 ulp, the
+// accuracy class WGSL allows for its own division).
+template <bool NORM_MIN0>
+__device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     DeRaw s = raw_empty();
     const float3 c = p;
     float dr = 1.0f;
     const uint32_t n = f.iterations;
-    const float l = f.limit;
+    const float l = f.limit, bt = f.bailout_t, mr2 = f.min_radius2, fr2 = f.fixed_radius2, kmin = f.fold_k_min;
+    const float sc = f.scale, asc = f.abs_scale;
     const bool sq = f.trap_squared != 0;
+    float t0 = SF_INF;
+    uint32_t it = 0;
     for (uint32_t i = 0; i < n; ++i) {
-        if (dot3(p, p) > f.bailout_t) break;
+        if (dot3(p, p) > bt) break;
         p = clamp3(p, -l, l) * 2.0f - p;
         float r2 = dot3(p, p);
-        float v = sq ? r2 : trap_measure(f.trap_measure, p);
-        trap_update(s, f.trap_slot, f.trap_mode, v);
-        float k = r2 < f.min_radius2 ? f.fold_k_min : (r2 < f.fixed_radius2 ? f.fixed_radius2 / r2 : 1.0f);
+        if (NORM_MIN0) {
+            t0 = fminf(t0, r2);
+        } else {
+            float v = sq ? r2 : trap_measure(f.trap_measure, p);
+            trap_update(s, f.trap_slot, f.trap_mode, v);
+        }
+        float k = __fdividef(fr2, r2);
+        k = r2 < fr2 ? k : 1.0f;
+        k = r2 < mr2 ? kmin : k;
         p = p * k;
         dr *= k;
-        p = p * f.scale;
-        dr *= f.abs_scale;
+        p = p * sc;
+        dr *= asc;
         p = p + c;
         dr += 1.0f;
-        s.iter++;
+        it++;
     }
+    s.iter = it;
     s.d = (len3(p) - f.fence[0]) / fabsf(dr);
     s.material = f.material;
-    if (sq) trap_sqrt(s, f.trap_slot);
+    if (NORM_MIN0) s.t0 = sqrtf(t0);
+    else if (sq) trap_sqrt(s, f.trap_slot);
     return s;
+}
+__device__ __forceinline__ DeRaw de_box(const FormParams& f, float3 p) {
+    if (f.trap_squared && f.trap_slot == 0 && f.trap_mode == SF_TRAP_MINIMUM) return de_box_t<true>(f, p);
+    return de_box_t<false>(f, p);
 }
 
 // Menger: Iterate{MengerFold, Trap} -> Box (graphs/menger.ron).
@@ -307,7 +326,7 @@ __device__ __forceinline__ float terrain_hash(int cx, int cy, int cz, uint32_t s
     h ^= h >> 16;
     return float(h >> 8) / 16777216.0f;
 }
-__device__ float terrain_noise(float3 p, uint32_t seed) {
+static __device__ float terrain_noise(float3 p, uint32_t seed) {
     float3 base = mk3(floorf(p.x), floorf(p.y), floorf(p.z));
     float3 f = p - base;
     float3 t = f * f * (mk3(3.f, 3.f, 3.f) - f * 2.0f);
@@ -322,7 +341,7 @@ __device__ float terrain_noise(float3 p, uint32_t seed) {
     return r;
 }
 
-__device__ void apply_point_op(const DeOp& op, PState& s, float3 c, float3 seed_p, float seed_dr) {
+static __device__ void apply_point_op(const DeOp& op, PState& s, float3 c, float3 seed_p, float seed_dr) {
     switch (op.code) {
     case SF_NODE_TRANSLATE: s.p = s.p + ld3(op.f); break;
     case SF_NODE_ROTATE: s.p = rotate_euler_xyz(s.p, mk3(to_rad(op.f[0]), to_rad(op.f[1]), to_rad(op.f[2]))); break;
@@ -432,7 +451,7 @@ __device__ void apply_point_op(const DeOp& op, PState& s, float3 c, float3 seed_
 }
 
 // fence (eval.rs:558-599).
-__device__ float fence_op(const DeOp& op, const PState& s) {
+static __device__ float fence_op(const DeOp& op, const PState& s) {
     switch (op.code) {
     case SF_NODE_SPHERE: return (len3(s.p) - op.f[0]) / s.dr;
     case SF_NODE_TORUS: {
@@ -476,7 +495,7 @@ __device__ __forceinline__ DeRaw dist_from(const PState& s, float d) {
 }
 
 // combine (eval.rs:601-657).
-__device__ DeRaw combine_op(uint32_t kind, float k, DeRaw a, DeRaw b) {
+static __device__ DeRaw combine_op(uint32_t kind, float k, DeRaw a, DeRaw b) {
     auto blend = [&](float h, float d) {
         DeRaw r;
         float ta[4] = {a.t0, a.t1, a.t2, a.t3}, tb[4] = {b.t0, b.t1, b.t2, b.t3}, tr[4];
@@ -512,7 +531,7 @@ __device__ DeRaw combine_op(uint32_t kind, float k, DeRaw a, DeRaw b) {
 }
 
 // Postfix interpreter over DeProgram.ops (generic graphs).
-__device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
+static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
     PState s;
     s.p = c; s.dr = 1.0f; s.iter = 0; s.t0 = s.t1 = s.t2 = s.t3 = SF_INF;
     uint32_t loop_count[SF_MAX_LOOP_DEPTH];

@@ -1067,7 +1067,7 @@ sf_status session_alloc(sf_session* s) {
     if (wf) {
         o_soa = take(N * 16 * 11 + N * 16);  // 11 float4/uint4 planes + vis (padded)
         o_lists = take(N * 4 * 6);
-        o_march = take(2 * N * 16 * 4);      // m0..m3 for continuation and shadow rows
+        o_march = take(2 * N * (16 + 16 + 4));  // m0, m1, m2 for continuation and shadow rows
         o_resume = take(2 * 2 * N * 4);
     }
     size_t o_counts = take(size_t(R + 1) * 4 * 4);
@@ -1104,8 +1104,7 @@ sf_status session_alloc(sf_session* s) {
         float4* m = reinterpret_cast<float4*>(base + o_march);
         s->soa.m0 = m;
         s->soa.m1 = m + 2 * N;
-        s->soa.m2 = m + 4 * N;
-        s->soa.m3 = m + 6 * N;
+        s->soa.m2 = reinterpret_cast<uint32_t*>(m + 4 * N);
         s->resume = reinterpret_cast<uint32_t*>(base + o_resume);
     }
     s->counts = reinterpret_cast<uint32_t*>(base + o_counts);
@@ -1222,7 +1221,7 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
             tl.next_resume_count = qc + 1;
             tl.quantum = j + 1 == Q ? 0u : s->quantum;  // the last launch runs segments to completion
             LaunchTimer t(c, true);
-            CU(sf_launch_trace(s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks, int(s->threads),
+            CU(sf_launch_trace(s->graph->prog.form, s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks,
                                int(s->min_blocks), st));
         }
         LaunchTimer t(c, false);

@@ -6,57 +6,7 @@
 #include "sf_kernels.cuh"
 #include "sf_trace.cuh"
 
-#define FULL_MASK 0xffffffffu
-
-static __device__ __forceinline__ uint32_t lane_id() { return threadIdx.x & 31u; }
-static __device__ __forceinline__ uint32_t lanemask_lt() { return (1u << lane_id()) - 1u; }
-
-// Warp-aggregated fetch of one work item per requesting lane: one atomic per warp.
-static __device__ __forceinline__ uint32_t warp_fetch(uint32_t* counter, bool want) {
-    uint32_t m = __ballot_sync(FULL_MASK, want);
-    uint32_t base = 0;
-    if (m) {
-        uint32_t leader = __ffs(m) - 1;
-        if (lane_id() == leader) base = atomicAdd(counter, __popc(m));
-        base = __shfl_sync(FULL_MASK, base, leader);
-    }
-    return base + __popc(m & lanemask_lt());
-}
-
-// Warp-aggregated append under an arbitrary active mask (grid-stride tails).
-static __device__ __forceinline__ void warp_append(uint32_t* counter, uint32_t* list, bool pred, uint32_t value) {
-    uint32_t active = __activemask();
-    uint32_t m = __ballot_sync(active, pred);
-    if (!m) return;
-    uint32_t leader = __ffs(m) - 1;
-    uint32_t base = 0;
-    if (lane_id() == leader) base = atomicAdd(counter, __popc(m));
-    base = __shfl_sync(active, base, leader);
-    if (pred) list[base + __popc(m & lanemask_lt())] = value;
-}
-
-// Sum of a per-lane counter into a 64-bit device counter (one atomic per warp).
-static __device__ __forceinline__ void warp_stat(unsigned long long* dst, unsigned long long v) {
-    uint32_t active = __activemask();
-#pragma unroll
-    for (int o = 16; o > 0; o >>= 1) v += __shfl_down_sync(active, v, o);
-    if (lane_id() == (uint32_t)(__ffs(active) - 1) && v) atomicAdd(dst, v);
-}
-
-// Stage the lowered graph (header + used ops) and scene constants in shared memory.
-static __device__ void stage_program(DeProgram& dst, const DeProgram* src) {
-    const uint32_t n_ops = src->n_ops;
-    const size_t header = offsetof(DeProgram, ops);
-    const size_t bytes = header + size_t(n_ops) * sizeof(DeOp);
-    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
-    uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
-    for (size_t i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = __ldg(s + i);
-}
-template <class T> static __device__ void stage_pod(T& dst, const T* src) {
-    const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
-    uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
-    for (size_t i = threadIdx.x; i < sizeof(T) / 4; i += blockDim.x) d[i] = __ldg(s + i);
-}
+#include "sf_warp.cuh"
 
 // ------------------------------------------------------------------ DE probe
 // de_probe.wgsl:9-17 / Renderer::probe_distances: one thread per point.
@@ -84,152 +34,6 @@ __global__ void __launch_bounds__(256) k_de_probe(const DeProgram* __restrict__ 
 // lockstep instead of waiting for the warp's longest march. Surface hits of
 // continuation rays run the four normal taps through the same DE call.
 enum { LANE_IDLE = 0, LANE_CONT = 1, LANE_SHADOW = 2, LANE_NORMAL = 3, LANE_DONE = 4 };
-
-// Segments are marched in quanta of `tl.quantum` steps: a segment still open at
-// the end of its quantum saves its march state (t, omega, previous radius, step,
-// candidate) and is re-queued for the next launch of the round. The tail of a
-// launch is thus bounded by one quantum instead of the longest ray.
-template <int MIN_BLOCKS>
-__global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace_path(const DeProgram* __restrict__ prog_g,
-                                                                const DevScene* __restrict__ scene_g, PathSoA soa,
-                                                                TraceLaunch tl, unsigned long long* stats) {
-    __shared__ DeProgram P;
-    __shared__ DevScene S;
-    stage_program(P, prog_g);
-    stage_pod(S, scene_g);
-    __syncthreads();
-    const bool first = tl.resume == nullptr;
-    const uint32_t n_cont = first ? tl.q.counts[1] : 0u;
-    const uint32_t total = first ? n_cont + tl.q.counts[2] : *tl.resume_count;
-    const uint32_t quantum = tl.quantum ? tl.quantum : 0xffffffffu;
-    const float accept = S.pixel_cone * S.pixel_tolerance;
-    const float safety = S.step_scale;
-    const uint32_t max_steps = S.max_steps;
-    const uint32_t cap = soa.capacity;
-
-    uint32_t state = LANE_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
-    March m;
-    float3 hp = mk3(0.f, 0.f, 0.f), grad = mk3(0.f, 0.f, 0.f);
-    float hstep = 0.f;
-    unsigned long long n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0, n_slots = 0;
-
-    while (true) {
-        uint32_t w = warp_fetch(tl.work_counter, state == LANE_IDLE);
-        if (state == LANE_IDLE) {
-            if (w >= total) {
-                state = LANE_DONE;
-            } else {
-                bool shadow, resumed = !first;
-                if (first) {
-                    shadow = w >= n_cont;
-                    path = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
-                } else {
-                    uint32_t item = tl.resume[w];
-                    path = item & 0x7fffffffu;
-                    shadow = (item >> 31) != 0;
-                }
-                float4 o = shadow ? soa.sh_o[path] : soa.o[path];
-                float4 d = shadow ? soa.sh_d[path] : soa.d[path];
-                float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
-                if (!resumed) {
-                    float t_end = nearest_emitter(S, ro, rd, shadow ? o.w : S.extent, li);
-                    march_begin(m, ro, rd, t_end);
-                    if (shadow) n_shseg++;
-                    else n_seg++;
-                } else {
-                    uint32_t row = path + (shadow ? cap : 0u);
-                    float4 a = soa.m0[row], b = soa.m1[row], c = soa.m2[row], e = soa.m3[row];
-                    m.ro = ro; m.rd = rd;
-                    m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
-                    m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
-                    m.cand.d = c.x; m.cand.t0 = c.y; m.cand.t1 = c.z; m.cand.t2 = c.w;
-                    m.cand.t3 = e.x; m.cand.iter = __float_as_uint(e.y); m.cand.material = __float_as_uint(e.z);
-                    li = __float_as_uint(e.w);
-                }
-                state = shadow ? LANE_SHADOW : LANE_CONT;
-                budget = quantum;
-            }
-        }
-        if (__all_sync(FULL_MASK, state == LANE_DONE)) break;
-        if (state == LANE_CONT || state == LANE_SHADOW || state == LANE_NORMAL) {
-            int r = MARCH_CONTINUE;
-            if (state != LANE_NORMAL) r = march_check(m, max_steps, accept);
-            DeRaw s;
-            bool evaluated = false;
-            if (r == MARCH_CONTINUE) {
-                float3 qp = state == LANE_NORMAL ? hp + tetra_offset(tap) * hstep : m.ro + m.rd * m.t;
-                s = de_raw(P, qp);
-                evaluated = true;
-                n_eval++;
-                n_iter += s.iter;
-                uint32_t act = __activemask();
-                uint32_t mx = __reduce_max_sync(act, s.iter);
-                if (lane_id() == (uint32_t)(__ffs(act) - 1)) {
-                    n_wcall++;
-                    n_slots += (unsigned long long)mx * __popc(act);
-                }
-            }
-            if (state == LANE_NORMAL) {
-                grad = grad + tetra_offset(tap) * s.d;
-                if (++tap == 4) {
-                    float3 n = normalize3(grad);
-                    float4 hn = soa.hit_n[path];
-                    soa.hit_n[path] = make_float4(n.x, n.y, n.z, hn.w);
-                    state = LANE_IDLE;
-                }
-            } else {
-                bool at_budget = !evaluated;  // march_check ended the segment
-                if (evaluated) {
-                    r = march_update(m, s, safety, accept, false);
-                    if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept), at_budget = r != MARCH_CONTINUE;
-                    if (r == MARCH_HIT && !at_budget) m.cand = s, m.cand_t = m.t;  // hit at this step
-                }
-                if (r == MARCH_CONTINUE && --budget == 0) {
-                    // quantum spent: save the march and hand the segment to the next launch
-                    bool shadow = state == LANE_SHADOW;
-                    uint32_t row = path + (shadow ? cap : 0u);
-                    soa.m0[row] = make_float4(m.t, m.omega, m.prev_radius, m.step_len);
-                    soa.m1[row] = make_float4(m.t_end, m.cand_t, m.cand_err, __uint_as_float(m.i));
-                    soa.m2[row] = make_float4(m.cand.d, m.cand.t0, m.cand.t1, m.cand.t2);
-                    soa.m3[row] = make_float4(m.cand.t3, __uint_as_float(m.cand.iter), __uint_as_float(m.cand.material),
-                                              __uint_as_float(li));
-                    warp_append(tl.next_resume_count, tl.next_resume, true, path | (shadow ? 0x80000000u : 0u));
-                    state = LANE_IDLE;
-                } else if (r != MARCH_CONTINUE) {
-                    if (state == LANE_SHADOW) {
-                        soa.vis[path] = (r == MARCH_MISS && li == SF_NO_LIGHT) ? 1u : 0u;
-                        state = LANE_IDLE;
-                    } else if (r == MARCH_HIT) {
-                        // surface hit (at this step, or the best candidate at the step budget)
-                        DeSampleF smp = de_finalize(P, m.cand);
-                        float t = m.cand_t;
-                        soa.hit[path] = make_uint4(__float_as_uint(t), m.i, SF_NO_LIGHT, SF_HF_HIT);
-                        soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
-                        soa.hit_n[path] = make_float4(0.f, 0.f, 0.f, __uint_as_float(smp.iter | (smp.material << 16)));
-                        hp = m.ro + m.rd * t;
-                        hstep = fmaxf(t * S.pixel_cone * 0.5f, 1e-4f) * S.pixel_tolerance;
-                        grad = mk3(0.f, 0.f, 0.f);
-                        tap = 0;
-                        state = LANE_NORMAL;
-                    } else if (r == MARCH_MISS && li != SF_NO_LIGHT) {
-                        soa.hit[path] = make_uint4(__float_as_uint(m.t_end), m.i, li, SF_HF_HIT);
-                        state = LANE_IDLE;
-                    } else {
-                        soa.hit[path] = make_uint4(__float_as_uint(m.t_end), m.i, SF_NO_LIGHT,
-                                                   r == MARCH_EXHAUSTED ? SF_HF_EXHAUSTED : 0u);
-                        state = LANE_IDLE;
-                    }
-                }
-            }
-        }
-    }
-    warp_stat(&stats[SF_STAT_DE_EVALS], n_eval);
-    warp_stat(&stats[SF_STAT_DE_ITERS], n_iter);
-    warp_stat(&stats[SF_STAT_SEGMENTS], n_seg + n_shseg);
-    warp_stat(&stats[SF_STAT_SHADOW_SEGMENTS], n_shseg);
-    warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
-    warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
-}
 
 // ------------------------------------------------------------------ primary rays
 // Primary rays through pixel centres (control.wgsl:270-273), the same relaxed
@@ -312,7 +116,7 @@ __global__ void __launch_bounds__(256) k_primary(const DeProgram* __restrict__ p
             } else {
                 bool at_budget = !evaluated;
                 if (evaluated) {
-                    r = march_update(m, s, P.form == 0xffffffffu ? 1.f : S.step_scale, accept, absolute);
+                    r = march_update(m, s.d, S.step_scale, accept, absolute);
                     if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept), at_budget = r != MARCH_CONTINUE;
                     if (r == MARCH_HIT && !at_budget) m.cand_t = m.t;
                 }
@@ -490,15 +294,20 @@ __global__ void __launch_bounds__(256) k_commit(PathSoA soa, DispatchGeom g, Fil
 // The plain per-pixel integrator (pathtrace.wgsl:1203-1276): one thread per
 // pixel runs every sample's whole path with blocking marches.
 static __device__ int march_full(const DeProgram& P, March& m, uint32_t max_steps, float safety, float accept,
-                                 unsigned long long& evals, unsigned long long& iters) {
+                                 DeRaw& hit, unsigned long long& evals, unsigned long long& iters) {
     int r = march_check(m, max_steps, accept);
     while (r == MARCH_CONTINUE) {
         DeRaw s = de_raw(P, m.ro + m.rd * m.t);
         evals++;
         iters += s.iter;
-        r = march_update(m, s, safety, accept, false);
-        if (r == MARCH_HIT) { m.cand = s; m.cand_t = m.t; return r; }
+        r = march_update(m, s.d, safety, accept, false);
+        if (r == MARCH_HIT) { hit = s; m.cand_t = m.t; return r; }
         if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept);
+    }
+    if (r == MARCH_HIT) {  // candidate accepted at the step budget
+        hit = de_raw(P, m.ro + m.rd * m.cand_t);
+        evals++;
+        iters += hit.iter;
     }
     return r;
 }
@@ -528,7 +337,8 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
             March m;
             float t_end = nearest_emitter(S, ps.o, ps.d, S.extent, li);
             march_begin(m, ps.o, ps.d, t_end);
-            int r = march_full(P, m, S.max_steps, S.step_scale, accept, evals, iters);
+            DeRaw hs;
+            int r = march_full(P, m, S.max_steps, S.step_scale, accept, hs, evals, iters);
             segs++;
             HitInfo h;
             h.hit = false;
@@ -539,7 +349,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
             if (r == MARCH_HIT) {
                 h.hit = true;
                 h.t = m.cand_t;
-                h.sample = de_finalize(P, m.cand);
+                h.sample = de_finalize(P, hs);
                 float3 hp = ps.o + ps.d * h.t;
                 float hs = fmaxf(h.t * S.pixel_cone * 0.5f, 1e-4f) * S.pixel_tolerance;
                 float3 grad = mk3(0.f, 0.f, 0.f);
@@ -569,7 +379,8 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 March sm;
                 float st_end = nearest_emitter(S, sh.o, sh.dir, sh.t_end, sli);
                 march_begin(sm, sh.o, sh.dir, st_end);
-                int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, evals, iters);
+                DeRaw shs;
+                int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, shs, evals, iters);
                 segs++;
                 if (sr == MARCH_MISS && sli == SF_NO_LIGHT) ps.L = ps.L + sh.contrib;
             }
@@ -909,16 +720,16 @@ cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom 
     k_generate<<<(g.paths + 255) / 256, 256, 0, st>>>(scene, soa, g, counts);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
-                            unsigned long long* stats, int blocks, int threads, int min_blocks, cudaStream_t st) {
-    if (threads <= 0) threads = 256;
-    if (blocks <= 0) blocks = sf_device_sm_count() * (min_blocks > 0 ? min_blocks : 2);
-    switch (min_blocks) {
-    case 3: k_trace_path<3><<<blocks, threads, 0, st>>>(prog, scene, soa, tl, stats); break;
-    case 4: k_trace_path<4><<<blocks, threads, 0, st>>>(prog, scene, soa, tl, stats); break;
-    default: k_trace_path<2><<<blocks, threads, 0, st>>>(prog, scene, soa, tl, stats); break;
+cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
+                            unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
+    if (min_blocks < 2 || min_blocks > 4) min_blocks = 2;
+    if (blocks <= 0) blocks = sf_device_sm_count() * min_blocks;
+    switch (form) {
+    case SF_FORM_BULB: return sf_launch_trace_bulb(prog, scene, soa, tl, stats, blocks, min_blocks, st);
+    case SF_FORM_BOX: return sf_launch_trace_box(prog, scene, soa, tl, stats, blocks, min_blocks, st);
+    case SF_FORM_MENGER: return sf_launch_trace_menger(prog, scene, soa, tl, stats, blocks, min_blocks, st);
+    default: return sf_launch_trace_any(prog, scene, soa, tl, stats, blocks, min_blocks, st);
     }
-    return cudaGetLastError();
 }
 cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
                             uint32_t* status, int final_round, cudaStream_t st) {

@@ -38,8 +38,7 @@ struct PathSoA {
     // and segment kind: continuation rows [0, capacity), shadow rows [capacity, 2*capacity))
     float4* m0;      // t, omega, prev_radius, step_len
     float4* m1;      // t_end, cand_t, cand_err, bits(steps)
-    float4* m2;      // candidate sample: d, traps 0..2
-    float4* m3;      // trap 3, bits(iterations), bits(material), bits(light index)
+    uint32_t* m2;    // light index ahead of the segment
     uint32_t capacity;
 };
 
@@ -103,8 +102,17 @@ cudaError_t sf_launch_primary(const DeProgram* prog, const DevScene* scene, uint
                               uint32_t* steps_out, float* normal_out, uint32_t* work_counter,
                               unsigned long long* stats, int persistent, cudaStream_t st);
 cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom g, uint32_t* counts, cudaStream_t st);
-cudaError_t sf_launch_trace(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
-                            unsigned long long* stats, int blocks, int threads, int min_blocks, cudaStream_t st);
+// Persistent trace kernel, one instantiation per form (sf_trace_<form>.cu).
+cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
+                            unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st);
+cudaError_t sf_launch_trace_bulb(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
+                                 cudaStream_t);
+cudaError_t sf_launch_trace_box(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
+                                cudaStream_t);
+cudaError_t sf_launch_trace_menger(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int,
+                                   int, cudaStream_t);
+cudaError_t sf_launch_trace_any(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
+                                cudaStream_t);
 cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
                             uint32_t* status, int final_round, cudaStream_t st);
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st);

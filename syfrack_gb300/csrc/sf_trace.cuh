@@ -56,37 +56,37 @@ __device__ __forceinline__ void camera_ray(const DevScene& S, uint32_t px, uint3
 // persistent kernel can interleave lanes: march_query() gives the point to
 // evaluate, march_update() consumes its DE. absolute = fixed-epsilon hit test.
 enum { MARCH_CONTINUE = 0, MARCH_HIT = 1, MARCH_MISS = 2, MARCH_EXHAUSTED = 3 };
+// The best candidate's sample is not kept: a candidate accepted at the step
+// budget is re-evaluated at cand_t (same point, same code, same sample).
 struct March {
     float3 ro, rd;
     float t, omega, prev_radius, step_len, t_end;
     float cand_t, cand_err;
-    DeRaw cand;
     uint32_t i;  // steps taken
 };
 __device__ __forceinline__ void march_begin(March& m, float3 ro, float3 rd, float t_end) {
     m.ro = ro; m.rd = rd; m.t = 0.0f; m.omega = 1.2f; m.prev_radius = 0.0f; m.step_len = 0.0f;
     m.t_end = t_end; m.cand_t = 0.0f; m.cand_err = 1e30f; m.i = 0;
-    m.cand.d = 200.0f; m.cand.t0 = m.cand.t1 = m.cand.t2 = m.cand.t3 = SF_INF;
-    m.cand.iter = 0; m.cand.material = 0;
 }
 // Before a step: decide whether the march continues; returns MARCH_CONTINUE when a
-// DE evaluation at m.ro + m.rd * m.t is needed.
-__device__ __forceinline__ int march_check(March& m, uint32_t max_steps, float accept) {
+// DE evaluation at m.ro + m.rd * m.t is needed. MARCH_HIT here means the step
+// budget ended on an accepted candidate (at m.cand_t).
+__device__ __forceinline__ int march_check(const March& m, uint32_t max_steps, float accept) {
     if (m.i >= max_steps) return m.cand_err < accept * 4.0f ? MARCH_HIT : MARCH_EXHAUSTED;
     if (m.t >= m.t_end) return MARCH_MISS;
     return MARCH_CONTINUE;
 }
-// After the DE at the current t: MARCH_HIT (hit at m.t, sample s), MARCH_MISS
+// After the DE distance d at the current t: MARCH_HIT (hit at m.t), MARCH_MISS
 // (proven clear) or MARCH_CONTINUE (t advanced).
-__device__ __forceinline__ int march_update(March& m, const DeRaw& s, float safety, float accept, bool absolute) {
+__device__ __forceinline__ int march_update(March& m, float d, float safety, float accept, bool absolute) {
     m.i += 1;
-    float radius = fabsf(s.d) * safety;
+    float radius = fabsf(d) * safety;
     bool sor_fail = m.omega > 1.0f && (radius + m.prev_radius) < m.step_len * 1.0001f;
     if (sor_fail) { m.step_len = m.step_len - m.omega * m.step_len; m.omega = 1.0f; }
     else m.step_len = radius * m.omega;
     m.prev_radius = radius;
     float err = absolute ? radius : radius / fmaxf(m.t, 1e-6f);
-    if (!sor_fail && err < m.cand_err) { m.cand_t = m.t; m.cand = s; m.cand_err = err; }
+    if (!sor_fail && err < m.cand_err) { m.cand_t = m.t; m.cand_err = err; }
     if (!sor_fail && (absolute ? err <= accept : err < accept)) return MARCH_HIT;
     if (!sor_fail && m.t + m.step_len >= m.t_end) {
         if (radius >= m.t_end - m.t) return MARCH_MISS;
@@ -129,7 +129,7 @@ __device__ __forceinline__ float mis_power(float a, float b) {
     return pa * pa / (pa * pa + pb * pb);
 }
 // Emitter hit by a continuation ray (area_emission, lights.wgsl:330-356).
-__device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, float distance, float prev_pdf, bool use_mis,
+static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, float distance, float prev_pdf, bool use_mis,
                                 float3 prev_normal, float prev_total) {
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
@@ -195,7 +195,7 @@ __device__ __forceinline__ float3 fresnel(float3 f0, float vh) {
     float p5 = m2 * m2 * m;  // pow(1 - vh, 5)
     return f0 + (mk3(1.f, 1.f, 1.f) - f0) * p5;
 }
-__device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1, float r2) {
+static __device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1, float r2) {
     float3 t, bt;
     tangent_frame(n, t, bt);
     float3 lv = mk3(dot3(t, v), dot3(bt, v), dot3(n, v));
@@ -215,7 +215,7 @@ __device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1, float 
     float3 nh = t1 * x + t2 * y + vh * sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y));
     return frame_mul(t, bt, n, safe_normalize3(mk3(alpha * nh.x, alpha * nh.y, fmaxf(nh.z, 0.0f))));
 }
-__device__ float3 brdf_eval(const Surface& s, float3 v, float3 l) {
+static __device__ float3 brdf_eval(const Surface& s, float3 v, float3 l) {
     float nl = dot3(s.n, l), nv = dot3(s.n, v);
     if (nl <= 0.0f || nv <= 0.0f) return mk3(0.f, 0.f, 0.f);
     float3 h = normalize3(v + l);
@@ -230,7 +230,7 @@ __device__ __forceinline__ float spec_probability(const Surface& s, float nv) {
     float3 f = fresnel(s.f0, nv);
     return fminf(fmaxf(luminance(f) / fmaxf(luminance(f) + luminance(s.diffuse), 1e-4f), 0.05f), 0.95f);
 }
-__device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_spec) {
+static __device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_spec) {
     float nl = dot3(s.n, l);
     if (nl <= 0.0f) return 0.0f;
     float3 hh = normalize3(v + l);
@@ -241,7 +241,7 @@ __device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_spec) {
     return p_spec * pdf_spec + (1.0f - p_spec) * nl / SF_PI;
 }
 // make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
-__device__ Surface make_surface(const DevScene& S, float3 n, const DeSampleF& smp) {
+static __device__ Surface make_surface(const DevScene& S, float3 n, const DeSampleF& smp) {
     const DevMaterial* m = &S.material;
     bool assigned = smp.material > 0 && smp.material <= S.finish_count;
     if (assigned) m = &S.finishes[smp.material - 1];
@@ -306,7 +306,7 @@ __device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uin
 // classification, emitter MIS, surface, next-event sampling (the visibility
 // test is returned in `sh` and its radiance added by the caller if clear) and
 // BSDF continuation with Russian roulette. Writes first-hit depth/aux at bounce 0.
-__device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, ShadowReq& sh, float* first_depth,
+static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, ShadowReq& sh, float* first_depth,
                            float4* first_aux) {
     sh.active = false;
     if (!h.hit) return PATH_DONE;  // no environment light: a miss adds nothing

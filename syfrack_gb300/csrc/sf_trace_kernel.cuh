@@ -1,0 +1,185 @@
+// The persistent trace kernel of the wavefront integrator (the counterpart of
+// wf_intersect, wavefront.wgsl:187-195, marching in resumable quanta), compiled
+// once per form so that each instantiation carries only its own DE routine.
+//
+// Every lane holds one segment. A lane whose segment ends fetches the next work
+// item at once (one atomic per warp), so the warp keeps evaluating the DE in
+// lockstep instead of waiting for its longest march. Continuation hits run the
+// four tetrahedral normal taps (common.wgsl:376-387) through the same DE call;
+// a candidate accepted at the step budget (pathtrace.wgsl:137-141) is
+// re-evaluated at its t, through that call too, for its sample. A segment still
+// open after `quantum` steps saves its march state and is re-queued, bounding
+// each launch's tail by one quantum.
+#pragma once
+#include "sf_kernels.cuh"
+#include "sf_trace.cuh"
+#include "sf_warp.cuh"
+
+enum { TL_IDLE = 0, TL_MARCH = 1, TL_CAND = 2, TL_NORMAL = 3, TL_DONE = 4 };
+#define SF_FORM_ANY 99u
+
+template <int FORM>
+__device__ __forceinline__ DeRaw de_form(const DeProgram& P, float3 p) {
+    if constexpr (FORM == SF_FORM_BULB) return de_bulb(P.fp, p);
+    else if constexpr (FORM == SF_FORM_BOX) return de_box(P.fp, p);
+    else if constexpr (FORM == SF_FORM_MENGER) return de_menger(P.fp, p);
+    else return de_raw(P, p);
+}
+
+template <int FORM, int MIN_BLOCKS>
+__global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __restrict__ prog_g,
+                                                           const DevScene* __restrict__ scene_g, PathSoA soa,
+                                                           TraceLaunch tl, unsigned long long* stats) {
+    __shared__ DeProgram P;
+    __shared__ DevScene S;
+    stage_program(P, prog_g);
+    stage_pod(S, scene_g);
+    __syncthreads();
+    const bool first = tl.resume == nullptr;
+    const uint32_t n_cont = first ? tl.q.counts[1] : 0u;
+    const uint32_t total = first ? n_cont + tl.q.counts[2] : *tl.resume_count;
+    const uint32_t quantum = tl.quantum ? tl.quantum : 0xffffffffu;
+    const float accept = S.pixel_cone * S.pixel_tolerance;
+    const float safety = S.step_scale;
+    const uint32_t max_steps = S.max_steps;
+    const uint32_t cap = soa.capacity;
+
+    uint32_t state = TL_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
+    bool shadow = false;
+    March m;
+    float3 grad = mk3(0.f, 0.f, 0.f);
+    float hstep = 0.f;
+    uint32_t n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0;
+    unsigned long long n_slots = 0;
+
+    // End of a continuation or shadow segment without a surface sample.
+    auto finish = [&](int r) {
+        if (shadow) soa.vis[path] = (r == MARCH_MISS && li == SF_NO_LIGHT) ? 1u : 0u;
+        else if (r == MARCH_MISS && li != SF_NO_LIGHT)
+            soa.hit[path] = make_uint4(__float_as_uint(m.t_end), m.i, li, SF_HF_HIT);
+        else
+            soa.hit[path] = make_uint4(__float_as_uint(m.t_end), m.i, SF_NO_LIGHT,
+                                       r == MARCH_EXHAUSTED ? SF_HF_EXHAUSTED : 0u);
+        state = TL_IDLE;
+    };
+    // Surface hit of a continuation segment at m.t with sample s: record it, then the normal taps.
+    auto surface_hit = [&](const DeRaw& s) {
+        DeSampleF smp = de_finalize(P, s);
+        soa.hit[path] = make_uint4(__float_as_uint(m.t), m.i, SF_NO_LIGHT, SF_HF_HIT);
+        soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
+        soa.hit_n[path] = make_float4(0.f, 0.f, 0.f, __uint_as_float(smp.iter | (smp.material << 16)));
+        hstep = fmaxf(m.t * S.pixel_cone * 0.5f, 1e-4f) * S.pixel_tolerance;
+        grad = mk3(0.f, 0.f, 0.f);
+        tap = 0;
+        state = TL_NORMAL;
+    };
+
+    while (true) {
+        uint32_t w = warp_fetch(tl.work_counter, state == TL_IDLE);
+        if (state == TL_IDLE) {
+            if (w >= total) {
+                state = TL_DONE;
+            } else {
+                if (first) {
+                    shadow = w >= n_cont;
+                    path = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
+                } else {
+                    uint32_t item = tl.resume[w];
+                    path = item & 0x7fffffffu;
+                    shadow = (item >> 31) != 0;
+                }
+                float4 o = shadow ? soa.sh_o[path] : soa.o[path];
+                float4 d = shadow ? soa.sh_d[path] : soa.d[path];
+                float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
+                if (first) {
+                    float t_end = nearest_emitter(S, ro, rd, shadow ? o.w : S.extent, li);
+                    march_begin(m, ro, rd, t_end);
+                    if (shadow) n_shseg++;
+                    else n_seg++;
+                } else {
+                    uint32_t row = path + (shadow ? cap : 0u);
+                    float4 a = soa.m0[row], b = soa.m1[row];
+                    m.ro = ro; m.rd = rd;
+                    m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
+                    m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
+                    li = soa.m2[row];
+                }
+                budget = quantum;
+                state = TL_MARCH;
+                int r = march_check(m, max_steps, accept);
+                if (r == MARCH_HIT) {
+                    if (shadow) finish(MARCH_HIT);
+                    else { m.t = m.cand_t; state = TL_CAND; }
+                } else if (r != MARCH_CONTINUE) {
+                    finish(r);
+                }
+            }
+        }
+        if (__all_sync(FULL_MASK, state == TL_DONE)) break;
+        if (state == TL_MARCH || state == TL_CAND || state == TL_NORMAL) {
+            float3 q = m.ro + m.rd * m.t;
+            if (state == TL_NORMAL) q = q + tetra_offset(tap) * hstep;
+            DeRaw s = de_form<FORM>(P, q);
+            n_eval++;
+            n_iter += s.iter;
+            uint32_t act = __activemask();
+            uint32_t mx = __reduce_max_sync(act, s.iter);
+            if (lane_id() == (uint32_t)(__ffs(act) - 1)) {
+                n_wcall++;
+                n_slots += (unsigned long long)mx * __popc(act);
+            }
+            if (state == TL_NORMAL) {
+                grad = grad + tetra_offset(tap) * s.d;
+                if (++tap == 4) {
+                    float3 n = normalize3(grad);
+                    float4 hn = soa.hit_n[path];
+                    soa.hit_n[path] = make_float4(n.x, n.y, n.z, hn.w);
+                    state = TL_IDLE;
+                }
+            } else if (state == TL_CAND) {
+                surface_hit(s);
+            } else {
+                int r = march_update(m, s.d, safety, accept, false);
+                if (r == MARCH_HIT) {
+                    if (shadow) finish(MARCH_HIT);
+                    else surface_hit(s);
+                } else if (r != MARCH_CONTINUE) {
+                    finish(r);
+                } else {
+                    r = march_check(m, max_steps, accept);
+                    if (r == MARCH_HIT) {  // candidate accepted at the step budget
+                        if (shadow) finish(MARCH_HIT);
+                        else { m.t = m.cand_t; state = TL_CAND; }
+                    } else if (r != MARCH_CONTINUE) {
+                        finish(r);
+                    } else if (--budget == 0) {
+                        // quantum spent: save the march and hand the segment to the next launch
+                        uint32_t row = path + (shadow ? cap : 0u);
+                        soa.m0[row] = make_float4(m.t, m.omega, m.prev_radius, m.step_len);
+                        soa.m1[row] = make_float4(m.t_end, m.cand_t, m.cand_err, __uint_as_float(m.i));
+                        soa.m2[row] = li;
+                        warp_append(tl.next_resume_count, tl.next_resume, true, path | (shadow ? 0x80000000u : 0u));
+                        state = TL_IDLE;
+                    }
+                }
+            }
+        }
+    }
+    warp_stat(&stats[SF_STAT_DE_EVALS], n_eval);
+    warp_stat(&stats[SF_STAT_DE_ITERS], n_iter);
+    warp_stat(&stats[SF_STAT_SEGMENTS], n_seg + n_shseg);
+    warp_stat(&stats[SF_STAT_SHADOW_SEGMENTS], n_shseg);
+    warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
+    warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
+}
+
+template <int FORM>
+static cudaError_t launch_trace_form(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
+                                     unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
+    switch (min_blocks) {
+    case 3: k_trace<FORM, 3><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
+    case 4: k_trace<FORM, 4><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
+    default: k_trace<FORM, 2><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
+    }
+    return cudaGetLastError();
+}
