@@ -1009,7 +1009,7 @@ struct sf_session {
     size_t mem_bytes = 0;
     std::vector<sf_tile> tiles;
     uint32_t tile_size = 0, dispatches = 0;
-    uint32_t min_blocks = 2, threads = 256, quantum = 64;
+    uint32_t min_blocks = 3, threads = 256, quantum = 128;
     uint32_t status_host = 0;
 };
 
