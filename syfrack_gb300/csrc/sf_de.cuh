@@ -254,12 +254,10 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
         float k = __fdividef(fr2, r2);
         k = r2 < fr2 ? k : 1.0f;
         k = r2 < mr2 ? kmin : k;
-        p = p * k;
-        dr *= k;
-        p = p * sc;
-        dr *= asc;
-        p = p + c;
-        dr += 1.0f;
+        // sphere fold, Scale and AddOrigin as one multiply-add per component
+        const float ks = k * sc;
+        p = mk3(fmaf(p.x, ks, c.x), fmaf(p.y, ks, c.y), fmaf(p.z, ks, c.z));
+        dr = fmaf(dr, k * asc, 1.0f);
         it++;
     }
     s.iter = it;
