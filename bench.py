@@ -259,7 +259,7 @@ def run_ours(args):
                        / (ms_max * 1e-3)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
                     "d2h_bytes_per_step": d2h // args.steps, "call": "Renderer.render (full 64-spp frame)"},
-            "roofline": {"bound": "fp32", "kernel": "k_trace_path", "achieved": achieved, "peak": peak.value,
+            "roofline": {"bound": "fp32", "kernel": "k_trace", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
                          "traffic": None, "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
                          "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
