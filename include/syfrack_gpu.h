@@ -336,6 +336,18 @@ typedef struct sf_deep_zoom_desc {
 } sf_deep_zoom_desc;
 sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth,
                        int reference_f64, uint32_t* iters_f64, float* smooth_f64, uint64_t* rebases);
+/* Deep zoom that allocates nothing; it has no counterpart in the reference. For
+ * callers that cannot let a library call cudaMalloc (hosts that own all device
+ * memory through their own pool; threads that cannot take cudaMalloc's implicit
+ * device-wide synchronisation). Outputs are the caller's DEVICE buffers of
+ * width*height entries; the work is queued on `stream` (a cudaStream_t, NULL for
+ * the legacy default stream) on the current device and the call returns without
+ * waiting. The reference orbit lives in a file-scope device array held by every
+ * GPU that loads the library until exit (1.5 MB): max_iter above 65536 is rejected
+ * with SF_ERR_INVALID. The first call on a device looks that array up, so make it
+ * before any stream capture. All calls share the array: calls that overlap on the
+ * GPU (two streams, two threads) race; order them on one stream. */
+sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth, void* stream);
 
 #ifdef __cplusplus
 }

@@ -106,6 +106,7 @@ SIGNATURES = {
     "sf_planar_probe": [vp, P(sf_planar_desc), fp, C.c_size_t, fp, fp, up],
     "sf_escape2d": [vp, P(sf_planar_desc), P(sf_canvas), abi.sf_tile, u32, fp, fp, up],
     "sf_deep_zoom": [vp, P(sf_deep_zoom_desc), up, fp, C.c_int, up, fp, P(u64)],
+    "sf_deep_zoom_noalloc": [P(sf_deep_zoom_desc), vp, vp, vp],
 }
 _RESTYPES = {"sf_status_string": C.c_char_p, "sf_last_error": C.c_char_p, "sf_abi_version": u32}
 

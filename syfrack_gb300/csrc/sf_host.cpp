@@ -724,6 +724,9 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
 
 }  // namespace
 
+// Error reporting for the other translation units of the library.
+sf_status sf_report_error(sf_status status, const std::string& message) { return fail(status, message); }
+
 // ------------------------------------------------------------------ ABI: basics
 extern "C" const char* sf_status_string(sf_status s) {
     static const char* names[] = {"SF_OK", "SF_ERR_INVALID", "SF_ERR_GRAPH", "SF_ERR_UNSUPPORTED", "SF_ERR_CUDA",

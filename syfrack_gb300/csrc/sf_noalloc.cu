@@ -1,0 +1,83 @@
+// Deep zoom without any device allocation (sf_deep_zoom_noalloc).
+//
+// Some callers cannot let a library call cudaMalloc: hosts that reserve the whole
+// device memory for their own pool at start-up (an embedding renderer or engine that
+// hands out every byte itself), and latency-critical threads where cudaMalloc's
+// implicit device-wide synchronisation is not acceptable. For them this entry point
+// takes the caller's device output buffers and keeps its scratch -- the reference
+// orbit in FP64 and FP32, its length and the statistics counters -- in one
+// file-scope device array, held by every GPU that loads the library until exit.
+#include <cuda_runtime.h>
+
+#include <mutex>
+#include <string>
+
+#include "../../include/syfrack_gpu.h"
+#include "sf_kernels.cuh"
+
+sf_status sf_report_error(sf_status status, const std::string& message);
+
+namespace {
+
+constexpr uint32_t kMaxIter = 65536;  // largest max_iter the scratch holds
+constexpr int kMaxDevices = 64;
+
+struct NoAllocScratch {
+    double2 orbit_d[kMaxIter + 2];
+    float2 orbit_f[kMaxIter + 2];
+    uint32_t orbit_len;
+    uint32_t pad;
+    unsigned long long stats[SF_STAT_COUNT];
+};
+
+// 1.5 MB per device. In host code this name is only a stand-in for the symbol:
+// kernels receive the address cudaGetSymbolAddress returns for the current device.
+static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
+
+std::mutex g_mu;
+NoAllocScratch* g_addr[kMaxDevices] = {};
+
+// Device address of the scratch for the current device, looked up once per device.
+sf_status scratch_address(NoAllocScratch** out) {
+    int dev = 0;
+    cudaError_t e = cudaGetDevice(&dev);
+    if (e != cudaSuccess) return sf_report_error(SF_ERR_CUDA, std::string("cudaGetDevice: ") + cudaGetErrorString(e));
+    if (dev < 0 || dev >= kMaxDevices) return sf_report_error(SF_ERR_INVALID, "device index above 63");
+    std::lock_guard<std::mutex> lk(g_mu);
+    if (!g_addr[dev]) {
+        void* p = nullptr;
+        e = cudaGetSymbolAddress(&p, g_noalloc_scratch);
+        if (e != cudaSuccess || !p)
+            return sf_report_error(SF_ERR_CUDA, std::string("cudaGetSymbolAddress: ") + cudaGetErrorString(e));
+        g_addr[dev] = static_cast<NoAllocScratch*>(p);
+    }
+    *out = g_addr[dev];
+    return SF_OK;
+}
+
+}  // namespace
+
+extern "C" sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth,
+                                          void* stream) {
+    if (!d || !iterations || !smooth) return sf_report_error(SF_ERR_INVALID, "null argument");
+    if (!d->width || !d->height || !d->max_iter) return sf_report_error(SF_ERR_INVALID, "empty deep-zoom request");
+    if (d->max_iter > kMaxIter)
+        return sf_report_error(SF_ERR_INVALID, "max_iter " + std::to_string(d->max_iter) +
+                                                   " exceeds the allocation-free limit of 65536 iterations");
+    if (!(d->bailout >= 2.0f)) return sf_report_error(SF_ERR_INVALID, "bailout must be at least 2");
+    NoAllocScratch* sc = nullptr;
+    sf_status s = scratch_address(&sc);
+    if (s != SF_OK) return s;
+    cudaStream_t st = static_cast<cudaStream_t>(stream);
+    // the counters start at zero; the orbit and its length are written before they are read
+    cudaError_t e = cudaMemsetAsync(sc->stats, 0, sizeof(sc->stats), st);
+    double cx = d->center_hi[0] + d->center_lo[0], cy = d->center_hi[1] + d->center_lo[1];
+    double pitch = d->width_units / double(d->width);
+    if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, sc->orbit_d, sc->orbit_f,
+                                                  &sc->orbit_len, st);
+    if (e == cudaSuccess)
+        e = sf_launch_perturb(sc->orbit_d, sc->orbit_f, &sc->orbit_len, d->width, d->height, float(pitch), 1.0f,
+                              d->max_iter, d->bailout, iterations, smooth, sc->stats, st);
+    if (e != cudaSuccess) return sf_report_error(SF_ERR_CUDA, std::string("sf_deep_zoom_noalloc: ") + cudaGetErrorString(e));
+    return SF_OK;
+}
