@@ -37,6 +37,18 @@ FLOPS_PER_ITER = 31
 FLOPS_PER_EVAL = 29
 
 
+def profiled_traffic():
+    """DRAM bytes per trace launch at 1280x720 from the committed ncu summary (or None)."""
+    path = os.path.join(ROOT, "profiles", "k_trace_mandelbox_640x360_ncu.md")
+    try:
+        for line in open(path):
+            if line.startswith("traffic_bytes_per_launch_1280x720:"):
+                return int(line.split(":")[1])
+    except OSError:
+        pass
+    return None
+
+
 def dist_env():
     n = int(os.environ.get("WORLD_SIZE", "1"))
     r = int(os.environ.get("RANK", "0"))
@@ -261,7 +273,9 @@ def run_ours(args):
                     "d2h_bytes_per_step": d2h // args.steps, "call": "Renderer.render (full 64-spp frame)"},
             "roofline": {"bound": "fp32", "kernel": "k_trace", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
-                         "traffic": None, "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
+                         "traffic": profiled_traffic() if (cfg.width, cfg.height) == (1280, 720) else None,
+                         "traffic_source": "dram__bytes_read+write per k_trace launch, ncu capture at 640x360 x4 "
+                                           "(profiles/k_trace_mandelbox_640x360_ncu.md)", "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
                          "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
                          "de_evals_per_step": st["de_evals"] / args.steps,
                          "de_iterations_per_step": st["de_iterations"] / args.steps,
