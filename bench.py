@@ -293,6 +293,67 @@ def run_ours(args):
     ctx.close()
 
 
+def run_batch(args):
+    """Uneven mixed batch: 64 seeded jobs (Mandelbulb powers 2-12, Mandelbox scales
+    -2.5..2.5, Menger levels 3-7; tiles 64-512 px; 1-16 spp; 2 bounces). Rendered
+    (a) job after job by the per-pixel megakernel (the reference's plain path),
+    (b) job after job by per-job wavefront sessions, (c) as one autotuned batch
+    replayed from a CUDA graph. Wall time from host descriptions to finished films."""
+    from syfrack_gb300 import Batch, GpuContext, Renderer, RenderSession, workloads
+
+    ctx = GpuContext(0)
+    r = Renderer(ctx)
+    jobs = workloads.mixed_batch(seed=7, jobs=args.jobs)
+    for sc, _ in jobs:
+        r.compile(sc.graph)
+
+    def sequential(integrator):
+        ctx.reset_stats()
+        t0 = time.perf_counter()
+        for sc, cfg in jobs:
+            c2 = type(cfg)(**{**cfg.__dict__, "integrator": integrator, "tile_size": 256 if integrator == "megakernel" else cfg.tile_size})
+            s = RenderSession(r, sc, c2)
+            while not s.step(0):
+                pass
+            s.close()
+        dt = time.perf_counter() - t0
+        return ctx.stats()["segments"] / dt / 1e6, dt
+
+    # warm-up of every code path on a few jobs
+    wb = Batch(r, jobs[:3])
+    wb.run(1)
+    wb.sync()
+    wb.close()
+    plain_mk, t_mk = sequential("megakernel")
+    plain_wf, t_wf = sequential("wavefront")
+    b = Batch(r, jobs)
+    mb, q, tune_ms = b.autotune()
+    ctx.reset_stats()
+    t0 = time.perf_counter()
+    b.run(1, use_graph=True)
+    b.sync(600000)
+    t_b = time.perf_counter() - t0
+    segs = ctx.stats()["segments"]
+    batched = segs / t_b / 1e6
+    # steady state: replays of the captured pass (accumulating further samples)
+    ctx.reset_stats()
+    t0 = time.perf_counter()
+    b.run(args.steps, use_graph=True)
+    b.sync(600000)
+    t_r = time.perf_counter() - t0
+    replay = ctx.stats()["segments"] / t_r / 1e6
+    b.close()
+    line = {"metric": METRIC, "workload": f"mixed_batch_{len(jobs)}_jobs", "unit": UNIT, "value": batched,
+            "value_steady_replays": replay, "plain_megakernel": plain_mk, "plain_wavefront_sessions": plain_wf,
+            "speedup_vs_plain_megakernel": batched / plain_mk, "seconds": {"megakernel": t_mk, "wavefront": t_wf,
+            "batch_first_pass": t_b, "batch_replays": t_r, "autotune_ms_best_pass": tune_ms},
+            "autotuned": {"min_blocks_per_sm": mb, "quantum": q}, "segments_per_pass": segs,
+            "paths_per_pass": int(sum(c.width * c.height * c.samples_per_pixel for _, c in jobs)),
+            "dtype": "f32", "data": "synthetic (seeded jobs)"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -306,9 +367,13 @@ def main():
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--workload", default="pathtrace", choices=["pathtrace", "batch"])
+    ap.add_argument("--jobs", type=int, default=64)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
+    elif args.workload == "batch":
+        run_batch(args)
     else:
         run_ours(args)
 

@@ -296,6 +296,31 @@ sf_status sf_session_destroy(sf_session* s);
  * quantum after which an open segment is saved and re-queued (0 = unbounded). */
 sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t threads, uint32_t quantum);
 
+/* ------------------------------------------------------------------ batches
+ * Many jobs -- different graphs, scenes, image sizes and sample counts -- rendered
+ * by one wavefront: one set of persistent trace launches per round covers every
+ * job's paths (the reference renders jobs one after another, each through its own
+ * Renderer/RenderSession, renderer.rs:668-693). A pass renders
+ * cfg.samples_per_dispatch samples of every job; the pass is captured once in a
+ * CUDA graph and replayed. Each job's image is its whole film (tile = image). */
+typedef struct sf_batch sf_batch;
+typedef struct sf_batch_job {
+    sf_graph* graph;
+    sf_scene_desc scene;
+    sf_render_config cfg;
+} sf_batch_job;
+sf_status sf_batch_create(sf_context* ctx, const sf_batch_job* jobs, uint32_t n_jobs, sf_batch** out);
+/* Trace-kernel shape for the batch: resident blocks per SM (2..4) and step quantum. */
+sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks_per_sm, uint32_t quantum);
+/* Autotuner: times one pass per candidate shape (2..4 blocks per SM x quanta 64,
+ * 128, 256), keeps the fastest, clears the films and rewinds the sample indices. */
+sf_status sf_batch_autotune(sf_batch* b, uint32_t* min_blocks_per_sm, uint32_t* quantum, float* best_ms);
+/* Queues `passes` passes (graph replays when use_graph != 0); asynchronous. */
+sf_status sf_batch_run(sf_batch* b, uint32_t passes, int use_graph);
+sf_status sf_batch_sync(sf_batch* b, uint32_t timeout_ms, uint32_t* status_word);
+sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes* out);
+sf_status sf_batch_destroy(sf_batch* b);
+
 /* ------------------------------------------------------------------ escape time
  * PlanarFractal (crates/syfrack-core/src/scene/planar.rs:20-39); family:
  * 0 Julia, 1 Mandelbrot, 2 BurningShip, 3 Newton, 4 Nova, 5 Phoenix. Angles in

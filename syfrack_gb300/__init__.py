@@ -5,11 +5,11 @@ package is its ctypes binding with the reference's Rust API names.
 """
 from . import abi, ron
 from .graph import Graph, Kind, Link, Node
-from .render import (Canvas, CompiledGraph, DeSample, GpuContext, PlanarFractal, RenderOutput, Renderer,
+from .render import (Batch, Canvas, CompiledGraph, DeSample, GpuContext, PlanarFractal, RenderOutput, Renderer,
                      RenderSession, deep_zoom, escape2d)
 from .scene import AreaLight, Camera, Finish, Material, RenderConfig, Scene, SurfaceVariation
 from ._lib import SyfrackError
 
-__all__ = ["abi", "ron", "Graph", "Kind", "Link", "Node", "Canvas", "CompiledGraph", "DeSample", "GpuContext",
+__all__ = ["abi", "ron", "Batch", "Graph", "Kind", "Link", "Node", "Canvas", "CompiledGraph", "DeSample", "GpuContext",
            "PlanarFractal", "RenderOutput", "Renderer", "RenderSession", "deep_zoom", "escape2d", "AreaLight",
            "Camera", "Finish", "Material", "RenderConfig", "Scene", "SurfaceVariation", "SyfrackError"]

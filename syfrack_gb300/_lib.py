@@ -65,6 +65,10 @@ class sf_canvas(C.Structure):
                 ("width", u32), ("height", u32), ("seed", u64)]
 
 
+class sf_batch_job(C.Structure):
+    _fields_ = [("graph", vp), ("scene", abi.sf_scene_desc), ("cfg", abi.sf_render_config)]
+
+
 class sf_deep_zoom_desc(C.Structure):
     _fields_ = [("center_hi", C.c_double * 2), ("center_lo", C.c_double * 2), ("width_units", C.c_double),
                 ("width", u32), ("height", u32), ("max_iter", u32), ("bailout", C.c_float)]
@@ -103,6 +107,13 @@ SIGNATURES = {
     "sf_session_resume": [vp, vp, C.c_char_p, P(vp)],
     "sf_session_destroy": [vp],
     "sf_session_set_launch": [vp, u32, u32, u32],
+    "sf_batch_create": [vp, P(sf_batch_job), u32, P(vp)],
+    "sf_batch_set_launch": [vp, u32, u32],
+    "sf_batch_autotune": [vp, up, up, P(C.c_float)],
+    "sf_batch_run": [vp, u32, C.c_int],
+    "sf_batch_sync": [vp, u32, up],
+    "sf_batch_readback": [vp, u32, P(sf_film_planes)],
+    "sf_batch_destroy": [vp],
     "sf_planar_probe": [vp, P(sf_planar_desc), fp, C.c_size_t, fp, fp, up],
     "sf_escape2d": [vp, P(sf_planar_desc), P(sf_canvas), abi.sf_tile, u32, fp, fp, up],
     "sf_deep_zoom": [vp, P(sf_deep_zoom_desc), up, fp, C.c_int, up, fp, P(u64)],

@@ -546,10 +546,10 @@ struct LaunchTimer {
     sf_context* c;
     cudaEvent_t a = nullptr;
     bool trace;
-    LaunchTimer(sf_context* ctx, bool is_trace) : c(ctx), trace(is_trace) {
+    LaunchTimer(sf_context* ctx, bool is_trace, bool timed = true) : c(ctx), trace(is_trace) {
         c->launches++;
         if (is_trace) c->trace_launches++;
-        if (c->profiling) {
+        if (c->profiling && timed) {
             a = get_event(c);
             cudaEventRecord(a, c->stream);
         }
@@ -1014,6 +1014,7 @@ struct sf_session {
     uint32_t tile_size = 0, dispatches = 0;
     uint32_t min_blocks = 3, threads = 256, quantum = 128;
     uint32_t status_host = 0;
+    double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
 };
 
 namespace {
@@ -1116,15 +1117,9 @@ sf_status session_alloc(sf_session* s) {
     DevScene S;
     scene_dev(s->scene, cfg, s->graph->info, S);
     CU(cudaMemcpyAsync(s->d_scene, &S, sizeof S, cudaMemcpyHostToDevice, c->stream));
-    CU(cudaMemsetAsync(s->film.accum, 0, px * 16, c->stream));
     // depth = -1 and aux = (0,0,0,-1) until sample 0 lands (RenderOutput conventions)
-    std::vector<float> init(px * 4);
-    for (size_t i = 0; i < px; ++i) { init[4 * i] = 0; init[4 * i + 1] = 0; init[4 * i + 2] = 0; init[4 * i + 3] = -1; }
-    CU(cudaMemcpyAsync(s->film.aux, init.data(), px * 16, cudaMemcpyHostToDevice, c->stream));
-    std::vector<float> dinit(px, -1.0f);
-    CU(cudaMemcpyAsync(s->film.depth, dinit.data(), px * 4, cudaMemcpyHostToDevice, c->stream));
+    CU(sf_launch_film_clear(s->film, c->stream));
     CU(cudaMemsetAsync(s->status, 0, 16, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
     tile_grid(s);
     return SF_OK;
 }
@@ -1254,6 +1249,10 @@ extern "C" sf_status sf_session_step(sf_session* s, uint32_t budget_ms, int* don
     if (!s) return fail(SF_ERR_INVALID, "null session");
     auto t0 = std::chrono::steady_clock::now();
     const uint32_t target = s->cfg.samples_per_pixel;
+    // Dispatches are queued on the session stream without waiting for each one; the
+    // host waits when the queued work is predicted to reach the budget (from the
+    // measured cost of earlier dispatches), then checks the budget on the wall clock.
+    double queued_ms = 0.0;
     for (;;) {
         // TileGrid::next_pending (tiles.rs:52-59): least-advanced tile below target, lowest index.
         int best = -1;
@@ -1264,12 +1263,23 @@ extern "C" sf_status sf_session_step(sf_session* s, uint32_t budget_ms, int* don
         uint32_t n = std::min(s->cfg.samples_per_dispatch, target - t.done);
         sf_status st = sf_session_dispatch(s, t, n);
         if (st != SF_OK) return st;
-        st = sf_session_sync(s, 10000, nullptr);  // DISPATCH_TIMEOUT, renderer.rs:236
-        if (st != SF_OK) return st;
         t.done += n;
+        double per_path_ms = s->ms_per_path > 0 ? s->ms_per_path : 0.0;
+        queued_ms += per_path_ms * double(t.w) * t.h * n;
         double el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
-        if (budget_ms && el >= budget_ms) break;
+        if (per_path_ms == 0.0 || !budget_ms || el + queued_ms >= budget_ms) {
+            auto w0 = std::chrono::steady_clock::now();
+            st = sf_session_sync(s, 10000, nullptr);  // DISPATCH_TIMEOUT, renderer.rs:236
+            if (st != SF_OK) return st;
+            double waited = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - w0).count();
+            if (per_path_ms == 0.0) s->ms_per_path = (waited + 1e-3) / (double(t.w) * t.h * n);
+            queued_ms = 0.0;
+            el = std::chrono::duration<double, std::milli>(std::chrono::steady_clock::now() - t0).count();
+            if (budget_ms && el >= budget_ms) break;
+        }
     }
+    sf_status st = sf_session_sync(s, 10000, nullptr);
+    if (st != SF_OK) return st;
     bool complete = true;
     for (auto& t : s->tiles)
         if (t.done < target) complete = false;
@@ -1732,5 +1742,329 @@ extern "C" sf_status sf_device_fp32_peak(sf_context* c, double* tflops) {
     if (e != cudaSuccess) return cuda_fail(e, "fp32 peak probe");
     double flops = double(blocks) * 256.0 * iters * 16.0 * 8.0 * 2.0;
     *tflops = flops / (best * 1e-3) / 1e12;
+    return SF_OK;
+}
+
+// ------------------------------------------------------------------ batches
+struct sf_batch {
+    sf_context* ctx = nullptr;
+    std::vector<sf_graph*> graphs;
+    std::vector<BatchJob> jobs;       // host copy (initial sample_start)
+    std::vector<sf_render_config> cfgs;
+    BatchTable bt{};
+    PathSoA soa{};
+    uint32_t capacity = 0, rounds = 0, max_steps = 0;
+    uint32_t* lists = nullptr;
+    uint32_t* resume = nullptr;
+    uint32_t* counts = nullptr;
+    uint32_t* qcounts = nullptr;
+    uint32_t* status = nullptr;
+    void* mem = nullptr;
+    size_t mem_bytes = 0;
+    bool any_generic = false;
+    uint32_t min_blocks = 3, quantum = 128;
+    cudaGraphExec_t exec = nullptr;
+    uint32_t status_host = 0;
+};
+
+namespace {
+
+// One pass of the batch on the context stream: every job renders its samples.
+sf_status batch_record_pass(sf_batch* b, bool timed) {
+    sf_context* c = b->ctx;
+    cudaStream_t st = c->stream;
+    const size_t N = b->capacity;
+    const uint32_t R = b->rounds;
+    const uint32_t Q = b->quantum ? std::min<uint32_t>((b->max_steps + b->quantum - 1) / b->quantum + 1, 64) : 1;
+    CU(cudaMemsetAsync(b->counts, 0, size_t(R + 1) * 16, st));
+    CU(cudaMemsetAsync(b->qcounts, 0, size_t(R) * 64 * 2 * 4, st));
+    {
+        LaunchTimer t(c, false, timed);
+        CU(sf_launch_generate_batch(b->bt, b->soa, b->counts, st));
+    }
+    const int blocks = int(b->min_blocks) * c->sm_count;
+    for (uint32_t r = 0; r < R; ++r) {
+        uint32_t cur = r & 1, nxt = cur ^ 1;
+        RoundQueues q;
+        q.active = r == 0 ? nullptr : b->lists + (cur * 3 + 0) * N;
+        q.cont = r == 0 ? nullptr : b->lists + (cur * 3 + 1) * N;
+        q.shadow = b->lists + (cur * 3 + 2) * N;
+        q.counts = b->counts + 4 * r;
+        q.next_active = b->lists + (nxt * 3 + 0) * N;
+        q.next_cont = b->lists + (nxt * 3 + 1) * N;
+        q.next_shadow = b->lists + (nxt * 3 + 2) * N;
+        q.next_counts = b->counts + 4 * (r + 1);
+        q.work_counter = b->counts + 4 * r + 3;
+        for (uint32_t j = 0; j < Q; ++j) {
+            TraceLaunch tl;
+            tl.q = q;
+            uint32_t* qc = b->qcounts + (size_t(r) * 64 + j) * 2;
+            tl.work_counter = qc;
+            tl.resume = j == 0 ? nullptr : b->resume + size_t((j - 1) & 1) * 2 * N;
+            tl.resume_count = j == 0 ? nullptr : qc - 2 + 1;
+            tl.next_resume = b->resume + size_t(j & 1) * 2 * N;
+            tl.next_resume_count = qc + 1;
+            tl.quantum = j + 1 == Q ? 0u : b->quantum;
+            LaunchTimer t(c, true, timed);
+            CU(sf_launch_trace_batch(b->bt, b->soa, tl, c->d_stats, blocks, int(b->min_blocks), b->any_generic ? 1 : 0,
+                                     st));
+        }
+        LaunchTimer t(c, false, timed);
+        CU(sf_launch_shade_batch(b->bt, b->soa, q, b->status, r + 1 == R ? 1 : 0, st));
+    }
+    {
+        LaunchTimer t(c, false, timed);
+        CU(sf_launch_commit_batch(b->bt, b->soa, st));
+    }
+    LaunchTimer t(c, false, timed);
+    CU(sf_launch_advance_batch(b->bt, st));
+    return SF_OK;
+}
+
+sf_status batch_reset(sf_batch* b) {
+    sf_context* c = b->ctx;
+    CU(cudaMemcpyAsync(b->bt.jobs, b->jobs.data(), b->jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice,
+                       c->stream));
+    for (auto& j : b->jobs) CU(sf_launch_film_clear(j.film, c->stream));
+    CU(cudaMemsetAsync(b->status, 0, 16, c->stream));
+    b->status_host = 0;
+    return SF_OK;
+}
+
+void batch_drop_graph(sf_batch* b) {
+    if (b->exec) {
+        cudaGraphExecDestroy(b->exec);
+        b->exec = nullptr;
+    }
+}
+
+}  // namespace
+
+extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, uint32_t n, sf_batch** out) {
+    if (!c || !jobs || !out) return fail(SF_ERR_INVALID, "null argument");
+    *out = nullptr;
+    if (n == 0 || n > SF_BATCH_MAX_JOBS) return fail(SF_ERR_INVALID, "a batch holds 1 to 1024 jobs");
+    uint64_t paths = 0, pixels = 0, film_bytes = 0;
+    uint32_t rounds = 0, max_steps = 0;
+    bool generic = false;
+    for (uint32_t i = 0; i < n; ++i) {
+        if (!jobs[i].graph || jobs[i].graph->ctx != c) return fail(SF_ERR_INVALID, "job graph missing or of another context");
+        sf_status st = validate_config(jobs[i].cfg);
+        if (st != SF_OK) return st;
+        if (jobs[i].scene.light_count > SF_MAX_LIGHTS || jobs[i].scene.finish_count > SF_MAX_FINISHES)
+            return fail(SF_ERR_INVALID, "too many lights or finishes");
+        const sf_render_config& cf = jobs[i].cfg;
+        uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
+                                                   cf.samples_per_pixel), 1);
+        paths += uint64_t(cf.width) * cf.height * spd;
+        pixels += uint64_t(cf.width) * cf.height;
+        film_bytes += ((uint64_t(cf.width) * cf.height * 36 + 255) & ~uint64_t(255));
+        rounds = std::max(rounds, cf.max_bounces + 2);
+        max_steps = std::max(max_steps, cf.max_steps);
+        generic |= jobs[i].graph->prog.form == SF_FORM_GENERIC;
+    }
+    if (paths > 0x7fffffffull) return fail(SF_ERR_INVALID, "batch too large (2^31 paths)");
+    cudaSetDevice(c->device);
+    auto* b = new sf_batch();
+    b->ctx = c;
+    b->capacity = uint32_t(paths);
+    b->rounds = rounds;
+    b->max_steps = max_steps;
+    b->any_generic = generic;
+    const size_t N = b->capacity;
+    size_t off = 0;
+    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
+    size_t o_jobs = take(n * sizeof(BatchJob)), o_scenes = take(n * sizeof(DevScene));
+    size_t o_films = take(film_bytes);
+    size_t o_Ls = take(N * 16), o_soa = take(N * 16 * 12), o_lists = take(N * 4 * 6);
+    size_t o_march = take(2 * N * (16 + 16 + 4)), o_resume = take(2 * 2 * N * 4);
+    size_t o_counts = take(size_t(rounds + 1) * 16), o_qcounts = take(size_t(rounds) * 64 * 8), o_status = take(16);
+    sf_status st = ctx_alloc(c, off, &b->mem);
+    if (st != SF_OK) { delete b; return st; }
+    b->mem_bytes = off;
+    char* base = static_cast<char*>(b->mem);
+    b->bt.jobs = reinterpret_cast<BatchJob*>(base + o_jobs);
+    b->bt.n_jobs = n;
+    b->bt.total_paths = uint32_t(paths);
+    b->bt.total_pixels = uint32_t(pixels);
+    DevScene* d_scenes = reinterpret_cast<DevScene*>(base + o_scenes);
+    std::vector<DevScene> scenes(n);
+    char* film = base + o_films;
+    uint32_t pbeg = 0, xbeg = 0;
+    for (uint32_t i = 0; i < n; ++i) {
+        const sf_render_config& cf = jobs[i].cfg;
+        uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
+                                                   cf.samples_per_pixel), 1);
+        scene_dev(jobs[i].scene, cf, jobs[i].graph->info, scenes[i]);
+        BatchJob j{};
+        j.prog = jobs[i].graph->d_prog;
+        j.scene = d_scenes + i;
+        size_t px = size_t(cf.width) * cf.height;
+        j.film.accum = reinterpret_cast<float4*>(film);
+        j.film.depth = reinterpret_cast<float*>(film + px * 16);
+        j.film.aux = reinterpret_cast<float4*>(film + px * 20);
+        j.film.width = cf.width;
+        j.film.height = cf.height;
+        film += (px * 36 + 255) & ~size_t(255);
+        j.geom = DispatchGeom{0, 0, cf.width, cf.height, 0, spd, uint32_t(px * spd)};
+        j.path_begin = pbeg;
+        j.pixel_begin = xbeg;
+        j.form = jobs[i].graph->prog.form;
+        pbeg += uint32_t(px * spd);
+        xbeg += uint32_t(px);
+        b->jobs.push_back(j);
+        b->cfgs.push_back(cf);
+        b->graphs.push_back(jobs[i].graph);
+        graph_retain(jobs[i].graph);
+    }
+    b->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
+    float4* p = reinterpret_cast<float4*>(base + o_soa);
+    b->soa.o = p; p += N;
+    b->soa.d = p; p += N;
+    b->soa.tp = p; p += N;
+    b->soa.L = p; p += N;
+    b->soa.pn = p; p += N;
+    b->soa.sh_o = p; p += N;
+    b->soa.sh_d = p; p += N;
+    b->soa.sh_c = p; p += N;
+    b->soa.hit = reinterpret_cast<uint4*>(p); p += N;
+    b->soa.hit_tr = p; p += N;
+    b->soa.hit_n = p; p += N;
+    b->soa.vis = reinterpret_cast<uint32_t*>(p);
+    float4* m = reinterpret_cast<float4*>(base + o_march);
+    b->soa.m0 = m;
+    b->soa.m1 = m + 2 * N;
+    b->soa.m2 = reinterpret_cast<uint32_t*>(m + 4 * N);
+    b->soa.capacity = b->capacity;
+    b->lists = reinterpret_cast<uint32_t*>(base + o_lists);
+    b->resume = reinterpret_cast<uint32_t*>(base + o_resume);
+    b->counts = reinterpret_cast<uint32_t*>(base + o_counts);
+    b->qcounts = reinterpret_cast<uint32_t*>(base + o_qcounts);
+    b->status = reinterpret_cast<uint32_t*>(base + o_status);
+    ctx_retain(c);
+    cudaError_t e = cudaMemcpyAsync(d_scenes, scenes.data(), n * sizeof(DevScene), cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess) st = batch_reset(b);
+    if (e == cudaSuccess && st == SF_OK) e = cudaStreamSynchronize(c->stream);
+    if (e != cudaSuccess || st != SF_OK) {
+        sf_batch_destroy(b);
+        return e != cudaSuccess ? cuda_fail(e, "batch upload") : st;
+    }
+    *out = b;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks, uint32_t quantum) {
+    if (!b) return fail(SF_ERR_INVALID, "null batch");
+    if (min_blocks < 2 || min_blocks > 4) return fail(SF_ERR_INVALID, "2..4 resident blocks per SM");
+    if (quantum != 0 && quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
+    if (b->min_blocks != min_blocks || b->quantum != quantum) batch_drop_graph(b);
+    b->min_blocks = min_blocks;
+    b->quantum = quantum;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_batch_run(sf_batch* b, uint32_t passes, int use_graph) {
+    if (!b) return fail(SF_ERR_INVALID, "null batch");
+    sf_context* c = b->ctx;
+    cudaSetDevice(c->device);
+    for (uint32_t i = 0; i < passes; ++i) {
+        if (!use_graph) {
+            sf_status st = batch_record_pass(b, true);
+            if (st != SF_OK) return st;
+            continue;
+        }
+        if (!b->exec) {
+            cudaGraph_t g = nullptr;
+            CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
+            sf_status st = batch_record_pass(b, false);
+            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
+            if (st != SF_OK) { if (g) cudaGraphDestroy(g); return st; }
+            if (e != cudaSuccess) return cuda_fail(e, "graph capture");
+            e = cudaGraphInstantiate(&b->exec, g, 0);
+            cudaGraphDestroy(g);
+            if (e != cudaSuccess) { b->exec = nullptr; return cuda_fail(e, "graph instantiate"); }
+        }
+        LaunchTimer t(c, false);
+        CU(cudaGraphLaunch(b->exec, c->stream));
+    }
+    return SF_OK;
+}
+
+extern "C" sf_status sf_batch_sync(sf_batch* b, uint32_t timeout_ms, uint32_t* status_word) {
+    if (!b) return fail(SF_ERR_INVALID, "null batch");
+    sf_context* c = b->ctx;
+    cudaSetDevice(c->device);
+    sf_status st = wait_stream(c->stream, timeout_ms);
+    if (st != SF_OK) return st;
+    uint32_t w = 0;
+    CU(cudaMemcpy(&w, b->status, 4, cudaMemcpyDeviceToHost));
+    b->status_host |= w;
+    if (status_word) *status_word = b->status_host;
+    if (b->status_host) return fail(SF_ERR_WAVEFRONT, "wavefront invariant word " + std::to_string(b->status_host));
+    return SF_OK;
+}
+
+extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t* best_q, float* best_ms) {
+    if (!b) return fail(SF_ERR_INVALID, "null batch");
+    sf_context* c = b->ctx;
+    cudaSetDevice(c->device);
+    cudaEvent_t e0, e1;
+    CU(cudaEventCreate(&e0));
+    CU(cudaEventCreate(&e1));
+    float best = 1e30f;
+    uint32_t bm = b->min_blocks, bq = b->quantum;
+    const uint32_t mbs[3] = {2, 3, 4}, qs[3] = {64, 128, 256};
+    for (uint32_t mb : mbs)
+        for (uint32_t q : qs) {
+            b->min_blocks = mb;
+            b->quantum = q;
+            cudaEventRecord(e0, c->stream);
+            sf_status st = batch_record_pass(b, false);
+            cudaEventRecord(e1, c->stream);
+            if (st != SF_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
+            cudaError_t e = cudaEventSynchronize(e1);
+            float ms = 0;
+            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
+            if (e != cudaSuccess) { cudaEventDestroy(e0); cudaEventDestroy(e1); return cuda_fail(e, "autotune"); }
+            if (ms < best) { best = ms; bm = mb; bq = q; }
+        }
+    cudaEventDestroy(e0);
+    cudaEventDestroy(e1);
+    batch_drop_graph(b);
+    b->min_blocks = bm;
+    b->quantum = bq;
+    sf_status st = batch_reset(b);
+    if (st != SF_OK) return st;
+    CU(cudaStreamSynchronize(c->stream));
+    if (best_mb) *best_mb = bm;
+    if (best_q) *best_q = bq;
+    if (best_ms) *best_ms = best;
+    return SF_OK;
+}
+
+extern "C" sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes* out) {
+    if (!b || !out) return fail(SF_ERR_INVALID, "null argument");
+    if (job >= b->jobs.size()) return fail(SF_ERR_INVALID, "job index out of range");
+    sf_context* c = b->ctx;
+    cudaSetDevice(c->device);
+    const FilmPlanes& f = b->jobs[job].film;
+    size_t px = size_t(f.width) * f.height;
+    if (out->accum) CU(cudaMemcpyAsync(out->accum, f.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
+    if (out->depth) CU(cudaMemcpyAsync(out->depth, f.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
+    if (out->aux) CU(cudaMemcpyAsync(out->aux, f.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
+    CU(cudaStreamSynchronize(c->stream));
+    return SF_OK;
+}
+
+extern "C" sf_status sf_batch_destroy(sf_batch* b) {
+    if (!b) return SF_OK;
+    sf_context* c = b->ctx;
+    cudaSetDevice(c->device);
+    cudaStreamSynchronize(c->stream);
+    batch_drop_graph(b);
+    ctx_free(c, b->mem, b->mem_bytes);
+    for (sf_graph* g : b->graphs) sf_graph_destroy(g);
+    delete b;
+    ctx_release(c);
     return SF_OK;
 }

@@ -6,7 +6,10 @@
 #include "sf_kernels.cuh"
 #include "sf_trace.cuh"
 
+#include "sf_stages.cuh"
 #include "sf_warp.cuh"
+
+static unsigned grid_for(size_t n, unsigned threads, unsigned per_sm);
 
 // ------------------------------------------------------------------ DE probe
 // de_probe.wgsl:9-17 / Renderer::probe_distances: one thread per point.
@@ -147,41 +150,6 @@ __global__ void __launch_bounds__(256) k_primary(const DeProgram* __restrict__ p
 }
 
 // ------------------------------------------------------------------ wavefront stages
-static __device__ __forceinline__ void path_pixel(const DispatchGeom& g, uint32_t path, uint32_t& px, uint32_t& py,
-                                                  uint32_t& sample) {
-    uint32_t tile_px = g.tile_w * g.tile_h;
-    uint32_t local = path % tile_px;
-    sample = g.sample_start + path / tile_px;
-    px = g.tile_x + local % g.tile_w;
-    py = g.tile_y + local / g.tile_w;
-}
-
-static __device__ __forceinline__ void store_path(PathSoA& soa, uint32_t path, const PathState& ps, uint32_t flags) {
-    soa.o[path] = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.prev_pdf);
-    soa.d[path] = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.prev_area_total);
-    soa.tp[path] = make_float4(ps.tp.x, ps.tp.y, ps.tp.z, __uint_as_float(ps.rng));
-    uint32_t f = flags | (ps.prev_from_bsdf ? SF_PF_FROM_BSDF : 0u);
-    soa.L[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, __uint_as_float(ps.bounce | (f << 16)));
-    soa.pn[path] = make_float4(ps.prev_normal.x, ps.prev_normal.y, ps.prev_normal.z, 0.f);
-}
-static __device__ __forceinline__ uint32_t load_path(const PathSoA& soa, uint32_t path, PathState& ps) {
-    float4 o = soa.o[path], d = soa.d[path], tp = soa.tp[path], L = soa.L[path], pn = soa.pn[path];
-    ps.o = mk3(o.x, o.y, o.z);
-    ps.prev_pdf = o.w;
-    ps.d = mk3(d.x, d.y, d.z);
-    ps.prev_area_total = d.w;
-    ps.tp = mk3(tp.x, tp.y, tp.z);
-    ps.rng = __float_as_uint(tp.w);
-    ps.L = mk3(L.x, L.y, L.z);
-    uint32_t bits = __float_as_uint(L.w);
-    ps.bounce = bits & 0xffffu;
-    uint32_t flags = bits >> 16;
-    ps.prev_from_bsdf = (flags & SF_PF_FROM_BSDF) != 0;
-    ps.prev_normal = mk3(pn.x, pn.y, pn.z);
-    return flags;
-}
-
-// wf_generate (wavefront.wgsl:160-179): camera ray and RNG per path.
 __global__ void __launch_bounds__(256) k_generate(const DevScene* __restrict__ scene_g, PathSoA soa, DispatchGeom g,
                                                   uint32_t* counts) {
     __shared__ DevScene S;
@@ -194,16 +162,11 @@ __global__ void __launch_bounds__(256) k_generate(const DevScene* __restrict__ s
         counts[2] = 0;
     }
     if (path >= g.paths) return;
-    uint32_t px, py, sample;
-    path_pixel(g, path, px, py, sample);
-    PathState ps;
-    path_begin(S, ps, px, py, sample);
-    store_path(soa, path, ps, SF_PF_CONT);
+    generate_path(S, soa, g, path, path);
 }
 
-// wf_shade + wf_compact (wavefront.wgsl:196-223): resolve last round's shadow
-// segment, run the bounce body on this round's hit, and compact the surviving
-// paths into the next round's queues with one atomic per warp and list.
+// Shade, then compact the surviving paths into the next round's queues with one
+// atomic per warp and list.
 __global__ void __launch_bounds__(256) k_shade(const DevScene* __restrict__ scene_g, PathSoA soa, RoundQueues q,
                                                DispatchGeom g, FilmPlanes film, uint32_t* status, int final_round) {
     __shared__ DevScene S;
@@ -212,82 +175,30 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene* __restrict__ scen
     const uint32_t n = q.counts[0];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         uint32_t path = q.active ? q.active[j] : j;
-        PathState ps;
-        uint32_t flags = load_path(soa, path, ps);
-        if ((flags & SF_PF_SHADOW) && soa.vis[path]) {
-            float4 c = soa.sh_c[path];
-            ps.L = ps.L + mk3(c.x, c.y, c.z);
-        }
-        uint32_t nf = 0;
-        if (flags & SF_PF_CONT) {
-            uint4 hr = soa.hit[path];
-            HitInfo h;
-            h.t = __uint_as_float(hr.x);
-            h.steps = hr.y;
-            h.light_index = hr.z;
-            h.hit = (hr.w & SF_HF_HIT) != 0;
-            h.exhausted = (hr.w & SF_HF_EXHAUSTED) != 0;
-            if (h.hit && h.light_index == SF_NO_LIGHT) {
-                float4 tr = soa.hit_tr[path], hn = soa.hit_n[path];
-                h.sample.traps[0] = tr.x; h.sample.traps[1] = tr.y; h.sample.traps[2] = tr.z; h.sample.traps[3] = tr.w;
-                uint32_t im = __float_as_uint(hn.w);
-                h.sample.iter = im & 0xffffu;
-                h.sample.material = im >> 16;
-                h.sample.d = 0.f;
-                h.n = mk3(hn.x, hn.y, hn.z);
-            }
-            uint32_t px, py, sample;
-            path_pixel(g, path, px, py, sample);
-            float* fd = nullptr;
-            float4* fa = nullptr;
-            if (sample == 0 && ps.bounce == 0) {
-                size_t idx = (size_t)py * film.width + px;
-                fd = film.depth + idx;
-                fa = film.aux + idx;
-            }
-            ShadowReq sh;
-            int r = bounce_body(S, ps, h, sh, fd, fa);
-            if (sh.active) {
-                soa.sh_o[path] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.t_end);
-                soa.sh_d[path] = make_float4(sh.dir.x, sh.dir.y, sh.dir.z, 0.f);
-                soa.sh_c[path] = make_float4(sh.contrib.x, sh.contrib.y, sh.contrib.z, 0.f);
-                nf |= SF_PF_SHADOW;
-            }
-            if (r == PATH_CONTINUE) nf |= SF_PF_CONT;
-        }
-        if (final_round && nf) {
-            atomicOr(status, SF_WF_ALIVE_AT_COMMIT);
-            nf = 0;
-        }
-        store_path(soa, path, ps, nf);
-        if (!nf) soa.Ls[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
-        if (!final_round) {
-            warp_append(&q.next_counts[0], q.next_active, nf != 0, path);
-            warp_append(&q.next_counts[1], q.next_cont, (nf & SF_PF_CONT) != 0, path);
-            warp_append(&q.next_counts[2], q.next_shadow, (nf & SF_PF_SHADOW) != 0, path);
-        }
+        uint32_t nf = shade_path(S, soa, g, film, path, path, status, final_round);
+        if (!final_round) enqueue_next(q, nf, path);
     }
 }
 
-// wf_commit (wavefront.wgsl:232-260): ordered per-sample film add, ascending
-// sample order, non-finite samples contribute (0, 1).
 __global__ void __launch_bounds__(256) k_commit(PathSoA soa, DispatchGeom g, FilmPlanes film) {
-    uint32_t tile_px = g.tile_w * g.tile_h;
     uint32_t local = blockIdx.x * blockDim.x + threadIdx.x;
-    if (local >= tile_px) return;
-    uint32_t px = g.tile_x + local % g.tile_w, py = g.tile_y + local / g.tile_w;
-    size_t idx = (size_t)py * film.width + px;
-    float4 acc = film.accum[idx];
-    for (uint32_t s = 0; s < g.samples; ++s) {
-        float4 L = soa.Ls[(size_t)s * tile_px + local];
-        bool ok = L.x == L.x && L.y == L.y && L.z == L.z && fabsf(L.x) < 1e30f && fabsf(L.y) < 1e30f &&
-                  fabsf(L.z) < 1e30f;
-        acc.x += ok ? L.x : 0.0f;
-        acc.y += ok ? L.y : 0.0f;
-        acc.z += ok ? L.z : 0.0f;
-        acc.w += 1.0f;
+    if (local >= g.tile_w * g.tile_h) return;
+    commit_pixel(soa, g, film, local, 0);
+}
+
+// Film reset: accum = 0, depth = -1, aux = (0, 0, 0, -1) (RenderOutput's miss conventions).
+__global__ void __launch_bounds__(256) k_film_clear(FilmPlanes film) {
+    size_t n = (size_t)film.width * film.height;
+    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
+        film.accum[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        film.depth[i] = -1.0f;
+        film.aux[i] = make_float4(0.f, 0.f, 0.f, -1.0f);
     }
-    film.accum[idx] = acc;
+}
+cudaError_t sf_launch_film_clear(FilmPlanes film, cudaStream_t st) {
+    size_t n = (size_t)film.width * film.height;
+    k_film_clear<<<grid_for(n, 256, 8), 256, 0, st>>>(film);
+    return cudaGetLastError();
 }
 
 // ------------------------------------------------------------------ megakernel

@@ -94,6 +94,28 @@ struct CanvasDev {
     uint32_t width, height, seed;
 };
 
+// One job of a batched wavefront: its graph, scene, film and tile, and where its
+// paths and pixels start in the batch's shared index spaces. Lives in device memory
+// (the graph replay advances sample_start there).
+struct BatchJob {
+    const DeProgram* prog;
+    const DevScene* scene;
+    FilmPlanes film;
+    DispatchGeom geom;
+    uint32_t path_begin;
+    uint32_t pixel_begin;
+    uint32_t form;
+    uint32_t pad;
+};
+#define SF_BATCH_MAX_JOBS 1024
+struct BatchTable {
+    BatchJob* jobs;
+    uint32_t n_jobs;
+    uint32_t total_paths;
+    uint32_t total_pixels;
+    uint32_t pad;
+};
+
 // ---- launchers (return cudaError_t of the launch) ----
 cudaError_t sf_launch_de_probe(const DeProgram* prog, const float* x, const float* y, const float* z, size_t n,
                                float* dist, float* traps, uint32_t* iters, uint32_t* mats, cudaStream_t st);
@@ -113,9 +135,18 @@ cudaError_t sf_launch_trace_menger(const DeProgram*, const DevScene*, PathSoA, T
                                    int, cudaStream_t);
 cudaError_t sf_launch_trace_any(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
                                 cudaStream_t);
+// Batched wavefront (sf_batch.cu): all jobs' paths in one set of launches.
+cudaError_t sf_launch_generate_batch(BatchTable bt, PathSoA soa, uint32_t* counts, cudaStream_t st);
+cudaError_t sf_launch_trace_batch(BatchTable bt, PathSoA soa, TraceLaunch tl, unsigned long long* stats, int blocks,
+                                  int min_blocks, int any_generic, cudaStream_t st);
+cudaError_t sf_launch_shade_batch(BatchTable bt, PathSoA soa, RoundQueues q, uint32_t* status, int final_round,
+                                  cudaStream_t st);
+cudaError_t sf_launch_commit_batch(BatchTable bt, PathSoA soa, cudaStream_t st);
+cudaError_t sf_launch_advance_batch(BatchTable bt, cudaStream_t st);
 cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
                             uint32_t* status, int final_round, cudaStream_t st);
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st);
+cudaError_t sf_launch_film_clear(FilmPlanes film, cudaStream_t st);
 cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, PathSoA soa, DispatchGeom g,
                                  FilmPlanes film, unsigned long long* stats, cudaStream_t st);
 cudaError_t sf_launch_planar(const PlanarDev* f, const float* x, const float* y, size_t n, float* dist, float* traps,

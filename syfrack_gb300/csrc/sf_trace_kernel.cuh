@@ -17,31 +17,65 @@
 
 enum { TL_IDLE = 0, TL_MARCH = 1, TL_CAND = 2, TL_NORMAL = 3, TL_DONE = 4 };
 #define SF_FORM_ANY 99u
+#define SF_FORM_MIXED 98u  // any of the three iterated forms, chosen per lane
 
 template <int FORM>
 __device__ __forceinline__ DeRaw de_form(const DeProgram& P, float3 p) {
     if constexpr (FORM == SF_FORM_BULB) return de_bulb(P.fp, p);
     else if constexpr (FORM == SF_FORM_BOX) return de_box(P.fp, p);
     else if constexpr (FORM == SF_FORM_MENGER) return de_menger(P.fp, p);
-    else return de_raw(P, p);
+    else if constexpr (FORM == SF_FORM_MIXED) {
+        switch (P.form) {
+        case SF_FORM_BULB: return de_bulb(P.fp, p);
+        case SF_FORM_BOX: return de_box(P.fp, p);
+        default: return de_menger(P.fp, p);
+        }
+    } else return de_raw(P, p);
 }
 
-template <int FORM, int MIN_BLOCKS>
+// Job of a batched path: binary search of the jobs' first paths (staged in shared memory).
+static __device__ __forceinline__ uint32_t find_job(const uint32_t* begins, uint32_t n, uint32_t path) {
+    uint32_t lo = 0, hi = n;
+    while (hi - lo > 1) {
+        uint32_t mid = (lo + hi) >> 1;
+        if (begins[mid] <= path) lo = mid;
+        else hi = mid;
+    }
+    return lo;
+}
+
+// MULTI: the work items belong to the jobs of a batch (bt); each lane reads its job's
+// program and scene (L1-cached global memory) when it takes an item.
+template <int FORM, int MIN_BLOCKS, bool MULTI = false>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __restrict__ prog_g,
                                                            const DevScene* __restrict__ scene_g, PathSoA soa,
-                                                           TraceLaunch tl, unsigned long long* stats) {
+                                                           TraceLaunch tl, unsigned long long* stats,
+                                                           BatchTable bt = BatchTable{}) {
     __shared__ DeProgram P;
     __shared__ DevScene S;
-    stage_program(P, prog_g);
-    stage_pod(S, scene_g);
+    __shared__ uint32_t begins[MULTI ? SF_BATCH_MAX_JOBS : 1];
+    if constexpr (MULTI) {
+        for (uint32_t i = threadIdx.x; i < bt.n_jobs; i += blockDim.x) begins[i] = bt.jobs[i].path_begin;
+    } else {
+        stage_program(P, prog_g);
+        stage_pod(S, scene_g);
+    }
     __syncthreads();
     const bool first = tl.resume == nullptr;
     const uint32_t n_cont = first ? tl.q.counts[1] : 0u;
     const uint32_t total = first ? n_cont + tl.q.counts[2] : *tl.resume_count;
     const uint32_t quantum = tl.quantum ? tl.quantum : 0xffffffffu;
-    const float accept = S.pixel_cone * S.pixel_tolerance;
-    const float safety = S.step_scale;
-    const uint32_t max_steps = S.max_steps;
+    const DeProgram* Pl = &P;
+    const DevScene* Sl = &S;
+    float accept = 0.f, safety = 0.f, cone = 0.f, tol = 0.f;
+    uint32_t max_steps = 0;
+    if constexpr (!MULTI) {
+        accept = S.pixel_cone * S.pixel_tolerance;
+        safety = S.step_scale;
+        max_steps = S.max_steps;
+        cone = S.pixel_cone;
+        tol = S.pixel_tolerance;
+    }
     const uint32_t cap = soa.capacity;
 
     uint32_t state = TL_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
@@ -63,11 +97,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     };
     // Surface hit of a continuation segment at m.t with sample s: record it, then the normal taps.
     auto surface_hit = [&](const DeRaw& s) {
-        DeSampleF smp = de_finalize(P, s);
+        DeSampleF smp = de_finalize(*Pl, s);
         soa.hit[path] = make_uint4(__float_as_uint(m.t), m.i, SF_NO_LIGHT, SF_HF_HIT);
         soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
         soa.hit_n[path] = make_float4(0.f, 0.f, 0.f, __uint_as_float(smp.iter | (smp.material << 16)));
-        hstep = fmaxf(m.t * S.pixel_cone * 0.5f, 1e-4f) * S.pixel_tolerance;
+        hstep = fmaxf(m.t * cone * 0.5f, 1e-4f) * tol;
         grad = mk3(0.f, 0.f, 0.f);
         tap = 0;
         state = TL_NORMAL;
@@ -87,11 +121,21 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     path = item & 0x7fffffffu;
                     shadow = (item >> 31) != 0;
                 }
+                if constexpr (MULTI) {
+                    const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
+                    Pl = job.prog;
+                    Sl = job.scene;
+                    cone = Sl->pixel_cone;
+                    tol = Sl->pixel_tolerance;
+                    accept = cone * tol;
+                    safety = Sl->step_scale;
+                    max_steps = Sl->max_steps;
+                }
                 float4 o = shadow ? soa.sh_o[path] : soa.o[path];
                 float4 d = shadow ? soa.sh_d[path] : soa.d[path];
                 float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
                 if (first) {
-                    float t_end = nearest_emitter(S, ro, rd, shadow ? o.w : S.extent, li);
+                    float t_end = nearest_emitter(*Sl, ro, rd, shadow ? o.w : Sl->extent, li);
                     march_begin(m, ro, rd, t_end);
                     if (shadow) n_shseg++;
                     else n_seg++;
@@ -118,7 +162,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         if (state == TL_MARCH || state == TL_CAND || state == TL_NORMAL) {
             float3 q = m.ro + m.rd * m.t;
             if (state == TL_NORMAL) q = q + tetra_offset(tap) * hstep;
-            DeRaw s = de_form<FORM>(P, q);
+            DeRaw s = de_form<FORM>(*Pl, q);
             n_eval++;
             n_iter += s.iter;
             if (lane_id() == (uint32_t)(__ffs(__activemask()) - 1)) n_wcall++;

@@ -289,6 +289,67 @@ class RenderSession:
         return cls(renderer, scene, cfg, _handle=h)
 
 
+class Batch:
+    """Many (scene, config) jobs rendered by one wavefront (sf_batch_*): one set of
+    persistent launches per round over all jobs' paths, captured in a CUDA graph."""
+
+    def __init__(self, renderer: Renderer, jobs):
+        from ._lib import sf_batch_job
+
+        self.renderer = renderer
+        self.ctx = renderer.ctx
+        self.jobs = list(jobs)
+        self._graphs = [renderer.compile(sc.graph) for sc, _ in self.jobs]
+        arr = (sf_batch_job * len(self.jobs))()
+        for i, (sc, cfg) in enumerate(self.jobs):
+            arr[i].graph = self._graphs[i].h
+            arr[i].scene = sc.desc(cfg.width, cfg.height)
+            arr[i].cfg = cfg.desc()
+        h = C.c_void_p()
+        check(self.ctx.lib.sf_batch_create(self.ctx.h, arr, len(self.jobs), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sf_batch_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 128):
+        check(self.ctx.lib.sf_batch_set_launch(self.h, min_blocks_per_sm, quantum))
+
+    def autotune(self):
+        mb, q, ms = C.c_uint32(), C.c_uint32(), C.c_float()
+        check(self.ctx.lib.sf_batch_autotune(self.h, C.byref(mb), C.byref(q), C.byref(ms)))
+        return mb.value, q.value, ms.value
+
+    def run(self, passes: int = 1, use_graph: bool = True):
+        check(self.ctx.lib.sf_batch_run(self.h, passes, 1 if use_graph else 0))
+
+    def sync(self, timeout_ms: int = 60000) -> int:
+        w = C.c_uint32()
+        check(self.ctx.lib.sf_batch_sync(self.h, timeout_ms, C.byref(w)))
+        return w.value
+
+    def readback(self, job: int) -> RenderOutput:
+        cfg = self.jobs[job][1]
+        w, h = cfg.width, cfg.height
+        acc = np.zeros((h, w, 4), np.float32)
+        depth = np.zeros((h, w), np.float32)
+        aux = np.zeros((h, w, 4), np.float32)
+        planes = sf_film_planes(_fp(acc), _fp(depth), _fp(aux))
+        check(self.ctx.lib.sf_batch_readback(self.h, job, C.byref(planes)))
+        color = np.ones_like(acc)
+        color[..., :3] = acc[..., :3] / np.maximum(acc[..., 3:4], 1.0)
+        n = int(acc[..., 3].min()) if acc.size else 0
+        return RenderOutput(color, acc, depth, aux, n, int(acc[..., 3].max()) if acc.size else 0, 0.0)
+
+
 # ---------------------------------------------------------------------- escape time
 FAMILIES = ["Julia", "Mandelbrot", "BurningShip", "Newton", "Nova", "Phoenix"]
 
@@ -385,5 +446,5 @@ def deep_zoom(ctx: GpuContext, center_hi, center_lo, width_units: float, width: 
     return out
 
 
-__all__ = ["GpuContext", "CompiledGraph", "Renderer", "RenderSession", "RenderOutput", "DeSample",
+__all__ = ["GpuContext", "CompiledGraph", "Renderer", "RenderSession", "RenderOutput", "DeSample", "Batch",
            "PlanarFractal", "Canvas", "escape2d", "deep_zoom", "SyfrackError"]
