@@ -1900,9 +1900,10 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
         j.prog = jobs[i].graph->d_prog;
         j.scene = d_scenes + i;
         size_t px = size_t(cf.width) * cf.height;
+        // accum | aux | depth: both float4 planes stay 16-byte aligned for any pixel count
         j.film.accum = reinterpret_cast<float4*>(film);
-        j.film.depth = reinterpret_cast<float*>(film + px * 16);
-        j.film.aux = reinterpret_cast<float4*>(film + px * 20);
+        j.film.aux = reinterpret_cast<float4*>(film + px * 16);
+        j.film.depth = reinterpret_cast<float*>(film + px * 32);
         j.film.width = cf.width;
         j.film.height = cf.height;
         film += (px * 36 + 255) & ~size_t(255);
