@@ -354,6 +354,162 @@ def run_batch(args):
     ctx.close()
 
 
+def _percentiles(xs):
+    import numpy as np
+
+    if not xs:
+        return {"n": 0}
+    a = np.asarray(xs, dtype=np.float64)
+    return {"n": int(a.size), "p50_ms": float(np.percentile(a, 50)), "p99_ms": float(np.percentile(a, 99)),
+            "mean_ms": float(a.mean()), "max_ms": float(a.max())}
+
+
+def _latency_report(lat, kinds):
+    out = {"all": _percentiles(list(lat.values()))}
+    for k in ("tile", "preview", "refine"):
+        out[k] = _percentiles([v for j, v in lat.items() if kinds[j] == k])
+    return out
+
+
+def serve_replay(renderer, ctx, events, args):
+    """Replays the stream in real time against a Server; latency = completion on the
+    server clock - scheduled arrival mapped onto that clock."""
+    from syfrack_gb300 import Server
+    from syfrack_gb300.serve import DONE, FAILED
+    from syfrack_gb300.workloads import SERVE_REFINE_WINDOW
+
+    srv = Server(renderer, hbm_budget=int(args.hbm_budget_gb * (1 << 30)), slots=args.slots,
+                 host_result_bytes=int(args.host_result_gb * (1 << 30)))
+    kinds = [e[1] for e in events]
+    tickets = [0] * len(events)
+    lat, failed, outstanding, window, lag = {}, 0, set(), [], 0.0
+    ctx.reset_stats()
+    t0 = time.perf_counter()
+    off = min(srv.stats()["now_ms"] - (time.perf_counter() - t0) * 1e3 for _ in range(5))
+    i = 0
+    last_done = 0.0
+    while i < len(events) or outstanding:
+        now = time.perf_counter() - t0
+        while i < len(events) and events[i][0] <= now:
+            t_arr, kind, payload = events[i]
+            if kind == "tile":
+                tickets[i] = srv.tile(*payload)
+            elif kind == "preview":
+                tickets[i] = srv.preview(*payload)
+                window.append(i)
+            else:
+                tickets[i] = srv.refine(tickets[payload], 8)
+            lag = max(lag, time.perf_counter() - t0 - t_arr)
+            outstanding.add(i)
+            i += 1
+        for j in list(outstanding):
+            res = srv.poll(tickets[j], copy=False)
+            if res.state == DONE or res.state == FAILED:
+                outstanding.discard(j)
+                if res.state == FAILED:
+                    failed += 1
+                lat[j] = res.done_ms - (events[j][0] * 1e3 + off)
+                last_done = max(last_done, res.done_ms - off)
+                if kinds[j] != "preview":
+                    srv.release(tickets[j])
+        # a preview's film is dropped once 16 newer previews exist (its queued refinements keep it)
+        while len(window) > SERVE_REFINE_WINDOW and window[0] not in outstanding:
+            srv.release(tickets[window.pop(0)])
+        nxt = events[i][0] - (time.perf_counter() - t0) if i < len(events) else 0.0005
+        time.sleep(min(max(nxt, 0.0), 0.0005))
+    span_s = last_done / 1e3 - events[0][0]
+    st = srv.stats()
+    segs = ctx.stats()["segments"]
+    srv.close()
+    return {"latency": _latency_report(lat, kinds), "failed": failed, "throughput_rps": len(lat) / span_s,
+            "span_s": span_s, "segments": segs, "mrays_per_s": segs / span_s / 1e6, "max_submit_lag_ms": lag * 1e3,
+            "batches": st["batches"], "mean_batch_requests": st["batched_requests"] / max(st["batches"], 1),
+            "admission_waits": st["admission_waits"], "hbm_peak_gb": st["hbm_peak"] / (1 << 30)}
+
+
+def plain_replay(renderer, ctx, events, cap_s):
+    """The same stream through the plain drop-in calls, one request at a time in
+    arrival order: RenderSession + dispatch(1 spp) + readback per preview, a further
+    dispatch(8) + readback on that session per refinement, sf_escape2d per tile."""
+    from syfrack_gb300 import RenderSession, escape2d
+    from syfrack_gb300.workloads import SERVE_REFINE_WINDOW
+
+    kinds = [e[1] for e in events]
+    sessions, window, lat = {}, [], {}
+    ctx.reset_stats()
+    t0 = time.perf_counter()
+    unserved = 0
+    last_done = 0.0
+    for j, (t_arr, kind, payload) in enumerate(events):
+        now = time.perf_counter() - t0
+        if now < t_arr:
+            time.sleep(t_arr - now)
+        if time.perf_counter() - t0 > cap_s:
+            unserved = len(events) - j
+            break
+        if kind == "tile":
+            escape2d(ctx, *payload)
+        elif kind == "preview":
+            sc, cfg = payload
+            # a session sized for its refinements: 8 samples per dispatch, open-ended target
+            cfg = type(cfg)(**{**cfg.__dict__, "samples_per_pixel": 1 << 16, "samples_per_dispatch": 8})
+            s = RenderSession(renderer, sc, cfg)
+            n = payload[1].samples_per_pixel
+            s.dispatch((0, 0, cfg.width, cfg.height, 0), n)
+            s.sync()
+            s.readback()
+            sessions[j] = [s, n]
+            window.append(j)
+            while len(window) > SERVE_REFINE_WINDOW:
+                sessions.pop(window.pop(0))[0].close()
+        else:
+            s, done = sessions[payload]
+            s.dispatch((0, 0, s.cfg.width, s.cfg.height, done), 8)  # samples done..done+7
+            s.sync()
+            s.readback()
+            sessions[payload][1] = done + 8
+        last_done = time.perf_counter() - t0
+        lat[j] = (last_done - t_arr) * 1e3
+    span_s = last_done - events[0][0]
+    segs = ctx.stats()["segments"]
+    for s, _ in sessions.values():
+        s.close()
+    return {"latency": _latency_report(lat, kinds), "unserved_at_cap": unserved, "cap_s": cap_s,
+            "throughput_rps": len(lat) / span_s, "span_s": span_s, "segments": segs,
+            "mrays_per_s": segs / span_s / 1e6}
+
+
+def run_serve(args):
+    """Serving stream: Poisson arrivals at --rate req/s for --duration s (seeded):
+    40% 2D tiles (Julia c = 0.7885 e^{ia} or a Burning Ship view; side 256-2048;
+    1k-20k iterations), 40% previews (480x270, 1 spp, 1 bounce, a random orbit of a
+    Mandelbulb or Mandelbox), 20% refinements (+8 spp into one of the 16 latest
+    previews' films). Replayed in real time against the Server (150 GB HBM budget)
+    and as sequential plain launches; p50/p99 latency and throughput of both."""
+    from syfrack_gb300 import GpuContext, Renderer, workloads
+
+    ctx = GpuContext(0)
+    r = Renderer(ctx)
+    for g in workloads.serving_graphs():
+        r.compile(g)
+    events = workloads.serving_stream(seed=args.seed, rate=args.rate, duration=args.duration)
+    warm = workloads.serving_stream(seed=args.seed + 1, rate=args.rate, duration=0.25)
+    serve_replay(r, ctx, warm, args)
+    plain_replay(r, ctx, warm, 60.0)
+    served = serve_replay(r, ctx, events, args)
+    plain = plain_replay(r, ctx, events, cap_s=args.duration * 3)
+    line = {"metric": "served p99 latency", "unit": "ms", "value": served["latency"]["all"].get("p99_ms"),
+            "higher_is_better": False, "workload": f"serving_stream_poisson{args.rate:g}_{args.duration:g}s",
+            "requests": len(events), "served": served, "plain_sequential": plain,
+            "throughput_ratio": served["throughput_rps"] / plain["throughput_rps"],
+            "config": {"slots": args.slots, "hbm_budget_gb": args.hbm_budget_gb,
+                       "host_result_gb": args.host_result_gb, "seed": args.seed,
+                       "preview": workloads.SERVE_PREVIEW, "refine_spp": workloads.SERVE_REFINE_SPP},
+            "dtype": "f32", "data": "synthetic (seeded Poisson stream)"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -367,13 +523,22 @@ def main():
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="pathtrace", choices=["pathtrace", "batch"])
+    ap.add_argument("--workload", default="pathtrace", choices=["pathtrace", "batch", "serve"])
     ap.add_argument("--jobs", type=int, default=64)
+    # serving stream
+    ap.add_argument("--rate", type=float, default=200.0)
+    ap.add_argument("--duration", type=float, default=60.0)
+    ap.add_argument("--slots", type=int, default=4)
+    ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
+    ap.add_argument("--host-result-gb", type=float, default=8.0)
+    ap.add_argument("--seed", type=int, default=5)
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
     elif args.workload == "batch":
         run_batch(args)
+    elif args.workload == "serve":
+        run_serve(args)
     else:
         run_ours(args)
 

@@ -35,6 +35,7 @@ enum {
     SF_ERR_CHECKPOINT = 9,   /* checkpoint corrupt or from another producer         */
     SF_ERR_WAVEFRONT = 10,   /* wavefront invariant word non-zero (wavefront.rs:414-417) */
     SF_ERR_NO_DEVICE = 11,   /* no CUDA device / extension not usable               */
+    SF_ERR_BUSY = 12,        /* request still queued or running                     */
 };
 
 /* Human-readable name of a status code. Never NULL. */
@@ -373,6 +374,85 @@ sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* it
  * before any stream capture. All calls share the array: calls that overlap on the
  * GPU (two streams, two threads) race; order them on one stream. */
 sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth, void* stream);
+
+/* ------------------------------------------------------------------ serving
+ * Continuous batching of the interactive requests of SyFrack's renderer: previews
+ * (RenderSession::new + the first dispatch, session.rs:165, wavefront.rs:310),
+ * progressive refinements that add samples to a preview's film (RenderSession::step,
+ * session.rs:694) and 2D escape-time tiles (PlanarFractal::sample over a canvas,
+ * planar.rs:77). The reference serves one session per thread with one dispatch in
+ * flight; here one scheduler thread per server forms batches from the queue whenever
+ * one of its slots (a wavefront arena with its own streams) is free and the HBM
+ * budget admits the batch's films and tile outputs. Films stay in device memory from
+ * a preview to its last refinement. A request's result does not depend on what it was
+ * batched with: 3D paths run the same kernel for a graph form in any batch and each
+ * pixel sums its samples in ascending order; 2D pixels are independent. */
+enum sf_request_kind { SF_REQ_PREVIEW = 0, SF_REQ_REFINE = 1, SF_REQ_TILE_2D = 2 };
+enum sf_request_state { SF_REQ_QUEUED = 0, SF_REQ_RUNNING = 1, SF_REQ_DONE = 2, SF_REQ_FAILED = 3 };
+/* What a 2D tile returns: everything sf_escape2d returns (distance, the four trap
+ * planes, iterations), or only iterations and the smooth time (trap 0), for which
+ * the ring, stripe and angle traps are not computed. */
+enum sf_tile_outputs { SF_TILE_ALL = 0, SF_TILE_COUNTS = 1 };
+typedef struct sf_server sf_server;
+typedef struct sf_server_config {
+    uint64_t hbm_budget;        /* device bytes for films and tile outputs together   */
+    uint64_t host_result_bytes; /* pinned host pool holding finished results          */
+    uint32_t slots;             /* batches in flight at once, 1..8                    */
+    uint32_t path_capacity;     /* paths per 3D batch (a request needs w*h*samples)   */
+    uint32_t max_jobs;          /* requests per batch, 1..1024                        */
+    uint32_t max_tile_pixels;   /* 2D pixels per batch                                */
+    uint32_t min_blocks, quantum; /* trace launch shape (sf_batch_set_launch)         */
+} sf_server_config;
+typedef struct sf_request {
+    uint32_t kind;              /* sf_request_kind                                    */
+    uint32_t samples;           /* REFINE: samples added to the parent's film         */
+    uint64_t parent;            /* REFINE: ticket of the preview that owns the film   */
+    sf_graph* graph;            /* PREVIEW                                            */
+    sf_scene_desc scene;        /* PREVIEW                                            */
+    sf_render_config cfg;       /* PREVIEW: size, samples_per_pixel of the first pass,
+                                   bounces and steps; later refinements keep them     */
+    sf_planar_desc planar;      /* TILE_2D                                            */
+    sf_canvas canvas;           /* TILE_2D: the whole canvas, sampled at pixel centres */
+    uint32_t tile_outputs;      /* TILE_2D: sf_tile_outputs                           */
+    uint32_t pad;
+} sf_request;
+typedef struct sf_result {
+    uint32_t state;             /* sf_request_state                                   */
+    sf_status status;           /* SF_OK unless FAILED                                */
+    uint32_t kind, width, height;
+    uint32_t samples;           /* 3D: samples in the film after this request         */
+    uint32_t batch_requests;    /* requests in the batch that carried it              */
+    uint32_t pad;
+    uint64_t work;              /* 3D: paths traced; 2D: pixels                       */
+    double submit_ms, start_ms, done_ms; /* server clock (ms since sf_server_create)  */
+    const float* accum;         /* 3D: width*height float4 sample sums (film order)   */
+    const uint32_t* iterations; /* 2D: width*height iteration counts                  */
+    const float* smooth;        /* 2D: width*height trap 0 (smooth time / iterations) */
+    const float* distance;      /* 2D, SF_TILE_ALL: width*height r/(1+r)              */
+    const float* traps;         /* 2D, SF_TILE_ALL: 4 planes of width*height (slot-major) */
+} sf_result;
+typedef struct sf_server_stats {
+    uint64_t submitted, completed, failed, batches, batched_requests;
+    uint64_t admission_waits;   /* batches cut short by the HBM budget                */
+    uint64_t hbm_used, hbm_peak, hbm_reserved, host_used;
+    uint64_t launches;
+    double now_ms;
+} sf_server_stats;
+/* Starts the scheduler thread. Defaults for zero fields: 4 slots, 4M paths, 256 jobs,
+ * 32M tile pixels, 1 GiB of host results, launch shape 3 blocks/SM and quantum 128. */
+sf_status sf_server_create(sf_context* ctx, const sf_server_config* cfg, sf_server** out);
+/* Queues a request; returns at once with its ticket (tickets start at 1). */
+sf_status sf_serve_submit(sf_server* s, const sf_request* req, uint64_t* ticket);
+/* Non-blocking state of a request; result pointers stay valid until sf_serve_release. */
+sf_status sf_serve_poll(sf_server* s, uint64_t ticket, sf_result* out);
+/* Waits up to timeout_ms (0 = no limit) for DONE or FAILED; SF_ERR_TIMEOUT otherwise. */
+sf_status sf_serve_wait(sf_server* s, uint64_t ticket, uint32_t timeout_ms, sf_result* out);
+/* Drops a finished request's result; a preview's film is freed once no queued
+ * refinement needs it. SF_ERR_BUSY while the request is queued or running. */
+sf_status sf_serve_release(sf_server* s, uint64_t ticket);
+sf_status sf_server_stats_get(sf_server* s, sf_server_stats* out);
+/* Stops the scheduler after the batches in flight; queued requests fail. */
+sf_status sf_server_destroy(sf_server* s);
 
 #ifdef __cplusplus
 }

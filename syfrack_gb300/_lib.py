@@ -74,6 +74,30 @@ class sf_deep_zoom_desc(C.Structure):
                 ("width", u32), ("height", u32), ("max_iter", u32), ("bailout", C.c_float)]
 
 
+class sf_server_config(C.Structure):
+    _fields_ = [("hbm_budget", u64), ("host_result_bytes", u64), ("slots", u32), ("path_capacity", u32),
+                ("max_jobs", u32), ("max_tile_pixels", u32), ("min_blocks", u32), ("quantum", u32)]
+
+
+class sf_request(C.Structure):
+    _fields_ = [("kind", u32), ("samples", u32), ("parent", u64), ("graph", vp), ("scene", abi.sf_scene_desc),
+                ("cfg", abi.sf_render_config), ("planar", sf_planar_desc), ("canvas", sf_canvas),
+                ("tile_outputs", u32), ("pad", u32)]
+
+
+class sf_result(C.Structure):
+    _fields_ = [("state", u32), ("status", st), ("kind", u32), ("width", u32), ("height", u32),
+                ("samples", u32), ("batch_requests", u32), ("pad", u32), ("work", u64),
+                ("submit_ms", C.c_double), ("start_ms", C.c_double), ("done_ms", C.c_double),
+                ("accum", fp), ("iterations", up), ("smooth", fp), ("distance", fp), ("traps", fp)]
+
+
+class sf_server_stats(C.Structure):
+    _fields_ = [("submitted", u64), ("completed", u64), ("failed", u64), ("batches", u64),
+                ("batched_requests", u64), ("admission_waits", u64), ("hbm_used", u64), ("hbm_peak", u64),
+                ("hbm_reserved", u64), ("host_used", u64), ("launches", u64), ("now_ms", C.c_double)]
+
+
 # name -> (argtypes); every function returns sf_status unless listed in _RESTYPES
 SIGNATURES = {
     "sf_status_string": [st],
@@ -118,6 +142,13 @@ SIGNATURES = {
     "sf_escape2d": [vp, P(sf_planar_desc), P(sf_canvas), abi.sf_tile, u32, fp, fp, up],
     "sf_deep_zoom": [vp, P(sf_deep_zoom_desc), up, fp, C.c_int, up, fp, P(u64)],
     "sf_deep_zoom_noalloc": [P(sf_deep_zoom_desc), vp, vp, vp],
+    "sf_server_create": [vp, P(sf_server_config), P(vp)],
+    "sf_serve_submit": [vp, P(sf_request), P(u64)],
+    "sf_serve_poll": [vp, u64, P(sf_result)],
+    "sf_serve_wait": [vp, u64, u32, P(sf_result)],
+    "sf_serve_release": [vp, u64],
+    "sf_server_stats_get": [vp, P(sf_server_stats)],
+    "sf_server_destroy": [vp],
 }
 _RESTYPES = {"sf_status_string": C.c_char_p, "sf_last_error": C.c_char_p, "sf_abi_version": u32}
 

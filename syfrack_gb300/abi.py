@@ -7,7 +7,7 @@ SF_OK = 0
 STATUS_NAMES = {
     0: "SF_OK", 1: "SF_ERR_INVALID", 2: "SF_ERR_GRAPH", 3: "SF_ERR_UNSUPPORTED",
     4: "SF_ERR_CUDA", 5: "SF_ERR_OOM", 6: "SF_ERR_TIMEOUT", 7: "SF_ERR_BUDGET",
-    8: "SF_ERR_IO", 9: "SF_ERR_CHECKPOINT", 10: "SF_ERR_WAVEFRONT", 11: "SF_ERR_NO_DEVICE",
+    8: "SF_ERR_IO", 9: "SF_ERR_CHECKPOINT", 10: "SF_ERR_WAVEFRONT", 11: "SF_ERR_NO_DEVICE", 12: "SF_ERR_BUSY",
 }
 
 # enum sf_node_kind: the order of NodeKind (crates/syfrack-core/src/scene/graph/mod.rs:105-257)

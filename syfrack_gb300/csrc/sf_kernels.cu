@@ -1,6 +1,6 @@
 // sm_103a kernels of the DE path: DE probe, primary rays, the wavefront
-// stages (generate -> [trace -> shade]* -> commit), the per-pixel megakernel,
-// escape-time sampling and the deep-zoom perturbation pair.
+// stages (generate -> [trace -> shade]* -> commit), the per-pixel megakernel
+// and the deep-zoom perturbation pair. Escape-time sampling is in sf_escape.cu.
 #include <cuda_runtime.h>
 
 #include "sf_kernels.cuh"
@@ -304,198 +304,6 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
     warp_stat(&stats[SF_STAT_SEGMENTS], segs);
 }
 
-// ------------------------------------------------------------------ escape time
-// PlanarFractal::sample (planar.rs:77-194) with the orbit arithmetic in
-// explicitly rounded binary32 operations (no contraction), so iteration counts
-// match the reference's f32 arithmetic exactly; traps use device libm.
-#define FM(a, b) __fmul_rn((a), (b))
-#define FA(a, b) __fadd_rn((a), (b))
-#define FS(a, b) __fsub_rn((a), (b))
-static __device__ __forceinline__ void cmul_rn(float ax, float ay, float bx, float by, float& rx, float& ry) {
-    rx = FS(FM(ax, bx), FM(ay, by));
-    ry = FA(FM(ax, by), FM(ay, bx));
-}
-static __device__ __forceinline__ void cpow_rn(float zx, float zy, uint32_t n, float& rx, float& ry) {
-    float x = 1.0f, y = 0.0f;
-    for (uint32_t i = 0; i < n; ++i) {
-        float nx, ny;
-        cmul_rn(x, y, zx, zy, nx, ny);
-        x = nx;
-        y = ny;
-    }
-    rx = x;
-    ry = y;
-}
-static __device__ __forceinline__ float len2_rn(float x, float y) { return __fsqrt_rn(FA(FM(x, x), FM(y, y))); }
-
-static __device__ void planar_sample_dev(const PlanarDev& f, float ix, float iy, float& dist, float* traps,
-                                         uint32_t& iterations, uint32_t& measured_out) {
-    float px = __fdiv_rn(FS(FM(f.angle_cos, ix), FM(f.angle_sin, iy)), f.zoom);
-    float py = __fdiv_rn(FA(FM(f.angle_sin, ix), FM(f.angle_cos, iy)), f.zoom);
-    if (f.inversion != 0.0f) {
-        float k = __fdiv_rn(f.inversion, fmaxf(FA(FM(px, px), FM(py, py)), 1e-8f));
-        px = FM(px, k);
-        py = FM(py, k);
-    }
-    px = FA(px, f.center[0]);
-    py = FA(py, f.center[1]);
-    const uint32_t fam = f.family;
-    const bool parameter_plane = fam == 1 || fam == 2;
-    const bool root = fam == 3 || fam == 4;
-    float cx = parameter_plane ? px : f.julia[0], cy = parameter_plane ? py : f.julia[1];
-    float zx = parameter_plane ? 0.0f : px, zy = parameter_plane ? 0.0f : py;
-    float qx = 0.0f, qy = 0.0f;  // previous
-    const float rcs = f.twist_cos, rsn = f.twist_sin;
-    const float lx = FM(rcs, f.relaxation), ly = FM(rsn, f.relaxation);
-    float ring = 1e20f, stripe = 0.0f, previous_error = 1.0f;
-    uint32_t count = 0, measured = 0;
-    float smooth = float(f.iterations);
-    bool escaped = false;
-    const float bail = f.bailout;
-    for (uint32_t it = 0; it < f.iterations; ++it) {
-        float radius = len2_rn(zx, zy);
-        if (radius > bail) { escaped = true; break; }
-        ring = fminf(ring, fabsf(radius - f.trap_radius));
-        float angle = radius == 0.0f ? 0.0f : atan2f(zy, zx);
-        stripe += 0.5f + 0.5f * sinf(f.stripes * angle);
-        measured += 1;
-        if (root) {
-            float rx, ry;
-            cpow_rn(zx, zy, f.power, rx, ry);
-            rx = FS(rx, 1.0f);
-            float rl2 = FA(FM(rx, rx), FM(ry, ry));
-            if (fam == 3 && rl2 < 1e-12f) {
-                float error = fmaxf(__fsqrt_rn(rl2), 1e-20f);
-                float fraction = fminf(fmaxf(logf(1e-6f / previous_error) / logf(error / previous_error), 0.0f), 1.0f);
-                smooth = count == 0 ? 0.0f : float(count) - 1.0f + fraction;
-                break;
-            }
-            previous_error = fmaxf(__fsqrt_rn(rl2), 1e-20f);
-            float ox = zx, oy = zy;
-            float dx, dy;
-            cpow_rn(zx, zy, f.power - 1, dx, dy);
-            dx = FM(dx, float(f.power));
-            dy = FM(dy, float(f.power));
-            // cdiv(residual, derivative) = residual * conj(derivative) / max(|derivative|^2, 1e-24)
-            float nx, ny;
-            cmul_rn(rx, ry, dx, -dy, nx, ny);
-            float den = fmaxf(FA(FM(dx, dx), FM(dy, dy)), 1e-24f);
-            nx = __fdiv_rn(nx, den);
-            ny = __fdiv_rn(ny, den);
-            float sx, sy;
-            cmul_rn(lx, ly, nx, ny, sx, sy);
-            zx = FS(zx, sx);
-            zy = FS(zy, sy);
-            if (fam == 4) {
-                zx = FA(zx, cx);
-                zy = FA(zy, cy);
-                float ex = FS(zx, ox), ey = FS(zy, oy);
-                if (FA(FM(ex, ex), FM(ey, ey)) < 1e-12f) { count += 1; smooth = float(count); break; }
-            }
-        } else {
-            float bx = fam == 2 ? fabsf(zx) : zx, by = fam == 2 ? fabsf(zy) : zy;
-            float wx, wy, nx, ny;
-            cpow_rn(bx, by, f.power, wx, wy);
-            cmul_rn(rcs, rsn, wx, wy, nx, ny);
-            nx = FA(nx, cx);
-            ny = FA(ny, cy);
-            if (fam == 5) {
-                nx = FA(nx, FM(qx, f.memory));
-                ny = FA(ny, FM(qy, f.memory));
-            }
-            qx = zx;
-            qy = zy;
-            zx = nx;
-            zy = ny;
-        }
-        count += 1;
-    }
-    float radius = fminf(len2_rn(zx, zy), 1e20f);
-    escaped = escaped || radius > bail;
-    float lnp = logf(float(f.power));
-    if (escaped && !root) smooth = float(count) + 1.0f - logf(logf(fmaxf(radius, 1.0001f))) / lnp;
-    else if (escaped) smooth = float(count);
-    const float TAU = 6.2831855f;
-    float final_angle = radius == 0.0f ? 0.5f : atan2f(zy, zx) / TAU + 0.5f;
-    float bands = stripe / float(measured > 1 ? measured : 1);
-    if (escaped && !root && measured > 0) {
-        float angle = radius == 0.0f ? 0.0f : atan2f(zy, zx);
-        float last = 0.5f + 0.5f * sinf(f.stripes * angle);
-        float full = (stripe + last) / float(measured + 1);
-        float t = fminf(fmaxf(1.0f + (logf(logf(bail)) - logf(logf(fmaxf(radius, 1.0001f)))) / lnp, 0.0f), 1.0f);
-        bands += (full - bands) * t;
-    }
-    dist = radius / (1.0f + radius);
-    traps[0] = fminf(fmaxf(smooth / float(f.iterations), 0.0f), 1.0f);
-    traps[1] = ring / (1.0f + ring);
-    traps[2] = bands;
-    traps[3] = final_angle;
-    iterations = count;
-    measured_out = measured;
-}
-
-__global__ void __launch_bounds__(256) k_planar(const PlanarDev* __restrict__ fg, const float* __restrict__ x,
-                                                const float* __restrict__ y, size_t n, float* dist, float* traps,
-                                                uint32_t* iters) {
-    __shared__ PlanarDev F;
-    stage_pod(F, fg);
-    __syncthreads();
-    for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        float tr[4];
-        uint32_t it, ms;
-        float d;
-        planar_sample_dev(F, x[i], y[i], d, tr, it, ms);
-        dist[i] = d;
-        traps[i] = tr[0];
-        traps[n + i] = tr[1];
-        traps[2 * n + i] = tr[2];
-        traps[3 * n + i] = tr[3];
-        iters[i] = it;
-    }
-}
-
-// Flat-canvas pixel mapping (pathtrace.wgsl:1226-1239): jittered (or centred,
-// sample = 0xffffffff) uv -> p = (u - 0.5, (0.5 - v) / aspect) * 6 / zoom, rotated, + centre.
-__global__ void __launch_bounds__(256) k_escape2d(const PlanarDev* __restrict__ fg, const CanvasDev* __restrict__ cg,
-                                                  uint32_t tile_x, uint32_t tile_y, uint32_t tile_w, uint32_t tile_h,
-                                                  uint32_t sample, float* dist, float* traps, uint32_t* iters,
-                                                  unsigned long long* stats) {
-    __shared__ PlanarDev F;
-    __shared__ CanvasDev K;
-    stage_pod(F, fg);
-    stage_pod(K, cg);
-    __syncthreads();
-    const uint32_t n = tile_w * tile_h;
-    unsigned long long total_iters = 0;
-    const float scale = __fdiv_rn(6.0f, K.zoom);
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < n; i += gridDim.x * blockDim.x) {
-        uint32_t px = tile_x + i % tile_w, py = tile_y + i / tile_w;
-        float jx = 0.5f, jy = 0.5f;
-        if (sample != 0xffffffffu) {
-            uint32_t rng = rng_init(px, py, sample, K.seed);
-            jx = rnd(rng);
-            jy = rnd(rng);
-        }
-        float u = __fdiv_rn(FA(float(px), jx), float(K.width));
-        float v = __fdiv_rn(FA(float(py), jy), float(K.height));
-        float ax = FM(FS(u, 0.5f), scale);
-        float ay = FM(__fdiv_rn(FS(0.5f, v), K.aspect), scale);
-        float qx = FA(K.center[0], FS(FM(K.rot_cos, ax), FM(K.rot_sin, ay)));
-        float qy = FA(K.center[1], FA(FM(K.rot_sin, ax), FM(K.rot_cos, ay)));
-        float tr[4], d;
-        uint32_t it, ms;
-        planar_sample_dev(F, qx, qy, d, tr, it, ms);
-        dist[i] = d;
-        traps[i] = tr[0];
-        traps[n + i] = tr[1];
-        traps[2 * n + i] = tr[2];
-        traps[3 * n + i] = tr[3];
-        iters[i] = it;
-        total_iters += ms;
-    }
-    warp_stat(&stats[SF_STAT_DE_ITERS], total_iters);
-}
-
 // ------------------------------------------------------------------ deep zoom
 // Reference orbit Z_n of c_ref in FP64 (one thread), stored in FP64 and FP32.
 __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d, float2* orbit_f,
@@ -656,21 +464,6 @@ cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, P
                                  FilmPlanes film, unsigned long long* stats, cudaStream_t st) {
     dim3 grid((g.tile_w + 7) / 8, (g.tile_h + 7) / 8);
     k_megakernel<<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
-    return cudaGetLastError();
-}
-cudaError_t sf_launch_planar(const PlanarDev* f, const float* x, const float* y, size_t n, float* dist, float* traps,
-                             uint32_t* iters, cudaStream_t st) {
-    if (!n) return cudaSuccess;
-    k_planar<<<grid_for(n, 256, 8), 256, 0, st>>>(f, x, y, n, dist, traps, iters);
-    return cudaGetLastError();
-}
-cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint32_t tile_x, uint32_t tile_y,
-                               uint32_t tile_w, uint32_t tile_h, uint32_t sample, float* dist, float* traps,
-                               uint32_t* iters, unsigned long long* stats, cudaStream_t st) {
-    size_t n = (size_t)tile_w * tile_h;
-    if (!n) return cudaSuccess;
-    k_escape2d<<<grid_for(n, 256, 8), 256, 0, st>>>(f, canvas, tile_x, tile_y, tile_w, tile_h, sample, dist, traps,
-                                                     iters, stats);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d,

@@ -82,11 +82,16 @@ struct DispatchGeom {
     uint32_t paths;  // tile_w * tile_h * samples
 };
 
+// stripe_k: the stripe count as an integer (|k| <= 64), else SF_STRIPES_GENERAL;
+// bail_t: the largest float whose correctly rounded square root is <= bailout.
+#define SF_STRIPES_GENERAL 0x7fffffff
 struct PlanarDev {
-    uint32_t family, power, iterations, pad;
+    uint32_t family, power, iterations;
+    int32_t stripe_k;
     float julia[2], center[2];
     float zoom, inversion, relaxation, memory, bailout, trap_radius, stripes;
     float angle_cos, angle_sin, twist_cos, twist_sin;
+    float bail_t;
 };
 
 struct CanvasDev {
@@ -151,9 +156,13 @@ cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, P
                                  FilmPlanes film, unsigned long long* stats, cudaStream_t st);
 cudaError_t sf_launch_planar(const PlanarDev* f, const float* x, const float* y, size_t n, float* dist, float* traps,
                              uint32_t* iters, cudaStream_t st);
+// with_traps = 0 writes only dist, traps[0 .. n) (smooth time) and iters. *work is
+// the tile's pixel counter and must be 0 when the launch starts; root != 0 for the
+// Newton and Nova families (planar family 3 and 4).
 cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint32_t tile_x, uint32_t tile_y,
                                uint32_t tile_w, uint32_t tile_h, uint32_t sample, float* dist, float* traps,
-                               uint32_t* iters, unsigned long long* stats, cudaStream_t st);
+                               uint32_t* iters, unsigned long long* stats, uint32_t* work, int with_traps, int root,
+                               cudaStream_t st);
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
 cudaError_t sf_launch_perturb(const double2* orbit_d, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width, uint32_t height,

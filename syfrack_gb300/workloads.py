@@ -125,3 +125,78 @@ def deep_zoom_center(seed: int = 2026, max_iter: int = 50000, steps: int = 64):
         else:
             lo_t = mid
     return (lo_t * dx, lo_t * dy)
+
+
+# ---------------------------------------------------------------------- serving stream
+SERVE_PREVIEW = dict(width=480, height=270, spp=1, bounces=1, steps=512)
+SERVE_REFINE_SPP = 8
+SERVE_REFINE_WINDOW = 16  # a refinement picks one of the 16 latest previews
+
+
+def serving_graphs():
+    """The forms a serving client orbits: Mandelbulb powers 6, 8, 10 and Mandelbox
+    scales -1.5, -2, 2 (compiled once, then cached by the renderer)."""
+    bulbs = [Graph.bundled("mandelbulb", power=p, iterations=10, bailout=4.0, safety=0.7, hint=2.5)
+             for p in (6.0, 8.0, 10.0)]
+    boxes = [mandelbox_graph(scale=s, iterations=12) for s in (-1.5, -2.0, 2.0)]
+    return bulbs + boxes
+
+
+def _preview_scene(rng, graphs):
+    g = graphs[int(rng.integers(0, len(graphs)))]
+    dist = float(rng.uniform(2.5, 4.0)) * max(1.0, g.bounding_radius_hint / 2.5)
+    v = rng.normal(size=3)
+    v /= np.linalg.norm(v)
+    cam = Camera.look_at(tuple((v * dist).tolist()), (0.0, 0.0, 0.0), 50.0)
+    light = AreaLight(position=tuple((v * dist * 0.5 + np.array([0, dist * 0.6, 0])).tolist()),
+                      normal=(0.0, -1.0, 0.0), size=(1.0, 1.0), intensity=10.0)
+    scene = Scene(graph=g, camera=cam, material=Material(albedo=(0.7, 0.7, 0.7), roughness=0.4),
+                  lights=[light], seed=int(rng.integers(0, 2**31)))
+    p = SERVE_PREVIEW
+    cfg = RenderConfig(width=p["width"], height=p["height"], samples_per_pixel=p["spp"], max_bounces=p["bounces"],
+                       max_steps=p["steps"], tile_size=max(p["width"], p["height"]),
+                       samples_per_dispatch=p["spp"], integrator="wavefront")
+    return scene, cfg
+
+
+def _tile(rng, side_range=(256, 2048), iter_range=(1000, 20000)):
+    from .render import Canvas, PlanarFractal
+
+    side = int(rng.integers(side_range[0], side_range[1] + 1))
+    iters = int(rng.integers(iter_range[0], iter_range[1] + 1))
+    if rng.random() < 0.5:
+        a = float(rng.uniform(0.0, 2.0 * math.pi))
+        f = PlanarFractal(family="Julia", iterations=iters, julia=(0.7885 * math.cos(a), 0.7885 * math.sin(a)))
+        canvas = Canvas(width=side, height=side, center=(0.0, 0.0), zoom=2.0)
+    else:
+        f = PlanarFractal(family="BurningShip", iterations=iters)
+        cx, cy = -0.45 + float(rng.uniform(-0.2, 0.2)), -0.5 + float(rng.uniform(-0.2, 0.2))
+        canvas = Canvas(width=side, height=side, center=(cx, cy), zoom=float(rng.uniform(1.5, 3.0)))
+    return f, canvas
+
+
+def serving_stream(seed: int = 5, rate: float = 200.0, duration: float = 60.0, tile_side=(256, 2048),
+                   tile_iters=(1000, 20000)):
+    """Seeded Poisson request stream: list of (arrival_s, kind, payload). Kinds:
+    'tile' 40% (Julia with c = 0.7885 e^{ia}, or a Burning Ship view; side and
+    iterations uniform in the given ranges), 'preview' 40% (480x270, 1 spp, 1
+    bounce, a random orbit of one of serving_graphs()), 'refine' 20% (+8 spp to one
+    of the 16 latest previews; payload = index of that preview's event)."""
+    rng = np.random.default_rng(seed)
+    graphs = serving_graphs()
+    out, previews = [], []
+    t = 0.0
+    while True:
+        t += float(rng.exponential(1.0 / rate))
+        if t >= duration:
+            break
+        u = float(rng.random())
+        if u < 0.4:
+            out.append((t, "tile", _tile(rng, tile_side, tile_iters)))
+        elif u < 0.8 or not previews:
+            previews.append(len(out))
+            out.append((t, "preview", _preview_scene(rng, graphs)))
+        else:
+            k = previews[-SERVE_REFINE_WINDOW:]
+            out.append((t, "refine", k[int(rng.integers(0, len(k)))]))
+    return out

@@ -98,3 +98,29 @@ def test_tiles_and_jitter(gpu_ctx):
     np.testing.assert_array_equal(part["iterations"], full["iterations"][8:28, 16:48])
     other = escape2d(gpu_ctx, f, c, sample=6)
     assert (other["iterations"] != full["iterations"]).any()
+
+
+@pytest.mark.parametrize("stripes", [12.0, -5.0, 7.5, 0.0])
+def test_stripe_bands_integer_and_general(gpu_ctx, oracle_mod, stripes):
+    # integer stripe counts use sin(k theta) = Im(u^k); others use sin(k * atan2)
+    f = PlanarFractal(family="Mandelbrot", iterations=400, stripes=stripes)
+    pts = np.random.default_rng(12).uniform(-2.0, 1.0, (6000, 2)).astype(np.float32)
+    gpu = f.sample(gpu_ctx, pts)
+    ref = oracle_mod.planar(oracle_params(oracle_mod, f), pts, precision=32)
+    np.testing.assert_array_equal(gpu["iterations"], ref["iterations"])
+    d = np.abs(gpu["traps"] - ref["traps"])
+    assert np.quantile(d, 0.999) <= 0.006
+
+
+def test_escape2d_without_traps_keeps_counts(gpu_ctx):
+    from syfrack_gb300 import Renderer, Server
+
+    c = Canvas(width=200, height=120, center=(-0.45, -0.5), zoom=2.0)
+    f = PlanarFractal(family="BurningShip", iterations=3000)
+    full = escape2d(gpu_ctx, f, c)
+    srv = Server(Renderer(gpu_ctx), hbm_budget=1 << 28)
+    lean = srv.wait(srv.tile(f, c, traps=False))
+    srv.close()
+    assert lean.traps is None and lean.distance is None
+    np.testing.assert_array_equal(lean.iterations, full["iterations"])
+    np.testing.assert_array_equal(lean.smooth, full["traps"][0])
