@@ -510,6 +510,152 @@ def run_serve(args):
     ctx.close()
 
 
+def run_primary(args):
+    """Plain Mandelbulb primary rays: 256x256, power 8, 12 iterations, bailout 2.0,
+    pinhole at (0,0,-3) looking at the origin, 60 degree FOV, 256 steps, epsilon 1e-4,
+    far 10; hit t, step count and central-difference normal per pixel. Device time
+    per launch from CUDA events (profiling on); e2e through Renderer.primary with
+    host outputs; the oracle in FP32 on all host cores over the same frame. A
+    2048x2048 frame of the same view gives the kernel's sustained rate."""
+    from syfrack_gb300 import GpuContext, Renderer, workloads
+
+    ctx = GpuContext(0)
+    r = Renderer(ctx)
+    g, cam, W, H, steps, eps, far = workloads.mandelbulb_primary()
+    for _ in range(max(args.warmup, 3)):
+        r.primary(g, cam, W, H, steps, "absolute", eps, far)
+        r.primary(g, cam, 2048, 2048, steps, "absolute", eps, far)
+    ctx.set_profiling(True)
+    frames = {}
+    for (w, h) in ((W, H), (2048, 2048)):
+        ctx.reset_stats()
+        t0 = time.perf_counter()
+        for _ in range(args.steps):
+            r.primary(g, cam, w, h, steps, "absolute", eps, far)
+        wall = time.perf_counter() - t0
+        st = ctx.stats()
+        launch_ms = st["trace_ms"] / max(st["trace_launches"], 1)
+        rays = w * h
+        frames[f"{w}x{h}"] = {"mrays_per_s": rays / (launch_ms * 1e-3) / 1e6, "launch_ms": launch_ms,
+                              "e2e_mrays_per_s": rays * args.steps / wall / 1e6,
+                              "de_evals_per_frame": st["de_evals"] / args.steps,
+                              "de_iterations_per_frame": st["de_iterations"] / args.steps}
+    ctx.set_profiling(False)
+    # oracle (FP32, all host cores) on the same 256x256 frame
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU restatement; used only as the baseline here
+
+    from syfrack_gb300 import abi as sfabi
+
+    og = oracle.OracleGraph(g)
+    b = cam.basis()
+    oc = sfabi.sf_camera()
+    oc.origin[:] = [float(x) for x in b.origin]
+    oc.forward[:] = [float(x) for x in b.forward]
+    oc.right[:] = [float(x) for x in b.right]
+    oc.up[:] = [float(x) for x in b.up]
+    oc.tan_half_fov = b.tan_half_fov
+    oc.aspect = 1.0
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    og.primary(oc, W, H, steps, 1, eps, far, precision=32, threads=threads)
+    cpu_s = time.perf_counter() - t0
+    main = frames[f"{W}x{H}"]
+    line = {"metric": "primary Mrays/s", "unit": "Mrays/s", "value": main["mrays_per_s"], "higher_is_better": True,
+            "workload": "mandelbulb_primary_256x256_256steps", "steps": args.steps, "frames": frames,
+            "e2e": {"value": main["e2e_mrays_per_s"], "unit": "Mrays/s", "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 20, "call": "Renderer.primary"},
+            "cpu_baseline": {"value": W * H / cpu_s / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
+                             "sample": f"the whole {W}x{H} frame, FP32"},
+            "dtype": "f32", "data": "synthetic (the C1 view)"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
+def run_deepzoom(args):
+    """Mandelbrot deep zoom: 3840x2160, max 50,000 iterations, width 1e-12 around a
+    seeded boundary point (FP64 bisection of the escape label along a random ray from
+    c = 0). FP64 reference orbit on the GPU, FP32 perturbation with rebasing. Reports
+    the perturbation's Giter/s (kernel time from CUDA events), the frame time through
+    the public call (host outputs), agreement of iteration counts with full-FP64
+    direct iteration on the GPU over every pixel, smooth-colouring error against it,
+    and, on a seeded 4096-pixel sample, agreement with the oracle's binary128
+    iteration (the truth) and FP64 iteration, timed as the CPU baseline."""
+    import numpy as np
+
+    from syfrack_gb300 import GpuContext, deep_zoom, workloads
+
+    ctx = GpuContext(0)
+    W, H, MI, width = 3840, 2160, 50000, 1e-12
+    c = workloads.deep_zoom_center(seed=2026, max_iter=MI)
+    for _ in range(max(args.warmup, 3)):
+        deep_zoom(ctx, c, (0.0, 0.0), width, 960, 540, MI, bailout=16.0)
+    ctx.set_profiling(True)
+    walls, kms, iters = [], [], []
+    out = None
+    for _ in range(args.steps):
+        ctx.reset_stats()
+        t0 = time.perf_counter()
+        out = deep_zoom(ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0)
+        walls.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        kms.append(st["trace_ms"])
+        iters.append(st["de_iterations"])
+    ctx.set_profiling(False)
+    full = deep_zoom(ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, reference_f64=True)
+    it, it64 = full["iterations"].ravel(), full["iterations_f64"].ravel()
+    agree64 = float((it == it64).mean())
+    near64 = float((np.abs(it.astype(np.int64) - it64.astype(np.int64)) <= 1).mean())
+    both = (it == it64) & (it < MI)
+    smooth_err = np.abs(full["smooth"].ravel()[both] - full["smooth_f64"].ravel()[both])
+    # truth: binary128 on a seeded sample (oracle, all host cores), timed as the CPU baseline
+    sys.path.insert(0, os.path.join(ROOT, "oracle"))
+    import oracle  # the CPU restatement; used only as the baseline and checker here
+
+    rng = np.random.default_rng(11)
+    idx = rng.choice(W * H, 4096, replace=False)
+    f32 = np.float32
+    pitch = f32(width / W)
+    px, py = idx % W, idx // W
+    off = np.stack([(px.astype(np.float32) - f32(W) * f32(0.5) + f32(0.5)) * pitch,
+                    (f32(H) * f32(0.5) - py.astype(np.float32) - f32(0.5)) * pitch], 1).astype(np.float64)
+    threads = os.cpu_count() or 1
+    t0 = time.perf_counter()
+    truth, _ = oracle.mandel_escape(np.array(c), np.zeros(2), off, MI, 16.0, precision=128, threads=threads)
+    t128 = time.perf_counter() - t0
+    t0 = time.perf_counter()
+    cpu64, _ = oracle.mandel_escape(np.array(c), np.zeros(2), off, MI, 16.0, precision=64, threads=threads)
+    t64 = time.perf_counter() - t0
+    iters_per_frame = float(np.median(iters))
+    kernel_ms = float(np.median(kms))
+    line = {"metric": "deep-zoom perturbation Giter/s", "unit": "Giter/s",
+            "value": iters_per_frame / (kernel_ms * 1e-3) / 1e9, "higher_is_better": True,
+            "workload": "mandelbrot_deep_zoom_3840x2160_50k_iter_width1e-12", "steps": args.steps,
+            "center": list(c), "kernel_ms_per_frame": kernel_ms, "iterations_per_frame": iters_per_frame,
+            "e2e": {"value": iters_per_frame / float(np.median(walls)) / 1e9, "unit": "Giter/s",
+                    "frame_ms": float(np.median(walls)) * 1e3, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 8, "call": "deep_zoom (sf_deep_zoom)"},
+            "rebases_per_frame": out["rebases"],
+            "agreement": {"perturbation_vs_fp64_direct_all_pixels": agree64,
+                          "perturbation_vs_fp64_direct_within_1": near64,
+                          "smooth_abs_err_vs_fp64_where_counts_agree": {
+                              "mean": float(smooth_err.mean()) if smooth_err.size else None,
+                              "max": float(smooth_err.max()) if smooth_err.size else None},
+                          "sample_pixels": len(idx),
+                          "perturbation_vs_binary128": float((it[idx] == truth).mean()),
+                          "perturbation_vs_binary128_within_1": float(
+                              (np.abs(it[idx].astype(np.int64) - truth.astype(np.int64)) <= 1).mean()),
+                          "fp64_direct_gpu_vs_binary128": float((it64[idx] == truth).mean()),
+                          "fp64_direct_cpu_vs_binary128": float((cpu64 == truth).mean())},
+            "cpu_baseline": {"value": float(np.sum(np.minimum(cpu64, MI))) / t64 / 1e9, "unit": "Giter/s",
+                             "cores": threads, "kind": "port",
+                             "sample": f"{len(idx)} seeded pixels, FP64 direct iteration "
+                                       f"({t64:.2f} s; binary128 on the same pixels {t128:.2f} s)"},
+            "dtype": "f32 deltas, f64 reference orbit", "data": "synthetic (seeded boundary point)"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def main():
     ap = argparse.ArgumentParser()
     ap.add_argument("--gpus", type=int, default=1)
@@ -523,7 +669,8 @@ def main():
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--workload", default="pathtrace", choices=["pathtrace", "batch", "serve"])
+    ap.add_argument("--workload", default="pathtrace",
+                    choices=["pathtrace", "batch", "serve", "primary", "deepzoom"])
     ap.add_argument("--jobs", type=int, default=64)
     # serving stream
     ap.add_argument("--rate", type=float, default=200.0)
@@ -539,6 +686,10 @@ def main():
         run_batch(args)
     elif args.workload == "serve":
         run_serve(args)
+    elif args.workload == "primary":
+        run_primary(args)
+    elif args.workload == "deepzoom":
+        run_deepzoom(args)
     else:
         run_ours(args)
 

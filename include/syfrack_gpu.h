@@ -369,7 +369,7 @@ sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* it
  * width*height entries; the work is queued on `stream` (a cudaStream_t, NULL for
  * the legacy default stream) on the current device and the call returns without
  * waiting. The reference orbit lives in a file-scope device array held by every
- * GPU that loads the library until exit (1.5 MB): max_iter above 65536 is rejected
+ * GPU that loads the library until exit (1 MB): max_iter above 65536 is rejected
  * with SF_ERR_INVALID. The first call on a device looks that array up, so make it
  * before any stream capture. All calls share the array: calls that overlap on the
  * GPU (two streams, two threads) race; order them on one stream. */

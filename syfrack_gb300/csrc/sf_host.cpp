@@ -1685,16 +1685,18 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     if (!(d->bailout >= 2.0f)) return fail(SF_ERR_INVALID, "bailout must be at least 2");
     cudaSetDevice(c->device);
     size_t n = size_t(d->width) * d->height;
-    size_t M = size_t(d->max_iter) + 2;
-    size_t bytes = M * 16 + M * 8 + 256 + n * 8 * (reference_f64 ? 2 : 1);
+    size_t M = size_t(d->max_iter) + 4;  // the orbit, two entries past its end, one spare
+    const size_t Mb = (M * 8 + 255) & ~size_t(255);
+    size_t bytes = 2 * Mb + 256 + n * 8 * (reference_f64 ? 2 : 1);
     void* buf = nullptr;
     sf_status st = ctx_alloc(c, bytes, &buf);
     if (st != SF_OK) return st;
     char* b = static_cast<char*>(buf);
-    double2* od = reinterpret_cast<double2*>(b);
-    float2* of = reinterpret_cast<float2*>(b + M * 16);
-    uint32_t* olen = reinterpret_cast<uint32_t*>(b + M * 24);
-    uint32_t* di = reinterpret_cast<uint32_t*>(b + M * 24 + 256);
+    float2* olo = reinterpret_cast<float2*>(b);
+    float2* of = reinterpret_cast<float2*>(b + Mb);
+    uint32_t* olen = reinterpret_cast<uint32_t*>(b + 2 * Mb);  // orbit length | pixel counter
+    uint32_t* work = olen + 1;
+    uint32_t* di = reinterpret_cast<uint32_t*>(b + 2 * Mb + 256);
     float* ds = reinterpret_cast<float*>(di + n);
     uint32_t* di64 = reinterpret_cast<uint32_t*>(ds + n);
     float* ds64 = reinterpret_cast<float*>(di64 + n);
@@ -1703,14 +1705,15 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     cudaError_t e = cudaSuccess;
     unsigned long long before[SF_STAT_COUNT];
     e = cudaMemcpyAsync(before, c->d_stats, sizeof before, cudaMemcpyDeviceToHost, c->stream);
+    if (e == cudaSuccess) e = cudaMemsetAsync(work, 0, 4, c->stream);
     {
         LaunchTimer t(c, false);
-        if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, od, of, olen, c->stream);
+        if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, olo, of, olen, c->stream);
     }
     if (e == cudaSuccess) {
         LaunchTimer t(c, true);
-        e = sf_launch_perturb(od, of, olen, d->width, d->height, float(pitch), 1.0f, d->max_iter, d->bailout, di, ds,
-                              c->d_stats, c->stream);
+        e = sf_launch_perturb(olo, of, olen, d->width, d->height, float(pitch), d->max_iter, d->bailout, di, ds,
+                              c->d_stats, work, c->stream);
     }
     if (e == cudaSuccess && reference_f64) {
         LaunchTimer t(c, false);

@@ -305,20 +305,30 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
 }
 
 // ------------------------------------------------------------------ deep zoom
-// Reference orbit Z_n of c_ref in FP64 (one thread), stored in FP64 and FP32.
-__global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d, float2* orbit_f,
+// Reference orbit Z_n of c_ref in FP64 (one thread).
+// Each entry is kept as the pair hi = float(Z), lo = float(Z - hi): hi + lo carries
+// about 48 bits of Z, so the perturbation kernel can rebase without FP64 arithmetic.
+// The arrays hold max_iter + 4 entries.
+__global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo, float2* orbit_f,
                             uint32_t* orbit_len) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
     double zx = 0.0, zy = 0.0, b2 = bailout * bailout;
     uint32_t n = 0;
     for (;;) {
-        orbit_d[n] = make_double2(zx, zy);
-        orbit_f[n] = make_float2((float)zx, (float)zy);
+        float hx = (float)zx, hy = (float)zy;
+        orbit_f[n] = make_float2(hx, hy);
+        orbit_lo[n] = make_float2((float)(zx - (double)hx), (float)(zy - (double)hy));
         if (n >= max_iter || zx * zx + zy * zy > b2) break;
         double nx = zx * zx - zy * zy + cx;
         zy = 2.0 * zx * zy + cy;
         zx = nx;
         ++n;
+    }
+    // two copies of the last entry past the end: the perturbation loads Z_(m+3)
+    // ahead of use without clamping (those copies are never used)
+    for (uint32_t k = 1; k <= 2; ++k) {
+        orbit_f[n + k] = orbit_f[n];
+        orbit_lo[n + k] = orbit_lo[n];
     }
     *orbit_len = n + 1;
 }
@@ -326,49 +336,121 @@ __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bail
 // FP32 perturbation with rebasing: z_n = Z_m + d, d' = (2 Z_m + d) d + dc;
 // when |z| < |d| or the reference ends, restart from Z_0 with d = z.
 // count = first n with |z_n| > bailout (max_iter if none), as the direct iteration.
-__global__ void __launch_bounds__(256) k_perturb(const double2* __restrict__ orbit_d, const float2* __restrict__ orbit,
+// At a rebase z = Z_m + d is formed from Z_m = hi + lo (about 48 bits) with an
+// error-free sum of hi and d, rounded once to binary32: |Z_m| >> |z| there, and
+// hi + d alone would cancel away the pixel's offset. The kernel has no FP64
+// arithmetic (the FP64 pipe of this part is narrow).
+// Each lane owns one pixel at a time and takes the next (warp-aggregated atomic on
+// *work, which starts at 0) when its orbit ends, checking every PERT_CHUNK
+// iterations, so pixels that escape early do not leave lanes idle beside pixels that
+// run the whole budget. Z_m, Z_(m+1) and Z_(m+2) are carried in registers and
+// Z_(m+3) is loaded two iterations before it is used, which hides the L2 latency of
+// the orbit (lanes walk it at different offsets once they have rebased); the orbit
+// arrays hold two entries past the end for these loads. The iteration count is
+// base + m, and one compare of m against stop = min(max_iter - base, M - 1) covers
+// both the budget and the end of the reference in the common path.
+constexpr int PERT_CHUNK = 30;
+
+struct OrbitWindow {
+    float2 z0, z1, z2;  // Z_m, Z_(m+1), Z_(m+2) (hi parts)
+};
+
+static __device__ __forceinline__ void orbit_window_at0(const float2* __restrict__ orbit, OrbitWindow& w) {
+    w.z0 = orbit[0];
+    w.z1 = orbit[1];
+    w.z2 = orbit[2];
+}
+
+// round(hi + lo + d) for |lo| <= ulp(hi)/2: s = hi + d with its exact error, plus lo.
+static __device__ __forceinline__ float add3(float hi, float lo, float d, float s) {
+    float bb = __fsub_rn(s, hi);
+    float err = __fadd_rn(__fsub_rn(hi, __fsub_rn(s, bb)), __fsub_rn(d, bb));
+    return __fadd_rn(s, __fadd_rn(err, lo));
+}
+
+__global__ void __launch_bounds__(256, 4) k_perturb(const float2* __restrict__ orbit_lo, const float2* __restrict__ orbit,
                                                  const uint32_t* __restrict__ orbit_len,
                                                  uint32_t width, uint32_t height, float pitch, uint32_t max_iter,
                                                  float bailout, uint32_t* iters, float* smooth,
-                                                 unsigned long long* stats) {
+                                                 unsigned long long* stats, uint32_t* work) {
     const uint32_t M = *orbit_len;
+    const uint32_t N = width * height;
     const float b2 = bailout * bailout;
     unsigned long long total = 0, rebases = 0;
-    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < width * height; i += gridDim.x * blockDim.x) {
-        uint32_t px = i % width, py = i / width;
-        float dcx = (float(px) - float(width) * 0.5f + 0.5f) * pitch;
-        float dcy = (float(height) * 0.5f - float(py) - 0.5f) * pitch;
-        float dx = 0.0f, dy = 0.0f;
-        uint32_t m = 0, n = 0;
-        float zx = 0.0f, zy = 0.0f, mag = 0.0f;
-        while (n < max_iter) {
-            float2 Z = orbit[m];
-            float tx = 2.0f * Z.x + dx, ty = 2.0f * Z.y + dy;
-            float ndx = tx * dx - ty * dy + dcx;
-            float ndy = tx * dy + ty * dx + dcy;
-            dx = ndx;
-            dy = ndy;
-            ++m;
-            ++n;
-            float2 Zn = orbit[m];
-            zx = Zn.x + dx;
-            zy = Zn.y + dy;
-            mag = zx * zx + zy * zy;
-            if (mag > b2) break;
-            if (mag < dx * dx + dy * dy || m + 1 >= M) {
-                // z = Z_m + d formed in FP64: |Z_m| >> |z| here, and an FP32 sum would
-                // cancel away the pixel's offset
-                double2 Zd = orbit_d[m];
-                dx = (float)(Zd.x + (double)dx);
-                dy = (float)(Zd.y + (double)dy);
-                m = 0;
-                ++rebases;
+    uint32_t pix = 0, m = 0, base = 0, stop = 0;
+    float dx = 0.0f, dy = 0.0f, dcx = 0.0f, dcy = 0.0f, mag = 0.0f;
+    OrbitWindow w;
+    w.z0 = w.z1 = w.z2 = make_float2(0.0f, 0.0f);
+    bool busy = false, live = true;
+    for (;;) {
+        // every lane of the warp reaches this point together
+        bool want = live && !busy;
+        uint32_t got = warp_fetch(work, want);
+        if (want) {
+            if (got < N) {
+                pix = got;
+                uint32_t px = pix % width, py = pix / width;
+                dcx = (float(px) - float(width) * 0.5f + 0.5f) * pitch;
+                dcy = (float(height) * 0.5f - float(py) - 0.5f) * pitch;
+                dx = dy = mag = 0.0f;
+                m = base = 0;
+                stop = min(max_iter, M - 1);
+                orbit_window_at0(orbit, w);
+                busy = true;
+            } else {
+                live = false;
             }
         }
-        iters[i] = n;
-        total += n;
-        float r = sqrtf(mag);
-        smooth[i] = n < max_iter ? float(n) + 1.0f - logf(logf(fmaxf(r, 1.0001f))) / logf(2.0f) : float(n);
+        if (!__any_sync(FULL_MASK, busy)) break;
+        if (busy) {
+            bool done = false;
+#pragma unroll 3
+            for (int j = 0; j < PERT_CHUNK; ++j) {
+                // Z_(m+3), used two iterations from now
+                const float2 z3 = orbit[m + 3];
+                float tx = 2.0f * w.z0.x + dx, ty = 2.0f * w.z0.y + dy;
+                float ndx = tx * dx - ty * dy + dcx;
+                float ndy = tx * dy + ty * dx + dcy;
+                dx = ndx;
+                dy = ndy;
+                ++m;
+                float zx = __fadd_rn(w.z1.x, dx), zy = __fadd_rn(w.z1.y, dy);
+                mag = zx * zx + zy * zy;
+                if (mag > b2) {
+                    done = true;
+                    break;
+                }
+                const bool small = mag < dx * dx + dy * dy;
+                if (small || m >= stop) {
+                    if (base + m >= max_iter) {
+                        done = true;
+                        break;
+                    }
+                    if (small || m + 1 >= M) {
+                        const float2 lo = orbit_lo[m];
+                        dx = add3(w.z1.x, lo.x, dx, zx);
+                        dy = add3(w.z1.y, lo.y, dy, zy);
+                        base += m;
+                        m = 0;
+                        stop = min(max_iter - base, M - 1);
+                        orbit_window_at0(orbit, w);
+                        ++rebases;
+                        continue;
+                    }
+                }
+                w.z0 = w.z1;
+                w.z1 = w.z2;
+                w.z2 = z3;
+            }
+            if (done) {
+                const uint32_t n = base + m;
+                iters[pix] = n;
+                total += n;
+                float r = sqrtf(mag);
+                smooth[pix] = n < max_iter ? float(n) + 1.0f - logf(logf(fmaxf(r, 1.0001f))) / logf(2.0f) : float(n);
+                busy = false;
+            }
+        }
     }
     warp_stat(&stats[SF_STAT_DE_ITERS], total);
     warp_stat(&stats[SF_STAT_STEPS], rebases);
@@ -466,17 +548,17 @@ cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, P
     k_megakernel<<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d,
+cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st) {
-    k_ref_orbit<<<1, 32, 0, st>>>(cx, cy, max_iter, bailout, orbit_d, orbit_f, orbit_len);
+    k_ref_orbit<<<1, 32, 0, st>>>(cx, cy, max_iter, bailout, orbit_lo, orbit_f, orbit_len);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_perturb(const double2* orbit_d, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,
-                              uint32_t height, float pitch, float, uint32_t max_iter, float bailout, uint32_t* iters,
-                              float* smooth, unsigned long long* stats, cudaStream_t st) {
+cudaError_t sf_launch_perturb(const float2* orbit_lo, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,
+                              uint32_t height, float pitch, uint32_t max_iter, float bailout, uint32_t* iters,
+                              float* smooth, unsigned long long* stats, uint32_t* work, cudaStream_t st) {
     size_t n = (size_t)width * height;
-    k_perturb<<<grid_for(n, 256, 8), 256, 0, st>>>(orbit_d, orbit_f, orbit_len, width, height, pitch, max_iter, bailout, iters,
-                                                    smooth, stats);
+    k_perturb<<<grid_for(n, 256, 4), 256, 0, st>>>(orbit_lo, orbit_f, orbit_len, width, height, pitch, max_iter, bailout,
+                                                    iters, smooth, stats, work);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch, uint32_t max_iter,

@@ -163,11 +163,13 @@ cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint
                                uint32_t tile_w, uint32_t tile_h, uint32_t sample, float* dist, float* traps,
                                uint32_t* iters, unsigned long long* stats, uint32_t* work, int with_traps, int root,
                                cudaStream_t st);
-cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, double2* orbit_d,
+// orbit_f[n] = float(Z_n), orbit_lo[n] = float(Z_n - orbit_f[n]), n < *orbit_len <= max_iter + 1.
+cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
-cudaError_t sf_launch_perturb(const double2* orbit_d, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width, uint32_t height,
-                              float pitch, float aspect_unused, uint32_t max_iter, float bailout, uint32_t* iters,
-                              float* smooth, unsigned long long* stats, cudaStream_t st);
+// *work is the pixel counter of the launch and must be 0 when it starts.
+cudaError_t sf_launch_perturb(const float2* orbit_lo, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,
+                              uint32_t height, float pitch, uint32_t max_iter, float bailout, uint32_t* iters,
+                              float* smooth, unsigned long long* stats, uint32_t* work, cudaStream_t st);
 cudaError_t sf_launch_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch, uint32_t max_iter,
                                  double bailout, uint32_t* iters, float* smooth, cudaStream_t st);
 int sf_device_sm_count();

@@ -5,10 +5,11 @@
 // hands out every byte itself), and latency-critical threads where cudaMalloc's
 // implicit device-wide synchronisation is not acceptable. For them this entry point
 // takes the caller's device output buffers and keeps its scratch -- the reference
-// orbit in FP64 and FP32, its length and the statistics counters -- in one
+// orbit as binary32 hi/lo pairs, its length and the statistics counters -- in one
 // file-scope device array, held by every GPU that loads the library until exit.
 #include <cuda_runtime.h>
 
+#include <cstddef>
 #include <mutex>
 #include <string>
 
@@ -23,14 +24,14 @@ constexpr uint32_t kMaxIter = 65536;  // largest max_iter the scratch holds
 constexpr int kMaxDevices = 64;
 
 struct NoAllocScratch {
-    double2 orbit_d[kMaxIter + 2];
-    float2 orbit_f[kMaxIter + 2];
+    float2 orbit_lo[kMaxIter + 4];  // the orbit and two entries past its end
+    float2 orbit_f[kMaxIter + 4];
     uint32_t orbit_len;
-    uint32_t pad;
+    uint32_t work;  // pixel counter of the perturbation launch
     unsigned long long stats[SF_STAT_COUNT];
 };
 
-// 1.5 MB per device. In host code this name is only a stand-in for the symbol:
+// 1 MB per device. In host code this name is only a stand-in for the symbol:
 // kernels receive the address cudaGetSymbolAddress returns for the current device.
 static __device__ __align__(256) NoAllocScratch g_noalloc_scratch;
 
@@ -69,15 +70,17 @@ extern "C" sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* 
     sf_status s = scratch_address(&sc);
     if (s != SF_OK) return s;
     cudaStream_t st = static_cast<cudaStream_t>(stream);
-    // the counters start at zero; the orbit and its length are written before they are read
-    cudaError_t e = cudaMemsetAsync(sc->stats, 0, sizeof(sc->stats), st);
+    // the pixel counter and the statistics start at zero (they are adjacent); the orbit
+    // and its length are written before they are read
+    static_assert(offsetof(NoAllocScratch, stats) == offsetof(NoAllocScratch, work) + 4, "work | stats layout");
+    cudaError_t e = cudaMemsetAsync(&sc->work, 0, 4 + sizeof(sc->stats), st);
     double cx = d->center_hi[0] + d->center_lo[0], cy = d->center_hi[1] + d->center_lo[1];
     double pitch = d->width_units / double(d->width);
-    if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, sc->orbit_d, sc->orbit_f,
+    if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, sc->orbit_lo, sc->orbit_f,
                                                   &sc->orbit_len, st);
     if (e == cudaSuccess)
-        e = sf_launch_perturb(sc->orbit_d, sc->orbit_f, &sc->orbit_len, d->width, d->height, float(pitch), 1.0f,
-                              d->max_iter, d->bailout, iterations, smooth, sc->stats, st);
+        e = sf_launch_perturb(sc->orbit_lo, sc->orbit_f, &sc->orbit_len, d->width, d->height, float(pitch),
+                              d->max_iter, d->bailout, iterations, smooth, sc->stats, &sc->work, st);
     if (e != cudaSuccess) return sf_report_error(SF_ERR_CUDA, std::string("sf_deep_zoom_noalloc: ") + cudaGetErrorString(e));
     return SF_OK;
 }
