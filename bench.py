@@ -176,7 +176,7 @@ def run_ours(args):
     cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=spp_total,
                                                samples_per_dispatch=SPP_PER_STEP)
     sess = RenderSession(renderer, scene, cfg)
-    sess.set_launch(args.min_blocks, 256, args.quantum)
+    sess.set_launch(args.min_blocks, args.quantum, args.regen)
     tile = (0, 0, cfg.width, cfg.height)
     peak = C.c_double()
     check(ctx.lib.sf_device_fp32_peak(ctx.h, C.byref(peak)))
@@ -265,6 +265,8 @@ def run_ours(args):
                        "width": cfg.width, "height": cfg.height, "spp_per_step": SPP_PER_STEP,
                        "paths_per_step": cfg.width * cfg.height * SPP_PER_STEP, "max_bounces": cfg.max_bounces,
                        "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
+                       "launch": {"min_blocks_per_sm": args.min_blocks, "quantum": args.quantum,
+                                  "regen": args.regen},
                        "l2": "inputs larger than L2 (path state 1.4 GB per step)",
                        "segments_per_step": segs_all / args.steps,
                        "pixel_samples_per_s": cfg.width * cfg.height * SPP_PER_STEP * args.steps * n_ranks
@@ -327,7 +329,7 @@ def run_batch(args):
     plain_mk, t_mk = sequential("megakernel")
     plain_wf, t_wf = sequential("wavefront")
     b = Batch(r, jobs)
-    mb, q, tune_ms = b.autotune()
+    mb, q, rg, tune_ms = b.autotune()
     ctx.reset_stats()
     t0 = time.perf_counter()
     b.run(1, use_graph=True)
@@ -347,7 +349,7 @@ def run_batch(args):
             "value_steady_replays": replay, "plain_megakernel": plain_mk, "plain_wavefront_sessions": plain_wf,
             "speedup_vs_plain_megakernel": batched / plain_mk, "seconds": {"megakernel": t_mk, "wavefront": t_wf,
             "batch_first_pass": t_b, "batch_replays": t_r, "autotune_ms_best_pass": tune_ms},
-            "autotuned": {"min_blocks_per_sm": mb, "quantum": q}, "segments_per_pass": segs,
+            "autotuned": {"min_blocks_per_sm": mb, "quantum": q, "regen": rg}, "segments_per_pass": segs,
             "paths_per_pass": int(sum(c.width * c.height * c.samples_per_pixel for _, c in jobs)),
             "dtype": "f32", "data": "synthetic (seeded jobs)"}
     print(json.dumps(line), flush=True)
@@ -664,6 +666,7 @@ def main():
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--min-blocks", type=int, default=3)
     ap.add_argument("--quantum", type=int, default=128)
+    ap.add_argument("--regen", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     # smaller frames are for profiler captures only; the measured workload is 1280x720
     ap.add_argument("--width", type=int, default=1280)

@@ -292,10 +292,12 @@ sf_status sf_session_stats(sf_session* s, sf_stats* out);
 sf_status sf_session_save(sf_session* s, const char* dir);
 sf_status sf_session_resume(sf_context* ctx, sf_graph* graph, const char* dir, sf_session** out);
 sf_status sf_session_destroy(sf_session* s);
-/* Autotuning knobs of the wavefront trace kernel: resident blocks per SM (2..4,
- * selecting the register budget), threads per block (256) and the march step
- * quantum after which an open segment is saved and re-queued (0 = unbounded). */
-sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t threads, uint32_t quantum);
+/* Autotuning knobs of the wavefront trace kernel (256 threads per block): resident
+ * blocks per SM (2..4, selecting the register budget; default 3), the march step
+ * quantum after which an open segment is saved and re-queued (0 = unbounded; default
+ * 128), and the regeneration threshold: how many lanes of a warp must be idle before
+ * they take new segments together (1..32, 1 = at once; default 4). */
+sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t quantum, uint32_t regen);
 
 /* ------------------------------------------------------------------ batches
  * Many jobs -- different graphs, scenes, image sizes and sample counts -- rendered
@@ -311,11 +313,14 @@ typedef struct sf_batch_job {
     sf_render_config cfg;
 } sf_batch_job;
 sf_status sf_batch_create(sf_context* ctx, const sf_batch_job* jobs, uint32_t n_jobs, sf_batch** out);
-/* Trace-kernel shape for the batch: resident blocks per SM (2..4) and step quantum. */
-sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks_per_sm, uint32_t quantum);
+/* Trace-kernel shape for the batch: resident blocks per SM (2..4), step quantum and
+ * regeneration threshold (as sf_session_set_launch). */
+sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks_per_sm, uint32_t quantum, uint32_t regen);
 /* Autotuner: times one pass per candidate shape (2..4 blocks per SM x quanta 64,
- * 128, 256), keeps the fastest, clears the films and rewinds the sample indices. */
-sf_status sf_batch_autotune(sf_batch* b, uint32_t* min_blocks_per_sm, uint32_t* quantum, float* best_ms);
+ * 128, 256, then regeneration thresholds 1, 4, 8, 16 lanes at the best of those),
+ * keeps the fastest, clears the films and rewinds the sample indices. */
+sf_status sf_batch_autotune(sf_batch* b, uint32_t* min_blocks_per_sm, uint32_t* quantum, uint32_t* regen,
+                            float* best_ms);
 /* Queues `passes` passes (graph replays when use_graph != 0); asynchronous. */
 sf_status sf_batch_run(sf_batch* b, uint32_t passes, int use_graph);
 sf_status sf_batch_sync(sf_batch* b, uint32_t timeout_ms, uint32_t* status_word);
@@ -401,7 +406,8 @@ typedef struct sf_server_config {
     uint32_t path_capacity;     /* paths per 3D batch (a request needs w*h*samples)   */
     uint32_t max_jobs;          /* requests per batch, 1..1024                        */
     uint32_t max_tile_pixels;   /* 2D pixels per batch                                */
-    uint32_t min_blocks, quantum; /* trace launch shape (sf_batch_set_launch)         */
+    uint32_t min_blocks, quantum, regen; /* trace launch shape (sf_batch_set_launch)  */
+    uint32_t pad;
 } sf_server_config;
 typedef struct sf_request {
     uint32_t kind;              /* sf_request_kind                                    */
@@ -439,7 +445,8 @@ typedef struct sf_server_stats {
     double now_ms;
 } sf_server_stats;
 /* Starts the scheduler thread. Defaults for zero fields: 4 slots, 4M paths, 256 jobs,
- * 32M tile pixels, 1 GiB of host results, launch shape 3 blocks/SM and quantum 128. */
+ * 32M tile pixels, 1 GiB of host results, launch shape 3 blocks/SM, quantum 128 and
+ * regeneration threshold 4. */
 sf_status sf_server_create(sf_context* ctx, const sf_server_config* cfg, sf_server** out);
 /* Queues a request; returns at once with its ticket (tickets start at 1). */
 sf_status sf_serve_submit(sf_server* s, const sf_request* req, uint64_t* ticket);

@@ -76,7 +76,8 @@ class sf_deep_zoom_desc(C.Structure):
 
 class sf_server_config(C.Structure):
     _fields_ = [("hbm_budget", u64), ("host_result_bytes", u64), ("slots", u32), ("path_capacity", u32),
-                ("max_jobs", u32), ("max_tile_pixels", u32), ("min_blocks", u32), ("quantum", u32)]
+                ("max_jobs", u32), ("max_tile_pixels", u32), ("min_blocks", u32), ("quantum", u32),
+                ("regen", u32), ("pad", u32)]
 
 
 class sf_request(C.Structure):
@@ -132,8 +133,8 @@ SIGNATURES = {
     "sf_session_destroy": [vp],
     "sf_session_set_launch": [vp, u32, u32, u32],
     "sf_batch_create": [vp, P(sf_batch_job), u32, P(vp)],
-    "sf_batch_set_launch": [vp, u32, u32],
-    "sf_batch_autotune": [vp, up, up, P(C.c_float)],
+    "sf_batch_set_launch": [vp, u32, u32, u32],
+    "sf_batch_autotune": [vp, up, up, up, P(C.c_float)],
     "sf_batch_run": [vp, u32, C.c_int],
     "sf_batch_sync": [vp, u32, up],
     "sf_batch_readback": [vp, u32, P(sf_film_planes)],

@@ -226,10 +226,15 @@ __device__ __forceinline__ DeRaw de_bulb(const FormParams& f, float3 p) {
     return s;
 }
 
+// Square root and quotient in the accuracy class WGSL gives its own sqrt and
+// division (a few ulp): one MUFU reciprocal square root / reciprocal and a multiply.
+__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.0f && x < SF_INF ? x * rsqrtf(x) : x; }
+
 // Mandelbox: Iterate{BoxFold, Trap, SphereFold, Scale, AddOrigin} -> NormFence.
 // NORM_MIN0: the bundled trap (slot 0, Norm, Minimum) kept as min |p|^2.
 // The sphere fold's fr^2 / r^2 uses the fast reciprocal division (<= 2 ulp, the
-// accuracy class WGSL allows for its own division).
+// accuracy class WGSL allows for its own division); for r^2 >= min_radius^2 its
+// factor is max(fr^2 / r^2, 1), which covers the r^2 >= fixed_radius^2 case.
 template <bool NORM_MIN0>
 __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     DeRaw s = raw_empty();
@@ -240,8 +245,8 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     const float sc = f.scale, asc = f.abs_scale;
     const bool sq = f.trap_squared != 0;
     float t0 = SF_INF;
-    uint32_t it = 0;
-    for (uint32_t i = 0; i < n; ++i) {
+    uint32_t i = 0;
+    for (; i < n; ++i) {
         if (dot3(p, p) > bt) break;
         p = clamp3(p, -l, l) * 2.0f - p;
         float r2 = dot3(p, p);
@@ -251,19 +256,16 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
             float v = sq ? r2 : trap_measure(f.trap_measure, p);
             trap_update(s, f.trap_slot, f.trap_mode, v);
         }
-        float k = __fdividef(fr2, r2);
-        k = r2 < fr2 ? k : 1.0f;
-        k = r2 < mr2 ? kmin : k;
+        const float k = r2 < mr2 ? kmin : fmaxf(__fdividef(fr2, r2), 1.0f);
         // sphere fold, Scale and AddOrigin as one multiply-add per component
         const float ks = k * sc;
         p = mk3(fmaf(p.x, ks, c.x), fmaf(p.y, ks, c.y), fmaf(p.z, ks, c.z));
         dr = fmaf(dr, k * asc, 1.0f);
-        it++;
     }
-    s.iter = it;
-    s.d = (len3(p) - f.fence[0]) / fabsf(dr);
+    s.iter = i;
+    s.d = __fdividef(sqrt_fast(dot3(p, p)) - f.fence[0], fabsf(dr));
     s.material = f.material;
-    if (NORM_MIN0) s.t0 = sqrtf(t0);
+    if (NORM_MIN0) s.t0 = sqrt_fast(t0);
     else if (sq) trap_sqrt(s, f.trap_slot);
     return s;
 }

@@ -1022,7 +1022,7 @@ struct sf_session {
     size_t mem_bytes = 0;
     std::vector<sf_tile> tiles;
     uint32_t tile_size = 0, dispatches = 0;
-    uint32_t min_blocks = 3, threads = 256, quantum = 128;
+    uint32_t min_blocks = 3, quantum = 128, regen = 4;
     uint32_t status_host = 0;
     double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
 };
@@ -1162,15 +1162,23 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
     return SF_OK;
 }
 
-extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t threads,
-                                           uint32_t quantum) {
-    if (!s) return fail(SF_ERR_INVALID, "null session");
-    if (threads != 256 || min_blocks_per_sm < 2 || min_blocks_per_sm > 4)
-        return fail(SF_ERR_INVALID, "trace launch: 256 threads and 2..4 resident blocks per SM");
+namespace {
+sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
+    if (min_blocks < 2 || min_blocks > 4) return fail(SF_ERR_INVALID, "trace launch: 2..4 resident blocks per SM");
     if (quantum != 0 && quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
+    if (regen < 1 || regen > 32) return fail(SF_ERR_INVALID, "regeneration threshold outside 1..32 lanes");
+    return SF_OK;
+}
+}  // namespace
+
+extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t quantum,
+                                           uint32_t regen) {
+    if (!s) return fail(SF_ERR_INVALID, "null session");
+    sf_status st = check_launch(min_blocks_per_sm, quantum, regen);
+    if (st != SF_OK) return st;
     s->min_blocks = min_blocks_per_sm;
-    s->threads = threads;
     s->quantum = quantum;
+    s->regen = regen;
     return SF_OK;
 }
 
@@ -1228,6 +1236,7 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
             tl.next_resume = s->resume + size_t(j & 1) * 2 * N;
             tl.next_resume_count = qc + 1;
             tl.quantum = j + 1 == Q ? 0u : s->quantum;  // the last launch runs segments to completion
+            tl.regen = s->regen;
             LaunchTimer t(c, true);
             CU(sf_launch_trace(s->graph->prog.form, s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks,
                                int(s->min_blocks), st));
@@ -1778,7 +1787,7 @@ struct WaveArena {
     void* mem = nullptr;
     size_t mem_bytes = 0;
     bool any_generic = false;
-    uint32_t min_blocks = 3, quantum = 128;
+    uint32_t min_blocks = 3, quantum = 128, regen = 4;
 };
 
 struct sf_batch {
@@ -1875,6 +1884,7 @@ sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, b
             tl.next_resume = a.resume + size_t(j & 1) * 2 * N;
             tl.next_resume_count = qc + 1;
             tl.quantum = j + 1 == Q ? 0u : a.quantum;
+            tl.regen = a.regen;
             LaunchTimer t(c, true, timed, st);
             CU(sf_launch_trace_batch(a.bt, a.soa, tl, c->d_stats, blocks, int(a.min_blocks), a.any_generic ? 1 : 0, st));
         }
@@ -1990,13 +2000,14 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     return SF_OK;
 }
 
-extern "C" sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks, uint32_t quantum) {
+extern "C" sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
     if (!b) return fail(SF_ERR_INVALID, "null batch");
-    if (min_blocks < 2 || min_blocks > 4) return fail(SF_ERR_INVALID, "2..4 resident blocks per SM");
-    if (quantum != 0 && quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
-    if (b->a.min_blocks != min_blocks || b->a.quantum != quantum) batch_drop_graph(b);
+    sf_status st = check_launch(min_blocks, quantum, regen);
+    if (st != SF_OK) return st;
+    if (b->a.min_blocks != min_blocks || b->a.quantum != quantum || b->a.regen != regen) batch_drop_graph(b);
     b->a.min_blocks = min_blocks;
     b->a.quantum = quantum;
+    b->a.regen = regen;
     return SF_OK;
 }
 
@@ -2041,7 +2052,8 @@ extern "C" sf_status sf_batch_sync(sf_batch* b, uint32_t timeout_ms, uint32_t* s
     return SF_OK;
 }
 
-extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t* best_q, float* best_ms) {
+extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t* best_q, uint32_t* best_regen,
+                                      float* best_ms) {
     if (!b) return fail(SF_ERR_INVALID, "null batch");
     sf_context* c = b->ctx;
     cudaSetDevice(c->device);
@@ -2049,32 +2061,47 @@ extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t*
     CU(cudaEventCreate(&e0));
     CU(cudaEventCreate(&e1));
     float best = 1e30f;
-    uint32_t bm = b->a.min_blocks, bq = b->a.quantum;
-    const uint32_t mbs[3] = {2, 3, 4}, qs[3] = {64, 128, 256};
+    uint32_t bm = b->a.min_blocks, bq = b->a.quantum, br = b->a.regen;
+    // one timed pass of a candidate shape
+    auto time_pass = [&](uint32_t mb, uint32_t q, uint32_t rg, float* ms) -> sf_status {
+        b->a.min_blocks = mb;
+        b->a.quantum = q;
+        b->a.regen = rg;
+        cudaEventRecord(e0, c->stream);
+        sf_status st = batch_record_pass(b, false);
+        cudaEventRecord(e1, c->stream);
+        if (st != SF_OK) return st;
+        cudaError_t e = cudaEventSynchronize(e1);
+        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
+        return e == cudaSuccess ? SF_OK : cuda_fail(e, "autotune");
+    };
+    // coordinate search: resident blocks x step quantum at regen 1, then the regeneration threshold
+    const uint32_t mbs[3] = {2, 3, 4}, qs[3] = {64, 128, 256}, rgs[4] = {1, 4, 8, 16};
+    sf_status st = SF_OK;
     for (uint32_t mb : mbs)
         for (uint32_t q : qs) {
-            b->a.min_blocks = mb;
-            b->a.quantum = q;
-            cudaEventRecord(e0, c->stream);
-            sf_status st = batch_record_pass(b, false);
-            cudaEventRecord(e1, c->stream);
-            if (st != SF_OK) { cudaEventDestroy(e0); cudaEventDestroy(e1); return st; }
-            cudaError_t e = cudaEventSynchronize(e1);
             float ms = 0;
-            if (e == cudaSuccess) cudaEventElapsedTime(&ms, e0, e1);
-            if (e != cudaSuccess) { cudaEventDestroy(e0); cudaEventDestroy(e1); return cuda_fail(e, "autotune"); }
-            if (ms < best) { best = ms; bm = mb; bq = q; }
+            if ((st = time_pass(mb, q, 1, &ms)) != SF_OK) break;
+            if (ms < best) { best = ms; bm = mb; bq = q; br = 1; }
         }
+    for (uint32_t i = 1; i < 4 && st == SF_OK; ++i) {
+        float ms = 0;
+        if ((st = time_pass(bm, bq, rgs[i], &ms)) != SF_OK) break;
+        if (ms < best) { best = ms; br = rgs[i]; }
+    }
     cudaEventDestroy(e0);
     cudaEventDestroy(e1);
+    if (st != SF_OK) return st;
     batch_drop_graph(b);
     b->a.min_blocks = bm;
     b->a.quantum = bq;
-    sf_status st = batch_reset(b);
+    b->a.regen = br;
+    st = batch_reset(b);
     if (st != SF_OK) return st;
     CU(cudaStreamSynchronize(c->stream));
     if (best_mb) *best_mb = bm;
     if (best_q) *best_q = bq;
+    if (best_regen) *best_regen = br;
     if (best_ms) *best_ms = best;
     return SF_OK;
 }
@@ -2629,12 +2656,13 @@ extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg
     if (!k.host_result_bytes) k.host_result_bytes = uint64_t(1) << 30;
     if (!k.min_blocks) k.min_blocks = 3;
     if (!k.quantum) k.quantum = 128;
+    if (!k.regen) k.regen = 4;
     if (!k.hbm_budget) return fail(SF_ERR_INVALID, "hbm_budget must be set");
     if (k.slots > kServeMaxSlots) return fail(SF_ERR_INVALID, "1..8 slots");
     if (k.max_jobs > SF_BATCH_MAX_JOBS) return fail(SF_ERR_INVALID, "a batch holds 1 to 1024 requests");
     if (k.path_capacity > 0x7fffffffu) return fail(SF_ERR_INVALID, "path capacity above 2^31");
-    if (k.min_blocks < 2 || k.min_blocks > 4) return fail(SF_ERR_INVALID, "2..4 resident blocks per SM");
-    if (k.quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
+    sf_status ls = check_launch(k.min_blocks, k.quantum, k.regen);
+    if (ls != SF_OK) return ls;
     cudaSetDevice(c->device);
     auto* s = new sf_server();
     s->ctx = c;
@@ -2667,6 +2695,7 @@ extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg
         if (st != SF_OK) return bail(st);
         sl.arena.min_blocks = k.min_blocks;
         sl.arena.quantum = k.quantum;
+        sl.arena.regen = k.regen;
     }
     s->t0 = ServeClock::now();
     s->thread = std::thread(serve_loop, s);

@@ -67,6 +67,7 @@ struct TraceLaunch {
     uint32_t* next_resume_count;
     uint32_t* work_counter;
     uint32_t quantum;             // march steps per segment per launch (0 = unbounded)
+    uint32_t regen;               // idle lanes a warp waits for before it takes new segments (1..32)
 };
 
 struct FilmPlanes {

@@ -107,9 +107,16 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         state = TL_NORMAL;
     };
 
+    const uint32_t regen = tl.regen ? tl.regen : 1u;
     while (true) {
-        uint32_t w = warp_fetch(tl.work_counter, state == TL_IDLE);
-        if (state == TL_IDLE) {
+        // Idle lanes take new segments together once `regen` of them are idle (or no
+        // lane is marching): the segment set-up then runs for many lanes at once
+        // instead of for one or two lanes in most iterations.
+        const uint32_t idle = __ballot_sync(FULL_MASK, state == TL_IDLE);
+        const uint32_t active = __ballot_sync(FULL_MASK, state == TL_MARCH || state == TL_CAND || state == TL_NORMAL);
+        const bool refill = idle && ((uint32_t)__popc(idle) >= regen || active == 0);
+        uint32_t w = warp_fetch(tl.work_counter, refill && state == TL_IDLE);
+        if (refill && state == TL_IDLE) {
             if (w >= total) {
                 state = TL_DONE;
             } else {
@@ -162,7 +169,10 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         if (state == TL_MARCH || state == TL_CAND || state == TL_NORMAL) {
             float3 q = m.ro + m.rd * m.t;
             if (state == TL_NORMAL) q = q + tetra_offset(tap) * hstep;
-            DeRaw s = de_form<FORM>(*Pl, q);
+            // the single-job kernel reads the program from shared memory by name (LDS)
+            DeRaw s;
+            if constexpr (MULTI) s = de_form<FORM>(*Pl, q);
+            else s = de_form<FORM>(P, q);
             n_eval++;
             n_iter += s.iter;
             if (lane_id() == (uint32_t)(__ffs(__activemask()) - 1)) n_wcall++;

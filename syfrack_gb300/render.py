@@ -229,9 +229,10 @@ class RenderSession:
         except Exception:
             pass
 
-    def set_launch(self, min_blocks_per_sm: int = 2, threads: int = 256, quantum: int = 64):
-        """Trace-kernel shape: resident blocks per SM (register budget), threads, step quantum."""
-        check(self.ctx.lib.sf_session_set_launch(self.h, min_blocks_per_sm, threads, quantum))
+    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 128, regen: int = 4):
+        """Trace-kernel shape: resident blocks per SM (register budget), step quantum,
+        regeneration threshold (idle lanes a warp waits for before taking new segments)."""
+        check(self.ctx.lib.sf_session_set_launch(self.h, min_blocks_per_sm, quantum, regen))
 
     def dispatch(self, tile, samples: int):
         """One tile, `samples` samples starting at tile.done; asynchronous."""
@@ -320,13 +321,14 @@ class Batch:
         except Exception:
             pass
 
-    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 128):
-        check(self.ctx.lib.sf_batch_set_launch(self.h, min_blocks_per_sm, quantum))
+    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 128, regen: int = 4):
+        check(self.ctx.lib.sf_batch_set_launch(self.h, min_blocks_per_sm, quantum, regen))
 
     def autotune(self):
-        mb, q, ms = C.c_uint32(), C.c_uint32(), C.c_float()
-        check(self.ctx.lib.sf_batch_autotune(self.h, C.byref(mb), C.byref(q), C.byref(ms)))
-        return mb.value, q.value, ms.value
+        """Returns (min_blocks_per_sm, quantum, regen, best pass ms)."""
+        mb, q, rg, ms = C.c_uint32(), C.c_uint32(), C.c_uint32(), C.c_float()
+        check(self.ctx.lib.sf_batch_autotune(self.h, C.byref(mb), C.byref(q), C.byref(rg), C.byref(ms)))
+        return mb.value, q.value, rg.value, ms.value
 
     def run(self, passes: int = 1, use_graph: bool = True):
         check(self.ctx.lib.sf_batch_run(self.h, passes, 1 if use_graph else 0))

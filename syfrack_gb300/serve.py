@@ -57,12 +57,12 @@ class Server:
 
     def __init__(self, renderer: Renderer, hbm_budget: int, slots: int = 4, path_capacity: int = 1 << 22,
                  max_jobs: int = 256, max_tile_pixels: int = 1 << 25, host_result_bytes: int = 1 << 30,
-                 min_blocks: int = 3, quantum: int = 128):
+                 min_blocks: int = 3, quantum: int = 128, regen: int = 4):
         self.renderer = renderer
         self.ctx = renderer.ctx
         k = sf_server_config(hbm_budget=hbm_budget, host_result_bytes=host_result_bytes, slots=slots,
                              path_capacity=path_capacity, max_jobs=max_jobs, max_tile_pixels=max_tile_pixels,
-                             min_blocks=min_blocks, quantum=quantum)
+                             min_blocks=min_blocks, quantum=quantum, regen=regen)
         h = C.c_void_p()
         check(self.ctx.lib.sf_server_create(self.ctx.h, C.byref(k), C.byref(h)))
         self.h = h

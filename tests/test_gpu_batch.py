@@ -66,8 +66,8 @@ def test_graph_replay_equals_direct_launches(renderer):
 def test_autotune_leaves_films_clean(renderer):
     jobs = small_jobs(3)
     b = Batch(renderer, jobs)
-    mb, q, ms = b.autotune()
-    assert mb in (2, 3, 4) and q in (64, 128, 256) and ms > 0
+    mb, q, rg, ms = b.autotune()
+    assert mb in (2, 3, 4) and q in (64, 128, 256) and rg in (1, 4, 8, 16) and ms > 0
     b.run(1)
     b.sync()
     for i, (sc, cfg) in enumerate(jobs):
