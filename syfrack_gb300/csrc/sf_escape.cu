@@ -120,9 +120,23 @@ static __device__ __forceinline__ float sin_multiple(float c, float s, int k) {
     return sign * b;
 }
 
+// sin(12 theta), the default stripe count of PlanarFractal: the recurrence unrolled.
+static __device__ __forceinline__ float sin_12(float c, float s) {
+    const float c2 = 2.0f * c;
+    float a = 0.0f, b = s;
+#pragma unroll
+    for (int j = 1; j < 12; ++j) {
+        float t = fmaf(c2, b, -a);
+        a = b;
+        b = t;
+    }
+    return b;
+}
+
 // One iteration; true once the orbit has escaped or spent its iteration budget.
-// POW2: the power is 2 (z^2 as one complex square).
-template <bool TRAPS, bool POW2>
+// POW2: the power is 2 (z^2 as one complex square). SK12: the stripe count is 12.
+// o.stripe accumulates sin(k theta); the bands use 0.5 n + 0.5 * that sum.
+template <bool TRAPS, bool POW2, bool SK12 = false>
 static __device__ __forceinline__ bool esc_step(const EscParams& p, EscOrbit& o) {
     if (o.count >= p.iterations) return true;
     float r2 = FA(FM(o.zx, o.zx), FM(o.zy, o.zy));
@@ -135,10 +149,12 @@ static __device__ __forceinline__ bool esc_step(const EscParams& p, EscOrbit& o)
         float radius = r2 > 0.0f ? r2 * rinv : 0.0f;
         o.ring = fminf(o.ring, fabsf(radius - p.trap_radius));
         float s = 0.0f;
-        if (r2 > 0.0f)
-            s = p.stripe_k != SF_STRIPES_GENERAL ? sin_multiple(o.zx * rinv, o.zy * rinv, p.stripe_k)
-                                                 : sinf(p.stripes * atan2f(o.zy, o.zx));
-        o.stripe += 0.5f + 0.5f * s;
+        if (r2 > 0.0f) {
+            if (SK12) s = sin_12(o.zx * rinv, o.zy * rinv);
+            else if (p.stripe_k != SF_STRIPES_GENERAL) s = sin_multiple(o.zx * rinv, o.zy * rinv, p.stripe_k);
+            else s = sinf(p.stripes * atan2f(o.zy, o.zx));
+        }
+        o.stripe += s;
     }
     float bx = p.ship ? fabsf(o.zx) : o.zx, by = p.ship ? fabsf(o.zy) : o.zy;
     float nx, ny;
@@ -207,7 +223,7 @@ static __device__ __forceinline__ void planar_sample_dev(const PlanarDev& f, flo
         while (!esc_step<TRAPS, false>(p, o)) {
         }
         planar_finish<TRAPS>(f, o.zx, o.zy, o.escaped, false, o.count, o.count, float(f.iterations), o.ring,
-                             o.stripe, dist, traps);
+                             0.5f * float(o.count) + 0.5f * o.stripe, dist, traps);
         iterations = measured_out = o.count;
         return;
     }
@@ -358,6 +374,14 @@ __global__ void __launch_bounds__(256) k_escape2d_root(const PlanarDev* __restri
 // Without TRAPS only dist, traps[0 .. n) (smooth time) and iters are written.
 constexpr int ESC_CHUNK = 16;
 
+// Up to ESC_CHUNK iterations; true once the orbit has ended.
+template <bool TRAPS, bool POW2, bool SK12>
+static __device__ __forceinline__ bool esc_chunk(const EscParams& p, EscOrbit& o) {
+    for (int j = 0; j < ESC_CHUNK; ++j)
+        if (esc_step<TRAPS, POW2, SK12>(p, o)) return true;
+    return false;
+}
+
 template <bool TRAPS>
 __global__ void __launch_bounds__(256, 5) k_escape2d(const PlanarDev* __restrict__ fg,
                                                      const CanvasDev* __restrict__ cg, uint32_t tile_x,
@@ -373,7 +397,7 @@ __global__ void __launch_bounds__(256, 5) k_escape2d(const PlanarDev* __restrict
     unsigned long long total_iters = 0;
     const float scale = __fdiv_rn(6.0f, K.zoom);
     const EscParams p = esc_params(F);
-    const bool pow2 = p.power == 2;
+    const bool pow2 = p.power == 2, sk12 = p.stripe_k == 12;
     EscOrbit o;
     uint32_t pix = 0;
     bool busy = false, live = true;
@@ -395,16 +419,14 @@ __global__ void __launch_bounds__(256, 5) k_escape2d(const PlanarDev* __restrict
         }
         if (!__any_sync(FULL_MASK, busy)) break;
         if (busy) {
-            bool done = false;
-            if (pow2) {
-                for (int j = 0; j < ESC_CHUNK && !done; ++j) done = esc_step<TRAPS, true>(p, o);
-            } else {
-                for (int j = 0; j < ESC_CHUNK && !done; ++j) done = esc_step<TRAPS, false>(p, o);
-            }
+            bool done;
+            if (pow2 && sk12) done = esc_chunk<TRAPS, true, true>(p, o);
+            else if (pow2) done = esc_chunk<TRAPS, true, false>(p, o);
+            else done = esc_chunk<TRAPS, false, false>(p, o);
             if (done) {
                 float tr[4], d;
                 planar_finish<TRAPS>(F, o.zx, o.zy, o.escaped, false, o.count, o.count, float(F.iterations), o.ring,
-                                     o.stripe, d, tr);
+                                     0.5f * float(o.count) + 0.5f * o.stripe, d, tr);
                 store_pixel(dist, traps, iters, n, pix, d, tr, o.count, TRAPS);
                 total_iters += o.count;
                 busy = false;
