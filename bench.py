@@ -574,6 +574,79 @@ def run_primary(args):
     ctx.close()
 
 
+def frame_size(args, w, h):
+    """The workload's frame, or --frame WxH (smaller frames are for profiler captures)."""
+    if not args.frame:
+        return w, h
+    fw, fh = args.frame.lower().split("x")
+    return int(fw), int(fh)
+
+
+def run_tile(args):
+    """The largest 2D tile of the serving mix through the plain call sf_escape2d:
+    Burning Ship, 2048x2048, 20,000 iterations, every trap (ring, stripe bands,
+    final angle), the canvas around the ship (centre (-0.45, -0.5), zoom 1.8) at
+    pixel centres. value = iterations per second of k_escape2d (CUDA events); e2e =
+    the same through the call with host outputs (24 B per pixel read back); the
+    oracle in FP32 on all host cores over a seeded pixel sample of the same tile."""
+    import numpy as np
+
+    from syfrack_gb300 import Canvas, GpuContext, PlanarFractal, escape2d
+
+    ctx = GpuContext(0)
+    W, H = frame_size(args, 2048, 2048)
+    f = PlanarFractal(family="BurningShip", iterations=20000)
+    canvas = Canvas(width=W, height=H, center=(-0.45, -0.5), zoom=1.8)
+    for _ in range(max(args.warmup, 3)):
+        escape2d(ctx, f, canvas)
+    ctx.set_profiling(True)
+    walls, kms, iters = [], [], []
+    for _ in range(args.steps):
+        ctx.reset_stats()
+        t0 = time.perf_counter()
+        out = escape2d(ctx, f, canvas)
+        walls.append(time.perf_counter() - t0)
+        st = ctx.stats()
+        kms.append(st["trace_ms"])
+        iters.append(st["de_iterations"])
+    ctx.set_profiling(False)
+    it_frame, kernel_ms, wall = float(np.median(iters)), float(np.median(kms)), float(np.median(walls))
+    line = {"metric": "2D escape-time Giter/s", "unit": "Giter/s", "value": it_frame / (kernel_ms * 1e-3) / 1e9,
+            "higher_is_better": True, "workload": f"burning_ship_{W}x{H}_20k_iter_traps", "steps": args.steps,
+            "kernel_ms_per_tile": kernel_ms, "iterations_per_tile": it_frame,
+            "mean_iterations_per_pixel": float(out["iterations"].mean()),
+            "e2e": {"value": it_frame / wall / 1e9, "unit": "Giter/s", "tile_ms": wall * 1e3,
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": W * H * 24, "call": "escape2d (sf_escape2d)"},
+            "dtype": "f32", "data": "synthetic (the serving mix's largest tile)"}
+    if not args.no_cpu_baseline:
+        sys.path.insert(0, os.path.join(ROOT, "oracle"))
+        import oracle  # the CPU restatement; used only as the baseline here
+
+        from syfrack_gb300.render import FAMILIES
+
+        rng = np.random.default_rng(4)
+        idx = rng.choice(W * H, 4096, replace=False)
+        f32 = np.float32
+        u = (idx % W).astype(np.float32) + f32(0.5)
+        v = (idx // W).astype(np.float32) + f32(0.5)
+        scale = f32(6.0) / f32(canvas.zoom)
+        qx = f32(canvas.center[0]) + (u / f32(W) - f32(0.5)) * scale
+        qy = f32(canvas.center[1]) + ((f32(0.5) - v / f32(H)) / (f32(W) / f32(H))) * scale
+        pp = oracle.PlanarParams()
+        pp.family = FAMILIES.index(f.family)
+        pp.power, pp.iterations = f.power, f.iterations
+        for k in ("zoom", "angle", "inversion", "twist", "relaxation", "memory", "bailout", "trap_radius", "stripes"):
+            setattr(pp, k, float(np.float32(getattr(f, k))))
+        threads = os.cpu_count() or 1
+        t0 = time.perf_counter()
+        ref = oracle.planar(pp, np.stack([qx, qy], 1), precision=32, threads=threads)
+        dt = time.perf_counter() - t0
+        line["cpu_baseline"] = {"value": float(ref["iterations"].sum()) / dt / 1e9, "unit": "Giter/s",
+                                "cores": threads, "kind": "port", "sample": f"{len(idx)} seeded pixels of the tile, FP32"}
+    print(json.dumps(line), flush=True)
+    ctx.close()
+
+
 def run_deepzoom(args):
     """Mandelbrot deep zoom: 3840x2160, max 50,000 iterations, width 1e-12 around a
     seeded boundary point (FP64 bisection of the escape label along a random ray from
@@ -588,10 +661,11 @@ def run_deepzoom(args):
     from syfrack_gb300 import GpuContext, deep_zoom, workloads
 
     ctx = GpuContext(0)
-    W, H, MI, width = 3840, 2160, 50000, 1e-12
+    W, H = frame_size(args, 3840, 2160)
+    MI, width = 50000, 1e-12
     c = workloads.deep_zoom_center(seed=2026, max_iter=MI)
     for _ in range(max(args.warmup, 3)):
-        deep_zoom(ctx, c, (0.0, 0.0), width, 960, 540, MI, bailout=16.0)
+        deep_zoom(ctx, c, (0.0, 0.0), width, min(W, 960), min(H, 540), MI, bailout=16.0)
     ctx.set_profiling(True)
     walls, kms, iters = [], [], []
     out = None
@@ -610,6 +684,26 @@ def run_deepzoom(args):
     near64 = float((np.abs(it.astype(np.int64) - it64.astype(np.int64)) <= 1).mean())
     both = (it == it64) & (it < MI)
     smooth_err = np.abs(full["smooth"].ravel()[both] - full["smooth_f64"].ravel()[both])
+    iters_per_frame = float(np.median(iters))
+    kernel_ms = float(np.median(kms))
+    line = {"metric": "deep-zoom perturbation Giter/s", "unit": "Giter/s",
+            "value": iters_per_frame / (kernel_ms * 1e-3) / 1e9, "higher_is_better": True,
+            "workload": f"mandelbrot_deep_zoom_{W}x{H}_50k_iter_width1e-12", "steps": args.steps,
+            "center": list(c), "kernel_ms_per_frame": kernel_ms, "iterations_per_frame": iters_per_frame,
+            "e2e": {"value": iters_per_frame / float(np.median(walls)) / 1e9, "unit": "Giter/s",
+                    "frame_ms": float(np.median(walls)) * 1e3, "h2d_bytes_per_step": 0,
+                    "d2h_bytes_per_step": W * H * 8, "call": "deep_zoom (sf_deep_zoom)"},
+            "rebases_per_frame": out["rebases"],
+            "agreement": {"perturbation_vs_fp64_direct_all_pixels": agree64,
+                          "perturbation_vs_fp64_direct_within_1": near64,
+                          "smooth_abs_err_vs_fp64_where_counts_agree": {
+                              "mean": float(smooth_err.mean()) if smooth_err.size else None,
+                              "max": float(smooth_err.max()) if smooth_err.size else None}},
+            "dtype": "f32 deltas, f64 reference orbit", "data": "synthetic (seeded boundary point)"}
+    if args.no_cpu_baseline:
+        print(json.dumps(line), flush=True)
+        ctx.close()
+        return
     # truth: binary128 on a seeded sample (oracle, all host cores), timed as the CPU baseline
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the CPU restatement; used only as the baseline and checker here
@@ -628,32 +722,17 @@ def run_deepzoom(args):
     t0 = time.perf_counter()
     cpu64, _ = oracle.mandel_escape(np.array(c), np.zeros(2), off, MI, 16.0, precision=64, threads=threads)
     t64 = time.perf_counter() - t0
-    iters_per_frame = float(np.median(iters))
-    kernel_ms = float(np.median(kms))
-    line = {"metric": "deep-zoom perturbation Giter/s", "unit": "Giter/s",
-            "value": iters_per_frame / (kernel_ms * 1e-3) / 1e9, "higher_is_better": True,
-            "workload": "mandelbrot_deep_zoom_3840x2160_50k_iter_width1e-12", "steps": args.steps,
-            "center": list(c), "kernel_ms_per_frame": kernel_ms, "iterations_per_frame": iters_per_frame,
-            "e2e": {"value": iters_per_frame / float(np.median(walls)) / 1e9, "unit": "Giter/s",
-                    "frame_ms": float(np.median(walls)) * 1e3, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": W * H * 8, "call": "deep_zoom (sf_deep_zoom)"},
-            "rebases_per_frame": out["rebases"],
-            "agreement": {"perturbation_vs_fp64_direct_all_pixels": agree64,
-                          "perturbation_vs_fp64_direct_within_1": near64,
-                          "smooth_abs_err_vs_fp64_where_counts_agree": {
-                              "mean": float(smooth_err.mean()) if smooth_err.size else None,
-                              "max": float(smooth_err.max()) if smooth_err.size else None},
-                          "sample_pixels": len(idx),
-                          "perturbation_vs_binary128": float((it[idx] == truth).mean()),
-                          "perturbation_vs_binary128_within_1": float(
-                              (np.abs(it[idx].astype(np.int64) - truth.astype(np.int64)) <= 1).mean()),
-                          "fp64_direct_gpu_vs_binary128": float((it64[idx] == truth).mean()),
-                          "fp64_direct_cpu_vs_binary128": float((cpu64 == truth).mean())},
-            "cpu_baseline": {"value": float(np.sum(np.minimum(cpu64, MI))) / t64 / 1e9, "unit": "Giter/s",
-                             "cores": threads, "kind": "port",
-                             "sample": f"{len(idx)} seeded pixels, FP64 direct iteration "
-                                       f"({t64:.2f} s; binary128 on the same pixels {t128:.2f} s)"},
-            "dtype": "f32 deltas, f64 reference orbit", "data": "synthetic (seeded boundary point)"}
+    line["agreement"].update({
+        "sample_pixels": len(idx),
+        "perturbation_vs_binary128": float((it[idx] == truth).mean()),
+        "perturbation_vs_binary128_within_1": float(
+            (np.abs(it[idx].astype(np.int64) - truth.astype(np.int64)) <= 1).mean()),
+        "fp64_direct_gpu_vs_binary128": float((it64[idx] == truth).mean()),
+        "fp64_direct_cpu_vs_binary128": float((cpu64 == truth).mean())})
+    line["cpu_baseline"] = {"value": float(np.sum(np.minimum(cpu64, MI))) / t64 / 1e9, "unit": "Giter/s",
+                            "cores": threads, "kind": "port",
+                            "sample": f"{len(idx)} seeded pixels, FP64 direct iteration "
+                                      f"({t64:.2f} s; binary128 on the same pixels {t128:.2f} s)"}
     print(json.dumps(line), flush=True)
     ctx.close()
 
@@ -673,7 +752,8 @@ def main():
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
     ap.add_argument("--workload", default="pathtrace",
-                    choices=["pathtrace", "batch", "serve", "primary", "deepzoom"])
+                    choices=["pathtrace", "batch", "serve", "primary", "deepzoom", "tile"])
+    ap.add_argument("--frame", default=None, help="WxH override of the deepzoom/tile frame (profiling only)")
     ap.add_argument("--jobs", type=int, default=64)
     # serving stream
     ap.add_argument("--rate", type=float, default=200.0)
@@ -693,6 +773,8 @@ def main():
         run_primary(args)
     elif args.workload == "deepzoom":
         run_deepzoom(args)
+    elif args.workload == "tile":
+        run_tile(args)
     else:
         run_ours(args)
 
