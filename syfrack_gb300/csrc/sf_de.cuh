@@ -64,8 +64,9 @@ struct DeSampleF {
     uint32_t material;
 };
 
+// (t / scale).min(1): the quotient in WGSL's division accuracy class (<= 2 ulp).
 __device__ __forceinline__ float trap_norm(float t, float scale) {
-    return isfinite(t) ? fminf(t / scale, 1.0f) : 1.0f;
+    return isfinite(t) ? fminf(__fdividef(t, scale), 1.0f) : 1.0f;
 }
 __device__ __forceinline__ DeSampleF de_finalize(const DeProgram& P, const DeRaw& r) {
     DeSampleF s;

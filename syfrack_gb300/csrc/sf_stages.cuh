@@ -39,6 +39,19 @@ static __device__ __forceinline__ uint32_t load_path(const PathSoA& soa, uint32_
     return flags;
 }
 
+// A segment's march state at its start -- the nearest emitter on the ray
+// (lights.wgsl:183-209) bounds it, then march_begin's fields -- written to the path's
+// continuation row (row = path) or shadow row (row = path + capacity) by the stage
+// that creates the ray, so the trace kernel only loads it.
+static __device__ __forceinline__ void begin_segment(const DevScene& S, PathSoA& soa, uint32_t row, float3 ro,
+                                                     float3 rd, float t_end) {
+    uint32_t li;
+    const float te = nearest_emitter(S, ro, rd, t_end, li);
+    soa.m0[row] = make_float4(0.0f, 1.2f, 0.0f, 0.0f);    // t, omega, previous radius, step
+    soa.m1[row] = make_float4(te, 0.0f, 1e30f, 0.0f);     // t_end, candidate t, candidate error, steps (0)
+    soa.m2[row] = li;
+}
+
 // wf_generate (wavefront.wgsl:160-179) for one path: camera ray and RNG.
 // `local` indexes the path within its job (g), `path` its row in the SoA.
 static __device__ __forceinline__ void generate_path(const DevScene& S, PathSoA& soa, const DispatchGeom& g,
@@ -48,6 +61,7 @@ static __device__ __forceinline__ void generate_path(const DevScene& S, PathSoA&
     PathState ps;
     path_begin(S, ps, px, py, sample);
     store_path(soa, path, ps, SF_PF_CONT);
+    begin_segment(S, soa, path, ps.o, ps.d, S.extent);
 }
 
 // wf_shade + wf_compact (wavefront.wgsl:196-223) for one path: resolve last round's
@@ -103,6 +117,11 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
         nf = 0;
     }
     store_path(soa, path, ps, nf);
+    if (nf & SF_PF_CONT) begin_segment(S, soa, path, ps.o, ps.d, S.extent);
+    if (nf & SF_PF_SHADOW) {
+        const float4 so = soa.sh_o[path], sd = soa.sh_d[path];
+        begin_segment(S, soa, path + soa.capacity, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w);
+    }
     if (!nf) soa.Ls[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
     return nf;
 }

@@ -140,19 +140,18 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                 }
                 float4 o = shadow ? soa.sh_o[path] : soa.o[path];
                 float4 d = shadow ? soa.sh_d[path] : soa.d[path];
-                float3 ro = mk3(o.x, o.y, o.z), rd = mk3(d.x, d.y, d.z);
+                // the march state: set by the stage that made the ray, or saved by the
+                // previous launch at its step quantum
+                const uint32_t row = path + (shadow ? cap : 0u);
+                const float4 a = soa.m0[row], b = soa.m1[row];
+                m.ro = mk3(o.x, o.y, o.z);
+                m.rd = mk3(d.x, d.y, d.z);
+                m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
+                m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
+                li = soa.m2[row];
                 if (first) {
-                    float t_end = nearest_emitter(*Sl, ro, rd, shadow ? o.w : Sl->extent, li);
-                    march_begin(m, ro, rd, t_end);
                     if (shadow) n_shseg++;
                     else n_seg++;
-                } else {
-                    uint32_t row = path + (shadow ? cap : 0u);
-                    float4 a = soa.m0[row], b = soa.m1[row];
-                    m.ro = ro; m.rd = rd;
-                    m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
-                    m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
-                    li = soa.m2[row];
                 }
                 budget = quantum;
                 state = TL_MARCH;
