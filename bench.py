@@ -154,6 +154,18 @@ def run_reference(args):
     print(json.dumps(line), flush=True)
 
 
+def reduce_ranks(dist, elapsed, work, device):
+    """Replicas: the slowest rank's time (max) and every rank's work (sum); with no
+    exchange on the data path these two numbers are all the ranks share."""
+    import torch
+
+    t = torch.tensor([float(elapsed), float(work)], dtype=torch.float64, device=device)
+    mx = t.clone()
+    dist.all_reduce(mx, op=dist.ReduceOp.MAX)
+    dist.all_reduce(t, op=dist.ReduceOp.SUM)
+    return float(mx[0]), float(t[1])
+
+
 def run_ours(args):
     import ctypes as C
 
@@ -208,13 +220,7 @@ def run_ours(args):
     st = ctx.stats()
     segs = st["segments"]
     if dist:
-        import torch
-
-        t = torch.tensor([ms, float(segs)], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        ms_max, segs_all = float(mx[0]), float(t[1])
+        ms_max, segs_all = reduce_ranks(dist, ms, segs, "cuda")
     else:
         ms_max, segs_all = ms, float(segs)
     value = segs_all / (ms_max * 1e-3) / 1e6
@@ -241,11 +247,7 @@ def run_ours(args):
         e2e_s = time.perf_counter() - t0
         e2e_segs = ctx.stats()["segments"]
     if dist:
-        t = torch.tensor([e2e_s, float(e2e_segs)], dtype=torch.float64, device="cuda")
-        mx = t.clone()
-        dist.all_reduce(mx, op=dist.ReduceOp.MAX)
-        dist.all_reduce(t, op=dist.ReduceOp.SUM)
-        e2e_s, e2e_segs = float(mx[0]), float(t[1])
+        e2e_s, e2e_segs = reduce_ranks(dist, e2e_s, e2e_segs, "cuda")
     e2e = e2e_segs / e2e_s / 1e6
     px = e2e_cfg.width * e2e_cfg.height
     d2h = px * (16 + 4 + 16)
@@ -267,7 +269,7 @@ def run_ours(args):
                        "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
                        "launch": {"min_blocks_per_sm": args.min_blocks, "quantum": args.quantum,
                                   "regen": args.regen},
-                       "l2": "inputs larger than L2 (path state 1.4 GB per step)",
+                       "l2": "inputs larger than L2 (path state 1.9 GB per step)",
                        "segments_per_step": segs_all / args.steps,
                        "pixel_samples_per_s": cfg.width * cfg.height * SPP_PER_STEP * args.steps * n_ranks
                        / (ms_max * 1e-3)},

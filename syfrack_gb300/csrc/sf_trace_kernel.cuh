@@ -83,6 +83,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     March m;
     float3 grad = mk3(0.f, 0.f, 0.f);
     float hstep = 0.f;
+    uint32_t hit_w = 0;  // iterations | material << 16 of the surface hit whose normal is being tapped
     uint32_t n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0;
 
     // End of a continuation or shadow segment without a surface sample.
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         DeSampleF smp = de_finalize(*Pl, s);
         soa.hit[path] = make_uint4(__float_as_uint(m.t), m.i, SF_NO_LIGHT, SF_HF_HIT);
         soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
-        soa.hit_n[path] = make_float4(0.f, 0.f, 0.f, __uint_as_float(smp.iter | (smp.material << 16)));
+        hit_w = smp.iter | (smp.material << 16);  // stored with the normal after the last tap
         hstep = fmaxf(m.t * cone * 0.5f, 1e-4f) * tol;
         grad = mk3(0.f, 0.f, 0.f);
         tap = 0;
@@ -178,9 +179,9 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             if (state == TL_NORMAL) {
                 grad = grad + tetra_offset(tap) * s.d;
                 if (++tap == 4) {
-                    float3 n = normalize3(grad);
-                    float4 hn = soa.hit_n[path];
-                    soa.hit_n[path] = make_float4(n.x, n.y, n.z, hn.w);
+                    // the taps of a hit end in the launch that found it (no quantum applies)
+                    const float3 n = grad * rsqrtf(dot3(grad, grad));
+                    soa.hit_n[path] = make_float4(n.x, n.y, n.z, __uint_as_float(hit_w));
                     state = TL_IDLE;
                 }
             } else if (state == TL_CAND) {
