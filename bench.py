@@ -708,7 +708,7 @@ def run_deepzoom(args):
         return
     # truth: binary128 on a seeded sample (oracle, all host cores), timed as the CPU baseline
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
-    import oracle  # the CPU restatement; used only as the baseline and checker here
+    import oracle  # the CPU restatement; the baseline here, and the truth for the counts
 
     rng = np.random.default_rng(11)
     idx = rng.choice(W * H, 4096, replace=False)

@@ -1,7 +1,7 @@
 // TEST INFRASTRUCTURE -- NOT THE PRODUCT.
 //
-// CPU restatement of SyFrack's distance-estimator path, used only as the
-// checker by tests/, __graft_entry__.smoke() and bench.py's cpu_baseline leg.
+// CPU restatement of SyFrack's distance-estimator path, used only to check
+// results in tests/ and __graft_entry__.smoke(), and as bench.py's CPU baseline.
 // Templated on the real type R:
 //   R = float  : the reference's own binary32 arithmetic, operation order kept
 //                (built with -ffp-contract=off, libm float functions, like Rust's
