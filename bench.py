@@ -746,7 +746,7 @@ def main():
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
     ap.add_argument("--min-blocks", type=int, default=3)
-    ap.add_argument("--quantum", type=int, default=128)
+    ap.add_argument("--quantum", type=int, default=0)
     ap.add_argument("--regen", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")
     # smaller frames are for profiler captures only; the measured workload is 1280x720

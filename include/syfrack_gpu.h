@@ -294,9 +294,9 @@ sf_status sf_session_resume(sf_context* ctx, sf_graph* graph, const char* dir, s
 sf_status sf_session_destroy(sf_session* s);
 /* Autotuning knobs of the wavefront trace kernel (256 threads per block): resident
  * blocks per SM (2..4, selecting the register budget; default 3), the march step
- * quantum after which an open segment is saved and re-queued (0 = unbounded; default
- * 128), and the regeneration threshold: how many lanes of a warp must be idle before
- * they take new segments together (1..32, 1 = at once; default 4). */
+ * quantum after which an open segment is saved and re-queued (0 = unbounded, the
+ * default), and the regeneration threshold: how many lanes of a warp must be idle
+ * before they take new segments together (1..32, 1 = at once; default 4). */
 sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t quantum, uint32_t regen);
 
 /* ------------------------------------------------------------------ batches
@@ -316,8 +316,8 @@ sf_status sf_batch_create(sf_context* ctx, const sf_batch_job* jobs, uint32_t n_
 /* Trace-kernel shape for the batch: resident blocks per SM (2..4), step quantum and
  * regeneration threshold (as sf_session_set_launch). */
 sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks_per_sm, uint32_t quantum, uint32_t regen);
-/* Autotuner: times one pass per candidate shape (2..4 blocks per SM x quanta 64,
- * 128, 256, then regeneration thresholds 1, 4, 8, 16 lanes at the best of those),
+/* Autotuner: times one pass per candidate shape (2..4 blocks per SM x quanta 0,
+ * 64, 128, 256, then regeneration thresholds 1, 4, 8, 16 lanes at the best of those),
  * keeps the fastest, clears the films and rewinds the sample indices. */
 sf_status sf_batch_autotune(sf_batch* b, uint32_t* min_blocks_per_sm, uint32_t* quantum, uint32_t* regen,
                             float* best_ms);

@@ -1022,7 +1022,7 @@ struct sf_session {
     size_t mem_bytes = 0;
     std::vector<sf_tile> tiles;
     uint32_t tile_size = 0, dispatches = 0;
-    uint32_t min_blocks = 3, quantum = 128, regen = 4;
+    uint32_t min_blocks = 3, quantum = 0, regen = 4;
     uint32_t status_host = 0;
     double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
 };
@@ -2075,8 +2075,8 @@ extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t*
         if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
         return e == cudaSuccess ? SF_OK : cuda_fail(e, "autotune");
     };
-    // coordinate search: resident blocks x step quantum at regen 1, then the regeneration threshold
-    const uint32_t mbs[3] = {2, 3, 4}, qs[3] = {64, 128, 256}, rgs[4] = {1, 4, 8, 16};
+    // coordinate search: resident blocks x step quantum (0 = none) at regen 1, then the regeneration threshold
+    const uint32_t mbs[3] = {2, 3, 4}, qs[4] = {0, 64, 128, 256}, rgs[4] = {1, 4, 8, 16};
     sf_status st = SF_OK;
     for (uint32_t mb : mbs)
         for (uint32_t q : qs) {

@@ -229,7 +229,7 @@ class RenderSession:
         except Exception:
             pass
 
-    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 128, regen: int = 4):
+    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 0, regen: int = 4):
         """Trace-kernel shape: resident blocks per SM (register budget), step quantum,
         regeneration threshold (idle lanes a warp waits for before taking new segments)."""
         check(self.ctx.lib.sf_session_set_launch(self.h, min_blocks_per_sm, quantum, regen))

@@ -67,7 +67,7 @@ def test_autotune_leaves_films_clean(renderer):
     jobs = small_jobs(3)
     b = Batch(renderer, jobs)
     mb, q, rg, ms = b.autotune()
-    assert mb in (2, 3, 4) and q in (64, 128, 256) and rg in (1, 4, 8, 16) and ms > 0
+    assert mb in (2, 3, 4) and q in (0, 64, 128, 256) and rg in (1, 4, 8, 16) and ms > 0
     b.run(1)
     b.sync()
     for i, (sc, cfg) in enumerate(jobs):

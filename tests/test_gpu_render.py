@@ -45,6 +45,29 @@ def test_wavefront_equals_megakernel(renderer):
     assert a.color[..., :3].mean() > 0.01  # the light reaches the form
 
 
+@pytest.mark.parametrize("shape", [(2, 16, 1), (4, 64, 8), (3, 256, 32)])
+def test_launch_shapes_give_the_same_film(renderer, shape):
+    # march state saved at a step quantum and resumed by the next launch, any
+    # regeneration threshold and any register budget: the same film bit for bit
+    scene = workloads.mandelbox_scene()
+    cfg = small_cfg("wavefront")
+    base = RenderSession(renderer, scene, cfg)
+    base.set_launch(3, 0, 4)
+    while not base.step(0):
+        pass
+    ref = base.readback()
+    base.close()
+    s = RenderSession(renderer, scene, cfg)
+    s.set_launch(*shape)
+    while not s.step(0):
+        pass
+    out = s.readback()
+    assert s.sync() == 0
+    s.close()
+    np.testing.assert_array_equal(out.accum, ref.accum)
+    np.testing.assert_array_equal(out.depth, ref.depth)
+
+
 def test_film_against_oracle(renderer, oracle_mod):
     scene = workloads.mandelbox_scene()
     cfg = small_cfg("wavefront", spp=16, spd=8)
