@@ -66,7 +66,9 @@ struct DeSampleF {
 
 // (t / scale).min(1): the quotient in WGSL's division accuracy class (<= 2 ulp).
 __device__ __forceinline__ float trap_norm(float t, float scale) {
-    return isfinite(t) ? fminf(__fdividef(t, scale), 1.0f) : 1.0f;
+    float q;
+    asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(q) : "f"(t), "f"(scale));
+    return isfinite(t) ? fminf(q, 1.0f) : 1.0f;
 }
 __device__ __forceinline__ DeSampleF de_finalize(const DeProgram& P, const DeRaw& r) {
     DeSampleF s;
@@ -117,14 +119,32 @@ __device__ __forceinline__ void trap_sqrt(DeRaw& s, uint32_t slot) {
     else s.t3 = sqrtf(s.t3);
 }
 
+// Square root and quotient in the accuracy class WGSL gives its own sqrt and
+// division (a few ulp): one MUFU reciprocal square root / reciprocal and a multiply.
+__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.0f && x < SF_INF ? x * rsqrtf(x) : x; }
+// 1/x by the hardware approximation (PTX rcp.approx.ftz.f32, max error 1 ulp):
+// x / y as x * rcp_approx(y) is within 2 ulp for normal y.
+__device__ __forceinline__ float rcp_approx(float x) {
+    float r;
+    asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+
 // integral_spherical_power (eval.rs:129-178): complex powers of the polar and
 // azimuthal unit vectors; n = 6, 8 by repeated squaring, other n by binary powers.
+// The quotients by r and rho use the hardware reciprocal (WGSL's division accuracy
+// class, as the reference's bulb_power68 on the GPU).
 __device__ __forceinline__ void spherical_power(float3 p, float r, uint32_t n, float3& out, float& deriv) {
     if (n == 1) { out = p; deriv = 1.0f; return; }
-    float rho = sqrtf(p.x * p.x + p.y * p.y);
-    float tx = fminf(fmaxf(p.z / r, -1.0f), 1.0f), ty = rho / r;
+    const float rho = sqrt_fast(p.x * p.x + p.y * p.y);
+    const float ir = rcp_approx(r);
+    float tx = fminf(fmaxf(p.z * ir, -1.0f), 1.0f), ty = rho * ir;
     float fx = 1.0f, fy = 0.0f;
-    if (rho > 0.0f) { fx = p.x / rho; fy = p.y / rho; }
+    if (rho > 0.0f) {
+        const float irho = rcp_approx(rho);
+        fx = p.x * irho;
+        fy = p.y * irho;
+    }
     if (n == 8 || n == 6) {
         float t2x = tx * tx - ty * ty, t2y = 2.0f * tx * ty;
         float f2x = fx * fx - fy * fy, f2y = 2.0f * fx * fy;
@@ -190,13 +210,13 @@ __device__ __forceinline__ void power_op(float3& p, float& dr, float radius, flo
 }
 
 __device__ __forceinline__ float bulb_fence(float3 p, float dr) {
-    float r = fmaxf(len3(p), 1e-12f);
-    return 0.5f * logf(r) * r / dr;
+    float r = fmaxf(sqrt_fast(dot3(p, p)), 1e-12f);
+    return 0.5f * logf(r) * r * rcp_approx(dr);
 }
 __device__ __forceinline__ float box_fence(float3 p, float3 half, float dr) {
     float3 q = abs3(p) - half;
     float3 qm = mk3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
-    return (len3(qm) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f)) / dr;
+    return (sqrt_fast(dot3(qm, qm)) + fminf(fmaxf(q.x, fmaxf(q.y, q.z)), 0.0f)) * rcp_approx(dr);
 }
 
 __device__ __forceinline__ DeRaw raw_empty() {
@@ -213,6 +233,8 @@ __device__ __forceinline__ DeRaw de_bulb(const FormParams& f, float3 p) {
     float dr = 1.0f;
     const uint32_t n = f.iterations;
     for (uint32_t i = 0; i < n; ++i) {
+        // |p| correctly rounded: the power raises it to the n-th, which would multiply
+        // any error by n
         float r = len3(p);
         if (r > f.bailout) break;
         float v = f.trap_measure == SF_MEASURE_NORM ? r : trap_measure(f.trap_measure, p);
@@ -227,9 +249,6 @@ __device__ __forceinline__ DeRaw de_bulb(const FormParams& f, float3 p) {
     return s;
 }
 
-// Square root and quotient in the accuracy class WGSL gives its own sqrt and
-// division (a few ulp): one MUFU reciprocal square root / reciprocal and a multiply.
-__device__ __forceinline__ float sqrt_fast(float x) { return x > 0.0f && x < SF_INF ? x * rsqrtf(x) : x; }
 
 // Mandelbox: Iterate{BoxFold, Trap, SphereFold, Scale, AddOrigin} -> NormFence.
 // NORM_MIN0: the bundled trap (slot 0, Norm, Minimum) kept as min |p|^2.
@@ -257,14 +276,14 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
             float v = sq ? r2 : trap_measure(f.trap_measure, p);
             trap_update(s, f.trap_slot, f.trap_mode, v);
         }
-        const float k = r2 < mr2 ? kmin : fmaxf(__fdividef(fr2, r2), 1.0f);
+        const float k = r2 < mr2 ? kmin : fmaxf(fr2 * rcp_approx(r2), 1.0f);
         // sphere fold, Scale and AddOrigin as one multiply-add per component
         const float ks = k * sc;
         p = mk3(fmaf(p.x, ks, c.x), fmaf(p.y, ks, c.y), fmaf(p.z, ks, c.z));
         dr = fmaf(dr, k * asc, 1.0f);
     }
     s.iter = i;
-    s.d = __fdividef(sqrt_fast(dot3(p, p)) - f.fence[0], fabsf(dr));
+    s.d = (sqrt_fast(dot3(p, p)) - f.fence[0]) * rcp_approx(fabsf(dr));
     s.material = f.material;
     if (NORM_MIN0) s.t0 = sqrt_fast(t0);
     else if (sq) trap_sqrt(s, f.trap_slot);

@@ -85,7 +85,7 @@ __device__ __forceinline__ int march_update(March& m, float d, float safety, flo
     if (sor_fail) { m.step_len = m.step_len - m.omega * m.step_len; m.omega = 1.0f; }
     else m.step_len = radius * m.omega;
     m.prev_radius = radius;
-    float err = absolute ? radius : __fdividef(radius, fmaxf(m.t, 1e-6f));
+    float err = absolute ? radius : radius * rcp_approx(fmaxf(m.t, 1e-6f));
     if (!sor_fail && err < m.cand_err) { m.cand_t = m.t; m.cand_err = err; }
     if (!sor_fail && (absolute ? err <= accept : err < accept)) return MARCH_HIT;
     if (!sor_fail && m.t + m.step_len >= m.t_end) {
