@@ -97,6 +97,29 @@ __device__ __forceinline__ int march_update(March& m, float d, float safety, flo
     return MARCH_CONTINUE;
 }
 
+// ------------------------------------------------------------------ shading arithmetic
+// The shading code below (not the march and not the DE) uses WGSL's accuracy class
+// for division (2.5 ulp) and sqrt: PTX div.approx / sqrt.approx and the reciprocal
+// square root, a few ulp each, instead of the correctly rounded slow paths.
+__device__ __forceinline__ float wdiv(float a, float b) {
+    float q;
+    asm("div.approx.ftz.f32 %0, %1, %2;" : "=f"(q) : "f"(a), "f"(b));
+    return q;
+}
+__device__ __forceinline__ float wsqrt(float x) {
+    float r;
+    asm("sqrt.approx.ftz.f32 %0, %1;" : "=f"(r) : "f"(x));
+    return r;
+}
+__device__ __forceinline__ float3 wnormalize(float3 v) { return v * rsqrtf(dot3(v, v)); }
+// glam try_normalize().unwrap_or(Y) (common.wgsl:241-246) with the reciprocal square root.
+__device__ __forceinline__ float3 wsafe_normalize(float3 v) {
+    const float l2 = dot3(v, v);
+    const float r = rsqrtf(l2);
+    if (!(l2 > 0.0f) || !(r <= 3.4028235e38f)) return mk3(0.f, 1.f, 0.f);
+    return v * r;
+}
+
 // ------------------------------------------------------------------ lights (lights.wgsl)
 __device__ __forceinline__ float area_intersection(float3 ro, float3 rd, const DevLight& l) {
     float3 n = ld3(l.n);
@@ -113,9 +136,9 @@ __device__ __forceinline__ float area_intersection(float3 ro, float3 rd, const D
 __device__ __forceinline__ float area_weight(float3 p, float3 n, const DevLight& l) {
     float3 to_light = ld3(l.a) - p;
     float dist2 = fmaxf(dot3(to_light, to_light), 1e-6f);
-    float3 dir = to_light / sqrtf(dist2);
+    float3 dir = to_light * rsqrtf(dist2);
     float facing = fmaxf(dot3(ld3(l.n), -dir), 0.0f);
-    return l.lum * l.area * facing * fmaxf(dot3(n, dir), 0.15f) / dist2;
+    return wdiv(l.lum * l.area * facing * fmaxf(dot3(n, dir), 0.15f), dist2);
 }
 __device__ __forceinline__ float area_total_weight(const DevScene& S, float3 p, float3 n) {
     float total = 0.0f;
@@ -125,8 +148,8 @@ __device__ __forceinline__ float area_total_weight(const DevScene& S, float3 p, 
 __device__ __forceinline__ float mis_power(float a, float b) {
     float scale = fmaxf(a, b);
     if (scale <= 0.0f) return 0.0f;
-    float pa = a / scale, pb = b / scale;
-    return pa * pa / (pa * pa + pb * pb);
+    float pa = wdiv(a, scale), pb = wdiv(b, scale);
+    return wdiv(pa * pa, pa * pa + pb * pb);
 }
 // Emitter hit by a continuation ray (area_emission, lights.wgsl:330-356).
 static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, float distance, float prev_pdf, bool use_mis,
@@ -140,9 +163,9 @@ static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, 
         if (fabsf(t - distance) > fmaxf(1e-6f, distance * 1e-6f)) continue;
         float w = 1.0f;
         if (use_mis) {
-            float pl = (distance * distance) / fmaxf(l.area * cos_l, 1e-20f);
+            float pl = wdiv(distance * distance, fmaxf(l.area * cos_l, 1e-20f));
             float selection = 0.0f;
-            if (prev_total > 0.0f) selection = area_weight(ro, prev_normal, l) / prev_total;
+            if (prev_total > 0.0f) selection = wdiv(area_weight(ro, prev_normal, l), prev_total);
             pl = pl * selection;
             w = mis_power(prev_pdf, pl);
         }
@@ -169,7 +192,7 @@ struct Surface {
 __device__ __forceinline__ float luminance(float3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
 __device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt) {
     float s = n.z >= 0.0f ? 1.0f : -1.0f;
-    float a = -1.0f / (s + n.z);
+    float a = wdiv(-1.0f, s + n.z);
     float b = n.x * n.y * a;
     t = mk3(1.0f + s * n.x * n.x * a, s * b, -s * n.x);
     bt = mk3(b, s + n.y * n.y * a, -n.y);
@@ -177,18 +200,20 @@ __device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt) {
 __device__ __forceinline__ float3 frame_mul(float3 t, float3 bt, float3 n, float3 v) { return t * v.x + bt * v.y + n * v.z; }
 __device__ __forceinline__ float3 cosine_sample(float3 n, float r1, float r2) {
     float phi = 2.0f * SF_PI * r1;
-    float r = sqrtf(r2);
+    float r = wsqrt(r2);
     float3 t, bt;
     tangent_frame(n, t, bt);
     float sp, cp;
     sincosf(phi, &sp, &cp);
-    return frame_mul(t, bt, n, mk3(r * cp, r * sp, sqrtf(fmaxf(0.0f, 1.0f - r2))));
+    return frame_mul(t, bt, n, mk3(r * cp, r * sp, wsqrt(fmaxf(0.0f, 1.0f - r2))));
 }
 __device__ __forceinline__ float ggx_d(float nh, float a2) {
     float d = nh * nh * (a2 - 1.0f) + 1.0f;
-    return a2 / (SF_PI * d * d);
+    return wdiv(a2, SF_PI * d * d);
 }
-__device__ __forceinline__ float smith_g1(float nv, float a2) { return 2.0f * nv / (nv + sqrtf(a2 + (1.0f - a2) * nv * nv)); }
+__device__ __forceinline__ float smith_g1(float nv, float a2) {
+    return wdiv(2.0f * nv, nv + wsqrt(a2 + (1.0f - a2) * nv * nv));
+}
 __device__ __forceinline__ float3 fresnel(float3 f0, float vh) {
     float m = 1.0f - vh;
     float m2 = m * m;
@@ -199,46 +224,46 @@ static __device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1,
     float3 t, bt;
     tangent_frame(n, t, bt);
     float3 lv = mk3(dot3(t, v), dot3(bt, v), dot3(n, v));
-    float3 vh = safe_normalize3(mk3(alpha * lv.x, alpha * lv.y, fmaxf(lv.z, 1e-5f)));
+    float3 vh = wsafe_normalize(mk3(alpha * lv.x, alpha * lv.y, fmaxf(lv.z, 1e-5f)));
     float lensq = vh.x * vh.x + vh.y * vh.y;
     float3 t1 = mk3(1.f, 0.f, 0.f);
-    if (lensq > 0.0f) t1 = mk3(-vh.y, vh.x, 0.0f) / sqrtf(lensq);
+    if (lensq > 0.0f) t1 = mk3(-vh.y, vh.x, 0.0f) * rsqrtf(lensq);
     float3 t2 = cross3(vh, t1);
-    float r = sqrtf(r1);
+    float r = wsqrt(r1);
     float phi = 2.0f * SF_PI * r2;
     float sp, cp;
     sincosf(phi, &sp, &cp);
     float x = r * cp;
     float blend = 0.5f * (1.0f + vh.z);
-    float y0 = sqrtf(fmaxf(0.0f, 1.0f - x * x));
+    float y0 = wsqrt(fmaxf(0.0f, 1.0f - x * x));
     float y = y0 * (1.0f - blend) + (r * sp) * blend;
-    float3 nh = t1 * x + t2 * y + vh * sqrtf(fmaxf(0.0f, 1.0f - x * x - y * y));
-    return frame_mul(t, bt, n, safe_normalize3(mk3(alpha * nh.x, alpha * nh.y, fmaxf(nh.z, 0.0f))));
+    float3 nh = t1 * x + t2 * y + vh * wsqrt(fmaxf(0.0f, 1.0f - x * x - y * y));
+    return frame_mul(t, bt, n, wsafe_normalize(mk3(alpha * nh.x, alpha * nh.y, fmaxf(nh.z, 0.0f))));
 }
 static __device__ float3 brdf_eval(const Surface& s, float3 v, float3 l) {
     float nl = dot3(s.n, l), nv = dot3(s.n, v);
     if (nl <= 0.0f || nv <= 0.0f) return mk3(0.f, 0.f, 0.f);
-    float3 h = normalize3(v + l);
+    float3 h = wnormalize(v + l);
     float nh = fmaxf(dot3(s.n, h), 0.0f);
     float vh = fmaxf(dot3(v, h), 0.0f);
     float a2 = s.alpha * s.alpha;
     float3 f = fresnel(s.f0, vh);
-    float3 spec = f * (ggx_d(nh, a2) * smith_g1(nv, a2) * smith_g1(nl, a2)) / fmaxf(4.0f * nv * nl, 1e-4f);
-    return s.diffuse * (mk3(1.f, 1.f, 1.f) - f) / SF_PI + spec;
+    float3 spec = f * wdiv(ggx_d(nh, a2) * smith_g1(nv, a2) * smith_g1(nl, a2), fmaxf(4.0f * nv * nl, 1e-4f));
+    return s.diffuse * (mk3(1.f, 1.f, 1.f) - f) * (1.0f / SF_PI) + spec;
 }
 __device__ __forceinline__ float spec_probability(const Surface& s, float nv) {
     float3 f = fresnel(s.f0, nv);
-    return fminf(fmaxf(luminance(f) / fmaxf(luminance(f) + luminance(s.diffuse), 1e-4f), 0.05f), 0.95f);
+    return fminf(fmaxf(wdiv(luminance(f), fmaxf(luminance(f) + luminance(s.diffuse), 1e-4f)), 0.05f), 0.95f);
 }
 static __device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_spec) {
     float nl = dot3(s.n, l);
     if (nl <= 0.0f) return 0.0f;
-    float3 hh = normalize3(v + l);
+    float3 hh = wnormalize(v + l);
     float nh = fmaxf(dot3(s.n, hh), 0.0f);
     float a2 = s.alpha * s.alpha;
     float nv = fmaxf(dot3(s.n, v), 1e-4f);
-    float pdf_spec = ggx_d(nh, a2) * smith_g1(nv, a2) / (4.0f * nv);
-    return p_spec * pdf_spec + (1.0f - p_spec) * nl / SF_PI;
+    float pdf_spec = wdiv(ggx_d(nh, a2) * smith_g1(nv, a2), 4.0f * nv);
+    return p_spec * pdf_spec + (1.0f - p_spec) * nl * (1.0f / SF_PI);
 }
 // make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
 static __device__ Surface make_surface(const DevScene& S, float3 n, const DeSampleF& smp) {
@@ -364,15 +389,16 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
         float3 to_q = q - p_off;
         float dist2 = dot3(to_q, to_q);
         if (dist2 >= 1e-8f) {
-            float dist = sqrtf(dist2);
-            float3 ldir = to_q / dist;
+            const float inv_dist = rsqrtf(dist2);
+            float dist = dist2 * inv_dist;
+            float3 ldir = to_q * inv_dist;
             float nl = dot3(s.n, ldir);
             float cos_l = dot3(ln, -ldir);
             if (!(nl <= 0.0f || cos_l <= 0.0f || dot3(n, ldir) <= 0.0f)) {
-                float pl = (selected_weight / area_total) * (dist2 / fmaxf(l.area * cos_l, 1e-20f));
+                float pl = wdiv(selected_weight, area_total) * wdiv(dist2, fmaxf(l.area * cos_l, 1e-20f));
                 float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
                 float w = last ? 1.0f : mis_power(pl, pb);
-                float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * w / pl;
+                float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * wdiv(w, pl);
                 sh.active = true;
                 sh.o = p_off;
                 sh.dir = ldir;
@@ -395,7 +421,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     if (nl <= 0.0f || dot3(n, ldir) <= 0.0f) return PATH_DONE;
     float pdf = bsdf_pdf(s, v, ldir, p_spec);
     if (pdf <= 1e-6f) return PATH_DONE;
-    ps.tp = ps.tp * (brdf_eval(s, v, ldir) * nl / pdf);
+    ps.tp = ps.tp * (brdf_eval(s, v, ldir) * wdiv(nl, pdf));
     ps.prev_pdf = pdf;
     ps.prev_from_bsdf = true;
     ps.prev_normal = s.n;
@@ -403,7 +429,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     if (ps.bounce >= 2) {
         float q = fminf(fmaxf(fmaxf(ps.tp.x, fmaxf(ps.tp.y, ps.tp.z)), 0.05f), 0.95f);
         if (rnd(ps.rng) > q) return PATH_DONE;
-        ps.tp = ps.tp / q;
+        ps.tp = ps.tp * wdiv(1.0f, q);
     }
     ps.o = p_off;
     ps.d = ldir;
