@@ -152,3 +152,35 @@ def test_destroy_with_requests_queued(renderer):
         f, c = small_tile(i, side=256, iterations=2000)
         srv.tile(f, c)
     srv.close()  # returns after the batch in flight; queued requests fail
+
+
+def test_concurrent_clients(renderer):
+    # several client threads submit and wait at once (the calls release the GIL); every
+    # request completes with the result it has alone
+    import threading
+
+    srv = Server(renderer, hbm_budget=2 * GB, slots=3)
+    tiles = [small_tile(20 + i, side=64, iterations=1500) for i in range(12)]
+    alone = [escape2d(renderer.ctx, f, c)["iterations"] for f, c in tiles]
+    out, errors = {}, []
+
+    def client(k):
+        try:
+            mine = list(range(k, len(tiles), 4))
+            tickets = [(i, srv.tile(*tiles[i])) for i in mine]
+            for i, t in tickets:
+                out[i] = srv.wait(t).iterations
+                srv.release(t)
+        except Exception as e:  # reported below, on the test's thread
+            errors.append(e)
+
+    threads = [threading.Thread(target=client, args=(k,)) for k in range(4)]
+    for t in threads:
+        t.start()
+    for t in threads:
+        t.join(timeout=120)
+    srv.close()
+    assert not errors, errors
+    assert sorted(out) == list(range(len(tiles)))
+    for i in range(len(tiles)):
+        np.testing.assert_array_equal(out[i], alone[i])
