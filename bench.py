@@ -489,7 +489,8 @@ def run_serve(args):
     1k-20k iterations), 40% previews (480x270, 1 spp, 1 bounce, a random orbit of a
     Mandelbulb or Mandelbox), 20% refinements (+8 spp into one of the 16 latest
     previews' films). Replayed in real time against the Server (150 GB HBM budget)
-    and as sequential plain launches; p50/p99 latency and throughput of both."""
+    and as sequential plain launches; p50/p99 latency and throughput of both. Then
+    the capacity of both: the stream's first --burst requests queued at once."""
     from syfrack_gb300 import GpuContext, Renderer, workloads
 
     ctx = GpuContext(0)
@@ -502,9 +503,19 @@ def run_serve(args):
     plain_replay(r, ctx, warm, 60.0)
     served = serve_replay(r, ctx, events, args)
     plain = plain_replay(r, ctx, events, cap_s=args.duration * 3)
+    # capacity: the first requests of the same stream all queued at once
+    burst = [(0.0, k, pl) for _, k, pl in events[:args.burst]]
+    cap_served = serve_replay(r, ctx, burst, args)
+    cap_plain = plain_replay(r, ctx, burst, cap_s=600.0)
+    capacity = {"requests": len(burst), "served_rps": cap_served["throughput_rps"],
+                "plain_rps": cap_plain["throughput_rps"],
+                "ratio": cap_served["throughput_rps"] / cap_plain["throughput_rps"],
+                "served_mrays_per_s": cap_served["mrays_per_s"], "plain_mrays_per_s": cap_plain["mrays_per_s"],
+                "served_batches": cap_served["batches"],
+                "served_mean_batch_requests": cap_served["mean_batch_requests"]}
     line = {"metric": "served p99 latency", "unit": "ms", "value": served["latency"]["all"].get("p99_ms"),
             "higher_is_better": False, "workload": f"serving_stream_poisson{args.rate:g}_{args.duration:g}s",
-            "requests": len(events), "served": served, "plain_sequential": plain,
+            "requests": len(events), "served": served, "plain_sequential": plain, "capacity": capacity,
             "throughput_ratio": served["throughput_rps"] / plain["throughput_rps"],
             "config": {"slots": args.slots, "hbm_budget_gb": args.hbm_budget_gb,
                        "host_result_gb": args.host_result_gb, "seed": args.seed,
@@ -764,6 +775,7 @@ def main():
     ap.add_argument("--hbm-budget-gb", type=float, default=150.0)
     ap.add_argument("--host-result-gb", type=float, default=8.0)
     ap.add_argument("--seed", type=int, default=5)
+    ap.add_argument("--burst", type=int, default=3000, help="requests queued at once for the capacity measure")
     args = ap.parse_args()
     if args.impl == "reference":
         run_reference(args)
