@@ -382,6 +382,43 @@ static __device__ __forceinline__ bool esc_chunk(const EscParams& p, EscOrbit& o
     return false;
 }
 
+// The common tile: z^2 without twist (Julia, Mandelbrot or, SHIP, Burning Ship), the
+// default 12 stripes. The budget is checked once per chunk instead of per iteration;
+// the arithmetic is esc_step's, so the results are the same bit for bit.
+template <bool TRAPS, bool SHIP>
+static __device__ __forceinline__ bool esc_chunk_z2(const EscParams& p, EscOrbit& o) {
+    const uint32_t left = p.iterations - o.count;  // count <= iterations
+    const int n = left < (uint32_t)ESC_CHUNK ? (int)left : ESC_CHUNK;
+    float zx = o.zx, zy = o.zy, ring = o.ring, stripe = o.stripe;
+    const float cx = o.cx, cy = o.cy, bt = p.bail_t, tr = p.trap_radius;
+    int j = 0;
+    bool escaped = false;
+    for (; j < n; ++j) {
+        const float r2 = FA(FM(zx, zx), FM(zy, zy));
+        if (r2 > bt) {
+            escaped = true;
+            break;
+        }
+        if (TRAPS) {
+            const float rinv = rsqrtf(r2);
+            ring = fminf(ring, fabsf((r2 > 0.0f ? r2 * rinv : 0.0f) - tr));
+            if (r2 > 0.0f) stripe += sin_12(zx * rinv, zy * rinv);
+        }
+        const float bx = SHIP ? fabsf(zx) : zx, by = SHIP ? fabsf(zy) : zy;
+        float nx, ny;
+        cmul_rn(bx, by, bx, by, nx, ny);
+        zx = FA(nx, cx);
+        zy = FA(ny, cy);
+    }
+    o.zx = zx;
+    o.zy = zy;
+    o.ring = ring;
+    o.stripe = stripe;
+    o.count += (uint32_t)j;
+    o.escaped = escaped;
+    return escaped || o.count >= p.iterations;
+}
+
 template <bool TRAPS>
 __global__ void __launch_bounds__(256, 5) k_escape2d(const PlanarDev* __restrict__ fg,
                                                      const CanvasDev* __restrict__ cg, uint32_t tile_x,
@@ -398,6 +435,7 @@ __global__ void __launch_bounds__(256, 5) k_escape2d(const PlanarDev* __restrict
     const float scale = __fdiv_rn(6.0f, K.zoom);
     const EscParams p = esc_params(F);
     const bool pow2 = p.power == 2, sk12 = p.stripe_k == 12;
+    const bool z2 = pow2 && sk12 && !p.rotate && !p.phoenix;
     EscOrbit o;
     uint32_t pix = 0;
     bool busy = false, live = true;
@@ -420,7 +458,9 @@ __global__ void __launch_bounds__(256, 5) k_escape2d(const PlanarDev* __restrict
         if (!__any_sync(FULL_MASK, busy)) break;
         if (busy) {
             bool done;
-            if (pow2 && sk12) done = esc_chunk<TRAPS, true, true>(p, o);
+            if (z2 && p.ship) done = esc_chunk_z2<TRAPS, true>(p, o);
+            else if (z2) done = esc_chunk_z2<TRAPS, false>(p, o);
+            else if (pow2 && sk12) done = esc_chunk<TRAPS, true, true>(p, o);
             else if (pow2) done = esc_chunk<TRAPS, true, false>(p, o);
             else done = esc_chunk<TRAPS, false, false>(p, o);
             if (done) {
