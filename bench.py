@@ -283,7 +283,8 @@ def run_ours(args):
                          "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
                          "de_evals_per_step": st["de_evals"] / args.steps,
                          "de_iterations_per_step": st["de_iterations"] / args.steps,
-                         "simt_lane_efficiency": st["de_evals"] / max(32 * st["warp_de_calls"], 1)},
+                         "simt_lane_efficiency": st["de_evals"] / max(32 * st["warp_de_calls"], 1),
+                         "iterate_lane_efficiency": st["de_iterations"] / max(st["iteration_slots"], 1)},
             "gpu_launches": st["launches"],
             "status_word": status,
             "clocks": clocks.summary(),

@@ -1754,22 +1754,26 @@ extern "C" sf_status sf_device_fp32_peak(sf_context* c, double* tflops) {
     cudaEventCreate(&a);
     cudaEventCreate(&b);
     cudaError_t e = sf_launch_ffma_peak(static_cast<float*>(buf), 64, blocks, c->stream);  // warm-up
-    float best = 1e30f;
-    for (int rep = 0; rep < 5 && e == cudaSuccess; ++rep) {
+    // the median of 7 timed launches: a single fastest run can land on a clock excursion
+    std::vector<float> times;
+    for (int rep = 0; rep < 7 && e == cudaSuccess; ++rep) {
         cudaEventRecord(a, c->stream);
         e = sf_launch_ffma_peak(static_cast<float*>(buf), iters, blocks, c->stream);
         cudaEventRecord(b, c->stream);
         if (e == cudaSuccess) e = cudaEventSynchronize(b);
         float ms = 0;
         if (e == cudaSuccess) cudaEventElapsedTime(&ms, a, b);
-        if (ms > 0 && ms < best) best = ms;
+        if (ms > 0) times.push_back(ms);
     }
     cudaEventDestroy(a);
     cudaEventDestroy(b);
     ctx_free(c, buf, 256);
     if (e != cudaSuccess) return cuda_fail(e, "fp32 peak probe");
+    if (times.empty()) return fail(SF_ERR_CUDA, "fp32 peak probe: no timing");
+    std::sort(times.begin(), times.end());
+    const float median = times[times.size() / 2];
     double flops = double(blocks) * 256.0 * iters * 16.0 * 8.0 * 2.0;
-    *tflops = flops / (best * 1e-3) / 1e12;
+    *tflops = flops / (median * 1e-3) / 1e12;
     return SF_OK;
 }
 

@@ -85,6 +85,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     float hstep = 0.f;
     uint32_t hit_w = 0;  // iterations | material << 16 of the surface hit whose normal is being tapped
     uint32_t n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0;
+    unsigned long long n_slots = 0;
 
     // End of a continuation or shadow segment without a surface sample.
     auto finish = [&](int r) {
@@ -175,7 +176,16 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             else s = de_form<FORM>(P, q);
             n_eval++;
             n_iter += s.iter;
-            if (lane_id() == (uint32_t)(__ffs(__activemask()) - 1)) n_wcall++;
+            {
+                // warp-level DE calls and, per call, the iterations the warp ran (its
+                // longest lane) times its active lanes
+                const uint32_t am = __activemask();
+                const uint32_t mx = __reduce_max_sync(am, s.iter);
+                if (lane_id() == (uint32_t)(__ffs(am) - 1)) {
+                    n_wcall++;
+                    n_slots += (unsigned long long)mx * __popc(am);
+                }
+            }
             if (state == TL_NORMAL) {
                 grad = grad + tetra_offset(tap) * s.d;
                 if (++tap == 4) {
@@ -218,6 +228,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     warp_stat(&stats[SF_STAT_SEGMENTS], n_seg + n_shseg);
     warp_stat(&stats[SF_STAT_SHADOW_SEGMENTS], n_shseg);
     warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
+    warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
 }
 
 template <int FORM>
