@@ -262,10 +262,16 @@ typedef struct sf_progress {
     uint64_t pixel_samples_done, pixel_samples_total;
     uint32_t status_word;   /* wavefront invariant bits 1/2/4 (wavefront.wgsl:183,:220,:236) */
 } sf_progress;
+/* The film planes of wf_commit (wavefront.wgsl:232-260). This path has no fog or
+ * volumes, so the volume contribution is zero: volume and moments hold (0, 0, 0,
+ * samples) and surface (= radiance - volume) equals accum. Any pointer may be NULL. */
 typedef struct sf_film_planes {
     float* accum;   /* 4*width*height: rgb sums and sample count */
     float* depth;   /* width*height */
     float* aux;     /* 4*width*height: normal xyz, steps (-1 on a miss) */
+    float* volume;  /* 4*width*height: volume sums and sample count */
+    float* moments; /* 4*width*height: volume Welford moments and sample count */
+    float* surface; /* 4*width*height: surface sums and sample count */
 } sf_film_planes;
 
 /* Session::new (session.rs:165). The integrator field selects the per-pixel

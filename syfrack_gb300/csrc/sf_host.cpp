@@ -1333,6 +1333,26 @@ extern "C" sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t ca
     return SF_OK;
 }
 
+namespace {
+// volume, moments (zero contribution, sample counts) and surface (= accum) planes,
+// filled on the host from the accum plane once the stream has delivered it.
+cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st) {
+    if (!out.volume && !out.moments && !out.surface) return cudaSuccess;
+    const size_t px = size_t(f.width) * f.height;
+    std::vector<float> acc(px * 4);
+    cudaError_t e = cudaMemcpyAsync(acc.data(), f.accum, px * 16, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess) e = cudaStreamSynchronize(st);
+    if (e != cudaSuccess) return e;
+    for (size_t i = 0; i < px; ++i) {
+        const float n = acc[4 * i + 3];
+        if (out.volume) { out.volume[4 * i] = out.volume[4 * i + 1] = out.volume[4 * i + 2] = 0.0f; out.volume[4 * i + 3] = n; }
+        if (out.moments) { out.moments[4 * i] = out.moments[4 * i + 1] = out.moments[4 * i + 2] = 0.0f; out.moments[4 * i + 3] = n; }
+    }
+    if (out.surface) std::memcpy(out.surface, acc.data(), px * 16);
+    return cudaSuccess;
+}
+}  // namespace
+
 extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
     if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
     sf_context* c = s->ctx;
@@ -1341,6 +1361,7 @@ extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
     if (out->accum) CU(cudaMemcpyAsync(out->accum, s->film.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
     if (out->depth) CU(cudaMemcpyAsync(out->depth, s->film.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
     if (out->aux) CU(cudaMemcpyAsync(out->aux, s->film.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
+    CU(derived_planes(s->film, *out, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     return SF_OK;
 }
@@ -2120,6 +2141,7 @@ extern "C" sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes
     if (out->accum) CU(cudaMemcpyAsync(out->accum, f.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
     if (out->depth) CU(cudaMemcpyAsync(out->depth, f.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
     if (out->aux) CU(cudaMemcpyAsync(out->aux, f.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
+    CU(derived_planes(f, *out, c->stream));
     CU(cudaStreamSynchronize(c->stream));
     return SF_OK;
 }

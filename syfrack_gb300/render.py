@@ -275,6 +275,16 @@ class RenderSession:
         return RenderOutput(color, acc, depth, aux, p["samples_min"], p["samples_max"],
                             time.perf_counter() - self.t0)
 
+    def film_planes(self) -> dict:
+        """Every plane of the film (wf_commit's order): accum, depth, aux, volume,
+        moments, surface."""
+        w, h = self.cfg.width, self.cfg.height
+        out = {k: np.zeros((h, w, 4), np.float32) for k in ("accum", "aux", "volume", "moments", "surface")}
+        out["depth"] = np.zeros((h, w), np.float32)
+        planes = sf_film_planes(*(_fp(out[k]) for k in ("accum", "depth", "aux", "volume", "moments", "surface")))
+        check(self.ctx.lib.sf_session_readback(self.h, C.byref(planes)))
+        return out
+
     def stats(self) -> dict:
         return self.ctx.stats()
 

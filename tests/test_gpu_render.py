@@ -68,6 +68,24 @@ def test_launch_shapes_give_the_same_film(renderer, shape):
     np.testing.assert_array_equal(out.depth, ref.depth)
 
 
+def test_film_planes(renderer):
+    # without fog or volumes: volume and moments carry only the sample counts, surface = accum
+    scene = workloads.mandelbox_scene()
+    cfg = small_cfg("wavefront", spp=4, spd=4, tile=96)
+    s = RenderSession(renderer, scene, cfg)
+    s.dispatch((0, 0, cfg.width, cfg.height, 0), 4)
+    s.sync()
+    p = s.film_planes()
+    r = s.readback()
+    s.close()
+    np.testing.assert_array_equal(p["accum"], r.accum)
+    np.testing.assert_array_equal(p["surface"], p["accum"])
+    for k in ("volume", "moments"):
+        assert (p[k][..., :3] == 0).all()
+        np.testing.assert_array_equal(p[k][..., 3], p["accum"][..., 3])
+    np.testing.assert_array_equal(p["depth"], r.depth)
+
+
 def test_film_against_oracle(renderer, oracle_mod):
     scene = workloads.mandelbox_scene()
     cfg = small_cfg("wavefront", spp=16, spd=8)
