@@ -9,7 +9,7 @@
  * No C++ exception crosses this boundary. One thread drives one handle.
  *
  * Arithmetic is IEEE binary32 on the device, like the reference's glam Vec3
- * and WGSL f32 (crates/syfrack-core/src/scene/graph/eval.rs, shaders/*.wgsl).
+ * and WGSL f32 (crates/syfrack-core/src/scene/graph/eval.rs and the WGSL shaders).
  */
 #ifndef SYFRACK_GPU_H
 #define SYFRACK_GPU_H

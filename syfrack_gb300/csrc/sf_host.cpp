@@ -26,10 +26,11 @@
 #include <unistd.h>
 
 #include "../../include/syfrack_gpu.h"
+#include "sf_host_internal.h"
 #include "sf_kernels.cuh"
 #include "sf_program.h"
 
-namespace {
+namespace sfh {
 
 thread_local std::string g_error;
 
@@ -37,43 +38,16 @@ sf_status fail(sf_status s, const std::string& msg) {
     g_error = msg;
     return s;
 }
+const std::string& last_error() { return g_error; }
 sf_status cuda_fail(cudaError_t e, const char* what) {
     g_error = std::string(what) + ": " + cudaGetErrorString(e);
     return e == cudaErrorMemoryAllocation ? SF_ERR_OOM : SF_ERR_CUDA;
 }
-#define CU(expr)                                               \
-    do {                                                       \
-        cudaError_t _e = (expr);                               \
-        if (_e != cudaSuccess) return cuda_fail(_e, #expr);    \
-    } while (0)
 
 constexpr uint32_t MAX_DEPTH = 3;          // graph/mod.rs:41
 constexpr uint32_t ABI_VERSION = (1u << 16) | 0u;
 
 // ------------------------------------------------------------------ graph preparation
-struct HostGraph {
-    std::vector<sf_node> nodes;
-    std::vector<sf_link> links;
-    std::vector<uint32_t> body;
-    float safety = 1.f, hint = 1.f;
-
-    const sf_node* node(uint32_t id) const {
-        for (auto& n : nodes)
-            if (n.id == id) return &n;
-        return nullptr;
-    }
-    bool input_of(uint32_t to, uint32_t port, uint32_t* from) const {
-        for (auto& l : links)
-            if (l.to_node == to && l.to_port == port) { *from = l.from_node; return true; }
-        return false;
-    }
-    std::vector<uint32_t> body_of(const sf_node& n) const {
-        std::vector<uint32_t> b;
-        if (n.kind == SF_NODE_ITERATE)
-            for (uint32_t i = 0; i < n.body_len; ++i) b.push_back(body[n.body_offset + i]);
-        return b;
-    }
-};
 
 bool is_point_kind(uint32_t k) {
     switch (k) {
@@ -310,7 +284,7 @@ struct Lowerer {
         if (!n) return push(mk(SF_OP_BEGIN));
         if (n->kind == SF_NODE_INPUT) return push(mk(SF_OP_BEGIN));
         if (!is_point_kind(n->kind)) { err = "distance value wired into a point port"; return false; }
-        uint32_t up;
+        uint32_t up = 0;
         bool has = g.input_of(src, 0, &up);
         if (!chain(has, up, guard + 1)) return false;
         return point_op(src);
@@ -323,7 +297,7 @@ struct Lowerer {
             return push(mk(SF_OP_EMPTY));
         }
         const sf_node& n = *g.node(src);
-        uint32_t a, b;
+        uint32_t a = 0, b = 0;
         bool ha = g.input_of(src, 0, &a), hb = g.input_of(src, 1, &b);
         if (is_fence_kind(n.kind)) {
             if (!chain(ha, a)) return false;
@@ -463,40 +437,11 @@ void detect_form(const HostGraph& g, DeProgram& P) {
     }
 }
 
-}  // namespace
+}  // namespace sfh
 
 // ------------------------------------------------------------------ context
-struct sf_context {
-    int device = 0;
-    cudaStream_t stream = nullptr;
-    uint64_t budget = 0, used = 0;
-    std::string device_name;
-    int cc_major = 0, cc_minor = 0, sm_count = 0;
-    bool profiling = false;
-    struct Timed { cudaEvent_t a, b; bool trace; };
-    std::vector<Timed> timed;
-    std::vector<cudaEvent_t> spare;
-    double kernel_ms = 0, trace_ms = 0;
-    std::atomic<uint64_t> launches{0}, trace_launches{0};
-    unsigned long long* d_stats = nullptr;  // SF_STAT_COUNT counters
-    uint32_t* d_work = nullptr;             // scratch work counters
-    // Graphs and sessions hold a reference, so handles may be destroyed in any order.
-    int refs = 1;
-    std::mutex mu;
-    std::mutex alloc_mu;  // budget accounting (a server thread allocates too)
-};
 
-struct sf_graph {
-    sf_context* ctx = nullptr;
-    int refs = 1;  // sessions hold a reference
-    HostGraph host;
-    DeProgram prog;
-    DeProgram* d_prog = nullptr;
-    sf_graph_info info;
-    std::string topology;
-};
-
-namespace {
+namespace sfh {
 
 sf_status ctx_alloc(sf_context* c, size_t bytes, void** p) {
     *p = nullptr;
@@ -549,29 +494,6 @@ cudaEvent_t get_event(sf_context* c) {
     cudaEventCreate(&e);
     return e;
 }
-// Scoped CUDA-event timing of one launch on the context stream.
-struct LaunchTimer {
-    sf_context* c;
-    cudaEvent_t a = nullptr;
-    bool trace;
-    cudaStream_t st;
-    LaunchTimer(sf_context* ctx, bool is_trace, bool timed = true, cudaStream_t stream = nullptr)
-        : c(ctx), trace(is_trace), st(stream ? stream : ctx->stream) {
-        c->launches++;
-        if (is_trace) c->trace_launches++;
-        if (c->profiling && timed) {
-            a = get_event(c);
-            cudaEventRecord(a, st);
-        }
-    }
-    ~LaunchTimer() {
-        if (a) {
-            cudaEvent_t b = get_event(c);
-            cudaEventRecord(b, st);
-            c->timed.push_back({a, b, trace});
-        }
-    }
-};
 void collect_timing(sf_context* c) {
     if (c->timed.empty()) return;
     cudaStreamSynchronize(c->stream);
@@ -651,7 +573,7 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     const sf_node* out = nullptr;
     for (auto& n : g.nodes)
         if (n.kind == SF_NODE_OUTPUT) out = &n;
-    uint32_t src;
+    uint32_t src = 0;
     bool has = g.input_of(out->id, 0, &src);
     if (!L.dist(has, src)) return fail(L.err.find("not supported") != std::string::npos ? SF_ERR_UNSUPPORTED : SF_ERR_GRAPH, L.err);
     if (L.max_stack > SF_MAX_DIST_STACK) return fail(SF_ERR_UNSUPPORTED, "distance tree wider than the device stack");
@@ -732,10 +654,12 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     for (uint32_t i = 0; i < S.light_count; ++i) light_dev(d.lights[i], S.lights[i]);
 }
 
-}  // namespace
+}  // namespace sfh
 
 // Error reporting for the other translation units of the library.
-sf_status sf_report_error(sf_status status, const std::string& message) { return fail(status, message); }
+sf_status sf_report_error(sf_status status, const std::string& message) { return sfh::fail(status, message); }
+
+using namespace sfh;
 
 // ------------------------------------------------------------------ ABI: basics
 extern "C" const char* sf_status_string(sf_status s) {
@@ -882,12 +806,12 @@ extern "C" sf_status sf_graph_update(sf_graph* g, const sf_graph_desc* d) {
     g->info = info;
     return SF_OK;
 }
-namespace {
+namespace sfh {
 void graph_retain(sf_graph* g) {
     std::lock_guard<std::mutex> lk(g->ctx->mu);
     g->refs++;
 }
-}  // namespace
+}  // namespace sfh
 extern "C" sf_status sf_graph_destroy(sf_graph* g) {
     if (!g) return SF_OK;
     sf_context* c = g->ctx;
@@ -1027,7 +951,7 @@ struct sf_session {
     double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
 };
 
-namespace {
+namespace sfh {
 
 uint32_t rounds_of(const sf_render_config& c) { return c.max_bounces + 2; }
 
@@ -1134,7 +1058,7 @@ sf_status session_alloc(sf_session* s) {
     return SF_OK;
 }
 
-}  // namespace
+}  // namespace sfh
 
 extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scene_desc* scene,
                                        const sf_render_config* cfg, sf_session** out) {
@@ -1162,14 +1086,14 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
     return SF_OK;
 }
 
-namespace {
+namespace sfh {
 sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
     if (min_blocks < 2 || min_blocks > 4) return fail(SF_ERR_INVALID, "trace launch: 2..4 resident blocks per SM");
     if (quantum != 0 && quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
     if (regen < 1 || regen > 32) return fail(SF_ERR_INVALID, "regeneration threshold outside 1..32 lanes");
     return SF_OK;
 }
-}  // namespace
+}  // namespace sfh
 
 extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t quantum,
                                            uint32_t regen) {
@@ -1333,7 +1257,7 @@ extern "C" sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t ca
     return SF_OK;
 }
 
-namespace {
+namespace sfh {
 // volume, moments (zero contribution, sample counts) and surface (= accum) planes,
 // filled on the host from the accum plane once the stream has delivered it.
 cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st) {
@@ -1351,7 +1275,7 @@ cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaS
     if (out.surface) std::memcpy(out.surface, acc.data(), px * 16);
     return cudaSuccess;
 }
-}  // namespace
+}  // namespace sfh
 
 extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
     if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
@@ -1385,7 +1309,7 @@ extern "C" sf_status sf_session_destroy(sf_session* s) {
 }
 
 // ------------------------------------------------------------------ checkpoints
-namespace {
+namespace sfh {
 
 uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
     const uint8_t* p = static_cast<const uint8_t*>(data);
@@ -1463,7 +1387,7 @@ void remove_tree(const std::string& dir) {
     rmdir(dir.c_str());
 }
 
-}  // namespace
+}  // namespace sfh
 
 extern "C" sf_status sf_session_save(sf_session* s, const char* dir) {
     if (!s || !dir || !*dir) return fail(SF_ERR_INVALID, "null argument");
@@ -1581,7 +1505,7 @@ extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* d
 }
 
 // ------------------------------------------------------------------ escape time
-namespace {
+namespace sfh {
 void planar_dev(const sf_planar_desc& f, PlanarDev& o) {
     std::memset(&o, 0, sizeof o);
     o.family = f.family;
@@ -1616,7 +1540,7 @@ sf_status planar_check(const sf_planar_desc* f) {
     if (!(f->zoom != 0.0f)) return fail(SF_ERR_INVALID, "zoom must be non-zero");
     return SF_OK;
 }
-}  // namespace
+}  // namespace sfh
 
 extern "C" sf_status sf_planar_probe(sf_context* c, const sf_planar_desc* f, const float* xy, size_t n, float* dist,
                                      float* traps, uint32_t* iters) {
@@ -1798,1112 +1722,3 @@ extern "C" sf_status sf_device_fp32_peak(sf_context* c, double* tflops) {
     return SF_OK;
 }
 
-// ------------------------------------------------------------------ batches
-// Device storage of one batched wavefront: the job table, path state and queues.
-struct WaveArena {
-    BatchTable bt{};
-    PathSoA soa{};
-    uint32_t capacity = 0, rounds = 0, max_steps = 0, max_jobs = 0;
-    uint32_t* lists = nullptr;
-    uint32_t* resume = nullptr;
-    uint32_t* counts = nullptr;
-    uint32_t* qcounts = nullptr;
-    uint32_t* status = nullptr;
-    void* mem = nullptr;
-    size_t mem_bytes = 0;
-    bool any_generic = false;
-    uint32_t min_blocks = 3, quantum = 128, regen = 4;
-};
-
-struct sf_batch {
-    sf_context* ctx = nullptr;
-    std::vector<sf_graph*> graphs;
-    std::vector<BatchJob> jobs;  // host copy (initial sample_start)
-    WaveArena a;
-    void* film_mem = nullptr;
-    size_t film_bytes = 0;
-    cudaGraphExec_t exec = nullptr;
-    uint32_t status_host = 0;
-};
-
-namespace {
-
-// Carves an arena for `capacity` paths and `max_jobs` jobs out of one allocation.
-sf_status arena_alloc(sf_context* c, WaveArena& a, uint32_t capacity, uint32_t max_jobs, uint32_t rounds,
-                      size_t extra_bytes, size_t* extra_offset) {
-    const size_t N = capacity;
-    size_t off = 0;
-    auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
-    size_t o_jobs = take(size_t(max_jobs) * sizeof(BatchJob));
-    size_t o_Ls = take(N * 16), o_soa = take(N * 16 * 12), o_lists = take(N * 4 * 6);
-    size_t o_march = take(2 * N * (16 + 16 + 4)), o_resume = take(2 * 2 * N * 4);
-    size_t o_counts = take(size_t(rounds + 1) * 16), o_qcounts = take(size_t(rounds) * 64 * 8), o_status = take(16);
-    size_t o_extra = take(extra_bytes);
-    sf_status st = ctx_alloc(c, off, &a.mem);
-    if (st != SF_OK) return st;
-    a.mem_bytes = off;
-    char* base = static_cast<char*>(a.mem);
-    a.bt.jobs = reinterpret_cast<BatchJob*>(base + o_jobs);
-    a.capacity = capacity;
-    a.max_jobs = max_jobs;
-    a.rounds = rounds;
-    a.soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
-    float4* p = reinterpret_cast<float4*>(base + o_soa);
-    a.soa.o = p; p += N;
-    a.soa.d = p; p += N;
-    a.soa.tp = p; p += N;
-    a.soa.L = p; p += N;
-    a.soa.pn = p; p += N;
-    a.soa.sh_o = p; p += N;
-    a.soa.sh_d = p; p += N;
-    a.soa.sh_c = p; p += N;
-    a.soa.hit = reinterpret_cast<uint4*>(p); p += N;
-    a.soa.hit_tr = p; p += N;
-    a.soa.hit_n = p; p += N;
-    a.soa.vis = reinterpret_cast<uint32_t*>(p);
-    float4* m = reinterpret_cast<float4*>(base + o_march);
-    a.soa.m0 = m;
-    a.soa.m1 = m + 2 * N;
-    a.soa.m2 = reinterpret_cast<uint32_t*>(m + 4 * N);
-    a.soa.capacity = capacity;
-    a.lists = reinterpret_cast<uint32_t*>(base + o_lists);
-    a.resume = reinterpret_cast<uint32_t*>(base + o_resume);
-    a.counts = reinterpret_cast<uint32_t*>(base + o_counts);
-    a.qcounts = reinterpret_cast<uint32_t*>(base + o_qcounts);
-    a.status = reinterpret_cast<uint32_t*>(base + o_status);
-    if (extra_offset) *extra_offset = o_extra;
-    return SF_OK;
-}
-
-// One pass of a batched wavefront on stream st: every job of a.bt renders its samples.
-sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, bool timed) {
-    const size_t N = a.capacity;
-    const uint32_t R = a.rounds;
-    const uint32_t Q = a.quantum ? std::min<uint32_t>((a.max_steps + a.quantum - 1) / a.quantum + 1, 64) : 1;
-    CU(cudaMemsetAsync(a.counts, 0, size_t(R + 1) * 16, st));
-    CU(cudaMemsetAsync(a.qcounts, 0, size_t(R) * 64 * 2 * 4, st));
-    {
-        LaunchTimer t(c, false, timed, st);
-        CU(sf_launch_generate_batch(a.bt, a.soa, a.counts, st));
-    }
-    const int blocks = int(a.min_blocks) * c->sm_count;
-    for (uint32_t r = 0; r < R; ++r) {
-        uint32_t cur = r & 1, nxt = cur ^ 1;
-        RoundQueues q;
-        q.active = r == 0 ? nullptr : a.lists + (cur * 3 + 0) * N;
-        q.cont = r == 0 ? nullptr : a.lists + (cur * 3 + 1) * N;
-        q.shadow = a.lists + (cur * 3 + 2) * N;
-        q.counts = a.counts + 4 * r;
-        q.next_active = a.lists + (nxt * 3 + 0) * N;
-        q.next_cont = a.lists + (nxt * 3 + 1) * N;
-        q.next_shadow = a.lists + (nxt * 3 + 2) * N;
-        q.next_counts = a.counts + 4 * (r + 1);
-        q.work_counter = a.counts + 4 * r + 3;
-        for (uint32_t j = 0; j < Q; ++j) {
-            TraceLaunch tl;
-            tl.q = q;
-            uint32_t* qc = a.qcounts + (size_t(r) * 64 + j) * 2;
-            tl.work_counter = qc;
-            tl.resume = j == 0 ? nullptr : a.resume + size_t((j - 1) & 1) * 2 * N;
-            tl.resume_count = j == 0 ? nullptr : qc - 2 + 1;
-            tl.next_resume = a.resume + size_t(j & 1) * 2 * N;
-            tl.next_resume_count = qc + 1;
-            tl.quantum = j + 1 == Q ? 0u : a.quantum;
-            tl.regen = a.regen;
-            LaunchTimer t(c, true, timed, st);
-            CU(sf_launch_trace_batch(a.bt, a.soa, tl, c->d_stats, blocks, int(a.min_blocks), a.any_generic ? 1 : 0, st));
-        }
-        LaunchTimer t(c, false, timed, st);
-        CU(sf_launch_shade_batch(a.bt, a.soa, q, a.status, r + 1 == R ? 1 : 0, st));
-    }
-    {
-        LaunchTimer t(c, false, timed, st);
-        CU(sf_launch_commit_batch(a.bt, a.soa, st));
-    }
-    LaunchTimer t(c, false, timed, st);
-    CU(sf_launch_advance_batch(a.bt, st));
-    return SF_OK;
-}
-
-sf_status batch_record_pass(sf_batch* b, bool timed) { return wave_record_pass(b->ctx, b->a, b->ctx->stream, timed); }
-
-sf_status batch_reset(sf_batch* b) {
-    sf_context* c = b->ctx;
-    CU(cudaMemcpyAsync(b->a.bt.jobs, b->jobs.data(), b->jobs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice,
-                       c->stream));
-    for (auto& j : b->jobs) CU(sf_launch_film_clear(j.film, c->stream));
-    CU(cudaMemsetAsync(b->a.status, 0, 16, c->stream));
-    b->status_host = 0;
-    return SF_OK;
-}
-
-void batch_drop_graph(sf_batch* b) {
-    if (b->exec) {
-        cudaGraphExecDestroy(b->exec);
-        b->exec = nullptr;
-    }
-}
-
-}  // namespace
-
-extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, uint32_t n, sf_batch** out) {
-    if (!c || !jobs || !out) return fail(SF_ERR_INVALID, "null argument");
-    *out = nullptr;
-    if (n == 0 || n > SF_BATCH_MAX_JOBS) return fail(SF_ERR_INVALID, "a batch holds 1 to 1024 jobs");
-    uint64_t paths = 0, pixels = 0, film_bytes = 0;
-    uint32_t rounds = 0, max_steps = 0;
-    bool generic = false;
-    for (uint32_t i = 0; i < n; ++i) {
-        if (!jobs[i].graph || jobs[i].graph->ctx != c) return fail(SF_ERR_INVALID, "job graph missing or of another context");
-        sf_status st = validate_config(jobs[i].cfg);
-        if (st != SF_OK) return st;
-        if (jobs[i].scene.light_count > SF_MAX_LIGHTS || jobs[i].scene.finish_count > SF_MAX_FINISHES)
-            return fail(SF_ERR_INVALID, "too many lights or finishes");
-        const sf_render_config& cf = jobs[i].cfg;
-        uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
-                                                   cf.samples_per_pixel), 1);
-        paths += uint64_t(cf.width) * cf.height * spd;
-        pixels += uint64_t(cf.width) * cf.height;
-        film_bytes += ((uint64_t(cf.width) * cf.height * 36 + 255) & ~uint64_t(255));
-        rounds = std::max(rounds, cf.max_bounces + 2);
-        max_steps = std::max(max_steps, cf.max_steps);
-        generic |= jobs[i].graph->prog.form == SF_FORM_GENERIC;
-    }
-    if (paths > 0x7fffffffull) return fail(SF_ERR_INVALID, "batch too large (2^31 paths)");
-    cudaSetDevice(c->device);
-    auto* b = new sf_batch();
-    b->ctx = c;
-    const size_t scene_bytes = (n * sizeof(DevScene) + 255) & ~size_t(255);
-    size_t extra = 0;
-    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, scene_bytes + film_bytes, &extra);
-    if (st != SF_OK) { delete b; return st; }
-    b->a.max_steps = max_steps;
-    b->a.any_generic = generic;
-    b->a.bt.n_jobs = n;
-    b->a.bt.total_paths = uint32_t(paths);
-    b->a.bt.total_pixels = uint32_t(pixels);
-    char* base = static_cast<char*>(b->a.mem) + extra;
-    DevScene* d_scenes = reinterpret_cast<DevScene*>(base);
-    std::vector<DevScene> scenes(n);
-    char* film = base + scene_bytes;
-    uint32_t pbeg = 0, xbeg = 0;
-    for (uint32_t i = 0; i < n; ++i) {
-        const sf_render_config& cf = jobs[i].cfg;
-        uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
-                                                   cf.samples_per_pixel), 1);
-        scene_dev(jobs[i].scene, cf, jobs[i].graph->info, scenes[i]);
-        BatchJob j{};
-        j.prog = jobs[i].graph->d_prog;
-        j.scene = d_scenes + i;
-        size_t px = size_t(cf.width) * cf.height;
-        // accum | aux | depth: both float4 planes stay 16-byte aligned for any pixel count
-        j.film.accum = reinterpret_cast<float4*>(film);
-        j.film.aux = reinterpret_cast<float4*>(film + px * 16);
-        j.film.depth = reinterpret_cast<float*>(film + px * 32);
-        j.film.width = cf.width;
-        j.film.height = cf.height;
-        film += (px * 36 + 255) & ~size_t(255);
-        j.geom = DispatchGeom{0, 0, cf.width, cf.height, 0, spd, uint32_t(px * spd)};
-        j.path_begin = pbeg;
-        j.pixel_begin = xbeg;
-        j.form = jobs[i].graph->prog.form;
-        pbeg += uint32_t(px * spd);
-        xbeg += uint32_t(px);
-        b->jobs.push_back(j);
-        b->graphs.push_back(jobs[i].graph);
-        graph_retain(jobs[i].graph);
-    }
-    ctx_retain(c);
-    cudaError_t e = cudaMemcpyAsync(d_scenes, scenes.data(), n * sizeof(DevScene), cudaMemcpyHostToDevice, c->stream);
-    if (e == cudaSuccess) st = batch_reset(b);
-    if (e == cudaSuccess && st == SF_OK) e = cudaStreamSynchronize(c->stream);
-    if (e != cudaSuccess || st != SF_OK) {
-        sf_batch_destroy(b);
-        return e != cudaSuccess ? cuda_fail(e, "batch upload") : st;
-    }
-    *out = b;
-    return SF_OK;
-}
-
-extern "C" sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
-    if (!b) return fail(SF_ERR_INVALID, "null batch");
-    sf_status st = check_launch(min_blocks, quantum, regen);
-    if (st != SF_OK) return st;
-    if (b->a.min_blocks != min_blocks || b->a.quantum != quantum || b->a.regen != regen) batch_drop_graph(b);
-    b->a.min_blocks = min_blocks;
-    b->a.quantum = quantum;
-    b->a.regen = regen;
-    return SF_OK;
-}
-
-extern "C" sf_status sf_batch_run(sf_batch* b, uint32_t passes, int use_graph) {
-    if (!b) return fail(SF_ERR_INVALID, "null batch");
-    sf_context* c = b->ctx;
-    cudaSetDevice(c->device);
-    for (uint32_t i = 0; i < passes; ++i) {
-        if (!use_graph) {
-            sf_status st = batch_record_pass(b, true);
-            if (st != SF_OK) return st;
-            continue;
-        }
-        if (!b->exec) {
-            cudaGraph_t g = nullptr;
-            CU(cudaStreamBeginCapture(c->stream, cudaStreamCaptureModeThreadLocal));
-            sf_status st = batch_record_pass(b, false);
-            cudaError_t e = cudaStreamEndCapture(c->stream, &g);
-            if (st != SF_OK) { if (g) cudaGraphDestroy(g); return st; }
-            if (e != cudaSuccess) return cuda_fail(e, "graph capture");
-            e = cudaGraphInstantiate(&b->exec, g, 0);
-            cudaGraphDestroy(g);
-            if (e != cudaSuccess) { b->exec = nullptr; return cuda_fail(e, "graph instantiate"); }
-        }
-        LaunchTimer t(c, false);
-        CU(cudaGraphLaunch(b->exec, c->stream));
-    }
-    return SF_OK;
-}
-
-extern "C" sf_status sf_batch_sync(sf_batch* b, uint32_t timeout_ms, uint32_t* status_word) {
-    if (!b) return fail(SF_ERR_INVALID, "null batch");
-    sf_context* c = b->ctx;
-    cudaSetDevice(c->device);
-    sf_status st = wait_stream(c->stream, timeout_ms);
-    if (st != SF_OK) return st;
-    uint32_t w = 0;
-    CU(cudaMemcpy(&w, b->a.status, 4, cudaMemcpyDeviceToHost));
-    b->status_host |= w;
-    if (status_word) *status_word = b->status_host;
-    if (b->status_host) return fail(SF_ERR_WAVEFRONT, "wavefront invariant word " + std::to_string(b->status_host));
-    return SF_OK;
-}
-
-extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t* best_q, uint32_t* best_regen,
-                                      float* best_ms) {
-    if (!b) return fail(SF_ERR_INVALID, "null batch");
-    sf_context* c = b->ctx;
-    cudaSetDevice(c->device);
-    cudaEvent_t e0, e1;
-    CU(cudaEventCreate(&e0));
-    CU(cudaEventCreate(&e1));
-    float best = 1e30f;
-    uint32_t bm = b->a.min_blocks, bq = b->a.quantum, br = b->a.regen;
-    // one timed pass of a candidate shape
-    auto time_pass = [&](uint32_t mb, uint32_t q, uint32_t rg, float* ms) -> sf_status {
-        b->a.min_blocks = mb;
-        b->a.quantum = q;
-        b->a.regen = rg;
-        cudaEventRecord(e0, c->stream);
-        sf_status st = batch_record_pass(b, false);
-        cudaEventRecord(e1, c->stream);
-        if (st != SF_OK) return st;
-        cudaError_t e = cudaEventSynchronize(e1);
-        if (e == cudaSuccess) e = cudaEventElapsedTime(ms, e0, e1);
-        return e == cudaSuccess ? SF_OK : cuda_fail(e, "autotune");
-    };
-    // coordinate search: resident blocks x step quantum (0 = none) at regen 1, then the regeneration threshold
-    const uint32_t mbs[3] = {2, 3, 4}, qs[4] = {0, 64, 128, 256}, rgs[4] = {1, 4, 8, 16};
-    sf_status st = SF_OK;
-    for (uint32_t mb : mbs)
-        for (uint32_t q : qs) {
-            float ms = 0;
-            if ((st = time_pass(mb, q, 1, &ms)) != SF_OK) break;
-            if (ms < best) { best = ms; bm = mb; bq = q; br = 1; }
-        }
-    for (uint32_t i = 1; i < 4 && st == SF_OK; ++i) {
-        float ms = 0;
-        if ((st = time_pass(bm, bq, rgs[i], &ms)) != SF_OK) break;
-        if (ms < best) { best = ms; br = rgs[i]; }
-    }
-    cudaEventDestroy(e0);
-    cudaEventDestroy(e1);
-    if (st != SF_OK) return st;
-    batch_drop_graph(b);
-    b->a.min_blocks = bm;
-    b->a.quantum = bq;
-    b->a.regen = br;
-    st = batch_reset(b);
-    if (st != SF_OK) return st;
-    CU(cudaStreamSynchronize(c->stream));
-    if (best_mb) *best_mb = bm;
-    if (best_q) *best_q = bq;
-    if (best_regen) *best_regen = br;
-    if (best_ms) *best_ms = best;
-    return SF_OK;
-}
-
-extern "C" sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes* out) {
-    if (!b || !out) return fail(SF_ERR_INVALID, "null argument");
-    if (job >= b->jobs.size()) return fail(SF_ERR_INVALID, "job index out of range");
-    sf_context* c = b->ctx;
-    cudaSetDevice(c->device);
-    const FilmPlanes& f = b->jobs[job].film;
-    size_t px = size_t(f.width) * f.height;
-    if (out->accum) CU(cudaMemcpyAsync(out->accum, f.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
-    if (out->depth) CU(cudaMemcpyAsync(out->depth, f.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (out->aux) CU(cudaMemcpyAsync(out->aux, f.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
-    CU(derived_planes(f, *out, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
-    return SF_OK;
-}
-
-extern "C" sf_status sf_batch_destroy(sf_batch* b) {
-    if (!b) return SF_OK;
-    sf_context* c = b->ctx;
-    cudaSetDevice(c->device);
-    cudaStreamSynchronize(c->stream);
-    batch_drop_graph(b);
-    ctx_free(c, b->a.mem, b->a.mem_bytes);
-    for (sf_graph* g : b->graphs) sf_graph_destroy(g);
-    delete b;
-    ctx_release(c);
-    return SF_OK;
-}
-
-// ------------------------------------------------------------------ serving
-// One scheduler thread per server. A slot is a wavefront arena plus two streams (high
-// priority for batches holding a preview, low for refinements and 2D tiles) and a
-// pinned staging area; it carries one batch at a time. Whenever a slot is free the
-// scheduler takes requests from the queue in arrival order into a batch of one class
-// (2D tiles, 3D on the per-form kernel, 3D on the generic interpreter), admitting each
-// only if the device pool and the host result pool hold its bytes. Every device byte
-// of films and tile outputs comes from chunks reserved once, so no request calls
-// cudaMalloc or cudaFree, which would serialise the device.
-namespace {
-
-using ServeClock = std::chrono::steady_clock;
-
-// First-fit range allocator with coalescing, over offsets of one region.
-struct RangeAlloc {
-    std::map<size_t, size_t> free_;  // offset -> bytes
-    void init(size_t n) {
-        free_.clear();
-        if (n) free_[0] = n;
-    }
-    bool take(size_t n, size_t* off) {
-        for (auto it = free_.begin(); it != free_.end(); ++it) {
-            if (it->second < n) continue;
-            *off = it->first;
-            size_t rest = it->second - n, roff = it->first + n;
-            free_.erase(it);
-            if (rest) free_[roff] = rest;
-            return true;
-        }
-        return false;
-    }
-    void give(size_t off, size_t n) {
-        auto it = free_.emplace(off, n).first;
-        auto nx = std::next(it);
-        if (nx != free_.end() && it->first + it->second == nx->first) {
-            it->second += nx->second;
-            free_.erase(nx);
-        }
-        if (it != free_.begin()) {
-            auto pv = std::prev(it);
-            if (pv->first + pv->second == it->first) {
-                pv->second += it->second;
-                free_.erase(it);
-            }
-        }
-    }
-};
-
-// Device memory of films and tile outputs: 1 GiB chunks (larger for a larger
-// request) reserved on demand up to the budget and held until the server ends.
-struct DevicePool {
-    struct Chunk {
-        char* base;
-        size_t bytes;
-        RangeAlloc ra;
-    };
-    std::vector<Chunk> chunks;
-    uint64_t budget = 0, reserved = 0, used = 0, peak = 0;
-    static constexpr size_t kChunk = size_t(1) << 30;
-
-    static size_t round(size_t n) { return (n + 255) & ~size_t(255); }
-    // SF_ERR_BUDGET without a message when the budget is full (the request waits).
-    sf_status alloc(sf_context* c, size_t n, void** out) {
-        n = round(n);
-        if (used + n > budget) return SF_ERR_BUDGET;
-        for (auto& ch : chunks) {
-            size_t off = 0;
-            if (ch.ra.take(n, &off)) {
-                *out = ch.base + off;
-                used += n;
-                peak = std::max(peak, used);
-                return SF_OK;
-            }
-        }
-        size_t want = std::min<uint64_t>(std::max(kChunk, n), budget - reserved);
-        if (want < n) return SF_ERR_BUDGET;
-        void* p = nullptr;
-        sf_status st = ctx_alloc(c, want, &p);
-        if (st != SF_OK) return st;
-        chunks.push_back({static_cast<char*>(p), want, {}});
-        chunks.back().ra.init(want);
-        reserved += want;
-        size_t off = 0;
-        chunks.back().ra.take(n, &off);
-        *out = static_cast<char*>(p) + off;
-        used += n;
-        peak = std::max(peak, used);
-        return SF_OK;
-    }
-    void release(void* p, size_t n) {
-        if (!p) return;
-        n = round(n);
-        char* q = static_cast<char*>(p);
-        for (auto& ch : chunks)
-            if (q >= ch.base && q < ch.base + ch.bytes) {
-                ch.ra.give(size_t(q - ch.base), n);
-                used -= std::min<uint64_t>(used, n);
-                return;
-            }
-    }
-    void destroy(sf_context* c) {
-        for (auto& ch : chunks) ctx_free(c, ch.base, ch.bytes);
-        chunks.clear();
-        reserved = used = 0;
-    }
-};
-
-// A preview's film, kept on the device until the preview is released and no
-// refinement still needs it. DevScene | accum | aux | depth.
-struct ServeFilm {
-    void* mem = nullptr;
-    size_t bytes = 0;
-    DevScene* scene = nullptr;
-    FilmPlanes planes{};
-    sf_graph* graph = nullptr;
-    uint32_t samples = 0;  // samples once every scheduled pass has finished
-    uint32_t max_bounces = 0, max_steps = 0;
-    bool busy = false;     // written by a batch in flight
-    int refs = 0;          // the preview until released, plus each refinement until it ends
-};
-
-enum ServeClass { SC_TILE = 0, SC_FORM = 1, SC_GENERIC = 2 };
-
-struct ServeReq {
-    uint64_t ticket = 0;
-    uint32_t kind = 0, state = SF_REQ_QUEUED;
-    sf_status status = SF_OK;
-    int cls = SC_TILE;
-    std::string error;
-    double t_submit = 0, t_start = 0, t_done = 0;
-    uint32_t width = 0, height = 0, samples = 0, sample_start = 0, batch_requests = 0;
-    uint64_t work = 0;
-    ServeFilm* film = nullptr;  // 3D
-    DevScene scene{};           // PREVIEW: uploaded with its first batch
-    PlanarDev F{};              // TILE_2D
-    CanvasDev K{};
-    bool traps = true;          // TILE_2D: SF_TILE_ALL
-    void* dmem = nullptr;       // TILE_2D: descriptors and outputs
-    size_t dbytes = 0;
-    size_t h_off = 0, h_bytes = 0;
-};
-
-constexpr uint32_t kServeMaxSlots = 8;
-constexpr uint32_t kServeMaxTiles = 64;  // 2D tiles per batch
-// A tile's device block starts with PlanarDev (0), CanvasDev (256) and its pixel
-// counter (512); the staging area holds the same bytes, counter zero.
-constexpr size_t kTileHeader = 768;
-static_assert(sizeof(PlanarDev) <= 256 && sizeof(CanvasDev) <= 256, "tile header layout");
-
-struct ServeSlot {
-    cudaStream_t hi = nullptr, lo = nullptr, st = nullptr;
-    cudaEvent_t done = nullptr;
-    WaveArena arena;
-    char* stage = nullptr;  // pinned: job table | scenes | tile descriptors | status word
-    size_t stage_bytes = 0;
-    std::vector<ServeReq*> reqs;
-    int cls = SC_TILE;
-    bool busy = false;
-};
-
-}  // namespace
-
-struct sf_server {
-    sf_context* ctx = nullptr;
-    sf_server_config cfg{};
-    ServeClock::time_point t0;
-    std::mutex mu;
-    std::condition_variable cv_work, cv_done;
-    std::thread thread;
-    bool stop = false;
-    uint64_t next_ticket = 1;
-    std::unordered_map<uint64_t, std::unique_ptr<ServeReq>> reqs;
-    std::deque<ServeReq*> queue;
-    std::vector<ServeSlot> slots;
-    DevicePool pool;
-    char* host = nullptr;  // pinned result pool
-    RangeAlloc host_ra;
-    uint64_t host_used = 0;
-    sf_server_stats stats{};
-};
-
-namespace {
-
-double serve_now(const sf_server* s) {
-    return std::chrono::duration<double, std::milli>(ServeClock::now() - s->t0).count();
-}
-
-size_t stage_jobs_off(const sf_server*) { return 0; }
-size_t stage_scenes_off(const sf_server* s) { return DevicePool::round(size_t(s->cfg.max_jobs) * sizeof(BatchJob)); }
-size_t stage_tiles_off(const sf_server* s) {
-    return stage_scenes_off(s) + DevicePool::round(size_t(s->cfg.max_jobs) * sizeof(DevScene));
-}
-size_t stage_status_off(const sf_server* s) { return stage_tiles_off(s) + size_t(kServeMaxTiles) * kTileHeader; }
-
-void film_unref(sf_server* s, ServeFilm* f) {
-    if (--f->refs > 0) return;
-    s->pool.release(f->mem, f->bytes);
-    sf_graph_destroy(f->graph);
-    delete f;
-}
-
-void finish_req(sf_server* s, ServeReq* r, sf_status st, const std::string& error = std::string()) {
-    r->state = st == SF_OK ? SF_REQ_DONE : SF_REQ_FAILED;
-    r->status = st;
-    r->error = error;
-    r->t_done = serve_now(s);
-    if (r->kind == SF_REQ_TILE_2D) {
-        s->pool.release(r->dmem, r->dbytes);
-        r->dmem = nullptr;
-    }
-    if (r->film) {
-        r->film->busy = false;
-        if (r->kind == SF_REQ_REFINE) {
-            film_unref(s, r->film);
-            r->film = nullptr;
-        }
-    }
-    if (st == SF_OK) s->stats.completed++;
-    else s->stats.failed++;
-}
-
-// Bytes a request needs when admitted: device (films, tile outputs) and host results.
-void request_bytes(const ServeReq* r, size_t* dev, size_t* host) {
-    size_t px = size_t(r->width) * r->height;
-    if (r->kind == SF_REQ_PREVIEW) *dev = DevicePool::round(sizeof(DevScene)) + DevicePool::round(px * 36);
-    else if (r->kind == SF_REQ_TILE_2D) *dev = kTileHeader + px * 24;
-    else *dev = 0;
-    // 3D: accum; 2D: iterations | smooth, or iterations | distance | 4 trap planes
-    *host = DevicePool::round(r->kind != SF_REQ_TILE_2D ? px * 16 : r->traps ? px * 24 : px * 8);
-}
-
-// Retires the batches whose completion event has fired. Returns true if any did.
-bool serve_retire(sf_server* s) {
-    bool any = false;
-    for (auto& sl : s->slots) {
-        if (!sl.busy) continue;
-        cudaError_t e = cudaEventQuery(sl.done);
-        if (e == cudaErrorNotReady) continue;
-        sf_status st = SF_OK;
-        std::string msg;
-        if (e != cudaSuccess) {
-            st = cuda_fail(e, "serving batch");
-            msg = g_error;
-        } else if (sl.cls != SC_TILE) {
-            uint32_t w = 0;
-            std::memcpy(&w, sl.stage + stage_status_off(s), 4);
-            if (w) {
-                st = SF_ERR_WAVEFRONT;
-                msg = "wavefront invariant word " + std::to_string(w);
-            }
-        }
-        for (ServeReq* r : sl.reqs) finish_req(s, r, st, msg);
-        sl.reqs.clear();
-        sl.busy = false;
-        any = true;
-    }
-    if (any) s->cv_done.notify_all();
-    return any;
-}
-
-sf_status launch_tiles(sf_server* s, ServeSlot& sl) {
-    cudaStream_t st = sl.st;
-    char* stage = sl.stage + stage_tiles_off(s);
-    for (size_t i = 0; i < sl.reqs.size(); ++i) {
-        ServeReq* r = sl.reqs[i];
-        size_t n = size_t(r->width) * r->height;
-        char* d = static_cast<char*>(r->dmem);
-        char* h = stage + i * kTileHeader;
-        std::memset(h, 0, kTileHeader);
-        std::memcpy(h, &r->F, sizeof r->F);
-        std::memcpy(h + 256, &r->K, sizeof r->K);
-        CU(cudaMemcpyAsync(d, h, kTileHeader, cudaMemcpyHostToDevice, st));
-        float* dist = reinterpret_cast<float*>(d + kTileHeader);
-        float* traps = dist + n;
-        uint32_t* iters = reinterpret_cast<uint32_t*>(traps + 4 * n);
-        s->ctx->launches++;
-        s->stats.launches++;
-        CU(sf_launch_escape2d(reinterpret_cast<PlanarDev*>(d), reinterpret_cast<CanvasDev*>(d + 256), 0, 0, r->width,
-                              r->height, 0xffffffffu, dist, traps, iters, s->ctx->d_stats,
-                              reinterpret_cast<uint32_t*>(d + 512), r->traps ? 1 : 0,
-                              r->F.family == 3 || r->F.family == 4, st));
-        char* out = s->host + r->h_off;
-        CU(cudaMemcpyAsync(out, iters, n * 4, cudaMemcpyDeviceToHost, st));
-        if (r->traps) CU(cudaMemcpyAsync(out + n * 4, dist, n * 4 * 5, cudaMemcpyDeviceToHost, st));  // dist | traps
-        else CU(cudaMemcpyAsync(out + n * 4, traps, n * 4, cudaMemcpyDeviceToHost, st));
-    }
-    return SF_OK;
-}
-
-sf_status launch_wave(sf_server* s, ServeSlot& sl) {
-    cudaStream_t st = sl.st;
-    WaveArena& a = sl.arena;
-    BatchJob* hj = reinterpret_cast<BatchJob*>(sl.stage + stage_jobs_off(s));
-    DevScene* hs = reinterpret_cast<DevScene*>(sl.stage + stage_scenes_off(s));
-    uint32_t paths = 0, pixels = 0, rounds = 0, steps = 0, n_scenes = 0;
-    for (size_t i = 0; i < sl.reqs.size(); ++i) {
-        ServeReq* r = sl.reqs[i];
-        ServeFilm* f = r->film;
-        uint32_t px = r->width * r->height;
-        BatchJob j{};
-        j.prog = f->graph->d_prog;
-        j.scene = f->scene;
-        j.film = f->planes;
-        j.geom = DispatchGeom{0, 0, r->width, r->height, r->sample_start, r->samples, px * r->samples};
-        j.path_begin = paths;
-        j.pixel_begin = pixels;
-        j.form = f->graph->prog.form;
-        hj[i] = j;
-        paths += px * r->samples;
-        pixels += px;
-        rounds = std::max(rounds, f->max_bounces + 2);
-        steps = std::max(steps, f->max_steps);
-        if (r->kind == SF_REQ_PREVIEW) {
-            hs[n_scenes] = r->scene;
-            CU(cudaMemcpyAsync(f->scene, hs + n_scenes, sizeof(DevScene), cudaMemcpyHostToDevice, st));
-            CU(sf_launch_film_clear(f->planes, st));
-            s->ctx->launches++;
-            s->stats.launches++;
-            n_scenes++;
-        }
-    }
-    a.bt.n_jobs = uint32_t(sl.reqs.size());
-    a.bt.total_paths = paths;
-    a.bt.total_pixels = pixels;
-    a.max_steps = steps;
-    a.any_generic = sl.cls == SC_GENERIC;
-    CU(cudaMemcpyAsync(a.bt.jobs, hj, sl.reqs.size() * sizeof(BatchJob), cudaMemcpyHostToDevice, st));
-    CU(cudaMemsetAsync(a.status, 0, 16, st));
-    // rounds vary per batch; the arena's queue counters are sized for its largest
-    WaveArena pass = a;
-    pass.rounds = rounds;
-    uint64_t before = s->ctx->launches;
-    sf_status rs = wave_record_pass(s->ctx, pass, st, false);
-    s->stats.launches += s->ctx->launches - before;
-    if (rs != SF_OK) return rs;
-    for (ServeReq* r : sl.reqs)
-        CU(cudaMemcpyAsync(s->host + r->h_off, r->film->planes.accum, size_t(r->width) * r->height * 16,
-                           cudaMemcpyDeviceToHost, st));
-    CU(cudaMemcpyAsync(sl.stage + stage_status_off(s), a.status, 4, cudaMemcpyDeviceToHost, st));
-    return SF_OK;
-}
-
-// Forms and launches one batch on a free slot. Returns true if it launched one.
-bool serve_admit(sf_server* s, ServeSlot& sl) {
-    std::vector<ServeReq*> take;
-    int cls = -1;
-    uint64_t paths = 0, pixels = 0;
-    uint32_t rounds = 0;
-    bool blocked = false;
-    // films with an earlier request left in the queue: their later requests wait, so
-    // each film's passes run in submission order
-    std::set<const ServeFilm*> held;
-    auto skip = [&](std::deque<ServeReq*>::iterator& it) {
-        if ((*it)->film) held.insert((*it)->film);
-        ++it;
-    };
-    for (auto it = s->queue.begin(); it != s->queue.end() && take.size() < s->cfg.max_jobs;) {
-        ServeReq* r = *it;
-        if (r->kind == SF_REQ_REFINE && (r->film->busy || !r->film->mem || held.count(r->film))) { skip(it); continue; }
-        if (cls >= 0 && r->cls != cls) { skip(it); continue; }
-        uint64_t px = uint64_t(r->width) * r->height;
-        if (r->kind == SF_REQ_TILE_2D) {
-            if (take.size() >= kServeMaxTiles || (pixels + px > s->cfg.max_tile_pixels && !take.empty())) break;
-        } else {
-            uint64_t need = px * r->samples;
-            if (paths + need > s->cfg.path_capacity) { skip(it); continue; }
-        }
-        size_t dev = 0, hb = 0;
-        request_bytes(r, &dev, &hb);
-        size_t hoff = 0;
-        if (!s->host_ra.take(hb, &hoff)) { blocked = true; break; }
-        void* dm = nullptr;
-        if (dev) {
-            sf_status st = s->pool.alloc(s->ctx, dev, &dm);
-            if (st != SF_OK) {
-                s->host_ra.give(hoff, hb);
-                blocked = true;
-                break;
-            }
-        }
-        r->h_off = hoff;
-        r->h_bytes = hb;
-        s->host_used += hb;
-        if (r->kind == SF_REQ_TILE_2D) {
-            r->dmem = dm;
-            r->dbytes = dev;
-        } else if (r->kind == SF_REQ_PREVIEW) {
-            ServeFilm* f = r->film;
-            f->mem = dm;
-            f->bytes = dev;
-            char* b = static_cast<char*>(dm);
-            size_t px2 = size_t(px);
-            f->scene = reinterpret_cast<DevScene*>(b);
-            char* film = b + DevicePool::round(sizeof(DevScene));
-            f->planes.accum = reinterpret_cast<float4*>(film);
-            f->planes.aux = reinterpret_cast<float4*>(film + px2 * 16);
-            f->planes.depth = reinterpret_cast<float*>(film + px2 * 32);
-            f->planes.width = r->width;
-            f->planes.height = r->height;
-        }
-        if (r->kind != SF_REQ_TILE_2D) {
-            r->sample_start = r->film->samples;
-            r->film->samples += r->samples;
-            r->film->busy = true;
-            paths += px * r->samples;
-            rounds = std::max(rounds, r->film->max_bounces + 2);
-            r->work = px * r->samples;
-        } else {
-            r->work = px;
-        }
-        pixels += px;
-        cls = r->cls;
-        take.push_back(r);
-        it = s->queue.erase(it);
-    }
-    if (blocked) s->stats.admission_waits++;
-    if (take.empty()) return false;
-    sl.reqs = take;
-    sl.cls = cls;
-    bool preview = false;
-    for (ServeReq* r : take) preview |= r->kind == SF_REQ_PREVIEW;
-    sl.st = preview ? sl.hi : sl.lo;
-    double now = serve_now(s);
-    for (ServeReq* r : take) {
-        r->state = SF_REQ_RUNNING;
-        r->t_start = now;
-        r->batch_requests = uint32_t(take.size());
-    }
-    sf_status st = cls == SC_TILE ? launch_tiles(s, sl) : launch_wave(s, sl);
-    cudaError_t e = st == SF_OK ? cudaEventRecord(sl.done, sl.st) : cudaSuccess;
-    if (st == SF_OK && e != cudaSuccess) st = cuda_fail(e, "cudaEventRecord");
-    s->stats.batches++;
-    s->stats.batched_requests += take.size();
-    if (st != SF_OK) {
-        // the stream may still run part of the batch: wait for it before failing the requests
-        std::string msg = g_error;
-        cudaStreamSynchronize(sl.st);
-        for (ServeReq* r : take) finish_req(s, r, st, msg);
-        sl.reqs.clear();
-        s->cv_done.notify_all();
-        return true;
-    }
-    sl.busy = true;
-    return true;
-}
-
-void serve_loop(sf_server* s) {
-    cudaSetDevice(s->ctx->device);
-    std::unique_lock<std::mutex> lk(s->mu);
-    while (!s->stop) {
-        bool progress = serve_retire(s);
-        bool busy = false;
-        bool admitting = true;
-        for (auto& sl : s->slots) {
-            // a scan that admits nothing would admit nothing for the next free slot either
-            if (admitting && !sl.busy && !s->queue.empty()) {
-                admitting = serve_admit(s, sl);
-                progress |= admitting;
-            }
-            busy |= sl.busy;
-        }
-        if (progress) continue;
-        if (busy) {
-            lk.unlock();
-            std::this_thread::sleep_for(std::chrono::microseconds(20));
-            lk.lock();
-        } else {
-            s->cv_work.wait_for(lk, std::chrono::milliseconds(2));
-        }
-    }
-    // drain the batches in flight
-    for (auto& sl : s->slots)
-        if (sl.busy) {
-            lk.unlock();
-            cudaEventSynchronize(sl.done);
-            lk.lock();
-        }
-    serve_retire(s);
-}
-
-void fill_result(const sf_server* s, const ServeReq* r, sf_result* o) {
-    std::memset(o, 0, sizeof *o);
-    o->state = r->state;
-    o->status = r->status;
-    o->kind = r->kind;
-    o->width = r->width;
-    o->height = r->height;
-    o->samples = r->kind == SF_REQ_TILE_2D ? 0 : r->sample_start + r->samples;
-    o->batch_requests = r->batch_requests;
-    o->work = r->work;
-    o->submit_ms = r->t_submit;
-    o->start_ms = r->t_start;
-    o->done_ms = r->t_done;
-    if (r->state != SF_REQ_DONE) return;
-    const char* h = s->host + r->h_off;
-    size_t n = size_t(r->width) * r->height;
-    if (r->kind == SF_REQ_TILE_2D) {
-        o->iterations = reinterpret_cast<const uint32_t*>(h);
-        if (r->traps) {
-            o->distance = reinterpret_cast<const float*>(h + n * 4);
-            o->traps = reinterpret_cast<const float*>(h + n * 8);
-            o->smooth = o->traps;
-        } else {
-            o->smooth = reinterpret_cast<const float*>(h + n * 4);
-        }
-    } else {
-        o->accum = reinterpret_cast<const float*>(h);
-    }
-}
-
-}  // namespace
-
-extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg, sf_server** out) {
-    if (!c || !out) return fail(SF_ERR_INVALID, "null argument");
-    *out = nullptr;
-    sf_server_config k = cfg ? *cfg : sf_server_config{};
-    if (!k.slots) k.slots = 4;
-    if (!k.path_capacity) k.path_capacity = 1u << 22;
-    if (!k.max_jobs) k.max_jobs = 256;
-    if (!k.max_tile_pixels) k.max_tile_pixels = 1u << 25;
-    if (!k.host_result_bytes) k.host_result_bytes = uint64_t(1) << 30;
-    if (!k.min_blocks) k.min_blocks = 3;
-    if (!k.quantum) k.quantum = 128;
-    if (!k.regen) k.regen = 4;
-    if (!k.hbm_budget) return fail(SF_ERR_INVALID, "hbm_budget must be set");
-    if (k.slots > kServeMaxSlots) return fail(SF_ERR_INVALID, "1..8 slots");
-    if (k.max_jobs > SF_BATCH_MAX_JOBS) return fail(SF_ERR_INVALID, "a batch holds 1 to 1024 requests");
-    if (k.path_capacity > 0x7fffffffu) return fail(SF_ERR_INVALID, "path capacity above 2^31");
-    sf_status ls = check_launch(k.min_blocks, k.quantum, k.regen);
-    if (ls != SF_OK) return ls;
-    cudaSetDevice(c->device);
-    auto* s = new sf_server();
-    s->ctx = c;
-    s->cfg = k;
-    s->pool.budget = k.hbm_budget;
-    ctx_retain(c);
-    auto bail = [&](sf_status st) {
-        sf_server_destroy(s);
-        return st;
-    };
-    cudaError_t e = cudaHostAlloc(reinterpret_cast<void**>(&s->host), k.host_result_bytes, cudaHostAllocDefault);
-    if (e != cudaSuccess) {
-        s->host = nullptr;
-        return bail(cuda_fail(e, "pinned result pool"));
-    }
-    s->host_ra.init(k.host_result_bytes);
-    int lo_prio = 0, hi_prio = 0;
-    cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
-    s->slots.resize(k.slots);
-    const uint32_t max_rounds = 32 + 2;  // bounces <= 32 (validate_config)
-    for (auto& sl : s->slots) {
-        sl.stage_bytes = stage_status_off(s) + 256;
-        e = cudaStreamCreateWithPriority(&sl.hi, cudaStreamNonBlocking, hi_prio);
-        if (e == cudaSuccess) e = cudaStreamCreateWithPriority(&sl.lo, cudaStreamNonBlocking, lo_prio);
-        if (e == cudaSuccess) e = cudaEventCreateWithFlags(&sl.done, cudaEventDisableTiming);
-        if (e == cudaSuccess)
-            e = cudaHostAlloc(reinterpret_cast<void**>(&sl.stage), sl.stage_bytes, cudaHostAllocDefault);
-        if (e != cudaSuccess) return bail(cuda_fail(e, "server slot"));
-        sf_status st = arena_alloc(c, sl.arena, k.path_capacity, k.max_jobs, max_rounds, 0, nullptr);
-        if (st != SF_OK) return bail(st);
-        sl.arena.min_blocks = k.min_blocks;
-        sl.arena.quantum = k.quantum;
-        sl.arena.regen = k.regen;
-    }
-    s->t0 = ServeClock::now();
-    s->thread = std::thread(serve_loop, s);
-    *out = s;
-    return SF_OK;
-}
-
-extern "C" sf_status sf_serve_submit(sf_server* s, const sf_request* q, uint64_t* ticket) {
-    if (!s || !q || !ticket) return fail(SF_ERR_INVALID, "null argument");
-    *ticket = 0;
-    auto r = std::make_unique<ServeReq>();
-    r->kind = q->kind;
-    if (q->kind == SF_REQ_PREVIEW) {
-        if (!q->graph || q->graph->ctx != s->ctx) return fail(SF_ERR_INVALID, "preview graph missing or of another context");
-        sf_status st = validate_config(q->cfg);
-        if (st != SF_OK) return st;
-        if (q->scene.light_count > SF_MAX_LIGHTS || q->scene.finish_count > SF_MAX_FINISHES)
-            return fail(SF_ERR_INVALID, "too many lights or finishes");
-        r->width = q->cfg.width;
-        r->height = q->cfg.height;
-        r->samples = q->cfg.samples_per_pixel;
-        scene_dev(q->scene, q->cfg, q->graph->info, r->scene);
-        r->cls = q->graph->prog.form == SF_FORM_GENERIC ? SC_GENERIC : SC_FORM;
-    } else if (q->kind == SF_REQ_REFINE) {
-        if (q->samples == 0) return fail(SF_ERR_INVALID, "a refinement adds at least one sample");
-    } else if (q->kind == SF_REQ_TILE_2D) {
-        sf_status st = planar_check(&q->planar);
-        if (st != SF_OK) return st;
-        if (!q->canvas.width || !q->canvas.height) return fail(SF_ERR_INVALID, "empty canvas");
-        r->width = q->canvas.width;
-        r->height = q->canvas.height;
-        planar_dev(q->planar, r->F);
-        std::memset(&r->K, 0, sizeof r->K);
-        r->K.center[0] = q->canvas.center[0];
-        r->K.center[1] = q->canvas.center[1];
-        r->K.zoom = q->canvas.zoom;
-        r->K.aspect = float(q->canvas.width) / float(q->canvas.height);
-        float rad = q->canvas.rotation_deg * (3.14159265358979323846f / 180.0f);
-        r->K.rot_sin = sinf(rad);
-        r->K.rot_cos = cosf(rad);
-        r->K.width = q->canvas.width;
-        r->K.height = q->canvas.height;
-        r->K.seed = uint32_t(q->canvas.seed) ^ uint32_t(q->canvas.seed >> 32);
-        r->cls = SC_TILE;
-        if (q->tile_outputs > SF_TILE_COUNTS) return fail(SF_ERR_INVALID, "unknown tile outputs");
-        r->traps = q->tile_outputs == SF_TILE_ALL;
-        if (uint64_t(r->width) * r->height > s->cfg.max_tile_pixels)
-            return fail(SF_ERR_INVALID, "tile larger than the server's max_tile_pixels");
-    } else {
-        return fail(SF_ERR_INVALID, "unknown request kind");
-    }
-    std::lock_guard<std::mutex> lk(s->mu);
-    if (s->stop) return fail(SF_ERR_INVALID, "server stopping");
-    if (q->kind == SF_REQ_REFINE) {
-        auto it = s->reqs.find(q->parent);
-        if (it == s->reqs.end() || it->second->kind != SF_REQ_PREVIEW || !it->second->film)
-            return fail(SF_ERR_INVALID, "refinement of an unknown or released preview");
-        ServeReq* p = it->second.get();
-        if (p->state == SF_REQ_FAILED) return fail(SF_ERR_INVALID, "refinement of a failed preview");
-        r->film = p->film;
-        r->width = p->width;
-        r->height = p->height;
-        r->samples = q->samples;
-        r->cls = p->cls;
-        r->film->refs++;
-    }
-    size_t dev = 0, hb = 0;
-    request_bytes(r.get(), &dev, &hb);
-    if (r->kind != SF_REQ_TILE_2D && uint64_t(r->width) * r->height * r->samples > s->cfg.path_capacity) {
-        if (r->film) film_unref(s, r->film);
-        return fail(SF_ERR_INVALID, "request needs more paths than the server's path_capacity");
-    }
-    if (dev > s->cfg.hbm_budget || hb > s->cfg.host_result_bytes) {
-        if (r->film) film_unref(s, r->film);
-        return fail(SF_ERR_BUDGET, "request larger than the server's HBM budget or result pool");
-    }
-    if (q->kind == SF_REQ_PREVIEW) {
-        auto* f = new ServeFilm();
-        f->graph = q->graph;
-        graph_retain(q->graph);
-        f->max_bounces = q->cfg.max_bounces;
-        f->max_steps = q->cfg.max_steps;
-        f->refs = 1;
-        r->film = f;
-    }
-    r->ticket = s->next_ticket++;
-    r->t_submit = serve_now(s);
-    *ticket = r->ticket;
-    s->queue.push_back(r.get());
-    s->reqs.emplace(r->ticket, std::move(r));
-    s->stats.submitted++;
-    s->cv_work.notify_one();
-    return SF_OK;
-}
-
-extern "C" sf_status sf_serve_poll(sf_server* s, uint64_t ticket, sf_result* out) {
-    if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return fail(SF_ERR_INVALID, "unknown ticket");
-    fill_result(s, it->second.get(), out);
-    return SF_OK;
-}
-
-extern "C" sf_status sf_serve_wait(sf_server* s, uint64_t ticket, uint32_t timeout_ms, sf_result* out) {
-    if (!s) return fail(SF_ERR_INVALID, "null server");
-    std::unique_lock<std::mutex> lk(s->mu);
-    auto deadline = ServeClock::now() + std::chrono::milliseconds(timeout_ms);
-    for (;;) {
-        auto it = s->reqs.find(ticket);
-        if (it == s->reqs.end()) return fail(SF_ERR_INVALID, "unknown ticket");
-        ServeReq* r = it->second.get();
-        if (r->state == SF_REQ_DONE || r->state == SF_REQ_FAILED) {
-            if (out) fill_result(s, r, out);
-            return r->state == SF_REQ_DONE ? SF_OK : fail(r->status, "request failed: " + r->error);
-        }
-        if (timeout_ms == 0) s->cv_done.wait(lk);
-        else if (s->cv_done.wait_until(lk, deadline) == std::cv_status::timeout && ServeClock::now() >= deadline)
-            return fail(SF_ERR_TIMEOUT, "request not finished in time");
-    }
-}
-
-extern "C" sf_status sf_serve_release(sf_server* s, uint64_t ticket) {
-    if (!s) return fail(SF_ERR_INVALID, "null server");
-    std::lock_guard<std::mutex> lk(s->mu);
-    auto it = s->reqs.find(ticket);
-    if (it == s->reqs.end()) return fail(SF_ERR_INVALID, "unknown ticket");
-    ServeReq* r = it->second.get();
-    if (r->state == SF_REQ_QUEUED || r->state == SF_REQ_RUNNING) return fail(SF_ERR_BUSY, "request in flight");
-    if (r->h_bytes) {
-        s->host_ra.give(r->h_off, r->h_bytes);
-        s->host_used -= r->h_bytes;
-    }
-    if (r->film) film_unref(s, r->film);
-    s->reqs.erase(it);
-    s->cv_work.notify_one();  // memory freed: queued requests may now fit
-    return SF_OK;
-}
-
-extern "C" sf_status sf_server_stats_get(sf_server* s, sf_server_stats* out) {
-    if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
-    std::lock_guard<std::mutex> lk(s->mu);
-    *out = s->stats;
-    out->hbm_used = s->pool.used;
-    out->hbm_peak = s->pool.peak;
-    out->hbm_reserved = s->pool.reserved;
-    out->host_used = s->host_used;
-    out->now_ms = serve_now(s);
-    return SF_OK;
-}
-
-extern "C" sf_status sf_server_destroy(sf_server* s) {
-    if (!s) return SF_OK;
-    sf_context* c = s->ctx;
-    cudaSetDevice(c->device);
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        s->stop = true;
-    }
-    s->cv_work.notify_all();
-    if (s->thread.joinable()) s->thread.join();
-    {
-        std::lock_guard<std::mutex> lk(s->mu);
-        for (ServeReq* r : s->queue) finish_req(s, r, SF_ERR_INVALID, "server stopped");
-        s->queue.clear();
-        s->cv_done.notify_all();
-        for (auto& kv : s->reqs)
-            if (kv.second->film) film_unref(s, kv.second->film);
-        s->reqs.clear();
-    }
-    for (auto& sl : s->slots) {
-        if (sl.hi) cudaStreamSynchronize(sl.hi);
-        if (sl.lo) cudaStreamSynchronize(sl.lo);
-        ctx_free(c, sl.arena.mem, sl.arena.mem_bytes);
-        if (sl.stage) cudaFreeHost(sl.stage);
-        if (sl.done) cudaEventDestroy(sl.done);
-        if (sl.hi) cudaStreamDestroy(sl.hi);
-        if (sl.lo) cudaStreamDestroy(sl.lo);
-    }
-    s->pool.destroy(c);
-    if (s->host) cudaFreeHost(s->host);
-    delete s;
-    ctx_release(c);
-    return SF_OK;
-}

@@ -1,0 +1,150 @@
+// Internal interface of the host runtime shared by its translation units
+// (sf_host.cpp: graphs, contexts, sessions, checkpoints, escape time; sf_batch_host.cpp:
+// batched wavefronts; sf_serve.cpp: the serving scheduler). Not part of the C ABI.
+#pragma once
+#include <cuda_runtime.h>
+
+#include <atomic>
+#include <mutex>
+#include <string>
+#include <vector>
+
+#include "../../include/syfrack_gpu.h"
+#include "sf_kernels.cuh"
+#include "sf_program.h"
+
+namespace sfh {
+
+// Error reporting: the calling thread's message for sf_last_error.
+sf_status fail(sf_status s, const std::string& msg);
+sf_status cuda_fail(cudaError_t e, const char* what);
+const std::string& last_error();
+#define CU(expr)                                                   \
+    do {                                                           \
+        cudaError_t _e = (expr);                                   \
+        if (_e != cudaSuccess) return sfh::cuda_fail(_e, #expr);   \
+    } while (0)
+
+// The graph as the host holds it after validation.
+struct HostGraph {
+    std::vector<sf_node> nodes;
+    std::vector<sf_link> links;
+    std::vector<uint32_t> body;
+    float safety = 1.f, hint = 1.f;
+
+    const sf_node* node(uint32_t id) const {
+        for (auto& n : nodes)
+            if (n.id == id) return &n;
+        return nullptr;
+    }
+    bool input_of(uint32_t to, uint32_t port, uint32_t* from) const {
+        for (auto& l : links)
+            if (l.to_node == to && l.to_port == port) { *from = l.from_node; return true; }
+        return false;
+    }
+    std::vector<uint32_t> body_of(const sf_node& n) const {
+        std::vector<uint32_t> b;
+        if (n.kind == SF_NODE_ITERATE)
+            for (uint32_t i = 0; i < n.body_len; ++i) b.push_back(body[n.body_offset + i]);
+        return b;
+    }
+};
+
+}  // namespace sfh
+
+// ------------------------------------------------------------------ context
+struct sf_context {
+    int device = 0;
+    cudaStream_t stream = nullptr;
+    uint64_t budget = 0, used = 0;
+    std::string device_name;
+    int cc_major = 0, cc_minor = 0, sm_count = 0;
+    bool profiling = false;
+    struct Timed { cudaEvent_t a, b; bool trace; };
+    std::vector<Timed> timed;
+    std::vector<cudaEvent_t> spare;
+    double kernel_ms = 0, trace_ms = 0;
+    std::atomic<uint64_t> launches{0}, trace_launches{0};
+    unsigned long long* d_stats = nullptr;  // SF_STAT_COUNT counters
+    uint32_t* d_work = nullptr;             // scratch work counters
+    // Graphs and sessions hold a reference, so handles may be destroyed in any order.
+    int refs = 1;
+    std::mutex mu;
+    std::mutex alloc_mu;  // budget accounting (a server thread allocates too)
+};
+
+struct sf_graph {
+    sf_context* ctx = nullptr;
+    int refs = 1;  // sessions hold a reference
+    sfh::HostGraph host;
+    DeProgram prog;
+    DeProgram* d_prog = nullptr;
+    sf_graph_info info;
+    std::string topology;
+};
+
+namespace sfh {
+
+// Device memory under the context's HBM admission budget.
+sf_status ctx_alloc(sf_context* c, size_t bytes, void** p);
+void ctx_free(sf_context* c, void* p, size_t bytes);
+void ctx_retain(sf_context* c);
+void ctx_release(sf_context* c);
+void graph_retain(sf_graph* g);
+cudaEvent_t get_event(sf_context* c);
+void collect_timing(sf_context* c);
+sf_status wait_stream(cudaStream_t st, uint32_t timeout_ms);
+
+// Scoped CUDA-event timing of one launch on the context stream.
+struct LaunchTimer {
+    sf_context* c;
+    cudaEvent_t a = nullptr;
+    bool trace;
+    cudaStream_t st;
+    LaunchTimer(sf_context* ctx, bool is_trace, bool timed = true, cudaStream_t stream = nullptr)
+        : c(ctx), trace(is_trace), st(stream ? stream : ctx->stream) {
+        c->launches++;
+        if (is_trace) c->trace_launches++;
+        if (c->profiling && timed) {
+            a = get_event(c);
+            cudaEventRecord(a, st);
+        }
+    }
+    ~LaunchTimer() {
+        if (a) {
+            cudaEvent_t b = get_event(c);
+            cudaEventRecord(b, st);
+            c->timed.push_back({a, b, trace});
+        }
+    }
+};
+
+float sqrt_threshold(float b);
+void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph_info& gi, DevScene& S);
+sf_status validate_config(const sf_render_config& c);
+sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen);
+void planar_dev(const sf_planar_desc& f, PlanarDev& o);
+sf_status planar_check(const sf_planar_desc* f);
+cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);
+
+// Device storage of one batched wavefront: the job table, path state and queues.
+struct WaveArena {
+    BatchTable bt{};
+    PathSoA soa{};
+    uint32_t capacity = 0, rounds = 0, max_steps = 0, max_jobs = 0;
+    uint32_t* lists = nullptr;
+    uint32_t* resume = nullptr;
+    uint32_t* counts = nullptr;
+    uint32_t* qcounts = nullptr;
+    uint32_t* status = nullptr;
+    void* mem = nullptr;
+    size_t mem_bytes = 0;
+    bool any_generic = false;
+    uint32_t min_blocks = 3, quantum = 128, regen = 4;
+};
+
+sf_status arena_alloc(sf_context* c, WaveArena& a, uint32_t capacity, uint32_t max_jobs, uint32_t rounds,
+                      size_t extra_bytes, size_t* extra_offset);
+sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, bool timed);
+
+}  // namespace sfh

@@ -80,7 +80,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
 
     uint32_t state = TL_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
     bool shadow = false;
-    March m;
+    March m{};  // set by each refill before use
     float3 grad = mk3(0.f, 0.f, 0.f);
     float hstep = 0.f;
     uint32_t hit_w = 0;  // iterations | material << 16 of the surface hit whose normal is being tapped
