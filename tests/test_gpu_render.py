@@ -188,3 +188,28 @@ def test_budget_admission(gpu_ctx):
         RenderSession(r, workloads.mandelbox_scene(), workloads.mandelbox_pathtrace_config())
     assert e.value.status == 7
     ctx.close()
+
+
+@pytest.mark.parametrize("name", ["mandelbulb", "mandelbox", "menger"])
+def test_unit_normals_each_fractal(renderer, name):
+    # first-hit normals (tetrahedral taps, normalised) are unit vectors on every form
+    g = Graph.bundled(name)
+    d = 3.0 if name != "mandelbox" else 7.0
+    cam = Camera.look_at((0.3 * d, 0.4 * d, -d), (0.0, 0.0, 0.0), 50.0)
+    light = AreaLight(position=(0.0, d, 0.0), normal=(0.0, -1.0, 0.0), size=(1.0, 1.0), intensity=10.0)
+    scene = Scene(graph=g, camera=cam, material=Material(albedo=(0.7, 0.7, 0.7)), lights=[light], seed=3)
+    cfg = small_cfg("wavefront", spp=1, spd=1, tile=96)
+    out = render(renderer, scene, cfg)
+    hit = out.depth >= 0
+    assert hit.mean() > 0.05
+    lengths = np.linalg.norm(out.normals[..., :3][hit], axis=-1)
+    assert np.abs(lengths - 1.0).max() < 1e-3
+
+
+def test_rerender_is_bit_identical(renderer):
+    scene = workloads.mandelbox_scene()
+    a = render(renderer, scene, small_cfg("wavefront"))
+    b = render(renderer, scene, small_cfg("wavefront"))
+    np.testing.assert_array_equal(a.accum, b.accum)
+    np.testing.assert_array_equal(a.depth, b.depth)
+    np.testing.assert_array_equal(a.normals, b.normals)
