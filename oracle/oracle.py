@@ -61,6 +61,7 @@ def lib():
         dp = C.POINTER(C.c_double)
         up = C.POINTER(C.c_uint32)
         L.or_de_eval.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, dp, up, up, C.c_int]
+        L.or_de_eval_fast.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, up, C.c_int]
         L.or_primary.restype = C.c_uint64
         L.or_primary.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.sf_camera), C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_double, C.c_double,
@@ -122,6 +123,16 @@ class OracleGraph:
         lib().or_de_eval(self.h, precision, _dp(pts), n, _dp(dist), _dp(traps), _up(iters), _up(mats),
                          threads or default_threads())
         return {"distance": dist, "traps": traps, "iterations": iters, "material": mats}
+
+    def de_fast(self, points, precision=64, threads=None):
+        """The GPU's march sample: skippable Bounded branches outside their margin
+        give their bound with flags = 1 (graph_wgsl.rs:800-814)."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(pts)
+        dist = np.zeros(n)
+        flags = np.zeros(n, dtype=np.uint32)
+        lib().or_de_eval_fast(self.h, precision, _dp(pts), n, _dp(dist), _up(flags), threads or default_threads())
+        return {"distance": dist, "flags": flags}
 
     def primary(self, camera: abi.sf_camera, width, height, max_steps, rule, eps, t_far, tol=1.0,
                 normal_mode=0, precision=64, first=0, count=None, threads=None):

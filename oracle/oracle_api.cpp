@@ -115,6 +115,24 @@ void or_de_eval(void* gp, int precision, const double* xyz, size_t n, double* di
     });
 }
 
+// The GPU's fast sample (de_sample, graph_wgsl.rs:800-814): distance and flags.
+void or_de_eval_fast(void* gp, int precision, const double* xyz, size_t n, double* dist, uint32_t* flags,
+                     int threads) {
+    const Graph& g = *static_cast<Graph*>(gp);
+    parallel_for(n, threads, [&](size_t i) {
+        if (precision == 32) {
+            auto s = evaluate<float>(g, V3<float>(float(xyz[3 * i]), float(xyz[3 * i + 1]), float(xyz[3 * i + 2])),
+                                     true);
+            dist[i] = s.distance;
+            flags[i] = s.flags;
+        } else {
+            auto s = evaluate<double>(g, V3<double>(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]), true);
+            dist[i] = s.distance;
+            flags[i] = s.flags;
+        }
+    });
+}
+
 uint64_t or_primary(void* gp, int precision, const sf_camera* cam, uint32_t w, uint32_t h, uint32_t first,
                     uint32_t count, uint32_t max_steps, int rule, double eps, double t_far, double tol,
                     int normal_mode, double* t_out, uint32_t* steps_out, double* n_out, int threads) {

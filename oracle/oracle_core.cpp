@@ -147,6 +147,29 @@ bool prepare(Graph& g) {
     for (uint32_t id : active_nodes(g)) lip_visit(g, id, g.hint, 0, &l);
     g.lipschitz = l;
     g.step_scale = g.safety / l;
+    // negative_bounds (graph_wgsl.rs:979-1006): a bound reached through an odd
+    // number of Subtraction second inputs is not a lower bound there.
+    std::set<uint32_t> unsafe;
+    std::set<std::pair<uint32_t, bool>> seen;
+    std::vector<std::pair<uint32_t, bool>> work{{g.output, false}};
+    while (!work.empty()) {
+        auto [id, negative] = work.back();
+        work.pop_back();
+        if (!seen.insert({id, negative}).second) continue;
+        const sf_node* n = g.node(id);
+        if (!n) continue;
+        if (negative && (n->kind == SF_NODE_BOUNDED || n->kind == SF_NODE_INSTANCES)) unsafe.insert(id);
+        for (uint32_t port = 0; port < input_count(n->kind); ++port) {
+            uint32_t from;
+            if (g.input_of(id, port, &from))
+                work.push_back({from, negative != (n->enabled && n->kind == SF_NODE_SUBTRACTION && port == 1)});
+        }
+    }
+    g.fast_bounds.clear();
+    for (uint32_t id : g.order) {
+        const sf_node* n = g.node(id);
+        if (n && n->enabled && n->kind == SF_NODE_BOUNDED && !unsafe.count(id)) g.fast_bounds.insert(id);
+    }
     g.ok = true;
     return true;
 }
@@ -465,30 +488,37 @@ template <class R> static DistState<R> combine(const sf_node& n, DistState<R> a,
         r.iter = h >= R(0.5) ? a.iter : b.iter;
         return r;
     };
+    // flags (graph_wgsl.rs:845-852): a union keeps its winner's, the others join both
+    DistState<R> r;
     switch (n.kind) {
-    case SF_NODE_UNION: { DistState<R> r = a.d <= b.d ? a : b; r.d = r_min(a.d, b.d); return r; }
-    case SF_NODE_INTERSECTION: { DistState<R> r = a.d >= b.d ? a : b; r.d = r_max(a.d, b.d); return r; }
-    case SF_NODE_SUBTRACTION: { DistState<R> r = a; r.d = r_max(a.d, -b.d); return r; }
+    case SF_NODE_UNION: { r = a.d <= b.d ? a : b; r.d = r_min(a.d, b.d); return r; }
+    case SF_NODE_INTERSECTION: { r = a.d >= b.d ? a : b; r.d = r_max(a.d, b.d); break; }
+    case SF_NODE_SUBTRACTION: { r = a; r.d = r_max(a.d, -b.d); break; }
     case SF_NODE_SMOOTH_UNION: {
-        if (is_empty(a.d)) return b;
-        if (is_empty(b.d)) return a;
+        if (is_empty(a.d)) { r = b; break; }
+        if (is_empty(b.d)) { r = a; break; }
         R k = R(n.f[0]);
         R h = r_clamp(R(0.5) + R(0.5) * (b.d - a.d) / k, R(0), R(1));
-        return blend(h, b.d + (a.d - b.d) * h - k * h * (R(1) - h));
+        r = blend(h, b.d + (a.d - b.d) * h - k * h * (R(1) - h));
+        break;
     }
     case SF_NODE_SMOOTH_INTERSECTION: {
-        if (is_empty(a.d)) { DistState<R> r = b; r.d = INF; return r; }
-        if (is_empty(b.d)) { DistState<R> r = a; r.d = INF; return r; }
+        if (is_empty(a.d)) { r = b; r.d = INF; break; }
+        if (is_empty(b.d)) { r = a; r.d = INF; break; }
         R k = R(n.f[0]);
         R h = r_clamp(R(0.5) - R(0.5) * (b.d - a.d) / k, R(0), R(1));
-        return blend(h, b.d + (a.d - b.d) * h + k * h * (R(1) - h));
+        r = blend(h, b.d + (a.d - b.d) * h + k * h * (R(1) - h));
+        break;
     }
     default: return a;
     }
+    r.flags = a.flags | b.flags;
+    return r;
 }
 
-// evaluate_raw (eval.rs:671-826) + PreparedGraph::evaluate (eval.rs:98-114).
-template <class R> Sample<R> evaluate(const Graph& g, V3<R> p) {
+// evaluate_raw (eval.rs:671-826) + PreparedGraph::evaluate (eval.rs:98-114); with
+// fast, the GPU's skippable bounds (graph_wgsl.rs:800-814).
+template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
     const R INF = std::numeric_limits<R>::infinity();
     DistState<R> empty{INF, 0, 0, {INF, INF, INF, INF}};
     PointState<R> start{p, R(1), 0, {INF, INF, INF, INF}};
@@ -538,7 +568,11 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p) {
             if (n.enabled) {
                 sf_node box = n;
                 box.kind = SF_NODE_BOX;
-                v.ds.d = r_max(v.ds.d, fence(box, get_point(id, 0)));
+                const R bound = fence(box, get_point(id, 0));
+                if (fast && g.fast_bounds.count(id) && bound > R(n.f[3]))
+                    v.ds = DistState<R>{bound, 0, 0, {INF, INF, INF, INF}, 1};
+                else
+                    v.ds.d = r_max(v.ds.d, bound);
             }
         } else if (!n.enabled) {
             v.point = false;
@@ -558,6 +592,7 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p) {
     for (int i = 0; i < 4; ++i)
         out.traps[i] = r_finite(r.traps[i]) ? r_min(r.traps[i] / R(g.trap_scales[i]), R(1)) : R(1);
     out.iterations = std::min(r.iter, g.iteration_product);
+    out.flags = r.flags;
     return out;
 }
 
@@ -631,16 +666,22 @@ Hit<R> march_segment(const Graph& g, V3<R> ro, V3<R> rd, R safety, R hit_cone, R
     for (uint32_t i = 0; i < max_steps; ++i) {
         if (t >= t_end) return out;
         out.steps = i + 1;
-        Sample<R> s = evaluate(g, ro + rd * t);
+        Sample<R> s = evaluate(g, ro + rd * t, true);
         if (de_evals) ++*de_evals;
         R radius = r_abs(s.distance) * safety;
+        // a bounding box is only a stepping aid: near acceptance, the exact sample
+        if (s.flags != 0 && (absolute_rule ? radius : radius / r_max(t, R(1e-6))) <= accept * R(5)) {
+            s = evaluate(g, ro + rd * t, false);
+            if (de_evals) ++*de_evals;
+            radius = r_abs(s.distance) * safety;
+        }
         bool sor_fail = omega > R(1) && (radius + prev_radius) < step_len * R(1.0001);
         if (sor_fail) { step_len = step_len - omega * step_len; omega = 1; }
         else step_len = radius * omega;
         prev_radius = radius;
         R err = absolute_rule ? radius : radius / r_max(t, R(1e-6));
-        if (!sor_fail && err < cand_err) { cand_t = t; cand = s; cand_err = err; }
-        if (!sor_fail && (absolute_rule ? err <= accept : err < accept)) {
+        if (!sor_fail && s.flags == 0 && err < cand_err) { cand_t = t; cand = s; cand_err = err; }
+        if (!sor_fail && s.flags == 0 && (absolute_rule ? err <= accept : err < accept)) {
             out.hit = true;
             out.t = t;
             out.sample = s;
@@ -662,14 +703,14 @@ Hit<R> march_segment(const Graph& g, V3<R> ro, V3<R> rd, R safety, R hit_cone, R
 template <class R> V3<R> normal_tetra(const Graph& g, V3<R> p, R h) {
     const V3<R> k[4] = {V3<R>(1, -1, -1), V3<R>(-1, -1, 1), V3<R>(-1, 1, -1), V3<R>(1, 1, 1)};
     V3<R> grad(0, 0, 0);
-    for (int i = 0; i < 4; ++i) grad = grad + k[i] * evaluate(g, p + k[i] * h).distance;
+    for (int i = 0; i < 4; ++i) grad = grad + k[i] * evaluate(g, p + k[i] * h, true).distance;
     return normalize(grad);
 }
 // Central difference, 6 taps (the primary-ray configuration's normal).
 template <class R> V3<R> normal_central(const Graph& g, V3<R> p, R h) {
-    V3<R> grad(evaluate(g, p + V3<R>(h, 0, 0)).distance - evaluate(g, p - V3<R>(h, 0, 0)).distance,
-               evaluate(g, p + V3<R>(0, h, 0)).distance - evaluate(g, p - V3<R>(0, h, 0)).distance,
-               evaluate(g, p + V3<R>(0, 0, h)).distance - evaluate(g, p - V3<R>(0, 0, h)).distance);
+    auto de = [&](V3<R> q) { return evaluate(g, q, true).distance; };
+    V3<R> grad(de(p + V3<R>(h, 0, 0)) - de(p - V3<R>(h, 0, 0)), de(p + V3<R>(0, h, 0)) - de(p - V3<R>(0, h, 0)),
+               de(p + V3<R>(0, 0, h)) - de(p - V3<R>(0, 0, h)));
     return normalize(grad);
 }
 
@@ -1084,8 +1125,8 @@ template <class R> Sample<R> planar_sample(const PlanarParams& f, V2<R> input) {
 }
 
 // explicit instantiations
-template Sample<float> evaluate<float>(const Graph&, V3<float>);
-template Sample<double> evaluate<double>(const Graph&, V3<double>);
+template Sample<float> evaluate<float>(const Graph&, V3<float>, bool);
+template Sample<double> evaluate<double>(const Graph&, V3<double>, bool);
 template Scene<float> make_scene<float>(const Graph&, const sf_scene_desc&, const sf_render_config&);
 template Scene<double> make_scene<double>(const Graph&, const sf_scene_desc&, const sf_render_config&);
 template PixelResult radiance<float>(const Graph&, const Scene<float>&, uint32_t, uint32_t, uint32_t);

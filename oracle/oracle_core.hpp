@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <set>
 #include <string>
 #include <vector>
 
@@ -121,6 +122,7 @@ struct Graph {
     float trap_scales[4] = {1, 1, 1, 1};
     uint32_t iteration_product = 1;
     float lipschitz = 1.f, step_scale = 1.f;
+    std::set<uint32_t> fast_bounds;  // Bounded nodes the GPU may skip (graph_wgsl.rs:1019-1031)
 
     const sf_node* node(uint32_t id) const {
         for (auto& n : nodes) if (n.id == id) return &n;
@@ -170,10 +172,13 @@ bool prepare(Graph& g);
 
 // ---------------------------------------------------------------- DE
 template <class R> struct PointState { V3<R> p; R dr; uint32_t iter; R traps[4]; };
-template <class R> struct DistState { R d; uint32_t material; uint32_t iter; R traps[4]; };
-template <class R> struct Sample { R distance; R traps[4]; uint32_t iterations; uint32_t material; };
+template <class R> struct DistState { R d; uint32_t material; uint32_t iter; R traps[4]; uint32_t flags = 0; };
+template <class R> struct Sample { R distance; R traps[4]; uint32_t iterations; uint32_t material; uint32_t flags = 0; };
 
-template <class R> Sample<R> evaluate(const Graph& g, V3<R> p);
+// fast = false: Graph::evaluate (eval.rs), identical to the GPU's de_sample_exact.
+// fast = true: the GPU's de_sample (graph_wgsl.rs:800-814): a skippable Bounded
+// branch outside its margin gives its bound, flagged (flags = 1).
+template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast = false);
 
 // ---------------------------------------------------------------- transport
 template <class R> struct Camera { V3<R> origin, forward, right, up; R tan_half, aspect, lens_radius, focus_distance; };

@@ -23,11 +23,17 @@ __device__ __forceinline__ float3 operator*(float3 a, float s) { return mk3(a.x 
 __device__ __forceinline__ float3 operator*(float3 a, float3 b) { return mk3(a.x * b.x, a.y * b.y, a.z * b.z); }
 __device__ __forceinline__ float3 operator/(float3 a, float s) { return mk3(a.x / s, a.y / s, a.z / s); }
 __device__ __forceinline__ float3 operator/(float3 a, float3 b) { return mk3(a.x / b.x, a.y / b.y, a.z / b.z); }
-__device__ __forceinline__ float dot3(float3 a, float3 b) { return a.x * b.x + a.y * b.y + a.z * b.z; }
+// Sums of products are written as explicit fused multiply-adds: contraction of
+// a*b + c*d may fuse either product, and the choice can differ between the kernels
+// a routine is inlined into. Fixed fusion gives every kernel the same bits.
+__device__ __forceinline__ float dot3(float3 a, float3 b) { return fmaf(a.z, b.z, fmaf(a.x, b.x, a.y * b.y)); }
+__device__ __forceinline__ float diff_of_products(float a, float b, float c, float d) { return fmaf(a, b, -(c * d)); }
+__device__ __forceinline__ float sum_of_products(float a, float b, float c, float d) { return fmaf(a, b, c * d); }
 __device__ __forceinline__ float len3(float3 a) { return sqrtf(dot3(a, a)); }
 __device__ __forceinline__ float3 abs3(float3 a) { return mk3(fabsf(a.x), fabsf(a.y), fabsf(a.z)); }
 __device__ __forceinline__ float3 cross3(float3 a, float3 b) {
-    return mk3(a.y * b.z - a.z * b.y, a.z * b.x - a.x * b.z, a.x * b.y - a.y * b.x);
+    return mk3(diff_of_products(a.y, b.z, a.z, b.y), diff_of_products(a.z, b.x, a.x, b.z),
+               diff_of_products(a.x, b.y, a.y, b.x));
 }
 __device__ __forceinline__ float3 ld3(const float* f) { return mk3(f[0], f[1], f[2]); }
 __device__ __forceinline__ float max3(float3 a) { return fmaxf(fmaxf(a.x, a.y), a.z); }
@@ -54,6 +60,7 @@ struct DeRaw {
     float t0, t1, t2, t3;  // raw trap slots (+inf = unwritten)
     uint32_t iter;
     uint32_t material;
+    uint32_t flags;  // bit 0: d is a skipped Bounded branch's conservative bound (DeSample.flags)
 };
 
 // Normalised sample (PreparedGraph::evaluate, eval.rs:98-114).
@@ -136,7 +143,7 @@ __device__ __forceinline__ float rcp_approx(float x) {
 // class, as the reference's bulb_power68 on the GPU).
 __device__ __forceinline__ void spherical_power(float3 p, float r, uint32_t n, float3& out, float& deriv) {
     if (n == 1) { out = p; deriv = 1.0f; return; }
-    const float rho = sqrt_fast(p.x * p.x + p.y * p.y);
+    const float rho = sqrt_fast(fmaf(p.x, p.x, p.y * p.y));
     const float ir = rcp_approx(r);
     float tx = fminf(fmaxf(p.z * ir, -1.0f), 1.0f), ty = rho * ir;
     float fx = 1.0f, fy = 0.0f;
@@ -146,19 +153,19 @@ __device__ __forceinline__ void spherical_power(float3 p, float r, uint32_t n, f
         fy = p.y * irho;
     }
     if (n == 8 || n == 6) {
-        float t2x = tx * tx - ty * ty, t2y = 2.0f * tx * ty;
-        float f2x = fx * fx - fy * fy, f2y = 2.0f * fx * fy;
-        float t4x = t2x * t2x - t2y * t2y, t4y = 2.0f * t2x * t2y;
-        float f4x = f2x * f2x - f2y * f2y, f4y = 2.0f * f2x * f2y;
+        float t2x = diff_of_products(tx, tx, ty, ty), t2y = 2.0f * tx * ty;
+        float f2x = diff_of_products(fx, fx, fy, fy), f2y = 2.0f * fx * fy;
+        float t4x = diff_of_products(t2x, t2x, t2y, t2y), t4y = 2.0f * t2x * t2y;
+        float f4x = diff_of_products(f2x, f2x, f2y, f2y), f4y = 2.0f * f2x * f2y;
         float r2 = r * r, r4 = r2 * r2;
         float ax, ay, bx, by, prev;
         if (n == 6) {
-            ax = t2x * t4x - t2y * t4y; ay = t2x * t4y + t2y * t4x;
-            bx = f2x * f4x - f2y * f4y; by = f2x * f4y + f2y * f4x;
+            ax = diff_of_products(t2x, t4x, t2y, t4y); ay = sum_of_products(t2x, t4y, t2y, t4x);
+            bx = diff_of_products(f2x, f4x, f2y, f4y); by = sum_of_products(f2x, f4y, f2y, f4x);
             prev = r4 * r;
         } else {
-            ax = t4x * t4x - t4y * t4y; ay = 2.0f * t4x * t4y;
-            bx = f4x * f4x - f4y * f4y; by = 2.0f * f4x * f4y;
+            ax = diff_of_products(t4x, t4x, t4y, t4y); ay = 2.0f * t4x * t4y;
+            bx = diff_of_products(f4x, f4x, f4y, f4y); by = 2.0f * f4x * f4y;
             prev = r4 * r2 * r;
         }
         float m = prev * r;
@@ -170,13 +177,13 @@ __device__ __forceinline__ void spherical_power(float3 p, float r, uint32_t n, f
     uint32_t e = n;
     while (e != 0) {
         if (e & 1u) {
-            float nx = ax * tx - ay * ty, ny = ax * ty + ay * tx; ax = nx; ay = ny;
-            nx = bx * fx - by * fy; ny = bx * fy + by * fx; bx = nx; by = ny;
+            float nx = diff_of_products(ax, tx, ay, ty), ny = sum_of_products(ax, ty, ay, tx); ax = nx; ay = ny;
+            nx = diff_of_products(bx, fx, by, fy); ny = sum_of_products(bx, fy, by, fx); bx = nx; by = ny;
         }
         e >>= 1;
         if (e != 0) {
-            float nx = tx * tx - ty * ty, ny = tx * ty + ty * tx; tx = nx; ty = ny;
-            nx = fx * fx - fy * fy; ny = fx * fy + fy * fx; fx = nx; fy = ny;
+            float nx = diff_of_products(tx, tx, ty, ty), ny = sum_of_products(tx, ty, ty, tx); tx = nx; ty = ny;
+            nx = diff_of_products(fx, fx, fy, fy); ny = sum_of_products(fx, fy, fy, fx); fx = nx; fy = ny;
         }
     }
     float prev = 1.0f;
@@ -221,7 +228,7 @@ __device__ __forceinline__ float box_fence(float3 p, float3 half, float dr) {
 
 __device__ __forceinline__ DeRaw raw_empty() {
     DeRaw r;
-    r.d = SF_INF; r.t0 = r.t1 = r.t2 = r.t3 = SF_INF; r.iter = 0; r.material = 0;
+    r.d = SF_INF; r.t0 = r.t1 = r.t2 = r.t3 = SF_INF; r.iter = 0; r.material = 0; r.flags = 0;
     return r;
 }
 
@@ -509,7 +516,7 @@ static __device__ float fence_op(const DeOp& op, const PState& s) {
 
 __device__ __forceinline__ DeRaw dist_from(const PState& s, float d) {
     DeRaw r;
-    r.d = d; r.material = 0; r.iter = s.iter;
+    r.d = d; r.material = 0; r.iter = s.iter; r.flags = 0;
     r.t0 = s.t0; r.t1 = s.t1; r.t2 = s.t2; r.t3 = s.t3;
     return r;
 }
@@ -530,28 +537,37 @@ static __device__ DeRaw combine_op(uint32_t kind, float k, DeRaw a, DeRaw b) {
         r.iter = h >= 0.5f ? a.iter : b.iter;
         return r;
     };
+    // flags (graph_wgsl.rs:845-852): a union keeps its winner's, the others join both
+    const uint32_t both = a.flags | b.flags;
+    DeRaw r;
     switch (kind) {
-    case SF_NODE_UNION: { DeRaw r = a.d <= b.d ? a : b; r.d = fminf(a.d, b.d); return r; }
-    case SF_NODE_INTERSECTION: { DeRaw r = a.d >= b.d ? a : b; r.d = fmaxf(a.d, b.d); return r; }
-    case SF_NODE_SUBTRACTION: { DeRaw r = a; r.d = fmaxf(a.d, -b.d); return r; }
+    case SF_NODE_UNION: { r = a.d <= b.d ? a : b; r.d = fminf(a.d, b.d); return r; }
+    case SF_NODE_INTERSECTION: { r = a.d >= b.d ? a : b; r.d = fmaxf(a.d, b.d); break; }
+    case SF_NODE_SUBTRACTION: { r = a; r.d = fmaxf(a.d, -b.d); break; }
     case SF_NODE_SMOOTH_UNION: {
-        if (a.d >= 1e30f) return b;
-        if (b.d >= 1e30f) return a;
+        if (a.d >= 1e30f) { r = b; break; }
+        if (b.d >= 1e30f) { r = a; break; }
         float h = fminf(fmaxf(0.5f + 0.5f * (b.d - a.d) / k, 0.0f), 1.0f);
-        return blend(h, b.d + (a.d - b.d) * h - k * h * (1.0f - h));
+        r = blend(h, b.d + (a.d - b.d) * h - k * h * (1.0f - h));
+        break;
     }
     case SF_NODE_SMOOTH_INTERSECTION: {
-        if (a.d >= 1e30f) { DeRaw r = b; r.d = SF_INF; return r; }
-        if (b.d >= 1e30f) { DeRaw r = a; r.d = SF_INF; return r; }
+        if (a.d >= 1e30f) { r = b; r.d = SF_INF; break; }
+        if (b.d >= 1e30f) { r = a; r.d = SF_INF; break; }
         float h = fminf(fmaxf(0.5f - 0.5f * (b.d - a.d) / k, 0.0f), 1.0f);
-        return blend(h, b.d + (a.d - b.d) * h + k * h * (1.0f - h));
+        r = blend(h, b.d + (a.d - b.d) * h + k * h * (1.0f - h));
+        break;
     }
     default: return a;
     }
+    r.flags = both;
+    return r;
 }
 
-// Postfix interpreter over DeProgram.ops (generic graphs).
-static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
+// Postfix interpreter over DeProgram.ops (generic graphs). exact = false is the
+// reference's de_sample (skippable Bounded branches skipped outside their margin,
+// the sample flagged); exact = true is de_sample_exact (every branch evaluated).
+static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bool exact) {
     PState s;
     s.p = c; s.dr = 1.0f; s.iter = 0; s.t0 = s.t1 = s.t2 = s.t3 = SF_INF;
     uint32_t loop_count[SF_MAX_LOOP_DEPTH];
@@ -605,6 +621,27 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c) {
         case SF_OP_BOUND:
             if (sp > 0) stack[sp - 1].d = fmaxf(stack[sp - 1].d, box_fence(s.p, ld3(op.f), s.dr));
             break;
+        case SF_OP_BOUND_FAST: {
+            if (sp >= SF_MAX_DIST_STACK) break;
+            DeRaw b = raw_empty();
+            b.d = box_fence(s.p, ld3(op.f), s.dr);
+            if (!exact && b.d > op.f[3]) {
+                b.flags = 1;
+                stack[sp++] = b;
+                pc = op.b;  // past BOUND_END
+                break;
+            }
+            stack[sp++] = b;
+            break;
+        }
+        case SF_OP_BOUND_END:
+            if (sp >= 2) {
+                DeRaw r = stack[sp - 1];
+                r.d = fmaxf(stack[sp - 2].d, r.d);
+                stack[sp - 2] = r;
+                sp--;
+            }
+            break;
         case SF_OP_COMBINE:
             if (sp >= 2) { stack[sp - 2] = combine_op(op.a, op.f[0], stack[sp - 2], stack[sp - 1]); sp--; }
             break;
@@ -628,6 +665,20 @@ __device__ __forceinline__ DeRaw de_raw(const DeProgram& P, float3 p) {
     case SF_FORM_BULB: return de_bulb(P.fp, p);
     case SF_FORM_BOX: return de_box(P.fp, p);
     case SF_FORM_MENGER: return de_menger(P.fp, p);
-    default: return de_generic(P, p);
+    default: return de_generic(P, p, false);
     }
+}
+// de_sample_exact: the generic program with every Bounded branch evaluated; the
+// specialised forms have no bounds.
+__device__ __forceinline__ DeRaw de_raw_exact(const DeProgram& P, float3 p) {
+    if (P.form != SF_FORM_GENERIC) return de_raw(P, p);
+    return de_generic(P, p, true);
+}
+// The march's sample (pathtrace.wgsl:100-106, lights.wgsl:234): a flagged sample
+// whose radius is within five hit cones of acceptance is replaced by the exact one.
+// absolute selects the fixed-epsilon rule of the primary-ray configuration.
+__device__ __forceinline__ bool needs_exact(const DeRaw& s, float t, float safety, float accept, bool absolute) {
+    if (!s.flags) return false;
+    const float radius = fabsf(s.d) * safety;
+    return absolute ? radius <= accept * 5.0f : radius / fmaxf(t, 1e-6f) <= accept * 5.0f;
 }

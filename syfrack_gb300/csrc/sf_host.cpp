@@ -227,9 +227,27 @@ void lip_visit(const HostGraph& g, uint32_t id, float radius, uint32_t depth, fl
 
 // ------------------------------------------------------------------ lowering
 float sqrt_threshold(float b);
+// negative_bounds (graph_wgsl.rs:976-1006): a lower bound stays safe only through
+// monotone combinations. A Bounded node reached through the second input of an
+// enabled Subtraction (its sign flipped) is evaluated exactly everywhere.
+void negative_bounds(const HostGraph& g, uint32_t id, bool negative, std::set<std::pair<uint32_t, bool>>& seen,
+                     std::set<uint32_t>& unsafe, int guard = 0) {
+    if (guard > 512 || !seen.insert({id, negative}).second) return;
+    const sf_node* n = g.node(id);
+    if (!n) return;
+    if (negative && (n->kind == SF_NODE_BOUNDED || n->kind == SF_NODE_INSTANCES)) unsafe.insert(id);
+    const uint32_t ports = uint32_t(in_ports(n->kind).size());
+    for (uint32_t port = 0; port < ports; ++port) {
+        const bool sign = negative ^ (n->enabled && n->kind == SF_NODE_SUBTRACTION && port == 1);
+        uint32_t src = 0;
+        if (g.input_of(id, port, &src)) negative_bounds(g, src, sign, seen, unsafe, guard + 1);
+    }
+}
+
 struct Lowerer {
     const HostGraph& g;
     DeProgram& P;
+    std::set<uint32_t> unsafe_bounds;
     std::string err;
     int stack_depth = 0, max_stack = 0;
 
@@ -316,6 +334,22 @@ struct Lowerer {
             return push(o);
         }
         if (n.kind == SF_NODE_BOUNDED) {
+            if (n.enabled && !unsafe_bounds.count(src)) {
+                // skippable bound (graph_wgsl.rs:800-814): bound first, detail only near it
+                if (!chain(ha, a)) return false;
+                const uint32_t at = P.n_ops;
+                DeOp o = mk(SF_OP_BOUND_FAST);
+                std::memcpy(o.f, n.f, sizeof o.f);
+                if (!push(o)) return false;
+                stack_depth++;
+                max_stack = std::max(max_stack, stack_depth);
+                if (!dist(hb, b, guard + 1)) return false;
+                if (!push(mk(SF_OP_BOUND_END))) return false;
+                stack_depth--;
+                P.ops[at].b = P.n_ops - 1;
+                P.fast_bounds++;
+                return true;
+            }
             if (!dist(hb, b, guard + 1)) return false;
             if (!n.enabled) return true;
             if (!chain(ha, a)) return false;
@@ -569,10 +603,14 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     P.iteration_product = any ? best : 1;
     float lip = 1.f;
     for (uint32_t id : active_nodes(g)) lip_visit(g, id, g.hint, 0, &lip);
-    Lowerer L{g, P};
+    Lowerer L{g, P, {}};
     const sf_node* out = nullptr;
     for (auto& n : g.nodes)
         if (n.kind == SF_NODE_OUTPUT) out = &n;
+    {
+        std::set<std::pair<uint32_t, bool>> seen;
+        negative_bounds(g, out->id, false, seen, L.unsafe_bounds);
+    }
     uint32_t src = 0;
     bool has = g.input_of(out->id, 0, &src);
     if (!L.dist(has, src)) return fail(L.err.find("not supported") != std::string::npos ? SF_ERR_UNSUPPORTED : SF_ERR_GRAPH, L.err);

@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(256) k_de_probe(const DeProgram* __restrict__ 
     stage_program(P, prog_g);
     __syncthreads();
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        DeSampleF s = de_finalize(P, de_raw(P, mk3(x[i], y[i], z[i])));
+        DeSampleF s = de_finalize(P, de_raw_exact(P, mk3(x[i], y[i], z[i])));
         dist[i] = s.d;
         traps[i] = s.traps[0];
         traps[n + i] = s.traps[1];
@@ -105,6 +105,11 @@ __global__ void __launch_bounds__(256) k_primary(const DeProgram* __restrict__ p
                 evaluated = true;
                 n_eval++;
                 n_iter += s.iter;
+                if (state == LANE_CONT && needs_exact(s, m.t, S.step_scale, accept, absolute)) {
+                    s = de_raw_exact(P, qp);
+                    n_eval++;
+                    n_iter += s.iter;
+                }
             }
             if (state == LANE_NORMAL) {
                 grad = grad + (normal_mode == 0 ? central_offset(tap) : tetra_offset(tap)) * s.d;
@@ -119,7 +124,7 @@ __global__ void __launch_bounds__(256) k_primary(const DeProgram* __restrict__ p
             } else {
                 bool at_budget = !evaluated;
                 if (evaluated) {
-                    r = march_update(m, s.d, S.step_scale, accept, absolute);
+                    r = march_update(m, s.d, s.flags, S.step_scale, accept, absolute);
                     if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept), at_budget = r != MARCH_CONTINUE;
                     if (r == MARCH_HIT && !at_budget) m.cand_t = m.t;
                 }
@@ -208,17 +213,29 @@ static __device__ int march_full(const DeProgram& P, March& m, uint32_t max_step
                                  DeRaw& hit, unsigned long long& evals, unsigned long long& iters) {
     int r = march_check(m, max_steps, accept);
     while (r == MARCH_CONTINUE) {
-        DeRaw s = de_raw(P, m.ro + m.rd * m.t);
+        const float3 q = m.ro + m.rd * m.t;
+        DeRaw s = de_raw(P, q);
         evals++;
         iters += s.iter;
-        r = march_update(m, s.d, safety, accept, false);
+        if (needs_exact(s, m.t, safety, accept, false)) {
+            s = de_raw_exact(P, q);
+            evals++;
+            iters += s.iter;
+        }
+        r = march_update(m, s.d, s.flags, safety, accept, false);
         if (r == MARCH_HIT) { hit = s; m.cand_t = m.t; return r; }
         if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept);
     }
     if (r == MARCH_HIT) {  // candidate accepted at the step budget
-        hit = de_raw(P, m.ro + m.rd * m.cand_t);
+        const float3 q = m.ro + m.rd * m.cand_t;
+        hit = de_raw(P, q);
         evals++;
         iters += hit.iter;
+        if (needs_exact(hit, m.cand_t, safety, accept, false)) {
+            hit = de_raw_exact(P, q);
+            evals++;
+            iters += hit.iter;
+        }
     }
     return r;
 }
@@ -270,7 +287,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                     iters += d.iter;
                     grad = grad + tetra_offset(k) * d.d;
                 }
-                h.n = normalize3(grad);
+                h.n = wnormalize(grad);  // as the trace kernel's taps: one rsqrt
             } else if (r == MARCH_MISS && li != SF_NO_LIGHT) {
                 h.hit = true;
                 h.light_index = li;

@@ -29,7 +29,14 @@ enum {
     SF_OP_TAG = 105,        // a = material index
     SF_OP_BOUND = 106,      // top.d = max(top.d, box(point)); f0..2 = half
     SF_OP_COMBINE = 107,    // a = node kind of the combination, f0 = k
-    SF_OP_END = 108
+    SF_OP_END = 108,
+    // A Bounded node the device may skip (graph_wgsl.rs:800-814): the op follows the
+    // port-0 point chain and computes bound = box(point, f0..2); in fast mode, when
+    // bound > f3 (margin), it pushes {bound, no traps, 0 iterations, material 0,
+    // flags 1} and jumps past the detail branch to b; otherwise it pushes the bound
+    // and the detail branch follows, closed by BOUND_END.
+    SF_OP_BOUND_FAST = 109,
+    SF_OP_BOUND_END = 110   // detail.d = max(bound, detail.d); the detail's payload and flags stay
 };
 
 struct DeOp {
@@ -61,6 +68,7 @@ struct DeProgram {
     uint32_t n_ops;
     uint32_t iteration_product;
     uint32_t max_stack;
+    uint32_t fast_bounds;  // number of BOUND_FAST ops: samples may carry the conservative flag
     float trap_scales[4];
     FormParams fp;
     DeOp ops[SF_MAX_OPS];

@@ -77,8 +77,10 @@ __device__ __forceinline__ int march_check(const March& m, uint32_t max_steps, f
     return MARCH_CONTINUE;
 }
 // After the DE distance d at the current t: MARCH_HIT (hit at m.t), MARCH_MISS
-// (proven clear) or MARCH_CONTINUE (t advanced).
-__device__ __forceinline__ int march_update(March& m, float d, float safety, float accept, bool absolute) {
+// (proven clear) or MARCH_CONTINUE (t advanced). A flagged sample (a skipped
+// Bounded branch's bound) steps the march but is never a hit or a candidate.
+__device__ __forceinline__ int march_update(March& m, float d, uint32_t flags, float safety, float accept,
+                                            bool absolute) {
     m.i += 1;
     float radius = fabsf(d) * safety;
     bool sor_fail = m.omega > 1.0f && (radius + m.prev_radius) < m.step_len * 1.0001f;
@@ -86,8 +88,9 @@ __device__ __forceinline__ int march_update(March& m, float d, float safety, flo
     else m.step_len = radius * m.omega;
     m.prev_radius = radius;
     float err = absolute ? radius : radius * rcp_approx(fmaxf(m.t, 1e-6f));
-    if (!sor_fail && err < m.cand_err) { m.cand_t = m.t; m.cand_err = err; }
-    if (!sor_fail && (absolute ? err <= accept : err < accept)) return MARCH_HIT;
+    const bool exact = flags == 0u;
+    if (!sor_fail && exact && err < m.cand_err) { m.cand_t = m.t; m.cand_err = err; }
+    if (!sor_fail && exact && (absolute ? err <= accept : err < accept)) return MARCH_HIT;
     if (!sor_fail && m.t + m.step_len >= m.t_end) {
         if (radius >= m.t_end - m.t) return MARCH_MISS;
         m.omega = 1.0f;

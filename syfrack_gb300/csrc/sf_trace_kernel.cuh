@@ -176,6 +176,15 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             else s = de_form<FORM>(P, q);
             n_eval++;
             n_iter += s.iter;
+            if constexpr (FORM == SF_FORM_ANY) {
+                // a flagged march or candidate sample near acceptance: the exact sample
+                if (state != TL_NORMAL && needs_exact(s, m.t, safety, accept, false)) {
+                    if constexpr (MULTI) s = de_raw_exact(*Pl, q);
+                    else s = de_raw_exact(P, q);
+                    n_eval++;
+                    n_iter += s.iter;
+                }
+            }
             {
                 // warp-level DE calls and, per call, the iterations the warp ran (its
                 // longest lane) times its active lanes
@@ -190,14 +199,14 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                 grad = grad + tetra_offset(tap) * s.d;
                 if (++tap == 4) {
                     // the taps of a hit end in the launch that found it (no quantum applies)
-                    const float3 n = grad * rsqrtf(dot3(grad, grad));
+                    const float3 n = wnormalize(grad);
                     soa.hit_n[path] = make_float4(n.x, n.y, n.z, __uint_as_float(hit_w));
                     state = TL_IDLE;
                 }
             } else if (state == TL_CAND) {
                 surface_hit(s);
             } else {
-                int r = march_update(m, s.d, safety, accept, false);
+                int r = march_update(m, s.d, s.flags, safety, accept, false);
                 if (r == MARCH_HIT) {
                     if (shadow) finish(MARCH_HIT);
                     else surface_hit(s);

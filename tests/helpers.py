@@ -51,3 +51,28 @@ def _jsonish_to_ron(g):
         n["pos"] = ron.Tuple(None, n["pos"])
     g["links"] = [{"from": ron.Tuple(None, l["from"]), "to": ron.Tuple(None, l["to"])} for l in g["links"]]
     return g
+
+
+def bounded_bulb(subtract=False, margin=0.05):
+    """A Mandelbulb clipped by a Bounded box (half 1.25, the GPU may skip it outside
+    the margin) beside a translated sphere. With subtract, the bounded bulb is the
+    second input of a Subtraction from a large sphere, where its bound is not a lower
+    bound and the GPU evaluates it exactly (graph_wgsl.rs:976-1006)."""
+    from syfrack_gb300.graph import Graph, Kind, Link, Node
+
+    g = Graph.bundled("mandelbulb", power=8.0, iterations=12, bailout=2.0, safety=0.7, hint=2.5)
+    g.links = [l for l in g.links if l.dst != (6, 0)]
+    g.nodes += [
+        Node(7, Kind("Bounded", half=[1.25, 1.25, 1.25], margin=margin)),
+        Node(8, Kind("Translate", offset=[2.2, 0.0, 0.0])),
+        Node(9, Kind("Sphere", radius=0.5)),
+        Node(10, Kind("Union")),
+    ]
+    g.links += [Link((0, 0), (7, 0)), Link((5, 0), (7, 1)), Link((0, 0), (8, 0)), Link((8, 0), (9, 0)),
+                Link((7, 0), (10, 0)), Link((9, 0), (10, 1))]
+    if subtract:
+        g.nodes += [Node(11, Kind("Sphere", radius=4.0)), Node(12, Kind("Subtraction"))]
+        g.links += [Link((0, 0), (11, 0)), Link((11, 0), (12, 0)), Link((10, 0), (12, 1)), Link((12, 0), (6, 0))]
+    else:
+        g.links.append(Link((10, 0), (6, 0)))
+    return g

@@ -44,3 +44,34 @@ def test_primary_tetrahedral_normals_are_unit(renderer):
     assert hit.sum() > 500
     np.testing.assert_allclose(np.linalg.norm(gpu["normal"][hit], axis=1), 1.0, atol=1e-5)
     assert np.all(gpu["normal"][~hit] == 0)
+
+
+@pytest.mark.parametrize("margin", [0.05, 10.0])
+def test_primary_with_skippable_bound(renderer, oracle_mod, margin):
+    """A Bounded branch the GPU skips outside its margin (graph_wgsl.rs:800-814): the
+    march steps by the box bound, re-evaluates exactly within five hit cones
+    (pathtrace.wgsl:100-106) and never accepts a flagged sample. The device follows
+    the f32 oracle's march; margin 10 never skips inside the view."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from helpers import bounded_bulb
+
+    _, cam, w, h, steps, eps, far = workloads.mandelbulb_primary()
+    g = bounded_bulb(margin=margin)
+    w = h = 128
+    gpu = renderer.primary(g, cam, w, h, max_steps=steps, rule="cone", eps=eps, t_far=far, normal="central")
+    og = oracle_mod.OracleGraph(g)
+    ref = og.primary(_camera_desc(cam, w, h), w, h, steps, 0, eps, far, 1.0, 0, precision=32)
+    hit_g, hit_r = gpu["t"] >= 0, ref["t"] >= 0
+    assert (hit_g == hit_r).mean() >= 0.995
+    both = hit_g & hit_r
+    assert both.sum() > 2000
+    assert (np.abs(gpu["t"][both] - ref["t"][both]) <= 1e-4 * ref["t"][both]).mean() >= 0.99
+    ds = np.abs(gpu["steps"].astype(np.int64) - ref["steps"].astype(np.int64))
+    assert (ds == 0).mean() >= 0.95 and (ds <= 2).mean() >= 0.99
+    if margin < 1.0:
+        wide = renderer.primary(bounded_bulb(margin=10.0), cam, w, h, max_steps=steps, rule="cone", eps=eps,
+                                t_far=far, normal="central")
+        # stepping by the bound far from the box takes more (cheaper) steps
+        assert gpu["steps"].sum() > wide["steps"].sum()
+        assert ((gpu["t"] >= 0) == (wide["t"] >= 0)).mean() >= 0.995

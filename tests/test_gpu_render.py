@@ -236,3 +236,35 @@ def test_image_error_at_the_fp32_floor(renderer, oracle_mod):
     print(f"image error vs FP64: device {device:.2e}, f32 oracle {floor:.2e}")
     assert np.median(per_pixel) < 1e-5  # most pixels follow the same paths
     assert device <= 1.5 * floor + 2e-3, (device, floor)
+
+
+@pytest.mark.parametrize("graph", ["bounded", "mandelbulb"])
+def test_skippable_bound_film(renderer, oracle_mod, graph):
+    """A Bounded Mandelbulb beside a sphere (and the plain Mandelbulb close up): the
+    trace kernel and the megakernel both march on the fast sample with the exact
+    re-evaluation near acceptance, and agree with each other and with the f32 oracle."""
+    from helpers import bounded_bulb
+
+    mat = Material(albedo=(0.7, 0.7, 0.7), roughness=0.2, metallic=0.0, specular=0.04)
+    light = AreaLight(position=(0.5, 3.0, -2.5), normal=(-0.5, -3.0, 2.5), size=(1.0, 1.0),
+                      color=(1.0, 1.0, 1.0), intensity=10.0)
+    g = bounded_bulb() if graph == "bounded" else workloads.mandelbulb_primary_graph()
+    scene = Scene(graph=g, camera=Camera.look_at((1.0, 0.8, -3.2), (0.6, 0.0, 0.0), 55.0),
+                  material=mat, lights=[light], seed=99)
+    a = render(renderer, scene, small_cfg("wavefront"))
+    b = render(renderer, scene, small_cfg("megakernel"))
+    # the two integrators run the same arithmetic (fixed fusion), so the films are equal
+    np.testing.assert_array_equal(a.accum, b.accum)
+    np.testing.assert_array_equal(a.depth, b.depth)
+    cfg = small_cfg("wavefront")
+    assert (a.depth >= 0).mean() > 0.2
+    rng = np.random.default_rng(3)
+    pix = np.stack([rng.integers(0, cfg.width, 96), rng.integers(0, cfg.height, 96)], 1).astype(np.uint32)
+    ref = oracle_mod.OracleGraph(scene.graph).render(scene.desc(cfg.width, cfg.height), cfg.desc(), pix, 0,
+                                                     cfg.samples_per_pixel, precision=32)
+    mine = a.accum[pix[:, 1], pix[:, 0], :3] / cfg.samples_per_pixel
+    rmse = float(np.sqrt(np.mean((mine - ref["accum"] / cfg.samples_per_pixel) ** 2)))
+    assert rmse <= 2e-2, rmse
+    hit = ref["depth"] >= 0
+    np.testing.assert_array_equal(a.depth[pix[:, 1], pix[:, 0]] >= 0, hit)
+    np.testing.assert_allclose(a.depth[pix[:, 1], pix[:, 0]][hit], ref["depth"][hit], rtol=1e-3)

@@ -154,3 +154,30 @@ def test_generic_graph_semantics(oracle_mod):
     og = oracle_mod.OracleGraph(Graph(nodes, links))
     r = og.de(np.array([[3.0, 0.0, 0.0]]))
     assert r["distance"][0] == pytest.approx(2.0)
+
+
+def test_bounded_fast_and_exact_samples(oracle_mod):
+    """graph_wgsl.rs:800-814 and :976-1006: outside bound + margin the GPU's march
+    sample is the box bound with flags 1 (never above the exact distance); inside it,
+    or through a Subtraction's second input, the sample is the exact one."""
+    from helpers import bounded_bulb
+
+    pts = lcg_points(4096, 3.0, 5)
+    for subtract in (False, True):
+        og = oracle_mod.OracleGraph(bounded_bulb(subtract))
+        for prec in (32, 64):
+            exact = og.de(pts, precision=prec)
+            fast = og.de_fast(pts, precision=prec)
+            flagged = fast["flags"] != 0
+            np.testing.assert_array_equal(fast["distance"][~flagged], exact["distance"][~flagged])
+            assert np.all(fast["distance"][flagged] <= exact["distance"][flagged] + 1e-6)
+            if subtract:
+                assert not flagged.any()
+            else:
+                assert 0.5 < flagged.mean() < 0.99
+                box = np.abs(pts).max(1)
+                assert np.all(box[flagged] > 1.25)  # only outside the box can a bound be skipped
+    # a wider margin evaluates the detail further out
+    a = oracle_mod.OracleGraph(bounded_bulb(margin=0.05)).de_fast(pts, precision=32)["flags"].mean()
+    b = oracle_mod.OracleGraph(bounded_bulb(margin=1.0)).de_fast(pts, precision=32)["flags"].mean()
+    assert b < a
