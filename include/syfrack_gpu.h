@@ -84,6 +84,8 @@ enum sf_trap_mode { SF_TRAP_MINIMUM = 0, SF_TRAP_MAXIMUM, SF_TRAP_LAST };
  *   Cylinder f0 radius f1 half_height | Box f0..2 half | RoundBox f0..2 half f3 radius
  *   Rock f0..2 half f3 erosion u0 seed | Plane f0..2 normal f3 offset | NormFence f0 inset
  *   MaterialTag u0 index | Bounded f0..2 half f3 margin | SmoothUnion/Intersection f0 k
+ *   Instances f0..2 half f3 margin u0 first placement u1 placement count
+ *     (placements[u0 .. u0+u1] of the descriptor; graph/mod.rs:241-246)
  */
 typedef struct sf_node {
     uint32_t id;
@@ -99,6 +101,14 @@ typedef struct sf_link {           /* Link{from:(node,port), to:(node,port)} */
     uint32_t from_node, from_port, to_node, to_port;
 } sf_link;
 
+/* Placement{position, angles (degrees, glam intrinsic XYZ), scale} (graph/mod.rs:26-30):
+ * one independently transformed copy of an Instances node's template. */
+typedef struct sf_placement {
+    float position[3];
+    float angles[3];
+    float scale[3];
+} sf_placement;
+
 typedef struct sf_graph_desc {
     const sf_node* nodes;
     uint32_t node_count;
@@ -108,6 +118,8 @@ typedef struct sf_graph_desc {
     uint32_t body_id_count;
     float safety;
     float bounding_radius_hint;
+    const sf_placement* placements;/* concatenated Instances placements (may be NULL) */
+    uint32_t placement_count;
 } sf_graph_desc;
 
 /* DeSample (crates/syfrack-core/src/scene/fractal.rs:18-27). */
@@ -145,6 +157,9 @@ sf_status sf_context_memory(sf_context* ctx, uint64_t* used, uint64_t* budget);
 
 /* Validates and lowers a graph. Replaces graph_wgsl::compile (graph_wgsl.rs:949-952)
  * + ParamLayout::pack; the lowered program lives in device memory. */
+/* Graph::validate (scene/graph/validate.rs:146-330) and the derived constants, on the
+ * host only (no context, no device): the checks sf_graph_compile makes before lowering. */
+sf_status sf_graph_validate(const sf_graph_desc* desc, sf_graph_info* out);
 sf_status sf_graph_compile(sf_context* ctx, const sf_graph_desc* desc, sf_graph** out);
 sf_status sf_graph_info_get(const sf_graph* graph, sf_graph_info* out);
 /* Value edits without re-lowering: same topology, new floats (topology_key semantics,

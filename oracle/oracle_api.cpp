@@ -78,6 +78,7 @@ void* or_graph_new(const sf_graph_desc* d) {
     g->nodes.assign(d->nodes, d->nodes + d->node_count);
     g->links.assign(d->links, d->links + d->link_count);
     if (d->body_ids && d->body_id_count) g->body.assign(d->body_ids, d->body_ids + d->body_id_count);
+    if (d->placements && d->placement_count) g->placements.assign(d->placements, d->placements + d->placement_count);
     g->safety = d->safety;
     g->hint = d->bounding_radius_hint;
     if (!prepare(*g)) { delete g; return nullptr; }

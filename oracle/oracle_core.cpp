@@ -122,6 +122,92 @@ static void needed(const Graph& g, uint32_t id, std::set<uint32_t>& set) {
     }
 }
 
+// glam Quat::from_euler(EulerRot::XYZ, a, b, c) = Qx(a) Qy(b) Qz(c) as (x, y, z, w),
+// and Quat * Vec3 (glam's mul_vec3); R = float restates the reference's f32 glam.
+template <class R> struct Q4 { R x, y, z, w; };
+template <class R> static Q4<R> qmul(const Q4<R>& a, const Q4<R>& b) {
+    return {a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y, a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x,
+            a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z};
+}
+template <class R> static Q4<R> quat_xyz(const float deg[3]) {
+    const R k = R(3.14159265358979323846) / R(180);
+    const R a = R(deg[0]) * k, b = R(deg[1]) * k, c = R(deg[2]) * k;
+    Q4<R> qx{r_sin(a * R(0.5)), 0, 0, r_cos(a * R(0.5))};
+    Q4<R> qy{0, r_sin(b * R(0.5)), 0, r_cos(b * R(0.5))};
+    Q4<R> qz{0, 0, r_sin(c * R(0.5)), r_cos(c * R(0.5))};
+    return qmul(qmul(qx, qy), qz);
+}
+template <class R> static V3<R> qrot(const Q4<R>& q, V3<R> v) {
+    V3<R> b(q.x, q.y, q.z);
+    R b2 = b.dot(b);
+    return v * (q.w * q.w - b2) + b * (v.dot(b) * R(2)) + b.cross(v) * (q.w * R(2));
+}
+
+// bvh::build (bvh.rs:26-102), in binary32 as the reference.
+static void bvh_split(std::vector<Graph::InstBounds>& leaves, size_t lo, size_t hi,
+                      std::vector<Graph::InstBounds>& nodes) {
+    float mn[3], mx[3];
+    for (int k = 0; k < 3; ++k) { mn[k] = INFINITY; mx[k] = -INFINITY; }
+    for (size_t i = lo; i < hi; ++i)
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = std::min(mn[k], leaves[i].center[k] - leaves[i].half[k]);
+            mx[k] = std::max(mx[k], leaves[i].center[k] + leaves[i].half[k]);
+        }
+    size_t index = nodes.size();
+    Graph::InstBounds n{};
+    for (int k = 0; k < 3; ++k) {
+        n.center[k] = mn[k] * 0.5f + mx[k] * 0.5f;
+        n.half[k] = std::max(mx[k] - n.center[k], n.center[k] - mn[k]) + 0.002f;
+    }
+    n.placement = -1;
+    nodes.push_back(n);
+    if (hi - lo == 1) {
+        nodes[index].placement = leaves[lo].placement;
+    } else {
+        float e[3] = {mx[0] - mn[0], mx[1] - mn[1], mx[2] - mn[2]};
+        int axis = (e[0] >= e[1] && e[0] >= e[2]) ? 0 : (e[1] >= e[2] ? 1 : 2);
+        size_t middle = lo + (hi - lo) / 2;
+        std::nth_element(leaves.begin() + lo, leaves.begin() + middle, leaves.begin() + hi,
+                         [axis](const Graph::InstBounds& a, const Graph::InstBounds& b) {
+                             if (a.center[axis] != b.center[axis]) return a.center[axis] < b.center[axis];
+                             return a.placement < b.placement;
+                         });
+        bvh_split(leaves, lo, middle, nodes);
+        bvh_split(leaves, middle, hi, nodes);
+    }
+    nodes[index].escape = nodes.size();
+}
+static std::vector<Graph::InstBounds> bvh_build(const sf_placement* pl, uint32_t count, const float* half) {
+    std::vector<Graph::InstBounds> leaves(count), nodes;
+    for (uint32_t i = 0; i < count; ++i) {
+        Q4<float> r = quat_xyz<float>(pl[i].angles);
+        V3<float> ext(0, 0, 0);
+        for (int a = 0; a < 3; ++a) {
+            V3<float> axis(a == 0, a == 1, a == 2);
+            V3<float> c = qrot(r, axis);
+            float h = half[a] * pl[i].scale[a];
+            ext = ext + V3<float>(std::fabs(c.x), std::fabs(c.y), std::fabs(c.z)) * h;
+        }
+        float e[3] = {ext.x, ext.y, ext.z};
+        for (int k = 0; k < 3; ++k) {
+            float pad = (std::fabs(pl[i].position[k]) + e[k]) * (16.0f * 1.1920929e-7f) + 0.002f;
+            leaves[i].center[k] = pl[i].position[k];
+            leaves[i].half[k] = e[k] + pad;
+        }
+        leaves[i].escape = 0;
+        leaves[i].placement = i;
+    }
+    if (count) bvh_split(leaves, 0, count, nodes);
+    return nodes;
+}
+// InstanceBounds::distance (bvh.rs:19-24).
+template <class R> static R inst_bound(const Graph::InstBounds& n, V3<R> p) {
+    V3<R> q(r_abs(p.x - R(n.center[0])) - R(n.half[0]), r_abs(p.y - R(n.center[1])) - R(n.half[1]),
+            r_abs(p.z - R(n.center[2])) - R(n.half[2]));
+    V3<R> m(r_max(q.x, R(0)), r_max(q.y, R(0)), r_max(q.z, R(0)));
+    return m.length() + r_min(r_max(q.x, r_max(q.y, q.z)), R(0));
+}
+
 bool prepare(Graph& g) {
     g.ok = false;
     if (!topo_order(g, g.order)) { g.error = "cycle"; return false; }
@@ -131,6 +217,22 @@ bool prepare(Graph& g) {
     needed(g, g.output, set);
     g.plan.clear();
     for (uint32_t id : g.order) if (set.count(id)) g.plan.push_back(id);
+    g.plans.clear();
+    g.instances.clear();
+    g.plans[g.output] = g.plan;
+    for (auto& n : g.nodes) {
+        if (!n.enabled || n.kind != SF_NODE_INSTANCES) continue;
+        if (size_t(n.u[0]) + n.u[1] > g.placements.size()) { g.error = "placements out of range"; return false; }
+        g.instances[n.id] = bvh_build(g.placements.data() + n.u[0], n.u[1], n.f);
+        uint32_t child;
+        if (g.input_of(n.id, 0, &child) && !g.plans.count(child)) {
+            std::set<uint32_t> sub;
+            needed(g, child, sub);
+            std::vector<uint32_t> plan;
+            for (uint32_t id : g.order) if (sub.count(id)) plan.push_back(id);
+            g.plans[child] = plan;
+        }
+    }
     for (int i = 0; i < 4; ++i) g.trap_scales[i] = 1.f;
     for (uint32_t id : g.order) trap_walk(g, id, 0, g.trap_scales);
     auto owners = body_owners(g);
@@ -168,7 +270,8 @@ bool prepare(Graph& g) {
     g.fast_bounds.clear();
     for (uint32_t id : g.order) {
         const sf_node* n = g.node(id);
-        if (n && n->enabled && n->kind == SF_NODE_BOUNDED && !unsafe.count(id)) g.fast_bounds.insert(id);
+        if (n && n->enabled && (n->kind == SF_NODE_BOUNDED || n->kind == SF_NODE_INSTANCES) && !unsafe.count(id))
+            g.fast_bounds.insert(id);
     }
     g.ok = true;
     return true;
@@ -516,15 +619,85 @@ template <class R> static DistState<R> combine(const sf_node& n, DistState<R> a,
     return r;
 }
 
+template <class R> static DistState<R> eval_raw(const Graph& g, uint32_t target, V3<R> p, bool fast, int depth);
+
+// Instances (eval.rs:749-814): the nearest copy found by the seeded stackless walk
+// over the fence hierarchy; with fast, the GPU's skips (graph_wgsl.rs:760-790): the
+// root fence beyond the margin, and copies whose fence is beyond it.
+template <class R>
+static DistState<R> eval_instances(const Graph& g, const sf_node& n, V3<R> p, bool fast, int depth) {
+    const R INF = std::numeric_limits<R>::infinity();
+    DistState<R> best{INF, 0, 0, {INF, INF, INF, INF}};
+    uint32_t child;
+    if (!g.input_of(n.id, 0, &child) || depth > int(MAX_DEPTH)) return best;
+    const auto& nodes = g.instances.at(n.id);
+    if (nodes.empty()) return best;
+    const bool skip = fast && g.fast_bounds.count(n.id);
+    const R margin = R(n.f[3]);
+    if (skip) {
+        best.d = R(1e30);
+        R env = inst_bound(nodes[0], p);
+        if (env > margin) return DistState<R>{env, 0, 0, {INF, INF, INF, INF}, 1};
+    }
+    size_t chosen = SIZE_MAX, seed = 0;
+    while (nodes[seed].placement < 0) {
+        size_t left = seed + 1, right = nodes[left].escape;
+        seed = inst_bound(nodes[left], p) <= inst_bound(nodes[right], p) ? left : right;
+    }
+    size_t cursor = seed;
+    bool seed_pass = true;
+    while (cursor < nodes.size()) {
+        size_t current = cursor;
+        bool first = seed_pass;
+        seed_pass = false;
+        cursor = first ? 0 : current + 1;
+        const auto& node = nodes[current];
+        if (inst_bound(node, p) > best.d) {
+            if (!first) cursor = node.escape;
+            continue;
+        }
+        if (!first && current == seed) continue;
+        if (node.placement < 0) continue;
+        size_t index = size_t(node.placement);
+        const sf_placement& pl = g.placements[n.u[0] + index];
+        Q4<R> rot = quat_xyz<R>(pl.angles);
+        Q4<R> conj{-rot.x, -rot.y, -rot.z, rot.w};
+        V3<R> sc(R(pl.scale[0]), R(pl.scale[1]), R(pl.scale[2]));
+        V3<R> q = qrot(conj, p - V3<R>(R(pl.position[0]), R(pl.position[1]), R(pl.position[2]))) / sc;
+        R smin = r_min(sc.x, r_min(sc.y, sc.z));
+        // the Box fence of half * scale at q * scale (eval.rs:796-804)
+        V3<R> qs = q * sc;
+        V3<R> e(r_abs(qs.x) - R(n.f[0]) * sc.x, r_abs(qs.y) - R(n.f[1]) * sc.y, r_abs(qs.z) - R(n.f[2]) * sc.z);
+        R bound = V3<R>(r_max(e.x, R(0)), r_max(e.y, R(0)), r_max(e.z, R(0))).length() +
+                  r_min(r_max(e.x, r_max(e.y, e.z)), R(0));
+        if (bound > best.d) continue;
+        DistState<R> d;
+        if (skip && bound > margin) {
+            d = DistState<R>{bound, 0, 0, {INF, INF, INF, INF}, 1};
+        } else {
+            d = eval_raw(g, child, q, fast, depth + 1);
+            d.d = r_max(d.d * smin, bound);
+        }
+        if (d.d < best.d || (d.d == best.d && index < chosen)) {
+            best = d;
+            chosen = index;
+        }
+    }
+    return best;
+}
+
 // evaluate_raw (eval.rs:671-826) + PreparedGraph::evaluate (eval.rs:98-114); with
 // fast, the GPU's skippable bounds (graph_wgsl.rs:800-814).
-template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
+template <class R> static DistState<R> eval_raw(const Graph& g, uint32_t target, V3<R> p, bool fast, int depth) {
     const R INF = std::numeric_limits<R>::infinity();
     DistState<R> empty{INF, 0, 0, {INF, INF, INF, INF}};
     PointState<R> start{p, R(1), 0, {INF, INF, INF, INF}};
     struct Val { bool point; PointState<R> ps; DistState<R> ds; };
+    auto pit = g.plans.find(target);
+    if (pit == g.plans.end()) return empty;
+    const std::vector<uint32_t>& plan = pit->second;
     std::unordered_map<uint32_t, Val> values;
-    values.reserve(g.plan.size() * 2);
+    values.reserve(plan.size() * 2);
     auto get_point = [&](uint32_t id, uint32_t port) {
         uint32_t from;
         if (g.input_of(id, port, &from)) {
@@ -541,7 +714,7 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
         }
         return empty;
     };
-    for (uint32_t id : g.plan) {
+    for (uint32_t id : plan) {
         const sf_node& n = *g.node(id);
         Val v{};
         uint32_t k = n.kind;
@@ -574,6 +747,9 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
                 else
                     v.ds.d = r_max(v.ds.d, bound);
             }
+        } else if (k == SF_NODE_INSTANCES && n.enabled) {
+            v.point = false;
+            v.ds = eval_instances(g, n, p, fast, depth);
         } else if (!n.enabled) {
             v.point = false;
             v.ds = get_dist(id, 0);
@@ -583,9 +759,13 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
         }
         values[id] = v;
     }
-    DistState<R> r = empty;
-    auto it = values.find(g.output);
-    if (it != values.end() && !it->second.point) r = it->second.ds;
+    auto it = values.find(target);
+    if (it != values.end() && !it->second.point) return it->second.ds;
+    return empty;
+}
+
+template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
+    DistState<R> r = eval_raw(g, g.output, p, fast, 0);
     Sample<R> out;
     out.distance = r.d;
     out.material = r.material;

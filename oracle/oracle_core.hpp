@@ -17,6 +17,7 @@
 #include <cstdint>
 #include <cstring>
 #include <limits>
+#include <map>
 #include <set>
 #include <string>
 #include <vector>
@@ -122,7 +123,13 @@ struct Graph {
     float trap_scales[4] = {1, 1, 1, 1};
     uint32_t iteration_product = 1;
     float lipschitz = 1.f, step_scale = 1.f;
-    std::set<uint32_t> fast_bounds;  // Bounded nodes the GPU may skip (graph_wgsl.rs:1019-1031)
+    std::set<uint32_t> fast_bounds;  // Bounded / Instances nodes the GPU may skip (graph_wgsl.rs:1019-1031)
+    std::vector<sf_placement> placements;
+    // Instances: the fence hierarchy per node (bvh.rs), and the evaluation plan of
+    // every target (the output and each enabled Instances node's template).
+    struct InstBounds { float center[3], half[3]; size_t escape; int64_t placement; };
+    std::map<uint32_t, std::vector<InstBounds>> instances;
+    std::map<uint32_t, std::vector<uint32_t>> plans;
 
     const sf_node* node(uint32_t id) const {
         for (auto& n : nodes) if (n.id == id) return &n;

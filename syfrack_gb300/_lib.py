@@ -113,6 +113,7 @@ SIGNATURES = {
     "sf_context_reset_stats": [vp],
     "sf_context_sync": [vp, u32],
     "sf_device_fp32_peak": [vp, P(C.c_double)],
+    "sf_graph_validate": [P(abi.sf_graph_desc), P(abi.sf_graph_info)],
     "sf_graph_compile": [vp, P(abi.sf_graph_desc), P(vp)],
     "sf_graph_info_get": [vp, P(abi.sf_graph_info)],
     "sf_graph_update": [vp, P(abi.sf_graph_desc)],

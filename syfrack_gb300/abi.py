@@ -41,11 +41,16 @@ class sf_link(C.Structure):
                 ("to_node", C.c_uint32), ("to_port", C.c_uint32)]
 
 
+class sf_placement(C.Structure):
+    _fields_ = [("position", C.c_float * 3), ("angles", C.c_float * 3), ("scale", C.c_float * 3)]
+
+
 class sf_graph_desc(C.Structure):
     _fields_ = [("nodes", C.POINTER(sf_node)), ("node_count", C.c_uint32),
                 ("links", C.POINTER(sf_link)), ("link_count", C.c_uint32),
                 ("body_ids", C.POINTER(C.c_uint32)), ("body_id_count", C.c_uint32),
-                ("safety", C.c_float), ("bounding_radius_hint", C.c_float)]
+                ("safety", C.c_float), ("bounding_radius_hint", C.c_float),
+                ("placements", C.POINTER(sf_placement)), ("placement_count", C.c_uint32)]
 
 
 class sf_de_sample(C.Structure):

@@ -44,7 +44,9 @@ def up_to_date() -> bool:
 def _compile(unit: str) -> str:
     src = os.path.join(CSRC, unit)
     obj = os.path.join(BUILD, unit + ".o")
-    flags = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-lineinfo"]
+    # host code rounds every operation (no contraction): the host-derived constants
+    # and instance hierarchies are then the same on x86-64 and aarch64 hosts
+    flags = ["-O3", "-std=c++17", "-Xcompiler", "-fPIC", "-Xcompiler", "-ffp-contract=off", "-lineinfo"]
     if unit.endswith(".cu"):
         flags += ARCH
     cmd = [nvcc(), *flags, "-c", src, "-o", obj]

@@ -564,10 +564,79 @@ static __device__ DeRaw combine_op(uint32_t kind, float k, DeRaw a, DeRaw b) {
     return r;
 }
 
+// ------------------------------------------------------------------ instances
+// box_distance (common.wgsl) without the derivative.
+__device__ __forceinline__ float box_dist(float3 p, float3 half) {
+    const float3 q = abs3(p) - half;
+    const float3 qm = mk3(fmaxf(q.x, 0.f), fmaxf(q.y, 0.f), fmaxf(q.z, 0.f));
+    return sqrt_fast(dot3(qm, qm)) + fminf(max3(q), 0.0f);
+}
+// A hierarchy node's signed box distance (bvh.rs:19-24; WGSL _cluster_bound).
+__device__ __forceinline__ float cluster_bound(const float* nd, float3 p) {
+    return box_dist(p - mk3(__ldg(nd), __ldg(nd + 1), __ldg(nd + 2)), mk3(__ldg(nd + 3), __ldg(nd + 4), __ldg(nd + 5)));
+}
+// The search over one Instances node's copies (graph_wgsl.rs:760-790): seeded at
+// the nearest leaf by a greedy descent, then a stackless preorder walk that skips
+// subtrees whose bound exceeds the best distance; ties go to the lower placement.
+struct InstFrame {
+    const float* rows;  // 12 floats per placement
+    const float* bvh;   // 8 floats per hierarchy node
+    float3 c, half, q;  // the point the node is evaluated at; fence half; current local point
+    float margin, w, fence;
+    uint32_t cursor, seed, end, chosen, j;
+    bool seed_pass, skip;
+    DeRaw best;
+};
+// Next copy whose template must run (its local point in F.q): true; or false when
+// the walk has ended (F.best holds the result). Copies skipped by their fence
+// (fast mode, fence > margin) are folded into F.best here.
+__device__ __forceinline__ bool inst_next(InstFrame& F) {
+    while (F.cursor < F.end) {
+        const uint32_t cur = F.cursor;
+        const bool first = F.seed_pass;
+        F.seed_pass = false;
+        F.cursor = first ? 0u : cur + 1u;
+        const float* nd = F.bvh + size_t(cur) * 8u;
+        if (cluster_bound(nd, F.c) > F.best.d) {
+            if (!first) F.cursor = uint32_t(__ldg(nd + 6));
+            continue;
+        }
+        const float leaf = __ldg(nd + 7);
+        if (leaf < 0.0f || (!first && cur == F.seed)) continue;
+        const uint32_t j = uint32_t(leaf);
+        // the copy's inverse affine rows: local point, per-axis scale and its minimum
+        const float* r = F.rows + size_t(j) * 12u;
+        const float4 x = make_float4(__ldg(r), __ldg(r + 1), __ldg(r + 2), __ldg(r + 3));
+        const float4 y = make_float4(__ldg(r + 4), __ldg(r + 5), __ldg(r + 6), __ldg(r + 7));
+        const float4 z = make_float4(__ldg(r + 8), __ldg(r + 9), __ldg(r + 10), __ldg(r + 11));
+        const float3 q = mk3(dot3(mk3(x.x, x.y, x.z), F.c) + x.w, dot3(mk3(y.x, y.y, y.z), F.c) + y.w,
+                             dot3(mk3(z.x, z.y, z.z), F.c) + z.w);
+        const float3 sc = mk3(rsqrtf(fmaf(x.z, x.z, fmaf(x.x, x.x, x.y * x.y))),
+                              rsqrtf(fmaf(y.z, y.z, fmaf(y.x, y.x, y.y * y.y))),
+                              rsqrtf(fmaf(z.z, z.z, fmaf(z.x, z.x, z.y * z.y))));
+        const float fence = box_dist(q * sc, F.half * sc);
+        if (fence > F.best.d) continue;
+        if (F.skip && fence > F.margin) {
+            DeRaw d = raw_empty();
+            d.d = fence;
+            d.flags = 1;
+            if (d.d < F.best.d || (d.d == F.best.d && j < F.chosen)) { F.best = d; F.chosen = j; }
+            continue;
+        }
+        F.j = j;
+        F.w = min3(sc);
+        F.fence = fence;
+        F.q = q;
+        return true;
+    }
+    return false;
+}
+
 // Postfix interpreter over DeProgram.ops (generic graphs). exact = false is the
 // reference's de_sample (skippable Bounded branches skipped outside their margin,
 // the sample flagged); exact = true is de_sample_exact (every branch evaluated).
 static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bool exact) {
+    InstFrame F;  // the copy search in flight (one level: templates hold no Instances)
     PState s;
     s.p = c; s.dr = 1.0f; s.iter = 0; s.t0 = s.t1 = s.t2 = s.t3 = SF_INF;
     uint32_t loop_count[SF_MAX_LOOP_DEPTH];
@@ -632,6 +701,56 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
                 break;
             }
             stack[sp++] = b;
+            break;
+        }
+        case SF_OP_INST_BEGIN: {
+            if (sp >= SF_MAX_DIST_STACK) { pc = op.b; break; }
+            const float* base = reinterpret_cast<const float*>(P.inst_data) + op.c;
+            F.rows = base;
+            F.bvh = base + size_t(op.a) * 12u;
+            F.c = c;
+            F.half = ld3(op.f);
+            F.margin = op.f[3];
+            F.skip = op.f[4] != 0.0f && !exact;
+            F.end = 2u * op.a - 1u;
+            if (F.skip) {
+                // empty space needs only the root fence (graph_wgsl.rs:769-771)
+                const float env = cluster_bound(F.bvh, c);
+                if (env > F.margin) {
+                    DeRaw e = raw_empty();
+                    e.d = env;
+                    e.flags = 1;
+                    stack[sp++] = e;
+                    pc = op.b;
+                    break;
+                }
+            }
+            uint32_t seed = 0;
+            while (seed + 1u < F.end && __ldg(F.bvh + size_t(seed) * 8u + 7u) < 0.0f) {
+                const uint32_t left = seed + 1u, right = uint32_t(__ldg(F.bvh + size_t(left) * 8u + 6u));
+                seed = (right >= F.end || cluster_bound(F.bvh + size_t(left) * 8u, c) <=
+                                              cluster_bound(F.bvh + size_t(right) * 8u, c))
+                           ? left
+                           : right;
+            }
+            F.seed = F.cursor = seed;
+            F.seed_pass = true;
+            F.chosen = op.a;
+            F.best = raw_empty();
+            F.best.d = 1e30f;
+            if (inst_next(F)) { c = F.q; break; }  // the template follows with the copy's point
+            stack[sp++] = F.best;
+            pc = op.b;
+            break;
+        }
+        case SF_OP_INST_END: {
+            if (sp < 1) break;
+            DeRaw d = stack[--sp];
+            d.d = fmaxf(d.d * F.w, F.fence);
+            if (d.d < F.best.d || (d.d == F.best.d && F.j < F.chosen)) { F.best = d; F.chosen = F.j; }
+            if (inst_next(F)) { c = F.q; pc = op.a; break; }  // next copy: the template again
+            c = F.c;
+            stack[sp++] = F.best;
             break;
         }
         case SF_OP_BOUND_END:

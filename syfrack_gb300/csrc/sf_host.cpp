@@ -12,6 +12,7 @@
 #include <cstdio>
 #include <cstring>
 #include <fstream>
+#include <cfloat>
 #include <functional>
 #include <map>
 #include <memory>
@@ -45,6 +46,8 @@ sf_status cuda_fail(cudaError_t e, const char* what) {
 }
 
 constexpr uint32_t MAX_DEPTH = 3;          // graph/mod.rs:41
+constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
+constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
 constexpr uint32_t ABI_VERSION = (1u << 16) | 0u;
 
 // ------------------------------------------------------------------ graph preparation
@@ -108,6 +111,21 @@ std::string validate(const HostGraph& g) {
         if (n.kind == SF_NODE_SCALE && std::fabs(n.f[0]) < 1e-3f) return "Scale factor cannot be zero";
         if (n.kind == SF_NODE_ITERATE && size_t(n.body_offset) + n.body_len > g.body.size())
             return "Iterate body out of range on node " + std::to_string(n.id);
+        if (n.kind == SF_NODE_INSTANCES) {
+            // validate.rs:198-207 and the placement bounds of graph/mod.rs:557-584
+            const std::string at = " on node " + std::to_string(n.id);
+            if (n.u[1] == 0 || n.u[1] > MAX_PLACEMENTS) return "Instances: between 1 and 16384 placements" + at;
+            if (size_t(n.u[0]) + n.u[1] > g.placements.size()) return "Instances placements out of range" + at;
+            if (!(n.f[3] >= 0.001f && n.f[3] <= 10.0f)) return "Instances margin out of [0.001, 10]" + at;
+            for (uint32_t i = 0; i < n.u[1]; ++i) {
+                const sf_placement& pl = g.placements[n.u[0] + i];
+                for (int k = 0; k < 3; ++k) {
+                    if (!(std::fabs(pl.position[k]) <= 1000.0f)) return "placement position out of [-1000, 1000]" + at;
+                    if (!(std::fabs(pl.angles[k]) <= 180.0f)) return "placement angle out of [-180, 180]" + at;
+                    if (!(pl.scale[k] >= 0.05f && pl.scale[k] <= 20.0f)) return "placement scale out of [0.05, 20]" + at;
+                }
+            }
+        }
     }
     if (inputs != 1) return "the graph must have exactly one Input";
     if (outputs != 1) return "the graph must have exactly one Output";
@@ -225,6 +243,104 @@ void lip_visit(const HostGraph& g, uint32_t id, float radius, uint32_t depth, fl
     for (uint32_t b : g.body_of(*n)) lip_visit(g, b, radius, depth + 1, l);
 }
 
+// ------------------------------------------------------------------ instances
+// Rotation of glam's Quat::from_euler(EulerRot::XYZ, a, b, c) = Qx(a) Qy(b) Qz(c),
+// kept as a unit quaternion (x, y, z, w) and applied with glam's mul_vec3 formula.
+struct Quat4 { float x, y, z, w; };
+Quat4 quat_mul(const Quat4& a, const Quat4& b) {
+    return {a.w * b.x + a.x * b.w + a.y * b.z - a.z * b.y, a.w * b.y - a.x * b.z + a.y * b.w + a.z * b.x,
+            a.w * b.z + a.x * b.y - a.y * b.x + a.z * b.w, a.w * b.w - a.x * b.x - a.y * b.y - a.z * b.z};
+}
+Quat4 quat_euler_xyz(const float deg[3]) {
+    const float k = 3.14159265358979323846f / 180.0f;
+    const float a = deg[0] * k, b = deg[1] * k, c = deg[2] * k;
+    Quat4 qx{std::sin(a * 0.5f), 0.f, 0.f, std::cos(a * 0.5f)};
+    Quat4 qy{0.f, std::sin(b * 0.5f), 0.f, std::cos(b * 0.5f)};
+    Quat4 qz{0.f, 0.f, std::sin(c * 0.5f), std::cos(c * 0.5f)};
+    return quat_mul(quat_mul(qx, qy), qz);
+}
+void quat_rotate(const Quat4& q, const float v[3], float out[3]) {
+    const float b2 = q.x * q.x + q.y * q.y + q.z * q.z;
+    const float vb = v[0] * q.x + v[1] * q.y + v[2] * q.z;
+    const float cr[3] = {q.y * v[2] - q.z * v[1], q.z * v[0] - q.x * v[2], q.x * v[1] - q.y * v[0]};
+    const float bq[3] = {q.x, q.y, q.z};
+    for (int i = 0; i < 3; ++i) out[i] = v[i] * (q.w * q.w - b2) + bq[i] * (vb * 2.0f) + cr[i] * (q.w * 2.0f);
+}
+
+// The copies' fence hierarchy (bvh.rs:26-102): leaves bound each rotated, scaled
+// fence box (padded for roundoff); interior nodes split at the median of the
+// longest axis, ties by placement index; preorder layout with escape indices.
+struct InstNode { float center[3], half[3]; uint32_t escape; int32_t placement; };
+void inst_split(std::vector<InstNode>& leaves, size_t lo, size_t hi, std::vector<InstNode>& nodes) {
+    float mn[3], mx[3];
+    for (int k = 0; k < 3; ++k) { mn[k] = INFINITY; mx[k] = -INFINITY; }
+    for (size_t i = lo; i < hi; ++i)
+        for (int k = 0; k < 3; ++k) {
+            mn[k] = std::min(mn[k], leaves[i].center[k] - leaves[i].half[k]);
+            mx[k] = std::max(mx[k], leaves[i].center[k] + leaves[i].half[k]);
+        }
+    const size_t index = nodes.size();
+    InstNode n{};
+    for (int k = 0; k < 3; ++k) {
+        n.center[k] = mn[k] * 0.5f + mx[k] * 0.5f;
+        n.half[k] = std::max(mx[k] - n.center[k], n.center[k] - mn[k]) + 0.002f;
+    }
+    n.placement = -1;
+    nodes.push_back(n);
+    if (hi - lo == 1) {
+        nodes[index].placement = leaves[lo].placement;
+    } else {
+        const float ex = mx[0] - mn[0], ey = mx[1] - mn[1], ez = mx[2] - mn[2];
+        const int axis = (ex >= ey && ex >= ez) ? 0 : (ey >= ez ? 1 : 2);
+        const size_t middle = lo + (hi - lo) / 2;
+        std::nth_element(leaves.begin() + lo, leaves.begin() + middle, leaves.begin() + hi,
+                         [axis](const InstNode& a, const InstNode& b) {
+                             if (a.center[axis] != b.center[axis]) return a.center[axis] < b.center[axis];
+                             return a.placement < b.placement;
+                         });
+        inst_split(leaves, lo, middle, nodes);
+        inst_split(leaves, middle, hi, nodes);
+    }
+    nodes[index].escape = uint32_t(nodes.size());
+}
+// Appends one Instances node's device block: per placement the inverse affine rows
+// (graph_wgsl.rs:140-152: row_i = (R e_i) / scale_i, w = -row_i . position), then the
+// hierarchy nodes as 8 floats (centre, half, escape, placement or -1).
+void pack_instances(const sf_placement* pl, uint32_t count, const float half[3], std::vector<float>& out) {
+    std::vector<InstNode> leaves(count);
+    for (uint32_t i = 0; i < count; ++i) {
+        const Quat4 r = quat_euler_xyz(pl[i].angles);
+        float ext[3] = {0.f, 0.f, 0.f};
+        for (int a = 0; a < 3; ++a) {
+            const float e[3] = {a == 0 ? 1.f : 0.f, a == 1 ? 1.f : 0.f, a == 2 ? 1.f : 0.f};
+            float col[3];
+            quat_rotate(r, e, col);
+            const float h = half[a] * pl[i].scale[a];
+            for (int k = 0; k < 3; ++k) ext[k] += std::fabs(col[k]) * h;
+            float row[4];
+            for (int k = 0; k < 3; ++k) row[k] = col[k] / pl[i].scale[a];
+            row[3] = -(row[0] * pl[i].position[0] + row[1] * pl[i].position[1] + row[2] * pl[i].position[2]);
+            out.insert(out.end(), row, row + 4);
+        }
+        InstNode& n = leaves[i];
+        for (int k = 0; k < 3; ++k) {
+            const float pad = (std::fabs(pl[i].position[k]) + ext[k]) * (16.0f * FLT_EPSILON) + 0.002f;
+            n.center[k] = pl[i].position[k];
+            n.half[k] = ext[k] + pad;
+        }
+        n.escape = 0;
+        n.placement = int32_t(i);
+    }
+    std::vector<InstNode> nodes;
+    nodes.reserve(2 * size_t(count) - 1);
+    inst_split(leaves, 0, leaves.size(), nodes);
+    for (const InstNode& n : nodes) {
+        const float v[8] = {n.center[0], n.center[1], n.center[2], n.half[0], n.half[1], n.half[2],
+                            float(n.escape), float(n.placement)};
+        out.insert(out.end(), v, v + 8);
+    }
+}
+
 // ------------------------------------------------------------------ lowering
 float sqrt_threshold(float b);
 // negative_bounds (graph_wgsl.rs:976-1006): a lower bound stays safe only through
@@ -248,8 +364,10 @@ struct Lowerer {
     const HostGraph& g;
     DeProgram& P;
     std::set<uint32_t> unsafe_bounds;
+    std::vector<float>* inst = nullptr;
     std::string err;
     int stack_depth = 0, max_stack = 0;
+    bool in_template = false;
 
     bool push(const DeOp& op) {
         if (P.n_ops >= SF_MAX_OPS) { err = "graph too large for the device program"; return false; }
@@ -357,7 +475,32 @@ struct Lowerer {
             std::memcpy(o.f, n.f, sizeof o.f);
             return push(o);
         }
-        if (n.kind == SF_NODE_INSTANCES) { err = "Instances nodes are not supported on the device"; return false; }
+        if (n.kind == SF_NODE_INSTANCES) {
+            if (!n.enabled) return dist(ha, a, guard + 1);  // passes its template through (eval.rs:816)
+            if (in_template) { err = "Instances nested in an Instances template are not supported on the device"; return false; }
+            if (!ha) {  // no template: the copies are empty (eval.rs:752-755)
+                stack_depth++;
+                max_stack = std::max(max_stack, stack_depth);
+                return push(mk(SF_OP_EMPTY));
+            }
+            const uint32_t at = P.n_ops;
+            DeOp o = mk(SF_OP_INST_BEGIN);
+            o.a = n.u[1];
+            o.c = uint32_t(inst->size());
+            std::memcpy(o.f, n.f, 4 * sizeof(float));
+            o.f[4] = unsafe_bounds.count(src) ? 0.f : 1.f;
+            pack_instances(g.placements.data() + n.u[0], n.u[1], n.f, *inst);
+            if (!push(o)) return false;
+            in_template = true;
+            const bool ok = dist(ha, a, guard + 1);
+            in_template = false;
+            if (!ok) return false;
+            DeOp e = mk(SF_OP_INST_END);
+            e.a = at;
+            if (!push(e)) return false;
+            P.ops[at].b = P.n_ops - 1;
+            return true;
+        }
         if (is_combine_kind(n.kind)) {
             if (!dist(ha, a, guard + 1)) return false;
             if (!n.enabled) return true;  // disabled: port 0 passes through (eval.rs:822)
@@ -575,18 +718,61 @@ std::string topology_of(const HostGraph& g) {
     return s;
 }
 
-sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_graph_info& info) {
+// Copies budget (validate.rs:340-372): along any path, at most 3 enabled Instances
+// and at most 65,536 copies in product.
+bool copies_budget(const HostGraph& g, uint32_t id, std::map<uint32_t, std::pair<uint32_t, uint64_t>>& memo,
+                   std::pair<uint32_t, uint64_t>& out, int guard = 0) {
+    auto it = memo.find(id);
+    if (it != memo.end()) { out = it->second; return true; }
+    if (guard > 512) return false;
+    const sf_node* n = g.node(id);
+    std::pair<uint32_t, uint64_t> b{0, 1};
+    if (n) {
+        const uint32_t ports = uint32_t(in_ports(n->kind).size());
+        for (uint32_t port = 0; port < ports; ++port) {
+            uint32_t src = 0;
+            if (!g.input_of(id, port, &src)) continue;
+            std::pair<uint32_t, uint64_t> c;
+            if (!copies_budget(g, src, memo, c, guard + 1)) return false;
+            b.first = std::max(b.first, c.first);
+            b.second = std::max(b.second, c.second);
+        }
+        if (n->kind == SF_NODE_INSTANCES && n->enabled) {
+            b.first += 1;
+            b.second = std::min<uint64_t>(b.second * n->u[1], 0xffffffffull);
+        }
+    }
+    memo[id] = b;
+    out = b;
+    return true;
+}
+
+sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_graph_info& info,
+                      std::vector<float>& inst) {
     if (!d || (!d->nodes && d->node_count)) return fail(SF_ERR_INVALID, "null graph descriptor");
     g.nodes.assign(d->nodes, d->nodes + d->node_count);
     g.links.assign(d->links ? d->links : nullptr, d->links ? d->links + d->link_count : nullptr);
     g.body.assign(d->body_ids ? d->body_ids : nullptr, d->body_ids ? d->body_ids + d->body_id_count : nullptr);
+    g.placements.assign(d->placements ? d->placements : nullptr,
+                        d->placements ? d->placements + d->placement_count : nullptr);
     g.safety = d->safety;
     g.hint = d->bounding_radius_hint;
     std::string e = validate(g);
     if (!e.empty()) return fail(SF_ERR_GRAPH, e);
     std::vector<uint32_t> order;
     if (!topo_order(g, order)) return fail(SF_ERR_GRAPH, "cycle in the graph");
+    {
+        std::map<uint32_t, std::pair<uint32_t, uint64_t>> memo;
+        for (auto& n : g.nodes) {
+            std::pair<uint32_t, uint64_t> b;
+            if (!copies_budget(g, n.id, memo, b)) return fail(SF_ERR_GRAPH, "graph too deep");
+            if (b.first > MAX_DEPTH || b.second > MAX_INSTANCE_PRODUCT)
+                return fail(SF_ERR_GRAPH, "nested Instances: at most 3 levels and 65536 copies on node " +
+                                              std::to_string(n.id));
+        }
+    }
     std::memset(&P, 0, sizeof P);
+    inst.clear();
     for (int i = 0; i < 4; ++i) P.trap_scales[i] = 1.f;
     for (uint32_t id : order) trap_walk(g, id, 0, P.trap_scales);
     std::set<uint32_t> owned;
@@ -603,7 +789,7 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     P.iteration_product = any ? best : 1;
     float lip = 1.f;
     for (uint32_t id : active_nodes(g)) lip_visit(g, id, g.hint, 0, &lip);
-    Lowerer L{g, P, {}};
+    Lowerer L{g, P, {}, &inst};
     const sf_node* out = nullptr;
     for (auto& n : g.nodes)
         if (n.kind == SF_NODE_OUTPUT) out = &n;
@@ -616,6 +802,7 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     if (!L.dist(has, src)) return fail(L.err.find("not supported") != std::string::npos ? SF_ERR_UNSUPPORTED : SF_ERR_GRAPH, L.err);
     if (L.max_stack > SF_MAX_DIST_STACK) return fail(SF_ERR_UNSUPPORTED, "distance tree wider than the device stack");
     P.max_stack = L.max_stack;
+    P.inst_floats = uint32_t(inst.size());
     detect_form(g, P);
     std::memset(&info, 0, sizeof info);
     info.step_scale = g.safety / lip;
@@ -799,23 +986,48 @@ extern "C" sf_status sf_context_sync(sf_context* c, uint32_t timeout_ms) {
 }
 
 // ------------------------------------------------------------------ ABI: graph
+extern "C" sf_status sf_graph_validate(const sf_graph_desc* d, sf_graph_info* out) {
+    HostGraph h;
+    DeProgram P;
+    sf_graph_info info;
+    std::vector<float> inst;
+    sf_status s = build_graph(d, h, P, info, inst);
+    if (s == SF_OK && out) *out = info;
+    return s;
+}
 extern "C" sf_status sf_graph_compile(sf_context* c, const sf_graph_desc* d, sf_graph** out) {
     if (!c || !out) return fail(SF_ERR_INVALID, "null argument");
     *out = nullptr;
     auto* g = new sf_graph();
     g->ctx = c;
-    sf_status s = build_graph(d, g->host, g->prog, g->info);
+    std::vector<float> inst;
+    sf_status s = build_graph(d, g->host, g->prog, g->info, inst);
     if (s != SF_OK) { delete g; return s; }
     g->topology = topology_of(g->host);
     cudaSetDevice(c->device);
     void* p = nullptr;
+    if (!inst.empty()) {
+        g->inst_bytes = inst.size() * sizeof(float);
+        s = ctx_alloc(c, g->inst_bytes, &p);
+        if (s != SF_OK) { delete g; return s; }
+        g->d_inst = static_cast<float*>(p);
+        g->prog.inst_data = reinterpret_cast<uint64_t>(g->d_inst);
+    }
     s = ctx_alloc(c, sizeof(DeProgram), &p);
-    if (s != SF_OK) { delete g; return s; }
+    if (s != SF_OK) {
+        if (g->d_inst) ctx_free(c, g->d_inst, g->inst_bytes);
+        delete g;
+        return s;
+    }
     g->d_prog = static_cast<DeProgram*>(p);
-    cudaError_t e = cudaMemcpyAsync(g->d_prog, &g->prog, sizeof(DeProgram), cudaMemcpyHostToDevice, c->stream);
+    cudaError_t e = cudaSuccess;
+    if (g->d_inst) e = cudaMemcpyAsync(g->d_inst, inst.data(), g->inst_bytes, cudaMemcpyHostToDevice, c->stream);
+    if (e == cudaSuccess)
+        e = cudaMemcpyAsync(g->d_prog, &g->prog, sizeof(DeProgram), cudaMemcpyHostToDevice, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
     if (e != cudaSuccess) {
         ctx_free(c, g->d_prog, sizeof(DeProgram));
+        if (g->d_inst) ctx_free(c, g->d_inst, g->inst_bytes);
         delete g;
         return cuda_fail(e, "graph upload");
     }
@@ -833,10 +1045,15 @@ extern "C" sf_status sf_graph_update(sf_graph* g, const sf_graph_desc* d) {
     HostGraph h;
     DeProgram P;
     sf_graph_info info;
-    sf_status s = build_graph(d, h, P, info);
+    std::vector<float> inst;
+    sf_status s = build_graph(d, h, P, info, inst);
     if (s != SF_OK) return s;
-    if (topology_of(h) != g->topology) return fail(SF_ERR_GRAPH, "topology changed: compile a new graph");
+    if (topology_of(h) != g->topology || inst.size() * sizeof(float) != g->inst_bytes)
+        return fail(SF_ERR_GRAPH, "topology changed: compile a new graph");
+    P.inst_data = reinterpret_cast<uint64_t>(g->d_inst);
     cudaSetDevice(g->ctx->device);
+    CU(cudaStreamSynchronize(g->ctx->stream));  // no launch may read the blocks being replaced
+    if (g->d_inst) CU(cudaMemcpyAsync(g->d_inst, inst.data(), g->inst_bytes, cudaMemcpyHostToDevice, g->ctx->stream));
     CU(cudaMemcpyAsync(g->d_prog, &P, sizeof P, cudaMemcpyHostToDevice, g->ctx->stream));
     CU(cudaStreamSynchronize(g->ctx->stream));
     g->host = h;
@@ -860,6 +1077,7 @@ extern "C" sf_status sf_graph_destroy(sf_graph* g) {
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
     ctx_free(c, g->d_prog, sizeof(DeProgram));
+    if (g->d_inst) ctx_free(c, g->d_inst, g->inst_bytes);
     delete g;
     ctx_release(c);
     return SF_OK;
@@ -1396,7 +1614,7 @@ struct Reader {
 };
 
 const uint32_t CK_MAGIC = 0x4b434653u;  // "SFCK"
-const uint32_t CK_VERSION = 1;
+const uint32_t CK_VERSION = 2;
 
 std::string producer_of(const sf_context* c) {
     return c->device_name + "|sm_" + std::to_string(c->cc_major) + std::to_string(c->cc_minor) + "|abi " +
@@ -1447,6 +1665,7 @@ extern "C" sf_status sf_session_save(sf_session* s, const char* dir) {
     w.put_str(s->graph->topology);
     w.put(uint32_t(s->graph->host.nodes.size()));
     w.put_bytes(s->graph->host.nodes.data(), s->graph->host.nodes.size() * sizeof(sf_node));
+    w.put(fnv1a(s->graph->host.placements.data(), s->graph->host.placements.size() * sizeof(sf_placement)));
     w.put(s->dispatches);
     w.put(s->tile_size);
     w.put(uint32_t(s->tiles.size()));
@@ -1498,6 +1717,7 @@ extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* d
     std::vector<sf_node> nodes(nn);
     if (nn > 4096) return fail(SF_ERR_CHECKPOINT, "checkpoint graph too large");
     r.get_bytes(nodes.data(), nn * sizeof(sf_node));
+    const uint64_t placements_hash = r.get<uint64_t>();
     uint32_t dispatches = r.get<uint32_t>();
     uint32_t tile_size = r.get<uint32_t>();
     uint32_t nt = r.get<uint32_t>();
@@ -1510,7 +1730,8 @@ extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* d
     if (film_bytes != filmb.size() || fnv1a(filmb.data(), filmb.size()) != film_hash)
         return fail(SF_ERR_CHECKPOINT, "checkpoint film hash mismatch");
     if (topo != g->topology || nn != g->host.nodes.size() ||
-        std::memcmp(nodes.data(), g->host.nodes.data(), nn * sizeof(sf_node)) != 0)
+        std::memcmp(nodes.data(), g->host.nodes.data(), nn * sizeof(sf_node)) != 0 ||
+        placements_hash != fnv1a(g->host.placements.data(), g->host.placements.size() * sizeof(sf_placement)))
         return fail(SF_ERR_CHECKPOINT, "checkpoint was made with another graph");
     size_t px = size_t(cfg.width) * cfg.height;
     if (filmb.size() != px * 36) return fail(SF_ERR_CHECKPOINT, "checkpoint film size mismatch");

@@ -30,6 +30,7 @@ struct HostGraph {
     std::vector<sf_node> nodes;
     std::vector<sf_link> links;
     std::vector<uint32_t> body;
+    std::vector<sf_placement> placements;
     float safety = 1.f, hint = 1.f;
 
     const sf_node* node(uint32_t id) const {
@@ -79,6 +80,8 @@ struct sf_graph {
     sfh::HostGraph host;
     DeProgram prog;
     DeProgram* d_prog = nullptr;
+    float* d_inst = nullptr;  // Instances blocks (DeProgram.inst_data)
+    size_t inst_bytes = 0;
     sf_graph_info info;
     std::string topology;
 };

@@ -36,7 +36,14 @@ enum {
     // flags 1} and jumps past the detail branch to b; otherwise it pushes the bound
     // and the detail branch follows, closed by BOUND_END.
     SF_OP_BOUND_FAST = 109,
-    SF_OP_BOUND_END = 110   // detail.d = max(bound, detail.d); the detail's payload and flags stay
+    SF_OP_BOUND_END = 110,  // detail.d = max(bound, detail.d); the detail's payload and flags stay
+    // Instances (graph_wgsl.rs:744-790): a = placement count, b = index of INST_END,
+    // c = offset of the node's block in inst_data (12 floats of inverse affine rows per
+    // placement, then 8 floats per hierarchy node: centre, half, escape, placement or -1),
+    // f0..2 = half, f3 = margin, f4 = 1 when the copies may be skipped (fast). The ops
+    // between INST_BEGIN and INST_END evaluate the template at a copy's local point.
+    SF_OP_INST_BEGIN = 111,
+    SF_OP_INST_END = 112    // a = index of the matching INST_BEGIN
 };
 
 struct DeOp {
@@ -69,6 +76,8 @@ struct DeProgram {
     uint32_t iteration_product;
     uint32_t max_stack;
     uint32_t fast_bounds;  // number of BOUND_FAST ops: samples may carry the conservative flag
+    uint32_t inst_floats;  // length of inst_data
+    uint64_t inst_data;    // device address of the Instances blocks (const float*), 0 when none
     float trap_scales[4];
     FormParams fp;
     DeOp ops[SF_MAX_OPS];

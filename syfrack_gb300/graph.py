@@ -50,7 +50,7 @@ class Link:
 
 
 def _v3(x):
-    return [float(a) for a in x]
+    return ron.vec(x)
 
 
 # (float slots, uint slots) per kind, following the table in include/syfrack_gpu.h.
@@ -130,7 +130,7 @@ def _pack_params(k: Kind):
         f[0] = d["inset"]
     elif n == "MaterialTag":
         u[0] = int(d["index"])
-    elif n == "Bounded":
+    elif n in ("Bounded", "Instances"):
         f[0:3] = _v3(d["half"])
         f[3] = d["margin"]
     elif n in ("SmoothUnion", "SmoothIntersection"):
@@ -193,6 +193,18 @@ class Graph:
             raise KeyError(name)
         return builders[name](**params)
 
+    def validate(self) -> dict:
+        """Graph::validate (validate.rs:146-330) through the library, on the host only:
+        raises SyfrackError for an invalid graph, else returns the derived constants."""
+        from ._lib import check, load
+
+        desc, keep = self.to_desc()
+        info = abi.sf_graph_info()
+        check(load().sf_graph_validate(C.byref(desc), C.byref(info)))
+        return {"step_scale": info.step_scale, "lipschitz": info.lipschitz,
+                "trap_scales": list(info.trap_scales), "iteration_product": info.iteration_product,
+                "form": abi.FORMS.get(info.form, info.form), "op_count": info.op_count}
+
     # -- C ABI packing -----------------------------------------------------------
     def to_desc(self):
         """Returns (sf_graph_desc, keepalive) -- keep `keepalive` referenced while
@@ -200,6 +212,7 @@ class Graph:
         n = len(self.nodes)
         nodes = (abi.sf_node * max(n, 1))()
         body_ids: list[int] = []
+        placements: list = []
         for i, nd in enumerate(self.nodes):
             f, u = _pack_params(nd.kind)
             s = nodes[i]
@@ -215,14 +228,35 @@ class Graph:
                 s.body_offset = len(body_ids)
                 s.body_len = len(body)
                 body_ids.extend(body)
+            if nd.kind.name == "Instances":
+                own = [placement_tuple(p) for p in nd.kind.fields.get("placements", [])]
+                s.u[0] = len(placements)
+                s.u[1] = len(own)
+                placements.extend(own)
         links = (abi.sf_link * max(len(self.links), 1))()
         for i, l in enumerate(self.links):
             links[i].from_node, links[i].from_port = l.src
             links[i].to_node, links[i].to_port = l.dst
         bodies = (C.c_uint32 * max(len(body_ids), 1))(*body_ids)
+        pl = (abi.sf_placement * max(len(placements), 1))()
+        for i, (pos, ang, sc) in enumerate(placements):
+            pl[i].position[:] = pos
+            pl[i].angles[:] = ang
+            pl[i].scale[:] = sc
         d = abi.sf_graph_desc(nodes, n, links, len(self.links), bodies, len(body_ids),
-                              self.safety, self.bounding_radius_hint)
-        return d, (nodes, links, bodies)
+                              self.safety, self.bounding_radius_hint, pl, len(placements))
+        return d, (nodes, links, bodies, pl)
+
+
+def placement_tuple(p):
+    """Placement{position, angles, scale} (graph/mod.rs:26-40) from a dict (RON or
+    keyword form) or a (position, angles, scale) triple; missing fields take the
+    defaults (origin, no rotation, unit scale)."""
+    if isinstance(p, dict):
+        get = lambda k, dflt: [float(x) for x in _v3(p.get(k, dflt))]
+        return (get("position", [0.0, 0.0, 0.0]), get("angles", [0.0, 0.0, 0.0]), get("scale", [1.0, 1.0, 1.0]))
+    pos, ang, sc = p
+    return ([float(x) for x in pos], [float(x) for x in ang], [float(x) for x in sc])
 
 
 def _chain_links(pairs):
