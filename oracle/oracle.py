@@ -62,6 +62,8 @@ def lib():
         up = C.POINTER(C.c_uint32)
         L.or_de_eval.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, dp, up, up, C.c_int]
         L.or_de_eval_fast.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, up, C.c_int]
+        L.or_bvh_build.argtypes = [C.POINTER(abi.sf_placement), C.c_uint32, C.POINTER(C.c_float),
+                                   C.POINTER(C.c_float)]
         L.or_primary.restype = C.c_uint64
         L.or_primary.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.sf_camera), C.c_uint32, C.c_uint32,
                                  C.c_uint32, C.c_uint32, C.c_uint32, C.c_int, C.c_double, C.c_double,
@@ -90,6 +92,21 @@ def _up(a):
 
 def default_threads() -> int:
     return max(1, os.cpu_count() or 1)
+
+
+def bvh_build(placements, half):
+    """The fence hierarchy of bvh.rs:26-102: (2n-1, 8) float32 rows (centre, half,
+    escape, placement or -1)."""
+    n = len(placements)
+    pl = (abi.sf_placement * n)()
+    for i, (pos, ang, sc) in enumerate(placements):
+        pl[i].position[:] = pos
+        pl[i].angles[:] = ang
+        pl[i].scale[:] = sc
+    h = (C.c_float * 3)(*half)
+    out = np.zeros((2 * n - 1, 8), np.float32)
+    lib().or_bvh_build(pl, n, h, out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out
 
 
 class OracleGraph:

@@ -87,6 +87,20 @@ void* or_graph_new(const sf_graph_desc* d) {
 
 void or_graph_free(void* g) { delete static_cast<Graph*>(g); }
 
+// The fence hierarchy of `count` placements: 8 floats per node (centre, half, escape,
+// placement or -1) into out (2 * count - 1 nodes).
+void or_bvh_build(const sf_placement* pl, uint32_t count, const float* half, float* out) {
+    auto nodes = bvh_build(pl, count, half);
+    for (size_t i = 0; i < nodes.size(); ++i) {
+        for (int k = 0; k < 3; ++k) {
+            out[8 * i + k] = nodes[i].center[k];
+            out[8 * i + 3 + k] = nodes[i].half[k];
+        }
+        out[8 * i + 6] = float(nodes[i].escape);
+        out[8 * i + 7] = float(nodes[i].placement);
+    }
+}
+
 void or_graph_info(void* gp, float* step_scale, float* lipschitz, float* trap_scales, uint32_t* iteration_product) {
     Graph* g = static_cast<Graph*>(gp);
     *step_scale = g->step_scale;

@@ -177,7 +177,7 @@ static void bvh_split(std::vector<Graph::InstBounds>& leaves, size_t lo, size_t 
     }
     nodes[index].escape = nodes.size();
 }
-static std::vector<Graph::InstBounds> bvh_build(const sf_placement* pl, uint32_t count, const float* half) {
+std::vector<Graph::InstBounds> bvh_build(const sf_placement* pl, uint32_t count, const float* half) {
     std::vector<Graph::InstBounds> leaves(count), nodes;
     for (uint32_t i = 0; i < count; ++i) {
         Q4<float> r = quat_xyz<float>(pl[i].angles);

@@ -176,6 +176,8 @@ inline uint32_t input_count(uint32_t k) {
 }
 
 bool prepare(Graph& g);
+// bvh::build (bvh.rs:26-102): the fence hierarchy of one Instances node.
+std::vector<Graph::InstBounds> bvh_build(const sf_placement* pl, uint32_t count, const float* half);
 
 // ---------------------------------------------------------------- DE
 template <class R> struct PointState { V3<R> p; R dr; uint32_t iter; R traps[4]; };

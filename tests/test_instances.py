@@ -233,3 +233,38 @@ def test_nested_copies_are_refused(renderer):
     with pytest.raises(SyfrackError) as e:
         renderer.compile(g)
     assert e.value.status == 3
+
+
+def test_fence_hierarchy_contains_every_copy_once(oracle_mod):
+    """bvh.rs:104-137: 1,031 rotated, scaled copies; every node's escape is past it,
+    every placement is one leaf, and every corner of a copy's fence box lies inside
+    its leaf and all the leaf's ancestors; far away the root is far."""
+    placements = [(((i % 31) * 3.0, float(i // 31), i * 0.01), (float(i), 31.0, -19.0), (0.2, 2.0, 1.3))
+                  for i in range(1031)]
+    half = np.array([1.0, 0.3, 2.0])
+    nodes = oracle_mod.bvh_build(placements, half).astype(np.float64)
+    assert len(nodes) == 2 * len(placements) - 1
+
+    def dist(n, p):
+        q = np.abs(p - n[:3]) - n[3:6]
+        return np.linalg.norm(np.maximum(q, 0.0)) + min(q.max(), 0.0)
+
+    seen = np.zeros(len(placements), bool)
+    for i, n in enumerate(nodes):
+        esc = int(n[6])
+        assert i < esc <= len(nodes)
+        leaf = int(n[7])
+        if leaf < 0:
+            continue
+        assert not seen[leaf]
+        seen[leaf] = True
+        pos, ang, sc = (np.array(x, np.float64) for x in placements[leaf])
+        r = rot_matrix(ang)
+        parents = [nodes[j] for j in range(i) if nodes[j][6] > i]
+        for corner in np.array(np.meshgrid([-1, 1], [-1, 1], [-1, 1])).reshape(3, -1).T:
+            c = pos + r @ (half * sc * corner)
+            assert dist(n, c) < 0.0
+            for par in parents:
+                assert dist(par, c) < 0.0
+    assert seen.all()
+    assert dist(nodes[0], np.full(3, 1e5)) > 1.0
