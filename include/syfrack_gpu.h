@@ -313,6 +313,29 @@ sf_status sf_session_stats(sf_session* s, sf_stats* out);
 sf_status sf_session_save(sf_session* s, const char* dir);
 sf_status sf_session_resume(sf_context* ctx, sf_graph* graph, const char* dir, sf_session** out);
 sf_status sf_session_destroy(sf_session* s);
+
+/* ------------------------------------------------------------------ tiled export
+ * ExportSession in ExportMode::Tiled (export.rs:95-300, TiledExport :830-900): the image
+ * lives in host memory; the device holds one tile-sized film and path arena. Each tile
+ * renders all its samples (camera and RNG in image coordinates, samples in ascending
+ * order, so the image equals a resident session's), then its planes are copied back
+ * while the next tile renders and are committed whole: a checkpoint never holds part
+ * of a tile. Checkpoints write state.bin and export.bin (the image) with FNV-1a
+ * checksums; resume refuses a changed image ("checksum") or another producer. */
+typedef struct sf_export sf_export;
+sf_status sf_export_create(sf_context* ctx, sf_graph* graph, const sf_scene_desc* scene,
+                           const sf_render_config* cfg, sf_export** out);
+/* ExportSession::step: renders tiles until budget_ms passes (0 = one tile); *done = 1
+ * once every tile is committed. */
+sf_status sf_export_step(sf_export* e, uint32_t budget_ms, int* done);
+sf_status sf_export_progress(sf_export* e, sf_progress* out);
+/* The host image (committed tiles; others hold the cleared planes). */
+sf_status sf_export_readback(sf_export* e, sf_film_planes* out);
+sf_status sf_export_save(sf_export* e, const char* dir);
+sf_status sf_export_resume(sf_context* ctx, sf_graph* graph, const char* dir, sf_export** out);
+/* Device bytes the export holds (TiledExport::device_buffer_bytes). */
+sf_status sf_export_device_bytes(sf_export* e, uint64_t* out);
+sf_status sf_export_destroy(sf_export* e);
 /* Autotuning knobs of the wavefront trace kernel (256 threads per block): resident
  * blocks per SM (2..4, selecting the register budget; default 3), the march step
  * quantum after which an open segment is saved and re-queued (0 = unbounded, the

@@ -151,6 +151,14 @@ SIGNATURES = {
     "sf_serve_release": [vp, u64],
     "sf_server_stats_get": [vp, P(sf_server_stats)],
     "sf_server_destroy": [vp],
+    "sf_export_create": [vp, vp, P(abi.sf_scene_desc), P(abi.sf_render_config), P(vp)],
+    "sf_export_step": [vp, u32, P(C.c_int)],
+    "sf_export_progress": [vp, P(sf_progress)],
+    "sf_export_readback": [vp, P(sf_film_planes)],
+    "sf_export_save": [vp, C.c_char_p],
+    "sf_export_resume": [vp, vp, C.c_char_p, P(vp)],
+    "sf_export_device_bytes": [vp, P(u64)],
+    "sf_export_destroy": [vp],
 }
 _RESTYPES = {"sf_status_string": C.c_char_p, "sf_last_error": C.c_char_p, "sf_abi_version": u32}
 

@@ -1184,28 +1184,6 @@ extern "C" sf_status sf_primary_trace(sf_graph* g, const sf_primary_desc* d, flo
 }
 
 // ------------------------------------------------------------------ sessions
-struct sf_session {
-    sf_context* ctx = nullptr;
-    sf_graph* graph = nullptr;
-    sf_scene_desc scene;
-    sf_render_config cfg;
-    DevScene* d_scene = nullptr;
-    FilmPlanes film{};
-    PathSoA soa{};
-    uint32_t capacity = 0;
-    uint32_t* lists = nullptr;     // 2 x {active, cont, shadow} x capacity
-    uint32_t* resume = nullptr;    // 2 x 2*capacity segments cut at a step quantum
-    uint32_t* qcounts = nullptr;   // per round and launch: {work counter, resumed count}
-    uint32_t* counts = nullptr;    // per round: {active, cont, shadow, work}
-    uint32_t* status = nullptr;
-    void* mem = nullptr;
-    size_t mem_bytes = 0;
-    std::vector<sf_tile> tiles;
-    uint32_t tile_size = 0, dispatches = 0;
-    uint32_t min_blocks = 3, quantum = 0, regen = 4;
-    uint32_t status_host = 0;
-    double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
-};
 
 namespace sfh {
 
@@ -1248,7 +1226,9 @@ sf_status session_alloc(sf_session* s) {
     if (cap64 > 0x7fffffffull) return fail(SF_ERR_INVALID, "tile_size^2 * samples_per_dispatch too large");
     s->capacity = uint32_t(cap64);
     const size_t N = s->capacity;
-    const size_t px = size_t(cfg.width) * cfg.height;
+    // a window session (a tiled export's) holds a tile-sized film; others the image
+    const uint32_t fw = s->window ? tw : cfg.width, fh = s->window ? th : cfg.height;
+    const size_t px = size_t(fw) * fh;
     const bool wf = cfg.integrator == SF_INTEGRATOR_WAVEFRONT;
     const uint32_t R = rounds_of(cfg);
     // layout
@@ -1275,8 +1255,8 @@ sf_status session_alloc(sf_session* s) {
     s->film.accum = reinterpret_cast<float4*>(base + o_acc);
     s->film.depth = reinterpret_cast<float*>(base + o_depth);
     s->film.aux = reinterpret_cast<float4*>(base + o_aux);
-    s->film.width = cfg.width;
-    s->film.height = cfg.height;
+    s->film.width = fw;
+    s->film.height = fh;
     std::memset(&s->soa, 0, sizeof s->soa);
     s->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
     s->soa.capacity = s->capacity;
@@ -1367,6 +1347,9 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
     if (tile.w == 0 || tile.h == 0 || samples == 0) return SF_OK;
     if (tile.x + tile.w > s->cfg.width || tile.y + tile.h > s->cfg.height)
         return fail(SF_ERR_INVALID, "tile outside the image");
+    if (s->window && (tile.x < s->film.x0 || tile.y < s->film.y0 || tile.x + tile.w > s->film.x0 + s->film.width ||
+                      tile.y + tile.h > s->film.y0 + s->film.height))
+        return fail(SF_ERR_INVALID, "tile outside the window film");
     uint64_t paths = uint64_t(tile.w) * tile.h * samples;
     if (paths > s->capacity) return fail(SF_ERR_INVALID, "tile * samples exceeds the session capacity");
     sf_context* c = s->ctx;
@@ -1567,7 +1550,7 @@ extern "C" sf_status sf_session_destroy(sf_session* s) {
 // ------------------------------------------------------------------ checkpoints
 namespace sfh {
 
-uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
+uint64_t fnv1a(const void* data, size_t n, uint64_t h) {
     const uint8_t* p = static_cast<const uint8_t*>(data);
     for (size_t i = 0; i < n; ++i) {
         h ^= p[i];
@@ -1576,42 +1559,6 @@ uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull) {
     return h;
 }
 
-struct Writer {
-    std::vector<uint8_t> buf;
-    template <class T> void put(const T& v) {
-        const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
-        buf.insert(buf.end(), p, p + sizeof(T));
-    }
-    void put_bytes(const void* p, size_t n) {
-        const uint8_t* q = static_cast<const uint8_t*>(p);
-        buf.insert(buf.end(), q, q + n);
-    }
-    void put_str(const std::string& s) { put(uint32_t(s.size())); put_bytes(s.data(), s.size()); }
-};
-struct Reader {
-    const std::vector<uint8_t>& buf;
-    size_t pos = 0;
-    bool ok = true;
-    template <class T> T get() {
-        T v{};
-        if (pos + sizeof(T) > buf.size()) { ok = false; return v; }
-        std::memcpy(&v, buf.data() + pos, sizeof(T));
-        pos += sizeof(T);
-        return v;
-    }
-    void get_bytes(void* p, size_t n) {
-        if (pos + n > buf.size()) { ok = false; return; }
-        std::memcpy(p, buf.data() + pos, n);
-        pos += n;
-    }
-    std::string get_str() {
-        uint32_t n = get<uint32_t>();
-        if (!ok || pos + n > buf.size()) { ok = false; return ""; }
-        std::string s(reinterpret_cast<const char*>(buf.data() + pos), n);
-        pos += n;
-        return s;
-    }
-};
 
 const uint32_t CK_MAGIC = 0x4b434653u;  // "SFCK"
 const uint32_t CK_VERSION = 2;
@@ -1639,8 +1586,29 @@ bool read_file(const std::string& path, std::vector<uint8_t>& data) {
     return bool(f) || f.eof();
 }
 void remove_tree(const std::string& dir) {
-    for (const char* name : {"state.bin", "film.bin"}) unlink((dir + "/" + name).c_str());
+    for (const char* name : {"state.bin", "film.bin", "export.bin"}) unlink((dir + "/" + name).c_str());
     rmdir(dir.c_str());
+}
+// Writes the files into a sibling directory, then swaps it into place (session.rs:33-45).
+sf_status install_checkpoint(const std::string& final_dir,
+                             const std::vector<std::pair<std::string, const std::vector<uint8_t>*>>& files) {
+    std::string tmp = final_dir + ".tmp-" + std::to_string(getpid()), old = final_dir + ".old";
+    remove_tree(tmp);
+    if (mkdir(tmp.c_str(), 0755) != 0) return fail(SF_ERR_IO, "cannot create " + tmp);
+    for (auto& f : files)
+        if (!write_file(tmp + "/" + f.first, *f.second)) {
+            remove_tree(tmp);
+            return fail(SF_ERR_IO, "cannot write checkpoint files");
+        }
+    struct stat st;
+    bool existed = stat(final_dir.c_str(), &st) == 0;
+    if (existed) {
+        remove_tree(old);
+        if (rename(final_dir.c_str(), old.c_str()) != 0) { remove_tree(tmp); return fail(SF_ERR_IO, "cannot move old checkpoint"); }
+    }
+    if (rename(tmp.c_str(), final_dir.c_str()) != 0) return fail(SF_ERR_IO, "cannot install checkpoint");
+    if (existed) remove_tree(old);
+    return SF_OK;
 }
 
 }  // namespace sfh
@@ -1674,23 +1642,7 @@ extern "C" sf_status sf_session_save(sf_session* s, const char* dir) {
     w.put(fnv1a(film.buf.data(), film.buf.size()));
     uint64_t h = fnv1a(w.buf.data(), w.buf.size());
     w.put(h);
-    // write a sibling directory, then swap it in (session.rs:33-45)
-    std::string final_dir(dir), tmp = final_dir + ".tmp-" + std::to_string(getpid()), old = final_dir + ".old";
-    remove_tree(tmp);
-    if (mkdir(tmp.c_str(), 0755) != 0) return fail(SF_ERR_IO, "cannot create " + tmp);
-    if (!write_file(tmp + "/film.bin", film.buf) || !write_file(tmp + "/state.bin", w.buf)) {
-        remove_tree(tmp);
-        return fail(SF_ERR_IO, "cannot write checkpoint files");
-    }
-    struct stat st;
-    bool existed = stat(final_dir.c_str(), &st) == 0;
-    if (existed) {
-        remove_tree(old);
-        if (rename(final_dir.c_str(), old.c_str()) != 0) { remove_tree(tmp); return fail(SF_ERR_IO, "cannot move old checkpoint"); }
-    }
-    if (rename(tmp.c_str(), final_dir.c_str()) != 0) return fail(SF_ERR_IO, "cannot install checkpoint");
-    if (existed) remove_tree(old);
-    return SF_OK;
+    return install_checkpoint(dir, {{"film.bin", &film.buf}, {"state.bin", &w.buf}});
 }
 
 extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* dir, sf_session** out) {

@@ -1,10 +1,12 @@
 // Internal interface of the host runtime shared by its translation units
 // (sf_host.cpp: graphs, contexts, sessions, checkpoints, escape time; sf_batch_host.cpp:
-// batched wavefronts; sf_serve.cpp: the serving scheduler). Not part of the C ABI.
+// batched wavefronts; sf_serve.cpp: the serving scheduler; sf_export.cpp: tiled
+// exports). Not part of the C ABI.
 #pragma once
 #include <cuda_runtime.h>
 
 #include <atomic>
+#include <cstring>
 #include <mutex>
 #include <string>
 #include <vector>
@@ -149,5 +151,83 @@ struct WaveArena {
 sf_status arena_alloc(sf_context* c, WaveArena& a, uint32_t capacity, uint32_t max_jobs, uint32_t rounds,
                       size_t extra_bytes, size_t* extra_offset);
 sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, bool timed);
+
+}  // namespace sfh
+
+// A render session (RenderSession, session.rs:165): scene constants, film and path state.
+struct sf_session {
+    sf_context* ctx = nullptr;
+    sf_graph* graph = nullptr;
+    sf_scene_desc scene;
+    sf_render_config cfg;
+    DevScene* d_scene = nullptr;
+    FilmPlanes film{};
+    PathSoA soa{};
+    uint32_t capacity = 0;
+    uint32_t* lists = nullptr;     // 2 x {active, cont, shadow} x capacity
+    uint32_t* resume = nullptr;    // 2 x 2*capacity segments cut at a step quantum
+    uint32_t* qcounts = nullptr;   // per round and launch: {work counter, resumed count}
+    uint32_t* counts = nullptr;    // per round: {active, cont, shadow, work}
+    uint32_t* status = nullptr;
+    void* mem = nullptr;
+    size_t mem_bytes = 0;
+    std::vector<sf_tile> tiles;
+    uint32_t tile_size = 0, dispatches = 0;
+    uint32_t min_blocks = 3, quantum = 0, regen = 4;
+    uint32_t status_host = 0;
+    double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
+    bool window = false;       // tiled export: a tile-sized film whose origin the export sets
+};
+
+namespace sfh {
+
+sf_status session_alloc(sf_session* s);
+void tile_grid(sf_session* s);
+
+// Checkpoint files: plain binary records, FNV-1a checksums, a producer identity,
+// and a sibling directory swapped into place (session.rs:33-45, :1194-1346).
+uint64_t fnv1a(const void* data, size_t n, uint64_t h = 0xcbf29ce484222325ull);
+std::string producer_of(const sf_context* c);
+bool write_file(const std::string& path, const std::vector<uint8_t>& data);
+bool read_file(const std::string& path, std::vector<uint8_t>& data);
+void remove_tree(const std::string& dir);
+sf_status install_checkpoint(const std::string& final_dir,
+                             const std::vector<std::pair<std::string, const std::vector<uint8_t>*>>& files);
+struct Writer {
+    std::vector<uint8_t> buf;
+    template <class T> void put(const T& v) {
+        const uint8_t* p = reinterpret_cast<const uint8_t*>(&v);
+        buf.insert(buf.end(), p, p + sizeof(T));
+    }
+    void put_bytes(const void* p, size_t n) {
+        const uint8_t* q = static_cast<const uint8_t*>(p);
+        buf.insert(buf.end(), q, q + n);
+    }
+    void put_str(const std::string& s) { put(uint32_t(s.size())); put_bytes(s.data(), s.size()); }
+};
+struct Reader {
+    const std::vector<uint8_t>& buf;
+    size_t pos = 0;
+    bool ok = true;
+    template <class T> T get() {
+        T v{};
+        if (pos + sizeof(T) > buf.size()) { ok = false; return v; }
+        std::memcpy(&v, buf.data() + pos, sizeof(T));
+        pos += sizeof(T);
+        return v;
+    }
+    void get_bytes(void* p, size_t n) {
+        if (pos + n > buf.size()) { ok = false; return; }
+        std::memcpy(p, buf.data() + pos, n);
+        pos += n;
+    }
+    std::string get_str() {
+        uint32_t n = get<uint32_t>();
+        if (!ok || pos + n > buf.size()) { ok = false; return ""; }
+        std::string s(reinterpret_cast<const char*>(buf.data() + pos), n);
+        pos += n;
+        return s;
+    }
+};
 
 }  // namespace sfh

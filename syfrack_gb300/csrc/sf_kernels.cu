@@ -293,7 +293,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 h.light_index = li;
             }
             if (sample == 0 && ps.bounce == 0) {
-                size_t idx = (size_t)py * film.width + px;
+                const size_t idx = film_index(film, px, py);
                 fd = film.depth + idx;
                 fa = film.aux + idx;
             } else {

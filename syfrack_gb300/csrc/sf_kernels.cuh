@@ -75,7 +75,11 @@ struct FilmPlanes {
     float* depth;   // first-hit distance, -1 for a miss (sample 0)
     float4* aux;    // first-hit normal and steps (sample 0)
     uint32_t width, height;
+    uint32_t x0, y0;  // image pixel of the planes' first element (a window film; 0, 0 for the image)
 };
+__device__ __forceinline__ size_t film_index(const FilmPlanes& f, uint32_t px, uint32_t py) {
+    return (size_t)(py - f.y0) * f.width + (px - f.x0);
+}
 
 struct DispatchGeom {
     uint32_t tile_x, tile_y, tile_w, tile_h;

@@ -98,7 +98,7 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
         float* fd = nullptr;
         float4* fa = nullptr;
         if (sample == 0 && ps.bounce == 0) {
-            size_t idx = (size_t)py * film.width + px;
+            const size_t idx = film_index(film, px, py);
             fd = film.depth + idx;
             fa = film.aux + idx;
         }
@@ -138,7 +138,7 @@ static __device__ __forceinline__ void commit_pixel(const PathSoA& soa, const Di
                                                     uint32_t local, uint32_t path_base) {
     uint32_t tile_px = g.tile_w * g.tile_h;
     uint32_t px = g.tile_x + local % g.tile_w, py = g.tile_y + local / g.tile_w;
-    size_t idx = (size_t)py * film.width + px;
+    const size_t idx = film_index(film, px, py);
     float4 acc = film.accum[idx];
     for (uint32_t s = 0; s < g.samples; ++s) {
         float4 L = soa.Ls[path_base + (size_t)s * tile_px + local];

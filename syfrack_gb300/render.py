@@ -300,6 +300,81 @@ class RenderSession:
         return cls(renderer, scene, cfg, _handle=h)
 
 
+class ExportSession:
+    """Tiled export (ExportSession / TiledExport, export.rs:95-300, :830-900): the image
+    in host memory, one tile-sized film on the device; tiles are committed whole."""
+
+    def __init__(self, renderer: Renderer, scene: Scene, cfg: RenderConfig, _handle=None):
+        self.renderer = renderer
+        self.ctx = renderer.ctx
+        self.scene = scene
+        self.cfg = cfg
+        self.graph = renderer.compile(scene.graph)
+        self.t0 = time.perf_counter()
+        if _handle is not None:
+            self.h = _handle
+            return
+        sd = scene.desc(cfg.width, cfg.height)
+        rc = cfg.desc()
+        h = C.c_void_p()
+        check(self.ctx.lib.sf_export_create(self.ctx.h, self.graph.h, C.byref(sd), C.byref(rc), C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sf_export_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def step(self, budget_ms: int = 250) -> bool:
+        done = C.c_int()
+        check(self.ctx.lib.sf_export_step(self.h, budget_ms, C.byref(done)))
+        return bool(done.value)
+
+    def progress(self) -> dict:
+        p = sf_progress()
+        check(self.ctx.lib.sf_export_progress(self.h, C.byref(p)))
+        return {k: getattr(p, k) for k, _ in sf_progress._fields_}
+
+    def device_bytes(self) -> int:
+        n = C.c_uint64()
+        check(self.ctx.lib.sf_export_device_bytes(self.h, C.byref(n)))
+        return n.value
+
+    def film_planes(self) -> dict:
+        w, h = self.cfg.width, self.cfg.height
+        out = {k: np.zeros((h, w, 4), np.float32) for k in ("accum", "aux", "volume", "moments", "surface")}
+        out["depth"] = np.zeros((h, w), np.float32)
+        planes = sf_film_planes(*(_fp(out[k]) for k in ("accum", "depth", "aux", "volume", "moments", "surface")))
+        check(self.ctx.lib.sf_export_readback(self.h, C.byref(planes)))
+        return out
+
+    def readback(self) -> RenderOutput:
+        p = self.film_planes()
+        acc = p["accum"]
+        color = np.ones_like(acc)
+        color[..., :3] = acc[..., :3] / np.maximum(acc[..., 3:4], 1.0)
+        pr = self.progress()
+        return RenderOutput(color, acc, p["depth"], p["aux"], pr["samples_min"], pr["samples_max"],
+                            time.perf_counter() - self.t0)
+
+    def save(self, directory: str):
+        check(self.ctx.lib.sf_export_save(self.h, directory.encode()))
+
+    @classmethod
+    def resume(cls, renderer: Renderer, scene: Scene, cfg: RenderConfig, directory: str) -> "ExportSession":
+        """ExportSession::resume (export.rs:135-190): refuses a changed export.bin."""
+        g = renderer.compile(scene.graph)
+        h = C.c_void_p()
+        check(renderer.ctx.lib.sf_export_resume(renderer.ctx.h, g.h, directory.encode(), C.byref(h)))
+        return cls(renderer, scene, cfg, _handle=h)
+
+
 class Batch:
     """Many (scene, config) jobs rendered by one wavefront (sf_batch_*): one set of
     persistent launches per round over all jobs' paths, captured in a CUDA graph."""
