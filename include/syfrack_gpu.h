@@ -314,6 +314,32 @@ sf_status sf_session_save(sf_session* s, const char* dir);
 sf_status sf_session_resume(sf_context* ctx, sf_graph* graph, const char* dir, sf_session** out);
 sf_status sf_session_destroy(sf_session* s);
 
+/* ------------------------------------------------------------------ preview
+ * ControlSession (crates/syfrack-render/src/control/mod.rs:172-530): an interactive
+ * preview of primary rays through pixel centres on the exact field, marched in
+ * resumable quanta of `quantum` DE evaluations per pixel (0 = 128) with no step
+ * budget, shaded with the control engine's fixed light (control.wgsl:54-99). No
+ * graph is ever compiled: a graph edit (sf_graph_update) or sf_preview_set uploads
+ * data; sf_preview_set restarts the image. The machine runs on its own
+ * highest-priority stream. */
+typedef struct sf_preview sf_preview;
+sf_status sf_preview_create(sf_context* ctx, sf_graph* graph, const sf_scene_desc* scene, uint32_t width,
+                            uint32_t height, uint32_t quantum, sf_preview** out);
+/* set_scene: another graph and/or scene (NULL keeps the current one); restarts. */
+sf_status sf_preview_set(sf_preview* p, sf_graph* graph, const sf_scene_desc* scene);
+/* tick: polls the previous quantum and submits at most one; never waits for the
+ * device. *complete = 1 once every pixel has ended. A non-finite distance fails
+ * the preview with SF_ERR_GRAPH. */
+sf_status sf_preview_tick(sf_preview* p, int* complete);
+/* wait_complete: ticks until complete or timeout_ms (SF_ERR_TIMEOUT); diagnostic. */
+sf_status sf_preview_wait(sf_preview* p, uint32_t timeout_ms);
+sf_status sf_preview_progress(sf_preview* p, uint32_t* completed_pixels, uint32_t* dispatches);
+/* accum = preview colour (1 in w), depth (-1 on a miss), aux = normal and march steps. */
+sf_status sf_preview_readback(sf_preview* p, sf_film_planes* out);
+/* pick(u, v) in [0, 1]^2: the pixel's depth (<= 0: nothing there) and aux. */
+sf_status sf_preview_pick(sf_preview* p, float u, float v, float* depth, float* aux);
+sf_status sf_preview_destroy(sf_preview* p);
+
 /* ------------------------------------------------------------------ tiled export
  * ExportSession in ExportMode::Tiled (export.rs:95-300, TiledExport :830-900): the image
  * lives in host memory; the device holds one tile-sized film and path arena. Each tile

@@ -5,13 +5,13 @@ package is its ctypes binding with the reference's Rust API names.
 """
 from . import abi, ron
 from .graph import Graph, Kind, Link, Node
-from .render import (Batch, Canvas, CompiledGraph, DeSample, ExportSession, GpuContext, PlanarFractal, RenderOutput,
-                     Renderer, RenderSession, deep_zoom, escape2d)
+from .render import (Batch, Canvas, CompiledGraph, DeSample, ExportSession, GpuContext, PlanarFractal, PreviewSession,
+                     RenderOutput, Renderer, RenderSession, deep_zoom, escape2d)
 from .serve import ServeResult, Server
 from .scene import AreaLight, Camera, Finish, Material, RenderConfig, Scene, SurfaceVariation
 from ._lib import SyfrackError
 
 __all__ = ["abi", "ron", "Batch", "Graph", "Kind", "Link", "Node", "Canvas", "CompiledGraph", "DeSample", "ExportSession",
-           "GpuContext",
+           "GpuContext", "PreviewSession",
            "PlanarFractal", "RenderOutput", "Renderer", "RenderSession", "ServeResult", "Server", "deep_zoom", "escape2d", "AreaLight",
            "Camera", "Finish", "Material", "RenderConfig", "Scene", "SurfaceVariation", "SyfrackError"]

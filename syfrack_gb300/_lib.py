@@ -159,6 +159,14 @@ SIGNATURES = {
     "sf_export_resume": [vp, vp, C.c_char_p, P(vp)],
     "sf_export_device_bytes": [vp, P(u64)],
     "sf_export_destroy": [vp],
+    "sf_preview_create": [vp, vp, P(abi.sf_scene_desc), u32, u32, u32, P(vp)],
+    "sf_preview_set": [vp, vp, P(abi.sf_scene_desc)],
+    "sf_preview_tick": [vp, P(C.c_int)],
+    "sf_preview_wait": [vp, u32],
+    "sf_preview_progress": [vp, up, up],
+    "sf_preview_readback": [vp, P(sf_film_planes)],
+    "sf_preview_pick": [vp, C.c_float, C.c_float, fp, fp],
+    "sf_preview_destroy": [vp],
 }
 _RESTYPES = {"sf_status_string": C.c_char_p, "sf_last_error": C.c_char_p, "sf_abi_version": u32}
 

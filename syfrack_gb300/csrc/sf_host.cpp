@@ -1052,7 +1052,7 @@ extern "C" sf_status sf_graph_update(sf_graph* g, const sf_graph_desc* d) {
         return fail(SF_ERR_GRAPH, "topology changed: compile a new graph");
     P.inst_data = reinterpret_cast<uint64_t>(g->d_inst);
     cudaSetDevice(g->ctx->device);
-    CU(cudaStreamSynchronize(g->ctx->stream));  // no launch may read the blocks being replaced
+    CU(cudaDeviceSynchronize());  // no launch on any stream (previews, server slots) may read what is replaced
     if (g->d_inst) CU(cudaMemcpyAsync(g->d_inst, inst.data(), g->inst_bytes, cudaMemcpyHostToDevice, g->ctx->stream));
     CU(cudaMemcpyAsync(g->d_prog, &P, sizeof P, cudaMemcpyHostToDevice, g->ctx->stream));
     CU(cudaStreamSynchronize(g->ctx->stream));

@@ -156,6 +156,22 @@ cudaError_t sf_launch_advance_batch(BatchTable bt, cudaStream_t st);
 cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
                             uint32_t* status, int final_round, cudaStream_t st);
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st);
+
+// The preview machine's per-pixel state and outputs (one row per pixel).
+struct PreviewState {
+    float4* march;  // t, omega, previous radius, step length
+    float4* grad;   // tap gradient xyz, tap offset
+    uint2* tags;    // state (0 march, 2..5 taps, 6 done, 8 error), march steps
+};
+struct PreviewOut {
+    float4* accum;  // preview colour, 1
+    float* depth;   // hit distance, -1 until hit (and on a miss)
+    float4* aux;    // normal, march steps (-1 until hit)
+};
+// One quantum (at most `quantum` DE evaluations per pixel); init starts every pixel
+// over. status[0] += pixels still open, status[2] += pixels that met an error.
+cudaError_t sf_launch_preview(const DeProgram* prog, const DevScene* scene, uint32_t pixels, PreviewState st,
+                              PreviewOut out, uint32_t quantum, uint32_t init, uint32_t* status, cudaStream_t s);
 cudaError_t sf_launch_film_clear(FilmPlanes film, cudaStream_t st);
 cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, PathSoA soa, DispatchGeom g,
                                  FilmPlanes film, unsigned long long* stats, cudaStream_t st);

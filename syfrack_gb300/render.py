@@ -112,6 +112,12 @@ class CompiledGraph:
         desc, keep = graph.to_desc()
         check(self.ctx.lib.sf_graph_update(self.h, C.byref(desc)))
         self.graph = graph
+        cache = getattr(self, "_cache", None)
+        if cache is not None:  # the renderer's cache now finds this handle under the new values
+            if cache.get(self._key) is self:
+                del cache[self._key]
+            self._key = Renderer.cache_key(graph)
+            cache.setdefault(self._key, self)
 
     def probe(self, points) -> dict:
         """Batched DE at points (n, 3) -> arrays distance, traps (n, 4), iterations, material."""
@@ -148,14 +154,21 @@ class Renderer:
         self.ctx = ctx or GpuContext()
         self._cache: dict = {}
 
-    def compile(self, graph: Graph) -> CompiledGraph:
+    @staticmethod
+    def cache_key(graph: Graph):
         desc, keep = graph.to_desc()
-        key = (bytes(C.string_at(desc.nodes, C.sizeof(abi.sf_node) * desc.node_count)),
-               bytes(C.string_at(desc.links, C.sizeof(abi.sf_link) * desc.link_count)),
-               bytes(C.string_at(desc.body_ids, 4 * desc.body_id_count)), desc.safety, desc.bounding_radius_hint)
+        return (bytes(C.string_at(desc.nodes, C.sizeof(abi.sf_node) * desc.node_count)),
+                bytes(C.string_at(desc.links, C.sizeof(abi.sf_link) * desc.link_count)),
+                bytes(C.string_at(desc.body_ids, 4 * desc.body_id_count)),
+                bytes(C.string_at(desc.placements, C.sizeof(abi.sf_placement) * desc.placement_count)),
+                desc.safety, desc.bounding_radius_hint)
+
+    def compile(self, graph: Graph) -> CompiledGraph:
+        key = self.cache_key(graph)
         g = self._cache.get(key)
         if g is None:
             g = CompiledGraph(self.ctx, graph)
+            g._cache, g._key = self._cache, key
             self._cache[key] = g
         return g
 
@@ -298,6 +311,75 @@ class RenderSession:
         h = C.c_void_p()
         check(renderer.ctx.lib.sf_session_resume(renderer.ctx.h, g.h, directory.encode(), C.byref(h)))
         return cls(renderer, scene, cfg, _handle=h)
+
+
+class PreviewSession:
+    """Interactive preview (ControlSession, control/mod.rs:172-530): primary rays on
+    the exact field in resumable quanta, no step budget; tick() never waits; edits
+    upload data and restart the image."""
+
+    def __init__(self, renderer: Renderer, scene: Scene, size, quantum: int = 128):
+        self.renderer = renderer
+        self.ctx = renderer.ctx
+        self.scene = scene
+        self.size = (int(size[0]), int(size[1]))
+        self.graph = renderer.compile(scene.graph)
+        sd = scene.desc(*self.size)
+        h = C.c_void_p()
+        check(self.ctx.lib.sf_preview_create(self.ctx.h, self.graph.h, C.byref(sd), self.size[0], self.size[1],
+                                             quantum, C.byref(h)))
+        self.h = h
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sf_preview_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+    def set_scene(self, scene: Scene):
+        """A new scene (graph and camera): uploaded, nothing compiled; the image restarts."""
+        g = self.renderer.compile(scene.graph)
+        sd = scene.desc(*self.size)
+        check(self.ctx.lib.sf_preview_set(self.h, g.h, C.byref(sd)))
+        self.scene, self.graph = scene, g
+
+    def update_graph(self, graph):
+        """A value edit of the current graph (same topology): sf_graph_update, then restart."""
+        self.graph.update(graph)
+        check(self.ctx.lib.sf_preview_set(self.h, None, None))
+
+    def tick(self) -> bool:
+        done = C.c_int()
+        check(self.ctx.lib.sf_preview_tick(self.h, C.byref(done)))
+        return bool(done.value)
+
+    def wait_complete(self, timeout_ms: int = 120000):
+        check(self.ctx.lib.sf_preview_wait(self.h, timeout_ms))
+
+    def progress(self) -> dict:
+        px, d = C.c_uint32(), C.c_uint32()
+        check(self.ctx.lib.sf_preview_progress(self.h, C.byref(px), C.byref(d)))
+        return {"completed_pixels": px.value, "dispatches": d.value}
+
+    def readback(self) -> dict:
+        w, h = self.size
+        out = {"accum": np.zeros((h, w, 4), np.float32), "depth": np.zeros((h, w), np.float32),
+               "aux": np.zeros((h, w, 4), np.float32)}
+        planes = sf_film_planes(_fp(out["accum"]), _fp(out["depth"]), _fp(out["aux"]))
+        check(self.ctx.lib.sf_preview_readback(self.h, C.byref(planes)))
+        return out
+
+    def pick(self, u: float, v: float):
+        """(depth, aux) at (u, v) in [0, 1]^2, or None where nothing was hit."""
+        d = C.c_float()
+        a = (C.c_float * 4)()
+        check(self.ctx.lib.sf_preview_pick(self.h, u, v, C.byref(d), a))
+        return None if d.value <= 0.0 else (d.value, list(a))
 
 
 class ExportSession:
