@@ -189,13 +189,35 @@ typedef struct sf_material {
     float roughness, metallic, specular;
     float emission[3];
 } sf_material;
-/* Light::Area packed as GpuLight (uniforms.rs:671-713): a = centre, b = full
- * width edge, c = full height edge, radiance = color * intensity. */
+/* One light of Scene.lights (light.rs:63-120), in scene order (next-event sampling
+ * visits them in that order). kind selects the fields:
+ *   Area (GpuLight, uniforms.rs:671-713): centre, full width edge (edge_u), full
+ *     height edge (edge_v), radiance = color * intensity;
+ *   Sun: direction toward the sun, angular_size = full angular diameter in degrees,
+ *     radiance = irradiance (color * intensity);
+ *   Environment: zenith, horizon and ground radiance (colors * intensity). */
+enum { SF_LIGHT_AREA = 0, SF_LIGHT_SUN = 1, SF_LIGHT_ENVIRONMENT = 2 };
 typedef struct sf_area_light {
     float center[3], edge_u[3], edge_v[3], radiance[3];
+    uint32_t kind;
+    float direction[3];
+    float angular_size;
+    float zenith[3], horizon[3], ground[3];
 } sf_area_light;
+typedef sf_area_light sf_light;
 #define SF_MAX_LIGHTS 8
 #define SF_MAX_FINISHES 8
+#define SF_MAX_RAMP_STOPS 16
+/* Material.coloring (material.rs:100-130) as GpuColoring (uniforms.rs:193-215): the
+ * ramp (palette.rs:74-100) multiplies the albedo by its value at the sample's trap
+ * slot (0..3), iteration fraction (4) or n.y * 0.5 + 0.5 (5); 0xffff = none. */
+typedef struct sf_coloring {
+    uint32_t slot;
+    uint32_t stop_count;              /* 0: white */
+    float stops[SF_MAX_RAMP_STOPS][4];/* rgb, position (evenly spaced unless positioned) */
+    uint32_t cyclic, smooth, positioned;
+    float frequency, phase, gamma;
+} sf_coloring;
 typedef struct sf_scene_desc {
     sf_camera camera;
     sf_material material;                 /* index 0: the global surface */
@@ -208,6 +230,7 @@ typedef struct sf_scene_desc {
     float variation_roughness[2], variation_metallic[2];
     float cavity_darkness;                /* atmosphere.b.w, 0 = off */
     uint64_t seed;                        /* Scene.seed; the device uses lo ^ hi */
+    sf_coloring coloring;                 /* slot 0xffff (or no stops): no colouring */
 } sf_scene_desc;
 
 /* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138). */

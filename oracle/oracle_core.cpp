@@ -803,10 +803,41 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
     for (uint32_t i = 0; i < s.finish_count; ++i) s.finishes[i] = mat(d.finishes[i]);
     s.light_count = std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
     for (uint32_t i = 0; i < s.light_count; ++i) {
-        s.lights[i].a = v3<R>(d.lights[i].center);
-        s.lights[i].b = v3<R>(d.lights[i].edge_u);
-        s.lights[i].c = v3<R>(d.lights[i].edge_v);
-        s.lights[i].color = v3<R>(d.lights[i].radiance);
+        const sf_area_light& l = d.lights[i];
+        Light<R>& o = s.lights[i];
+        o.kind = l.kind;
+        o.color = v3<R>(l.radiance);
+        if (l.kind == SF_LIGHT_SUN) {
+            // GpuLight::from_light (uniforms.rs:656-668), in binary32 as the reference
+            o.a = v3<R>(l.direction);
+            o.cos_max = R(std::cos((l.angular_size * 0.5f) * (3.14159265f / 180.0f)));
+        } else if (l.kind == SF_LIGHT_ENVIRONMENT) {
+            o.a = v3<R>(l.zenith);
+            o.b = v3<R>(l.horizon);
+            o.c = v3<R>(l.ground);
+            auto lum = [](const float* c) { return R(c[0]) * R(0.2126) + R(c[1]) * R(0.7152) + R(c[2]) * R(0.0722); };
+            o.energy = r_max(r_max(lum(l.zenith), lum(l.horizon)), lum(l.ground));
+            R peak = 0;
+            for (int k = 0; k < 3; ++k) peak = r_max(peak, r_max(R(l.zenith[k]), r_max(R(l.horizon[k]), R(l.ground[k]))));
+            o.peak = peak;
+        } else {
+            o.a = v3<R>(l.center);
+            o.b = v3<R>(l.edge_u);
+            o.c = v3<R>(l.edge_v);
+        }
+    }
+    const sf_coloring& col = d.coloring;
+    s.coloring.slot = col.slot;
+    s.coloring.n = std::min<uint32_t>(col.stop_count, SF_MAX_RAMP_STOPS);
+    s.coloring.cyclic = col.cyclic != 0;
+    s.coloring.smooth = col.smooth != 0;
+    s.coloring.positioned = col.positioned != 0;
+    s.coloring.frequency = R(col.frequency);
+    s.coloring.phase = R(col.phase);
+    s.coloring.gamma = R(col.gamma);
+    for (uint32_t i = 0; i < s.coloring.n; ++i) {
+        s.coloring.stops[i] = V3<R>(R(col.stops[i][0]), R(col.stops[i][1]), R(col.stops[i][2]));
+        s.coloring.pos[i] = R(col.stops[i][3]);
     }
     s.variation_slot = d.variation_slot;
     s.variation_enabled = d.variation_enabled;
@@ -920,7 +951,8 @@ template <class R> static R area_weight(V3<R> p, V3<R> n, const Light<R>& l) {
 }
 template <class R> static R area_total_weight(const Scene<R>& sc, V3<R> p, V3<R> n) {
     R total = 0;
-    for (uint32_t i = 0; i < sc.light_count; ++i) total += area_weight(p, n, sc.lights[i]);
+    for (uint32_t i = 0; i < sc.light_count; ++i)
+        if (sc.lights[i].kind == SF_LIGHT_AREA) total += area_weight(p, n, sc.lights[i]);
     return total;
 }
 template <class R> static R area_direction_pdf(const Light<R>& l, R dist2, R cos_l) {
@@ -937,6 +969,7 @@ template <class R> static V3<R> area_emission(const Scene<R>& sc, V3<R> ro, V3<R
     V3<R> L(0, 0, 0);
     for (uint32_t i = 0; i < sc.light_count; ++i) {
         const Light<R>& l = sc.lights[i];
+        if (l.kind != SF_LIGHT_AREA) continue;
         R cos_l = area_normal(l).dot(-rd);
         if (cos_l <= R(0)) continue;
         R t = area_intersection(ro, rd, l);
@@ -1019,9 +1052,47 @@ template <class R> static R bsdf_pdf(const Surface<R>& s, V3<R> v, V3<R> l, R p_
 }
 
 // make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
+// palette_sample (common.wgsl:331-362).
+template <class R> static V3<R> ramp_sample(const Coloring<R>& c, R value) {
+    const uint32_t n = c.n;
+    if (n == 0) return V3<R>(1, 1, 1);
+    if (n == 1) return c.stops[0];
+    auto mix = [&](uint32_t a, uint32_t b, R amount) {
+        R f = r_clamp(amount, R(0), R(1));
+        if (c.smooth) f = f * f * (R(3) - R(2) * f);
+        return c.stops[a] * (R(1) - f) + c.stops[b] * f;
+    };
+    R t = value * c.frequency + c.phase;
+    if (c.cyclic) t = t - std::floor(t);
+    else t = r_clamp(t, R(0), R(1));
+    if (c.gamma != R(1)) t = std::pow(t, c.gamma);
+    if (!c.positioned && !c.cyclic) {
+        R x = t * R(float(n - 1));
+        uint32_t i = std::min<uint32_t>(uint32_t(std::floor(x)), n - 2);
+        return mix(i, i + 1, x - R(float(i)));
+    }
+    R first = c.pos[0], last = c.pos[n - 1];
+    if (c.cyclic && (t < first || t >= last)) {
+        R x = t < first ? t + R(1) : t;
+        return mix(n - 1, 0, (x - last) / r_max(R(1) + first - last, R(1e-8)));
+    }
+    if (t <= first) return c.stops[0];
+    if (t >= last) return c.stops[n - 1];
+    for (uint32_t i = 0; i + 1 < n; ++i)
+        if (t < c.pos[i + 1]) return mix(i, i + 1, (t - c.pos[i]) / (c.pos[i + 1] - c.pos[i]));
+    return c.stops[n - 1];
+}
+
 template <class R> static Surface<R> make_surface(const Scene<R>& sc, V3<R> n, const Sample<R>& smp) {
     V3<R> albedo = sc.material.albedo;
     bool assigned = smp.material > 0 && smp.material <= sc.finish_count;
+    if (!assigned && sc.coloring.n) {  // pathtrace.wgsl:275-288
+        const uint32_t slot = sc.coloring.slot;
+        if (slot < 4) albedo = albedo * ramp_sample(sc.coloring, smp.traps[slot]);
+        else if (slot == 5) albedo = albedo * ramp_sample(sc.coloring, n.y * R(0.5) + R(0.5));
+        else if (slot == 4)
+            albedo = albedo * ramp_sample(sc.coloring, R(float(smp.iterations)) / r_max(R(float(sc.iteration_product)), R(1)));
+    }
     R rough = sc.material.roughness, metallic = sc.material.metallic, spec = sc.material.specular;
     V3<R> emission(0, 0, 0);
     if (assigned) {
@@ -1052,12 +1123,56 @@ template <class R> static Surface<R> make_surface(const Scene<R>& sc, V3<R> n, c
     return s;
 }
 
+// Sky lights (pathtrace.wgsl:149-215, :432-468).
+template <class R> static V3<R> environment_value(const Light<R>& l, V3<R> dir) {
+    if (dir.y >= R(0)) return mixv(l.b, l.a, r_sqrt(dir.y));
+    return mixv(l.b, l.c, r_sqrt(-dir.y));
+}
+template <class R> static R environment_probability(const Light<R>& l, R area_total) {
+    if (l.energy <= R(0)) return 0;
+    const R e = R(4) * R(PI_W) * l.energy;
+    return r_clamp(e / (e + area_total), R(0.05), R(1));
+}
+template <class R>
+static V3<R> environment_emission(const Scene<R>& sc, V3<R> dir, R pdf, bool use_mis, V3<R> n, R area_total) {
+    V3<R> L(0, 0, 0);
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        const Light<R>& l = sc.lights[i];
+        if (l.kind != SF_LIGHT_ENVIRONMENT) continue;
+        R w = 1;
+        if (use_mis) w = mis_power(pdf, environment_probability(l, area_total) * r_max(n.dot(dir), R(0)) / R(PI_W));
+        L = L + environment_value(l, dir) * w;
+    }
+    return L;
+}
+template <class R> static R sun_pdf(R cos_max) { return R(1) / (R(2) * R(PI_W) * r_max(R(1) - cos_max, R(1e-7))); }
+template <class R> static V3<R> sun_radiance(const Scene<R>& sc, V3<R> dir, R pdf_bsdf, bool use_mis) {
+    V3<R> L(0, 0, 0);
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        const Light<R>& l = sc.lights[i];
+        if (l.kind != SF_LIGHT_SUN || dir.dot(l.a) < l.cos_max) continue;
+        R pl = sun_pdf(l.cos_max);
+        R w = use_mis ? mis_power(pdf_bsdf, pl) : R(1);
+        L = L + l.color * (pl * w);
+    }
+    return L;
+}
+template <class R> static V3<R> cone_sample(V3<R> dir, R cos_max, R r1, R r2) {
+    R cos_t = R(1) - r1 * (R(1) - cos_max);
+    R sin_t = r_sqrt(r_max(R(0), R(1) - cos_t * cos_t));
+    R phi = R(2) * R(PI_W) * r2;
+    V3<R> t, bt;
+    tangent_frame(dir, &t, &bt);
+    return t * (sin_t * r_cos(phi)) + bt * (sin_t * r_sin(phi)) + dir * cos_t;
+}
+
 // trace_geometry_lights (lights.wgsl:183-209) around march_segment.
 template <class R>
 static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd, R pixel_cone, R t_end, uint64_t* evals) {
     R nearest = t_end;
     uint32_t light_index = 0xffffffffu;
     for (uint32_t i = 0; i < sc.light_count; ++i) {
+        if (sc.lights[i].kind != SF_LIGHT_AREA) continue;
         R t = area_intersection(ro, rd, sc.lights[i]);
         if (t < nearest) { nearest = t; light_index = i; }
     }
@@ -1072,7 +1187,7 @@ static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd
 }
 
 // radiance (pathtrace.wgsl:802-1201) with fog, optics, ocean, portals, guiding,
-// textures, sun and environment disabled (those branches are identities when off),
+// textures and HDRI disabled (those branches are identities when off),
 // camera_ray (:781-800) and the per-sample film terms of main (:1203-1276).
 template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint32_t px, uint32_t py, uint32_t sample) {
     PixelResult res{};
@@ -1113,7 +1228,12 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
             }
             if (bounce == 0) { first_depth = h.t; aux[0] = gn.x; aux[1] = gn.y; aux[2] = gn.z; aux[3] = R(h.steps); }
         }
-        if (!h.hit) break;  // no environment: a miss adds nothing
+        if (!h.hit) {  // the sky (pathtrace.wgsl:1026-1040)
+            if (!h.exhausted)
+                L = L + throughput * (environment_emission(sc, rd, prev_pdf, prev_from_bsdf, prev_normal, prev_area_total) +
+                                      sun_radiance(sc, rd, prev_pdf, prev_from_bsdf));
+            break;
+        }
         V3<R> p = ro + rd * h.t;
         if (h.light_index != 0xffffffffu) {
             if (bounce == 0) {
@@ -1140,7 +1260,8 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
         R p_spec = spec_probability(s, nv);
         R area_total = area_total_weight(sc, p_off, s.n);
         bool last = bounce == sc.max_bounces;
-        // direct_light (pathtrace.wgsl:471-558), area emitters.
+        // direct_light (pathtrace.wgsl:471-558): the area light selected by weight,
+        // then every light in scene order; each clear shadow segment adds its radiance.
         {
             uint32_t selected = 0xffffffffu;
             R selected_weight = 0;
@@ -1148,6 +1269,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                 R threshold = rnd<R>(&rng) * area_total;
                 R sum = 0;
                 for (uint32_t i = 0; i < sc.light_count; ++i) {
+                    if (sc.lights[i].kind != SF_LIGHT_AREA) continue;
                     R w = area_weight(p_off, s.n, sc.lights[i]);
                     sum += w;
                     if (w > R(0)) {
@@ -1157,34 +1279,59 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     }
                 }
             }
-            V3<R> Ld(0, 0, 0);
-            if (selected != 0xffffffffu) {
-                const Light<R>& l = sc.lights[selected];
-                R u1 = rnd<R>(&rng);
-                R u2 = rnd<R>(&rng);
-                V3<R> q = l.a + l.b * (u1 - R(0.5)) + l.c * (u2 - R(0.5));
-                V3<R> ln = area_normal(l);
-                V3<R> to_q = q - p_off;
-                R dist2 = to_q.dot(to_q);
-                if (dist2 >= R(1e-8)) {
+            auto visible = [&](V3<R> dir, R t_end) {
+                Hit<R> sh = trace_scene(g, sc, p_off, dir, pixel_cone, t_end, &res.de_evals);
+                res.segments++;
+                return !sh.hit && !sh.exhausted;
+            };
+            for (uint32_t i = 0; i < sc.light_count; ++i) {
+                const Light<R>& l = sc.lights[i];
+                if (l.kind == SF_LIGHT_ENVIRONMENT) {
+                    if (l.peak <= R(0)) continue;
+                    R probability = environment_probability(l, area_total);
+                    if (rnd<R>(&rng) >= probability) continue;
+                    R r1 = rnd<R>(&rng);
+                    R r2 = rnd<R>(&rng);
+                    V3<R> ldir = cosine_sample(s.n, r1, r2);
+                    R nl = r_max(s.n.dot(ldir), R(0));
+                    if (n.dot(ldir) <= R(0) || nl <= R(0)) continue;
+                    if (!visible(ldir, extent)) continue;
+                    R pl = probability * nl / R(PI_W);
+                    R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
+                    R w = last ? R(1) : mis_power(pl, pb);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * w / pl);
+                } else if (l.kind == SF_LIGHT_SUN) {
+                    R r1 = rnd<R>(&rng);
+                    R r2 = rnd<R>(&rng);
+                    V3<R> ldir = cone_sample(l.a, l.cos_max, r1, r2);
+                    R nl = s.n.dot(ldir);
+                    if (nl <= R(0) || n.dot(ldir) <= R(0)) continue;
+                    if (!visible(ldir, extent)) continue;
+                    R pl = sun_pdf(l.cos_max);
+                    R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
+                    R w = last ? R(1) : mis_power(pl, pb);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * w);
+                } else if (i == selected) {
+                    R u1 = rnd<R>(&rng);
+                    R u2 = rnd<R>(&rng);
+                    V3<R> q = l.a + l.b * (u1 - R(0.5)) + l.c * (u2 - R(0.5));
+                    V3<R> ln = area_normal(l);
+                    V3<R> to_q = q - p_off;
+                    R dist2 = to_q.dot(to_q);
+                    if (dist2 < R(1e-8)) continue;
                     R dist = r_sqrt(dist2);
                     V3<R> ldir = to_q / dist;
                     R nl = s.n.dot(ldir);
                     R cos_l = ln.dot(-ldir);
-                    if (!(nl <= R(0) || cos_l <= R(0) || n.dot(ldir) <= R(0))) {
-                        R endpoint = r_max(R(0), dist - r_max(R(1e-5), dist * R(1e-6)));
-                        Hit<R> sh = trace_scene(g, sc, p_off, ldir, pixel_cone, endpoint, &res.de_evals);
-                        res.segments++;
-                        if (!sh.hit && !sh.exhausted) {
-                            R pl = (selected_weight / area_total) * area_direction_pdf(l, dist2, cos_l);
-                            R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
-                            R w = last ? R(1) : mis_power(pl, pb);
-                            Ld = brdf_eval(s, v, ldir) * nl * l.color * R(1) * w / pl;
-                        }
-                    }
+                    if (nl <= R(0) || cos_l <= R(0) || n.dot(ldir) <= R(0)) continue;
+                    R endpoint = r_max(R(0), dist - r_max(R(1e-5), dist * R(1e-6)));
+                    if (!visible(ldir, endpoint)) continue;
+                    R pl = (selected_weight / area_total) * area_direction_pdf(l, dist2, cos_l);
+                    R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
+                    R w = last ? R(1) : mis_power(pl, pb);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * R(1) * w / pl);
                 }
             }
-            L = L + throughput * Ld;
         }
         if (last) break;
         R r0 = rnd<R>(&rng), r1 = rnd<R>(&rng), r2 = rnd<R>(&rng);

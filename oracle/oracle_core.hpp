@@ -191,7 +191,16 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast = false
 
 // ---------------------------------------------------------------- transport
 template <class R> struct Camera { V3<R> origin, forward, right, up; R tan_half, aspect, lens_radius, focus_distance; };
-template <class R> struct Light { V3<R> a, b, c, color; };
+// kind 0 Area: a centre, b/c full edges, color radiance; 1 Sun: a unit direction,
+// color irradiance, cos_max; 2 Environment: a/b/c zenith/horizon/ground radiance.
+template <class R> struct Light { V3<R> a, b, c, color; uint32_t kind = 0; R cos_max = 1, energy = 0, peak = 0; };
+template <class R> struct Coloring {
+    uint32_t slot = 0xffff, n = 0;
+    bool cyclic = false, smooth = false, positioned = false;
+    R frequency = 1, phase = 0, gamma = 1;
+    V3<R> stops[SF_MAX_RAMP_STOPS];
+    R pos[SF_MAX_RAMP_STOPS];
+};
 template <class R> struct Mat { V3<R> albedo; R roughness, metallic, specular; V3<R> emission; };
 template <class R> struct Scene {
     Camera<R> cam;
@@ -200,6 +209,7 @@ template <class R> struct Scene {
     uint32_t finish_count = 0;
     Light<R> lights[SF_MAX_LIGHTS];
     uint32_t light_count = 0;
+    Coloring<R> coloring;
     uint32_t variation_slot = 0, variation_enabled = 0;
     R var_rough[2] = {0, 0}, var_metal[2] = {0, 0};
     R cavity = 0;

@@ -75,9 +75,24 @@ class sf_material(C.Structure):
                 ("specular", C.c_float), ("emission", C.c_float * 3)]
 
 
+SF_LIGHT_AREA, SF_LIGHT_SUN, SF_LIGHT_ENVIRONMENT = 0, 1, 2
+SF_MAX_RAMP_STOPS = 16
+
+
 class sf_area_light(C.Structure):
     _fields_ = [("center", C.c_float * 3), ("edge_u", C.c_float * 3), ("edge_v", C.c_float * 3),
-                ("radiance", C.c_float * 3)]
+                ("radiance", C.c_float * 3), ("kind", C.c_uint32), ("direction", C.c_float * 3),
+                ("angular_size", C.c_float), ("zenith", C.c_float * 3), ("horizon", C.c_float * 3),
+                ("ground", C.c_float * 3)]
+
+
+sf_light = sf_area_light
+
+
+class sf_coloring(C.Structure):
+    _fields_ = [("slot", C.c_uint32), ("stop_count", C.c_uint32), ("stops", (C.c_float * 4) * SF_MAX_RAMP_STOPS),
+                ("cyclic", C.c_uint32), ("smooth", C.c_uint32), ("positioned", C.c_uint32),
+                ("frequency", C.c_float), ("phase", C.c_float), ("gamma", C.c_float)]
 
 
 class sf_scene_desc(C.Structure):
@@ -86,7 +101,7 @@ class sf_scene_desc(C.Structure):
                 ("lights", sf_area_light * SF_MAX_LIGHTS), ("light_count", C.c_uint32),
                 ("variation_slot", C.c_uint32), ("variation_enabled", C.c_uint32),
                 ("variation_roughness", C.c_float * 2), ("variation_metallic", C.c_float * 2),
-                ("cavity_darkness", C.c_float), ("seed", C.c_uint64)]
+                ("cavity_darkness", C.c_float), ("seed", C.c_uint64), ("coloring", sf_coloring)]
 
 
 class sf_render_config(C.Structure):

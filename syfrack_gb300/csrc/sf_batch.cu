@@ -35,7 +35,7 @@ __global__ void __launch_bounds__(256) k_shade_batch(BatchTable bt, PathSoA soa,
         const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
         uint32_t nf = shade_path(*job.scene, soa, job.geom, job.film, path - job.path_begin, path, status,
                                  final_round);
-        if (!final_round) enqueue_next(q, nf, path);
+        if (!final_round) enqueue_next(q, soa, nf, path);
     }
 }
 

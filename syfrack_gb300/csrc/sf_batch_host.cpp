@@ -26,13 +26,14 @@ namespace sfh {
 
 // Carves an arena for `capacity` paths and `max_jobs` jobs out of one allocation.
 sf_status arena_alloc(sf_context* c, WaveArena& a, uint32_t capacity, uint32_t max_jobs, uint32_t rounds,
-                      size_t extra_bytes, size_t* extra_offset) {
+                      uint32_t shadow_slots, size_t extra_bytes, size_t* extra_offset) {
     const size_t N = capacity;
+    const uint32_t K = std::max<uint32_t>(shadow_slots, 1);
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
     size_t o_jobs = take(size_t(max_jobs) * sizeof(BatchJob));
-    size_t o_Ls = take(N * 16), o_soa = take(N * 16 * 12), o_lists = take(N * 4 * 6);
-    size_t o_march = take(2 * N * (16 + 16 + 4)), o_resume = take(2 * 2 * N * 4);
+    size_t o_Ls = take(N * 16), o_soa = take(wave_soa_bytes(N, K)), o_lists = take(wave_lists_bytes(N, K));
+    size_t o_march = take(wave_march_bytes(N, K)), o_resume = take(wave_resume_bytes(N, K));
     size_t o_counts = take(size_t(rounds + 1) * 16), o_qcounts = take(size_t(rounds) * 64 * 8), o_status = take(16);
     size_t o_extra = take(extra_bytes);
     sf_status st = ctx_alloc(c, off, &a.mem);
@@ -43,25 +44,8 @@ sf_status arena_alloc(sf_context* c, WaveArena& a, uint32_t capacity, uint32_t m
     a.capacity = capacity;
     a.max_jobs = max_jobs;
     a.rounds = rounds;
+    wave_bind(a.soa, base + o_soa, base + o_march, capacity, K);
     a.soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
-    float4* p = reinterpret_cast<float4*>(base + o_soa);
-    a.soa.o = p; p += N;
-    a.soa.d = p; p += N;
-    a.soa.tp = p; p += N;
-    a.soa.L = p; p += N;
-    a.soa.pn = p; p += N;
-    a.soa.sh_o = p; p += N;
-    a.soa.sh_d = p; p += N;
-    a.soa.sh_c = p; p += N;
-    a.soa.hit = reinterpret_cast<uint4*>(p); p += N;
-    a.soa.hit_tr = p; p += N;
-    a.soa.hit_n = p; p += N;
-    a.soa.vis = reinterpret_cast<uint32_t*>(p);
-    float4* m = reinterpret_cast<float4*>(base + o_march);
-    a.soa.m0 = m;
-    a.soa.m1 = m + 2 * N;
-    a.soa.m2 = reinterpret_cast<uint32_t*>(m + 4 * N);
-    a.soa.capacity = capacity;
     a.lists = reinterpret_cast<uint32_t*>(base + o_lists);
     a.resume = reinterpret_cast<uint32_t*>(base + o_resume);
     a.counts = reinterpret_cast<uint32_t*>(base + o_counts);
@@ -83,26 +67,18 @@ sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, b
         CU(sf_launch_generate_batch(a.bt, a.soa, a.counts, st));
     }
     const int blocks = int(a.min_blocks) * c->sm_count;
+    const uint32_t K = a.soa.shadow_slots;
     for (uint32_t r = 0; r < R; ++r) {
-        uint32_t cur = r & 1, nxt = cur ^ 1;
         RoundQueues q;
-        q.active = r == 0 ? nullptr : a.lists + (cur * 3 + 0) * N;
-        q.cont = r == 0 ? nullptr : a.lists + (cur * 3 + 1) * N;
-        q.shadow = a.lists + (cur * 3 + 2) * N;
-        q.counts = a.counts + 4 * r;
-        q.next_active = a.lists + (nxt * 3 + 0) * N;
-        q.next_cont = a.lists + (nxt * 3 + 1) * N;
-        q.next_shadow = a.lists + (nxt * 3 + 2) * N;
-        q.next_counts = a.counts + 4 * (r + 1);
-        q.work_counter = a.counts + 4 * r + 3;
+        wave_round_queues(q, a.lists, N, K, r, a.counts);
         for (uint32_t j = 0; j < Q; ++j) {
             TraceLaunch tl;
             tl.q = q;
             uint32_t* qc = a.qcounts + (size_t(r) * 64 + j) * 2;
             tl.work_counter = qc;
-            tl.resume = j == 0 ? nullptr : a.resume + size_t((j - 1) & 1) * 2 * N;
+            tl.resume = j == 0 ? nullptr : wave_resume(a.resume, N, K, j - 1);
             tl.resume_count = j == 0 ? nullptr : qc - 2 + 1;
-            tl.next_resume = a.resume + size_t(j & 1) * 2 * N;
+            tl.next_resume = wave_resume(a.resume, N, K, j);
             tl.next_resume_count = qc + 1;
             tl.quantum = j + 1 == Q ? 0u : a.quantum;
             tl.regen = a.regen;
@@ -157,8 +133,7 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
         if (!jobs[i].graph || jobs[i].graph->ctx != c) return fail(SF_ERR_INVALID, "job graph missing or of another context");
         sf_status st = validate_config(jobs[i].cfg);
         if (st != SF_OK) return st;
-        if (jobs[i].scene.light_count > SF_MAX_LIGHTS || jobs[i].scene.finish_count > SF_MAX_FINISHES)
-            return fail(SF_ERR_INVALID, "too many lights or finishes");
+        if (const sf_status sc = scene_check(jobs[i].scene); sc != SF_OK) return sc;
         const sf_render_config& cf = jobs[i].cfg;
         uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
                                                    cf.samples_per_pixel), 1);
@@ -175,7 +150,13 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     b->ctx = c;
     const size_t scene_bytes = (n * sizeof(DevScene) + 255) & ~size_t(255);
     size_t extra = 0;
-    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, scene_bytes + film_bytes, &extra);
+    uint32_t K = 1;  // the most shadow segments one bounce of any job issues
+    for (uint32_t i = 0; i < n; ++i) {
+        uint32_t k = 1;
+        for (uint32_t l = 0; l < jobs[i].scene.light_count; ++l) k += jobs[i].scene.lights[l].kind != SF_LIGHT_AREA;
+        K = std::max(K, k);
+    }
+    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, K, scene_bytes + film_bytes, &extra);
     if (st != SF_OK) { delete b; return st; }
     b->a.max_steps = max_steps;
     b->a.any_generic = generic;

@@ -127,8 +127,7 @@ sf_status export_alloc(sf_context* c, sf_graph* g, const sf_scene_desc& scene, c
                        sf_export** out) {
     sf_status st = validate_config(cfg);
     if (st != SF_OK) return st;
-    if (scene.light_count > SF_MAX_LIGHTS || scene.finish_count > SF_MAX_FINISHES)
-        return fail(SF_ERR_INVALID, "too many lights or finishes");
+    if (const sf_status sc = scene_check(scene); sc != SF_OK) return sc;
     cudaSetDevice(c->device);
     auto* w = new sf_session();
     w->ctx = c;

@@ -815,7 +815,37 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     return SF_OK;
 }
 
+sf_status scene_check(const sf_scene_desc& d) {
+    if (d.light_count > SF_MAX_LIGHTS || d.finish_count > SF_MAX_FINISHES)
+        return fail(SF_ERR_INVALID, "too many lights or finishes");
+    for (uint32_t i = 0; i < d.light_count; ++i)
+        if (d.lights[i].kind > SF_LIGHT_ENVIRONMENT) return fail(SF_ERR_UNSUPPORTED, "light kind not built on the device");
+    if (d.coloring.slot == 6 && d.coloring.stop_count)
+        return fail(SF_ERR_UNSUPPORTED, "orbit colouring is not built on the device");
+    if (d.coloring.stop_count > SF_MAX_RAMP_STOPS) return fail(SF_ERR_INVALID, "more than 16 ramp stops");
+    return SF_OK;
+}
 void light_dev(const sf_area_light& l, DevLight& o) {
+    std::memset(&o, 0, sizeof o);
+    o.kind = l.kind;
+    auto lum = [](const float* c) { return c[0] * 0.2126f + c[1] * 0.7152f + c[2] * 0.0722f; };
+    if (l.kind == SF_LIGHT_SUN) {
+        // GpuLight::from_light (uniforms.rs:656-668): normalised direction, cos of the half angle
+        std::memcpy(o.a, l.direction, 12);
+        std::memcpy(o.color, l.radiance, 12);
+        o.cos_max = cosf((l.angular_size * 0.5f) * (3.14159265f / 180.0f));
+        return;
+    }
+    if (l.kind == SF_LIGHT_ENVIRONMENT) {
+        std::memcpy(o.a, l.zenith, 12);
+        std::memcpy(o.b, l.horizon, 12);
+        std::memcpy(o.c, l.ground, 12);
+        o.energy = std::max(std::max(lum(l.zenith), lum(l.horizon)), lum(l.ground));
+        float peak = 0.0f;
+        for (int k = 0; k < 3; ++k) peak = std::max({peak, l.zenith[k], l.horizon[k], l.ground[k]});
+        o.peak = peak;
+        return;
+    }
     std::memcpy(o.a, l.center, 12);
     std::memcpy(o.b, l.edge_u, 12);
     std::memcpy(o.c, l.edge_v, 12);
@@ -832,7 +862,7 @@ void light_dev(const sf_area_light& l, DevLight& o) {
     float cc = l.edge_v[0] * l.edge_v[0] + l.edge_v[1] * l.edge_v[1] + l.edge_v[2] * l.edge_v[2];
     o.inv_bb = 1.0f / bb;
     o.inv_cc = 1.0f / cc;
-    o.lum = l.radiance[0] * 0.2126f + l.radiance[1] * 0.7152f + l.radiance[2] * 0.0722f;
+    o.lum = lum(l.radiance);
 }
 void material_dev(const sf_material& m, DevMaterial& o) {
     std::memcpy(o.albedo, m.albedo, 12);
@@ -876,7 +906,22 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     S.iteration_product = gi.iteration_product;
     material_dev(d.material, S.material);
     for (uint32_t i = 0; i < S.finish_count; ++i) material_dev(d.finishes[i], S.finishes[i]);
-    for (uint32_t i = 0; i < S.light_count; ++i) light_dev(d.lights[i], S.lights[i]);
+    uint32_t shadows = 1;  // the selected area light
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        light_dev(d.lights[i], S.lights[i]);
+        if (d.lights[i].kind != SF_LIGHT_AREA) shadows++;
+    }
+    S.shadow_slots = shadows;
+    const sf_coloring& col = d.coloring;
+    S.col_slot = col.slot;
+    S.col_n = std::min<uint32_t>(col.stop_count, SF_MAX_RAMP);
+    S.col_cyclic = col.cyclic;
+    S.col_smooth = col.smooth;
+    S.col_positioned = col.positioned;
+    S.col_map[0] = col.frequency;
+    S.col_map[1] = col.phase;
+    S.col_map[2] = col.gamma;
+    std::memcpy(S.col_stops, col.stops, sizeof S.col_stops);
 }
 
 }  // namespace sfh
@@ -1238,11 +1283,16 @@ sf_status session_alloc(sf_session* s) {
     size_t o_acc = take(px * 16), o_depth = take(px * 4), o_aux = take(px * 16);
     size_t o_Ls = take(N * 16);
     size_t o_soa = 0, o_lists = 0, o_march = 0, o_resume = 0;
+    // shadow segments one bounce may issue: the selected area light, each sun and sky
+    uint32_t K = 1;
+    for (uint32_t i = 0; i < std::min<uint32_t>(s->scene.light_count, SF_MAX_LIGHTS); ++i)
+        if (s->scene.lights[i].kind != SF_LIGHT_AREA) K++;
+    s->shadow_slots = K;
     if (wf) {
-        o_soa = take(N * 16 * 11 + N * 16);  // 11 float4/uint4 planes + vis (padded)
-        o_lists = take(N * 4 * 6);
-        o_march = take(2 * N * (16 + 16 + 4));  // m0, m1, m2 for continuation and shadow rows
-        o_resume = take(2 * 2 * N * 4);
+        o_soa = take(wave_soa_bytes(N, K));
+        o_lists = take(wave_lists_bytes(N, K));
+        o_march = take(wave_march_bytes(N, K));
+        o_resume = take(wave_resume_bytes(N, K));
     }
     size_t o_counts = take(size_t(R + 1) * 4 * 4);
     size_t o_qcounts = take(size_t(R) * 64 * 2 * 4);
@@ -1258,29 +1308,14 @@ sf_status session_alloc(sf_session* s) {
     s->film.width = fw;
     s->film.height = fh;
     std::memset(&s->soa, 0, sizeof s->soa);
-    s->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
     s->soa.capacity = s->capacity;
+    s->soa.shadow_slots = K;
     if (wf) {
-        float4* p = reinterpret_cast<float4*>(base + o_soa);
-        s->soa.o = p; p += N;
-        s->soa.d = p; p += N;
-        s->soa.tp = p; p += N;
-        s->soa.L = p; p += N;
-        s->soa.pn = p; p += N;
-        s->soa.sh_o = p; p += N;
-        s->soa.sh_d = p; p += N;
-        s->soa.sh_c = p; p += N;
-        s->soa.hit = reinterpret_cast<uint4*>(p); p += N;
-        s->soa.hit_tr = p; p += N;
-        s->soa.hit_n = p; p += N;
-        s->soa.vis = reinterpret_cast<uint32_t*>(p);
+        wave_bind(s->soa, base + o_soa, base + o_march, s->capacity, K);
         s->lists = reinterpret_cast<uint32_t*>(base + o_lists);
-        float4* m = reinterpret_cast<float4*>(base + o_march);
-        s->soa.m0 = m;
-        s->soa.m1 = m + 2 * N;
-        s->soa.m2 = reinterpret_cast<uint32_t*>(m + 4 * N);
         s->resume = reinterpret_cast<uint32_t*>(base + o_resume);
     }
+    s->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
     s->counts = reinterpret_cast<uint32_t*>(base + o_counts);
     s->qcounts = reinterpret_cast<uint32_t*>(base + o_qcounts);
     s->status = reinterpret_cast<uint32_t*>(base + o_status);
@@ -1302,8 +1337,7 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
     *out = nullptr;
     sf_status st = validate_config(*cfg);
     if (st != SF_OK) return st;
-    if (scene->light_count > SF_MAX_LIGHTS || scene->finish_count > SF_MAX_FINISHES)
-        return fail(SF_ERR_INVALID, "too many lights or finishes");
+    if (const sf_status sc = scene_check(*scene); sc != SF_OK) return sc;
     cudaSetDevice(c->device);
     auto* s = new sf_session();
     s->ctx = c;
@@ -1377,26 +1411,18 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
         CU(sf_launch_generate(s->d_scene, s->soa, g, s->counts, st));
     }
     const int blocks = int(s->min_blocks) * c->sm_count;
+    const uint32_t K = s->shadow_slots;
     for (uint32_t r = 0; r < R; ++r) {
-        uint32_t cur = r & 1, nxt = cur ^ 1;
         RoundQueues q;
-        q.active = r == 0 ? nullptr : s->lists + (cur * 3 + 0) * N;
-        q.cont = r == 0 ? nullptr : s->lists + (cur * 3 + 1) * N;
-        q.shadow = s->lists + (cur * 3 + 2) * N;
-        q.counts = s->counts + 4 * r;
-        q.next_active = s->lists + (nxt * 3 + 0) * N;
-        q.next_cont = s->lists + (nxt * 3 + 1) * N;
-        q.next_shadow = s->lists + (nxt * 3 + 2) * N;
-        q.next_counts = s->counts + 4 * (r + 1);
-        q.work_counter = s->counts + 4 * r + 3;
+        wave_round_queues(q, s->lists, N, K, r, s->counts);
         for (uint32_t j = 0; j < Q; ++j) {
             TraceLaunch tl;
             tl.q = q;
             uint32_t* qc = s->qcounts + (size_t(r) * 64 + j) * 2;
             tl.work_counter = qc;
-            tl.resume = j == 0 ? nullptr : s->resume + size_t((j - 1) & 1) * 2 * N;
+            tl.resume = j == 0 ? nullptr : wave_resume(s->resume, N, K, j - 1);
             tl.resume_count = j == 0 ? nullptr : qc - 2 + 1;  // previous launch's resumed count
-            tl.next_resume = s->resume + size_t(j & 1) * 2 * N;
+            tl.next_resume = wave_resume(s->resume, N, K, j);
             tl.next_resume_count = qc + 1;
             tl.quantum = j + 1 == Q ? 0u : s->quantum;  // the last launch runs segments to completion
             tl.regen = s->regen;

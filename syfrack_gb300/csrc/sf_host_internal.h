@@ -127,10 +127,61 @@ struct LaunchTimer {
 float sqrt_threshold(float b);
 void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph_info& gi, DevScene& S);
 sf_status validate_config(const sf_render_config& c);
+// Scene limits and the light kinds and colouring the device path supports.
+sf_status scene_check(const sf_scene_desc& d);
 sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen);
 void planar_dev(const sf_planar_desc& f, PlanarDev& o);
 sf_status planar_check(const sf_planar_desc* f);
 cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);
+
+// Wavefront path state for N paths with K shadow slots (a bounce issues at most K
+// shadow segments): eight path planes, K sets of shadow planes and visibility words,
+// march rows for the continuation (row = path) and each shadow (row = N + k*N + path),
+// round lists (active, continuation, K*N shadow rows) in two parities, and two
+// resume lists of (1 + K) * N items.
+inline size_t wave_soa_bytes(size_t N, uint32_t K) { return N * 16 * 8 + size_t(K) * N * (16 * 3 + 4); }
+inline size_t wave_march_bytes(size_t N, uint32_t K) { return (1 + size_t(K)) * N * (16 + 16 + 4); }
+inline size_t wave_lists_bytes(size_t N, uint32_t K) { return 2 * (2 + size_t(K)) * N * 4; }
+inline size_t wave_resume_bytes(size_t N, uint32_t K) { return 2 * (1 + size_t(K)) * N * 4; }
+inline void wave_bind(PathSoA& soa, void* soa_mem, void* march_mem, uint32_t N, uint32_t K) {
+    float4* p = static_cast<float4*>(soa_mem);
+    soa.o = p; p += N;
+    soa.d = p; p += N;
+    soa.tp = p; p += N;
+    soa.L = p; p += N;
+    soa.pn = p; p += N;
+    soa.hit = reinterpret_cast<uint4*>(p); p += N;
+    soa.hit_tr = p; p += N;
+    soa.hit_n = p; p += N;
+    soa.sh_o = p; p += size_t(K) * N;
+    soa.sh_d = p; p += size_t(K) * N;
+    soa.sh_c = p; p += size_t(K) * N;
+    soa.vis = reinterpret_cast<uint32_t*>(p);
+    float4* m = static_cast<float4*>(march_mem);
+    const size_t rows = (1 + size_t(K)) * N;
+    soa.m0 = m;
+    soa.m1 = m + rows;
+    soa.m2 = reinterpret_cast<uint32_t*>(m + 2 * rows);
+    soa.capacity = N;
+    soa.shadow_slots = K;
+}
+inline void wave_round_queues(RoundQueues& q, uint32_t* lists, size_t N, uint32_t K, uint32_t r, uint32_t* counts) {
+    const size_t stride = (2 + size_t(K)) * N;
+    uint32_t* cur = lists + (r & 1) * stride;
+    uint32_t* nxt = lists + ((r & 1) ^ 1) * stride;
+    q.active = r == 0 ? nullptr : cur;
+    q.cont = r == 0 ? nullptr : cur + N;
+    q.shadow = cur + 2 * N;
+    q.counts = counts + 4 * r;
+    q.next_active = nxt;
+    q.next_cont = nxt + N;
+    q.next_shadow = nxt + 2 * N;
+    q.next_counts = counts + 4 * (r + 1);
+    q.work_counter = counts + 4 * r + 3;
+}
+inline uint32_t* wave_resume(uint32_t* resume, size_t N, uint32_t K, uint32_t parity) {
+    return resume + size_t(parity & 1) * (1 + size_t(K)) * N;
+}
 
 // Device storage of one batched wavefront: the job table, path state and queues.
 struct WaveArena {
@@ -149,7 +200,7 @@ struct WaveArena {
 };
 
 sf_status arena_alloc(sf_context* c, WaveArena& a, uint32_t capacity, uint32_t max_jobs, uint32_t rounds,
-                      size_t extra_bytes, size_t* extra_offset);
+                      uint32_t shadow_slots, size_t extra_bytes, size_t* extra_offset);
 sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, bool timed);
 
 }  // namespace sfh
@@ -177,6 +228,7 @@ struct sf_session {
     uint32_t status_host = 0;
     double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
     bool window = false;       // tiled export: a tile-sized film whose origin the export sets
+    uint32_t shadow_slots = 1; // shadow segments a bounce may issue (1 + suns + skies)
 };
 
 namespace sfh {

@@ -181,7 +181,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene* __restrict__ scen
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         uint32_t path = q.active ? q.active[j] : j;
         uint32_t nf = shade_path(S, soa, g, film, path, path, status, final_round);
-        if (!final_round) enqueue_next(q, nf, path);
+        if (!final_round) enqueue_next(q, soa, nf, path);
     }
 }
 
@@ -300,9 +300,9 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 fd = nullptr;
                 fa = nullptr;
             }
-            ShadowReq sh;
-            int cont = bounce_body(S, ps, h, sh, fd, fa);
-            if (sh.active) {
+            // each shadow segment is traced as it is issued; its radiance lands in the
+            // order the wavefront adds it (issue order, after the bounce's own terms)
+            auto emit = [&](const ShadowReq& sh) {
                 uint32_t sli;
                 March sm;
                 float st_end = nearest_emitter(S, sh.o, sh.dir, sh.t_end, sli);
@@ -310,8 +310,9 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 DeRaw shs;
                 int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, shs, evals, iters);
                 segs++;
-                if (sr == MARCH_MISS && sli == SF_NO_LIGHT) ps.L = ps.L + sh.contrib;
-            }
+                if (sr == MARCH_MISS && sli == SF_NO_LIGHT) ps.L = add_rn(ps.L, sh.contrib);
+            };
+            int cont = bounce_body(S, ps, h, emit, fd, fa);
             if (cont != PATH_CONTINUE) break;
         }
         soa.Ls[(size_t)s * tile_px + local] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);

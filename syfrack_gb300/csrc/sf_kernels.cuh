@@ -7,6 +7,7 @@
 
 // Path flags kept in the path state.
 enum { SF_PF_CONT = 1u, SF_PF_SHADOW = 2u, SF_PF_FROM_BSDF = 4u };
+#define SF_PF_SHADOW_SHIFT 8  // bits 8..15 of the flags: which shadow slots hold a segment
 // Hit record flags.
 enum { SF_HF_HIT = 1u, SF_HF_EXHAUSTED = 2u };
 // Wavefront invariant word (wavefront.wgsl:183/:220/:236 bits 1, 2, 4).
@@ -34,12 +35,13 @@ struct PathSoA {
     float4* hit_n;   // normal, w = bits(iterations | material << 16)
     uint32_t* vis;   // shadow visibility (1 = clear)
     float4* Ls;      // per-path final radiance (committed in ascending sample order)
-    // resumable march state of a segment cut at the step quantum (one row per path
-    // and segment kind: continuation rows [0, capacity), shadow rows [capacity, 2*capacity))
+    // resumable march state of a segment cut at the step quantum: continuation rows
+    // [0, capacity), shadow rows capacity + [0, K * capacity)
     float4* m0;      // t, omega, prev_radius, step_len
     float4* m1;      // t_end, cand_t, cand_err, bits(steps)
     uint32_t* m2;    // light index ahead of the segment
     uint32_t capacity;
+    uint32_t shadow_slots;  // K: sh_o/sh_d/sh_c/vis have K * capacity rows (row = k * capacity + path)
 };
 
 // Queues of one round: active paths, continuation rays, shadow rays (ids),
@@ -58,7 +60,8 @@ struct RoundQueues {
 
 // One launch of the persistent trace kernel: the round's fresh segments
 // (continuations then shadows) or the segments resumed after a step quantum.
-// Item encoding in resume lists: path | (shadow ? 1u << 31 : 0).
+// Item encoding: continuation lists hold paths, shadow lists shadow rows
+// (k * capacity + path); resume lists hold path or shadow row | (shadow ? 1u << 31 : 0).
 struct TraceLaunch {
     RoundQueues q;
     const uint32_t* resume;       // null on the first launch of a round

@@ -72,8 +72,7 @@ extern "C" sf_status sf_preview_create(sf_context* c, sf_graph* g, const sf_scen
     *out = nullptr;
     if (!width || !height || uint64_t(width) * height > (1u << 26)) return fail(SF_ERR_INVALID, "preview size");
     if (quantum == 0) quantum = 128;  // QUANTUM, control/mod.rs:18
-    if (scene->light_count > SF_MAX_LIGHTS || scene->finish_count > SF_MAX_FINISHES)
-        return fail(SF_ERR_INVALID, "too many lights or finishes");
+    if (const sf_status sc = scene_check(*scene); sc != SF_OK) return sc;
     cudaSetDevice(c->device);
     auto* p = new sf_preview();
     p->ctx = c;
@@ -126,8 +125,7 @@ extern "C" sf_status sf_preview_set(sf_preview* p, sf_graph* g, const sf_scene_d
     if (!p) return fail(SF_ERR_INVALID, "null preview");
     cudaSetDevice(p->ctx->device);
     if (scene) {
-        if (scene->light_count > SF_MAX_LIGHTS || scene->finish_count > SF_MAX_FINISHES)
-            return fail(SF_ERR_INVALID, "too many lights or finishes");
+        if (const sf_status sc = scene_check(*scene); sc != SF_OK) return sc;
         p->scene = *scene;
     }
     if (g && g != p->graph) {

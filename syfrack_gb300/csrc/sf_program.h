@@ -85,13 +85,20 @@ struct DeProgram {
 
 // One area light in device form (GpuLight of uniforms.rs:671-713 with the
 // derived quantities the shading code needs every bounce).
+// kind SF_LIGHT_AREA: a = centre, b/c = full edges, color = radiance, n/area/inv_*;
+// SF_LIGHT_SUN: a = unit direction toward the sun, color = irradiance, cos_max;
+// SF_LIGHT_ENVIRONMENT: a/b/c = zenith/horizon/ground radiance, energy = their largest
+// luminance, peak = their largest component.
 struct DevLight {
     float a[3], b[3], c[3], color[3];
     float n[3];          // safe_normalize(cross(b, c))
     float area;          // |cross(b, c)|
     float inv_bb, inv_cc;// 1 / dot(b,b), 1 / dot(c,c)
     float lum;           // luminance(color)
+    uint32_t kind;
+    float cos_max, energy, peak;
 };
+#define SF_MAX_RAMP 16
 
 struct DevMaterial {
     float albedo[3], roughness, metallic, specular, emission[3];
@@ -112,6 +119,11 @@ struct DevScene {
     float pixel_tolerance, step_scale, extent;  // extent = max(200, far)
     float pixel_cone;                           // tan_half * 2 / width
     uint32_t iteration_product;
+    // Material.coloring: slot (0..3 trap, 4 iterations, 5 normal, else none) and ramp
+    uint32_t col_slot, col_n, col_cyclic, col_smooth, col_positioned;
+    float col_map[3];                 // frequency, phase, gamma
+    float col_stops[SF_MAX_RAMP][4];  // rgb, position
+    uint32_t shadow_slots;            // shadow requests a bounce can make: 1 + suns + environments
     DevMaterial material;
     DevMaterial finishes[8];
     DevLight lights[8];

@@ -164,6 +164,7 @@ struct ServeReq {
 };
 
 constexpr uint32_t kServeMaxSlots = 8;
+constexpr uint32_t kServeShadowSlots = 3;  // shadow segments per bounce the slot arenas hold
 constexpr uint32_t kServeMaxTiles = 64;  // 2D tiles per batch
 // A tile's device block starts with PlanarDev (0), CanvasDev (256) and its pixel
 // counter (512); the staging area holds the same bytes, counter zero.
@@ -579,7 +580,7 @@ extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg
         if (e == cudaSuccess)
             e = cudaHostAlloc(reinterpret_cast<void**>(&sl.stage), sl.stage_bytes, cudaHostAllocDefault);
         if (e != cudaSuccess) return bail(cuda_fail(e, "server slot"));
-        sf_status st = arena_alloc(c, sl.arena, k.path_capacity, k.max_jobs, max_rounds, 0, nullptr);
+        sf_status st = arena_alloc(c, sl.arena, k.path_capacity, k.max_jobs, max_rounds, kServeShadowSlots, 0, nullptr);
         if (st != SF_OK) return bail(st);
         sl.arena.min_blocks = k.min_blocks;
         sl.arena.quantum = k.quantum;
@@ -600,8 +601,11 @@ extern "C" sf_status sf_serve_submit(sf_server* s, const sf_request* q, uint64_t
         if (!q->graph || q->graph->ctx != s->ctx) return fail(SF_ERR_INVALID, "preview graph missing or of another context");
         sf_status st = validate_config(q->cfg);
         if (st != SF_OK) return st;
-        if (q->scene.light_count > SF_MAX_LIGHTS || q->scene.finish_count > SF_MAX_FINISHES)
-            return fail(SF_ERR_INVALID, "too many lights or finishes");
+        if (const sf_status sc = scene_check(q->scene); sc != SF_OK) return sc;
+        uint32_t shadows = 1;
+        for (uint32_t l = 0; l < q->scene.light_count; ++l) shadows += q->scene.lights[l].kind != SF_LIGHT_AREA;
+        if (shadows > kServeShadowSlots)
+            return fail(SF_ERR_UNSUPPORTED, "the server's arenas hold 3 shadow segments per bounce (area + 2 sky lights)");
         r->width = q->cfg.width;
         r->height = q->cfg.height;
         r->samples = q->cfg.samples_per_pixel;

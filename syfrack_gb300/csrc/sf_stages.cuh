@@ -71,9 +71,16 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
                                                       uint32_t* status, int final_round) {
     PathState ps;
     uint32_t flags = load_path(soa, path, ps);
-    if ((flags & SF_PF_SHADOW) && soa.vis[path]) {
-        float4 c = soa.sh_c[path];
-        ps.L = ps.L + mk3(c.x, c.y, c.z);
+    const size_t cap = soa.capacity;
+    if (flags & SF_PF_SHADOW) {  // last round's shadow segments, in slot order
+        const uint32_t mask = (flags >> SF_PF_SHADOW_SHIFT) & 0xffu;
+        for (uint32_t k = 0; k < soa.shadow_slots; ++k) {
+            const size_t row = k * cap + path;
+            if (((mask >> k) & 1u) && soa.vis[row]) {
+                const float4 c = soa.sh_c[row];
+                ps.L = add_rn(ps.L, mk3(c.x, c.y, c.z));
+            }
+        }
     }
     uint32_t nf = 0;
     if (flags & SF_PF_CONT) {
@@ -102,14 +109,19 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
             fd = film.depth + idx;
             fa = film.aux + idx;
         }
-        ShadowReq sh;
-        int r = bounce_body(S, ps, h, sh, fd, fa);
-        if (sh.active) {
-            soa.sh_o[path] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.t_end);
-            soa.sh_d[path] = make_float4(sh.dir.x, sh.dir.y, sh.dir.z, 0.f);
-            soa.sh_c[path] = make_float4(sh.contrib.x, sh.contrib.y, sh.contrib.z, 0.f);
-            nf |= SF_PF_SHADOW;
-        }
+        uint32_t n_sh = 0, sh_mask = 0;
+        auto emit = [&](const ShadowReq& sh) {  // the k-th shadow segment of this bounce
+            if (n_sh >= soa.shadow_slots) return;
+            const size_t row = n_sh * cap + path;
+            soa.sh_o[row] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.t_end);
+            soa.sh_d[row] = make_float4(sh.dir.x, sh.dir.y, sh.dir.z, 0.f);
+            soa.sh_c[row] = make_float4(sh.contrib.x, sh.contrib.y, sh.contrib.z, 0.f);
+            begin_segment(S, soa, uint32_t(cap + row), sh.o, sh.dir, sh.t_end);
+            sh_mask |= 1u << n_sh;
+            n_sh++;
+        };
+        int r = bounce_body(S, ps, h, emit, fd, fa);
+        if (sh_mask) nf |= SF_PF_SHADOW | (sh_mask << SF_PF_SHADOW_SHIFT);
         if (r == PATH_CONTINUE) nf |= SF_PF_CONT;
     }
     if (final_round && nf) {
@@ -118,18 +130,17 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
     }
     store_path(soa, path, ps, nf);
     if (nf & SF_PF_CONT) begin_segment(S, soa, path, ps.o, ps.d, S.extent);
-    if (nf & SF_PF_SHADOW) {
-        const float4 so = soa.sh_o[path], sd = soa.sh_d[path];
-        begin_segment(S, soa, path + soa.capacity, mk3(so.x, so.y, so.z), mk3(sd.x, sd.y, sd.z), so.w);
-    }
     if (!nf) soa.Ls[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
     return nf;
 }
 
-static __device__ __forceinline__ void enqueue_next(const RoundQueues& q, uint32_t nf, uint32_t path) {
+static __device__ __forceinline__ void enqueue_next(const RoundQueues& q, const PathSoA& soa, uint32_t nf,
+                                                    uint32_t path) {
     warp_append(&q.next_counts[0], q.next_active, nf != 0, path);
     warp_append(&q.next_counts[1], q.next_cont, (nf & SF_PF_CONT) != 0, path);
-    warp_append(&q.next_counts[2], q.next_shadow, (nf & SF_PF_SHADOW) != 0, path);
+    const uint32_t mask = (nf & SF_PF_SHADOW) ? (nf >> SF_PF_SHADOW_SHIFT) & 0xffu : 0u;
+    for (uint32_t k = 0; k < soa.shadow_slots; ++k)
+        warp_append(&q.next_counts[2], q.next_shadow, ((mask >> k) & 1u) != 0, k * soa.capacity + path);
 }
 
 // wf_commit (wavefront.wgsl:232-260) for one pixel: ordered per-sample film add in

@@ -145,14 +145,15 @@ __device__ __forceinline__ float area_weight(float3 p, float3 n, const DevLight&
 }
 __device__ __forceinline__ float area_total_weight(const DevScene& S, float3 p, float3 n) {
     float total = 0.0f;
-    for (uint32_t i = 0; i < S.light_count; ++i) total += area_weight(p, n, S.lights[i]);
+    for (uint32_t i = 0; i < S.light_count; ++i)
+        if (S.lights[i].kind == SF_LIGHT_AREA) total += area_weight(p, n, S.lights[i]);
     return total;
 }
 __device__ __forceinline__ float mis_power(float a, float b) {
     float scale = fmaxf(a, b);
     if (scale <= 0.0f) return 0.0f;
     float pa = wdiv(a, scale), pb = wdiv(b, scale);
-    return wdiv(pa * pa, pa * pa + pb * pb);
+    return wdiv(pa * pa, fmaf(pa, pa, pb * pb));
 }
 // Emitter hit by a continuation ray (area_emission, lights.wgsl:330-356).
 static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, float distance, float prev_pdf, bool use_mis,
@@ -160,6 +161,7 @@ static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, 
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
         const DevLight& l = S.lights[i];
+        if (l.kind != SF_LIGHT_AREA) continue;
         float cos_l = dot3(ld3(l.n), -rd);
         if (cos_l <= 0.0f) continue;
         float t = area_intersection(ro, rd, l);
@@ -181,6 +183,7 @@ __device__ __forceinline__ float nearest_emitter(const DevScene& S, float3 ro, f
     float nearest = t_end;
     li = SF_NO_LIGHT;
     for (uint32_t i = 0; i < S.light_count; ++i) {
+        if (S.lights[i].kind != SF_LIGHT_AREA) continue;
         float t = area_intersection(ro, rd, S.lights[i]);
         if (t < nearest) { nearest = t; li = i; }
     }
@@ -192,7 +195,7 @@ struct Surface {
     float3 n, diffuse, f0, emission;
     float alpha;
 };
-__device__ __forceinline__ float luminance(float3 c) { return c.x * 0.2126f + c.y * 0.7152f + c.z * 0.0722f; }
+__device__ __forceinline__ float luminance(float3 c) { return fmaf(c.z, 0.0722f, fmaf(c.x, 0.2126f, c.y * 0.7152f)); }
 __device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt) {
     float s = n.z >= 0.0f ? 1.0f : -1.0f;
     float a = wdiv(-1.0f, s + n.z);
@@ -200,7 +203,21 @@ __device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt) {
     t = mk3(1.0f + s * n.x * n.x * a, s * b, -s * n.x);
     bt = mk3(b, s + n.y * n.y * a, -n.y);
 }
-__device__ __forceinline__ float3 frame_mul(float3 t, float3 bt, float3 n, float3 v) { return t * v.x + bt * v.y + n * v.z; }
+// t*v.x + bt*v.y + n*v.z and x*(1-f) + y*f with fixed fusion (the first product of
+// each sum fused last), so every kernel that inlines them rounds the same way.
+__device__ __forceinline__ float3 frame_mul(float3 t, float3 bt, float3 n, float3 v) {
+    return mk3(fmaf(n.x, v.z, fmaf(t.x, v.x, bt.x * v.y)), fmaf(n.y, v.z, fmaf(t.y, v.x, bt.y * v.y)),
+               fmaf(n.z, v.z, fmaf(t.z, v.x, bt.z * v.y)));
+}
+// L + c rounded as an add (never fused with the product that made c): the wavefront
+// adds a shadow segment's radiance from memory a round later, the megakernel inline.
+__device__ __forceinline__ float3 add_rn(float3 a, float3 b) {
+    return mk3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 lerp3(float3 x, float3 y, float f) {
+    const float g = 1.0f - f;
+    return mk3(fmaf(x.x, g, y.x * f), fmaf(x.y, g, y.y * f), fmaf(x.z, g, y.z * f));
+}
 __device__ __forceinline__ float3 cosine_sample(float3 n, float r1, float r2) {
     float phi = 2.0f * SF_PI * r1;
     float r = wsqrt(r2);
@@ -228,7 +245,7 @@ static __device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1,
     tangent_frame(n, t, bt);
     float3 lv = mk3(dot3(t, v), dot3(bt, v), dot3(n, v));
     float3 vh = wsafe_normalize(mk3(alpha * lv.x, alpha * lv.y, fmaxf(lv.z, 1e-5f)));
-    float lensq = vh.x * vh.x + vh.y * vh.y;
+    float lensq = fmaf(vh.x, vh.x, vh.y * vh.y);
     float3 t1 = mk3(1.f, 0.f, 0.f);
     if (lensq > 0.0f) t1 = mk3(-vh.y, vh.x, 0.0f) * rsqrtf(lensq);
     float3 t2 = cross3(vh, t1);
@@ -239,8 +256,8 @@ static __device__ float3 sample_ggx_h(float3 n, float3 v, float alpha, float r1,
     float x = r * cp;
     float blend = 0.5f * (1.0f + vh.z);
     float y0 = wsqrt(fmaxf(0.0f, 1.0f - x * x));
-    float y = y0 * (1.0f - blend) + (r * sp) * blend;
-    float3 nh = t1 * x + t2 * y + vh * wsqrt(fmaxf(0.0f, 1.0f - x * x - y * y));
+    float y = fmaf(y0, 1.0f - blend, (r * sp) * blend);
+    float3 nh = frame_mul(t1, t2, vh, mk3(x, y, wsqrt(fmaxf(0.0f, fmaf(-y, y, fmaf(-x, x, 1.0f))))));
     return frame_mul(t, bt, n, wsafe_normalize(mk3(alpha * nh.x, alpha * nh.y, fmaxf(nh.z, 0.0f))));
 }
 static __device__ float3 brdf_eval(const Surface& s, float3 v, float3 l) {
@@ -266,14 +283,52 @@ static __device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_s
     float a2 = s.alpha * s.alpha;
     float nv = fmaxf(dot3(s.n, v), 1e-4f);
     float pdf_spec = wdiv(ggx_d(nh, a2) * smith_g1(nv, a2), 4.0f * nv);
-    return p_spec * pdf_spec + (1.0f - p_spec) * nl * (1.0f / SF_PI);
+    return fmaf(p_spec, pdf_spec, (1.0f - p_spec) * nl * (1.0f / SF_PI));
 }
+// palette_sample (common.wgsl:331-362) of the colouring ramp.
+static __device__ float3 ramp_sample(const DevScene& S, float value) {
+    const uint32_t n = S.col_n;
+    if (n == 0) return mk3(1.f, 1.f, 1.f);
+    if (n == 1) return ld3(S.col_stops[0]);
+    auto mixs = [&](uint32_t a, uint32_t b, float amount) {
+        float f = fminf(fmaxf(amount, 0.0f), 1.0f);
+        if (S.col_smooth) f = f * f * (3.0f - 2.0f * f);
+        return lerp3(ld3(S.col_stops[a]), ld3(S.col_stops[b]), f);
+    };
+    float t = value * S.col_map[0] + S.col_map[1];
+    if (S.col_cyclic) t = t - floorf(t);
+    else t = fminf(fmaxf(t, 0.0f), 1.0f);
+    if (S.col_map[2] != 1.0f) t = powf(t, S.col_map[2]);
+    if (!S.col_positioned && !S.col_cyclic) {
+        const float x = t * float(n - 1);
+        const uint32_t i = min(uint32_t(floorf(x)), n - 2);
+        return mixs(i, i + 1, x - float(i));
+    }
+    const float first = S.col_stops[0][3], last = S.col_stops[n - 1][3];
+    if (S.col_cyclic && (t < first || t >= last)) {
+        const float x = t < first ? t + 1.0f : t;
+        return mixs(n - 1, 0, wdiv(x - last, fmaxf(1.0f + first - last, 1e-8f)));
+    }
+    if (t <= first) return ld3(S.col_stops[0]);
+    if (t >= last) return ld3(S.col_stops[n - 1]);
+    for (uint32_t i = 0; i + 1 < n; ++i)
+        if (t < S.col_stops[i + 1][3])
+            return mixs(i, i + 1, wdiv(t - S.col_stops[i][3], S.col_stops[i + 1][3] - S.col_stops[i][3]));
+    return ld3(S.col_stops[n - 1]);
+}
+
 // make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
 static __device__ Surface make_surface(const DevScene& S, float3 n, const DeSampleF& smp) {
     const DevMaterial* m = &S.material;
     bool assigned = smp.material > 0 && smp.material <= S.finish_count;
     if (assigned) m = &S.finishes[smp.material - 1];
     float3 albedo = ld3(m->albedo);
+    if (!assigned && S.col_n) {  // the colouring ramp (pathtrace.wgsl:275-288)
+        const uint32_t slot = S.col_slot;
+        if (slot < 4) albedo = albedo * ramp_sample(S, smp.traps[slot]);
+        else if (slot == 5) albedo = albedo * ramp_sample(S, n.y * 0.5f + 0.5f);
+        else if (slot == 4) albedo = albedo * ramp_sample(S, float(smp.iter) / fmaxf(float(S.iteration_product), 1.0f));
+    }
     float rough = m->roughness, metallic = m->metallic, spec = m->specular;
     float3 emission = assigned ? ld3(m->emission) : mk3(0.f, 0.f, 0.f);
     if (!assigned && S.variation_enabled) {
@@ -311,11 +366,11 @@ struct HitInfo {
 };
 // Next-event request: a visibility segment and the radiance it carries if clear.
 struct ShadowReq {
-    bool active;
     float3 o, dir;
     float t_end;
     float3 contrib;
 };
+#define SF_MAX_SHADOWS 8  // shadow requests of one bounce: at most one per light
 enum { PATH_CONTINUE = 1, PATH_DONE = 0 };
 
 __device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uint32_t px, uint32_t py, uint32_t sample) {
@@ -330,14 +385,70 @@ __device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uin
     ps.bounce = 0;
 }
 
+// ------------------------------------------------------------------ sky lights
+// environment_value / _probability / _emission (pathtrace.wgsl:164-190).
+__device__ __forceinline__ float3 environment_value(const DevLight& l, float3 dir) {
+    if (dir.y >= 0.0f) return lerp3(ld3(l.b), ld3(l.a), wsqrt(dir.y));
+    return lerp3(ld3(l.b), ld3(l.c), wsqrt(-dir.y));
+}
+__device__ __forceinline__ float environment_probability(const DevLight& l, float area_total) {
+    if (l.energy <= 0.0f) return 0.0f;
+    const float e = 4.0f * SF_PI * l.energy;
+    return fminf(fmaxf(wdiv(e, e + area_total), 0.05f), 1.0f);
+}
+static __device__ float3 environment_emission(const DevScene& S, float3 dir, float pdf, bool use_mis, float3 n,
+                                              float area_total) {
+    float3 L = mk3(0.f, 0.f, 0.f);
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        if (l.kind != SF_LIGHT_ENVIRONMENT) continue;
+        float w = 1.0f;
+        if (use_mis) w = mis_power(pdf, environment_probability(l, area_total) * fmaxf(dot3(n, dir), 0.0f) * (1.0f / SF_PI));
+        L = L + environment_value(l, dir) * w;
+    }
+    return L;
+}
+// sun_pdf, sun_radiance (pathtrace.wgsl:432-468): a disk of cos_max around a.
+__device__ __forceinline__ float sun_pdf(float cos_max) { return wdiv(1.0f, 2.0f * SF_PI * fmaxf(1.0f - cos_max, 1e-7f)); }
+static __device__ float3 sun_radiance(const DevScene& S, float3 dir, float pdf_bsdf, bool use_mis) {
+    float3 L = mk3(0.f, 0.f, 0.f);
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        if (l.kind != SF_LIGHT_SUN || dot3(dir, ld3(l.a)) < l.cos_max) continue;
+        const float pl = sun_pdf(l.cos_max);
+        const float w = use_mis ? mis_power(pdf_bsdf, pl) : 1.0f;
+        L = L + ld3(l.color) * (pl * w);
+    }
+    return L;
+}
+// cone_sample (pathtrace.wgsl:210-215).
+__device__ __forceinline__ float3 cone_sample(float3 dir, float cos_max, float r1, float r2) {
+    const float cos_t = 1.0f - r1 * (1.0f - cos_max);
+    const float sin_t = wsqrt(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+    float sp, cp;
+    sincosf(2.0f * SF_PI * r2, &sp, &cp);
+    float3 t, bt;
+    tangent_frame(dir, t, bt);
+    return frame_mul(t, bt, dir, mk3(sin_t * cp, sin_t * sp, cos_t));
+}
+
 // One bounce of `radiance` (pathtrace.wgsl:841-1196) after its trace: hit
-// classification, emitter MIS, surface, next-event sampling (the visibility
-// test is returned in `sh` and its radiance added by the caller if clear) and
-// BSDF continuation with Russian roulette. Writes first-hit depth/aux at bounce 0.
-static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, ShadowReq& sh, float* first_depth,
-                           float4* first_aux) {
-    sh.active = false;
-    if (!h.hit) return PATH_DONE;  // no environment light: a miss adds nothing
+// classification, sky and emitter emission with MIS, surface, next-event sampling
+// (direct_light, pathtrace.wgsl:471-558: every environment and sun, and the one
+// selected area light, in scene order; each visibility test is handed to `emit`,
+// which adds its radiance if the segment is clear) and BSDF continuation with
+// Russian roulette. Writes first-hit depth/aux at bounce 0.
+template <class Emit>
+static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, Emit&& emit, float* first_depth,
+                                  float4* first_aux) {
+    if (!h.hit) {
+        if (!h.exhausted) {  // the sky (pathtrace.wgsl:1026-1040)
+            ps.L = ps.L + ps.tp * (environment_emission(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
+                                                        ps.prev_area_total) +
+                                   sun_radiance(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf));
+        }
+        return PATH_DONE;
+    }
     float3 p = ps.o + ps.d * h.t;
     if (h.light_index != SF_NO_LIGHT) {
         if (ps.bounce == 0 && first_depth) {
@@ -367,13 +478,14 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     float p_spec = spec_probability(s, nv);
     float area_total = area_total_weight(S, p_off, s.n);
     bool last = ps.bounce == S.max_bounces;
-    // direct_light (pathtrace.wgsl:471-558), area emitters
+    // direct_light: the area light selected by weight, then every light in order
     uint32_t selected = SF_NO_LIGHT;
     float selected_weight = 0.0f;
     if (area_total > 0.0f) {
         float threshold = rnd(ps.rng) * area_total;
         float sum = 0.0f;
         for (uint32_t i = 0; i < S.light_count; ++i) {
+            if (S.lights[i].kind != SF_LIGHT_AREA) continue;
             float w = area_weight(p_off, s.n, S.lights[i]);
             sum += w;
             if (w > 0.0f) {
@@ -383,31 +495,65 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             }
         }
     }
-    if (selected != SF_NO_LIGHT) {
-        const DevLight& l = S.lights[selected];
-        float u1 = rnd(ps.rng);
-        float u2 = rnd(ps.rng);
-        float3 q = ld3(l.a) + ld3(l.b) * (u1 - 0.5f) + ld3(l.c) * (u2 - 0.5f);
-        float3 ln = ld3(l.n);
-        float3 to_q = q - p_off;
-        float dist2 = dot3(to_q, to_q);
-        if (dist2 >= 1e-8f) {
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        if (l.kind == SF_LIGHT_ENVIRONMENT) {
+            if (l.peak <= 0.0f) continue;
+            const float probability = environment_probability(l, area_total);
+            if (rnd(ps.rng) >= probability) continue;
+            const float r1 = rnd(ps.rng);
+            const float r2 = rnd(ps.rng);
+            const float3 ldir = cosine_sample(s.n, r1, r2);
+            const float nl = fmaxf(dot3(s.n, ldir), 0.0f);
+            if (dot3(n, ldir) <= 0.0f || nl <= 0.0f) continue;
+            const float pl = probability * nl * (1.0f / SF_PI);
+            const float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
+            const float w = last ? 1.0f : mis_power(pl, pb);
+            ShadowReq sh;
+            sh.o = p_off;
+            sh.dir = ldir;
+            sh.t_end = S.extent;
+            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * wdiv(w, pl));
+            emit(sh);
+        } else if (l.kind == SF_LIGHT_SUN) {
+            const float r1 = rnd(ps.rng);
+            const float r2 = rnd(ps.rng);
+            const float3 ldir = cone_sample(ld3(l.a), l.cos_max, r1, r2);
+            const float nl = dot3(s.n, ldir);
+            if (nl <= 0.0f || dot3(n, ldir) <= 0.0f) continue;
+            const float pl = sun_pdf(l.cos_max);
+            const float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
+            const float w = last ? 1.0f : mis_power(pl, pb);
+            ShadowReq sh;
+            sh.o = p_off;
+            sh.dir = ldir;
+            sh.t_end = S.extent;
+            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * ld3(l.color) * w);
+            emit(sh);
+        } else if (i == selected) {
+            float u1 = rnd(ps.rng);
+            float u2 = rnd(ps.rng);
+            float3 q = ld3(l.a) + ld3(l.b) * (u1 - 0.5f) + ld3(l.c) * (u2 - 0.5f);
+            float3 ln = ld3(l.n);
+            float3 to_q = q - p_off;
+            float dist2 = dot3(to_q, to_q);
+            if (dist2 < 1e-8f) continue;
             const float inv_dist = rsqrtf(dist2);
             float dist = dist2 * inv_dist;
             float3 ldir = to_q * inv_dist;
             float nl = dot3(s.n, ldir);
             float cos_l = dot3(ln, -ldir);
-            if (!(nl <= 0.0f || cos_l <= 0.0f || dot3(n, ldir) <= 0.0f)) {
-                float pl = wdiv(selected_weight, area_total) * wdiv(dist2, fmaxf(l.area * cos_l, 1e-20f));
-                float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
-                float w = last ? 1.0f : mis_power(pl, pb);
-                float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * wdiv(w, pl);
-                sh.active = true;
-                sh.o = p_off;
-                sh.dir = ldir;
-                sh.t_end = fmaxf(0.0f, dist - fmaxf(1e-5f, dist * 1e-6f));
-                sh.contrib = ps.tp * Ld;
-            }
+            if (nl <= 0.0f || cos_l <= 0.0f || dot3(n, ldir) <= 0.0f) continue;
+            float pl = wdiv(selected_weight, area_total) * wdiv(dist2, fmaxf(l.area * cos_l, 1e-20f));
+            float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
+            float w = last ? 1.0f : mis_power(pl, pb);
+            float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * wdiv(w, pl);
+            ShadowReq sh;
+            sh.o = p_off;
+            sh.dir = ldir;
+            sh.t_end = fmaxf(0.0f, dist - fmaxf(1e-5f, dist * 1e-6f));
+            sh.contrib = ps.tp * Ld;
+            emit(sh);
         }
     }
     if (last) return PATH_DONE;

@@ -78,7 +78,8 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     }
     const uint32_t cap = soa.capacity;
 
-    uint32_t state = TL_IDLE, path = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
+    // item: the continuation path, or the shadow row (k * cap + path) of a shadow segment
+    uint32_t state = TL_IDLE, path = 0, item = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
     bool shadow = false;
     March m{};  // set by each refill before use
     float3 grad = mk3(0.f, 0.f, 0.f);
@@ -89,7 +90,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
 
     // End of a continuation or shadow segment without a surface sample.
     auto finish = [&](int r) {
-        if (shadow) soa.vis[path] = (r == MARCH_MISS && li == SF_NO_LIGHT) ? 1u : 0u;
+        if (shadow) soa.vis[item] = (r == MARCH_MISS && li == SF_NO_LIGHT) ? 1u : 0u;
         else if (r == MARCH_MISS && li != SF_NO_LIGHT)
             soa.hit[path] = make_uint4(__float_as_uint(m.t_end), m.i, li, SF_HF_HIT);
         else
@@ -124,12 +125,13 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             } else {
                 if (first) {
                     shadow = w >= n_cont;
-                    path = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
+                    item = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
                 } else {
-                    uint32_t item = tl.resume[w];
-                    path = item & 0x7fffffffu;
-                    shadow = (item >> 31) != 0;
+                    const uint32_t it = tl.resume[w];
+                    item = it & 0x7fffffffu;
+                    shadow = (it >> 31) != 0;
                 }
+                path = shadow ? item % cap : item;
                 if constexpr (MULTI) {
                     const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
                     Pl = job.prog;
@@ -140,11 +142,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     safety = Sl->step_scale;
                     max_steps = Sl->max_steps;
                 }
-                float4 o = shadow ? soa.sh_o[path] : soa.o[path];
-                float4 d = shadow ? soa.sh_d[path] : soa.d[path];
+                float4 o = shadow ? soa.sh_o[item] : soa.o[path];
+                float4 d = shadow ? soa.sh_d[item] : soa.d[path];
                 // the march state: set by the stage that made the ray, or saved by the
                 // previous launch at its step quantum
-                const uint32_t row = path + (shadow ? cap : 0u);
+                const uint32_t row = shadow ? cap + item : item;
                 const float4 a = soa.m0[row], b = soa.m1[row];
                 m.ro = mk3(o.x, o.y, o.z);
                 m.rd = mk3(d.x, d.y, d.z);
@@ -221,11 +223,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                         finish(r);
                     } else if (--budget == 0) {
                         // quantum spent: save the march and hand the segment to the next launch
-                        uint32_t row = path + (shadow ? cap : 0u);
+                        const uint32_t row = shadow ? cap + item : item;
                         soa.m0[row] = make_float4(m.t, m.omega, m.prev_radius, m.step_len);
                         soa.m1[row] = make_float4(m.t_end, m.cand_t, m.cand_err, __uint_as_float(m.i));
                         soa.m2[row] = li;
-                        warp_append(tl.next_resume_count, tl.next_resume, true, path | (shadow ? 0x80000000u : 0u));
+                        warp_append(tl.next_resume_count, tl.next_resume, true, item | (shadow ? 0x80000000u : 0u));
                         state = TL_IDLE;
                     }
                 }

@@ -110,6 +110,97 @@ class AreaLight:
         return out
 
 
+def kelvin_to_linear(kelvin: float):
+    """Color::Kelvin (light.rs:28-58): Tanner Helland's black-body approximation,
+    sRGB to linear, normalised so the brightest channel is 1 (binary32)."""
+    t = f32(min(max(kelvin, 1000.0), 40000.0)) / f32(100.0)
+    if t <= 66.0:
+        r = f32(255.0)
+        g = f32(99.4708) * f32(math.log(t)) - f32(161.11957)
+    else:
+        r = f32(329.69873) * f32((t - f32(60.0)) ** f32(-0.13320476))
+        g = f32(288.12217) * f32((t - f32(60.0)) ** f32(-0.07551485))
+    if t >= 66.0:
+        b = f32(255.0)
+    elif t <= 19.0:
+        b = f32(0.0)
+    else:
+        b = f32(138.51773) * f32(math.log(t - f32(10.0))) - f32(305.0448)
+
+    def srgb_to_linear(v):
+        v = f32(v)
+        return v / f32(12.92) if v <= 0.04045 else f32(((v + f32(0.055)) / f32(1.055)) ** f32(2.4))
+
+    c = [srgb_to_linear(min(max(f32(x) / f32(255.0), 0.0), 1.0)) for x in (r, g, b)]
+    m = max(c[0], c[1], c[2], f32(1e-6))
+    return tuple(float(f32(x) / m) for x in c)
+
+
+def _color(c):
+    """A light colour: ("kelvin", K) / {"Kelvin": K} or a linear RGB triple."""
+    if isinstance(c, (int, float)):
+        return kelvin_to_linear(float(c))
+    if isinstance(c, dict) and "Kelvin" in c:
+        return kelvin_to_linear(float(c["Kelvin"]))
+    if isinstance(c, tuple) and len(c) == 2 and c[0] == "kelvin":
+        return kelvin_to_linear(float(c[1]))
+    return tuple(float(x) for x in c)
+
+
+@dataclass
+class SunLight:
+    """Light::Sun{direction (toward the sun), color, intensity (irradiance), angular_size (deg)}."""
+    direction: tuple = (-0.4, 0.8, 0.3)
+    color: tuple = (1.0, 1.0, 1.0)
+    intensity: float = 6.0
+    angular_size: float = 1.0
+
+    def packed(self) -> abi.sf_area_light:
+        out = abi.sf_area_light()
+        out.kind = abi.SF_LIGHT_SUN
+        out.direction[:] = [float(x) for x in _normalize_or(_v(self.direction), (0, 1, 0))]
+        out.angular_size = self.angular_size
+        out.radiance[:] = [float(f32(c) * f32(self.intensity)) for c in _color(self.color)]
+        return out
+
+
+@dataclass
+class EnvironmentLight:
+    """Light::Environment{zenith, horizon, ground, intensity}: a vertical gradient sky."""
+    zenith: tuple = (0.2, 0.35, 0.7)
+    horizon: tuple = (0.6, 0.65, 0.7)
+    ground: tuple = (0.15, 0.12, 0.1)
+    intensity: float = 1.0
+
+    def packed(self) -> abi.sf_area_light:
+        out = abi.sf_area_light()
+        out.kind = abi.SF_LIGHT_ENVIRONMENT
+        k = f32(self.intensity)
+        out.zenith[:] = [float(f32(c) * k) for c in _color(self.zenith)]
+        out.horizon[:] = [float(f32(c) * k) for c in _color(self.horizon)]
+        out.ground[:] = [float(f32(c) * k) for c in _color(self.ground)]
+        return out
+
+
+@dataclass
+class Ramp:
+    """Ramp (palette.rs:74-100): stops, optional positions, cyclic, frequency, phase, gamma."""
+    stops: list = field(default_factory=lambda: [(0.0, 0.0, 0.0), (1.0, 1.0, 1.0)])
+    positions: list = field(default_factory=list)
+    cyclic: bool = False
+    frequency: float = 1.0
+    phase: float = 0.0
+    gamma: float = 1.0
+    smooth: bool = False
+
+
+@dataclass
+class Coloring:
+    """Coloring::Trap{slot, ramp} (material.rs:100-130); slot 4 = iterations, 5 = normal."""
+    slot: int = 0
+    ramp: Ramp = field(default_factory=Ramp)
+
+
 @dataclass
 class Finish:
     albedo: tuple = (0.7, 0.7, 0.7)
@@ -138,6 +229,7 @@ class SurfaceVariation:
 class Material(Finish):
     finishes: list = field(default_factory=list)
     surface: SurfaceVariation | None = None
+    coloring: Coloring | None = None
 
 
 @dataclass
@@ -169,7 +261,7 @@ class Scene:
             d.finishes[i] = f.packed()
         d.finish_count = len(self.material.finishes)
         if len(self.lights) > abi.SF_MAX_LIGHTS:
-            raise ValueError("at most 8 area lights on the device path")
+            raise ValueError("at most 8 lights on the device path")
         for i, l in enumerate(self.lights):
             d.lights[i] = l.packed()
         d.light_count = len(self.lights)
@@ -181,6 +273,23 @@ class Scene:
             d.variation_metallic[:] = list(sv.metallic)
         d.cavity_darkness = self.cavity_darkness
         d.seed = self.seed & 0xFFFFFFFFFFFFFFFF
+        col = self.material.coloring
+        d.coloring.slot = 0xFFFF
+        if col is not None:
+            r = col.ramp
+            if len(r.stops) > abi.SF_MAX_RAMP_STOPS:
+                raise ValueError("at most 16 ramp stops")
+            d.coloring.slot = col.slot
+            d.coloring.stop_count = len(r.stops)
+            n = len(r.stops)
+            for i, c in enumerate(r.stops):
+                # Ramp::position (palette.rs:106-115): given, else i / (n or n - 1)
+                pos = r.positions[i] if r.positions else float(f32(i) / f32(n if r.cyclic else max(n - 1, 1)))
+                d.coloring.stops[i][:] = [float(c[0]), float(c[1]), float(c[2]), float(pos)]
+            d.coloring.cyclic = int(r.cyclic)
+            d.coloring.smooth = int(r.smooth)
+            d.coloring.positioned = int(bool(r.positions))
+            d.coloring.frequency, d.coloring.phase, d.coloring.gamma = r.frequency, r.phase, r.gamma
         return d
 
 
@@ -205,3 +314,74 @@ class RenderConfig:
         c.pixel_tolerance = self.pixel_tolerance
         c.tile_size, c.samples_per_dispatch = self.tile_size, self.samples_per_dispatch
         return c
+
+
+# ---------------------------------------------------------------------------- scene files
+def _rgb(c):
+    """Color::Kelvin(K) / Color::Linear((r, g, b)) as RON values, or a bare triple."""
+    from . import ron
+
+    if isinstance(c, ron.Tuple) and c.name == "Kelvin":
+        return kelvin_to_linear(float(c.items[0]))
+    if isinstance(c, ron.Tuple) and c.name == "Linear":
+        return tuple(ron.vec(c.items[0]))
+    return tuple(ron.vec(c))
+
+
+def scene_from_ron_value(v) -> Scene:
+    """Scene (crates/syfrack-core/src/scene/mod.rs) from a parsed scenes/*.ron value: the
+    graph fractal, Orbit/Free camera, Sun/Environment/Area lights, the material with its
+    Trap/iteration/normal colouring, and the seed. Fog, ocean, textures, finishes with
+    detail and HDRI are not on this path and raise ValueError when enabled."""
+    from . import ron
+
+    frac = v["fractal"]
+    if not (isinstance(frac, ron.Tuple) and frac.name == "Graph"):
+        raise ValueError("only graph fractals are on this path")
+    graph = Graph.from_ron_value(frac.items[0])
+    cam_v = v["camera"]
+    mode = cam_v["mode"]
+    if mode["__name__"] == "Orbit":
+        cam = Camera.orbit(tuple(ron.vec(mode["point"])), float(mode["distance"]), float(mode["azimuth"]),
+                           float(mode["elevation"]), float(mode.get("roll", 0.0)), float(cam_v["focal_mm"]))
+    else:
+        cam = Camera(tuple(ron.vec(mode["position"])), tuple(ron.vec(mode["target"])), float(mode.get("roll", 0.0)),
+                     float(cam_v["focal_mm"]))
+    cam.f_number = float(cam_v.get("f_number", 0.0))
+    cam.focus_distance = float(cam_v.get("focus_distance", 3.0))
+    lights = []
+    for l in v.get("lights", []):
+        kind = l["__name__"]
+        if kind == "Sun":
+            lights.append(SunLight(tuple(ron.vec(l["direction"])), _rgb(l["color"]), float(l["intensity"]),
+                                   float(l["angular_size"])))
+        elif kind == "Environment":
+            if float(l.get("rotation", 0.0)) != 0.0:
+                pass  # a vertical gradient does not change under rotation about y
+            lights.append(EnvironmentLight(_rgb(l["zenith"]), _rgb(l["horizon"]), _rgb(l["ground"]),
+                                           float(l["intensity"])))
+        elif kind == "Area":
+            lights.append(AreaLight(tuple(ron.vec(l["position"])), tuple(ron.vec(l["normal"])),
+                                    tuple(ron.vec(l["size"])), _rgb(l["color"]), float(l["intensity"])))
+        else:
+            raise ValueError(f"{kind} lights are not on this path")
+    m = v["material"]
+    col = None
+    c = m.get("coloring")
+    if isinstance(c, dict) and c.get("__name__") == "Trap":
+        r = c.get("ramp", {})
+        ramp = Ramp(stops=[tuple(ron.vec(s)) for s in r.get("stops", [])] or Ramp().stops,
+                    positions=[float(x) for x in r.get("positions", [])], cyclic=bool(r.get("cyclic", False)),
+                    frequency=float(r.get("frequency", 1.0)), phase=float(r.get("phase", 0.0)),
+                    gamma=float(r.get("gamma", 1.0)),
+                    smooth=isinstance(r.get("interpolation"), ron.Unit) and r["interpolation"].name == "Smooth")
+        col = Coloring(int(c["slot"]), ramp)
+    elif c is not None and not (isinstance(c, ron.Unit) and c.name == "None"):
+        raise ValueError("only Trap colouring is on this path")
+    mat = Material(albedo=tuple(ron.vec(m["albedo"])), roughness=float(m["roughness"]),
+                   metallic=float(m["metallic"]), specular=float(m["specular"]), coloring=col)
+    atm = v.get("atmosphere", {})
+    if float(atm.get("fog_density", 0.0)) != 0.0:
+        raise ValueError("fog is not on this path")
+    return Scene(graph=graph, camera=cam, material=mat, lights=lights, seed=int(v.get("seed", 0)),
+                 cavity_darkness=float(atm.get("cavity_darkness", 0.0)))

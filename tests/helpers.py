@@ -76,3 +76,34 @@ def bounded_bulb(subtract=False, margin=0.05):
     else:
         g.links.append(Link((10, 0), (6, 0)))
     return g
+
+
+def golden_scene(name):
+    """scenes/<name>.ron from its JSON copy, read by the package's scene-file reader."""
+    from syfrack_gb300 import ron
+    from syfrack_gb300.scene import scene_from_ron_value
+
+    with open(os.path.join(GOLDEN, f"scene_{name}.json")) as f:
+        d = json.load(f)
+
+    def back(v):
+        if isinstance(v, dict) and "__items__" in v:
+            items = [back(x) for x in v["__items__"]]
+            if v["__name__"] == "Graph":
+                items = [_jsonish_to_ron(v["__items__"][0])]
+            return ron.Tuple(v["__name__"], items)
+        if isinstance(v, dict):
+            return {k: back(x) for k, x in v.items()}
+        if isinstance(v, list):
+            return [back(x) for x in v]
+        if isinstance(v, str) and v in ("None", "Smooth", "Linear"):
+            return ron.Unit(v)
+        return v
+
+    return scene_from_ron_value(back(d["scene"]))
+
+
+def golden_film_blocks(name):
+    with open(os.path.join(GOLDEN, f"film_{name}_blocks.json")) as f:
+        d = json.load(f)
+    return np.array(d["blocks"]).reshape(len(d["blocks"]), -1, 3), d
