@@ -73,3 +73,28 @@ def test_autotune_leaves_films_clean(renderer):
     for i, (sc, cfg) in enumerate(jobs):
         assert b.readback(i).accum[..., 3].max() == cfg.samples_per_dispatch
     b.close()
+
+
+def test_sky_lit_jobs_in_a_batch(renderer):
+    """Jobs with a sun and a sky (three shadow slots in the batch's arena) next to
+    area-lit jobs (one): each film equals the job alone."""
+    import sys, os
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from helpers import golden_scene
+    from syfrack_gb300.scene import RenderConfig
+
+    jobs = small_jobs(3)
+    for name in ("menger", "mandelbulb"):
+        jobs.append((golden_scene(name), RenderConfig(48, 32, 4, max_bounces=3, max_steps=256, pixel_tolerance=1.0,
+                                                      tile_size=48, samples_per_dispatch=4, integrator="wavefront")))
+    b = Batch(renderer, jobs)
+    b.run(1, use_graph=False)
+    assert b.sync() == 0
+    for i, (sc, cfg) in enumerate(jobs):
+        got = b.readback(i)
+        ref = alone(renderer, sc, cfg)
+        scale = max(1.0, float(np.abs(ref.accum[..., :3]).max()))
+        assert np.abs(got.accum[..., :3] - ref.accum[..., :3]).max() <= 1e-4 * scale, i
+        np.testing.assert_allclose(got.depth, ref.depth, rtol=1e-6, atol=1e-6)
+    assert b.readback(len(jobs) - 1).accum[..., :3].mean() > 0.05  # the sky lights reach the form
+    b.close()

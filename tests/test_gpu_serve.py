@@ -184,3 +184,36 @@ def test_concurrent_clients(renderer):
     assert sorted(out) == list(range(len(tiles)))
     for i in range(len(tiles)):
         np.testing.assert_array_equal(out[i], alone[i])
+
+
+def test_sky_lit_preview_served(renderer):
+    """A preview lit by a sun and a sky (three shadow segments per bounce, what the
+    server's arenas hold) matches the same render through a session; a scene with more
+    sky lights than the arenas hold is refused before it is queued."""
+    import os
+    import sys
+    sys.path.insert(0, os.path.dirname(os.path.abspath(__file__)))
+    from helpers import golden_scene
+    from syfrack_gb300.scene import RenderConfig, SunLight
+
+    sc = golden_scene("mandelbulb")
+    cfg = RenderConfig(64, 40, 1, max_bounces=1, max_steps=512, pixel_tolerance=1.0, tile_size=64,
+                       samples_per_dispatch=1, integrator="wavefront")
+    srv = Server(renderer, hbm_budget=GB, path_capacity=1 << 16)
+    t = srv.preview(sc, cfg)
+    r = srv.wait(t)
+    assert r.state == DONE and r.status == 0
+    s = RenderSession(renderer, sc, cfg)
+    while not s.step(0):
+        pass
+    ref = s.readback()
+    s.close()
+    # the server runs the batched kernel (per-job form switch), the session the per-form one
+    scale = max(1.0, float(np.abs(ref.accum[..., :3]).max()))
+    assert np.abs(r.accum[..., :3] - ref.accum[..., :3]).max() <= 1e-4 * scale
+    assert r.accum[..., :3].mean() > 0.05
+    srv.release(t)
+    sc.lights = list(sc.lights) + [SunLight(direction=(0.3, 0.9, -0.2))]
+    with pytest.raises(SyfrackError, match="SF_ERR_UNSUPPORTED"):
+        srv.preview(sc, cfg)
+    srv.close()
