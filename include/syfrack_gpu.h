@@ -144,6 +144,7 @@ enum { SF_FORM_GENERIC = 0, SF_FORM_BULB = 1, SF_FORM_BOX = 2, SF_FORM_MENGER = 
 
 typedef struct sf_context sf_context;
 typedef struct sf_graph sf_graph;
+typedef struct sf_environment sf_environment;  /* an HDRI panorama on the device */
 
 /* Device context: owns the CUDA stream, the module and the HBM admission
  * budget (0 = 90% of free memory). Replaces GpuContext::new (gpu.rs:15-36)
@@ -161,6 +162,19 @@ sf_status sf_context_memory(sf_context* ctx, uint64_t* used, uint64_t* budget);
  * host only (no context, no device): the checks sf_graph_compile makes before lowering. */
 sf_status sf_graph_validate(const sf_graph_desc* desc, sf_graph_info* out);
 sf_status sf_graph_compile(sf_context* ctx, const sf_graph_desc* desc, sf_graph** out);
+
+/* EnvironmentMap::from_rgb (crates/syfrack-render/src/environment.rs:271-366): an
+ * equirectangular linear RGB panorama (width*height*3 floats, row 0 at the zenith,
+ * finite, at most 8192x4096) reduced in solid angle to at most 2048x1024 texels, each
+ * with the cumulative luminance x solid-angle distribution of its importance sampling
+ * (the bilinear halo included). sf_environment_build runs on the host only: it writes
+ * out_width*out_height texels (rgb, cdf) when `texels` is not NULL; pass NULL first to
+ * learn the size. sf_environment_create keeps the texels on the device. */
+sf_status sf_environment_build(const float* rgb, uint32_t width, uint32_t height, float* texels,
+                               uint32_t* out_width, uint32_t* out_height, int* uniform);
+sf_status sf_environment_create(sf_context* ctx, const float* rgb, uint32_t width, uint32_t height,
+                                sf_environment** out);
+sf_status sf_environment_destroy(sf_environment* env);
 sf_status sf_graph_info_get(const sf_graph* graph, sf_graph_info* out);
 /* Value edits without re-lowering: same topology, new floats (topology_key semantics,
  * graph/mod.rs:397-425). Fails with SF_ERR_GRAPH if the topology changed. */
@@ -195,14 +209,19 @@ typedef struct sf_material {
  *     height edge (edge_v), radiance = color * intensity;
  *   Sun: direction toward the sun, angular_size = full angular diameter in degrees,
  *     radiance = irradiance (color * intensity);
- *   Environment: zenith, horizon and ground radiance (colors * intensity). */
-enum { SF_LIGHT_AREA = 0, SF_LIGHT_SUN = 1, SF_LIGHT_ENVIRONMENT = 2 };
+ *   Environment: zenith, horizon and ground radiance (colors * intensity);
+ *   Hdri: an equirectangular panorama (below), intensity in radiance[0], rotation. */
+enum { SF_LIGHT_AREA = 0, SF_LIGHT_SUN = 1, SF_LIGHT_ENVIRONMENT = 2, SF_LIGHT_HDRI = 3 };
 typedef struct sf_area_light {
     float center[3], edge_u[3], edge_v[3], radiance[3];
     uint32_t kind;
     float direction[3];
     float angular_size;
     float zenith[3], horizon[3], ground[3];
+    /* Hdri: the panorama (sf_environment_create), radiance[0] = intensity, rotation in
+     * degrees about +y. The panorama must outlive the sessions that render with it. */
+    sf_environment* environment;
+    float rotation;
 } sf_area_light;
 typedef sf_area_light sf_light;
 #define SF_MAX_LIGHTS 8

@@ -62,6 +62,9 @@ def lib():
         up = C.POINTER(C.c_uint32)
         L.or_de_eval.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, dp, up, up, C.c_int]
         L.or_de_eval_fast.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, up, C.c_int]
+        L.or_panorama.argtypes = [C.c_uint64, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.POINTER(C.c_float),
+                                  up, up]
+        L.or_panorama.restype = C.c_int
         L.or_bvh_build.argtypes = [C.POINTER(abi.sf_placement), C.c_uint32, C.POINTER(C.c_float),
                                    C.POINTER(C.c_float)]
         L.or_primary.restype = C.c_uint64
@@ -92,6 +95,20 @@ def _up(a):
 
 def default_threads() -> int:
     return max(1, os.cpu_count() or 1)
+
+
+def panorama(rgb, key=0):
+    """The oracle's panorama tables (environment.rs:271-366): texels[h, w, 4]; with a key
+    (a Panorama handle value) scenes whose HDRI light carries it render with them."""
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    h, w = rgb.shape[:2]
+    fpp = C.POINTER(C.c_float)
+    ow, oh = C.c_uint32(), C.c_uint32()
+    if not lib().or_panorama(0, rgb.ctypes.data_as(fpp), w, h, None, C.byref(ow), C.byref(oh)):
+        raise ValueError("invalid panorama")
+    out = np.zeros((oh.value, ow.value, 4), np.float32)
+    lib().or_panorama(key, rgb.ctypes.data_as(fpp), w, h, out.ctypes.data_as(fpp), C.byref(ow), C.byref(oh))
+    return out
 
 
 def bvh_build(placements, half):

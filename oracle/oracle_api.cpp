@@ -87,6 +87,19 @@ void* or_graph_new(const sf_graph_desc* d) {
 
 void or_graph_free(void* g) { delete static_cast<Graph*>(g); }
 
+// A panorama's tables, registered under the key scenes carry in their environment field;
+// writes w*h*4 floats into texels when not NULL.
+int or_panorama(uint64_t key, const float* rgb, uint32_t width, uint32_t height, float* texels, uint32_t* w,
+                uint32_t* h) {
+    Panorama p;
+    if (!panorama_tables(rgb, width, height, p)) return 0;
+    if (w) *w = p.w;
+    if (h) *h = p.h;
+    if (texels) std::memcpy(texels, p.texels.data(), p.texels.size() * sizeof(float));
+    if (key) panorama_register(key, p);
+    return 1;
+}
+
 // The fence hierarchy of `count` placements: 8 floats per node (centre, half, escape,
 // placement or -1) into out (2 * count - 1 nodes).
 void or_bvh_build(const sf_placement* pl, uint32_t count, const float* half, float* out) {

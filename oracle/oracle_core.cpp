@@ -807,7 +807,12 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
         Light<R>& o = s.lights[i];
         o.kind = l.kind;
         o.color = v3<R>(l.radiance);
-        if (l.kind == SF_LIGHT_SUN) {
+        if (l.kind == SF_LIGHT_HDRI) {
+            const float r = l.rotation * (3.14159265f / 180.0f);
+            o.pano = panorama_find(reinterpret_cast<uint64_t>(l.environment));
+            o.a = V3<R>(R(std::cos(r)), R(std::sin(r)), R(o.pano && o.pano->uniform ? 1 : 0));
+            o.color = V3<R>(R(l.radiance[0]), 0, 0);
+        } else if (l.kind == SF_LIGHT_SUN) {
             // GpuLight::from_light (uniforms.rs:656-668), in binary32 as the reference
             o.a = v3<R>(l.direction);
             o.cos_max = R(std::cos((l.angular_size * 0.5f) * (3.14159265f / 180.0f)));
@@ -1123,6 +1128,168 @@ template <class R> static Surface<R> make_surface(const Scene<R>& sc, V3<R> n, c
     return s;
 }
 
+// ---------------------------------------------------------------- panoramas
+// EnvironmentMap::from_rgb (environment.rs:271-366), restated in double precision.
+static std::map<uint64_t, Panorama>& panoramas() {
+    static std::map<uint64_t, Panorama> m;
+    return m;
+}
+void panorama_register(uint64_t key, const Panorama& p) { panoramas()[key] = p; }
+const Panorama* panorama_find(uint64_t key) {
+    auto it = panoramas().find(key);
+    return it == panoramas().end() ? nullptr : &it->second;
+}
+static double pano_cell_area(uint32_t w, uint32_t h, uint32_t row) {
+    const double pi = 3.14159265358979323846;
+    const double top = pi * row / h, bottom = pi * (row + 1) / h;
+    return 2.0 * pi / w * 2.0 * std::sin((top + bottom) * 0.5) * std::sin((bottom - top) * 0.5);
+}
+bool panorama_tables(const float* rgb, uint32_t width, uint32_t height, Panorama& out) {
+    if (!rgb || !width || !height || uint64_t(width) * height > 8192ull * 4096ull) return false;
+    for (size_t i = 0; i < size_t(width) * height * 3; ++i)
+        if (!std::isfinite(rgb[i])) return false;
+    const double pi = 3.14159265358979323846;
+    const double scale = std::max({double(width) / 2048.0, double(height) / 1024.0, 1.0});
+    const uint32_t ow = uint32_t(std::max(std::floor(width / scale), 1.0));
+    const uint32_t oh = uint32_t(std::max(std::floor(height / scale), 1.0));
+    out.w = ow;
+    out.h = oh;
+    out.texels.assign(size_t(ow) * oh * 4, 0.0f);
+    for (uint32_t oy = 0; oy < oh; ++oy) {
+        const double top = double(oy) * height / oh, bottom = double(oy + 1) * height / oh;
+        for (uint32_t ox = 0; ox < ow; ++ox) {
+            const double left = double(ox) * width / ow, right = double(ox + 1) * width / ow;
+            double sum[3] = {0, 0, 0}, total = 0;
+            for (uint32_t iy = uint32_t(std::floor(top)); iy < std::min<uint32_t>(uint32_t(std::ceil(bottom)), height); ++iy) {
+                const double lat = std::cos(pi * std::max(top, double(iy)) / height) -
+                                   std::cos(pi * std::min(bottom, double(iy + 1)) / height);
+                for (uint32_t ix = uint32_t(std::floor(left)); ix < std::min<uint32_t>(uint32_t(std::ceil(right)), width); ++ix) {
+                    const double wgt = lat * (std::min(right, double(ix + 1)) - std::max(left, double(ix)));
+                    for (int c = 0; c < 3; ++c) sum[c] += double(std::max(rgb[(size_t(iy) * width + ix) * 3 + c], 0.0f)) * wgt;
+                    total += wgt;
+                }
+            }
+            for (int c = 0; c < 3; ++c) out.texels[(size_t(oy) * ow + ox) * 4 + c] = float(sum[c] / total);
+        }
+    }
+    const size_t n = size_t(ow) * oh;
+    out.uniform = true;
+    for (size_t i = 1; i < n && out.uniform; ++i)
+        for (int c = 0; c < 3; ++c) out.uniform = out.uniform && out.texels[i * 4 + c] == out.texels[c];
+    if (out.uniform) { out.texels[(n - 1) * 4 + 3] = 1.0f; return true; }
+    auto lum = [&](size_t i) {
+        return double(out.texels[i * 4]) * 0.2126 + double(out.texels[i * 4 + 1]) * 0.7152 + double(out.texels[i * 4 + 2]) * 0.0722;
+    };
+    std::vector<double> w(n);
+    double total = 0;
+    const int dd[3] = {-1, 0, 1};
+    const double ww[3] = {0.125, 0.75, 0.125};
+    for (uint32_t y = 0; y < oh; ++y)
+        for (uint32_t x = 0; x < ow; ++x) {
+            double acc = 0;
+            for (int j = 0; j < 3; ++j) {
+                const int row = std::min(std::max(int(y) + dd[j], 0), int(oh) - 1);
+                for (int k = 0; k < 3; ++k) {
+                    const int col = ((int(x) + dd[k]) % int(ow) + int(ow)) % int(ow);
+                    acc += lum(size_t(row) * ow + col) * ww[k] * ww[j];
+                }
+            }
+            w[size_t(y) * ow + x] = acc * pano_cell_area(ow, oh, y);
+            total += w[size_t(y) * ow + x];
+        }
+    double cum = 0;
+    for (size_t i = 0; i < n; ++i) {
+        cum += total > 0 ? w[i] / total : pano_cell_area(ow, oh, uint32_t(i / ow)) / (4.0 * pi);
+        out.texels[i * 4 + 3] = float(std::min(cum, 1.0));
+    }
+    out.texels[(n - 1) * 4 + 3] = 1.0f;
+    return true;
+}
+// environment.wgsl:7-107.
+template <class R> static V3<R> hdri_local(const Light<R>& l, V3<R> d) {
+    return V3<R>(l.a.x * d.x + l.a.y * d.z, d.y, -l.a.y * d.x + l.a.x * d.z);
+}
+template <class R> static V3<R> hdri_world(const Light<R>& l, V3<R> d) {
+    return V3<R>(l.a.x * d.x - l.a.y * d.z, d.y, l.a.y * d.x + l.a.x * d.z);
+}
+template <class R> static void hdri_uv(const Light<R>& l, V3<R> dir, R* u, R* v) {
+    V3<R> q = hdri_local(l, dir);
+    R x = r_atan2(q.z, q.x) / (R(2) * R(PI_W)) + R(1);
+    *u = x - std::floor(x);
+    *v = std::acos(r_clamp(q.y, R(-1), R(1))) / R(PI_W);
+}
+template <class R> static R hdri_cell_area(const Light<R>& l, uint32_t row) {
+    R step = R(PI_W) / R(float(l.pano->h));
+    return (R(2) * R(PI_W) / R(float(l.pano->w))) * R(2) * r_sin((R(float(row)) + R(0.5)) * step) * r_sin(step * R(0.5));
+}
+template <class R> static V3<R> hdri_texel(const Light<R>& l, int x, int y) {
+    const int w = int(l.pano->w);
+    const uint32_t col = uint32_t(((x % w) + w) % w), row = uint32_t(std::min(std::max(y, 0), int(l.pano->h) - 1));
+    const float* t = &l.pano->texels[(size_t(row) * l.pano->w + col) * 4];
+    return V3<R>(R(t[0]), R(t[1]), R(t[2]));
+}
+template <class R> static V3<R> hdri_lookup(const Light<R>& l, V3<R> dir) {
+    if (!l.pano) return V3<R>(0, 0, 0);
+    R u, v;
+    hdri_uv(l, dir, &u, &v);
+    R px = u * R(float(l.pano->w)) - R(0.5), py = v * R(float(l.pano->h)) - R(0.5);
+    R bx = std::floor(px), by = std::floor(py);
+    R fx = px - bx, fy = py - by;
+    int x = int(bx), y = int(by);
+    V3<R> top = mixv(hdri_texel(l, x, y), hdri_texel(l, x + 1, y), fx);
+    V3<R> bottom = mixv(hdri_texel(l, x, y + 1), hdri_texel(l, x + 1, y + 1), fx);
+    return mixv(top, bottom, fy) * l.color.x;
+}
+template <class R> static R hdri_pdf(const Light<R>& l, V3<R> dir) {
+    const R mix = R(0.0625);
+    if (!l.pano || l.a.z > R(0)) return R(1) / (R(4) * R(PI_W));
+    R u, v;
+    hdri_uv(l, dir, &u, &v);
+    const uint32_t col = std::min(uint32_t(u * R(float(l.pano->w))), l.pano->w - 1);
+    const uint32_t row = std::min(uint32_t(v * R(float(l.pano->h))), l.pano->h - 1);
+    const size_t index = size_t(row) * l.pano->w + col;
+    const R before = index > 0 ? R(l.pano->texels[(index - 1) * 4 + 3]) : R(0);
+    const R mass = r_max(R(l.pano->texels[index * 4 + 3]) - before, R(0));
+    return (R(1) - mix) * mass / hdri_cell_area(l, row) + mix / (R(4) * R(PI_W));
+}
+template <class R> static V3<R> hdri_sample(const Light<R>& l, R r0, R r1, R r2) {
+    const R mix = R(0.0625);
+    R phi = R(2) * R(PI_W) * r1;
+    R cos_theta = R(1) - R(2) * r2;
+    R sin_squared = r_max(R(0), R(1) - cos_theta * cos_theta);
+    if (l.pano && l.a.z <= R(0) && r0 >= mix) {
+        const R cdf_sample = (r0 - mix) / (R(1) - mix);
+        uint32_t lo = 0, hi = l.pano->w * l.pano->h;
+        while (lo < hi) {
+            const uint32_t mid = lo + (hi - lo) / 2u;
+            if (R(l.pano->texels[size_t(mid) * 4 + 3]) <= cdf_sample) lo = mid + 1u;
+            else hi = mid;
+        }
+        const uint32_t index = std::min(lo, l.pano->w * l.pano->h - 1u);
+        const uint32_t col = index % l.pano->w, row = index / l.pano->w;
+        phi = R(2) * R(PI_W) * (R(float(col)) + r1) / R(float(l.pano->w));
+        const R top = R(PI_W) * R(float(row)) / R(float(l.pano->h));
+        const R bottom = R(PI_W) * R(float(row + 1)) / R(float(l.pano->h));
+        const R band = R(2) * r_sin((top + bottom) * R(0.5)) * r_sin((bottom - top) * R(0.5));
+        const R cap = R(2) * r_sin(top * R(0.5)) * r_sin(top * R(0.5)) + r2 * band;
+        const R lower_cap = R(2) * r_cos(bottom * R(0.5)) * r_cos(bottom * R(0.5)) + (R(1) - r2) * band;
+        if (row < l.pano->h / 2u) { cos_theta = R(1) - cap; sin_squared = cap * (R(2) - cap); }
+        else { cos_theta = lower_cap - R(1); sin_squared = lower_cap * (R(2) - lower_cap); }
+    }
+    const R sin_theta = r_sqrt(r_max(R(0), sin_squared));
+    return hdri_world(l, V3<R>(sin_theta * r_cos(phi), cos_theta, sin_theta * r_sin(phi)));
+}
+template <class R> static V3<R> hdri_emission(const Scene<R>& sc, V3<R> dir, R previous_pdf, bool use_mis) {
+    V3<R> L(0, 0, 0);
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        const Light<R>& l = sc.lights[i];
+        if (l.kind != SF_LIGHT_HDRI) continue;
+        R w = use_mis ? mis_power(previous_pdf, hdri_pdf(l, dir)) : R(1);
+        L = L + hdri_lookup(l, dir) * w;
+    }
+    return L;
+}
+
 // Sky lights (pathtrace.wgsl:149-215, :432-468).
 template <class R> static V3<R> environment_value(const Light<R>& l, V3<R> dir) {
     if (dir.y >= R(0)) return mixv(l.b, l.a, r_sqrt(dir.y));
@@ -1186,8 +1353,8 @@ static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd
     return h;
 }
 
-// radiance (pathtrace.wgsl:802-1201) with fog, optics, ocean, portals, guiding,
-// textures and HDRI disabled (those branches are identities when off),
+// radiance (pathtrace.wgsl:802-1201) with fog, optics, ocean, portals, guiding and
+// textures disabled (those branches are identities when off),
 // camera_ray (:781-800) and the per-sample film terms of main (:1203-1276).
 template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint32_t px, uint32_t py, uint32_t sample) {
     PixelResult res{};
@@ -1228,10 +1395,12 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
             }
             if (bounce == 0) { first_depth = h.t; aux[0] = gn.x; aux[1] = gn.y; aux[2] = gn.z; aux[3] = R(h.steps); }
         }
-        if (!h.hit) {  // the sky (pathtrace.wgsl:1026-1040)
-            if (!h.exhausted)
-                L = L + throughput * (environment_emission(sc, rd, prev_pdf, prev_from_bsdf, prev_normal, prev_area_total) +
-                                      sun_radiance(sc, rd, prev_pdf, prev_from_bsdf));
+        if (!h.hit) {  // the sky, the panoramas, the suns (pathtrace.wgsl:1026-1040)
+            if (!h.exhausted) {
+                L = L + throughput * environment_emission(sc, rd, prev_pdf, prev_from_bsdf, prev_normal, prev_area_total);
+                L = L + throughput * hdri_emission(sc, rd, prev_pdf, prev_from_bsdf);
+                L = L + throughput * sun_radiance(sc, rd, prev_pdf, prev_from_bsdf);
+            }
             break;
         }
         V3<R> p = ro + rd * h.t;
@@ -1300,6 +1469,19 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
                     L = L + throughput * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * w / pl);
+                } else if (l.kind == SF_LIGHT_HDRI) {
+                    if (l.color.x <= R(0)) continue;
+                    R r0 = rnd<R>(&rng);
+                    R r1 = rnd<R>(&rng);
+                    R r2 = rnd<R>(&rng);
+                    V3<R> ldir = hdri_sample(l, r0, r1, r2);
+                    R nl = s.n.dot(ldir);
+                    if (nl <= R(0) || n.dot(ldir) <= R(0)) continue;
+                    if (!visible(ldir, extent)) continue;
+                    R pl = hdri_pdf(l, ldir);
+                    R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
+                    R w = last ? R(1) : mis_power(pl, pb);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * w / pl);
                 } else if (l.kind == SF_LIGHT_SUN) {
                     R r1 = rnd<R>(&rng);
                     R r2 = rnd<R>(&rng);

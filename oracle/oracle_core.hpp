@@ -193,7 +193,18 @@ template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast = false
 template <class R> struct Camera { V3<R> origin, forward, right, up; R tan_half, aspect, lens_radius, focus_distance; };
 // kind 0 Area: a centre, b/c full edges, color radiance; 1 Sun: a unit direction,
 // color irradiance, cos_max; 2 Environment: a/b/c zenith/horizon/ground radiance.
-template <class R> struct Light { V3<R> a, b, c, color; uint32_t kind = 0; R cos_max = 1, energy = 0, peak = 0; };
+// A panorama's tables (environment.rs:271-366): w x h texels of (r, g, b, cdf).
+struct Panorama { uint32_t w = 0, h = 0; bool uniform = false; std::vector<float> texels; };
+bool panorama_tables(const float* rgb, uint32_t width, uint32_t height, Panorama& out);
+// Panoramas by the key the scene descriptor's environment field carries.
+void panorama_register(uint64_t key, const Panorama& p);
+const Panorama* panorama_find(uint64_t key);
+template <class R> struct Light {
+    V3<R> a, b, c, color;
+    uint32_t kind = 0;
+    R cos_max = 1, energy = 0, peak = 0;
+    const Panorama* pano = nullptr;  // HDRI: a = (cos, sin of the rotation, uniform), color.x = intensity
+};
 template <class R> struct Coloring {
     uint32_t slot = 0xffff, n = 0;
     bool cyclic = false, smooth = false, positioned = false;

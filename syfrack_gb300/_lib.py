@@ -114,6 +114,9 @@ SIGNATURES = {
     "sf_context_sync": [vp, u32],
     "sf_device_fp32_peak": [vp, P(C.c_double)],
     "sf_graph_validate": [P(abi.sf_graph_desc), P(abi.sf_graph_info)],
+    "sf_environment_build": [fp, u32, u32, fp, up, up, P(C.c_int)],
+    "sf_environment_create": [vp, fp, u32, u32, P(vp)],
+    "sf_environment_destroy": [vp],
     "sf_graph_compile": [vp, P(abi.sf_graph_desc), P(vp)],
     "sf_graph_info_get": [vp, P(abi.sf_graph_info)],
     "sf_graph_update": [vp, P(abi.sf_graph_desc)],

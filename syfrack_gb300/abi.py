@@ -75,7 +75,7 @@ class sf_material(C.Structure):
                 ("specular", C.c_float), ("emission", C.c_float * 3)]
 
 
-SF_LIGHT_AREA, SF_LIGHT_SUN, SF_LIGHT_ENVIRONMENT = 0, 1, 2
+SF_LIGHT_AREA, SF_LIGHT_SUN, SF_LIGHT_ENVIRONMENT, SF_LIGHT_HDRI = 0, 1, 2, 3
 SF_MAX_RAMP_STOPS = 16
 
 
@@ -83,7 +83,7 @@ class sf_area_light(C.Structure):
     _fields_ = [("center", C.c_float * 3), ("edge_u", C.c_float * 3), ("edge_v", C.c_float * 3),
                 ("radiance", C.c_float * 3), ("kind", C.c_uint32), ("direction", C.c_float * 3),
                 ("angular_size", C.c_float), ("zenith", C.c_float * 3), ("horizon", C.c_float * 3),
-                ("ground", C.c_float * 3)]
+                ("ground", C.c_float * 3), ("environment", C.c_void_p), ("rotation", C.c_float)]
 
 
 sf_light = sf_area_light

@@ -18,7 +18,7 @@ LIB = os.path.join(HERE, "libsyfrack_gpu.so")
 ARCH = ["-gencode", "arch=compute_103a,code=sm_103a"]
 UNITS = ["sf_kernels.cu", "sf_escape.cu", "sf_trace_box.cu", "sf_trace_bulb.cu", "sf_trace_menger.cu", "sf_trace_any.cu",
          "sf_batch.cu", "sf_noalloc.cu", "sf_preview.cu", "sf_host.cpp",
-         "sf_batch_host.cpp", "sf_serve.cpp", "sf_export.cpp", "sf_preview.cpp"]
+         "sf_batch_host.cpp", "sf_serve.cpp", "sf_export.cpp", "sf_preview.cpp", "sf_environment.cpp"]
 
 
 def nvcc() -> str:

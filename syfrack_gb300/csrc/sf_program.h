@@ -89,6 +89,8 @@ struct DeProgram {
 // SF_LIGHT_SUN: a = unit direction toward the sun, color = irradiance, cos_max;
 // SF_LIGHT_ENVIRONMENT: a/b/c = zenith/horizon/ground radiance, energy = their largest
 // luminance, peak = their largest component.
+// SF_LIGHT_HDRI: a.x/a.y = cos/sin of the rotation, a.z = 1 for uniform sampling,
+// color.x = intensity, texels = the panorama's (rgb, cdf) rows of tw x th texels.
 struct DevLight {
     float a[3], b[3], c[3], color[3];
     float n[3];          // safe_normalize(cross(b, c))
@@ -97,6 +99,8 @@ struct DevLight {
     float lum;           // luminance(color)
     uint32_t kind;
     float cos_max, energy, peak;
+    uint32_t tw, th;
+    uint64_t texels;     // device address of float4 texels (HDRI)
 };
 #define SF_MAX_RAMP 16
 

@@ -421,6 +421,98 @@ static __device__ float3 sun_radiance(const DevScene& S, float3 dir, float pdf_b
     }
     return L;
 }
+// HDRI panoramas (environment.wgsl:7-107): equirectangular texels (rgb, cdf), bilinear
+// lookups, and a CDF proposal mixed with 1/16 uniform sampling.
+#define SF_HDRI_UNIFORM_MIX 0.0625f
+__device__ __forceinline__ float3 hdri_local(const DevLight& l, float3 d) {
+    return mk3(fmaf(l.a[0], d.x, l.a[1] * d.z), d.y, fmaf(-l.a[1], d.x, l.a[0] * d.z));
+}
+__device__ __forceinline__ float3 hdri_world(const DevLight& l, float3 d) {
+    return mk3(fmaf(l.a[0], d.x, -(l.a[1] * d.z)), d.y, fmaf(l.a[1], d.x, l.a[0] * d.z));
+}
+__device__ __forceinline__ float2 hdri_uv(const DevLight& l, float3 dir) {
+    const float3 q = hdri_local(l, dir);
+    const float u = atan2f(q.z, q.x) / (2.0f * SF_PI) + 1.0f;
+    return make_float2(u - floorf(u), acosf(fminf(fmaxf(q.y, -1.0f), 1.0f)) / SF_PI);
+}
+__device__ __forceinline__ float hdri_cell_area(const DevLight& l, uint32_t row) {
+    const float step = SF_PI / float(l.th);
+    return (2.0f * SF_PI / float(l.tw)) * 2.0f * sinf((float(row) + 0.5f) * step) * sinf(step * 0.5f);
+}
+__device__ __forceinline__ float4 hdri_fetch(const DevLight& l, uint32_t index) {
+    return __ldg(reinterpret_cast<const float4*>(l.texels) + index);
+}
+__device__ __forceinline__ float3 hdri_texel(const DevLight& l, int x, int y) {
+    const int w = int(l.tw);
+    const uint32_t col = uint32_t(((x % w) + w) % w);
+    const uint32_t row = uint32_t(min(max(y, 0), int(l.th) - 1));
+    const float4 t = hdri_fetch(l, row * l.tw + col);
+    return mk3(t.x, t.y, t.z);
+}
+static __device__ float3 hdri_lookup(const DevLight& l, float3 dir) {
+    const float2 uv = hdri_uv(l, dir);
+    const float px = uv.x * float(l.tw) - 0.5f, py = uv.y * float(l.th) - 0.5f;
+    const float bx = floorf(px), by = floorf(py);
+    const float fx = px - bx, fy = py - by;
+    const int x = int(bx), y = int(by);
+    const float3 top = lerp3(hdri_texel(l, x, y), hdri_texel(l, x + 1, y), fx);
+    const float3 bottom = lerp3(hdri_texel(l, x, y + 1), hdri_texel(l, x + 1, y + 1), fx);
+    return lerp3(top, bottom, fy) * l.color[0];
+}
+static __device__ float hdri_pdf(const DevLight& l, float3 dir) {
+    if (l.a[2] > 0.0f) return 1.0f / (4.0f * SF_PI);
+    const float2 uv = hdri_uv(l, dir);
+    const uint32_t col = min(uint32_t(uv.x * float(l.tw)), l.tw - 1);
+    const uint32_t row = min(uint32_t(uv.y * float(l.th)), l.th - 1);
+    const uint32_t index = row * l.tw + col;
+    const float before = index > 0 ? hdri_fetch(l, index - 1).w : 0.0f;
+    const float mass = fmaxf(hdri_fetch(l, index).w - before, 0.0f);
+    return fmaf(1.0f - SF_HDRI_UNIFORM_MIX, wdiv(mass, hdri_cell_area(l, row)), SF_HDRI_UNIFORM_MIX / (4.0f * SF_PI));
+}
+static __device__ float3 hdri_sample(const DevLight& l, float r0, float r1, float r2) {
+    float phi = 2.0f * SF_PI * r1;
+    float cos_theta = 1.0f - 2.0f * r2;
+    float sin_squared = fmaxf(0.0f, fmaf(-cos_theta, cos_theta, 1.0f));
+    if (l.a[2] <= 0.0f && r0 >= SF_HDRI_UNIFORM_MIX) {
+        const float cdf_sample = wdiv(r0 - SF_HDRI_UNIFORM_MIX, 1.0f - SF_HDRI_UNIFORM_MIX);
+        uint32_t lo = 0, hi = l.tw * l.th;
+        while (lo < hi) {  // the first texel whose cumulative share exceeds the sample
+            const uint32_t mid = lo + (hi - lo) / 2u;
+            if (hdri_fetch(l, mid).w <= cdf_sample) lo = mid + 1u;
+            else hi = mid;
+        }
+        const uint32_t index = min(lo, l.tw * l.th - 1u);
+        const uint32_t col = index % l.tw, row = index / l.tw;
+        phi = 2.0f * SF_PI * (float(col) + r1) / float(l.tw);
+        const float top = SF_PI * float(row) / float(l.th);
+        const float bottom = SF_PI * float(row + 1u) / float(l.th);
+        const float band = 2.0f * sinf((top + bottom) * 0.5f) * sinf((bottom - top) * 0.5f);
+        const float cap = fmaf(r2, band, 2.0f * sinf(top * 0.5f) * sinf(top * 0.5f));
+        const float lower_cap = fmaf(1.0f - r2, band, 2.0f * cosf(bottom * 0.5f) * cosf(bottom * 0.5f));
+        if (row < l.th / 2u) {
+            cos_theta = 1.0f - cap;
+            sin_squared = cap * (2.0f - cap);
+        } else {
+            cos_theta = lower_cap - 1.0f;
+            sin_squared = lower_cap * (2.0f - lower_cap);
+        }
+    }
+    const float sin_theta = wsqrt(fmaxf(0.0f, sin_squared));
+    float sp, cp;
+    sincosf(phi, &sp, &cp);
+    return hdri_world(l, mk3(sin_theta * cp, cos_theta, sin_theta * sp));
+}
+static __device__ float3 hdri_emission(const DevScene& S, float3 dir, float previous_pdf, bool use_mis) {
+    float3 L = mk3(0.f, 0.f, 0.f);
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        if (l.kind != SF_LIGHT_HDRI) continue;
+        const float w = use_mis ? mis_power(previous_pdf, hdri_pdf(l, dir)) : 1.0f;
+        L = L + hdri_lookup(l, dir) * w;
+    }
+    return L;
+}
+
 // cone_sample (pathtrace.wgsl:210-215).
 __device__ __forceinline__ float3 cone_sample(float3 dir, float cos_max, float r1, float r2) {
     const float cos_t = 1.0f - r1 * (1.0f - cos_max);
@@ -442,10 +534,11 @@ template <class Emit>
 static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, Emit&& emit, float* first_depth,
                                   float4* first_aux) {
     if (!h.hit) {
-        if (!h.exhausted) {  // the sky (pathtrace.wgsl:1026-1040)
-            ps.L = ps.L + ps.tp * (environment_emission(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
-                                                        ps.prev_area_total) +
-                                   sun_radiance(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf));
+        if (!h.exhausted) {  // the sky, the panoramas, the suns (pathtrace.wgsl:1026-1040)
+            ps.L = ps.L + ps.tp * environment_emission(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
+                                                       ps.prev_area_total);
+            ps.L = ps.L + ps.tp * hdri_emission(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf);
+            ps.L = ps.L + ps.tp * sun_radiance(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf);
         }
         return PATH_DONE;
     }
@@ -514,6 +607,23 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             sh.dir = ldir;
             sh.t_end = S.extent;
             sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * wdiv(w, pl));
+            emit(sh);
+        } else if (l.kind == SF_LIGHT_HDRI) {
+            if (l.color[0] <= 0.0f) continue;
+            const float r0 = rnd(ps.rng);
+            const float r1 = rnd(ps.rng);
+            const float r2 = rnd(ps.rng);
+            const float3 ldir = hdri_sample(l, r0, r1, r2);
+            const float nl = dot3(s.n, ldir);
+            if (nl <= 0.0f || dot3(n, ldir) <= 0.0f) continue;
+            const float pl = hdri_pdf(l, ldir);
+            const float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
+            const float w = last ? 1.0f : mis_power(pl, pb);
+            ShadowReq sh;
+            sh.o = p_off;
+            sh.dir = ldir;
+            sh.t_end = S.extent;
+            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * wdiv(w, pl));
             emit(sh);
         } else if (l.kind == SF_LIGHT_SUN) {
             const float r1 = rnd(ps.rng);

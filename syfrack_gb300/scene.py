@@ -182,6 +182,70 @@ class EnvironmentLight:
         return out
 
 
+def panorama_tables(rgb):
+    """EnvironmentMap::from_rgb through the library, on the host only: (texels[h, w, 4]
+    of rgb and cumulative distribution, uniform)."""
+    import ctypes as C
+
+    from ._lib import check, load
+
+    rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+    h, w = rgb.shape[:2]
+    lib = load()
+    fp = C.POINTER(C.c_float)
+    ow, oh, uni = C.c_uint32(), C.c_uint32(), C.c_int()
+    check(lib.sf_environment_build(rgb.ctypes.data_as(fp), w, h, None, C.byref(ow), C.byref(oh), C.byref(uni)))
+    out = np.zeros((oh.value, ow.value, 4), np.float32)
+    check(lib.sf_environment_build(rgb.ctypes.data_as(fp), w, h, out.ctypes.data_as(fp), C.byref(ow), C.byref(oh),
+                                   C.byref(uni)))
+    return out, bool(uni.value)
+
+
+class Panorama:
+    """An equirectangular linear RGB panorama on the device (sf_environment_create):
+    rgb[h, w, 3], row 0 at the zenith. Keep it alive while scenes render with it."""
+
+    def __init__(self, ctx, rgb):
+        import ctypes as C
+
+        from ._lib import check
+
+        self.ctx = ctx
+        self.rgb = np.ascontiguousarray(rgb, dtype=np.float32)
+        h, w = self.rgb.shape[:2]
+        handle = C.c_void_p()
+        check(ctx.lib.sf_environment_create(ctx.h, self.rgb.ctypes.data_as(C.POINTER(C.c_float)), w, h,
+                                            C.byref(handle)))
+        self.h = handle
+
+    def close(self):
+        if getattr(self, "h", None):
+            self.ctx.lib.sf_environment_destroy(self.h)
+            self.h = None
+
+    def __del__(self):
+        try:
+            self.close()
+        except Exception:
+            pass
+
+
+@dataclass
+class HdriLight:
+    """Light::Hdri{intensity, rotation (degrees about +y)} over a Panorama."""
+    panorama: Panorama = None
+    intensity: float = 1.0
+    rotation: float = 0.0
+
+    def packed(self) -> abi.sf_area_light:
+        out = abi.sf_area_light()
+        out.kind = abi.SF_LIGHT_HDRI
+        out.environment = self.panorama.h.value if self.panorama is not None else None
+        out.radiance[0] = self.intensity
+        out.rotation = self.rotation
+        return out
+
+
 @dataclass
 class Ramp:
     """Ramp (palette.rs:74-100): stops, optional positions, cyclic, frequency, phase, gamma."""
