@@ -237,6 +237,15 @@ typedef struct sf_coloring {
     uint32_t cyclic, smooth, positioned;
     float frequency, phase, gamma;
 } sf_coloring;
+/* Height fog, Atmosphere (atmosphere.rs:7-28) as GpuAtmosphere.a/b (uniforms.rs:217-227):
+ * extinction `density` at and below `height`, decaying as exp(-(y - height) * falloff)
+ * above it; Henyey-Greenstein `anisotropy` (-0.99..0.99); scattering albedo `color`.
+ * density 0 = no fog. A fog scene issues one shadow segment per area light for its
+ * line integral besides the surface's: at most 8 shadow segments per bounce. */
+typedef struct sf_fog {
+    float density, height, falloff, anisotropy;
+    float color[3];
+} sf_fog;
 typedef struct sf_scene_desc {
     sf_camera camera;
     sf_material material;                 /* index 0: the global surface */
@@ -250,6 +259,7 @@ typedef struct sf_scene_desc {
     float cavity_darkness;                /* atmosphere.b.w, 0 = off */
     uint64_t seed;                        /* Scene.seed; the device uses lo ^ hi */
     sf_coloring coloring;                 /* slot 0xffff (or no stops): no colouring */
+    sf_fog fog;
 } sf_scene_desc;
 
 /* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138). */
@@ -317,11 +327,13 @@ typedef struct sf_session sf_session;
 typedef struct sf_progress {
     uint32_t tiles, dispatches, samples_min, samples_max, target;
     uint64_t pixel_samples_done, pixel_samples_total;
-    uint32_t status_word;   /* wavefront invariant bits 1/2/4 (wavefront.wgsl:183,:220,:236) */
+    uint32_t status_word;   /* wavefront invariant bits 1/2/4 (wavefront.wgsl:183,:220,:236); 8 = a bounce
+                               issued more shadow segments than the arena holds */
 } sf_progress;
-/* The film planes of wf_commit (wavefront.wgsl:232-260). This path has no fog or
- * volumes, so the volume contribution is zero: volume and moments hold (0, 0, 0,
- * samples) and surface (= radiance - volume) equals accum. Any pointer may be NULL. */
+/* The film planes of wf_commit (wavefront.wgsl:232-260). The volume layer split
+ * (pathtrace.wgsl:1197-1199: primary in-scattering and paths that first scatter in fog)
+ * is not kept: fog radiance is in accum, volume and moments hold (0, 0, 0, samples)
+ * and surface (= radiance - volume) equals accum. Any pointer may be NULL. */
 typedef struct sf_film_planes {
     float* accum;   /* 4*width*height: rgb sums and sample count */
     float* depth;   /* width*height */

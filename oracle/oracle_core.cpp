@@ -851,6 +851,11 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
     s.var_metal[0] = R(d.variation_metallic[0]);
     s.var_metal[1] = R(d.variation_metallic[1]);
     s.cavity = R(d.cavity_darkness);
+    s.fog[0] = R(d.fog.density);
+    s.fog[1] = R(d.fog.height);
+    s.fog[2] = R(d.fog.falloff);
+    s.fog[3] = R(d.fog.anisotropy);
+    s.fog_color = V3<R>(R(d.fog.color[0]), R(d.fog.color[1]), R(d.fog.color[2]));
     s.seed = uint32_t(d.seed) ^ uint32_t(d.seed >> 32);
     s.pixel_tolerance = R(c.pixel_tolerance);
     // uniforms.rs:781-782: far = max(2*hint + |origin|, 200), computed in f32.
@@ -1301,13 +1306,17 @@ template <class R> static R environment_probability(const Light<R>& l, R area_to
     return r_clamp(e / (e + area_total), R(0.05), R(1));
 }
 template <class R>
-static V3<R> environment_emission(const Scene<R>& sc, V3<R> dir, R pdf, bool use_mis, V3<R> n, R area_total) {
+static V3<R> environment_emission(const Scene<R>& sc, V3<R> dir, R pdf, bool use_mis, V3<R> n, bool from_volume,
+                                  R area_total) {
     V3<R> L(0, 0, 0);
     for (uint32_t i = 0; i < sc.light_count; ++i) {
         const Light<R>& l = sc.lights[i];
         if (l.kind != SF_LIGHT_ENVIRONMENT) continue;
         R w = 1;
-        if (use_mis) w = mis_power(pdf, environment_probability(l, area_total) * r_max(n.dot(dir), R(0)) / R(PI_W));
+        if (use_mis) {
+            const R proposal = from_volume ? R(1) / (R(4) * R(PI_W)) : r_max(n.dot(dir), R(0)) / R(PI_W);
+            w = mis_power(pdf, environment_probability(l, area_total) * proposal);
+        }
         L = L + environment_value(l, dir) * w;
     }
     return L;
@@ -1333,6 +1342,99 @@ template <class R> static V3<R> cone_sample(V3<R> dir, R cos_max, R r1, R r2) {
     return t * (sin_t * r_cos(phi)) + bt * (sin_t * r_sin(phi)) + dir * cos_t;
 }
 
+// ---------------------------------------------------------------- height fog
+// fog_sigma .. fog_free_flight (pathtrace.wgsl:562-615).
+template <class R> static R fog_sigma(const Scene<R>& sc, V3<R> p) {
+    return sc.fog[0] * r_exp(r_min(R(0), -(p.y - sc.fog[1]) * sc.fog[2]));
+}
+template <class R> static R fog_segment_tau(const Scene<R>& sc, V3<R> ro, V3<R> rd, R begin, R end) {
+    const R distance = r_max(end - begin, R(0));
+    if (distance == R(0)) return 0;
+    const R sigma = fog_sigma(sc, ro + rd * begin);
+    const R mid_height = (ro + rd * ((begin + end) * R(0.5))).y;
+    if (mid_height <= sc.fog[1] || sc.fog[2] == R(0)) return sc.fog[0] * distance;
+    const R k = rd.y * sc.fog[2];
+    const R x = k * distance;
+    if (r_abs(x) < R(0.001)) return sigma * distance * (R(1) - x * R(0.5) + x * x / R(6));
+    return r_max(R(0), (sigma - fog_sigma(sc, ro + rd * end)) / k);
+}
+template <class R> static R fog_split(const Scene<R>& sc, V3<R> ro, V3<R> rd, R distance) {
+    if (r_abs(rd.y) < R(1e-8)) return distance;
+    return r_clamp((sc.fog[1] - ro.y) / rd.y, R(0), distance);
+}
+template <class R> static R fog_optical_depth(const Scene<R>& sc, V3<R> ro, V3<R> rd, R distance) {
+    const R split = fog_split(sc, ro, rd, distance);
+    return fog_segment_tau(sc, ro, rd, R(0), split) + fog_segment_tau(sc, ro, rd, split, distance);
+}
+template <class R> static R fog_transmittance(const Scene<R>& sc, V3<R> ro, V3<R> rd, R distance) {
+    return r_exp(-fog_optical_depth(sc, ro, rd, distance));
+}
+template <class R> static R fog_invert_segment(const Scene<R>& sc, V3<R> ro, V3<R> rd, R begin, R end, R tau) {
+    const R sigma = fog_sigma(sc, ro + rd * begin);
+    const R k = rd.y * sc.fog[2];
+    if ((ro + rd * ((begin + end) * R(0.5))).y <= sc.fog[1] || r_abs(k * (end - begin)) < R(0.0001))
+        return r_min(end, begin + tau / r_max(sigma, R(1e-30)));
+    if (sigma > R(1e-20)) return r_clamp(begin - r_log(r_max(R(1e-7), R(1) - tau * k / sigma)) / k, begin, end);
+    const R remaining = r_max(R(0), fog_segment_tau(sc, ro, rd, begin, end) - tau);
+    const R end_sigma = fog_sigma(sc, ro + rd * end);
+    return r_clamp(end + r_log(r_max(R(1e-7), R(1) + remaining * k / r_max(end_sigma, R(1e-30)))) / (-k), begin, end);
+}
+template <class R> static R fog_free_flight(const Scene<R>& sc, V3<R> ro, V3<R> rd, R t_end, uint32_t* rng) {
+    if (sc.fog[0] <= R(0)) return t_end;
+    const R tau = -r_log(r_max(R(1) - rnd<R>(rng), R(1e-7)));
+    const R split = fog_split(sc, ro, rd, t_end);
+    const R first = fog_segment_tau(sc, ro, rd, R(0), split);
+    const R total = first + fog_segment_tau(sc, ro, rd, split, t_end);
+    if (tau >= total) return t_end;
+    if (tau < first) return fog_invert_segment(sc, ro, rd, R(0), split, tau);
+    return fog_invert_segment(sc, ro, rd, split, t_end, tau - first);
+}
+// hg_phase, hg_sample (pathtrace.wgsl:717-731).
+template <class R> static R hg_phase(R cos_theta, R g) {
+    const R d = R(1) + g * g - R(2) * g * cos_theta;
+    return (R(1) - g * g) / (R(4) * R(PI_W) * d * r_sqrt(d));
+}
+template <class R> static V3<R> hg_sample(V3<R> dir, R g, R r1, R r2) {
+    R cos_t = R(1) - R(2) * r1;
+    if (r_abs(g) > R(1e-3)) {
+        const R sq = (R(1) - g * g) / (R(1) - g + R(2) * g * r1);
+        cos_t = (R(1) + g * g - sq * sq) / (R(2) * g);
+    }
+    const R sin_t = r_sqrt(r_max(R(0), R(1) - cos_t * cos_t));
+    const R phi = R(2) * R(PI_W) * r2;
+    V3<R> t, bt;
+    tangent_frame(dir, &t, &bt);
+    return t * (sin_t * r_cos(phi)) + bt * (sin_t * r_sin(phi)) + dir * cos_t;
+}
+// volume_coordinate (pathtrace.wgsl:43-58), computed in f32 as the shader does.
+static float volume_coordinate(uint32_t sample_index, uint32_t dimension, uint32_t stream) {
+    static const uint32_t bases[6] = {2, 3, 5, 7, 11, 13};
+    const uint32_t base = bases[dimension];
+    uint32_t index = sample_index + 1u;
+    float inverse = 1.0f / float(base);
+    float value = 0.0f;
+    while (index != 0u) {
+        value += float(index % base) * inverse;
+        index /= base;
+        inverse /= float(base);
+    }
+    const float shift = float(pcg(stream ^ (dimension * 0x9e3779b9u)) >> 8u) / 16777216.0f;
+    const float v = value + shift;
+    return v - std::floor(v);
+}
+// fog_segment_weight (pathtrace.wgsl:621-633) and volume_light_probability
+// (lights.wgsl:319-323) for rectangles.
+template <class R> static R fog_segment_weight(V3<R> ro, V3<R> rd, R end, const Light<R>& l) {
+    const R along = r_clamp((l.a - ro).dot(rd), R(0), end);
+    const V3<R> delta = l.a - (ro + rd * along);
+    const R area = emitter_area(l);
+    return r_max(r_max(l.color.x, l.color.y), l.color.z) * area / (delta.dot(delta) + area);
+}
+template <class R> static R volume_light_probability(R weight, R total) {
+    if (total <= R(0)) return 0;
+    return r_min(R(1), R(3) * weight / total);
+}
+
 // trace_geometry_lights (lights.wgsl:183-209) around march_segment.
 template <class R>
 static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd, R pixel_cone, R t_end, uint64_t* evals) {
@@ -1353,8 +1455,139 @@ static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd
     return h;
 }
 
-// radiance (pathtrace.wgsl:802-1201) with fog, optics, ocean, portals, guiding and
-// textures disabled (those branches are identities when off),
+// fog_segment_direct (pathtrace.wgsl:635-715) for rectangles: every area light's
+// independent roulette, a point on the segment by one-sample MIS of equiangular and
+// optical-depth sampling, a visibility test from there to a point on the light.
+// Returns the segment's in-scattered radiance (times the fog colour).
+template <class R, class Visible>
+static V3<R> fog_segment_direct(const Scene<R>& sc, V3<R> ro, V3<R> rd, R end, uint32_t* rng, uint32_t point_index,
+                                uint32_t point_stream, bool primary, Visible&& visible) {
+    V3<R> result(0, 0, 0);
+    if (end <= R(0) || r_max(r_max(sc.fog_color.x, sc.fog_color.y), sc.fog_color.z) <= R(0)) return result;
+    const R tau_end = fog_optical_depth(sc, ro, rd, end);
+    if (tau_end <= R(0)) return result;
+    R total = 0;
+    for (uint32_t i = 0; i < sc.light_count; ++i)
+        if (sc.lights[i].kind == SF_LIGHT_AREA) total += fog_segment_weight(ro, rd, end, sc.lights[i]);
+    const R g = sc.fog[3];
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        const Light<R>& l = sc.lights[i];
+        if (l.kind != SF_LIGHT_AREA) continue;
+        const R probability = volume_light_probability(fog_segment_weight(ro, rd, end, l), total);
+        const uint32_t stream = pcg(point_stream ^ (i * 0x85ebca6bu));
+        R selection = rnd<R>(rng);
+        if (primary) selection = R(volume_coordinate(point_index, 5, stream));
+        if (probability <= R(0) || selection >= probability) continue;
+        R u1 = rnd<R>(rng);
+        R u2 = rnd<R>(rng);
+        if (primary) {
+            u1 = R(volume_coordinate(point_index, 0, stream));
+            u2 = R(volume_coordinate(point_index, 1, stream));
+        }
+        const V3<R> q = l.a + l.b * (u1 - R(0.5)) + l.c * (u2 - R(0.5));
+        const R tau_begin = fog_optical_depth(sc, ro, rd, R(0));
+        const R tau_finish = fog_optical_depth(sc, ro, rd, end);
+        const R tau_span = r_max(R(0), tau_finish - tau_begin);
+        if (tau_span <= R(0)) continue;
+        R conditional_mass = R(1) - r_exp(-tau_span);
+        if (tau_span < R(0.001)) conditional_mass = tau_span * (R(1) - tau_span * R(0.5) + tau_span * tau_span / R(6));
+        const R interval_mass = r_exp(-tau_begin) * conditional_mass;
+        if (interval_mass < R(1e-30)) continue;
+        const V3<R> delta = q - ro;
+        const R projection = delta.dot(rd);
+        const R perpendicular = (delta - rd * projection).length();
+        const R theta_a = r_atan2(R(0) - projection, r_max(perpendicular, R(1e-6)));
+        const R theta_b = r_atan2(end - projection, r_max(perpendicular, R(1e-6)));
+        const R span = theta_b - theta_a;
+        const bool regular = perpendicular > R(1e-4) && span > R(1e-5);
+        R xi = rnd<R>(rng);
+        R technique = rnd<R>(rng);
+        if (primary) {
+            xi = R(volume_coordinate(point_index, 3, stream));
+            technique = R(volume_coordinate(point_index, 4, stream));
+        }
+        R t = end * xi;  // mix(0, end, xi)
+        if (technique < R(0.5)) {
+            if (regular)
+                t = r_clamp(projection + perpendicular * r_tan(theta_a * (R(1) - xi) + theta_b * xi), R(0), end);
+        } else {
+            const R tau = tau_begin - r_log(r_max(R(1) - xi * conditional_mass, R(1e-7)));
+            const R split = fog_split(sc, ro, rd, end);
+            const R first = fog_segment_tau(sc, ro, rd, R(0), split);
+            t = tau < first ? fog_invert_segment(sc, ro, rd, R(0), split, tau)
+                            : fog_invert_segment(sc, ro, rd, split, end, tau - first);
+        }
+        const V3<R> p = ro + rd * t;
+        const R transmittance = r_exp(-fog_optical_depth(sc, ro, rd, t));
+        const R sigma = fog_sigma(sc, p);
+        R angular_pdf = R(1) / end;
+        if (regular)
+            angular_pdf = perpendicular / (span * (perpendicular * perpendicular + (t - projection) * (t - projection)));
+        const R distance_pdf = R(0.5) * (angular_pdf + sigma * transmittance / interval_mass);
+        const V3<R> to_light = q - p;
+        const R distance2 = to_light.dot(to_light);
+        if (distance2 < R(1e-8)) continue;
+        const R distance = r_sqrt(distance2);
+        const V3<R> wi = to_light / distance;
+        const R cosine = area_normal(l).dot(-wi);
+        if (cosine <= R(0)) continue;
+        if (!visible(p, wi, r_max(R(0), distance - r_max(R(1e-5), distance * R(1e-6))))) continue;
+        const R tr = transmittance * r_exp(-fog_optical_depth(sc, p, wi, distance));
+        result = result + l.color * (sigma * tr * hg_phase(rd.dot(wi), g) /
+                                     (probability * distance_pdf * area_direction_pdf(l, distance2, cosine)));
+    }
+    return result * sc.fog_color;
+}
+// fog_direct_light (pathtrace.wgsl:733-772): a scattering point's next events for the
+// sky lights, phase function in place of the BRDF.
+template <class R, class Visible>
+static V3<R> fog_direct_light(const Scene<R>& sc, V3<R> p, V3<R> rd, R area_total, bool last, uint32_t* rng,
+                              Visible&& visible) {
+    const R g = sc.fog[3];
+    const R extent = r_max(R(200), sc.far);
+    V3<R> L(0, 0, 0);
+    for (uint32_t i = 0; i < sc.light_count; ++i) {
+        const Light<R>& l = sc.lights[i];
+        if (l.kind == SF_LIGHT_ENVIRONMENT) {
+            if (l.peak <= R(0)) continue;
+            const R probability = environment_probability(l, area_total);
+            if (rnd<R>(rng) >= probability) continue;
+            const R z = R(1) - R(2) * rnd<R>(rng);
+            const R phi = R(2) * R(PI_W) * rnd<R>(rng);
+            const R radius = r_sqrt(r_max(R(0), R(1) - z * z));
+            const V3<R> dir(radius * r_cos(phi), z, radius * r_sin(phi));
+            if (!visible(p, dir, extent)) continue;
+            const R tr = fog_transmittance(sc, p, dir, extent);
+            const R ph = hg_phase(rd.dot(dir), g);
+            const R pl = probability / (R(4) * R(PI_W));
+            L = L + environment_value(l, dir) * ph * tr * (last ? R(1) : mis_power(pl, ph)) / pl;
+        } else if (l.kind == SF_LIGHT_HDRI) {
+            if (l.color.x <= R(0)) continue;
+            const R r0 = rnd<R>(rng);
+            const R r1 = rnd<R>(rng);
+            const R r2 = rnd<R>(rng);
+            const V3<R> dir = hdri_sample(l, r0, r1, r2);
+            if (!visible(p, dir, extent)) continue;
+            const R tr = fog_transmittance(sc, p, dir, extent);
+            const R ph = hg_phase(rd.dot(dir), g);
+            const R pl = hdri_pdf(l, dir);
+            L = L + hdri_lookup(l, dir) * ph * tr * (last ? R(1) : mis_power(pl, ph)) / pl;
+        } else if (l.kind == SF_LIGHT_SUN) {
+            const R r1 = rnd<R>(rng);
+            const R r2 = rnd<R>(rng);
+            const V3<R> dir = cone_sample(l.a, l.cos_max, r1, r2);
+            if (!visible(p, dir, extent)) continue;
+            const R tr = fog_transmittance(sc, p, dir, extent);
+            const R ph = hg_phase(rd.dot(dir), g);
+            const R pl = sun_pdf(l.cos_max);
+            L = L + l.color * ph * tr * (last ? R(1) : mis_power(pl, ph));
+        }
+    }
+    return L;
+}
+
+// radiance (pathtrace.wgsl:802-1201) with the height fog, and with optics, ocean,
+// portals, nebulae, guiding and textures disabled (those branches are identities when off),
 // camera_ray (:781-800) and the per-sample film terms of main (:1203-1276).
 template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint32_t px, uint32_t py, uint32_t sample) {
     PixelResult res{};
@@ -1380,6 +1613,14 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
     R prev_pdf = 0, prev_area_total = 0;
     bool prev_from_bsdf = false;
     V3<R> prev_normal(0, 0, 0);
+    bool prev_from_volume = false;  // prev_volume_nee is the same flag without ocean and nebulae
+    const uint32_t point_stream = pcg(pcg(px ^ sc.seed) ^ pcg(py ^ 0x27d4eb2du));
+    const bool in_fog = sc.fog[0] > R(0);
+    auto visible_from = [&](V3<R> o, V3<R> dir, R t_end) {
+        Hit<R> sh = trace_scene(g, sc, o, dir, pixel_cone, t_end, &res.de_evals);
+        res.segments++;
+        return !sh.hit && !sh.exhausted;
+    };
     R first_depth = -1;
     R aux[4] = {0, 0, 0, -1};
     R extent = r_max(R(200), sc.far);
@@ -1395,9 +1636,38 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
             }
             if (bounce == 0) { first_depth = h.t; aux[0] = gn.x; aux[1] = gn.y; aux[2] = gn.z; aux[3] = R(h.steps); }
         }
+        if (in_fog) {  // pathtrace.wgsl:980-1011
+            const R t_end = h.hit ? h.t : extent;
+            L = L + throughput * fog_segment_direct(sc, ro, rd, t_end, &rng, sample, point_stream, bounce == 0,
+                                                    visible_from);
+            const R t_s = fog_free_flight(sc, ro, rd, t_end, &rng);
+            if (t_s < t_end) {
+                if (bounce == 0 && !h.hit) first_depth = t_s;
+                const V3<R> p_s = ro + rd * t_s;
+                const R volume_area_total = area_total_weight(sc, p_s, V3<R>(0, 0, 0));
+                const bool last = bounce == sc.max_bounces;
+                L = L + throughput * sc.fog_color *
+                            fog_direct_light(sc, p_s, rd, volume_area_total, last, &rng, visible_from);
+                throughput = throughput * sc.fog_color;
+                if (last) break;
+                const R r1 = rnd<R>(&rng);
+                const R r2 = rnd<R>(&rng);
+                const V3<R> nd = hg_sample(rd, sc.fog[3], r1, r2);
+                prev_pdf = hg_phase(rd.dot(nd), sc.fog[3]);
+                prev_from_bsdf = true;
+                prev_from_volume = true;
+                prev_normal = V3<R>(0, 0, 0);
+                prev_area_total = volume_area_total;
+                ro = p_s;
+                rd = nd;
+                bounce++;
+                continue;
+            }
+        }
         if (!h.hit) {  // the sky, the panoramas, the suns (pathtrace.wgsl:1026-1040)
             if (!h.exhausted) {
-                L = L + throughput * environment_emission(sc, rd, prev_pdf, prev_from_bsdf, prev_normal, prev_area_total);
+                L = L + throughput * environment_emission(sc, rd, prev_pdf, prev_from_bsdf, prev_normal,
+                                                          prev_from_volume, prev_area_total);
                 L = L + throughput * hdri_emission(sc, rd, prev_pdf, prev_from_bsdf);
                 L = L + throughput * sun_radiance(sc, rd, prev_pdf, prev_from_bsdf);
             }
@@ -1410,7 +1680,10 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                 V3<R> en = area_normal(sc.lights[h.light_index]);
                 aux[0] = en.x; aux[1] = en.y; aux[2] = en.z; aux[3] = R(h.steps);
             }
-            L = L + throughput * area_emission(sc, ro, rd, h.t, prev_pdf, prev_from_bsdf, prev_normal, prev_area_total);
+            // after a fog scattering point its segment estimate already holds the emitters
+            if (!prev_from_volume)
+                L = L + throughput * area_emission(sc, ro, rd, h.t, prev_pdf, prev_from_bsdf, prev_normal,
+                                                   prev_area_total);
             break;
         }
         V3<R> n = gn;
@@ -1448,11 +1721,9 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     }
                 }
             }
-            auto visible = [&](V3<R> dir, R t_end) {
-                Hit<R> sh = trace_scene(g, sc, p_off, dir, pixel_cone, t_end, &res.de_evals);
-                res.segments++;
-                return !sh.hit && !sh.exhausted;
-            };
+            auto visible = [&](V3<R> dir, R t_end) { return visible_from(p_off, dir, t_end); };
+            // direct_light's fog transmittance toward each light (pathtrace.wgsl:501-549)
+            auto fog_tr = [&](V3<R> dir, R dist) { return in_fog ? fog_transmittance(sc, p_off, dir, dist) : R(1); };
             for (uint32_t i = 0; i < sc.light_count; ++i) {
                 const Light<R>& l = sc.lights[i];
                 if (l.kind == SF_LIGHT_ENVIRONMENT) {
@@ -1468,7 +1739,8 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R pl = probability * nl / R(PI_W);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * w / pl);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) *
+                                          fog_tr(ldir, extent) * w / pl);
                 } else if (l.kind == SF_LIGHT_HDRI) {
                     if (l.color.x <= R(0)) continue;
                     R r0 = rnd<R>(&rng);
@@ -1481,7 +1753,8 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R pl = hdri_pdf(l, ldir);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * w / pl);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * fog_tr(ldir, extent) *
+                                          w / pl);
                 } else if (l.kind == SF_LIGHT_SUN) {
                     R r1 = rnd<R>(&rng);
                     R r2 = rnd<R>(&rng);
@@ -1492,7 +1765,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R pl = sun_pdf(l.cos_max);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * w);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * w * fog_tr(ldir, extent));
                 } else if (i == selected) {
                     R u1 = rnd<R>(&rng);
                     R u2 = rnd<R>(&rng);
@@ -1511,7 +1784,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R pl = (selected_weight / area_total) * area_direction_pdf(l, dist2, cos_l);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * R(1) * w / pl);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * fog_tr(ldir, dist) * w / pl);
                 }
             }
         }
@@ -1530,6 +1803,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
         throughput = throughput * (brdf_eval(s, v, ldir) * nl / pdf);
         prev_pdf = pdf;
         prev_from_bsdf = true;
+        prev_from_volume = false;
         prev_normal = s.n;
         prev_area_total = area_total;
         if (bounce >= 2) {

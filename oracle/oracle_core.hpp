@@ -39,6 +39,10 @@ inline float r_log(float x) { return logf(x); }
 inline double r_log(double x) { return std::log(x); }
 inline float r_log1p(float x) { return log1pf(x); }
 inline double r_log1p(double x) { return std::log1p(x); }
+inline float r_exp(float x) { return expf(x); }
+inline double r_exp(double x) { return std::exp(x); }
+inline float r_tan(float x) { return tanf(x); }
+inline double r_tan(double x) { return std::tan(x); }
 inline float r_pow(float x, float y) { return powf(x, y); }
 inline double r_pow(double x, double y) { return std::pow(x, y); }
 inline float r_acos(float x) { return acosf(x); }
@@ -224,6 +228,8 @@ template <class R> struct Scene {
     uint32_t variation_slot = 0, variation_enabled = 0;
     R var_rough[2] = {0, 0}, var_metal[2] = {0, 0};
     R cavity = 0;
+    R fog[4] = {0, 0, 0, 0};  // density, height, falloff, anisotropy (atmosphere.a)
+    V3<R> fog_color;          // atmosphere.b.xyz
     uint32_t seed = 0;
     // fractal uniforms (uniforms.rs:183-189, :781-782)
     R pixel_tolerance = 1, far = 200, step_scale = 1;

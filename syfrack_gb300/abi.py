@@ -95,13 +95,19 @@ class sf_coloring(C.Structure):
                 ("frequency", C.c_float), ("phase", C.c_float), ("gamma", C.c_float)]
 
 
+class sf_fog(C.Structure):
+    _fields_ = [("density", C.c_float), ("height", C.c_float), ("falloff", C.c_float),
+                ("anisotropy", C.c_float), ("color", C.c_float * 3)]
+
+
 class sf_scene_desc(C.Structure):
     _fields_ = [("camera", sf_camera), ("material", sf_material),
                 ("finishes", sf_material * SF_MAX_FINISHES), ("finish_count", C.c_uint32),
                 ("lights", sf_area_light * SF_MAX_LIGHTS), ("light_count", C.c_uint32),
                 ("variation_slot", C.c_uint32), ("variation_enabled", C.c_uint32),
                 ("variation_roughness", C.c_float * 2), ("variation_metallic", C.c_float * 2),
-                ("cavity_darkness", C.c_float), ("seed", C.c_uint64), ("coloring", sf_coloring)]
+                ("cavity_darkness", C.c_float), ("seed", C.c_uint64), ("coloring", sf_coloring),
+                ("fog", sf_fog)]
 
 
 class sf_render_config(C.Structure):

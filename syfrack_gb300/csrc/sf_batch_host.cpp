@@ -152,9 +152,7 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     size_t extra = 0;
     uint32_t K = 1;  // the most shadow segments one bounce of any job issues
     for (uint32_t i = 0; i < n; ++i) {
-        uint32_t k = 1;
-        for (uint32_t l = 0; l < jobs[i].scene.light_count; ++l) k += jobs[i].scene.lights[l].kind != SF_LIGHT_AREA;
-        K = std::max(K, k);
+        K = std::max(K, shadow_slots_of(jobs[i].scene));
     }
     sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, K, scene_bytes + film_bytes, &extra);
     if (st != SF_OK) { delete b; return st; }

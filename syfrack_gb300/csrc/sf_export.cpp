@@ -20,7 +20,7 @@ using namespace sfh;
 namespace {
 
 constexpr uint32_t EX_MAGIC = 0x58454653u;  // "SFEX"
-constexpr uint32_t EX_VERSION = 1;
+constexpr uint32_t EX_VERSION = 2;  // 2: the scene carries its fog
 constexpr int kStages = 2;
 
 struct Stage {
@@ -231,7 +231,8 @@ extern "C" sf_status sf_export_readback(sf_export* e, sf_film_planes* out) {
     if (out->accum) std::memcpy(out->accum, e->accum.data(), px * 16);
     if (out->depth) std::memcpy(out->depth, e->depth.data(), px * 4);
     if (out->aux) std::memcpy(out->aux, e->aux.data(), px * 16);
-    // no fog or volumes on this path: zero volume contribution, surface = radiance
+    // the volume layer split is not kept (fog radiance is in accum): zero volume
+    // contribution, surface = radiance
     for (size_t i = 0; i < px; ++i) {
         const float n = e->accum[4 * i + 3];
         for (float* p : {out->volume, out->moments})

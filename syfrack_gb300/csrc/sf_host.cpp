@@ -826,7 +826,20 @@ sf_status scene_check(const sf_scene_desc& d) {
     if (d.coloring.slot == 6 && d.coloring.stop_count)
         return fail(SF_ERR_UNSUPPORTED, "orbit colouring is not built on the device");
     if (d.coloring.stop_count > SF_MAX_RAMP_STOPS) return fail(SF_ERR_INVALID, "more than 16 ramp stops");
+    if (!(d.fog.density >= 0.0f) || !(std::fabs(d.fog.anisotropy) < 1.0f))
+        return fail(SF_ERR_INVALID, "fog density must be >= 0 and anisotropy in (-1, 1)");
+    if (shadow_slots_of(d) > 8)
+        return fail(SF_ERR_UNSUPPORTED, "more than 8 shadow segments per bounce (too many lights)");
     return SF_OK;
+}
+// Shadow segments one bounce can issue: the surface's next events (the selected area
+// light, every sky light) or a fog scattering point's (every sky light), plus, in fog,
+// one per area light for the segment's line integral.
+uint32_t shadow_slots_of(const sf_scene_desc& d) {
+    uint32_t area = 0, sky = 0;
+    for (uint32_t i = 0; i < std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS); ++i)
+        (d.lights[i].kind == SF_LIGHT_AREA ? area : sky)++;
+    return 1 + sky + (d.fog.density > 0.0f ? area : 0);
 }
 void light_dev(const sf_area_light& l, DevLight& o) {
     std::memset(&o, 0, sizeof o);
@@ -918,12 +931,14 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     S.iteration_product = gi.iteration_product;
     material_dev(d.material, S.material);
     for (uint32_t i = 0; i < S.finish_count; ++i) material_dev(d.finishes[i], S.finishes[i]);
-    uint32_t shadows = 1;  // the selected area light
-    for (uint32_t i = 0; i < S.light_count; ++i) {
-        light_dev(d.lights[i], S.lights[i]);
-        if (d.lights[i].kind != SF_LIGHT_AREA) shadows++;
-    }
-    S.shadow_slots = shadows;
+    for (uint32_t i = 0; i < S.light_count; ++i) light_dev(d.lights[i], S.lights[i]);
+    S.shadow_slots = shadow_slots_of(d);
+    // GpuAtmosphere (uniforms.rs:217-227): fog in a, its colour in b
+    S.fog[0] = d.fog.density;
+    S.fog[1] = d.fog.height;
+    S.fog[2] = d.fog.falloff;
+    S.fog[3] = d.fog.anisotropy;
+    std::memcpy(S.fog_color, d.fog.color, 12);
     const sf_coloring& col = d.coloring;
     S.col_slot = col.slot;
     S.col_n = std::min<uint32_t>(col.stop_count, SF_MAX_RAMP);
@@ -1295,10 +1310,7 @@ sf_status session_alloc(sf_session* s) {
     size_t o_acc = take(px * 16), o_depth = take(px * 4), o_aux = take(px * 16);
     size_t o_Ls = take(N * 16);
     size_t o_soa = 0, o_lists = 0, o_march = 0, o_resume = 0;
-    // shadow segments one bounce may issue: the selected area light, each sun and sky
-    uint32_t K = 1;
-    for (uint32_t i = 0; i < std::min<uint32_t>(s->scene.light_count, SF_MAX_LIGHTS); ++i)
-        if (s->scene.lights[i].kind != SF_LIGHT_AREA) K++;
+    const uint32_t K = shadow_slots_of(s->scene);  // shadow segments one bounce may issue
     s->shadow_slots = K;
     if (wf) {
         o_soa = take(wave_soa_bytes(N, K));
@@ -1599,7 +1611,7 @@ uint64_t fnv1a(const void* data, size_t n, uint64_t h) {
 
 
 const uint32_t CK_MAGIC = 0x4b434653u;  // "SFCK"
-const uint32_t CK_VERSION = 2;
+const uint32_t CK_VERSION = 3;  // 3: the scene carries its fog
 
 std::string producer_of(const sf_context* c) {
     return c->device_name + "|sm_" + std::to_string(c->cc_major) + std::to_string(c->cc_minor) + "|abi " +

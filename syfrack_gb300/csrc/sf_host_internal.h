@@ -129,6 +129,7 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
 sf_status validate_config(const sf_render_config& c);
 // Scene limits and the light kinds and colouring the device path supports.
 sf_status scene_check(const sf_scene_desc& d);
+uint32_t shadow_slots_of(const sf_scene_desc& d);
 // Panorama tables (sf_environment.cpp) and an HDRI light's device fields.
 sf_status environment_tables(const float* rgb, uint32_t width, uint32_t height, std::vector<float>& texels,
                              uint32_t& ow, uint32_t& oh, bool& uniform);

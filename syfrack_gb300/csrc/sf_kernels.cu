@@ -254,6 +254,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
     uint32_t tile_px = g.tile_w * g.tile_h, local = ly * g.tile_w + lx;
     const float accept = S.pixel_cone * S.pixel_tolerance;
     unsigned long long evals = 0, iters = 0, segs = 0;
+    const uint32_t stream = point_stream_of(S, px, py);
     for (uint32_t s = 0; s < g.samples; ++s) {
         uint32_t sample = g.sample_start + s;
         PathState ps;
@@ -312,7 +313,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 segs++;
                 if (sr == MARCH_MISS && sli == SF_NO_LIGHT) ps.L = add_rn(ps.L, sh.contrib);
             };
-            int cont = bounce_body(S, ps, h, emit, fd, fa);
+            int cont = bounce_body(S, ps, h, emit, fd, fa, sample, stream);
             if (cont != PATH_CONTINUE) break;
         }
         soa.Ls[(size_t)s * tile_px + local] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);

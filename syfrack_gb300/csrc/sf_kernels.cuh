@@ -6,12 +6,12 @@
 #include "sf_program.h"
 
 // Path flags kept in the path state.
-enum { SF_PF_CONT = 1u, SF_PF_SHADOW = 2u, SF_PF_FROM_BSDF = 4u };
+enum { SF_PF_CONT = 1u, SF_PF_SHADOW = 2u, SF_PF_FROM_BSDF = 4u, SF_PF_FROM_VOLUME = 8u };
 #define SF_PF_SHADOW_SHIFT 8  // bits 8..15 of the flags: which shadow slots hold a segment
 // Hit record flags.
 enum { SF_HF_HIT = 1u, SF_HF_EXHAUSTED = 2u };
 // Wavefront invariant word (wavefront.wgsl:183/:220/:236 bits 1, 2, 4).
-enum { SF_WF_QUEUE_OVERFLOW = 1u, SF_WF_COMPACT_OVERFLOW = 2u, SF_WF_ALIVE_AT_COMMIT = 4u };
+enum { SF_WF_QUEUE_OVERFLOW = 1u, SF_WF_COMPACT_OVERFLOW = 2u, SF_WF_ALIVE_AT_COMMIT = 4u, SF_WF_SHADOW_OVERFLOW = 8u };
 
 // Statistics accumulated by the trace kernels (64-bit device counters).
 // WARP_DE_CALLS counts warp-level DE invocations; ITER_SLOTS sums, per invocation,

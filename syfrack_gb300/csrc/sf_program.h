@@ -127,7 +127,9 @@ struct DevScene {
     uint32_t col_slot, col_n, col_cyclic, col_smooth, col_positioned;
     float col_map[3];                 // frequency, phase, gamma
     float col_stops[SF_MAX_RAMP][4];  // rgb, position
-    uint32_t shadow_slots;            // shadow requests a bounce can make: 1 + suns + environments
+    uint32_t shadow_slots;            // shadow requests a bounce can make (shadow_slots_of)
+    float fog[4];                     // density, height, falloff, anisotropy (atmosphere.a)
+    float fog_color[3];               // scattering albedo (atmosphere.b.xyz)
     DevMaterial material;
     DevMaterial finishes[8];
     DevLight lights[8];

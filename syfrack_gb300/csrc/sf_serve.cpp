@@ -603,10 +603,8 @@ extern "C" sf_status sf_serve_submit(sf_server* s, const sf_request* q, uint64_t
         if (st != SF_OK) return st;
         if (const sf_status sc = scene_check(q->scene); sc != SF_OK) return sc;
         if (has_hdri(q->scene)) return fail(SF_ERR_UNSUPPORTED, "HDRI panoramas are rendered by sessions, not served");
-        uint32_t shadows = 1;
-        for (uint32_t l = 0; l < q->scene.light_count; ++l) shadows += q->scene.lights[l].kind != SF_LIGHT_AREA;
-        if (shadows > kServeShadowSlots)
-            return fail(SF_ERR_UNSUPPORTED, "the server's arenas hold 3 shadow segments per bounce (area + 2 sky lights)");
+        if (shadow_slots_of(q->scene) > kServeShadowSlots)
+            return fail(SF_ERR_UNSUPPORTED, "the server's arenas hold 3 shadow segments per bounce");
         r->width = q->cfg.width;
         r->height = q->cfg.height;
         r->samples = q->cfg.samples_per_pixel;

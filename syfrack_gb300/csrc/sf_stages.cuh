@@ -18,7 +18,7 @@ static __device__ __forceinline__ void store_path(PathSoA& soa, uint32_t path, c
     soa.o[path] = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.prev_pdf);
     soa.d[path] = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.prev_area_total);
     soa.tp[path] = make_float4(ps.tp.x, ps.tp.y, ps.tp.z, __uint_as_float(ps.rng));
-    uint32_t f = flags | (ps.prev_from_bsdf ? SF_PF_FROM_BSDF : 0u);
+    uint32_t f = flags | (ps.prev_from_bsdf ? SF_PF_FROM_BSDF : 0u) | (ps.prev_from_volume ? SF_PF_FROM_VOLUME : 0u);
     soa.L[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, __uint_as_float(ps.bounce | (f << 16)));
     soa.pn[path] = make_float4(ps.prev_normal.x, ps.prev_normal.y, ps.prev_normal.z, 0.f);
 }
@@ -35,6 +35,7 @@ static __device__ __forceinline__ uint32_t load_path(const PathSoA& soa, uint32_
     ps.bounce = bits & 0xffffu;
     uint32_t flags = bits >> 16;
     ps.prev_from_bsdf = (flags & SF_PF_FROM_BSDF) != 0;
+    ps.prev_from_volume = (flags & SF_PF_FROM_VOLUME) != 0;
     ps.prev_normal = mk3(pn.x, pn.y, pn.z);
     return flags;
 }
@@ -111,7 +112,10 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
         }
         uint32_t n_sh = 0, sh_mask = 0;
         auto emit = [&](const ShadowReq& sh) {  // the k-th shadow segment of this bounce
-            if (n_sh >= soa.shadow_slots) return;
+            if (n_sh >= soa.shadow_slots) {  // more segments than the arena's slots: a host sizing error
+                atomicOr(status, SF_WF_SHADOW_OVERFLOW);
+                return;
+            }
             const size_t row = n_sh * cap + path;
             soa.sh_o[row] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.t_end);
             soa.sh_d[row] = make_float4(sh.dir.x, sh.dir.y, sh.dir.z, 0.f);
@@ -120,7 +124,7 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
             sh_mask |= 1u << n_sh;
             n_sh++;
         };
-        int r = bounce_body(S, ps, h, emit, fd, fa);
+        int r = bounce_body(S, ps, h, emit, fd, fa, sample, point_stream_of(S, px, py));
         if (sh_mask) nf |= SF_PF_SHADOW | (sh_mask << SF_PF_SHADOW_SHIFT);
         if (r == PATH_CONTINUE) nf |= SF_PF_CONT;
     }

@@ -355,6 +355,7 @@ struct PathState {
     float prev_pdf, prev_area_total;
     uint32_t rng, bounce;
     bool prev_from_bsdf;
+    bool prev_from_volume;  // the segment left a fog scattering point (its emitters were estimated there)
 };
 // Result of a continuation trace (Hit of pathtrace.wgsl:60-74 plus the normal).
 struct HitInfo {
@@ -382,7 +383,13 @@ __device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uin
     ps.prev_pdf = 0.0f;
     ps.prev_area_total = 0.0f;
     ps.prev_from_bsdf = false;
+    ps.prev_from_volume = false;
     ps.bounce = 0;
+}
+// point_stream of radiance (pathtrace.wgsl:823): the pixel's rotation of the
+// radical-inverse points.
+__device__ __forceinline__ uint32_t point_stream_of(const DevScene& S, uint32_t px, uint32_t py) {
+    return pcg(pcg(px ^ S.seed) ^ pcg(py ^ 0x27d4eb2du));
 }
 
 // ------------------------------------------------------------------ sky lights
@@ -397,13 +404,16 @@ __device__ __forceinline__ float environment_probability(const DevLight& l, floa
     return fminf(fmaxf(wdiv(e, e + area_total), 0.05f), 1.0f);
 }
 static __device__ float3 environment_emission(const DevScene& S, float3 dir, float pdf, bool use_mis, float3 n,
-                                              float area_total) {
+                                              bool from_volume, float area_total) {
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
         const DevLight& l = S.lights[i];
         if (l.kind != SF_LIGHT_ENVIRONMENT) continue;
         float w = 1.0f;
-        if (use_mis) w = mis_power(pdf, environment_probability(l, area_total) * fmaxf(dot3(n, dir), 0.0f) * (1.0f / SF_PI));
+        if (use_mis) {
+            const float density = from_volume ? 1.0f / (4.0f * SF_PI) : fmaxf(dot3(n, dir), 0.0f) * (1.0f / SF_PI);
+            w = mis_power(pdf, environment_probability(l, area_total) * density);
+        }
         L = L + environment_value(l, dir) * w;
     }
     return L;
@@ -524,19 +534,303 @@ __device__ __forceinline__ float3 cone_sample(float3 dir, float cos_max, float r
     return frame_mul(t, bt, dir, mk3(sin_t * cp, sin_t * sp, cos_t));
 }
 
+// ------------------------------------------------------------------ height fog
+// fog_sigma .. fog_free_flight (pathtrace.wgsl:562-615): the capped exponential
+// height fog, its optical depth integrated exactly on each side of the fog height,
+// and collision distances drawn by inverting that integral. S.fog = density, height,
+// falloff, anisotropy.
+__device__ __forceinline__ float fog_sigma(const DevScene& S, float3 p) {
+    return S.fog[0] * expf(fminf(0.0f, -(p.y - S.fog[1]) * S.fog[2]));
+}
+static __device__ float fog_segment_tau(const DevScene& S, float3 ro, float3 rd, float begin, float end) {
+    const float distance = fmaxf(end - begin, 0.0f);
+    if (distance == 0.0f) return 0.0f;
+    const float sigma = fog_sigma(S, ro + rd * begin);
+    const float mid_height = ro.y + rd.y * ((begin + end) * 0.5f);
+    if (mid_height <= S.fog[1] || S.fog[2] == 0.0f) return S.fog[0] * distance;
+    const float k = rd.y * S.fog[2];
+    const float x = k * distance;
+    if (fabsf(x) < 0.001f) return sigma * distance * (1.0f - x * 0.5f + x * x / 6.0f);
+    return fmaxf(0.0f, wdiv(sigma - fog_sigma(S, ro + rd * end), k));
+}
+__device__ __forceinline__ float fog_split(const DevScene& S, float3 ro, float3 rd, float distance) {
+    if (fabsf(rd.y) < 1e-8f) return distance;
+    return fminf(fmaxf(wdiv(S.fog[1] - ro.y, rd.y), 0.0f), distance);
+}
+static __device__ float fog_optical_depth(const DevScene& S, float3 ro, float3 rd, float distance) {
+    const float split = fog_split(S, ro, rd, distance);
+    return fog_segment_tau(S, ro, rd, 0.0f, split) + fog_segment_tau(S, ro, rd, split, distance);
+}
+__device__ __forceinline__ float fog_transmittance(const DevScene& S, float3 ro, float3 rd, float distance) {
+    return expf(-fog_optical_depth(S, ro, rd, distance));
+}
+static __device__ float fog_invert_segment(const DevScene& S, float3 ro, float3 rd, float begin, float end, float tau) {
+    const float sigma = fog_sigma(S, ro + rd * begin);
+    const float k = rd.y * S.fog[2];
+    if (ro.y + rd.y * ((begin + end) * 0.5f) <= S.fog[1] || fabsf(k * (end - begin)) < 0.0001f)
+        return fminf(end, begin + wdiv(tau, fmaxf(sigma, 1e-30f)));
+    if (sigma > 1e-20f)
+        return fminf(fmaxf(begin - wdiv(logf(fmaxf(1e-7f, 1.0f - wdiv(tau * k, sigma))), k), begin), end);
+    const float remaining = fmaxf(0.0f, fog_segment_tau(S, ro, rd, begin, end) - tau);
+    const float end_sigma = fog_sigma(S, ro + rd * end);
+    return fminf(fmaxf(end + wdiv(logf(fmaxf(1e-7f, 1.0f + wdiv(remaining * k, fmaxf(end_sigma, 1e-30f)))), -k), begin),
+                 end);
+}
+static __device__ float fog_free_flight(const DevScene& S, float3 ro, float3 rd, float t_end, uint32_t& rng) {
+    if (S.fog[0] <= 0.0f) return t_end;
+    const float tau = -logf(fmaxf(1.0f - rnd(rng), 1e-7f));
+    const float split = fog_split(S, ro, rd, t_end);
+    const float first = fog_segment_tau(S, ro, rd, 0.0f, split);
+    const float total = first + fog_segment_tau(S, ro, rd, split, t_end);
+    if (tau >= total) return t_end;
+    if (tau < first) return fog_invert_segment(S, ro, rd, 0.0f, split, tau);
+    return fog_invert_segment(S, ro, rd, split, t_end, tau - first);
+}
+// hg_phase, hg_sample (pathtrace.wgsl:717-731).
+__device__ __forceinline__ float hg_phase(float cos_theta, float g) {
+    const float d = 1.0f + g * g - 2.0f * g * cos_theta;
+    return wdiv(1.0f - g * g, 4.0f * SF_PI * d * wsqrt(d));
+}
+__device__ __forceinline__ float3 hg_sample(float3 dir, float g, float r1, float r2) {
+    float cos_t = 1.0f - 2.0f * r1;
+    if (fabsf(g) > 1e-3f) {
+        const float sq = wdiv(1.0f - g * g, 1.0f - g + 2.0f * g * r1);
+        cos_t = wdiv(1.0f + g * g - sq * sq, 2.0f * g);
+    }
+    const float sin_t = wsqrt(fmaxf(0.0f, 1.0f - cos_t * cos_t));
+    float sp, cp;
+    sincosf(2.0f * SF_PI * r2, &sp, &cp);
+    float3 t, bt;
+    tangent_frame(dir, t, bt);
+    return frame_mul(t, bt, dir, mk3(sin_t * cp, sin_t * sp, cos_t));
+}
+// volume_coordinate (pathtrace.wgsl:43-58): the radical inverse of the sample index
+// in the dimension's prime base, rotated per pixel and emitter.
+__device__ __forceinline__ float volume_coordinate(uint32_t sample_index, uint32_t dimension, uint32_t stream) {
+    const uint32_t base = dimension == 0 ? 2u : dimension == 1 ? 3u : dimension == 2 ? 5u
+                        : dimension == 3 ? 7u : dimension == 4 ? 11u : 13u;
+    uint32_t index = sample_index + 1u;
+    float inverse = 1.0f / float(base);
+    float value = 0.0f;
+    while (index != 0u) {
+        value = __fadd_rn(value, __fmul_rn(float(index % base), inverse));
+        index /= base;
+        inverse = inverse / float(base);
+    }
+    const float shift = float(pcg(stream ^ (dimension * 0x9e3779b9u)) >> 8u) / 16777216.0f;
+    const float v = value + shift;
+    return v - floorf(v);
+}
+// fog_segment_weight (pathtrace.wgsl:621-633) for a rectangle: max-channel power over
+// the distance from the segment's closest point to the light's centre.
+__device__ __forceinline__ float fog_segment_weight(float3 ro, float3 rd, float end, const DevLight& l) {
+    const float3 center = ld3(l.a);
+    const float along = fminf(fmaxf(dot3(center - ro, rd), 0.0f), end);
+    const float3 delta = center - (ro + rd * along);
+    return wdiv(fmaxf(fmaxf(l.color[0], l.color[1]), l.color[2]) * l.area, dot3(delta, delta) + l.area);
+}
+// volume_light_probability (lights.wgsl:319-323): independent per-emitter roulette.
+__device__ __forceinline__ float volume_light_probability(float weight, float total) {
+    if (total <= 0.0f) return 0.0f;
+    return fminf(1.0f, wdiv(3.0f * weight, total));
+}
+__device__ __forceinline__ float mixf(float x, float y, float a) { return fmaf(x, 1.0f - a, y * a); }
+
+// fog_segment_direct (pathtrace.wgsl:635-715): in-scattered emitter light along the
+// segment [0, end] of the current ray as a line integral. Each area light passes an
+// independent roulette; the point on the segment mixes equiangular sampling about a
+// sampled emitter point with the truncated optical-depth distribution (one-sample
+// MIS, balance weights). Primary segments use the rotated radical-inverse points.
+// Each sample is one shadow segment, handed to `emit` with radiance `tp` × (its
+// estimate) × colour.
+template <class Emit>
+static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 ro, float3 rd, float end, uint32_t& rng,
+                                          uint32_t point_index, uint32_t point_stream, bool primary, Emit&& emit) {
+    const float3 color = ld3(S.fog_color);
+    if (end <= 0.0f || fmaxf(fmaxf(color.x, color.y), color.z) <= 0.0f) return;
+    const float tau_end = fog_optical_depth(S, ro, rd, end);
+    if (tau_end <= 0.0f) return;
+    float total = 0.0f;
+    for (uint32_t i = 0; i < S.light_count; ++i)
+        if (S.lights[i].kind == SF_LIGHT_AREA) total += fog_segment_weight(ro, rd, end, S.lights[i]);
+    const float g = S.fog[3];
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        if (l.kind != SF_LIGHT_AREA) continue;
+        const float probability = volume_light_probability(fog_segment_weight(ro, rd, end, l), total);
+        const uint32_t stream = pcg(point_stream ^ (i * 0x85ebca6bu));
+        float selection = rnd(rng);
+        if (primary) selection = volume_coordinate(point_index, 5u, stream);
+        if (probability <= 0.0f || selection >= probability) continue;
+        float u1 = rnd(rng);
+        float u2 = rnd(rng);
+        if (primary) {
+            u1 = volume_coordinate(point_index, 0u, stream);
+            u2 = volume_coordinate(point_index, 1u, stream);
+        }
+        const float3 q = ld3(l.a) + ld3(l.b) * (u1 - 0.5f) + ld3(l.c) * (u2 - 0.5f);
+        const float tau_begin = fog_optical_depth(S, ro, rd, 0.0f);
+        const float tau_finish = fog_optical_depth(S, ro, rd, end);
+        const float tau_span = fmaxf(0.0f, tau_finish - tau_begin);
+        if (tau_span <= 0.0f) continue;
+        float conditional_mass = 1.0f - expf(-tau_span);
+        if (tau_span < 0.001f) conditional_mass = tau_span * (1.0f - tau_span * 0.5f + tau_span * tau_span / 6.0f);
+        const float interval_mass = expf(-tau_begin) * conditional_mass;
+        if (interval_mass < 1e-30f) continue;
+        const float3 delta = q - ro;
+        const float projection = dot3(delta, rd);
+        const float3 perp_v = delta - rd * projection;
+        const float perpendicular = wsqrt(dot3(perp_v, perp_v));
+        const float theta_a = atan2f(0.0f - projection, fmaxf(perpendicular, 1e-6f));
+        const float theta_b = atan2f(end - projection, fmaxf(perpendicular, 1e-6f));
+        const float span = theta_b - theta_a;
+        const bool regular = perpendicular > 1e-4f && span > 1e-5f;
+        float xi = rnd(rng);
+        float technique = rnd(rng);
+        if (primary) {
+            xi = volume_coordinate(point_index, 3u, stream);
+            technique = volume_coordinate(point_index, 4u, stream);
+        }
+        float t = mixf(0.0f, end, xi);
+        if (technique < 0.5f) {
+            if (regular) t = fminf(fmaxf(projection + perpendicular * tanf(mixf(theta_a, theta_b, xi)), 0.0f), end);
+        } else {
+            const float tau = tau_begin - logf(fmaxf(1.0f - xi * conditional_mass, 1e-7f));
+            const float split = fog_split(S, ro, rd, end);
+            const float first = fog_segment_tau(S, ro, rd, 0.0f, split);
+            t = tau < first ? fog_invert_segment(S, ro, rd, 0.0f, split, tau)
+                            : fog_invert_segment(S, ro, rd, split, end, tau - first);
+        }
+        const float3 p = ro + rd * t;
+        const float transmittance = expf(-fog_optical_depth(S, ro, rd, t));
+        const float sigma = fog_sigma(S, p);
+        float angular_pdf = wdiv(1.0f, end - 0.0f);
+        if (regular) {
+            const float dt = t - projection;
+            angular_pdf = wdiv(perpendicular, span * (perpendicular * perpendicular + dt * dt));
+        }
+        const float distance_pdf = 0.5f * (angular_pdf + wdiv(sigma * transmittance, interval_mass));
+        const float3 to_light = q - p;
+        const float distance2 = dot3(to_light, to_light);
+        if (distance2 < 1e-8f) continue;
+        const float distance = wsqrt(distance2);
+        const float3 wi = to_light * wdiv(1.0f, distance);
+        const float cosine = dot3(ld3(l.n), -wi);
+        if (cosine <= 0.0f) continue;
+        const float tr = transmittance * expf(-fog_optical_depth(S, p, wi, distance));
+        const float light_pdf = wdiv(distance2, fmaxf(l.area * cosine, 1e-20f));
+        const float scale = wdiv(sigma * tr * hg_phase(dot3(rd, wi), g), probability * distance_pdf * light_pdf);
+        ShadowReq sh;
+        sh.o = p;
+        sh.dir = wi;
+        sh.t_end = fmaxf(0.0f, distance - fmaxf(1e-5f, distance * 1e-6f));
+        sh.contrib = tp * ((ld3(l.color) * scale) * color);
+        emit(sh);
+    }
+}
+// fog_direct_light (pathtrace.wgsl:733-772): next events at a scattering point for
+// the sky lights (environment: uniform sphere with its roulette; panoramas; suns),
+// phase function in place of the BRDF; `tpc` = throughput × fog colour.
+template <class Emit>
+static __device__ void fog_direct_light(const DevScene& S, float3 tpc, float3 p, float3 rd, float area_total, bool last,
+                                        uint32_t& rng, Emit&& emit) {
+    const float g = S.fog[3];
+    for (uint32_t i = 0; i < S.light_count; ++i) {
+        const DevLight& l = S.lights[i];
+        float3 dir, value;
+        float pl;
+        if (l.kind == SF_LIGHT_ENVIRONMENT) {
+            if (l.peak <= 0.0f) continue;
+            const float probability = environment_probability(l, area_total);
+            if (rnd(rng) >= probability) continue;
+            const float z = 1.0f - 2.0f * rnd(rng);
+            const float phi = 2.0f * SF_PI * rnd(rng);
+            const float radius = wsqrt(fmaxf(0.0f, 1.0f - z * z));
+            float sp, cp;
+            sincosf(phi, &sp, &cp);
+            dir = mk3(radius * cp, z, radius * sp);
+            pl = probability * (1.0f / (4.0f * SF_PI));
+            value = environment_value(l, dir);
+        } else if (l.kind == SF_LIGHT_HDRI) {
+            if (l.color[0] <= 0.0f) continue;
+            const float r0 = rnd(rng);
+            const float r1 = rnd(rng);
+            const float r2 = rnd(rng);
+            dir = hdri_sample(l, r0, r1, r2);
+            pl = hdri_pdf(l, dir);
+            value = hdri_lookup(l, dir);
+        } else if (l.kind == SF_LIGHT_SUN) {
+            const float r1 = rnd(rng);
+            const float r2 = rnd(rng);
+            dir = cone_sample(ld3(l.a), l.cos_max, r1, r2);
+            pl = sun_pdf(l.cos_max);
+            value = ld3(l.color);
+        } else {
+            continue;
+        }
+        const float tr = fog_transmittance(S, p, dir, S.extent);
+        const float ph = hg_phase(dot3(rd, dir), g);
+        const float w = last ? 1.0f : mis_power(pl, ph);
+        ShadowReq sh;
+        sh.o = p;
+        sh.dir = dir;
+        sh.t_end = S.extent;
+        // the sun's colour is its irradiance: no division by the disk's pdf
+        sh.contrib = tpc * (l.kind == SF_LIGHT_SUN ? value * ph * tr * w : value * ph * tr * wdiv(w, pl));
+        emit(sh);
+    }
+}
+
 // One bounce of `radiance` (pathtrace.wgsl:841-1196) after its trace: hit
 // classification, sky and emitter emission with MIS, surface, next-event sampling
 // (direct_light, pathtrace.wgsl:471-558: every environment and sun, and the one
 // selected area light, in scene order; each visibility test is handed to `emit`,
 // which adds its radiance if the segment is clear) and BSDF continuation with
-// Russian roulette. Writes first-hit depth/aux at bounce 0.
+// Russian roulette. Writes first-hit depth/aux at bounce 0. In fog (pathtrace.wgsl:
+// 980-1011) the segment first adds its in-scattered emitter light, then a collision
+// drawn along it may scatter the path (next events for the sky lights, phase-sampled
+// continuation) before the hit is reached. `point_index` is the sample index and
+// `point_stream` the pixel's rotation (point_stream_of) of the primary segment's points.
 template <class Emit>
 static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, Emit&& emit, float* first_depth,
-                                  float4* first_aux) {
+                                  float4* first_aux, uint32_t point_index, uint32_t point_stream) {
+    if (h.hit && ps.bounce == 0 && first_depth) {
+        *first_depth = h.t;
+        const float3 en = h.light_index != SF_NO_LIGHT ? ld3(S.lights[h.light_index].n) : h.n;
+        *first_aux = make_float4(en.x, en.y, en.z, float(h.steps));
+    }
+    const bool fog = S.fog[0] > 0.0f;
+    if (fog) {
+        const float t_end = h.hit ? h.t : S.extent;
+        fog_segment_direct(S, ps.tp, ps.o, ps.d, t_end, ps.rng, point_index, point_stream, ps.bounce == 0, emit);
+        const float t_s = fog_free_flight(S, ps.o, ps.d, t_end, ps.rng);
+        if (t_s < t_end) {
+            if (ps.bounce == 0 && !h.hit && first_depth) *first_depth = t_s;
+            const float3 p_s = ps.o + ps.d * t_s;
+            const float volume_area_total = area_total_weight(S, p_s, mk3(0.f, 0.f, 0.f));
+            const bool last = ps.bounce == S.max_bounces;
+            const float3 tpc = ps.tp * ld3(S.fog_color);
+            fog_direct_light(S, tpc, p_s, ps.d, volume_area_total, last, ps.rng, emit);
+            ps.tp = tpc;
+            if (last) return PATH_DONE;
+            const float r1 = rnd(ps.rng);
+            const float r2 = rnd(ps.rng);
+            const float3 nd = hg_sample(ps.d, S.fog[3], r1, r2);
+            ps.prev_pdf = hg_phase(dot3(ps.d, nd), S.fog[3]);
+            ps.prev_from_bsdf = true;
+            ps.prev_from_volume = true;
+            ps.prev_normal = mk3(0.f, 0.f, 0.f);
+            ps.prev_area_total = volume_area_total;
+            ps.o = p_s;
+            ps.d = nd;
+            ps.bounce += 1;
+            return PATH_CONTINUE;
+        }
+    }
     if (!h.hit) {
         if (!h.exhausted) {  // the sky, the panoramas, the suns (pathtrace.wgsl:1026-1040)
             ps.L = ps.L + ps.tp * environment_emission(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
-                                                       ps.prev_area_total);
+                                                       ps.prev_from_volume, ps.prev_area_total);
             ps.L = ps.L + ps.tp * hdri_emission(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf);
             ps.L = ps.L + ps.tp * sun_radiance(S, ps.d, ps.prev_pdf, ps.prev_from_bsdf);
         }
@@ -544,21 +838,14 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     }
     float3 p = ps.o + ps.d * h.t;
     if (h.light_index != SF_NO_LIGHT) {
-        if (ps.bounce == 0 && first_depth) {
-            *first_depth = h.t;
-            float3 en = ld3(S.lights[h.light_index].n);
-            *first_aux = make_float4(en.x, en.y, en.z, float(h.steps));
-        }
-        ps.L = ps.L + ps.tp * area_emission(S, ps.o, ps.d, h.t, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
-                                            ps.prev_area_total);
+        // after a fog scattering point its segment estimate already holds the emitters
+        if (!ps.prev_from_volume)
+            ps.L = ps.L + ps.tp * area_emission(S, ps.o, ps.d, h.t, ps.prev_pdf, ps.prev_from_bsdf, ps.prev_normal,
+                                                ps.prev_area_total);
         return PATH_DONE;
     }
     float3 n = h.n;
     if (ps.bounce == 0) {
-        if (first_depth) {
-            *first_depth = h.t;
-            *first_aux = make_float4(n.x, n.y, n.z, float(h.steps));
-        }
         float x = fminf(fmaxf(float(h.steps) / 96.0f, 0.0f), 1.0f);
         ps.tp = ps.tp * (1.0f - S.cavity * (x * x * (3.0f - 2.0f * x)));
     }
@@ -606,7 +893,8 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             sh.o = p_off;
             sh.dir = ldir;
             sh.t_end = S.extent;
-            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * wdiv(w, pl));
+            const float tr = fog ? fog_transmittance(S, p_off, ldir, S.extent) : 1.0f;
+            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) * tr * wdiv(w, pl));
             emit(sh);
         } else if (l.kind == SF_LIGHT_HDRI) {
             if (l.color[0] <= 0.0f) continue;
@@ -623,7 +911,8 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             sh.o = p_off;
             sh.dir = ldir;
             sh.t_end = S.extent;
-            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * wdiv(w, pl));
+            const float tr = fog ? fog_transmittance(S, p_off, ldir, S.extent) : 1.0f;
+            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * tr * wdiv(w, pl));
             emit(sh);
         } else if (l.kind == SF_LIGHT_SUN) {
             const float r1 = rnd(ps.rng);
@@ -638,7 +927,8 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             sh.o = p_off;
             sh.dir = ldir;
             sh.t_end = S.extent;
-            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * ld3(l.color) * w);
+            const float tr = fog ? fog_transmittance(S, p_off, ldir, S.extent) : 1.0f;
+            sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * ld3(l.color) * w * tr);
             emit(sh);
         } else if (i == selected) {
             float u1 = rnd(ps.rng);
@@ -657,7 +947,8 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             float pl = wdiv(selected_weight, area_total) * wdiv(dist2, fmaxf(l.area * cos_l, 1e-20f));
             float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
             float w = last ? 1.0f : mis_power(pl, pb);
-            float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * wdiv(w, pl);
+            const float tr = fog ? fog_transmittance(S, p_off, ldir, dist) : 1.0f;
+            float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * tr * wdiv(w, pl);
             ShadowReq sh;
             sh.o = p_off;
             sh.dir = ldir;
@@ -683,6 +974,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     ps.tp = ps.tp * (brdf_eval(s, v, ldir) * wdiv(nl, pdf));
     ps.prev_pdf = pdf;
     ps.prev_from_bsdf = true;
+    ps.prev_from_volume = false;
     ps.prev_normal = s.n;
     ps.prev_area_total = area_total;
     if (ps.bounce >= 2) {

@@ -297,6 +297,18 @@ class Material(Finish):
 
 
 @dataclass
+class Fog:
+    """Atmosphere's height fog (atmosphere.rs:7-28): extinction `density` at and below
+    `height`, decaying as exp(-(y - height) * falloff) above it; Henyey-Greenstein
+    `anisotropy`; scattering albedo `color` (0 = purely absorbing)."""
+    density: float = 0.0
+    color: tuple = (1.0, 1.0, 1.0)
+    height: float = 0.0
+    falloff: float = 1.0
+    anisotropy: float = 0.0
+
+
+@dataclass
 class Scene:
     graph: Graph
     camera: Camera = field(default_factory=Camera)
@@ -304,6 +316,7 @@ class Scene:
     lights: list = field(default_factory=list)
     seed: int = 0
     cavity_darkness: float = 0.0
+    fog: Fog | None = None
 
     def desc(self, width: int, height: int) -> abi.sf_scene_desc:
         """The scene half of Uniforms::from_scene (uniforms.rs:748-830)."""
@@ -336,6 +349,12 @@ class Scene:
             d.variation_roughness[:] = list(sv.roughness)
             d.variation_metallic[:] = list(sv.metallic)
         d.cavity_darkness = self.cavity_darkness
+        if self.fog is not None and self.fog.density > 0.0:
+            d.fog.density = self.fog.density
+            d.fog.height = self.fog.height
+            d.fog.falloff = self.fog.falloff
+            d.fog.anisotropy = self.fog.anisotropy
+            d.fog.color[:] = [float(c) for c in self.fog.color]
         d.seed = self.seed & 0xFFFFFFFFFFFFFFFF
         col = self.material.coloring
         d.coloring.slot = 0xFFFF
@@ -445,7 +464,10 @@ def scene_from_ron_value(v) -> Scene:
     mat = Material(albedo=tuple(ron.vec(m["albedo"])), roughness=float(m["roughness"]),
                    metallic=float(m["metallic"]), specular=float(m["specular"]), coloring=col)
     atm = v.get("atmosphere", {})
-    if float(atm.get("fog_density", 0.0)) != 0.0:
-        raise ValueError("fog is not on this path")
+    fog = None
+    if float(atm.get("fog_density", 0.0)) > 0.0:
+        fog = Fog(density=float(atm["fog_density"]), color=tuple(ron.vec(atm.get("fog_color", (1.0, 1.0, 1.0)))),
+                  height=float(atm.get("fog_height", 0.0)), falloff=float(atm.get("fog_falloff", 1.0)),
+                  anisotropy=float(atm.get("anisotropy", 0.0)))
     return Scene(graph=graph, camera=cam, material=mat, lights=lights, seed=int(v.get("seed", 0)),
-                 cavity_darkness=float(atm.get("cavity_darkness", 0.0)))
+                 cavity_darkness=float(atm.get("cavity_darkness", 0.0)), fog=fog)

@@ -78,8 +78,9 @@ def bounded_bulb(subtract=False, margin=0.05):
     return g
 
 
-def golden_scene(name):
-    """scenes/<name>.ron from its JSON copy, read by the package's scene-file reader."""
+def golden_scene(name, atmosphere=None):
+    """scenes/<name>.ron from its JSON copy, read by the package's scene-file reader;
+    `atmosphere` overrides fields of the file's atmosphere."""
     from syfrack_gb300 import ron
     from syfrack_gb300.scene import scene_from_ron_value
 
@@ -100,6 +101,8 @@ def golden_scene(name):
             return ron.Unit(v)
         return v
 
+    if atmosphere:
+        d["scene"].setdefault("atmosphere", {}).update(atmosphere)
     return scene_from_ron_value(back(d["scene"]))
 
 
