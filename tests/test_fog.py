@@ -204,3 +204,31 @@ def test_fog_scenes_past_eight_shadow_segments_are_refused(renderer):
     s.fog = Fog(density=0.1)
     with pytest.raises(SyfrackError, match="SF_ERR_UNSUPPORTED"):
         RenderSession(renderer, s, cfg)
+
+
+@pytest.mark.gpu
+def test_fog_jobs_in_a_batch_equal_their_sessions(renderer):
+    """A fog job (four shadow slots: area, sun, sky and the segment's area estimate)
+    batched with an area-lit job: each film equals the job rendered alone."""
+    from syfrack_gb300 import Batch, RenderSession
+
+    cfg = RenderConfig(48, 32, 4, max_bounces=3, max_steps=256, pixel_tolerance=1.0, tile_size=48,
+                       samples_per_dispatch=4, integrator="wavefront")
+    fog = fog_bulb_scene()
+    clear = fog_bulb_scene()
+    clear.fog = None
+    clear.lights = clear.lights[:1]
+    jobs = [(clear, cfg), (fog, cfg)]
+    b = Batch(renderer, jobs)
+    b.run(1, use_graph=False)
+    assert b.sync() == 0
+    for i, (sc, c) in enumerate(jobs):
+        got = b.readback(i)
+        s = RenderSession(renderer, sc, c)
+        while not s.step(0):
+            pass
+        ref = s.readback()
+        s.close()
+        scale = max(1.0, float(np.abs(ref.accum[..., :3]).max()))
+        assert np.abs(got.accum[..., :3] - ref.accum[..., :3]).max() <= 1e-4 * scale, i
+    b.close()
