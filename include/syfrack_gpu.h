@@ -341,6 +341,7 @@ typedef struct sf_film_planes {
     float* volume;  /* 4*width*height: volume sums and sample count */
     float* moments; /* 4*width*height: volume Welford moments and sample count */
     float* surface; /* 4*width*height: surface sums and sample count */
+    float* color;   /* 4*width*height: accum rgb / max(count, 1), alpha 1 (RenderOutput.color) */
 } sf_film_planes;
 
 /* Session::new (session.rs:165). The integrator field selects the per-pixel

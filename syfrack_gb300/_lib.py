@@ -49,7 +49,8 @@ class sf_progress(C.Structure):
 
 
 class sf_film_planes(C.Structure):
-    _fields_ = [("accum", fp), ("depth", fp), ("aux", fp), ("volume", fp), ("moments", fp), ("surface", fp)]
+    _fields_ = [("accum", fp), ("depth", fp), ("aux", fp), ("volume", fp), ("moments", fp), ("surface", fp),
+                ("color", fp)]
 
 
 class sf_planar_desc(C.Structure):

@@ -315,13 +315,7 @@ extern "C" sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes
     if (job >= b->jobs.size()) return fail(SF_ERR_INVALID, "job index out of range");
     sf_context* c = b->ctx;
     cudaSetDevice(c->device);
-    const FilmPlanes& f = b->jobs[job].film;
-    size_t px = size_t(f.width) * f.height;
-    if (out->accum) CU(cudaMemcpyAsync(out->accum, f.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
-    if (out->depth) CU(cudaMemcpyAsync(out->depth, f.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (out->aux) CU(cudaMemcpyAsync(out->aux, f.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
-    CU(derived_planes(f, *out, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
+    CU(film_readback(c, b->jobs[job].film, *out, c->stream));
     return SF_OK;
 }
 

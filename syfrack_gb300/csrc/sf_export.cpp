@@ -237,6 +237,11 @@ extern "C" sf_status sf_export_readback(sf_export* e, sf_film_planes* out) {
         const float n = e->accum[4 * i + 3];
         for (float* p : {out->volume, out->moments})
             if (p) { p[4 * i] = p[4 * i + 1] = p[4 * i + 2] = 0.0f; p[4 * i + 3] = n; }
+        if (out->color) {  // RenderOutput.color: accum.rgb / max(count, 1), alpha 1
+            const float d = std::max(n, 1.0f);
+            for (int k = 0; k < 3; ++k) out->color[4 * i + k] = e->accum[4 * i + k] / d;
+            out->color[4 * i + 3] = 1.0f;
+        }
     }
     if (out->surface) std::memcpy(out->surface, e->accum.data(), px * 16);
     return SF_OK;

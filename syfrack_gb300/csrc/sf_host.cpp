@@ -48,7 +48,7 @@ sf_status cuda_fail(cudaError_t e, const char* what) {
 constexpr uint32_t MAX_DEPTH = 3;          // graph/mod.rs:41
 constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
 constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
-constexpr uint32_t ABI_VERSION = (1u << 16) | 0u;
+constexpr uint32_t ABI_VERSION = (1u << 16) | 1u;  // 1.1: sf_film_planes.color
 
 // ------------------------------------------------------------------ graph preparation
 
@@ -657,6 +657,7 @@ void ctx_release(sf_context* c) {
     collect_timing(c);
     for (auto e : c->spare) cudaEventDestroy(e);
     ctx_free(c, c->d_stats, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t));
+    if (c->stage) cudaFreeHost(c->stage);
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -1547,21 +1548,62 @@ extern "C" sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t ca
 }
 
 namespace sfh {
-// volume, moments (zero contribution, sample counts) and surface (= accum) planes,
-// filled on the host from the accum plane once the stream has delivered it.
-cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st) {
-    if (!out.volume && !out.moments && !out.surface) return cudaSuccess;
+// Runs f(begin, end) over [0, n) on up to 8 host threads (one below 1 M items).
+template <class F> void host_parallel(size_t n, F&& f) {
+    const size_t parts = std::min<size_t>(8, std::max<size_t>(1, n >> 20));
+    if (parts == 1) { f(size_t(0), n); return; }
+    std::vector<std::thread> pool;
+    for (size_t k = 0; k < parts; ++k) pool.emplace_back([&, k] { f(n * k / parts, n * (k + 1) / parts); });
+    for (auto& t : pool) t.join();
+}
+
+// Film readback through the context's pinned staging: the device planes arrive at
+// full link speed, then the host threads copy them into the caller's (pageable)
+// buffers and derive the others: color = accum.rgb / max(count, 1) with alpha 1
+// (RenderOutput.color), volume and moments (no volume layer: zero contribution and
+// the sample count) and surface (= accum).
+cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st) {
     const size_t px = size_t(f.width) * f.height;
-    std::vector<float> acc(px * 4);
-    cudaError_t e = cudaMemcpyAsync(acc.data(), f.accum, px * 16, cudaMemcpyDeviceToHost, st);
+    const bool need_acc = out.accum || out.color || out.volume || out.moments || out.surface;
+    const size_t bytes = (need_acc ? px * 16 : 0) + (out.depth ? px * 4 : 0) + (out.aux ? px * 16 : 0);
+    if (!bytes) return cudaSuccess;
+    std::lock_guard<std::mutex> lk(c->stage_mu);
+    if (c->stage_bytes < bytes) {
+        if (c->stage) cudaFreeHost(c->stage);
+        c->stage = nullptr;
+        c->stage_bytes = 0;
+        cudaError_t e = cudaHostAlloc(&c->stage, bytes, cudaHostAllocDefault);
+        if (e != cudaSuccess) return e;
+        c->stage_bytes = bytes;
+    }
+    float* acc = static_cast<float*>(c->stage);
+    float* depth = acc + (need_acc ? px * 4 : 0);
+    float* aux = depth + (out.depth ? px : 0);
+    cudaError_t e = cudaSuccess;
+    if (need_acc) e = cudaMemcpyAsync(acc, f.accum, px * 16, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && out.depth) e = cudaMemcpyAsync(depth, f.depth, px * 4, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && out.aux) e = cudaMemcpyAsync(aux, f.aux, px * 16, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
-    for (size_t i = 0; i < px; ++i) {
-        const float n = acc[4 * i + 3];
-        if (out.volume) { out.volume[4 * i] = out.volume[4 * i + 1] = out.volume[4 * i + 2] = 0.0f; out.volume[4 * i + 3] = n; }
-        if (out.moments) { out.moments[4 * i] = out.moments[4 * i + 1] = out.moments[4 * i + 2] = 0.0f; out.moments[4 * i + 3] = n; }
-    }
-    if (out.surface) std::memcpy(out.surface, acc.data(), px * 16);
+    host_parallel(px, [&](size_t b, size_t end) {
+        const size_t n = end - b;
+        if (out.accum) std::memcpy(out.accum + 4 * b, acc + 4 * b, n * 16);
+        if (out.surface) std::memcpy(out.surface + 4 * b, acc + 4 * b, n * 16);
+        if (out.depth) std::memcpy(out.depth + b, depth + b, n * 4);
+        if (out.aux) std::memcpy(out.aux + 4 * b, aux + 4 * b, n * 16);
+        for (size_t i = b; i < end; ++i) {
+            const float cnt = acc[4 * i + 3];
+            if (out.color) {
+                const float d = std::max(cnt, 1.0f);
+                out.color[4 * i] = acc[4 * i] / d;
+                out.color[4 * i + 1] = acc[4 * i + 1] / d;
+                out.color[4 * i + 2] = acc[4 * i + 2] / d;
+                out.color[4 * i + 3] = 1.0f;
+            }
+            if (out.volume) { out.volume[4 * i] = out.volume[4 * i + 1] = out.volume[4 * i + 2] = 0.0f; out.volume[4 * i + 3] = cnt; }
+            if (out.moments) { out.moments[4 * i] = out.moments[4 * i + 1] = out.moments[4 * i + 2] = 0.0f; out.moments[4 * i + 3] = cnt; }
+        }
+    });
     return cudaSuccess;
 }
 }  // namespace sfh
@@ -1570,12 +1612,7 @@ extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
     if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
     sf_context* c = s->ctx;
     cudaSetDevice(c->device);
-    size_t px = size_t(s->cfg.width) * s->cfg.height;
-    if (out->accum) CU(cudaMemcpyAsync(out->accum, s->film.accum, px * 16, cudaMemcpyDeviceToHost, c->stream));
-    if (out->depth) CU(cudaMemcpyAsync(out->depth, s->film.depth, px * 4, cudaMemcpyDeviceToHost, c->stream));
-    if (out->aux) CU(cudaMemcpyAsync(out->aux, s->film.aux, px * 16, cudaMemcpyDeviceToHost, c->stream));
-    CU(derived_planes(s->film, *out, c->stream));
-    CU(cudaStreamSynchronize(c->stream));
+    CU(film_readback(c, s->film, *out, c->stream));
     return SF_OK;
 }
 

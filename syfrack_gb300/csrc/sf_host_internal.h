@@ -74,6 +74,10 @@ struct sf_context {
     int refs = 1;
     std::mutex mu;
     std::mutex alloc_mu;  // budget accounting (a server thread allocates too)
+    // pinned staging of film readbacks, grown on demand and reused by every session
+    void* stage = nullptr;
+    size_t stage_bytes = 0;
+    std::mutex stage_mu;
 };
 
 struct sf_graph {
@@ -138,7 +142,7 @@ bool has_hdri(const sf_scene_desc& d);
 sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen);
 void planar_dev(const sf_planar_desc& f, PlanarDev& o);
 sf_status planar_check(const sf_planar_desc* f);
-cudaError_t derived_planes(const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);
+cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);
 
 // Wavefront path state for N paths with K shadow slots (a bounce issues at most K
 // shadow segments): eight path planes, K sets of shadow planes and visibility words,

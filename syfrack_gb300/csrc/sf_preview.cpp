@@ -199,11 +199,13 @@ extern "C" sf_status sf_preview_progress(sf_preview* p, uint32_t* completed_pixe
 extern "C" sf_status sf_preview_readback(sf_preview* p, sf_film_planes* out) {
     if (!p || !out) return fail(SF_ERR_INVALID, "null argument");
     cudaSetDevice(p->ctx->device);
-    const size_t n = size_t(p->width) * p->height;
-    if (out->accum) CU(cudaMemcpyAsync(out->accum, p->out.accum, n * 16, cudaMemcpyDeviceToHost, p->stream));
-    if (out->depth) CU(cudaMemcpyAsync(out->depth, p->out.depth, n * 4, cudaMemcpyDeviceToHost, p->stream));
-    if (out->aux) CU(cudaMemcpyAsync(out->aux, p->out.aux, n * 16, cudaMemcpyDeviceToHost, p->stream));
-    CU(cudaStreamSynchronize(p->stream));
+    FilmPlanes f{};
+    f.accum = p->out.accum;
+    f.depth = p->out.depth;
+    f.aux = p->out.aux;
+    f.width = p->width;
+    f.height = p->height;
+    CU(film_readback(p->ctx, f, *out, p->stream));
     return SF_OK;
 }
 

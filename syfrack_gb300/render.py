@@ -276,14 +276,11 @@ class RenderSession:
 
     def readback(self) -> RenderOutput:
         w, h = self.cfg.width, self.cfg.height
-        acc = np.zeros((h, w, 4), np.float32)
-        depth = np.zeros((h, w), np.float32)
-        aux = np.zeros((h, w, 4), np.float32)
-        planes = sf_film_planes(_fp(acc), _fp(depth), _fp(aux))
+        acc, aux, color = (np.empty((h, w, 4), np.float32) for _ in range(3))
+        depth = np.empty((h, w), np.float32)
+        # the library fills every plane, the mean colour included (pinned staging, host threads)
+        planes = sf_film_planes(_fp(acc), _fp(depth), _fp(aux), None, None, None, _fp(color))
         check(self.ctx.lib.sf_session_readback(self.h, C.byref(planes)))
-        color = np.ones_like(acc)
-        cnt = np.maximum(acc[..., 3:4], 1.0)
-        color[..., :3] = acc[..., :3] / cnt
         p = self.progress()
         return RenderOutput(color, acc, depth, aux, p["samples_min"], p["samples_max"],
                             time.perf_counter() - self.t0)
@@ -508,13 +505,10 @@ class Batch:
     def readback(self, job: int) -> RenderOutput:
         cfg = self.jobs[job][1]
         w, h = cfg.width, cfg.height
-        acc = np.zeros((h, w, 4), np.float32)
-        depth = np.zeros((h, w), np.float32)
-        aux = np.zeros((h, w, 4), np.float32)
-        planes = sf_film_planes(_fp(acc), _fp(depth), _fp(aux))
+        acc, aux, color = (np.empty((h, w, 4), np.float32) for _ in range(3))
+        depth = np.empty((h, w), np.float32)
+        planes = sf_film_planes(_fp(acc), _fp(depth), _fp(aux), None, None, None, _fp(color))
         check(self.ctx.lib.sf_batch_readback(self.h, job, C.byref(planes)))
-        color = np.ones_like(acc)
-        color[..., :3] = acc[..., :3] / np.maximum(acc[..., 3:4], 1.0)
         n = int(acc[..., 3].min()) if acc.size else 0
         return RenderOutput(color, acc, depth, aux, n, int(acc[..., 3].max()) if acc.size else 0, 0.0)
 

@@ -114,6 +114,16 @@ def test_step_equals_one_shot(renderer):
     np.testing.assert_array_equal(a.depth, b.depth)
 
 
+def test_readback_colour_is_the_mean(renderer):
+    """RenderOutput.color (renderer.rs:151-164) is filled by the library's readback:
+    accum rgb / max(count, 1), alpha 1, the same numbers numpy gives."""
+    scene = workloads.mandelbox_scene()
+    out = render(renderer, scene, small_cfg("wavefront", spp=4, spd=4, tile=128))
+    want = out.accum[..., :3] / np.maximum(out.accum[..., 3:4], np.float32(1.0))
+    np.testing.assert_array_equal(out.color[..., :3], want)
+    assert np.all(out.color[..., 3] == 1.0)
+
+
 def test_save_resume_bit_for_bit(renderer, tmp_path):
     scene = workloads.mandelbox_scene()
     cfg = small_cfg("wavefront", spp=8, spd=4)
