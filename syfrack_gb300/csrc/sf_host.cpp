@@ -658,6 +658,7 @@ void ctx_release(sf_context* c) {
     for (auto e : c->spare) cudaEventDestroy(e);
     ctx_free(c, c->d_stats, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t));
     if (c->stage) cudaFreeHost(c->stage);
+    ctx_free(c, c->scratch, c->scratch_bytes);
     cudaStreamDestroy(c->stream);
     delete c;
 }
@@ -697,6 +698,26 @@ sf_status wait_stream(cudaStream_t st, uint32_t timeout_ms) {
         if (timeout_ms && el > timeout_ms) return fail(SF_ERR_TIMEOUT, "dispatch exceeded its time limit");
         std::this_thread::sleep_for(std::chrono::microseconds(200));
     }
+}
+
+// Runs f(begin, end) over [0, n) on up to 8 host threads (one below 1 M items).
+template <class F> void host_parallel(size_t n, F&& f) {
+    const size_t parts = std::min<size_t>(8, std::max<size_t>(1, n >> 20));
+    if (parts == 1) { f(size_t(0), n); return; }
+    std::vector<std::thread> pool;
+    for (size_t k = 0; k < parts; ++k) pool.emplace_back([&, k] { f(n * k / parts, n * (k + 1) / parts); });
+    for (auto& t : pool) t.join();
+}
+
+// The context's pinned staging at `bytes` or more (stage_mu held).
+cudaError_t ensure_stage(sf_context* c, size_t bytes) {
+    if (c->stage_bytes >= bytes) return cudaSuccess;
+    if (c->stage) cudaFreeHost(c->stage);
+    c->stage = nullptr;
+    c->stage_bytes = 0;
+    cudaError_t e = cudaHostAlloc(&c->stage, bytes, cudaHostAllocDefault);
+    if (e == cudaSuccess) c->stage_bytes = bytes;
+    return e;
 }
 
 std::string topology_of(const HostGraph& g) {
@@ -1232,10 +1253,18 @@ extern "C" sf_status sf_primary_trace(sf_graph* g, const sf_primary_desc* d, flo
     rc.pixel_tolerance = d->pixel_tolerance > 0 ? d->pixel_tolerance : 1.0f;
     DevScene S;
     scene_dev(sd, rc, g->info, S);
-    size_t bytes = sizeof(DevScene) + n * (1 + 1 + 3) * 4;
-    void* buf = nullptr;
-    sf_status s = ctx_alloc(c, bytes, &buf);
-    if (s != SF_OK) return s;
+    const size_t bytes = sizeof(DevScene) + n * (1 + 1 + 3) * 4;
+    // the context's scratch and pinned staging, kept between calls
+    std::lock_guard<std::mutex> lk(c->stage_mu);
+    if (c->scratch_bytes < bytes) {
+        ctx_free(c, c->scratch, c->scratch_bytes);
+        c->scratch = nullptr;
+        c->scratch_bytes = 0;
+        sf_status s = ctx_alloc(c, bytes, &c->scratch);
+        if (s != SF_OK) return s;
+        c->scratch_bytes = bytes;
+    }
+    void* buf = c->scratch;
     DevScene* dS = static_cast<DevScene*>(buf);
     float* dt = reinterpret_cast<float*>(reinterpret_cast<char*>(buf) + sizeof(DevScene));
     uint32_t* ds = reinterpret_cast<uint32_t*>(dt + n);
@@ -1247,12 +1276,17 @@ extern "C" sf_status sf_primary_trace(sf_graph* g, const sf_primary_desc* d, flo
         e = sf_launch_primary(g->d_prog, dS, d->width, d->height, d->max_steps, d->rule, d->eps, d->t_far,
                               d->normal_mode, dt, ds, dn, c->d_work, c->d_stats, 1, c->stream);
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(t_out, dt, n * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(steps_out, ds, n * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(normal_out, dn, 3 * n * 4, cudaMemcpyDeviceToHost, c->stream);
+    // t, steps and normals are contiguous after the scene: one copy into the staging
+    if (e == cudaSuccess) e = ensure_stage(c, n * 20);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->stage, dt, n * 20, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    ctx_free(c, buf, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "sf_primary_trace");
+    const char* st = static_cast<const char*>(c->stage);
+    host_parallel(n, [&](size_t b, size_t end) {
+        std::memcpy(t_out + b, st + b * 4, (end - b) * 4);
+        std::memcpy(steps_out + b, st + n * 4 + b * 4, (end - b) * 4);
+        std::memcpy(normal_out + 3 * b, st + n * 8 + b * 12, (end - b) * 12);
+    });
     return SF_OK;
 }
 
@@ -1548,15 +1582,6 @@ extern "C" sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t ca
 }
 
 namespace sfh {
-// Runs f(begin, end) over [0, n) on up to 8 host threads (one below 1 M items).
-template <class F> void host_parallel(size_t n, F&& f) {
-    const size_t parts = std::min<size_t>(8, std::max<size_t>(1, n >> 20));
-    if (parts == 1) { f(size_t(0), n); return; }
-    std::vector<std::thread> pool;
-    for (size_t k = 0; k < parts; ++k) pool.emplace_back([&, k] { f(n * k / parts, n * (k + 1) / parts); });
-    for (auto& t : pool) t.join();
-}
-
 // Film readback through the context's pinned staging: the device planes arrive at
 // full link speed, then the host threads copy them into the caller's (pageable)
 // buffers and derive the others: color = accum.rgb / max(count, 1) with alpha 1
@@ -1568,14 +1593,7 @@ cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_plan
     const size_t bytes = (need_acc ? px * 16 : 0) + (out.depth ? px * 4 : 0) + (out.aux ? px * 16 : 0);
     if (!bytes) return cudaSuccess;
     std::lock_guard<std::mutex> lk(c->stage_mu);
-    if (c->stage_bytes < bytes) {
-        if (c->stage) cudaFreeHost(c->stage);
-        c->stage = nullptr;
-        c->stage_bytes = 0;
-        cudaError_t e = cudaHostAlloc(&c->stage, bytes, cudaHostAllocDefault);
-        if (e != cudaSuccess) return e;
-        c->stage_bytes = bytes;
-    }
+    if (cudaError_t e = ensure_stage(c, bytes); e != cudaSuccess) return e;
     float* acc = static_cast<float*>(c->stage);
     float* depth = acc + (need_acc ? px * 4 : 0);
     float* aux = depth + (out.depth ? px : 0);

@@ -74,9 +74,12 @@ struct sf_context {
     int refs = 1;
     std::mutex mu;
     std::mutex alloc_mu;  // budget accounting (a server thread allocates too)
-    // pinned staging of film readbacks, grown on demand and reused by every session
+    // pinned staging of readbacks and the primary-ray scratch, grown on demand and
+    // reused by every call (stage_mu guards both)
     void* stage = nullptr;
     size_t stage_bytes = 0;
+    void* scratch = nullptr;
+    size_t scratch_bytes = 0;
     std::mutex stage_mu;
 };
 
