@@ -331,15 +331,18 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
 __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo, float2* orbit_f,
                             uint32_t* orbit_len) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
-    double zx = 0.0, zy = 0.0, b2 = bailout * bailout;
+    double zx = 0.0, zy = 0.0;
+    const double b2 = __dmul_rn(bailout, bailout);
     uint32_t n = 0;
     for (;;) {
         float hx = (float)zx, hy = (float)zy;
         orbit_f[n] = make_float2(hx, hy);
         orbit_lo[n] = make_float2((float)(zx - (double)hx), (float)(zy - (double)hy));
-        if (n >= max_iter || zx * zx + zy * zy > b2) break;
-        double nx = zx * zx - zy * zy + cx;
-        zy = 2.0 * zx * zy + cy;
+        // unfused, in the order of the host's orbit (sf_host.cpp host_ref_orbit), so
+        // both give the same Z_n to the last bit
+        if (n >= max_iter || __dadd_rn(__dmul_rn(zx, zx), __dmul_rn(zy, zy)) > b2) break;
+        const double nx = __dadd_rn(__dsub_rn(__dmul_rn(zx, zx), __dmul_rn(zy, zy)), cx);
+        zy = __dadd_rn(__dmul_rn(__dmul_rn(2.0, zx), zy), cy);
         zx = nx;
         ++n;
     }
