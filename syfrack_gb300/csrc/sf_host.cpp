@@ -620,10 +620,20 @@ void detect_form(const HostGraph& g, DeProgram& P) {
 
 namespace sfh {
 
-sf_status ctx_alloc(sf_context* c, size_t bytes, void** p) {
+sf_status ctx_alloc(sf_context* c, size_t bytes, void** p, bool trim) {
     *p = nullptr;
     if (bytes == 0) return SF_OK;
     std::lock_guard<std::mutex> lk(c->alloc_mu);
+    if (trim && c->used + bytes > c->budget) {
+        // the cached scratch of primary and escape-time calls gives way to an admission
+        std::unique_lock<std::mutex> sl(c->stage_mu, std::try_to_lock);
+        if (sl.owns_lock() && c->scratch) {
+            cudaFree(c->scratch);
+            c->used -= c->scratch_bytes;
+            c->scratch = nullptr;
+            c->scratch_bytes = 0;
+        }
+    }
     if (c->used + bytes > c->budget)
         return fail(SF_ERR_BUDGET, "HBM admission budget exceeded: " + std::to_string(c->used + bytes) + " > " +
                                        std::to_string(c->budget) + " bytes");
@@ -718,6 +728,17 @@ cudaError_t ensure_stage(sf_context* c, size_t bytes) {
     cudaError_t e = cudaHostAlloc(&c->stage, bytes, cudaHostAllocDefault);
     if (e == cudaSuccess) c->stage_bytes = bytes;
     return e;
+}
+
+// The context's device scratch at `bytes` or more (stage_mu held), within the budget.
+sf_status ensure_scratch(sf_context* c, size_t bytes) {
+    if (c->scratch_bytes >= bytes) return SF_OK;
+    ctx_free(c, c->scratch, c->scratch_bytes);
+    c->scratch = nullptr;
+    c->scratch_bytes = 0;
+    const sf_status s = ctx_alloc(c, bytes, &c->scratch, false);  // stage_mu is held: no trim
+    if (s == SF_OK) c->scratch_bytes = bytes;
+    return s;
 }
 
 std::string topology_of(const HostGraph& g) {
@@ -1256,14 +1277,7 @@ extern "C" sf_status sf_primary_trace(sf_graph* g, const sf_primary_desc* d, flo
     const size_t bytes = sizeof(DevScene) + n * (1 + 1 + 3) * 4;
     // the context's scratch and pinned staging, kept between calls
     std::lock_guard<std::mutex> lk(c->stage_mu);
-    if (c->scratch_bytes < bytes) {
-        ctx_free(c, c->scratch, c->scratch_bytes);
-        c->scratch = nullptr;
-        c->scratch_bytes = 0;
-        sf_status s = ctx_alloc(c, bytes, &c->scratch);
-        if (s != SF_OK) return s;
-        c->scratch_bytes = bytes;
-    }
+    if (const sf_status s = ensure_scratch(c, bytes); s != SF_OK) return s;
     void* buf = c->scratch;
     DevScene* dS = static_cast<DevScene*>(buf);
     float* dt = reinterpret_cast<float*>(reinterpret_cast<char*>(buf) + sizeof(DevScene));
@@ -1929,9 +1943,11 @@ extern "C" sf_status sf_escape2d(sf_context* c, const sf_planar_desc* f, const s
     K.height = canvas->height;
     K.seed = uint32_t(canvas->seed) ^ uint32_t(canvas->seed >> 32);
     size_t bytes = 768 + n * 4 * 6;  // descriptors | pixel counter | outputs
-    void* buf = nullptr;
-    st = ctx_alloc(c, bytes, &buf);
+    // the context's device scratch and pinned staging, kept between calls
+    std::unique_lock<std::mutex> lk(c->stage_mu);
+    st = ensure_scratch(c, bytes);
     if (st != SF_OK) return st;
+    void* buf = c->scratch;
     PlanarDev* dF = static_cast<PlanarDev*>(buf);
     CanvasDev* dK = reinterpret_cast<CanvasDev*>(static_cast<char*>(buf) + 256);
     uint32_t* dW = reinterpret_cast<uint32_t*>(static_cast<char*>(buf) + 512);
@@ -1946,12 +1962,19 @@ extern "C" sf_status sf_escape2d(sf_context* c, const sf_planar_desc* f, const s
         e = sf_launch_escape2d(dF, dK, tile.x, tile.y, tile.w, tile.h, sample, dd, dt, di, c->d_stats, dW, 1,
                                F.family == 3 || F.family == 4, c->stream);
     }
-    if (e == cudaSuccess) e = cudaMemcpyAsync(dist, dd, n * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(traps, dt, 4 * n * 4, cudaMemcpyDeviceToHost, c->stream);
-    if (e == cudaSuccess) e = cudaMemcpyAsync(iters, di, n * 4, cudaMemcpyDeviceToHost, c->stream);
+    // distance, traps and iterations are contiguous: one copy into the pinned staging,
+    // then host threads split it into the caller's arrays
+    if (e == cudaSuccess) e = ensure_stage(c, n * 24);
+    if (e == cudaSuccess) e = cudaMemcpyAsync(c->stage, dd, n * 24, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaStreamSynchronize(c->stream);
-    ctx_free(c, buf, bytes);
     if (e != cudaSuccess) return cuda_fail(e, "sf_escape2d");
+    const char* stg = static_cast<const char*>(c->stage);
+    host_parallel(n, [&](size_t b0, size_t b1) {
+        std::memcpy(dist + b0, stg + b0 * 4, (b1 - b0) * 4);
+        for (int k = 0; k < 4; ++k)  // traps are four planes of n
+            std::memcpy(traps + k * n + b0, stg + (n + k * n + b0) * 4, (b1 - b0) * 4);
+        std::memcpy(iters + b0, stg + (5 * n + b0) * 4, (b1 - b0) * 4);
+    });
     return SF_OK;
 }
 

@@ -98,7 +98,9 @@ struct sf_graph {
 namespace sfh {
 
 // Device memory under the context's HBM admission budget.
-sf_status ctx_alloc(sf_context* c, size_t bytes, void** p);
+// Device memory within the context's budget; `trim` lets the cached scratch of
+// primary and escape-time calls be released first (callers holding stage_mu pass false).
+sf_status ctx_alloc(sf_context* c, size_t bytes, void** p, bool trim = true);
 void ctx_free(sf_context* c, void* p, size_t bytes);
 void ctx_retain(sf_context* c);
 void ctx_release(sf_context* c);
