@@ -130,6 +130,19 @@ __device__ __forceinline__ void trap_sqrt(DeRaw& s, uint32_t slot) {
 // division (a few ulp): one MUFU reciprocal square root / reciprocal and a multiply.
 __device__ __forceinline__ float sqrt_fast(float x) { return x > 0.0f && x < SF_INF ? x * rsqrtf(x) : x; }
 // 1/x by the hardware approximation (PTX rcp.approx.ftz.f32, max error 1 ulp):
+// (a.x * b + c.x, a.y * b + c.y) as one packed FMA (fma.rn.f32x2, sm_100 and later):
+// each lane rounds exactly as fmaf does, in one issue slot instead of two.
+__device__ __forceinline__ float2 fma2_scalar(float ax, float ay, float b, float cx, float cy) {
+    unsigned long long ra, rb, rc, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(ax), "f"(ay));
+    asm("mov.b64 %0, {%1, %1};" : "=l"(rb) : "f"(b));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rc) : "f"(cx), "f"(cy));
+    asm("fma.rn.f32x2 %0, %1, %2, %3;" : "=l"(rd) : "l"(ra), "l"(rb), "l"(rc));
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(rd));
+    return r;
+}
+
 // x / y as x * rcp_approx(y) is within 2 ulp for normal y.
 __device__ __forceinline__ float rcp_approx(float x) {
     float r;
@@ -286,7 +299,8 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
         const float k = r2 < mr2 ? kmin : fmaxf(fr2 * rcp_approx(r2), 1.0f);
         // sphere fold, Scale and AddOrigin as one multiply-add per component
         const float ks = k * sc;
-        p = mk3(fmaf(p.x, ks, c.x), fmaf(p.y, ks, c.y), fmaf(p.z, ks, c.z));
+        const float2 pxy = fma2_scalar(p.x, p.y, ks, c.x, c.y);
+        p = mk3(pxy.x, pxy.y, fmaf(p.z, ks, c.z));
         dr = fmaf(dr, k * asc, 1.0f);
     }
     s.iter = i;
