@@ -53,6 +53,20 @@ def test_status_strings(lib):
     assert lib.sf_abi_version() >> 16 == 1
 
 
+def test_film_planes_struct_matches_the_header(lib):
+    """sf_film_planes at ABI 1.1: seven plane pointers, the colour plane last."""
+    import ctypes as C
+    from syfrack_gb300._lib import sf_film_planes
+
+    assert lib.sf_abi_version() & 0xFFFF >= 1
+    assert [f[0] for f in sf_film_planes._fields_] == ["accum", "depth", "aux", "volume", "moments", "surface",
+                                                       "color"]
+    assert C.sizeof(sf_film_planes) == 7 * C.sizeof(C.c_void_p)
+    header = open(os.path.join(os.path.dirname(os.path.abspath(__file__)), "..", "include", "syfrack_gpu.h")).read()
+    body = header[header.index("typedef struct sf_film_planes"):header.index("} sf_film_planes;")]
+    assert body.count("float*") == 7
+
+
 def test_null_arguments_are_rejected(lib):
     assert lib.sf_context_create(0, 0, None) == 1  # SF_ERR_INVALID
     assert lib.sf_graph_compile(None, None, None) == 1
