@@ -262,13 +262,20 @@ typedef struct sf_scene_desc {
     sf_fog fog;
 } sf_scene_desc;
 
-/* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138). */
+/* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138).
+ * hit_epsilon (ABI 1.2) has no field in the reference: 0 keeps the reference's
+ * cone-relative hit test radius / t < pixel_cone * pixel_tolerance
+ * (pathtrace.wgsl:117-122) for every segment; a value > 0 replaces it with the
+ * fixed-epsilon test radius <= hit_epsilon (candidates accepted at the step budget
+ * within 4 * hit_epsilon), the rule of a benchmark stated as "epsilon 1e-4". The
+ * normal-tap step and bounce offsets keep their pixel-cone formulas either way. */
 enum { SF_INTEGRATOR_MEGAKERNEL = 0, SF_INTEGRATOR_WAVEFRONT = 1 };
 typedef struct sf_render_config {
     uint32_t integrator;
     uint32_t width, height, samples_per_pixel, max_bounces, max_steps;
     float pixel_tolerance;
     uint32_t tile_size, samples_per_dispatch;
+    float hit_epsilon;
 } sf_render_config;
 
 /* Tile{x,y,w,h,done} (crates/syfrack-render/src/tiles.rs:4-11). */

@@ -858,6 +858,7 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
     s.fog_color = V3<R>(R(d.fog.color[0]), R(d.fog.color[1]), R(d.fog.color[2]));
     s.seed = uint32_t(d.seed) ^ uint32_t(d.seed >> 32);
     s.pixel_tolerance = R(c.pixel_tolerance);
+    s.hit_eps = R(c.hit_epsilon);
     // uniforms.rs:781-782: far = max(2*hint + |origin|, 200), computed in f32.
     float origin_len = sqrtf(d.camera.origin[0] * d.camera.origin[0] + d.camera.origin[1] * d.camera.origin[1] +
                              d.camera.origin[2] * d.camera.origin[2]);
@@ -1445,8 +1446,9 @@ static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd
         R t = area_intersection(ro, rd, sc.lights[i]);
         if (t < nearest) { nearest = t; light_index = i; }
     }
-    Hit<R> h = march_segment(g, ro, rd, sc.step_scale, pixel_cone * sc.pixel_tolerance, nearest, sc.max_steps, false,
-                             R(0), evals);
+    // the reference's cone-relative test, or a fixed epsilon when the render states one
+    Hit<R> h = march_segment(g, ro, rd, sc.step_scale, pixel_cone * sc.pixel_tolerance, nearest, sc.max_steps,
+                             sc.hit_eps > R(0), sc.hit_eps, evals);
     if (!h.hit && !h.exhausted && light_index != 0xffffffffu) {
         h.hit = true;
         h.t = nearest;

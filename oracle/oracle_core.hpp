@@ -233,6 +233,7 @@ template <class R> struct Scene {
     uint32_t seed = 0;
     // fractal uniforms (uniforms.rs:183-189, :781-782)
     R pixel_tolerance = 1, far = 200, step_scale = 1;
+    R hit_eps = 0;  // > 0: fixed-epsilon hit test radius <= hit_eps; 0: cone-relative
     uint32_t iteration_product = 1;
     uint32_t width = 1, height = 1, max_bounces = 4, max_steps = 256;
 };

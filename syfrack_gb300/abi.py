@@ -114,7 +114,8 @@ class sf_render_config(C.Structure):
     _fields_ = [("integrator", C.c_uint32), ("width", C.c_uint32), ("height", C.c_uint32),
                 ("samples_per_pixel", C.c_uint32), ("max_bounces", C.c_uint32),
                 ("max_steps", C.c_uint32), ("pixel_tolerance", C.c_float),
-                ("tile_size", C.c_uint32), ("samples_per_dispatch", C.c_uint32)]
+                ("tile_size", C.c_uint32), ("samples_per_dispatch", C.c_uint32),
+                ("hit_epsilon", C.c_float)]
 
 
 class sf_tile(C.Structure):

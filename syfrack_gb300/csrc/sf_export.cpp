@@ -20,7 +20,7 @@ using namespace sfh;
 namespace {
 
 constexpr uint32_t EX_MAGIC = 0x58454653u;  // "SFEX"
-constexpr uint32_t EX_VERSION = 2;  // 2: the scene carries its fog
+constexpr uint32_t EX_VERSION = 3;  // 2: the scene carries its fog; 3: the config its hit epsilon
 constexpr int kStages = 2;
 
 struct Stage {

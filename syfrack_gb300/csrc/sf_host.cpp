@@ -48,7 +48,7 @@ sf_status cuda_fail(cudaError_t e, const char* what) {
 constexpr uint32_t MAX_DEPTH = 3;          // graph/mod.rs:41
 constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
 constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
-constexpr uint32_t ABI_VERSION = (1u << 16) | 1u;  // 1.1: sf_film_planes.color
+constexpr uint32_t ABI_VERSION = (1u << 16) | 2u;  // 1.1: sf_film_planes.color; 1.2: sf_render_config.hit_epsilon
 
 // ------------------------------------------------------------------ graph preparation
 
@@ -971,6 +971,7 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     float far = std::max(2.0f * gi.bounding_radius_hint + ol, 200.0f);  // uniforms.rs:781-782
     S.extent = std::max(200.0f, far);                                   // ray_extent, common.wgsl:206-208
     S.pixel_cone = d.camera.tan_half_fov * 2.0f / float(c.width);
+    S.hit_eps = c.hit_epsilon;
     S.iteration_product = gi.iteration_product;
     material_dev(d.material, S.material);
     for (uint32_t i = 0; i < S.finish_count; ++i) material_dev(d.finishes[i], S.finishes[i]);
@@ -1330,6 +1331,8 @@ sf_status validate_config(const sf_render_config& c) {
     if (c.max_steps < 1) return fail(SF_ERR_INVALID, "max_steps must be at least 1");
     if (!(c.pixel_tolerance >= 0.125f && c.pixel_tolerance <= 1.0f))
         return fail(SF_ERR_INVALID, "pixel_tolerance must be between 0.125 and 1.0");
+    if (!(c.hit_epsilon >= 0.0f && c.hit_epsilon <= 1.0f))
+        return fail(SF_ERR_INVALID, "hit_epsilon must be between 0 (cone-relative test) and 1.0");
     if (c.integrator > SF_INTEGRATOR_WAVEFRONT) return fail(SF_ERR_INVALID, "unknown integrator");
     return SF_OK;
 }
@@ -1680,7 +1683,7 @@ uint64_t fnv1a(const void* data, size_t n, uint64_t h) {
 
 
 const uint32_t CK_MAGIC = 0x4b434653u;  // "SFCK"
-const uint32_t CK_VERSION = 3;  // 3: the scene carries its fog
+const uint32_t CK_VERSION = 4;  // 3: the scene carries its fog; 4: the config its hit epsilon
 
 std::string producer_of(const sf_context* c) {
     return c->device_name + "|sm_" + std::to_string(c->cc_major) + std::to_string(c->cc_minor) + "|abi " +
@@ -1794,8 +1797,9 @@ extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* d
     sf_scene_desc scene = r.get<sf_scene_desc>();
     std::string topo = r.get_str();
     uint32_t nn = r.get<uint32_t>();
+    // bounded before anything is sized from it: the hash does not authenticate the file
+    if (!r.ok || nn > 4096) return fail(SF_ERR_CHECKPOINT, "checkpoint graph too large or truncated");
     std::vector<sf_node> nodes(nn);
-    if (nn > 4096) return fail(SF_ERR_CHECKPOINT, "checkpoint graph too large");
     r.get_bytes(nodes.data(), nn * sizeof(sf_node));
     const uint64_t placements_hash = r.get<uint64_t>();
     uint32_t dispatches = r.get<uint32_t>();

@@ -210,19 +210,19 @@ cudaError_t sf_launch_film_clear(FilmPlanes film, cudaStream_t st) {
 // The plain per-pixel integrator (pathtrace.wgsl:1203-1276): one thread per
 // pixel runs every sample's whole path with blocking marches.
 static __device__ int march_full(const DeProgram& P, March& m, uint32_t max_steps, float safety, float accept,
-                                 DeRaw& hit, unsigned long long& evals, unsigned long long& iters) {
+                                 bool absolute, DeRaw& hit, unsigned long long& evals, unsigned long long& iters) {
     int r = march_check(m, max_steps, accept);
     while (r == MARCH_CONTINUE) {
         const float3 q = m.ro + m.rd * m.t;
         DeRaw s = de_raw(P, q);
         evals++;
         iters += s.iter;
-        if (needs_exact(s, m.t, safety, accept, false)) {
+        if (needs_exact(s, m.t, safety, accept, absolute)) {
             s = de_raw_exact(P, q);
             evals++;
             iters += s.iter;
         }
-        r = march_update(m, s.d, s.flags, safety, accept, false);
+        r = march_update(m, s.d, s.flags, safety, accept, absolute);
         if (r == MARCH_HIT) { hit = s; m.cand_t = m.t; return r; }
         if (r == MARCH_CONTINUE) r = march_check(m, max_steps, accept);
     }
@@ -231,7 +231,7 @@ static __device__ int march_full(const DeProgram& P, March& m, uint32_t max_step
         hit = de_raw(P, q);
         evals++;
         iters += hit.iter;
-        if (needs_exact(hit, m.cand_t, safety, accept, false)) {
+        if (needs_exact(hit, m.cand_t, safety, accept, absolute)) {
             hit = de_raw_exact(P, q);
             evals++;
             iters += hit.iter;
@@ -252,7 +252,8 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
     if (lx >= g.tile_w || ly >= g.tile_h) return;
     uint32_t px = g.tile_x + lx, py = g.tile_y + ly;
     uint32_t tile_px = g.tile_w * g.tile_h, local = ly * g.tile_w + lx;
-    const float accept = S.pixel_cone * S.pixel_tolerance;
+    const float accept = hit_accept(S);
+    const bool absolute = hit_absolute(S);
     unsigned long long evals = 0, iters = 0, segs = 0;
     const uint32_t stream = point_stream_of(S, px, py);
     for (uint32_t s = 0; s < g.samples; ++s) {
@@ -267,7 +268,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
             float t_end = nearest_emitter(S, ps.o, ps.d, S.extent, li);
             march_begin(m, ps.o, ps.d, t_end);
             DeRaw hs;
-            int r = march_full(P, m, S.max_steps, S.step_scale, accept, hs, evals, iters);
+            int r = march_full(P, m, S.max_steps, S.step_scale, accept, absolute, hs, evals, iters);
             segs++;
             HitInfo h;
             h.hit = false;
@@ -309,7 +310,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 float st_end = nearest_emitter(S, sh.o, sh.dir, sh.t_end, sli);
                 march_begin(sm, sh.o, sh.dir, st_end);
                 DeRaw shs;
-                int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, shs, evals, iters);
+                int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, absolute, shs, evals, iters);
                 segs++;
                 if (sr == MARCH_MISS && sli == SF_NO_LIGHT) ps.L = add_rn(ps.L, sh.contrib);
             };

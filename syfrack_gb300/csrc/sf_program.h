@@ -122,6 +122,7 @@ struct DevScene {
     float cavity;
     float pixel_tolerance, step_scale, extent;  // extent = max(200, far)
     float pixel_cone;                           // tan_half * 2 / width
+    float hit_eps;                              // > 0: fixed-epsilon hit test; 0: cone-relative
     uint32_t iteration_product;
     // Material.coloring: slot (0..3 trap, 4 iterations, 5 normal, else none) and ramp
     uint32_t col_slot, col_n, col_cyclic, col_smooth, col_positioned;

@@ -100,6 +100,13 @@ __device__ __forceinline__ int march_update(March& m, float d, uint32_t flags, f
     return MARCH_CONTINUE;
 }
 
+// The scene's hit rule: a fixed epsilon when the render asks for one, else the
+// reference's cone-relative test at the pixel tolerance.
+__device__ __forceinline__ bool hit_absolute(const DevScene& S) { return S.hit_eps > 0.0f; }
+__device__ __forceinline__ float hit_accept(const DevScene& S) {
+    return S.hit_eps > 0.0f ? S.hit_eps : S.pixel_cone * S.pixel_tolerance;
+}
+
 // ------------------------------------------------------------------ shading arithmetic
 // The shading code below (not the march and not the DE) uses WGSL's accuracy class
 // for division (2.5 ulp) and sqrt: PTX div.approx / sqrt.approx and the reciprocal

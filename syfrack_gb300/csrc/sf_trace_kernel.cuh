@@ -69,8 +69,10 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     const DevScene* Sl = &S;
     float accept = 0.f, safety = 0.f, cone = 0.f, tol = 0.f;
     uint32_t max_steps = 0;
+    bool absolute = false;
     if constexpr (!MULTI) {
-        accept = S.pixel_cone * S.pixel_tolerance;
+        accept = hit_accept(S);
+        absolute = hit_absolute(S);
         safety = S.step_scale;
         max_steps = S.max_steps;
         cone = S.pixel_cone;
@@ -138,7 +140,8 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     Sl = job.scene;
                     cone = Sl->pixel_cone;
                     tol = Sl->pixel_tolerance;
-                    accept = cone * tol;
+                    accept = hit_accept(*Sl);
+                    absolute = hit_absolute(*Sl);
                     safety = Sl->step_scale;
                     max_steps = Sl->max_steps;
                 }
@@ -180,7 +183,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             n_iter += s.iter;
             if constexpr (FORM == SF_FORM_ANY) {
                 // a flagged march or candidate sample near acceptance: the exact sample
-                if (state != TL_NORMAL && needs_exact(s, m.t, safety, accept, false)) {
+                if (state != TL_NORMAL && needs_exact(s, m.t, safety, accept, absolute)) {
                     if constexpr (MULTI) s = de_raw_exact(*Pl, q);
                     else s = de_raw_exact(P, q);
                     n_eval++;
@@ -208,7 +211,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             } else if (state == TL_CAND) {
                 surface_hit(s);
             } else {
-                int r = march_update(m, s.d, s.flags, safety, accept, false);
+                int r = march_update(m, s.d, s.flags, safety, accept, absolute);
                 if (r == MARCH_HIT) {
                     if (shadow) finish(MARCH_HIT);
                     else surface_hit(s);

@@ -388,6 +388,8 @@ class RenderConfig:
     tile_size: int = 256
     samples_per_dispatch: int = 8
     integrator: str = "megakernel"  # or "wavefront"
+    # 0: the reference's cone-relative hit test; > 0: fixed epsilon radius <= hit_epsilon
+    hit_epsilon: float = 0.0
 
     def desc(self) -> abi.sf_render_config:
         c = abi.sf_render_config()
@@ -396,6 +398,7 @@ class RenderConfig:
         c.max_bounces, c.max_steps = self.max_bounces, self.max_steps
         c.pixel_tolerance = self.pixel_tolerance
         c.tile_size, c.samples_per_dispatch = self.tile_size, self.samples_per_dispatch
+        c.hit_epsilon = self.hit_epsilon
         return c
 
 

@@ -5,7 +5,9 @@ and parameter ranges).
 mandelbulb_primary : 256x256 primary rays, Mandelbulb power 8, 12 iterations,
                      bailout 2.0, pinhole at (0,0,-3) looking at the origin with a
                      60 degree horizontal field of view, 256 steps, epsilon 1e-4, far 10.
-mandelbox_pathtrace: 1280x720, 64 spp, 4 bounces, 512 steps; Mandelbox scale -1.5
+mandelbox_pathtrace: 1280x720, 64 spp, 4 bounces, 512 steps, hit epsilon 1e-4
+                     (fixed-epsilon hit test; rule="cone" gives the reference's
+                     cone-relative test at pixel tolerance 1); Mandelbox scale -1.5
                      (box fold 1, min radius 0.5, fixed radius 1, 15 iterations,
                      bailout 1000, NormFence); Lambert albedo 0.7 blending into a
                      metal of roughness 0.2 by orbit trap 0; one 1x1 area light of
@@ -53,11 +55,17 @@ def mandelbox_scene(seed: int = 20261203) -> Scene:
     return Scene(graph=mandelbox_graph(), camera=cam, material=mat, lights=[light], seed=seed)
 
 
+PATHTRACE_EPSILON = 1e-4
+
+
 def mandelbox_pathtrace_config(integrator="wavefront", width=1280, height=720, spp=64,
-                               samples_per_dispatch=8) -> RenderConfig:
+                               samples_per_dispatch=8, rule="epsilon") -> RenderConfig:
+    """rule "epsilon": hits at radius <= 1e-4 (the stated march epsilon); "cone": the
+    reference's cone-relative test radius / t < pixel_cone at pixel tolerance 1."""
+    eps = {"epsilon": PATHTRACE_EPSILON, "cone": 0.0}[rule]
     return RenderConfig(width=width, height=height, samples_per_pixel=spp, max_bounces=4, max_steps=512,
                         pixel_tolerance=1.0, tile_size=max(width, height),
-                        samples_per_dispatch=samples_per_dispatch, integrator=integrator)
+                        samples_per_dispatch=samples_per_dispatch, integrator=integrator, hit_epsilon=eps)
 
 
 def mixed_batch(seed: int = 7, jobs: int = 64):
