@@ -509,7 +509,11 @@ sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* it
  * GPU that loads the library until exit (1 MB): max_iter above 65536 is rejected
  * with SF_ERR_INVALID. The first call on a device looks that array up, so make it
  * before any stream capture. All calls share the array: calls that overlap on the
- * GPU (two streams, two threads) race; order them on one stream. */
+ * GPU (two streams, two threads) race; order them on one stream. The array's address
+ * is looked up once per device and kept for the life of the process: after
+ * cudaDeviceReset (or anything else that re-creates the device's primary context)
+ * the kept address is stale, so do not call this entry point again in that process.
+ * Frames hold at most 2^31 pixels (SF_ERR_INVALID beyond), as for sf_deep_zoom. */
 sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth, void* stream);
 
 /* ------------------------------------------------------------------ serving

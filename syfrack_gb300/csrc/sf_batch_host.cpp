@@ -17,6 +17,7 @@ struct sf_batch {
     sf_context* ctx = nullptr;
     std::vector<sf_graph*> graphs;
     std::vector<BatchJob> jobs;  // host copy (initial sample_start)
+    std::vector<sf_scene_desc> scenes;
     WaveArena a;
     cudaGraphExec_t exec = nullptr;
     uint32_t status_host = 0;
@@ -148,6 +149,7 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     cudaSetDevice(c->device);
     auto* b = new sf_batch();
     b->ctx = c;
+    for (uint32_t i = 0; i < n; ++i) b->scenes.push_back(jobs[i].scene);
     const size_t scene_bytes = (n * sizeof(DevScene) + 255) & ~size_t(255);
     size_t extra = 0;
     uint32_t K = 1;  // the most shadow segments one bounce of any job issues
@@ -313,6 +315,7 @@ extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t*
 extern "C" sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes* out) {
     if (!b || !out) return fail(SF_ERR_INVALID, "null argument");
     if (job >= b->jobs.size()) return fail(SF_ERR_INVALID, "job index out of range");
+    if (const sf_status st = check_volume_planes(b->scenes[job], *out); st != SF_OK) return st;
     sf_context* c = b->ctx;
     cudaSetDevice(c->device);
     CU(film_readback(c, b->jobs[job].film, *out, c->stream));

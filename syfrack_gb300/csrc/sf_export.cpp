@@ -224,6 +224,7 @@ extern "C" sf_status sf_export_progress(sf_export* e, sf_progress* out) {
 
 extern "C" sf_status sf_export_readback(sf_export* e, sf_film_planes* out) {
     if (!e || !out) return fail(SF_ERR_INVALID, "null argument");
+    if (const sf_status vs = check_volume_planes(e->win->scene, *out); vs != SF_OK) return vs;
     cudaSetDevice(e->ctx->device);
     sf_status st = flush(e);
     if (st != SF_OK) return st;

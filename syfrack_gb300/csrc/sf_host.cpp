@@ -623,11 +623,19 @@ namespace sfh {
 sf_status ctx_alloc(sf_context* c, size_t bytes, void** p, bool trim) {
     *p = nullptr;
     if (bytes == 0) return SF_OK;
-    std::lock_guard<std::mutex> lk(c->alloc_mu);
+    std::unique_lock<std::mutex> lk(c->alloc_mu);
     if (trim && c->used + bytes > c->budget) {
-        // the cached scratch of primary and escape-time calls gives way to an admission
+        // The cached scratch of primary and escape-time calls gives way to an admission.
+        // Its owner (stage_mu) may be in a readback: then wait for it, taking the locks in
+        // the order the scratch's users take them (stage_mu, then alloc_mu), so that the
+        // admission's outcome does not depend on timing. No caller that trims holds stage_mu.
         std::unique_lock<std::mutex> sl(c->stage_mu, std::try_to_lock);
-        if (sl.owns_lock() && c->scratch) {
+        if (!sl.owns_lock()) {
+            lk.unlock();
+            sl.lock();
+            lk.lock();
+        }
+        if (c->scratch && c->used + bytes > c->budget) {
             cudaFree(c->scratch);
             c->used -= c->scratch_bytes;
             c->scratch = nullptr;
@@ -1643,8 +1651,18 @@ cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_plan
 }
 }  // namespace sfh
 
+namespace sfh {
+sf_status check_volume_planes(const sf_scene_desc& scene, const sf_film_planes& out) {
+    if (scene.fog.density > 0.0f && (out.volume || out.moments || out.surface))
+        return fail(SF_ERR_UNSUPPORTED, "the volume layer split of a fog scene is not kept on the device film: "
+                                        "read accum, depth, aux or color");
+    return SF_OK;
+}
+}  // namespace sfh
+
 extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
     if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
+    if (const sf_status st = check_volume_planes(s->scene, *out); st != SF_OK) return st;
     sf_context* c = s->ctx;
     cudaSetDevice(c->device);
     CU(film_readback(c, s->film, *out, c->stream));
@@ -2019,6 +2037,8 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     if (!iters || !smooth) return fail(SF_ERR_INVALID, "null output");
     if (reference_f64 && (!iters64 || !smooth64)) return fail(SF_ERR_INVALID, "null FP64 output");
     if (!(d->bailout >= 2.0f)) return fail(SF_ERR_INVALID, "bailout must be at least 2");
+    // the perturbation kernel indexes pixels with 32-bit counters
+    if (uint64_t(d->width) * d->height > (1ull << 31)) return fail(SF_ERR_INVALID, "deep-zoom frames hold at most 2^31 pixels");
     cudaSetDevice(c->device);
     size_t n = size_t(d->width) * d->height;
     size_t M = size_t(d->max_iter) + 4;  // the orbit, two entries past its end, one spare

@@ -62,6 +62,8 @@ extern "C" sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* 
                                           void* stream) {
     if (!d || !iterations || !smooth) return sf_report_error(SF_ERR_INVALID, "null argument");
     if (!d->width || !d->height || !d->max_iter) return sf_report_error(SF_ERR_INVALID, "empty deep-zoom request");
+    if (uint64_t(d->width) * d->height > (1ull << 31))
+        return sf_report_error(SF_ERR_INVALID, "deep-zoom frames hold at most 2^31 pixels");
     if (d->max_iter > kMaxIter)
         return sf_report_error(SF_ERR_INVALID, "max_iter " + std::to_string(d->max_iter) +
                                                    " exceeds the allocation-free limit of 65536 iterations");

@@ -68,24 +68,41 @@ def mandelbox_pathtrace_config(integrator="wavefront", width=1280, height=720, s
                         samples_per_dispatch=samples_per_dispatch, integrator=integrator, hit_epsilon=eps)
 
 
+def mandelbox_radius(scale: float) -> float:
+    """Radius of a sphere enclosing the Mandelbox of this scale: scales <= 1 stay in
+    the cube [-2, 2]^3, scales s > 1 reach 2(s+1)/(s-1) along each axis (the band near
+    s = 1 is capped at 12, beyond which the form is thin shells)."""
+    half = 2.0 if scale <= 1.0 else min(2.0 * (scale + 1.0) / (scale - 1.0), 12.0)
+    return half * math.sqrt(3.0)
+
+
+def mixed_batch_graph(kind: str, value) -> Graph:
+    """One form of the uneven batch: ("mandelbulb", power), ("mandelbox", scale) or
+    ("menger", level)."""
+    if kind == "mandelbulb":
+        return Graph.bundled("mandelbulb", power=float(value), iterations=10, bailout=4.0, safety=0.7, hint=2.5)
+    if kind == "mandelbox":
+        g = mandelbox_graph(scale=float(value), iterations=12)
+        g.bounding_radius_hint = mandelbox_radius(float(value))
+        return g
+    return Graph.bundled("menger", iterations=int(value))
+
+
 def mixed_batch(seed: int = 7, jobs: int = 64):
-    """Seeded list of (scene, config) for the uneven batch."""
+    """Seeded list of (scene, config) for the uneven batch: Mandelbulb powers U{2..12},
+    Mandelbox scales U[-2.5, 2.5] (the whole range), Menger levels U{3..7}; the camera
+    at 2.5-4 units (Mandelbulb, Menger) or 2.5-4 half-radii of the Mandelbox's
+    enclosing sphere from the origin, in a uniform random direction."""
     rng = np.random.default_rng(seed)
     out = []
     for j in range(jobs):
         kind = j % 3
         if kind == 0:
-            g = Graph.bundled("mandelbulb", power=float(rng.integers(2, 13)), iterations=10, bailout=4.0,
-                              safety=0.7, hint=2.5)
+            g = mixed_batch_graph("mandelbulb", int(rng.integers(2, 13)))
         elif kind == 1:
-            s = float(rng.uniform(-2.5, 2.5))
-            if abs(s) < 1.05:
-                s = math.copysign(1.05, s if s != 0 else 1.0)
-            g = mandelbox_graph(scale=s, iterations=12)
-            if abs(s) > 2.0:
-                g.bounding_radius_hint = 2.0 * (abs(s) + 1.0) / (abs(s) - 1.0) * math.sqrt(3.0)
+            g = mixed_batch_graph("mandelbox", float(rng.uniform(-2.5, 2.5)))
         else:
-            g = Graph.bundled("menger", iterations=int(rng.integers(3, 8)))
+            g = mixed_batch_graph("menger", int(rng.integers(3, 8)))
         dist = float(rng.uniform(2.5, 4.0))
         if kind == 1:
             dist *= g.bounding_radius_hint / 2.0

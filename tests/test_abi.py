@@ -72,3 +72,27 @@ def test_null_arguments_are_rejected(lib):
     assert lib.sf_graph_compile(None, None, None) == 1
     assert lib.sf_session_dispatch(None, __import__("syfrack_gb300").abi.sf_tile(0, 0, 1, 1, 0), 1) == 1
     assert lib.sf_last_error() != b""
+
+
+def test_render_config_struct_matches_the_header(lib):
+    """sf_render_config at ABI 1.2: the hit epsilon follows samples_per_dispatch."""
+    from syfrack_gb300 import abi
+
+    assert lib.sf_abi_version() == (1 << 16) | 2
+    assert [f[0] for f in abi.sf_render_config._fields_][-1] == "hit_epsilon"
+    assert C.sizeof(abi.sf_render_config) == 10 * 4
+    header = open(os.path.join(ROOT, "include", "syfrack_gpu.h")).read()
+    body = header[header.index("typedef struct sf_render_config"):header.index("} sf_render_config;")]
+    assert body.rstrip().endswith("float hit_epsilon;")
+
+
+def test_deep_zoom_frames_beyond_2_31_pixels_are_refused(lib):
+    """The perturbation kernel counts pixels in 32 bits: the allocation-free entry
+    point refuses larger frames before it touches the device (no GPU needed)."""
+    from syfrack_gb300._lib import sf_deep_zoom_desc
+
+    d = sf_deep_zoom_desc()
+    d.width, d.height, d.max_iter, d.bailout, d.width_units = 65536, 32769, 100, 2.0, 1e-3
+    dummy = C.c_void_p(16)  # never dereferenced: the size check comes first
+    assert lib.sf_deep_zoom_noalloc(C.byref(d), dummy, dummy, None) == 1  # SF_ERR_INVALID
+    assert b"2^31" in lib.sf_last_error()

@@ -98,3 +98,44 @@ def test_sky_lit_jobs_in_a_batch(renderer):
         np.testing.assert_allclose(got.depth, ref.depth, rtol=1e-6, atol=1e-6)
     assert b.readback(len(jobs) - 1).accum[..., :3].mean() > 0.05  # the sky lights reach the form
     b.close()
+
+
+def test_batched_jobs_against_oracle(renderer, oracle_mod):
+    """Three jobs of the uneven batch (a Mandelbulb of an odd power, a Mandelbox of a
+    scale below 1.05 in magnitude, a Menger sponge), batched, against the f32 oracle
+    on seeded pixels: film RMSE within 2e-2 and first-hit depth within 1e-3 where both
+    hit."""
+    from syfrack_gb300.scene import AreaLight, Scene
+
+    picks = [("mandelbulb", 5), ("mandelbox", -0.8), ("menger", 4)]
+    base = workloads.mixed_batch(seed=7, jobs=3)
+    jobs = []
+    for (kind, value), (sc, cfg) in zip(picks, base):
+        g = workloads.mixed_batch_graph(kind, value)
+        scale = g.bounding_radius_hint / 2.0 if kind == "mandelbox" else 1.0
+        d = np.asarray(sc.camera.position, np.float64)
+        pos = d / np.linalg.norm(d) * 3.0 * scale
+        cam = type(sc.camera).look_at(tuple(pos.tolist()), (0.0, 0.0, 0.0), 50.0)
+        light = AreaLight(position=tuple((pos * 0.5 + np.array([0.0, 1.8 * scale, 0.0])).tolist()),
+                          normal=(0.0, -1.0, 0.0), size=(1.0, 1.0), intensity=10.0)
+        scene = Scene(graph=g, camera=cam, material=sc.material, lights=[light], seed=sc.seed)
+        cfg.width = cfg.height = cfg.tile_size = 96
+        cfg.samples_per_pixel = cfg.samples_per_dispatch = 8
+        jobs.append((scene, cfg))
+    b = Batch(renderer, jobs)
+    b.run(1, use_graph=True)
+    assert b.sync() == 0
+    rng = np.random.default_rng(17)
+    for i, (sc, cfg) in enumerate(jobs):
+        got = b.readback(i)
+        pix = np.stack([rng.integers(0, 96, 256), rng.integers(0, 96, 256)], 1).astype(np.uint32)
+        ref = oracle_mod.OracleGraph(sc.graph).render(sc.desc(96, 96), cfg.desc(), pix, 0, 8, precision=32)
+        mine = got.accum[pix[:, 1], pix[:, 0], :3] / 8
+        rmse = float(np.sqrt(np.mean((mine - ref["accum"] / 8) ** 2)))
+        assert rmse <= 2e-2, (picks[i], rmse)
+        dd, rd = got.depth[pix[:, 1], pix[:, 0]], ref["depth"]
+        assert (dd >= 0).mean() > 0.05, picks[i]  # the form is in view
+        assert ((dd >= 0) == (rd >= 0)).mean() >= 0.97, picks[i]
+        both = (dd >= 0) & (rd >= 0)
+        assert np.median(np.abs(dd[both] - rd[both]) / np.maximum(rd[both], 1.0)) <= 1e-3, picks[i]
+    b.close()

@@ -1,0 +1,112 @@
+"""The Mandelbox path trace at its measured size (1280x720, 4 bounces, 512 steps,
+hit epsilon 1e-4) against the FP64 oracle on 4096 seeded pixels.
+
+The estimator branches on values that a last-ulp difference can flip (hit or
+miss, light selection, Russian roulette), so a binary32 render and an FP64 one
+take different paths for a few samples; one flipped sample moves its pixel by
+up to delta/64. The tests below separate that noise from the rest:
+
+* per-sample radiance of device and oracle (the device film read back after
+  every sample) classifies each sample as following the oracle's path (same
+  radiance within 1e-4) or not;
+* over pixels whose 64 samples all follow the oracle, the image error must be
+  below 1e-3 (the image-error bound of the configuration);
+* the frame mean and the flipped samples' radiance differences carry no bias
+  beyond their Monte Carlo error;
+* the flip noise falls as 1/sqrt(spp): on 2048 of the pixels, the error of the
+  256-sample mean is half the RMS error of its four 64-sample means.
+"""
+import ctypes as C
+
+import numpy as np
+import pytest
+
+from syfrack_gb300 import RenderSession, workloads
+from syfrack_gb300._lib import check, sf_film_planes
+
+pytestmark = pytest.mark.gpu
+
+W, H, SPP, SPP_LONG = 1280, 720, 64, 256
+N_PIX, N_LONG = 4096, 2048
+MATCH = 1e-4  # per-sample radiance agreement of a sample that follows the oracle's path
+
+
+def _accum(sess):
+    acc = np.empty((H, W, 4), np.float32)
+    planes = sf_film_planes(acc.ctypes.data_as(C.POINTER(C.c_float)), None, None, None, None, None, None)
+    check(sess.ctx.lib.sf_session_readback(sess.h, C.byref(planes)))
+    return acc
+
+
+@pytest.fixture(scope="module")
+def c2(renderer, oracle_mod):
+    scene = workloads.mandelbox_scene()
+    cfg = workloads.mandelbox_pathtrace_config(spp=SPP_LONG, samples_per_dispatch=1)
+    assert cfg.hit_epsilon == 1e-4 and (cfg.width, cfg.height, cfg.max_bounces, cfg.max_steps) == (W, H, 4, 512)
+    rng = np.random.default_rng(2026)
+    idx = rng.choice(W * H, N_PIX, replace=False)
+    pix = np.stack([idx % W, idx // W], 1).astype(np.uint32)
+    # device: one sample per dispatch, the film read back after each of the first 64,
+    # then after every further 64
+    sess = RenderSession(renderer, scene, cfg)
+    per_dev = np.empty((SPP, N_PIX, 3))
+    groups_dev = np.empty((SPP_LONG // SPP, N_PIX, 3))
+    prev = np.zeros((N_PIX, 3))
+    for k in range(SPP_LONG):
+        sess.dispatch((0, 0, W, H, k), 1)
+        if k < SPP or (k + 1) % SPP == 0:
+            assert sess.sync(120000) == 0
+            cur = _accum(sess)[pix[:, 1], pix[:, 0], :3].astype(np.float64)
+            if k < SPP:
+                per_dev[k] = cur - prev
+                prev = cur
+            if (k + 1) % SPP == 0:
+                groups_dev[k // SPP] = cur
+    sess.close()
+    groups_dev = np.diff(np.concatenate([np.zeros((1, N_PIX, 3)), groups_dev]), axis=0)
+    # FP64 oracle: every sample of the first 64 alone, then 64-sample groups on N_LONG pixels
+    og = oracle_mod.OracleGraph(scene.graph)
+    desc, cd = scene.desc(W, H), cfg.desc()
+    per_ref = np.stack([og.render(desc, cd, pix, k, 1, precision=64)["accum"] for k in range(SPP)])
+    groups_ref = [per_ref.sum(0)[:N_LONG]]
+    for g in range(1, SPP_LONG // SPP):
+        groups_ref.append(og.render(desc, cd, pix[:N_LONG], g * SPP, SPP, precision=64)["accum"])
+    return {"per_dev": per_dev, "per_ref": per_ref, "groups_dev": groups_dev[:, :N_LONG],
+            "groups_ref": np.stack(groups_ref)}
+
+
+def test_image_error_against_fp64_is_branch_flip_noise(c2):
+    per_dev, per_ref = c2["per_dev"], c2["per_ref"]
+    mean_dev, mean_ref = per_dev.mean(0), per_ref.mean(0)
+    rmse = float(np.sqrt(np.mean((mean_dev - mean_ref) ** 2)))
+    # a sample follows the oracle's path when its radiance agrees on every channel
+    follows = np.all(np.abs(per_dev - per_ref) <= MATCH * np.maximum(1.0, np.abs(per_ref)), axis=2)
+    all_follow = follows.all(axis=0)
+    rmse_follow = float(np.sqrt(np.mean((mean_dev[all_follow] - mean_ref[all_follow]) ** 2)))
+    flipped = ~follows
+    delta = (per_dev - per_ref)[flipped]  # (n_flips, 3)
+    frame_bias = float((mean_dev - mean_ref).mean())
+    frame_sigma = float((mean_dev - mean_ref).mean(axis=1).std() / np.sqrt(N_PIX))
+    print(f"C2 vs FP64 on {N_PIX} px x {SPP} spp: RMSE {rmse:.3e}; "
+          f"{all_follow.mean():.1%} of pixels follow the oracle on every sample, RMSE there {rmse_follow:.2e}; "
+          f"flipped samples {flipped.mean():.3%}; frame bias {frame_bias:.2e} (MC sigma {frame_sigma:.2e})")
+    # the configuration's image-error bound holds wherever the paths are the same
+    assert all_follow.mean() > 0.8
+    assert rmse_follow <= 1e-3, rmse_follow
+    # no bias: the frame mean and the flipped samples' differences are within their MC error
+    assert abs(frame_bias) <= 4.0 * frame_sigma + 1e-6, (frame_bias, frame_sigma)
+    if len(delta) >= 30:
+        d = delta.mean(axis=1)
+        assert abs(d.mean()) <= 4.0 * d.std() / np.sqrt(len(d)) + 1e-6, (d.mean(), d.std(), len(d))
+    # and the whole error is the flips': without them the error is at float rounding
+    fixed = np.where(flipped[..., None], per_ref, per_dev).mean(0)
+    assert float(np.sqrt(np.mean((fixed - mean_ref) ** 2))) <= 1e-5
+
+
+def test_branch_flip_noise_falls_as_inverse_sqrt_spp(c2):
+    e = (c2["groups_dev"] - c2["groups_ref"]) / SPP  # (4 groups, N_LONG, 3): errors of 64-sample means
+    rmse_64 = float(np.sqrt(np.mean(e ** 2)))
+    rmse_256 = float(np.sqrt(np.mean(e.mean(axis=0) ** 2)))
+    ratio = rmse_256 / rmse_64
+    print(f"branch-flip RMSE: 64 spp {rmse_64:.3e}, 256 spp {rmse_256:.3e}, ratio {ratio:.3f} (1/sqrt(4) = 0.5)")
+    assert 0.3 <= ratio <= 0.7, ratio

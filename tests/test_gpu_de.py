@@ -150,3 +150,42 @@ def test_invalid_graphs_are_rejected(renderer):
                 [Link((1, 0), (2, 0)), Link((2, 0), (1, 0)), Link((2, 0), (3, 0)), Link((3, 0), (4, 0))])
     with pytest.raises(SyfrackError):
         renderer.compile(cyc)
+
+
+def _c3_extent(kind, value):
+    if kind == "mandelbox":  # negative scales fill the cube [-2, 2]^3; positive ones reach 2(s+1)/(s-1)
+        return 4.0 if value <= 1.0 else min(2.0 * (value + 1.0) / (value - 1.0), 12.0) * 1.2
+    return 1.6
+
+
+C3_FORMS = ([("mandelbulb", float(p)) for p in range(2, 13)] +
+            [("mandelbox", s) for s in (-2.5, -2.0, -1.5, -1.05, -0.8, -0.3, 0.0, 0.4, 0.9, 1.05, 1.5, 2.0, 2.5)] +
+            [("menger", lv) for lv in range(3, 8)])
+
+
+@pytest.mark.parametrize("kind,value", C3_FORMS, ids=[f"{k}-{v:g}" for k, v in C3_FORMS])
+def test_mixed_batch_forms_against_oracle(renderer, oracle_mod, kind, value):
+    """Every form the uneven batch draws (Mandelbulb powers 2-12, including the
+    binary-exponentiation powers of eval.rs:157-177; Mandelbox scales across -2.5..2.5,
+    |s| < 1.05 included; Menger levels 3-7) on the device against the f32 and f64
+    oracle: the gpu_de.rs rule, and against f32 99% of relative errors below 1e-5
+    with at least 99.5% of iteration counts equal."""
+    from syfrack_gb300 import workloads
+
+    if kind == "mandelbulb":
+        g = workloads.mixed_batch_graph("mandelbulb", value)
+    elif kind == "mandelbox":
+        g = workloads.mixed_batch_graph("mandelbox", value)
+    else:
+        g = workloads.mixed_batch_graph("menger", int(value))
+    pts = lcg_points(4096, _c3_extent(kind, value), 29)
+    cg = renderer.compile(g)
+    assert cg.info()["form"] == {"mandelbulb": "bulb", "mandelbox": "box", "menger": "menger"}[kind]
+    gpu = cg.probe(pts)
+    og = oracle_mod.OracleGraph(g)
+    ref32, ref64 = og.de(pts, precision=32), og.de(pts, precision=64)
+    assert gpu_de_rule(gpu, ref64) <= 0.005
+    assert gpu_de_rule(gpu, ref32) <= 0.005
+    rel = np.abs(gpu["distance"] - ref32["distance"]) / np.maximum(np.abs(ref32["distance"]), 1.0)
+    assert np.quantile(rel, 0.99) < 1e-5, np.quantile(rel, 0.99)
+    assert (gpu["iterations"] == ref32["iterations"]).mean() >= 0.995
