@@ -1,15 +1,22 @@
 """Benchmark of the DE path on GB300: DE-traced Mrays/s of the Mandelbox
-wavefront path trace (1280x720, 64 spp, 4 bounces, 512 steps).
+wavefront path trace (1280x720, 64 spp, 4 bounces, 512 steps, hit epsilon 1e-4).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
 A step is one progressive pass of 8 samples per pixel over the whole frame
-(7,372,800 paths); the default K = 8 covers the full 64-spp image. `value` is
-device-timed (CUDA events on the library stream, max over ranks); `e2e` is the
-same metric through the public API with host buffers: a full render via
-Renderer.render (scene and graph uploaded from the host, film read back).
-With N > 1 (torchrun) every rank renders its own replica (the path has no
-exchange step; see the scaling note in the JSON line).
+(7,372,800 paths). `value` is device-timed (CUDA events on the library stream,
+max over ranks); `e2e` is the same metric through the public API with host
+buffers: one full 64-spp frame via Renderer.render (scene and graph uploaded
+from the host, film read back). With N > 1 (torchrun) every rank renders its
+own replica (the path has no exchange step).
+
+At N = 1 the same line also carries the other configurations, measured in the
+same run: `c2_cone_rule` (the headline frame with the reference's cone-relative
+hit test), `c1` (Mandelbulb primary rays), `c3` (the uneven 64-job batch against
+plain launches), `c4` (the 3840x2160 deep zoom with its agreement against
+binary128 and FP64) and `c5` (the 200 req/s serving stream against sequential
+plain launches, and both capacities); --no-extras leaves them out. The other
+workloads also run alone with --workload.
 """
 from __future__ import annotations
 
@@ -231,12 +238,25 @@ def run_ours(args):
     per_launch_flops = flops / trace_launches
     avg_launch_s = trace_ms * 1e-3 / trace_launches
     achieved = per_launch_flops / avg_launch_s / 1e12 if avg_launch_s > 0 else 0.0
+    # after the timed region: one more step on the diagnostic trace kernel, which counts
+    # warp-level DE calls and iteration slots (lane use), on a separate session
+    ctx.set_profiling(True, lane_stats=True)
+    ctx.reset_stats()
+    lane_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=SPP_PER_STEP,
+                                                    samples_per_dispatch=SPP_PER_STEP)
+    lane_sess = RenderSession(renderer, scene, lane_cfg)
+    lane_sess.set_launch(args.min_blocks, args.quantum, args.regen)
+    lane_sess.dispatch(tile + (0,), SPP_PER_STEP)
+    lane_sess.sync(600000)
+    lst = ctx.stats()
+    lane_sess.close()
     ctx.set_profiling(False)
     sess.close()
 
-    # end to end through the public API: a full 64-spp render from host descriptions
-    e2e_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height,
-                                                   spp=SPP_PER_STEP * args.steps, samples_per_dispatch=SPP_PER_STEP)
+    # end to end through the public API: one full 64-spp frame (8 dispatches of 8 spp)
+    # rendered from host descriptions, film read back
+    e2e_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=64,
+                                                   samples_per_dispatch=SPP_PER_STEP)
     ctx.reset_stats()
     if dist:
         dist.barrier()
@@ -250,8 +270,12 @@ def run_ours(args):
         e2e_s, e2e_segs = reduce_ranks(dist, e2e_s, e2e_segs, "cuda")
     e2e = e2e_segs / e2e_s / 1e6
     px = e2e_cfg.width * e2e_cfg.height
+    e2e_steps = e2e_cfg.samples_per_pixel // SPP_PER_STEP
     d2h = px * (16 + 4 + 16)
     h2d = C.sizeof(__import__("syfrack_gb300").abi.sf_scene_desc) + 4096
+    cone = None
+    if n_ranks == 1 and not args.no_extras:
+        cone = pathtrace_variant(renderer, ctx, scene, args, "cone")
 
     if rank == 0:
         cpu = None
@@ -265,6 +289,7 @@ def run_ours(args):
             "data": "synthetic (seeded Mandelbox scene; no dataset)",
             "config": {"workload": WORKLOAD if (cfg.width, cfg.height) == (1280, 720) else f"profiling case {cfg.width}x{cfg.height}",
                        "width": cfg.width, "height": cfg.height, "spp_per_step": SPP_PER_STEP,
+                       "hit_rule": f"fixed epsilon {cfg.hit_epsilon:g} (radius <= epsilon)",
                        "paths_per_step": cfg.width * cfg.height * SPP_PER_STEP, "max_bounces": cfg.max_bounces,
                        "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
                        "launch": {"min_blocks_per_sm": args.min_blocks, "quantum": args.quantum,
@@ -273,8 +298,10 @@ def run_ours(args):
                        "segments_per_step": segs_all / args.steps,
                        "pixel_samples_per_s": cfg.width * cfg.height * SPP_PER_STEP * args.steps * n_ranks
                        / (ms_max * 1e-3)},
-            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // args.steps,
-                    "d2h_bytes_per_step": d2h // args.steps, "call": "Renderer.render (full 64-spp frame)"},
+            "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
+                    "d2h_bytes_per_step": d2h // e2e_steps,
+                    "call": "Renderer.render: one full 64-spp frame (8 dispatches of 8 spp), film read back; "
+                            "bytes per 8-spp step"},
             "roofline": {"bound": "fp32", "kernel": "k_trace", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
                          "traffic": profiled_traffic() if (cfg.width, cfg.height) == (1280, 720) else None,
@@ -283,22 +310,103 @@ def run_ours(args):
                          "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
                          "de_evals_per_step": st["de_evals"] / args.steps,
                          "de_iterations_per_step": st["de_iterations"] / args.steps,
-                         "simt_lane_efficiency": st["de_evals"] / max(32 * st["warp_de_calls"], 1),
-                         "iterate_lane_efficiency": st["de_iterations"] / max(st["iteration_slots"], 1)},
+                         "simt_lane_efficiency": lst["de_evals"] / max(32 * lst["warp_de_calls"], 1),
+                         "iterate_lane_efficiency": lst["de_iterations"] / max(lst["iteration_slots"], 1),
+                         "lane_efficiency_source": "one further 8-spp step on the diagnostic trace kernel"},
             "gpu_launches": st["launches"],
             "status_word": status,
             "clocks": clocks.summary(),
             "cpu_baseline": cpu,
         }
+        if cone is not None:
+            line["c2_cone_rule"] = cone
+    if n_ranks == 1 and not args.no_extras:
+        renderer = None
+        ctx.close()
+        ctx = None
+        line.update(extras(args))
+    if rank == 0:
         print(json.dumps(line), flush=True)
     if dist:
         dist.barrier()
         dist.destroy_process_group()
     renderer = None
-    ctx.close()
+    if ctx is not None:
+        ctx.close()
 
 
-def run_batch(args):
+def pathtrace_variant(renderer, ctx, scene, args, rule, steps=5, warmup=2):
+    """The headline frame with another hit rule ("cone": the reference's
+    cone-relative test at pixel tolerance 1), device-timed like the headline."""
+    from syfrack_gb300 import RenderSession, workloads
+
+    cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height,
+                                               spp=SPP_PER_STEP * (steps + warmup),
+                                               samples_per_dispatch=SPP_PER_STEP, rule=rule)
+    sess = RenderSession(renderer, scene, cfg)
+    sess.set_launch(args.min_blocks, args.quantum, args.regen)
+    for k in range(warmup):
+        sess.dispatch((0, 0, cfg.width, cfg.height, k * SPP_PER_STEP), SPP_PER_STEP)
+    sess.sync(600000)
+    ctx.reset_stats()
+    import torch
+
+    stream = torch.cuda.ExternalStream(ctx.stream)
+    ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
+    ev0.record(stream)
+    for k in range(warmup, warmup + steps):
+        sess.dispatch((0, 0, cfg.width, cfg.height, k * SPP_PER_STEP), SPP_PER_STEP)
+    ev1.record(stream)
+    ev1.synchronize()
+    ms = ev0.elapsed_time(ev1)
+    st = ctx.stats()
+    sess.close()
+    return {"value": st["segments"] / (ms * 1e-3) / 1e6, "unit": UNIT, "ms_per_step": ms / steps, "steps": steps,
+            "de_evals_per_segment": st["de_evals"] / max(st["segments"], 1),
+            "hit_rule": "cone-relative radius / t < pixel_cone (the reference's rule, pixel tolerance 1)"}
+
+
+def extras(args):
+    """The other configurations, measured in the same run (one GPU): primary rays,
+    the uneven batch, the deep zoom and the serving stream, each summarised."""
+    base = dict(vars(args))
+
+    def ns(**kw):
+        d = dict(base)
+        d.update(kw)
+        return argparse.Namespace(**d)
+
+    out = {}
+    t0 = time.perf_counter()
+    p = measure_primary(ns(steps=10, warmup=3))
+    out["c1"] = {"workload": p["workload"], "value": p["value"], "unit": p["unit"],
+                 "launch_ms": p["frames"]["256x256"]["launch_ms"], "e2e": p["e2e"],
+                 "frame_2048x2048_mrays_per_s": p["frames"]["2048x2048"]["mrays_per_s"],
+                 "cpu_baseline": p["cpu_baseline"]}
+    b = measure_batch(ns(steps=3, jobs=64))
+    out["c3"] = {"workload": b["workload"], "unit": UNIT, "batched": b["value"],
+                 "batched_steady_replays": b["value_steady_replays"], "plain_megakernel": b["plain_megakernel"],
+                 "plain_wavefront_sessions": b["plain_wavefront_sessions"],
+                 "speedup_vs_plain_megakernel": b["value"] / b["plain_megakernel"],
+                 "speedup_vs_plain_wavefront": b["value"] / b["plain_wavefront_sessions"],
+                 "autotuned": b["autotuned"], "paths_per_pass": b["paths_per_pass"], "seconds": b["seconds"]}
+    d = measure_deepzoom(ns(steps=3, warmup=3, frame=None))
+    out["c4"] = {k: d[k] for k in ("workload", "value", "unit", "kernel_ms_per_frame", "orbit", "orbit_kernel_ms",
+                                   "e2e", "host_orbit_variant", "agreement", "cpu_baseline") if k in d}
+    sv = measure_serve(ns())
+    summ = lambda r: {"p50_ms": r["latency"]["all"].get("p50_ms"), "p99_ms": r["latency"]["all"].get("p99_ms"),
+                      "throughput_rps": r["throughput_rps"], "mrays_per_s": r["mrays_per_s"]}
+    out["c5"] = {"workload": sv["workload"], "requests": sv["requests"],
+                 "served": {**summ(sv["served"]), "mean_batch_requests": sv["served"]["mean_batch_requests"],
+                            "per_kind_p99_ms": {k: sv["served"]["latency"][k].get("p99_ms")
+                                                for k in ("tile", "preview", "refine")}},
+                 "plain_sequential": summ(sv["plain_sequential"]), "capacity": sv["capacity"],
+                 "throughput_ratio": sv["throughput_ratio"]}
+    out["extras_seconds"] = time.perf_counter() - t0
+    return out
+
+
+def measure_batch(args):
     """Uneven mixed batch: 64 seeded jobs (Mandelbulb powers 2-12, Mandelbox scales
     -2.5..2.5, Menger levels 3-7; tiles 64-512 px; 1-16 spp; 2 bounces). Rendered
     (a) job after job by the per-pixel megakernel (the reference's plain path),
@@ -355,8 +463,8 @@ def run_batch(args):
             "autotuned": {"min_blocks_per_sm": mb, "quantum": q, "regen": rg}, "segments_per_pass": segs,
             "paths_per_pass": int(sum(c.width * c.height * c.samples_per_pixel for _, c in jobs)),
             "dtype": "f32", "data": "synthetic (seeded jobs)"}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
 def _percentiles(xs):
@@ -484,7 +592,7 @@ def plain_replay(renderer, ctx, events, cap_s):
             "mrays_per_s": segs / span_s / 1e6}
 
 
-def run_serve(args):
+def measure_serve(args):
     """Serving stream: Poisson arrivals at --rate req/s for --duration s (seeded):
     40% 2D tiles (Julia c = 0.7885 e^{ia} or a Burning Ship view; side 256-2048;
     1k-20k iterations), 40% previews (480x270, 1 spp, 1 bounce, a random orbit of a
@@ -522,11 +630,11 @@ def run_serve(args):
                        "host_result_gb": args.host_result_gb, "seed": args.seed,
                        "preview": workloads.SERVE_PREVIEW, "refine_spp": workloads.SERVE_REFINE_SPP},
             "dtype": "f32", "data": "synthetic (seeded Poisson stream)"}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
-def run_primary(args):
+def measure_primary(args):
     """Plain Mandelbulb primary rays: 256x256, power 8, 12 iterations, bailout 2.0,
     pinhole at (0,0,-3) looking at the origin, 60 degree FOV, 256 steps, epsilon 1e-4,
     far 10; hit t, step count and central-difference normal per pixel. Device time
@@ -584,8 +692,8 @@ def run_primary(args):
             "cpu_baseline": {"value": W * H / cpu_s / 1e6, "unit": "Mrays/s", "cores": threads, "kind": "port",
                              "sample": f"the whole {W}x{H} frame, FP32"},
             "dtype": "f32", "data": "synthetic (the C1 view)"}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
 def frame_size(args, w, h):
@@ -596,7 +704,7 @@ def frame_size(args, w, h):
     return int(fw), int(fh)
 
 
-def run_tile(args):
+def measure_tile(args):
     """The largest 2D tile of the serving mix through the plain call sf_escape2d:
     Burning Ship, 2048x2048, 20,000 iterations, every trap (ring, stripe bands,
     final angle), the canvas around the ship (centre (-0.45, -0.5), zoom 1.8) at
@@ -657,19 +765,22 @@ def run_tile(args):
         dt = time.perf_counter() - t0
         line["cpu_baseline"] = {"value": float(ref["iterations"].sum()) / dt / 1e9, "unit": "Giter/s",
                                 "cores": threads, "kind": "port", "sample": f"{len(idx)} seeded pixels of the tile, FP32"}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
-def run_deepzoom(args):
+def measure_deepzoom(args):
     """Mandelbrot deep zoom: 3840x2160, max 50,000 iterations, width 1e-12 around a
     seeded boundary point (FP64 bisection of the escape label along a random ray from
     c = 0). FP64 reference orbit on the GPU, FP32 perturbation with rebasing. Reports
     the perturbation's Giter/s (kernel time from CUDA events), the frame time through
-    the public call (host outputs), agreement of iteration counts with full-FP64
-    direct iteration on the GPU over every pixel, smooth-colouring error against it,
-    and, on a seeded 4096-pixel sample, agreement with the oracle's binary128
-    iteration (the truth) and FP64 iteration, timed as the CPU baseline."""
+    the public call (host outputs) with the orbit on the GPU and, beside it, on a host
+    core; agreement of iteration counts with full-FP64 direct iteration on the GPU over
+    every pixel; smooth-colouring error against it; and on a seeded 4096-pixel sample,
+    agreement with the oracle's binary128 iteration (the truth) for the perturbation
+    with the FP64 orbit, with the oracle's binary128 orbit (the decomposition: orbit
+    error against FP32-delta error) and for FP64 direct iteration, the sample timed as
+    the CPU baseline."""
     import numpy as np
 
     from syfrack_gb300 import GpuContext, deep_zoom, workloads
@@ -680,33 +791,41 @@ def run_deepzoom(args):
     c = workloads.deep_zoom_center(seed=2026, max_iter=MI)
     for _ in range(max(args.warmup, 3)):
         deep_zoom(ctx, c, (0.0, 0.0), width, min(W, 960), min(H, 540), MI, bailout=16.0)
-    ctx.set_profiling(True)
-    walls, kms, iters = [], [], []
-    out = None
-    for _ in range(args.steps):
-        ctx.reset_stats()
-        t0 = time.perf_counter()
-        out = deep_zoom(ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0)
-        walls.append(time.perf_counter() - t0)
-        st = ctx.stats()
-        kms.append(st["trace_ms"])
-        iters.append(st["de_iterations"])
-    ctx.set_profiling(False)
+
+    def frames(orbit):
+        ctx.set_profiling(True)
+        walls, kms, oms, iters, out = [], [], [], [], None
+        for _ in range(args.steps):
+            ctx.reset_stats()
+            t0 = time.perf_counter()
+            out = deep_zoom(ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, orbit=orbit)
+            walls.append(time.perf_counter() - t0)
+            st = ctx.stats()
+            kms.append(st["trace_ms"])
+            oms.append(st["kernel_ms"] - st["trace_ms"])
+            iters.append(st["de_iterations"])
+        ctx.set_profiling(False)
+        return out, float(np.median(iters)), float(np.median(kms)), float(np.median(oms)), float(np.median(walls))
+
+    out, iters_per_frame, kernel_ms, orbit_ms, wall = frames("device")
+    out_h, _, kernel_ms_h, _, wall_h = frames("host")
     full = deep_zoom(ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, reference_f64=True)
     it, it64 = full["iterations"].ravel(), full["iterations_f64"].ravel()
     agree64 = float((it == it64).mean())
     near64 = float((np.abs(it.astype(np.int64) - it64.astype(np.int64)) <= 1).mean())
     both = (it == it64) & (it < MI)
     smooth_err = np.abs(full["smooth"].ravel()[both] - full["smooth_f64"].ravel()[both])
-    iters_per_frame = float(np.median(iters))
-    kernel_ms = float(np.median(kms))
     line = {"metric": "deep-zoom perturbation Giter/s", "unit": "Giter/s",
             "value": iters_per_frame / (kernel_ms * 1e-3) / 1e9, "higher_is_better": True,
             "workload": f"mandelbrot_deep_zoom_{W}x{H}_50k_iter_width1e-12", "steps": args.steps,
             "center": list(c), "kernel_ms_per_frame": kernel_ms, "iterations_per_frame": iters_per_frame,
-            "e2e": {"value": iters_per_frame / float(np.median(walls)) / 1e9, "unit": "Giter/s",
-                    "frame_ms": float(np.median(walls)) * 1e3, "h2d_bytes_per_step": 0,
-                    "d2h_bytes_per_step": W * H * 8, "call": "deep_zoom (sf_deep_zoom)"},
+            "orbit": "FP64 on the GPU (k_ref_orbit, one thread)", "orbit_kernel_ms": orbit_ms,
+            "e2e": {"value": iters_per_frame / wall / 1e9, "unit": "Giter/s", "frame_ms": wall * 1e3,
+                    "h2d_bytes_per_step": 0, "d2h_bytes_per_step": W * H * 8, "call": "deep_zoom (sf_deep_zoom)"},
+            "host_orbit_variant": {"e2e_giter_per_s": iters_per_frame / wall_h / 1e9, "frame_ms": wall_h * 1e3,
+                                   "kernel_ms_per_frame": kernel_ms_h,
+                                   "same_counts_as_device_orbit": bool(np.array_equal(out["iterations"],
+                                                                                      out_h["iterations"]))},
             "rebases_per_frame": out["rebases"],
             "agreement": {"perturbation_vs_fp64_direct_all_pixels": agree64,
                           "perturbation_vs_fp64_direct_within_1": near64,
@@ -715,9 +834,8 @@ def run_deepzoom(args):
                               "max": float(smooth_err.max()) if smooth_err.size else None}},
             "dtype": "f32 deltas, f64 reference orbit", "data": "synthetic (seeded boundary point)"}
     if args.no_cpu_baseline:
-        print(json.dumps(line), flush=True)
         ctx.close()
-        return
+        return line
     # truth: binary128 on a seeded sample (oracle, all host cores), timed as the CPU baseline
     sys.path.insert(0, os.path.join(ROOT, "oracle"))
     import oracle  # the CPU restatement; the baseline here, and the truth for the counts
@@ -736,19 +854,25 @@ def run_deepzoom(args):
     t0 = time.perf_counter()
     cpu64, _ = oracle.mandel_escape(np.array(c), np.zeros(2), off, MI, 16.0, precision=64, threads=threads)
     t64 = time.perf_counter() - t0
+    # the decomposition: the same frame on the oracle's binary128 orbit (as hi/lo float pairs)
+    q = deep_zoom(ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, orbit="given",
+                  given_orbit=oracle.mandel_orbit(c, MI, 16.0, precision=128))["iterations"].ravel()
+    match = lambda a: float((a[idx] == truth).mean()) if len(a) == W * H else float((a == truth).mean())
     line["agreement"].update({
         "sample_pixels": len(idx),
-        "perturbation_vs_binary128": float((it[idx] == truth).mean()),
+        "perturbation_vs_binary128": match(it),
         "perturbation_vs_binary128_within_1": float(
             (np.abs(it[idx].astype(np.int64) - truth.astype(np.int64)) <= 1).mean()),
-        "fp64_direct_gpu_vs_binary128": float((it64[idx] == truth).mean()),
-        "fp64_direct_cpu_vs_binary128": float((cpu64 == truth).mean())})
+        "perturbation_binary128_orbit_vs_binary128": match(q),
+        "fp64_direct_gpu_vs_binary128": match(it64),
+        "fp64_direct_cpu_vs_binary128": match(cpu64),
+        "sample_interior_fraction": float((truth == MI).mean())})
     line["cpu_baseline"] = {"value": float(np.sum(np.minimum(cpu64, MI))) / t64 / 1e9, "unit": "Giter/s",
                             "cores": threads, "kind": "port",
                             "sample": f"{len(idx)} seeded pixels, FP64 direct iteration "
                                       f"({t64:.2f} s; binary128 on the same pixels {t128:.2f} s)"}
-    print(json.dumps(line), flush=True)
     ctx.close()
+    return line
 
 
 def main():
@@ -765,6 +889,8 @@ def main():
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--no-extras", action="store_true",
+                    help="the headline only (without the other configurations' summaries)")
     ap.add_argument("--workload", default="pathtrace",
                     choices=["pathtrace", "batch", "serve", "primary", "deepzoom", "tile"])
     ap.add_argument("--frame", default=None, help="WxH override of the deepzoom/tile frame (profiling only)")
@@ -778,18 +904,12 @@ def main():
     ap.add_argument("--seed", type=int, default=5)
     ap.add_argument("--burst", type=int, default=3000, help="requests queued at once for the capacity measure")
     args = ap.parse_args()
+    measures = {"batch": measure_batch, "serve": measure_serve, "primary": measure_primary,
+                "deepzoom": measure_deepzoom, "tile": measure_tile}
     if args.impl == "reference":
         run_reference(args)
-    elif args.workload == "batch":
-        run_batch(args)
-    elif args.workload == "serve":
-        run_serve(args)
-    elif args.workload == "primary":
-        run_primary(args)
-    elif args.workload == "deepzoom":
-        run_deepzoom(args)
-    elif args.workload == "tile":
-        run_tile(args)
+    elif args.workload in measures:
+        print(json.dumps(measures[args.workload](args)), flush=True)
     else:
         run_ours(args)
 

@@ -313,7 +313,10 @@ typedef struct sf_stats {
     uint64_t warp_de_calls;    /* warp-level DE invocations of the trace kernel */
     uint64_t iteration_slots;  /* per invocation: warp max iterations x active lanes */
 } sf_stats;
-/* Per-kernel CUDA-event timing on the context stream (off by default). */
+/* Per-kernel CUDA-event timing on the context stream (off by default): 0 off, 1 on,
+ * 2 on and the trace kernel also counts warp_de_calls and iteration_slots (a
+ * diagnostic instantiation that pays a warp reduction per DE call; with 0 or 1 those
+ * two counters stay unchanged). */
 sf_status sf_context_set_profiling(sf_context* ctx, int enable);
 sf_status sf_context_stats(sf_context* ctx, sf_stats* out);
 sf_status sf_context_reset_stats(sf_context* ctx);
@@ -486,16 +489,30 @@ sf_status sf_escape2d(sf_context* ctx, const sf_planar_desc* f, const sf_canvas*
                       uint32_t sample, float* distance, float* traps, uint32_t* iterations);
 
 /* Deep zoom (no counterpart in the reference, which caps zoom at 1e4): Mandelbrot
- * z <- z^2 + c around centre (hi + lo), pixel pitch = width_units / image width.
- * FP64 reference orbit on the GPU, FP32 perturbation deltas with rebasing.
+ * z <- z^2 + c around the double-double centre hi + lo, pixel pitch = width_units /
+ * image width. The reference orbit is that of c_ref = hi; each pixel's FP32 offset
+ * from it is lo + its position times the pitch, so lo keeps the centre's digits
+ * below an FP64 ulp of hi. FP32 perturbation deltas with rebasing.
  * Outputs per pixel: iteration count (first n with |z_n| > bailout, else max_iter)
  * and smooth value n + 1 - log2(ln|z_n|). reference_f64 != 0 also runs the
- * full-FP64 direct iteration into iters_f64/smooth_f64 (may be NULL otherwise). */
+ * full-FP64 direct iteration at c = hi + (lo + offset) into iters_f64/smooth_f64
+ * (may be NULL otherwise).
+ * orbit_mode (ABI 1.2) says where the reference orbit Z_n of c_ref comes from:
+ * SF_ORBIT_DEVICE (0), FP64 on the GPU (one thread); SF_ORBIT_HOST (1), FP64 on a
+ * host core, uploaded (the same unfused operations: the same orbit to the last
+ * bit); SF_ORBIT_GIVEN (2), the caller's orbit: orbit_len entries of four floats
+ * (Re hi, Im hi, Re lo, Im lo) with Z_n = hi + lo, from Z_0 = 0 through the last
+ * entry the perturbation may use (its escape or max_iter), 1 <= orbit_len <=
+ * max_iter + 1 -- a diagnostic that lets an orbit of higher precision stand in. */
+enum { SF_ORBIT_DEVICE = 0, SF_ORBIT_HOST = 1, SF_ORBIT_GIVEN = 2 };
 typedef struct sf_deep_zoom_desc {
     double center_hi[2], center_lo[2];
     double width_units;
     uint32_t width, height, max_iter;
     float bailout;
+    uint32_t orbit_mode;
+    uint32_t orbit_len;
+    const float* orbit;
 } sf_deep_zoom_desc;
 sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth,
                        int reference_f64, uint32_t* iters_f64, float* smooth_f64, uint64_t* rebases);
@@ -513,7 +530,8 @@ sf_status sf_deep_zoom(sf_context* ctx, const sf_deep_zoom_desc* d, uint32_t* it
  * is looked up once per device and kept for the life of the process: after
  * cudaDeviceReset (or anything else that re-creates the device's primary context)
  * the kept address is stale, so do not call this entry point again in that process.
- * Frames hold at most 2^31 pixels (SF_ERR_INVALID beyond), as for sf_deep_zoom. */
+ * Frames hold at most 2^31 pixels (SF_ERR_INVALID beyond), as for sf_deep_zoom. The
+ * orbit is always computed on the device here (orbit_mode must be SF_ORBIT_DEVICE). */
 sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* iterations, float* smooth, void* stream);
 
 /* ------------------------------------------------------------------ serving

@@ -78,6 +78,9 @@ def lib():
         L.or_planar.argtypes = [C.c_int, C.POINTER(PlanarParams), dp, C.c_size_t, dp, dp, up, C.c_int]
         L.or_mandel_escape.argtypes = [C.c_int, dp, dp, dp, C.c_size_t, C.c_uint32, C.c_double, up, dp,
                                        C.c_int]
+        L.or_mandel_orbit.restype = C.c_uint32
+        L.or_mandel_orbit.argtypes = [C.c_int, C.c_double, C.c_double, C.c_uint32, C.c_double,
+                                      C.POINTER(C.c_float)]
         L.or_mandel_escapes.restype = C.c_int
         L.or_mandel_escapes.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_uint32]
@@ -216,3 +219,12 @@ def mandel_escape(center_hi, center_lo, offsets, max_iter, bailout=2.0, precisio
     lib().or_mandel_escape(precision, _dp(hi), _dp(lo), _dp(off), n, max_iter, bailout, _up(iters),
                            _dp(mag2), threads or default_threads())
     return iters, mag2
+
+
+def mandel_orbit(c_ref, max_iter, bailout=2.0, precision=128):
+    """Reference orbit of c_ref as (n, 4) float32 rows (Re hi, Im hi, Re lo, Im lo),
+    computed in binary128 (or binary64), through its escape or max_iter."""
+    out = np.zeros((max_iter + 1, 4), np.float32)
+    n = lib().or_mandel_orbit(precision, float(c_ref[0]), float(c_ref[1]), max_iter, bailout,
+                              out.ctypes.data_as(C.POINTER(C.c_float)))
+    return out[:n].copy()

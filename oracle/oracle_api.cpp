@@ -240,6 +240,34 @@ void or_planar(int precision, const PlanarParams* f, const double* xy, size_t n,
 // c = center + offset, with center given as a double-double (hi + lo) and the
 // offsets as doubles. precision 64: double; 128: IEEE binary128 (the deep-zoom
 // truth). Also returns |z|^2 at escape (as double) for smooth colouring.
+// Reference orbit Z_0 = 0, Z_(n+1) = Z_n^2 + c_ref of c_ref = (cx, cy) in binary128
+// (precision 128) or binary64, through the first n with |Z_n| > bailout or n = max_iter,
+// as the perturbation kernel reads it: four floats per entry (Re hi, Im hi, Re lo,
+// Im lo) with hi = float(Z_n) and lo = float(Z_n - hi). Returns the entry count.
+uint32_t or_mandel_orbit(int precision, double cx, double cy, uint32_t max_iter, double bailout, float* out) {
+    auto run = [&](auto zero) {
+        using T = decltype(zero);
+        const T x0 = T(cx), y0 = T(cy), b2 = T(bailout) * T(bailout);
+        T zx = 0, zy = 0;
+        uint32_t n = 0;
+        for (;;) {
+            const float hx = float(zx), hy = float(zy);
+            out[4 * n] = hx;
+            out[4 * n + 1] = hy;
+            out[4 * n + 2] = float(zx - T(hx));
+            out[4 * n + 3] = float(zy - T(hy));
+            const T x2 = zx * zx, y2 = zy * zy;
+            if (n >= max_iter || x2 + y2 > b2) break;
+            const T nx = (x2 - y2) + x0;
+            zy = (T(2) * zx) * zy + y0;
+            zx = nx;
+            ++n;
+        }
+        return n + 1;
+    };
+    return precision == 128 ? run(real128(0)) : run(double(0));
+}
+
 void or_mandel_escape(int precision, const double* center_hi, const double* center_lo, const double* offsets,
                       size_t n, uint32_t max_iter, double bailout, uint32_t* iters, double* mag2, int threads) {
     parallel_for(n, threads, [&](size_t i) {

@@ -72,7 +72,8 @@ class sf_batch_job(C.Structure):
 
 class sf_deep_zoom_desc(C.Structure):
     _fields_ = [("center_hi", C.c_double * 2), ("center_lo", C.c_double * 2), ("width_units", C.c_double),
-                ("width", u32), ("height", u32), ("max_iter", u32), ("bailout", C.c_float)]
+                ("width", u32), ("height", u32), ("max_iter", u32), ("bailout", C.c_float),
+                ("orbit_mode", u32), ("orbit_len", u32), ("orbit", fp)]
 
 
 class sf_server_config(C.Structure):

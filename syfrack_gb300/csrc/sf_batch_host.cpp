@@ -73,7 +73,7 @@ sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, b
         RoundQueues q;
         wave_round_queues(q, a.lists, N, K, r, a.counts);
         for (uint32_t j = 0; j < Q; ++j) {
-            TraceLaunch tl;
+            TraceLaunch tl{};
             tl.q = q;
             uint32_t* qc = a.qcounts + (size_t(r) * 64 + j) * 2;
             tl.work_counter = qc;

@@ -270,12 +270,27 @@ __device__ __forceinline__ DeRaw de_bulb(const FormParams& f, float3 p) {
 }
 
 
+// (a.x * b.x, a.y * b.y) as one packed multiply (mul.rn.f32x2): each lane rounds as
+// a binary32 multiply.
+__device__ __forceinline__ float2 mul2(float ax, float ay, float bx, float by) {
+    unsigned long long ra, rb, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(ax), "f"(ay));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(bx), "f"(by));
+    asm("mul.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(rd));
+    return r;
+}
+
 // Mandelbox: Iterate{BoxFold, Trap, SphereFold, Scale, AddOrigin} -> NormFence.
 // NORM_MIN0: the bundled trap (slot 0, Norm, Minimum) kept as min |p|^2.
 // The sphere fold's fr^2 / r^2 uses the fast reciprocal division (<= 2 ulp, the
-// accuracy class WGSL allows for its own division); for r^2 >= min_radius^2 its
-// factor is max(fr^2 / r^2, 1), which covers the r^2 >= fixed_radius^2 case.
-template <bool NORM_MIN0>
+// accuracy class WGSL allows for its own division). CLAMPED (fr >= mr): the
+// reference's three cases (eval.rs:408-414) are min(fr^2/mr^2, max(fr^2/r^2, 1)),
+// two min/max instead of a compare and a select; otherwise the factor for
+// r^2 >= min_radius^2 is max(fr^2 / r^2, 1), which covers r^2 >= fixed_radius^2.
+// The factor's products with the scale and with |scale| share one packed multiply.
+template <bool NORM_MIN0, bool CLAMPED>
 __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     DeRaw s = raw_empty();
     const float3 c = p;
@@ -286,6 +301,7 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     const bool sq = f.trap_squared != 0;
     float t0 = SF_INF;
     uint32_t i = 0;
+#pragma unroll 2
     for (; i < n; ++i) {
         if (dot3(p, p) > bt) break;
         p = clamp3(p, -l, l) * 2.0f - p;
@@ -296,12 +312,13 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
             float v = sq ? r2 : trap_measure(f.trap_measure, p);
             trap_update(s, f.trap_slot, f.trap_mode, v);
         }
-        const float k = r2 < mr2 ? kmin : fmaxf(fr2 * rcp_approx(r2), 1.0f);
+        const float q = fr2 * rcp_approx(r2);
+        const float k = CLAMPED ? fminf(kmin, fmaxf(q, 1.0f)) : (r2 < mr2 ? kmin : fmaxf(q, 1.0f));
         // sphere fold, Scale and AddOrigin as one multiply-add per component
-        const float ks = k * sc;
-        const float2 pxy = fma2_scalar(p.x, p.y, ks, c.x, c.y);
-        p = mk3(pxy.x, pxy.y, fmaf(p.z, ks, c.z));
-        dr = fmaf(dr, k * asc, 1.0f);
+        const float2 kk = mul2(k, k, sc, asc);  // (k * scale, k * |scale|)
+        const float2 pxy = fma2_scalar(p.x, p.y, kk.x, c.x, c.y);
+        p = mk3(pxy.x, pxy.y, fmaf(p.z, kk.x, c.z));
+        dr = fmaf(dr, kk.y, 1.0f);
     }
     s.iter = i;
     s.d = (sqrt_fast(dot3(p, p)) - f.fence[0]) * rcp_approx(fabsf(dr));
@@ -311,8 +328,9 @@ __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     return s;
 }
 __device__ __forceinline__ DeRaw de_box(const FormParams& f, float3 p) {
-    if (f.trap_squared && f.trap_slot == 0 && f.trap_mode == SF_TRAP_MINIMUM) return de_box_t<true>(f, p);
-    return de_box_t<false>(f, p);
+    if (f.trap_squared && f.trap_slot == 0 && f.trap_mode == SF_TRAP_MINIMUM)
+        return f.fold_clamped ? de_box_t<true, true>(f, p) : de_box_t<true, false>(f, p);
+    return f.fold_clamped ? de_box_t<false, true>(f, p) : de_box_t<false, false>(f, p);
 }
 
 // Menger: Iterate{MengerFold, Trap} -> Box (graphs/menger.ron).

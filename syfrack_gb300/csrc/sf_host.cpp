@@ -597,6 +597,7 @@ void detect_form(const HostGraph& g, DeProgram& P) {
         f.min_radius2 = mr * mr;
         f.fixed_radius2 = fr * fr;
         f.fold_k_min = f.fixed_radius2 / f.min_radius2;
+        f.fold_clamped = f.fold_k_min >= 1.0f ? 1u : 0u;
         f.scale = body[3]->f[0];
         f.abs_scale = std::fabs(f.scale);
         f.fence[0] = fence->f[0];
@@ -1069,8 +1070,10 @@ extern "C" sf_status sf_context_memory(sf_context* c, uint64_t* used, uint64_t* 
 }
 extern "C" sf_status sf_context_set_profiling(sf_context* c, int enable) {
     if (!c) return fail(SF_ERR_INVALID, "null context");
+    if (enable < 0 || enable > 2) return fail(SF_ERR_INVALID, "profiling level must be 0, 1 or 2");
     collect_timing(c);
     c->profiling = enable != 0;
+    c->lane_stats = enable == 2;
     return SF_OK;
 }
 extern "C" sf_status sf_context_reset_stats(sf_context* c) {
@@ -1500,7 +1503,7 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
         RoundQueues q;
         wave_round_queues(q, s->lists, N, K, r, s->counts);
         for (uint32_t j = 0; j < Q; ++j) {
-            TraceLaunch tl;
+            TraceLaunch tl{};
             tl.q = q;
             uint32_t* qc = s->qcounts + (size_t(r) * 64 + j) * 2;
             tl.work_counter = qc;
@@ -1510,6 +1513,7 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
             tl.next_resume_count = qc + 1;
             tl.quantum = j + 1 == Q ? 0u : s->quantum;  // the last launch runs segments to completion
             tl.regen = s->regen;
+            tl.lane_stats = c->lane_stats ? 1u : 0u;
             LaunchTimer t(c, true);
             CU(sf_launch_trace(s->graph->prog.form, s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks,
                                int(s->min_blocks), st));
@@ -2039,6 +2043,9 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     if (!(d->bailout >= 2.0f)) return fail(SF_ERR_INVALID, "bailout must be at least 2");
     // the perturbation kernel indexes pixels with 32-bit counters
     if (uint64_t(d->width) * d->height > (1ull << 31)) return fail(SF_ERR_INVALID, "deep-zoom frames hold at most 2^31 pixels");
+    if (d->orbit_mode > SF_ORBIT_GIVEN) return fail(SF_ERR_INVALID, "unknown orbit_mode");
+    if (d->orbit_mode == SF_ORBIT_GIVEN && (!d->orbit || d->orbit_len < 1 || d->orbit_len > uint64_t(d->max_iter) + 1))
+        return fail(SF_ERR_INVALID, "a given orbit needs 1 to max_iter + 1 entries");
     cudaSetDevice(c->device);
     size_t n = size_t(d->width) * d->height;
     size_t M = size_t(d->max_iter) + 4;  // the orbit, two entries past its end, one spare
@@ -2056,31 +2063,50 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     float* ds = reinterpret_cast<float*>(di + n);
     uint32_t* di64 = reinterpret_cast<uint32_t*>(ds + n);
     float* ds64 = reinterpret_cast<float*>(di64 + n);
-    double cx = d->center_hi[0] + d->center_lo[0], cy = d->center_hi[1] + d->center_lo[1];
+    // the orbit of c_ref = centre hi; the centre's lo part joins every pixel's offset
+    const double cx = d->center_hi[0], cy = d->center_hi[1];
+    const float2 c_lo = make_float2(float(d->center_lo[0]), float(d->center_lo[1]));
     double pitch = d->width_units / double(d->width);
     cudaError_t e = cudaSuccess;
     unsigned long long before[SF_STAT_COUNT];
     e = cudaMemcpyAsync(before, c->d_stats, sizeof before, cudaMemcpyDeviceToHost, c->stream);
     if (e == cudaSuccess) e = cudaMemsetAsync(work, 0, 4, c->stream);
-    // the orbit on the host, uploaded from the pinned staging (lo, hi, then its length)
     const size_t planes = reference_f64 ? 4 : 2;
     std::unique_lock<std::mutex> lk(c->stage_mu);
     if (e == cudaSuccess) e = ensure_stage(c, std::max(2 * Mb + 16, n * 4 * planes));
-    if (e == cudaSuccess) {
+    if (e == cudaSuccess && d->orbit_mode == SF_ORBIT_DEVICE) {
+        LaunchTimer t(c, false);
+        e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, olo, of, olen, c->stream);
+    } else if (e == cudaSuccess) {
+        // the host's orbit, or the caller's, uploaded from the pinned staging (lo, hi, then its length)
         char* stg = static_cast<char*>(c->stage);
-        const uint32_t len = host_ref_orbit(cx, cy, d->max_iter, double(d->bailout), reinterpret_cast<float*>(stg),
-                                            reinterpret_cast<float*>(stg + Mb));
+        float* lo = reinterpret_cast<float*>(stg);
+        float* hi = reinterpret_cast<float*>(stg + Mb);
+        uint32_t len = 0;
+        if (d->orbit_mode == SF_ORBIT_HOST) {
+            len = host_ref_orbit(cx, cy, d->max_iter, double(d->bailout), lo, hi);
+        } else {
+            len = d->orbit_len;
+            for (uint32_t k = 0; k < len + 2; ++k) {  // two copies of the last entry past the end
+                const float* z = d->orbit + 4 * size_t(std::min(k, len - 1));
+                hi[2 * k] = z[0];
+                hi[2 * k + 1] = z[1];
+                lo[2 * k] = z[2];
+                lo[2 * k + 1] = z[3];
+            }
+        }
         std::memcpy(stg + 2 * Mb, &len, 4);
         e = cudaMemcpyAsync(olo, stg, 2 * Mb + 4, cudaMemcpyHostToDevice, c->stream);
     }
     if (e == cudaSuccess) {
         LaunchTimer t(c, true);
-        e = sf_launch_perturb(olo, of, olen, d->width, d->height, float(pitch), d->max_iter, d->bailout, di, ds,
+        e = sf_launch_perturb(olo, of, olen, d->width, d->height, float(pitch), c_lo, d->max_iter, d->bailout, di, ds,
                               c->d_stats, work, c->stream);
     }
     if (e == cudaSuccess && reference_f64) {
         LaunchTimer t(c, false);
-        e = sf_launch_direct_f64(cx, cy, d->width, d->height, pitch, d->max_iter, d->bailout, di64, ds64, c->stream);
+        e = sf_launch_direct_f64(cx, cy, d->center_lo[0], d->center_lo[1], d->width, d->height, pitch, d->max_iter,
+                                 d->bailout, di64, ds64, c->stream);
     }
     // the output planes are contiguous from di: one copy into the pinned staging (after
     // the orbit's upload from it, in stream order), then host threads split it into the

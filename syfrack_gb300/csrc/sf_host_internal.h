@@ -63,6 +63,7 @@ struct sf_context {
     std::string device_name;
     int cc_major = 0, cc_minor = 0, sm_count = 0;
     bool profiling = false;
+    bool lane_stats = false;  // the trace kernel's per-call lane statistics (a slower instantiation)
     struct Timed { cudaEvent_t a, b; bool trace; };
     std::vector<Timed> timed;
     std::vector<cudaEvent_t> spare;

@@ -393,8 +393,8 @@ static __device__ __forceinline__ float add3(float hi, float lo, float d, float 
 
 __global__ void __launch_bounds__(256, 4) k_perturb(const float2* __restrict__ orbit_lo, const float2* __restrict__ orbit,
                                                  const uint32_t* __restrict__ orbit_len,
-                                                 uint32_t width, uint32_t height, float pitch, uint32_t max_iter,
-                                                 float bailout, uint32_t* iters, float* smooth,
+                                                 uint32_t width, uint32_t height, float pitch, float2 c_lo,
+                                                 uint32_t max_iter, float bailout, uint32_t* iters, float* smooth,
                                                  unsigned long long* stats, uint32_t* work) {
     const uint32_t M = *orbit_len;
     const uint32_t N = width * height;
@@ -413,8 +413,9 @@ __global__ void __launch_bounds__(256, 4) k_perturb(const float2* __restrict__ o
             if (got < N) {
                 pix = got;
                 uint32_t px = pix % width, py = pix / width;
-                dcx = (float(px) - float(width) * 0.5f + 0.5f) * pitch;
-                dcy = (float(height) * 0.5f - float(py) - 0.5f) * pitch;
+                // offset from c_ref = centre hi: the centre's lo part plus the pixel's position
+                dcx = __fadd_rn(c_lo.x, (float(px) - float(width) * 0.5f + 0.5f) * pitch);
+                dcy = __fadd_rn(c_lo.y, (float(height) * 0.5f - float(py) - 0.5f) * pitch);
                 dx = dy = mag = 0.0f;
                 m = base = 0;
                 stop = min(max_iter, M - 1);
@@ -479,16 +480,17 @@ __global__ void __launch_bounds__(256, 4) k_perturb(const float2* __restrict__ o
     warp_stat(&stats[SF_STAT_STEPS], rebases);
 }
 
-// Full-FP64 direct iteration at the same pixel offsets (validation of the
-// perturbation result; weak FP64 rate on this part).
-__global__ void __launch_bounds__(256) k_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch,
-                                                    uint32_t max_iter, double bailout, uint32_t* iters, float* smooth) {
+// Full-FP64 direct iteration at the same pixel offsets, c = hi + (lo + offset)
+// (validation of the perturbation result; weak FP64 rate on this part).
+__global__ void __launch_bounds__(256) k_direct_f64(double cx, double cy, double lox, double loy, uint32_t width,
+                                                    uint32_t height, double pitch, uint32_t max_iter, double bailout,
+                                                    uint32_t* iters, float* smooth) {
     const double b2 = bailout * bailout;
     for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < width * height; i += gridDim.x * blockDim.x) {
         uint32_t px = i % width, py = i / width;
         float dcx = (float(px) - float(width) * 0.5f + 0.5f) * (float)pitch;
         float dcy = (float(height) * 0.5f - float(py) - 0.5f) * (float)pitch;
-        double c_x = cx + (double)dcx, c_y = cy + (double)dcy;
+        double c_x = cx + (lox + (double)dcx), c_y = cy + (loy + (double)dcy);
         double zx = 0.0, zy = 0.0, mag = 0.0;
         uint32_t n = 0;
         for (; n < max_iter; ++n) {
@@ -577,17 +579,20 @@ cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double 
     return cudaGetLastError();
 }
 cudaError_t sf_launch_perturb(const float2* orbit_lo, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,
-                              uint32_t height, float pitch, uint32_t max_iter, float bailout, uint32_t* iters,
-                              float* smooth, unsigned long long* stats, uint32_t* work, cudaStream_t st) {
+                              uint32_t height, float pitch, float2 c_lo, uint32_t max_iter, float bailout,
+                              uint32_t* iters, float* smooth, unsigned long long* stats, uint32_t* work,
+                              cudaStream_t st) {
     size_t n = (size_t)width * height;
-    k_perturb<<<grid_for(n, 256, 4), 256, 0, st>>>(orbit_lo, orbit_f, orbit_len, width, height, pitch, max_iter, bailout,
-                                                    iters, smooth, stats, work);
+    k_perturb<<<grid_for(n, 256, 4), 256, 0, st>>>(orbit_lo, orbit_f, orbit_len, width, height, pitch, c_lo, max_iter,
+                                                    bailout, iters, smooth, stats, work);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch, uint32_t max_iter,
-                                 double bailout, uint32_t* iters, float* smooth, cudaStream_t st) {
+cudaError_t sf_launch_direct_f64(double cx, double cy, double lox, double loy, uint32_t width, uint32_t height,
+                                 double pitch, uint32_t max_iter, double bailout, uint32_t* iters, float* smooth,
+                                 cudaStream_t st) {
     size_t n = (size_t)width * height;
-    k_direct_f64<<<grid_for(n, 256, 8), 256, 0, st>>>(cx, cy, width, height, pitch, max_iter, bailout, iters, smooth);
+    k_direct_f64<<<grid_for(n, 256, 8), 256, 0, st>>>(cx, cy, lox, loy, width, height, pitch, max_iter, bailout, iters,
+                                                       smooth);
     return cudaGetLastError();
 }
 

@@ -71,6 +71,7 @@ struct TraceLaunch {
     uint32_t* work_counter;
     uint32_t quantum;             // march steps per segment per launch (0 = unbounded)
     uint32_t regen;               // idle lanes a warp waits for before it takes new segments (1..32)
+    uint32_t lane_stats;          // 1: count warp-level DE calls and iteration slots (diagnostic kernel)
 };
 
 struct FilmPlanes {
@@ -190,11 +191,14 @@ cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint
 // orbit_f[n] = float(Z_n), orbit_lo[n] = float(Z_n - orbit_f[n]), n < *orbit_len <= max_iter + 1.
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
-// *work is the pixel counter of the launch and must be 0 when it starts.
+// *work is the pixel counter of the launch and must be 0 when it starts. c_lo: the
+// centre's part below the orbit's c_ref, added to every pixel's offset.
 cudaError_t sf_launch_perturb(const float2* orbit_lo, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,
-                              uint32_t height, float pitch, uint32_t max_iter, float bailout, uint32_t* iters,
-                              float* smooth, unsigned long long* stats, uint32_t* work, cudaStream_t st);
-cudaError_t sf_launch_direct_f64(double cx, double cy, uint32_t width, uint32_t height, double pitch, uint32_t max_iter,
-                                 double bailout, uint32_t* iters, float* smooth, cudaStream_t st);
+                              uint32_t height, float pitch, float2 c_lo, uint32_t max_iter, float bailout,
+                              uint32_t* iters, float* smooth, unsigned long long* stats, uint32_t* work,
+                              cudaStream_t st);
+cudaError_t sf_launch_direct_f64(double cx, double cy, double lox, double loy, uint32_t width, uint32_t height,
+                                 double pitch, uint32_t max_iter, double bailout, uint32_t* iters, float* smooth,
+                                 cudaStream_t st);
 int sf_device_sm_count();
 cudaError_t sf_launch_ffma_peak(float* out, uint32_t iters, int blocks, cudaStream_t st);

@@ -68,6 +68,8 @@ extern "C" sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* 
         return sf_report_error(SF_ERR_INVALID, "max_iter " + std::to_string(d->max_iter) +
                                                    " exceeds the allocation-free limit of 65536 iterations");
     if (!(d->bailout >= 2.0f)) return sf_report_error(SF_ERR_INVALID, "bailout must be at least 2");
+    if (d->orbit_mode != SF_ORBIT_DEVICE)
+        return sf_report_error(SF_ERR_INVALID, "the allocation-free deep zoom computes its orbit on the device");
     NoAllocScratch* sc = nullptr;
     sf_status s = scratch_address(&sc);
     if (s != SF_OK) return s;
@@ -76,12 +78,14 @@ extern "C" sf_status sf_deep_zoom_noalloc(const sf_deep_zoom_desc* d, uint32_t* 
     // and its length are written before they are read
     static_assert(offsetof(NoAllocScratch, stats) == offsetof(NoAllocScratch, work) + 4, "work | stats layout");
     cudaError_t e = cudaMemsetAsync(&sc->work, 0, 4 + sizeof(sc->stats), st);
-    double cx = d->center_hi[0] + d->center_lo[0], cy = d->center_hi[1] + d->center_lo[1];
+    // the orbit of c_ref = centre hi; the centre's lo part joins every pixel's offset
+    const double cx = d->center_hi[0], cy = d->center_hi[1];
+    const float2 c_lo = make_float2(float(d->center_lo[0]), float(d->center_lo[1]));
     double pitch = d->width_units / double(d->width);
     if (e == cudaSuccess) e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, sc->orbit_lo, sc->orbit_f,
                                                   &sc->orbit_len, st);
     if (e == cudaSuccess)
-        e = sf_launch_perturb(sc->orbit_lo, sc->orbit_f, &sc->orbit_len, d->width, d->height, float(pitch),
+        e = sf_launch_perturb(sc->orbit_lo, sc->orbit_f, &sc->orbit_len, d->width, d->height, float(pitch), c_lo,
                               d->max_iter, d->bailout, iterations, smooth, sc->stats, &sc->work, st);
     if (e != cudaSuccess) return sf_report_error(SF_ERR_CUDA, std::string("sf_deep_zoom_noalloc: ") + cudaGetErrorString(e));
     return SF_OK;

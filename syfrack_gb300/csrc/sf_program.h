@@ -63,6 +63,7 @@ struct FormParams {
     uint32_t power_int;  // Bulb: 0 = trigonometric path, else the integer exponent 1..16
     float limit;         // Box: fold limit
     float min_radius2, fixed_radius2, fold_k_min;  // Box: mr^2, fr^2, fr^2/mr^2
+    uint32_t fold_clamped;  // Box: fr >= mr, so the fold factor is min(fr^2/mr^2, max(fr^2/r^2, 1))
     float scale;         // Box: Scale factor; Menger: fold scale
     float abs_scale;     // Box: |scale|
     float offset[3];     // Menger: fold offset

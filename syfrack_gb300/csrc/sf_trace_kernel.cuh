@@ -46,7 +46,9 @@ static __device__ __forceinline__ uint32_t find_job(const uint32_t* begins, uint
 
 // MULTI: the work items belong to the jobs of a batch (bt); each lane reads its job's
 // program and scene (L1-cached global memory) when it takes an item.
-template <int FORM, int MIN_BLOCKS, bool MULTI = false>
+// LANE_STATS: also count warp-level DE calls and, per call, the warp's longest
+// iteration count times its active lanes (a diagnostic of SIMT lane use).
+template <int FORM, int MIN_BLOCKS, bool MULTI = false, bool LANE_STATS = false>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __restrict__ prog_g,
                                                            const DevScene* __restrict__ scene_g, PathSoA soa,
                                                            TraceLaunch tl, unsigned long long* stats,
@@ -190,7 +192,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     n_iter += s.iter;
                 }
             }
-            {
+            if constexpr (LANE_STATS) {
                 // warp-level DE calls and, per call, the iterations the warp ran (its
                 // longest lane) times its active lanes
                 const uint32_t am = __activemask();
@@ -241,13 +243,19 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     warp_stat(&stats[SF_STAT_DE_ITERS], n_iter);
     warp_stat(&stats[SF_STAT_SEGMENTS], n_seg + n_shseg);
     warp_stat(&stats[SF_STAT_SHADOW_SEGMENTS], n_shseg);
-    warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
-    warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
+    if constexpr (LANE_STATS) {
+        warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
+        warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
+    }
 }
 
 template <int FORM>
 static cudaError_t launch_trace_form(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
                                      unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
+    if (tl.lane_stats && min_blocks == 3) {
+        k_trace<FORM, 3, false, true><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats);
+        return cudaGetLastError();
+    }
     switch (min_blocks) {
     case 3: k_trace<FORM, 3><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
     case 4: k_trace<FORM, 4><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;

@@ -67,8 +67,10 @@ class GpuContext:
         check(self.lib.sf_context_memory(self.h, C.byref(used), C.byref(budget)))
         return used.value, budget.value
 
-    def set_profiling(self, on: bool):
-        check(self.lib.sf_context_set_profiling(self.h, 1 if on else 0))
+    def set_profiling(self, on, lane_stats: bool = False):
+        """Per-kernel CUDA-event timing; lane_stats also counts the trace kernel's
+        warp-level DE calls and iteration slots (a slower diagnostic kernel)."""
+        check(self.lib.sf_context_set_profiling(self.h, (2 if lane_stats else 1) if on else 0))
 
     def stats(self) -> dict:
         s = sf_stats()
@@ -588,12 +590,24 @@ def escape2d(ctx: GpuContext, fractal: PlanarFractal, canvas: Canvas, tile=None,
     return {"distance": dist.reshape(h, w), "traps": traps.reshape(4, h, w), "iterations": iters.reshape(h, w)}
 
 
+ORBIT_MODES = {"device": 0, "host": 1, "given": 2}
+
+
 def deep_zoom(ctx: GpuContext, center_hi, center_lo, width_units: float, width: int, height: int,
-              max_iter: int, bailout: float = 16.0, reference_f64: bool = False) -> dict:
+              max_iter: int, bailout: float = 16.0, reference_f64: bool = False, orbit: str = "device",
+              given_orbit=None) -> dict:
+    """sf_deep_zoom. orbit: "device" (FP64 on the GPU), "host" (FP64 on a host core) or
+    "given" (given_orbit: (n, 4) float32 rows Re hi, Im hi, Re lo, Im lo of Z_0..Z_(n-1)
+    for c_ref = center_hi)."""
     d = sf_deep_zoom_desc()
     d.center_hi[:] = list(center_hi)
     d.center_lo[:] = list(center_lo)
     d.width_units, d.width, d.height, d.max_iter, d.bailout = width_units, width, height, max_iter, bailout
+    d.orbit_mode = ORBIT_MODES[orbit]
+    keep = None
+    if orbit == "given":
+        keep = np.ascontiguousarray(given_orbit, dtype=np.float32).reshape(-1, 4)
+        d.orbit_len, d.orbit = len(keep), _fp(keep)
     n = width * height
     it = np.zeros(n, np.uint32)
     sm = np.zeros(n, np.float32)

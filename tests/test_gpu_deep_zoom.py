@@ -53,3 +53,56 @@ def test_shallow_zoom_matches_fp64_everywhere(gpu_ctx):
     near = (np.abs(out["iterations"].astype(np.int64) - out["iterations_f64"].astype(np.int64)) <= 1).mean()
     print(f"shallow zoom: perturbation vs FP64 {agree:.4f} (+-1: {near:.4f})")
     assert agree >= 0.93 and near >= 0.95, (agree, near)
+
+
+def test_full_frame_against_binary128_with_orbit_decomposition(gpu_ctx, oracle_mod):
+    """The deep-zoom configuration as stated (3840x2160, 50,000 iterations, width
+    1e-12 around the seeded boundary point, FP64 reference orbit on the GPU, FP32
+    deltas with rebasing) on 4096 seeded pixels against binary128 direct iteration.
+    The same frame with the oracle's binary128 reference orbit (stored as the same
+    hi/lo float pairs) separates the FP64 orbit's error from the FP32 deltas'; the
+    host's FP64 orbit gives the device's bit for bit."""
+    MI, W, H, width = 50000, 3840, 2160, 1e-12
+    c = workloads.deep_zoom_center(seed=2026, max_iter=MI)
+    dev = deep_zoom(gpu_ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, reference_f64=True)
+    host = deep_zoom(gpu_ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, orbit="host")
+    np.testing.assert_array_equal(dev["iterations"], host["iterations"])
+    np.testing.assert_array_equal(dev["smooth"], host["smooth"])
+    q = deep_zoom(gpu_ctx, c, (0.0, 0.0), width, W, H, MI, bailout=16.0, orbit="given",
+                  given_orbit=oracle_mod.mandel_orbit(c, MI, 16.0, precision=128))
+    idx = np.random.default_rng(11).choice(W * H, 4096, replace=False)
+    truth, _ = oracle_mod.mandel_escape(np.array(c), np.zeros(2), offsets(W, H, np.float32(width / W), idx), MI, 16.0,
+                                        precision=128)
+    it, it64, itq = (x.ravel()[idx] for x in (dev["iterations"], dev["iterations_f64"], q["iterations"]))
+    m = lambda a: float((a == truth).mean())
+    near = float((np.abs(it.astype(np.int64) - truth.astype(np.int64)) <= 1).mean())
+    agree64 = float((dev["iterations"] == dev["iterations_f64"]).mean())
+    print(f"deep zoom 3840x2160 50k vs binary128 on 4096 px: perturbation (FP64 orbit) {m(it):.3f} (+-1 {near:.3f}), "
+          f"perturbation (binary128 orbit) {m(itq):.3f}, FP64 direct {m(it64):.3f}; "
+          f"perturbation vs FP64 direct on all pixels {agree64:.3f}; interior {(truth == MI).mean():.3f}")
+    assert it.min() < MI and (truth == MI).mean() < 0.9  # the view straddles the boundary
+    # floors of this chaotic view (pixel pitch ~1 FP64 ulp of c): no worse than full-FP64 iteration
+    assert m(it) >= 0.25 and near >= 0.30, (m(it), near)
+    assert m(it) >= m(it64) - 0.05, (m(it), m(it64))
+    # a more accurate orbit does not make the perturbation worse
+    assert m(itq) >= m(it) - 0.05, (m(itq), m(it))
+
+
+def test_centre_lo_moves_the_view_below_an_fp64_ulp(gpu_ctx, oracle_mod):
+    """The centre's lo part (a fraction of a pixel here, below an FP64 ulp of hi) joins
+    every pixel's offset: the counts change, and they follow binary128 iteration at
+    hi + lo as well as the lo = 0 view follows its own."""
+    max_iter, w, h, width = 20000, 192, 108, 1e-12
+    c = workloads.deep_zoom_center(seed=2026, max_iter=max_iter)
+    pitch = np.float32(width / w)
+    lo = (0.37 * float(pitch), -0.21 * float(pitch))
+    a = deep_zoom(gpu_ctx, c, (0.0, 0.0), width, w, h, max_iter, bailout=16.0)["iterations"].ravel()
+    b = deep_zoom(gpu_ctx, c, lo, width, w, h, max_iter, bailout=16.0)["iterations"].ravel()
+    assert (a != b).mean() > 0.05
+    idx = np.random.default_rng(5).choice(w * h, 96, replace=False)
+    off = offsets(w, h, pitch, idx)
+    ta, _ = oracle_mod.mandel_escape(np.array(c), np.zeros(2), off, max_iter, 16.0, precision=128)
+    tb, _ = oracle_mod.mandel_escape(np.array(c), np.array(lo), off, max_iter, 16.0, precision=128)
+    print(f"centre lo: view changed on {(a != b).mean():.3f} of pixels; match vs binary128 lo=0 "
+          f"{(a[idx] == ta).mean():.3f}, with lo {(b[idx] == tb).mean():.3f}")
+    assert (b[idx] == tb).mean() >= 0.6
