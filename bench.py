@@ -312,6 +312,7 @@ def run_ours(args):
                          "de_iterations_per_step": st["de_iterations"] / args.steps,
                          "simt_lane_efficiency": lst["de_evals"] / max(32 * lst["warp_de_calls"], 1),
                          "iterate_lane_efficiency": lst["de_iterations"] / max(lst["iteration_slots"], 1),
+                         "launch_tail_fraction": lst["tail_cycles"] / max(lst["warp_cycles"], 1),
                          "lane_efficiency_source": "one further 8-spp step on the diagnostic trace kernel"},
             "gpu_launches": st["launches"],
             "status_word": status,

@@ -312,6 +312,8 @@ typedef struct sf_stats {
     uint64_t trace_launches;
     uint64_t warp_de_calls;    /* warp-level DE invocations of the trace kernel */
     uint64_t iteration_slots;  /* per invocation: warp max iterations x active lanes */
+    uint64_t warp_cycles;      /* trace kernel, profiling level 2: SM cycles of its warps */
+    uint64_t tail_cycles;      /* of which after the warp first found the launch's work exhausted */
 } sf_stats;
 /* Per-kernel CUDA-event timing on the context stream (off by default): 0 off, 1 on,
  * 2 on and the trace kernel also counts warp_de_calls and iteration_slots (a
@@ -341,9 +343,14 @@ typedef struct sf_progress {
                                issued more shadow segments than the arena holds */
 } sf_progress;
 /* The film planes of wf_commit (wavefront.wgsl:232-260). The volume layer split
- * (pathtrace.wgsl:1197-1199: primary in-scattering and paths that first scatter in fog)
- * is not kept: fog radiance is in accum, volume and moments hold (0, 0, 0, samples)
- * and surface (= radiance - volume) equals accum. Any pointer may be NULL. */
+ * (pathtrace.wgsl:1197-1199, 1243-1266): a sample's volume part is all its radiance
+ * when its camera segment scattered in the fog, else that segment's in-scattered
+ * emitter light; volume sums it, moments holds the Welford sums of
+ * max(0, delta * (v - new_mean)) in ascending sample order, surface sums radiance -
+ * volume; each plane's w is the sample count. Fog scenes keep these planes on the
+ * device (48 more bytes per pixel and 16 per path); without fog the volume part is
+ * zero: volume and moments read (0, 0, 0, samples) and surface equals accum. Any
+ * pointer may be NULL. */
 typedef struct sf_film_planes {
     float* accum;   /* 4*width*height: rgb sums and sample count */
     float* depth;   /* width*height */

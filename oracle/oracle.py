@@ -74,7 +74,7 @@ def lib():
         L.or_render.restype = C.c_uint64
         L.or_render.argtypes = [C.c_void_p, C.c_int, C.POINTER(abi.sf_scene_desc),
                                 C.POINTER(abi.sf_render_config), up, C.c_size_t, C.c_uint32, C.c_uint32,
-                                dp, dp, dp, C.POINTER(C.c_uint64), C.c_int]
+                                dp, dp, dp, C.POINTER(C.c_uint64), C.c_int, dp, dp, dp]
         L.or_planar.argtypes = [C.c_int, C.POINTER(PlanarParams), dp, C.c_size_t, dp, dp, up, C.c_int]
         L.or_mandel_escape.argtypes = [C.c_int, dp, dp, dp, C.c_size_t, C.c_uint32, C.c_double, up, dp,
                                        C.c_int]
@@ -184,18 +184,23 @@ class OracleGraph:
         return {"t": t, "steps": steps, "normal": nrm, "de_evals": int(evals)}
 
     def render(self, scene: abi.sf_scene_desc, cfg: abi.sf_render_config, pixels, sample_start,
-               samples, precision=64, threads=None):
+               samples, precision=64, threads=None, planes=False):
+        """Radiance sums of `samples` samples per pixel; planes=True adds the volume,
+        moments and surface planes (sums and counts, each pixel's starting at zero)."""
         px = np.ascontiguousarray(pixels, dtype=np.uint32).reshape(-1, 2)
         n = len(px)
         accum = np.zeros((n, 3))
         depth = np.full(n, np.nan)
         aux = np.full((n, 4), np.nan)
+        extra = {k: np.zeros((n, 4)) for k in ("volume", "moments", "surface")} if planes else {}
         evals = C.c_uint64()
         segs = lib().or_render(self.h, precision, C.byref(scene), C.byref(cfg), _up(px), n,
                                sample_start, samples, _dp(accum), _dp(depth), _dp(aux), C.byref(evals),
-                               threads or default_threads())
+                               threads or default_threads(),
+                               *((_dp(extra[k]) for k in ("volume", "moments", "surface")) if planes
+                                 else (None, None, None)))
         return {"accum": accum, "depth": depth, "aux": aux, "segments": int(segs),
-                "de_evals": int(evals.value)}
+                "de_evals": int(evals.value), **extra}
 
 
 def planar(params: PlanarParams, xy, precision=64, threads=None):

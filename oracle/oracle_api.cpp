@@ -2,6 +2,7 @@
 // C entry points of the CPU oracle (oracle_core.*), loaded with ctypes by the
 // tests, the smoke check and the CPU-baseline leg of the benchmark. Every
 // function takes a thread count; work is split in contiguous chunks.
+#include <algorithm>
 #include <atomic>
 #include <thread>
 
@@ -69,6 +70,30 @@ static void primary_one(const Graph& g, const sf_camera& cam, uint32_t w, uint32
     n_out[3 * idx + 1] = n.y;
     n_out[3 * idx + 2] = n.z;
 }
+
+// Film planes of main (pathtrace.wgsl:1243-1266) over `samples` samples from
+// sample_start, each pixel's planes starting at zero: volume (sums, count), its
+// Welford moments (sums of max(0, delta * (v - new_mean)), count) and surface
+// (sums of radiance - volume, count), accumulated in the oracle's precision.
+template <class R> struct FilmAcc {
+    R acc[3] = {0, 0, 0}, vol[4] = {0, 0, 0, 0}, mom[4] = {0, 0, 0, 0}, surf[4] = {0, 0, 0, 0};
+    void add(const PixelResult& r) {
+        for (int c = 0; c < 3; ++c) acc[c] += R(r.L[c]);
+        const R n = vol[3];
+        for (int c = 0; c < 3; ++c) {
+            const R v = R(r.V[c]);
+            const R old_mean = vol[c] / std::max(n, R(1));
+            const R delta = v - old_mean;
+            const R new_mean = old_mean + delta / (n + R(1));
+            mom[c] += std::max(R(0), delta * (v - new_mean));
+            vol[c] += v;
+            surf[c] += R(r.L[c]) - v;
+        }
+        vol[3] += R(1);
+        mom[3] += R(1);
+        surf[3] += R(1);
+    }
+};
 
 extern "C" {
 
@@ -184,7 +209,8 @@ uint64_t or_primary(void* gp, int precision, const sf_camera* cam, uint32_t w, u
 // depth/aux come from sample 0 when sample_start == 0. Returns the number of traced segments.
 uint64_t or_render(void* gp, int precision, const sf_scene_desc* scene, const sf_render_config* cfg,
                    const uint32_t* pixels, size_t n, uint32_t sample_start, uint32_t samples, double* accum,
-                   double* depth, double* aux, uint64_t* de_evals, int threads) {
+                   double* depth, double* aux, uint64_t* de_evals, int threads, double* volume, double* moments,
+                   double* surface) {
     const Graph& g = *static_cast<Graph*>(gp);
     std::atomic<uint64_t> segs{0}, evals{0};
     Scene<float> s32;
@@ -193,24 +219,27 @@ uint64_t or_render(void* gp, int precision, const sf_scene_desc* scene, const sf
     else s64 = make_scene<double>(g, *scene, *cfg);
     parallel_for(n, threads, [&](size_t i) {
         uint32_t px = pixels[2 * i], py = pixels[2 * i + 1];
-        float af[3] = {0, 0, 0};
-        double ad[3] = {0, 0, 0};
+        FilmAcc<float> af;
+        FilmAcc<double> ad;
         uint64_t sg = 0, ev = 0;
         for (uint32_t k = 0; k < samples; ++k) {
             uint32_t sample = sample_start + k;
             PixelResult r = precision == 32 ? radiance<float>(g, s32, px, py, sample) : radiance<double>(g, s64, px, py, sample);
             sg += r.segments;
             ev += r.de_evals;
-            for (int c = 0; c < 3; ++c) {
-                af[c] += float(r.L[c]);
-                ad[c] += r.L[c];
-            }
+            if (precision == 32) af.add(r);
+            else ad.add(r);
             if (sample == 0) {
                 depth[i] = r.depth;
                 for (int c = 0; c < 4; ++c) aux[4 * i + c] = r.aux[c];
             }
         }
-        for (int c = 0; c < 3; ++c) accum[3 * i + c] = precision == 32 ? double(af[c]) : ad[c];
+        for (int c = 0; c < 4; ++c) {
+            if (c < 3) accum[3 * i + c] = precision == 32 ? double(af.acc[c]) : ad.acc[c];
+            if (volume) volume[4 * i + c] = precision == 32 ? double(af.vol[c]) : ad.vol[c];
+            if (moments) moments[4 * i + c] = precision == 32 ? double(af.mom[c]) : ad.mom[c];
+            if (surface) surface[4 * i + c] = precision == 32 ? double(af.surf[c]) : ad.surf[c];
+        }
         segs += sg;
         evals += ev;
     });

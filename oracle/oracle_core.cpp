@@ -1612,6 +1612,8 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
     }
     V3<R> ro = origin, rd = dir;
     V3<R> throughput(1, 1, 1), L(0, 0, 0);
+    V3<R> primary_volume(0, 0, 0);  // the camera segment's in-scattered light (pathtrace.wgsl:821-822)
+    bool volume_path = false;        // the camera segment scattered in the fog
     R prev_pdf = 0, prev_area_total = 0;
     bool prev_from_bsdf = false;
     V3<R> prev_normal(0, 0, 0);
@@ -1640,10 +1642,13 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
         }
         if (in_fog) {  // pathtrace.wgsl:980-1011
             const R t_end = h.hit ? h.t : extent;
-            L = L + throughput * fog_segment_direct(sc, ro, rd, t_end, &rng, sample, point_stream, bounce == 0,
-                                                    visible_from);
+            const V3<R> direct_volume = throughput * fog_segment_direct(sc, ro, rd, t_end, &rng, sample, point_stream,
+                                                                        bounce == 0, visible_from);
+            L = L + direct_volume;
+            if (bounce == 0) primary_volume = primary_volume + direct_volume;
             const R t_s = fog_free_flight(sc, ro, rd, t_end, &rng);
             if (t_s < t_end) {
+                if (bounce == 0) volume_path = true;
                 if (bounce == 0 && !h.hit) first_depth = t_s;
                 const V3<R> p_s = ro + rd * t_s;
                 const R volume_area_total = area_total_weight(sc, p_s, V3<R>(0, 0, 0));
@@ -1822,6 +1827,10 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
     res.L[0] = ok ? double(L.x) : 0.0;
     res.L[1] = ok ? double(L.y) : 0.0;
     res.L[2] = ok ? double(L.z) : 0.0;
+    const V3<R> volume = volume_path ? L : primary_volume;  // pathtrace.wgsl:1198
+    res.V[0] = ok ? double(volume.x) : 0.0;
+    res.V[1] = ok ? double(volume.y) : 0.0;
+    res.V[2] = ok ? double(volume.z) : 0.0;
     res.depth = double(first_depth);
     for (int i = 0; i < 4; ++i) res.aux[i] = double(aux[i]);
     return res;

@@ -239,7 +239,10 @@ template <class R> struct Scene {
 };
 template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, const sf_render_config& c);
 
-struct PixelResult { double L[3]; double depth; double aux[4]; uint32_t segments; uint64_t de_evals; };
+// L: the sample's radiance; V: its volume part (pathtrace.wgsl:1197-1198: all of L when
+// the camera segment scattered in fog, else that segment's in-scattered emitter light);
+// both zero when L is not finite (main's `ok`, :1243-1250).
+struct PixelResult { double L[3]; double V[3]; double depth; double aux[4]; uint32_t segments; uint64_t de_evals; };
 template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint32_t px, uint32_t py, uint32_t sample);
 
 template <class R> struct Hit { bool hit; R t; uint32_t steps; Sample<R> sample; bool exhausted; uint32_t light_index; };

@@ -39,7 +39,8 @@ class sf_primary_desc(C.Structure):
 class sf_stats(C.Structure):
     _fields_ = [("de_evals", u64), ("de_iterations", u64), ("segments", u64), ("shadow_segments", u64),
                 ("steps", u64), ("launches", u64), ("kernel_ms", C.c_double), ("trace_ms", C.c_double),
-                ("trace_launches", u64), ("warp_de_calls", u64), ("iteration_slots", u64)]
+                ("trace_launches", u64), ("warp_de_calls", u64), ("iteration_slots", u64),
+                ("warp_cycles", u64), ("tail_cycles", u64)]
 
 
 class sf_progress(C.Structure):

@@ -140,7 +140,8 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
                                                    cf.samples_per_pixel), 1);
         paths += uint64_t(cf.width) * cf.height * spd;
         pixels += uint64_t(cf.width) * cf.height;
-        film_bytes += ((uint64_t(cf.width) * cf.height * 36 + 255) & ~uint64_t(255));
+        // accum | aux | depth, and for fog scenes volume | moments | surface
+        film_bytes += ((uint64_t(cf.width) * cf.height * (has_fog(jobs[i].scene) ? 84 : 36) + 255) & ~uint64_t(255));
         rounds = std::max(rounds, cf.max_bounces + 2);
         max_steps = std::max(max_steps, cf.max_steps);
         generic |= jobs[i].graph->prog.form == SF_FORM_GENERIC;
@@ -153,10 +154,14 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     const size_t scene_bytes = (n * sizeof(DevScene) + 255) & ~size_t(255);
     size_t extra = 0;
     uint32_t K = 1;  // the most shadow segments one bounce of any job issues
+    bool any_fog = false;
     for (uint32_t i = 0; i < n; ++i) {
         K = std::max(K, shadow_slots_of(jobs[i].scene));
+        any_fog |= has_fog(jobs[i].scene);
     }
-    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, K, scene_bytes + film_bytes, &extra);
+    // a fog job keeps the volume layer split: every path gets a volume row
+    const size_t pv_bytes = any_fog ? size_t(paths) * 16 : 0;
+    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, K, scene_bytes + pv_bytes + film_bytes, &extra);
     if (st != SF_OK) { delete b; return st; }
     b->a.max_steps = max_steps;
     b->a.any_generic = generic;
@@ -166,7 +171,8 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     char* base = static_cast<char*>(b->a.mem) + extra;
     DevScene* d_scenes = reinterpret_cast<DevScene*>(base);
     std::vector<DevScene> scenes(n);
-    char* film = base + scene_bytes;
+    if (any_fog) b->a.soa.pv = reinterpret_cast<float4*>(base + scene_bytes);
+    char* film = base + scene_bytes + pv_bytes;
     uint32_t pbeg = 0, xbeg = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const sf_render_config& cf = jobs[i].cfg;
@@ -177,13 +183,20 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
         j.prog = jobs[i].graph->d_prog;
         j.scene = d_scenes + i;
         size_t px = size_t(cf.width) * cf.height;
-        // accum | aux | depth: both float4 planes stay 16-byte aligned for any pixel count
+        // accum | aux (| volume | moments | surface for fog scenes) | depth: every float4
+        // plane stays 16-byte aligned for any pixel count
+        const bool fog = has_fog(jobs[i].scene);
         j.film.accum = reinterpret_cast<float4*>(film);
         j.film.aux = reinterpret_cast<float4*>(film + px * 16);
-        j.film.depth = reinterpret_cast<float*>(film + px * 32);
+        if (fog) {
+            j.film.vol = reinterpret_cast<float4*>(film + px * 32);
+            j.film.vmom = j.film.vol + px;
+            j.film.surf = j.film.vmom + px;
+        }
+        j.film.depth = reinterpret_cast<float*>(film + px * (fog ? 80 : 32));
         j.film.width = cf.width;
         j.film.height = cf.height;
-        film += (px * 36 + 255) & ~size_t(255);
+        film += (px * (fog ? 84 : 36) + 255) & ~size_t(255);
         j.geom = DispatchGeom{0, 0, cf.width, cf.height, 0, spd, uint32_t(px * spd)};
         j.path_begin = pbeg;
         j.pixel_begin = xbeg;
@@ -315,7 +328,6 @@ extern "C" sf_status sf_batch_autotune(sf_batch* b, uint32_t* best_mb, uint32_t*
 extern "C" sf_status sf_batch_readback(sf_batch* b, uint32_t job, sf_film_planes* out) {
     if (!b || !out) return fail(SF_ERR_INVALID, "null argument");
     if (job >= b->jobs.size()) return fail(SF_ERR_INVALID, "job index out of range");
-    if (const sf_status st = check_volume_planes(b->scenes[job], *out); st != SF_OK) return st;
     sf_context* c = b->ctx;
     cudaSetDevice(c->device);
     CU(film_readback(c, b->jobs[job].film, *out, c->stream));

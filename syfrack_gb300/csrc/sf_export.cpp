@@ -25,6 +25,7 @@ constexpr int kStages = 2;
 
 struct Stage {
     float* host = nullptr;      // pinned: accum (16 B/px) | depth (4 B/px) | aux (16 B/px)
+                                // (| volume | moments | surface, 16 B/px each, for fog scenes)
     cudaEvent_t ready = nullptr;
     int tile = -1;              // tile whose planes are in flight or staged, -1 when free
 };
@@ -36,6 +37,7 @@ struct sf_export {
     sf_session* win = nullptr;  // holds the graph reference
     std::vector<sf_tile> tiles; // done = samples_per_pixel once committed
     std::vector<float> accum, depth, aux;
+    std::vector<float> vol;     // fog scenes: volume | moments | surface planes of the image (4 floats/px each)
     Stage stage[kStages];
     int next_stage = 0;
     uint32_t tile_size = 0;
@@ -66,11 +68,16 @@ sf_status commit_stage(sf_export* e, Stage& s) {
     const float* acc = s.host;
     const float* dep = s.host + 4 * n;
     const float* aux = s.host + 5 * n;
+    const float* vol = s.host + 9 * n;
+    const size_t px = e->depth.size();
     for (uint32_t y = 0; y < t.h; ++y) {
         const size_t dst = size_t(t.y + y) * W + t.x, src = size_t(y) * t.w;
         std::memcpy(&e->accum[4 * dst], acc + 4 * src, size_t(t.w) * 16);
         std::memcpy(&e->depth[dst], dep + src, size_t(t.w) * 4);
         std::memcpy(&e->aux[4 * dst], aux + 4 * src, size_t(t.w) * 16);
+        if (!e->vol.empty())
+            for (size_t k = 0; k < 3; ++k)
+                std::memcpy(&e->vol[4 * (k * px + dst)], vol + 4 * (k * n + src), size_t(t.w) * 16);
     }
     t.done = e->win->cfg.samples_per_pixel;
     s.tile = -1;
@@ -111,6 +118,11 @@ sf_status render_tile(sf_export* e, int index) {
     CU(cudaMemcpyAsync(s.host, w->film.accum, n * 16, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaMemcpyAsync(s.host + 4 * n, w->film.depth, n * 4, cudaMemcpyDeviceToHost, c->stream));
     CU(cudaMemcpyAsync(s.host + 5 * n, w->film.aux, n * 16, cudaMemcpyDeviceToHost, c->stream));
+    if (w->film.vol) {
+        CU(cudaMemcpyAsync(s.host + 9 * n, w->film.vol, n * 16, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaMemcpyAsync(s.host + 13 * n, w->film.vmom, n * 16, cudaMemcpyDeviceToHost, c->stream));
+        CU(cudaMemcpyAsync(s.host + 17 * n, w->film.surf, n * 16, cudaMemcpyDeviceToHost, c->stream));
+    }
     CU(cudaEventRecord(s.ready, c->stream));
     s.tile = index;
     e->next_stage = (e->next_stage + 1) % kStages;
@@ -154,7 +166,10 @@ sf_status export_alloc(sf_context* c, sf_graph* g, const sf_scene_desc& scene, c
     e->depth.assign(px, -1.0f);
     e->aux.assign(4 * px, 0.0f);
     for (size_t i = 0; i < px; ++i) e->aux[4 * i + 3] = -1.0f;
-    const size_t stage_bytes = size_t(std::min(w->tile_size, cfg.width)) * std::min(w->tile_size, cfg.height) * 36;
+    const bool fog = w->film.vol != nullptr;
+    if (fog) e->vol.assign(12 * px, 0.0f);
+    const size_t stage_bytes =
+        size_t(std::min(w->tile_size, cfg.width)) * std::min(w->tile_size, cfg.height) * (fog ? 84 : 36);
     for (Stage& s : e->stage) {
         cudaError_t err = cudaHostAlloc(reinterpret_cast<void**>(&s.host), stage_bytes, cudaHostAllocDefault);
         if (err == cudaSuccess) err = cudaEventCreateWithFlags(&s.ready, cudaEventDisableTiming);
@@ -224,7 +239,6 @@ extern "C" sf_status sf_export_progress(sf_export* e, sf_progress* out) {
 
 extern "C" sf_status sf_export_readback(sf_export* e, sf_film_planes* out) {
     if (!e || !out) return fail(SF_ERR_INVALID, "null argument");
-    if (const sf_status vs = check_volume_planes(e->win->scene, *out); vs != SF_OK) return vs;
     cudaSetDevice(e->ctx->device);
     sf_status st = flush(e);
     if (st != SF_OK) return st;
@@ -232,19 +246,25 @@ extern "C" sf_status sf_export_readback(sf_export* e, sf_film_planes* out) {
     if (out->accum) std::memcpy(out->accum, e->accum.data(), px * 16);
     if (out->depth) std::memcpy(out->depth, e->depth.data(), px * 4);
     if (out->aux) std::memcpy(out->aux, e->aux.data(), px * 16);
-    // the volume layer split is not kept (fog radiance is in accum): zero volume
-    // contribution, surface = radiance
+    const bool split = !e->vol.empty();
+    if (split) {  // the volume layer split of a fog scene
+        if (out->volume) std::memcpy(out->volume, e->vol.data(), px * 16);
+        if (out->moments) std::memcpy(out->moments, e->vol.data() + 4 * px, px * 16);
+        if (out->surface) std::memcpy(out->surface, e->vol.data() + 8 * px, px * 16);
+    }
+    // without fog the volume contribution is zero and surface = radiance
     for (size_t i = 0; i < px; ++i) {
         const float n = e->accum[4 * i + 3];
-        for (float* p : {out->volume, out->moments})
-            if (p) { p[4 * i] = p[4 * i + 1] = p[4 * i + 2] = 0.0f; p[4 * i + 3] = n; }
+        if (!split)
+            for (float* p : {out->volume, out->moments})
+                if (p) { p[4 * i] = p[4 * i + 1] = p[4 * i + 2] = 0.0f; p[4 * i + 3] = n; }
         if (out->color) {  // RenderOutput.color: accum.rgb / max(count, 1), alpha 1
             const float d = std::max(n, 1.0f);
             for (int k = 0; k < 3; ++k) out->color[4 * i + k] = e->accum[4 * i + k] / d;
             out->color[4 * i + 3] = 1.0f;
         }
     }
-    if (out->surface) std::memcpy(out->surface, e->accum.data(), px * 16);
+    if (out->surface && !split) std::memcpy(out->surface, e->accum.data(), px * 16);
     return SF_OK;
 }
 
@@ -259,6 +279,7 @@ extern "C" sf_status sf_export_save(sf_export* e, const char* dir) {
     image.put_bytes(e->accum.data(), px * 16);
     image.put_bytes(e->depth.data(), px * 4);
     image.put_bytes(e->aux.data(), px * 16);
+    if (!e->vol.empty()) image.put_bytes(e->vol.data(), px * 48);
     const sf_graph* g = e->win->graph;
     Writer w;
     w.put(EX_MAGIC);
@@ -317,7 +338,7 @@ extern "C" sf_status sf_export_resume(sf_context* c, sf_graph* g, const char* di
         placements_hash != fnv1a(g->host.placements.data(), g->host.placements.size() * sizeof(sf_placement)))
         return fail(SF_ERR_CHECKPOINT, "export was made with another graph");
     const size_t px = size_t(cfg.width) * cfg.height;
-    if (image.size() != px * 36) return fail(SF_ERR_CHECKPOINT, "export image size mismatch");
+    if (image.size() != px * (has_fog(scene) ? 84 : 36)) return fail(SF_ERR_CHECKPOINT, "export image size mismatch");
     sf_export* e = nullptr;
     sf_status st = export_alloc(c, g, scene, cfg, &e);
     if (st != SF_OK) return st;
@@ -336,6 +357,7 @@ extern "C" sf_status sf_export_resume(sf_context* c, sf_graph* g, const char* di
     std::memcpy(e->accum.data(), image.data(), px * 16);
     std::memcpy(e->depth.data(), image.data() + px * 16, px * 4);
     std::memcpy(e->aux.data(), image.data() + px * 20, px * 16);
+    if (!e->vol.empty()) std::memcpy(e->vol.data(), image.data() + px * 36, px * 48);
     *out = e;
     return SF_OK;
 }

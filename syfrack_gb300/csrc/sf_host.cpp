@@ -1100,6 +1100,8 @@ extern "C" sf_status sf_context_stats(sf_context* c, sf_stats* out) {
     out->steps = h[SF_STAT_STEPS];
     out->warp_de_calls = h[SF_STAT_WARP_DE_CALLS];
     out->iteration_slots = h[SF_STAT_ITER_SLOTS];
+    out->warp_cycles = h[SF_STAT_WARP_CYCLES];
+    out->tail_cycles = h[SF_STAT_TAIL_CYCLES];
     out->launches = c->launches;
     out->kernel_ms = c->kernel_ms;
     out->trace_ms = c->trace_ms;
@@ -1372,6 +1374,9 @@ sf_status session_alloc(sf_session* s) {
     size_t o_scene = take(sizeof(DevScene));
     size_t o_acc = take(px * 16), o_depth = take(px * 4), o_aux = take(px * 16);
     size_t o_Ls = take(N * 16);
+    // fog scenes keep the film's volume layer split: a per-path volume row and three planes
+    const bool split = has_fog(s->scene);
+    size_t o_pv = split ? take(N * 16) : 0, o_vol = split ? take(px * 48) : 0;
     size_t o_soa = 0, o_lists = 0, o_march = 0, o_resume = 0;
     const uint32_t K = shadow_slots_of(s->scene);  // shadow segments one bounce may issue
     s->shadow_slots = K;
@@ -1403,6 +1408,12 @@ sf_status session_alloc(sf_session* s) {
         s->resume = reinterpret_cast<uint32_t*>(base + o_resume);
     }
     s->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
+    if (split) {
+        s->soa.pv = reinterpret_cast<float4*>(base + o_pv);
+        s->film.vol = reinterpret_cast<float4*>(base + o_vol);
+        s->film.vmom = s->film.vol + px;
+        s->film.surf = s->film.vmom + px;
+    }
     s->counts = reinterpret_cast<uint32_t*>(base + o_counts);
     s->qcounts = reinterpret_cast<uint32_t*>(base + o_qcounts);
     s->status = reinterpret_cast<uint32_t*>(base + o_status);
@@ -1613,31 +1624,42 @@ extern "C" sf_status sf_session_tiles(sf_session* s, sf_tile* tiles, uint32_t ca
 namespace sfh {
 // Film readback through the context's pinned staging: the device planes arrive at
 // full link speed, then the host threads copy them into the caller's (pageable)
-// buffers and derive the others: color = accum.rgb / max(count, 1) with alpha 1
-// (RenderOutput.color), volume and moments (no volume layer: zero contribution and
-// the sample count) and surface (= accum).
+// buffers and derive color = accum.rgb / max(count, 1) with alpha 1
+// (RenderOutput.color). A film without the volume layer split (no fog) has a zero
+// volume contribution: volume and moments are (0, 0, 0, samples) and surface = accum.
 cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st) {
     const size_t px = size_t(f.width) * f.height;
-    const bool need_acc = out.accum || out.color || out.volume || out.moments || out.surface;
-    const size_t bytes = (need_acc ? px * 16 : 0) + (out.depth ? px * 4 : 0) + (out.aux ? px * 16 : 0);
+    const bool split = f.vol != nullptr;
+    const bool need_acc = out.accum || out.color || (!split && (out.volume || out.moments || out.surface));
+    const bool need_vol = split && (out.volume || out.moments || out.surface);
+    const size_t bytes = (need_acc ? px * 16 : 0) + (out.depth ? px * 4 : 0) + (out.aux ? px * 16 : 0) +
+                         (need_vol ? px * 48 : 0);
     if (!bytes) return cudaSuccess;
     std::lock_guard<std::mutex> lk(c->stage_mu);
     if (cudaError_t e = ensure_stage(c, bytes); e != cudaSuccess) return e;
     float* acc = static_cast<float*>(c->stage);
     float* depth = acc + (need_acc ? px * 4 : 0);
     float* aux = depth + (out.depth ? px : 0);
+    float* vol = aux + (out.aux ? px * 4 : 0);  // volume | moments | surface (contiguous on the device)
     cudaError_t e = cudaSuccess;
     if (need_acc) e = cudaMemcpyAsync(acc, f.accum, px * 16, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && out.depth) e = cudaMemcpyAsync(depth, f.depth, px * 4, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess && out.aux) e = cudaMemcpyAsync(aux, f.aux, px * 16, cudaMemcpyDeviceToHost, st);
+    if (e == cudaSuccess && need_vol) e = cudaMemcpyAsync(vol, f.vol, px * 48, cudaMemcpyDeviceToHost, st);
     if (e == cudaSuccess) e = cudaStreamSynchronize(st);
     if (e != cudaSuccess) return e;
     host_parallel(px, [&](size_t b, size_t end) {
         const size_t n = end - b;
         if (out.accum) std::memcpy(out.accum + 4 * b, acc + 4 * b, n * 16);
-        if (out.surface) std::memcpy(out.surface + 4 * b, acc + 4 * b, n * 16);
         if (out.depth) std::memcpy(out.depth + b, depth + b, n * 4);
         if (out.aux) std::memcpy(out.aux + 4 * b, aux + 4 * b, n * 16);
+        if (split) {
+            if (out.volume) std::memcpy(out.volume + 4 * b, vol + 4 * b, n * 16);
+            if (out.moments) std::memcpy(out.moments + 4 * b, vol + 4 * (px + b), n * 16);
+            if (out.surface) std::memcpy(out.surface + 4 * b, vol + 4 * (2 * px + b), n * 16);
+        } else if (out.surface) {
+            std::memcpy(out.surface + 4 * b, acc + 4 * b, n * 16);
+        }
         for (size_t i = b; i < end; ++i) {
             const float cnt = acc[4 * i + 3];
             if (out.color) {
@@ -1647,6 +1669,7 @@ cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_plan
                 out.color[4 * i + 2] = acc[4 * i + 2] / d;
                 out.color[4 * i + 3] = 1.0f;
             }
+            if (split) continue;
             if (out.volume) { out.volume[4 * i] = out.volume[4 * i + 1] = out.volume[4 * i + 2] = 0.0f; out.volume[4 * i + 3] = cnt; }
             if (out.moments) { out.moments[4 * i] = out.moments[4 * i + 1] = out.moments[4 * i + 2] = 0.0f; out.moments[4 * i + 3] = cnt; }
         }
@@ -1655,18 +1678,8 @@ cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_plan
 }
 }  // namespace sfh
 
-namespace sfh {
-sf_status check_volume_planes(const sf_scene_desc& scene, const sf_film_planes& out) {
-    if (scene.fog.density > 0.0f && (out.volume || out.moments || out.surface))
-        return fail(SF_ERR_UNSUPPORTED, "the volume layer split of a fog scene is not kept on the device film: "
-                                        "read accum, depth, aux or color");
-    return SF_OK;
-}
-}  // namespace sfh
-
 extern "C" sf_status sf_session_readback(sf_session* s, sf_film_planes* out) {
     if (!s || !out) return fail(SF_ERR_INVALID, "null argument");
-    if (const sf_status st = check_volume_planes(s->scene, *out); st != SF_OK) return st;
     sf_context* c = s->ctx;
     cudaSetDevice(c->device);
     CU(film_readback(c, s->film, *out, c->stream));
@@ -1773,10 +1786,12 @@ extern "C" sf_status sf_session_save(sf_session* s, const char* dir) {
     CU(cudaStreamSynchronize(c->stream));
     size_t px = size_t(s->cfg.width) * s->cfg.height;
     Writer film;
-    film.buf.resize(px * 36);
+    // accum | depth | aux (| volume | moments | surface for fog scenes)
+    film.buf.resize(px * (s->film.vol ? 84 : 36));
     CU(cudaMemcpy(film.buf.data(), s->film.accum, px * 16, cudaMemcpyDeviceToHost));
     CU(cudaMemcpy(film.buf.data() + px * 16, s->film.depth, px * 4, cudaMemcpyDeviceToHost));
     CU(cudaMemcpy(film.buf.data() + px * 20, s->film.aux, px * 16, cudaMemcpyDeviceToHost));
+    if (s->film.vol) CU(cudaMemcpy(film.buf.data() + px * 36, s->film.vol, px * 48, cudaMemcpyDeviceToHost));
     Writer w;
     w.put(CK_MAGIC);
     w.put(CK_VERSION);
@@ -1840,7 +1855,7 @@ extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* d
         placements_hash != fnv1a(g->host.placements.data(), g->host.placements.size() * sizeof(sf_placement)))
         return fail(SF_ERR_CHECKPOINT, "checkpoint was made with another graph");
     size_t px = size_t(cfg.width) * cfg.height;
-    if (filmb.size() != px * 36) return fail(SF_ERR_CHECKPOINT, "checkpoint film size mismatch");
+    if (filmb.size() != px * (has_fog(scene) ? 84 : 36)) return fail(SF_ERR_CHECKPOINT, "checkpoint film size mismatch");
     sf_session* s = nullptr;
     sf_status st = sf_session_create(c, g, &scene, &cfg, &s);
     if (st != SF_OK) return st;
@@ -1861,6 +1876,8 @@ extern "C" sf_status sf_session_resume(sf_context* c, sf_graph* g, const char* d
     cudaError_t e = cudaMemcpy(s->film.accum, filmb.data(), px * 16, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(s->film.depth, filmb.data() + px * 16, px * 4, cudaMemcpyHostToDevice);
     if (e == cudaSuccess) e = cudaMemcpy(s->film.aux, filmb.data() + px * 20, px * 16, cudaMemcpyHostToDevice);
+    if (e == cudaSuccess && s->film.vol)
+        e = cudaMemcpy(s->film.vol, filmb.data() + px * 36, px * 48, cudaMemcpyHostToDevice);
     if (e != cudaSuccess) {
         sf_session_destroy(s);
         return cuda_fail(e, "checkpoint upload");
@@ -2004,12 +2021,13 @@ extern "C" sf_status sf_escape2d(sf_context* c, const sf_planar_desc* f, const s
     return SF_OK;
 }
 
-// The reference orbit Z_n of c_ref in FP64 on the host, as k_ref_orbit writes it on
-// the device (hi = float(Z), lo = float(Z - hi), two copies of the last entry past the
-// end) and with the same unfused operations (this file is compiled without
-// contraction), so the two orbits are equal. One host core runs the sequential
-// recurrence in well under a millisecond per 10^5 iterations; the single device
-// thread took 26 ms for 50,000 on this part's narrow FP64 pipe. Returns the length.
+// The reference orbit Z_n of c_ref in FP64 on the host, as the device writes it
+// (hi = float(Z), lo = float(Z - hi), two copies of the last entry past the end) and
+// with the same operations: |Z|^2 = fma(x, x, y*y); Re Z' = fma(x, x, -y*y) + Re c;
+// Im Z' = fma(x + x, y, Im c) (this file is compiled without contraction, so the
+// explicit fma calls are the only fused operations), so the two orbits are equal.
+// One host core runs the sequential recurrence in well under a millisecond per 10^5
+// iterations. Returns the length.
 static uint32_t host_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float* lo, float* hi) {
     double zx = 0.0, zy = 0.0;
     const double b2 = bailout * bailout;
@@ -2020,9 +2038,10 @@ static uint32_t host_ref_orbit(double cx, double cy, uint32_t max_iter, double b
         hi[2 * n + 1] = hy;
         lo[2 * n] = float(zx - double(hx));
         lo[2 * n + 1] = float(zy - double(hy));
-        if (n >= max_iter || zx * zx + zy * zy > b2) break;
-        const double nx = (zx * zx - zy * zy) + cx;
-        zy = (2.0 * zx) * zy + cy;
+        const double y2 = zy * zy;
+        if (n >= max_iter || std::fma(zx, zx, y2) > b2) break;
+        const double nx = std::fma(zx, zx, -y2) + cx;
+        zy = std::fma(zx + zx, zy, cy);
         zx = nx;
         ++n;
     }
@@ -2050,7 +2069,10 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     size_t n = size_t(d->width) * d->height;
     size_t M = size_t(d->max_iter) + 4;  // the orbit, two entries past its end, one spare
     const size_t Mb = (M * 8 + 255) & ~size_t(255);
-    size_t bytes = 2 * Mb + 256 + n * 8 * (reference_f64 ? 2 : 1);
+    // the device orbit's FP64 values (split into hi/lo pairs by a parallel kernel)
+    const size_t Zb = d->orbit_mode == SF_ORBIT_DEVICE ? ((M * 16 + 255) & ~size_t(255)) : 0;
+    const size_t z_off = (2 * Mb + 256 + n * 8 * (reference_f64 ? 2 : 1) + 255) & ~size_t(255);
+    size_t bytes = z_off + Zb;
     void* buf = nullptr;
     sf_status st = ctx_alloc(c, bytes, &buf);
     if (st != SF_OK) return st;
@@ -2063,6 +2085,7 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     float* ds = reinterpret_cast<float*>(di + n);
     uint32_t* di64 = reinterpret_cast<uint32_t*>(ds + n);
     float* ds64 = reinterpret_cast<float*>(di64 + n);
+    double2* oz = Zb ? reinterpret_cast<double2*>(b + z_off) : nullptr;  // 256-byte aligned
     // the orbit of c_ref = centre hi; the centre's lo part joins every pixel's offset
     const double cx = d->center_hi[0], cy = d->center_hi[1];
     const float2 c_lo = make_float2(float(d->center_lo[0]), float(d->center_lo[1]));
@@ -2076,7 +2099,7 @@ extern "C" sf_status sf_deep_zoom(sf_context* c, const sf_deep_zoom_desc* d, uin
     if (e == cudaSuccess) e = ensure_stage(c, std::max(2 * Mb + 16, n * 4 * planes));
     if (e == cudaSuccess && d->orbit_mode == SF_ORBIT_DEVICE) {
         LaunchTimer t(c, false);
-        e = sf_launch_ref_orbit(cx, cy, d->max_iter, d->bailout, olo, of, olen, c->stream);
+        e = sf_launch_ref_orbit_split(cx, cy, d->max_iter, d->bailout, oz, olo, of, olen, c->stream);
     } else if (e == cudaSuccess) {
         // the host's orbit, or the caller's, uploaded from the pinned staging (lo, hi, then its length)
         char* stg = static_cast<char*>(c->stage);

@@ -149,9 +149,8 @@ sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen);
 void planar_dev(const sf_planar_desc& f, PlanarDev& o);
 sf_status planar_check(const sf_planar_desc* f);
 cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);
-// A fog scene's volume, moments and surface planes are not kept by the device film:
-// a readback that asks for them is refused instead of returning the no-fog planes.
-sf_status check_volume_planes(const sf_scene_desc& scene, const sf_film_planes& out);
+// Fog scenes keep the film's volume layer split (volume, moments and surface planes).
+inline bool has_fog(const sf_scene_desc& d) { return d.fog.density > 0.0f; }
 
 // Wavefront path state for N paths with K shadow slots (a bounce issues at most K
 // shadow segments): eight path planes, K sets of shadow planes and visibility words,

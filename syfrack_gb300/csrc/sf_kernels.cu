@@ -198,6 +198,11 @@ __global__ void __launch_bounds__(256) k_film_clear(FilmPlanes film) {
         film.accum[i] = make_float4(0.f, 0.f, 0.f, 0.f);
         film.depth[i] = -1.0f;
         film.aux[i] = make_float4(0.f, 0.f, 0.f, -1.0f);
+        if (film.vol) {
+            film.vol[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            film.vmom[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+            film.surf[i] = make_float4(0.f, 0.f, 0.f, 0.f);
+        }
     }
 }
 cudaError_t sf_launch_film_clear(FilmPlanes film, cudaStream_t st) {
@@ -312,12 +317,19 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
                 DeRaw shs;
                 int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, absolute, shs, evals, iters);
                 segs++;
-                if (sr == MARCH_MISS && sli == SF_NO_LIGHT) ps.L = add_rn(ps.L, sh.contrib);
+                if (sr == MARCH_MISS && sli == SF_NO_LIGHT) {
+                    ps.L = add_rn(ps.L, sh.contrib);
+                    if (sh.volume) ps.pv = add_rn(ps.pv, sh.contrib);
+                }
             };
             int cont = bounce_body(S, ps, h, emit, fd, fa, sample, stream);
             if (cont != PATH_CONTINUE) break;
         }
         soa.Ls[(size_t)s * tile_px + local] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
+        if (soa.pv) {  // the sample's volume part (pathtrace.wgsl:1198)
+            const float3 v = path_volume(ps);
+            soa.pv[(size_t)s * tile_px + local] = make_float4(v.x, v.y, v.z, 0.f);
+        }
     }
     warp_stat(&stats[SF_STAT_DE_EVALS], evals);
     warp_stat(&stats[SF_STAT_DE_ITERS], iters);
@@ -325,10 +337,31 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
 }
 
 // ------------------------------------------------------------------ deep zoom
-// Reference orbit Z_n of c_ref in FP64 (one thread).
-// Each entry is kept as the pair hi = float(Z), lo = float(Z - hi): hi + lo carries
-// about 48 bits of Z, so the perturbation kernel can rebase without FP64 arithmetic.
-// The arrays hold max_iter + 4 entries.
+// Reference orbit Z_n of c_ref in FP64 (one thread), one step:
+// |Z|^2 = fma(x, x, y*y) against the bailout, Re Z' = fma(x, x, -y*y) + Re c,
+// Im Z' = fma(x + x, y, Im c). Seven FP64 instructions per iteration: on this part's
+// narrow FP64 pipe the serial orbit is bound by their issue, so the hi/lo split of each
+// entry (four conversions and two subtractions) runs in a separate parallel kernel.
+// The host's orbit (sf_host.cpp host_ref_orbit) performs the same operations.
+static __device__ __forceinline__ bool orbit_escaped(double zx, double zy, double b2, double& y2) {
+    y2 = __dmul_rn(zy, zy);
+    return __fma_rn(zx, zx, y2) > b2;
+}
+static __device__ __forceinline__ void orbit_step(double& zx, double& zy, double y2, double cx, double cy) {
+    const double nx = __dadd_rn(__fma_rn(zx, zx, -y2), cx);
+    zy = __fma_rn(__dadd_rn(zx, zx), zy, cy);
+    zx = nx;
+}
+// Each entry as the pair hi = float(Z), lo = float(Z - hi): hi + lo carries about 48
+// bits of Z, so the perturbation kernel can rebase without FP64 arithmetic.
+static __device__ __forceinline__ void orbit_split(double zx, double zy, float2& lo, float2& hi) {
+    const float hx = (float)zx, hy = (float)zy;
+    hi = make_float2(hx, hy);
+    lo = make_float2((float)(zx - (double)hx), (float)(zy - (double)hy));
+}
+
+// The orbit as hi/lo pairs in one kernel (the allocation-free path). The arrays hold
+// max_iter + 4 entries.
 __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo, float2* orbit_f,
                             uint32_t* orbit_len) {
     if (threadIdx.x != 0 || blockIdx.x != 0) return;
@@ -336,15 +369,10 @@ __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bail
     const double b2 = __dmul_rn(bailout, bailout);
     uint32_t n = 0;
     for (;;) {
-        float hx = (float)zx, hy = (float)zy;
-        orbit_f[n] = make_float2(hx, hy);
-        orbit_lo[n] = make_float2((float)(zx - (double)hx), (float)(zy - (double)hy));
-        // unfused, in the order of the host's orbit (sf_host.cpp host_ref_orbit), so
-        // both give the same Z_n to the last bit
-        if (n >= max_iter || __dadd_rn(__dmul_rn(zx, zx), __dmul_rn(zy, zy)) > b2) break;
-        const double nx = __dadd_rn(__dsub_rn(__dmul_rn(zx, zx), __dmul_rn(zy, zy)), cx);
-        zy = __dadd_rn(__dmul_rn(__dmul_rn(2.0, zx), zy), cy);
-        zx = nx;
+        orbit_split(zx, zy, orbit_lo[n], orbit_f[n]);
+        double y2;
+        if (n >= max_iter || orbit_escaped(zx, zy, b2, y2)) break;
+        orbit_step(zx, zy, y2, cx, cy);
         ++n;
     }
     // two copies of the last entry past the end: the perturbation loads Z_(m+3)
@@ -354,6 +382,35 @@ __global__ void k_ref_orbit(double cx, double cy, uint32_t max_iter, double bail
         orbit_lo[n + k] = orbit_lo[n];
     }
     *orbit_len = n + 1;
+}
+
+// The orbit's FP64 values only (one thread): z holds max_iter + 4 entries.
+__global__ void k_ref_orbit_z(double cx, double cy, uint32_t max_iter, double bailout, double2* z,
+                              uint32_t* orbit_len) {
+    if (threadIdx.x != 0 || blockIdx.x != 0) return;
+    double zx = 0.0, zy = 0.0;
+    const double b2 = __dmul_rn(bailout, bailout);
+    uint32_t n = 0;
+    for (;;) {
+        z[n] = make_double2(zx, zy);
+        double y2;
+        if (n >= max_iter || orbit_escaped(zx, zy, b2, y2)) break;
+        orbit_step(zx, zy, y2, cx, cy);
+        ++n;
+    }
+    *orbit_len = n + 1;
+}
+
+// The split of k_ref_orbit_z's values into hi/lo pairs, with the two copies of the
+// last entry past the end: entries [0, len + 2).
+__global__ void k_orbit_split(const double2* __restrict__ z, const uint32_t* __restrict__ orbit_len, uint32_t max_entries,
+                              float2* orbit_lo, float2* orbit_f) {
+    const uint32_t len = *orbit_len;
+    const uint32_t end = min(len + 2, max_entries);
+    for (uint32_t i = blockIdx.x * blockDim.x + threadIdx.x; i < end; i += gridDim.x * blockDim.x) {
+        const double2 v = z[min(i, len - 1)];
+        orbit_split(v.x, v.y, orbit_lo[i], orbit_f[i]);
+    }
 }
 
 // FP32 perturbation with rebasing: z_n = Z_m + d, d' = (2 Z_m + d) d + dc;
@@ -576,6 +633,13 @@ cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, P
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st) {
     k_ref_orbit<<<1, 32, 0, st>>>(cx, cy, max_iter, bailout, orbit_lo, orbit_f, orbit_len);
+    return cudaGetLastError();
+}
+cudaError_t sf_launch_ref_orbit_split(double cx, double cy, uint32_t max_iter, double bailout, double2* z,
+                                      float2* orbit_lo, float2* orbit_f, uint32_t* orbit_len, cudaStream_t st) {
+    k_ref_orbit_z<<<1, 32, 0, st>>>(cx, cy, max_iter, bailout, z, orbit_len);
+    const uint32_t entries = max_iter + 3;  // the orbit's largest length plus the two copies
+    k_orbit_split<<<grid_for(entries, 256, 4), 256, 0, st>>>(z, orbit_len, entries, orbit_lo, orbit_f);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_perturb(const float2* orbit_lo, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,

@@ -18,7 +18,7 @@ enum { SF_WF_QUEUE_OVERFLOW = 1u, SF_WF_COMPACT_OVERFLOW = 2u, SF_WF_ALIVE_AT_CO
 // the warp's largest iteration count times its active lanes (SIMT efficiency:
 // DE_EVALS / (32 * WARP_DE_CALLS) and DE_ITERS / ITER_SLOTS).
 enum { SF_STAT_DE_EVALS = 0, SF_STAT_DE_ITERS, SF_STAT_SEGMENTS, SF_STAT_STEPS, SF_STAT_SHADOW_SEGMENTS,
-       SF_STAT_WARP_DE_CALLS, SF_STAT_ITER_SLOTS, SF_STAT_COUNT = 8 };
+       SF_STAT_WARP_DE_CALLS, SF_STAT_ITER_SLOTS, SF_STAT_WARP_CYCLES, SF_STAT_TAIL_CYCLES, SF_STAT_COUNT = 10 };
 
 // Structure-of-arrays path storage for one dispatch of `capacity` paths.
 struct PathSoA {
@@ -40,6 +40,10 @@ struct PathSoA {
     float4* m0;      // t, omega, prev_radius, step_len
     float4* m1;      // t_end, cand_t, cand_err, bits(steps)
     uint32_t* m2;    // light index ahead of the segment
+    // fog scenes only (null otherwise): primary volume xyz, w = bits(volume tags of the
+    // pending shadow slots | the camera segment scattered << 8); the sample's volume
+    // part once the path ends
+    float4* pv;
     uint32_t capacity;
     uint32_t shadow_slots;  // K: sh_o/sh_d/sh_c/vis have K * capacity rows (row = k * capacity + path)
 };
@@ -78,6 +82,11 @@ struct FilmPlanes {
     float4* accum;  // sum of (L, 1) per sample
     float* depth;   // first-hit distance, -1 for a miss (sample 0)
     float4* aux;    // first-hit normal and steps (sample 0)
+    // the volume layer split of fog scenes (null otherwise): sums of (volume, 1), their
+    // Welford moments, sums of (radiance - volume, 1)
+    float4* vol;
+    float4* vmom;
+    float4* surf;
     uint32_t width, height;
     uint32_t x0, y0;  // image pixel of the planes' first element (a window film; 0, 0 for the image)
 };
@@ -191,6 +200,10 @@ cudaError_t sf_launch_escape2d(const PlanarDev* f, const CanvasDev* canvas, uint
 // orbit_f[n] = float(Z_n), orbit_lo[n] = float(Z_n - orbit_f[n]), n < *orbit_len <= max_iter + 1.
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,
                                 float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
+// The same orbit in two launches: the serial FP64 recurrence into z (max_iter + 4
+// entries), then its parallel split into the hi/lo arrays.
+cudaError_t sf_launch_ref_orbit_split(double cx, double cy, uint32_t max_iter, double bailout, double2* z,
+                                      float2* orbit_lo, float2* orbit_f, uint32_t* orbit_len, cudaStream_t st);
 // *work is the pixel counter of the launch and must be 0 when it starts. c_lo: the
 // centre's part below the orbit's c_ref, added to every pixel's offset.
 cudaError_t sf_launch_perturb(const float2* orbit_lo, const float2* orbit_f, const uint32_t* orbit_len, uint32_t width,

@@ -62,6 +62,7 @@ static __device__ __forceinline__ void generate_path(const DevScene& S, PathSoA&
     PathState ps;
     path_begin(S, ps, px, py, sample);
     store_path(soa, path, ps, SF_PF_CONT);
+    if (soa.pv) soa.pv[path] = make_float4(0.f, 0.f, 0.f, 0.f);
     begin_segment(S, soa, path, ps.o, ps.d, S.extent);
 }
 
@@ -73,6 +74,17 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
     PathState ps;
     uint32_t flags = load_path(soa, path, ps);
     const size_t cap = soa.capacity;
+    // the volume layer split (fog scenes): the camera segment's in-scattered light and
+    // the volume tags of last round's shadow slots
+    uint32_t vbits = 0;
+    ps.pv = mk3(0.f, 0.f, 0.f);
+    ps.volume_path = false;
+    if (soa.pv) {
+        const float4 v = soa.pv[path];
+        ps.pv = mk3(v.x, v.y, v.z);
+        vbits = __float_as_uint(v.w);
+        ps.volume_path = (vbits >> 8) & 1u;
+    }
     if (flags & SF_PF_SHADOW) {  // last round's shadow segments, in slot order
         const uint32_t mask = (flags >> SF_PF_SHADOW_SHIFT) & 0xffu;
         for (uint32_t k = 0; k < soa.shadow_slots; ++k) {
@@ -80,9 +92,11 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
             if (((mask >> k) & 1u) && soa.vis[row]) {
                 const float4 c = soa.sh_c[row];
                 ps.L = add_rn(ps.L, mk3(c.x, c.y, c.z));
+                if ((vbits >> k) & 1u) ps.pv = add_rn(ps.pv, mk3(c.x, c.y, c.z));
             }
         }
     }
+    uint32_t vmask = 0;  // volume tags of this bounce's shadow slots
     uint32_t nf = 0;
     if (flags & SF_PF_CONT) {
         uint4 hr = soa.hit[path];
@@ -122,6 +136,7 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
             soa.sh_c[row] = make_float4(sh.contrib.x, sh.contrib.y, sh.contrib.z, 0.f);
             begin_segment(S, soa, uint32_t(cap + row), sh.o, sh.dir, sh.t_end);
             sh_mask |= 1u << n_sh;
+            if (sh.volume) vmask |= 1u << n_sh;
             n_sh++;
         };
         int r = bounce_body(S, ps, h, emit, fd, fa, sample, point_stream_of(S, px, py));
@@ -135,6 +150,15 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
     store_path(soa, path, ps, nf);
     if (nf & SF_PF_CONT) begin_segment(S, soa, path, ps.o, ps.d, S.extent);
     if (!nf) soa.Ls[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
+    if (soa.pv) {
+        if (!nf) {  // the sample's volume part (pathtrace.wgsl:1198)
+            const float3 v = path_volume(ps);
+            soa.pv[path] = make_float4(v.x, v.y, v.z, 0.f);
+        } else {
+            soa.pv[path] = make_float4(ps.pv.x, ps.pv.y, ps.pv.z,
+                                       __uint_as_float(vmask | (ps.volume_path ? 256u : 0u)));
+        }
+    }
     return nf;
 }
 
@@ -155,14 +179,42 @@ static __device__ __forceinline__ void commit_pixel(const PathSoA& soa, const Di
     uint32_t px = g.tile_x + local % g.tile_w, py = g.tile_y + local / g.tile_w;
     const size_t idx = film_index(film, px, py);
     float4 acc = film.accum[idx];
+    const bool split = film.vol != nullptr;
+    float4 vol = make_float4(0.f, 0.f, 0.f, 0.f), mom = vol, surf = vol;
+    if (split) {
+        vol = film.vol[idx];
+        mom = film.vmom[idx];
+        surf = film.surf[idx];
+    }
     for (uint32_t s = 0; s < g.samples; ++s) {
-        float4 L = soa.Ls[path_base + (size_t)s * tile_px + local];
+        const size_t row = path_base + (size_t)s * tile_px + local;
+        float4 L = soa.Ls[row];
         bool ok = L.x == L.x && L.y == L.y && L.z == L.z && fabsf(L.x) < 1e30f && fabsf(L.y) < 1e30f &&
                   fabsf(L.z) < 1e30f;
         acc.x += ok ? L.x : 0.0f;
         acc.y += ok ? L.y : 0.0f;
         acc.z += ok ? L.z : 0.0f;
         acc.w += 1.0f;
+        if (split) {  // volume Welford moments and the surface sums (pathtrace.wgsl:1246-1266)
+            const float4 pv = soa.pv[row];
+            const float3 v = ok ? mk3(pv.x, pv.y, pv.z) : mk3(0.f, 0.f, 0.f);
+            const float3 sv = ok ? mk3(L.x - pv.x, L.y - pv.y, L.z - pv.z) : mk3(0.f, 0.f, 0.f);
+            const float nm = fmaxf(vol.w, 1.0f), n1 = vol.w + 1.0f;
+            const float3 old_mean = mk3(__fdiv_rn(vol.x, nm), __fdiv_rn(vol.y, nm), __fdiv_rn(vol.z, nm));
+            const float3 delta = v - old_mean;
+            const float3 new_mean = old_mean + mk3(__fdiv_rn(delta.x, n1), __fdiv_rn(delta.y, n1), __fdiv_rn(delta.z, n1));
+            mom.x += fmaxf(0.0f, delta.x * (v.x - new_mean.x));
+            mom.y += fmaxf(0.0f, delta.y * (v.y - new_mean.y));
+            mom.z += fmaxf(0.0f, delta.z * (v.z - new_mean.z));
+            mom.w += 1.0f;
+            vol = make_float4(vol.x + v.x, vol.y + v.y, vol.z + v.z, vol.w + 1.0f);
+            surf = make_float4(surf.x + sv.x, surf.y + sv.y, surf.z + sv.z, surf.w + 1.0f);
+        }
     }
     film.accum[idx] = acc;
+    if (split) {
+        film.vol[idx] = vol;
+        film.vmom[idx] = mom;
+        film.surf[idx] = surf;
+    }
 }

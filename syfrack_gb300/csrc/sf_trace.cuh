@@ -359,11 +359,15 @@ static __device__ Surface make_surface(const DevScene& S, float3 n, const DeSamp
 // ------------------------------------------------------------------ path state
 struct PathState {
     float3 o, d, tp, L, prev_normal;
+    float3 pv;  // primary_volume (pathtrace.wgsl:821): the camera segment's in-scattered emitter light
     float prev_pdf, prev_area_total;
     uint32_t rng, bounce;
     bool prev_from_bsdf;
     bool prev_from_volume;  // the segment left a fog scattering point (its emitters were estimated there)
+    bool volume_path;       // the camera segment scattered in the fog (pathtrace.wgsl:822)
 };
+// The sample's volume part for the film's volume planes (pathtrace.wgsl:1198).
+__device__ __forceinline__ float3 path_volume(const PathState& ps) { return ps.volume_path ? ps.L : ps.pv; }
 // Result of a continuation trace (Hit of pathtrace.wgsl:60-74 plus the normal).
 struct HitInfo {
     bool hit, exhausted;
@@ -377,6 +381,7 @@ struct ShadowReq {
     float3 o, dir;
     float t_end;
     float3 contrib;
+    bool volume = false;  // the camera segment's in-scattered light: also counted in PathState.pv
 };
 #define SF_MAX_SHADOWS 8  // shadow requests of one bounce: at most one per light
 enum { PATH_CONTINUE = 1, PATH_DONE = 0 };
@@ -391,6 +396,8 @@ __device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uin
     ps.prev_area_total = 0.0f;
     ps.prev_from_bsdf = false;
     ps.prev_from_volume = false;
+    ps.pv = mk3(0.f, 0.f, 0.f);
+    ps.volume_path = false;
     ps.bounce = 0;
 }
 // point_stream of radiance (pathtrace.wgsl:823): the pixel's rotation of the
@@ -732,6 +739,7 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
         sh.dir = wi;
         sh.t_end = fmaxf(0.0f, distance - fmaxf(1e-5f, distance * 1e-6f));
         sh.contrib = tp * ((ld3(l.color) * scale) * color);
+        sh.volume = primary;  // pathtrace.wgsl:985: bounce 0's direct volume
         emit(sh);
     }
 }
@@ -812,6 +820,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
         fog_segment_direct(S, ps.tp, ps.o, ps.d, t_end, ps.rng, point_index, point_stream, ps.bounce == 0, emit);
         const float t_s = fog_free_flight(S, ps.o, ps.d, t_end, ps.rng);
         if (t_s < t_end) {
+            if (ps.bounce == 0) ps.volume_path = true;
             if (ps.bounce == 0 && !h.hit && first_depth) *first_depth = t_s;
             const float3 p_s = ps.o + ps.d * t_s;
             const float volume_area_total = area_total_weight(S, p_s, mk3(0.f, 0.f, 0.f));

@@ -91,6 +91,10 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     uint32_t hit_w = 0;  // iterations | material << 16 of the surface hit whose normal is being tapped
     uint32_t n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0;
     unsigned long long n_slots = 0;
+    // LANE_STATS: the warp's cycles, and those after its first failed fetch (the tail,
+    // when the launch's work is exhausted and lanes idle beside the last segments)
+    long long t_start = 0, t_dry = 0;
+    if constexpr (LANE_STATS) t_start = clock64();
 
     // End of a continuation or shadow segment without a surface sample.
     auto finish = [&](int r) {
@@ -123,6 +127,9 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         const uint32_t active = __ballot_sync(FULL_MASK, state == TL_MARCH || state == TL_CAND || state == TL_NORMAL);
         const bool refill = idle && ((uint32_t)__popc(idle) >= regen || active == 0);
         uint32_t w = warp_fetch(tl.work_counter, refill && state == TL_IDLE);
+        if constexpr (LANE_STATS) {
+            if (t_dry == 0 && __any_sync(FULL_MASK, refill && state == TL_IDLE && w >= total)) t_dry = clock64();
+        }
         if (refill && state == TL_IDLE) {
             if (w >= total) {
                 state = TL_DONE;
@@ -246,6 +253,11 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     if constexpr (LANE_STATS) {
         warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
         warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
+        if (lane_id() == 0) {
+            const long long t_end = clock64();
+            atomicAdd(&stats[SF_STAT_WARP_CYCLES], (unsigned long long)(t_end - t_start));
+            atomicAdd(&stats[SF_STAT_TAIL_CYCLES], (unsigned long long)(t_dry ? t_end - t_dry : 0));
+        }
     }
 }
 

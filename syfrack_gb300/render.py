@@ -514,6 +514,16 @@ class Batch:
         n = int(acc[..., 3].min()) if acc.size else 0
         return RenderOutput(color, acc, depth, aux, n, int(acc[..., 3].max()) if acc.size else 0, 0.0)
 
+    def film_planes(self, job: int) -> dict:
+        """Every plane of a job's film: accum, depth, aux, volume, moments, surface."""
+        cfg = self.jobs[job][1]
+        w, h = cfg.width, cfg.height
+        out = {k: np.zeros((h, w, 4), np.float32) for k in ("accum", "aux", "volume", "moments", "surface")}
+        out["depth"] = np.zeros((h, w), np.float32)
+        planes = sf_film_planes(*(_fp(out[k]) for k in ("accum", "depth", "aux", "volume", "moments", "surface")))
+        check(self.ctx.lib.sf_batch_readback(self.h, job, C.byref(planes)))
+        return out
+
 
 # ---------------------------------------------------------------------- escape time
 FAMILIES = ["Julia", "Mandelbrot", "BurningShip", "Newton", "Nova", "Phoenix"]

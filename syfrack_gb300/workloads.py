@@ -100,7 +100,10 @@ def mixed_batch(seed: int = 7, jobs: int = 64):
         if kind == 0:
             g = mixed_batch_graph("mandelbulb", int(rng.integers(2, 13)))
         elif kind == 1:
-            g = mixed_batch_graph("mandelbox", float(rng.uniform(-2.5, 2.5)))
+            s = float(rng.uniform(-2.5, 2.5))
+            while abs(s) < 1e-3:  # Scale factors below 1e-3 fail validation (validate.rs:187-196)
+                s = float(rng.uniform(-2.5, 2.5))
+            g = mixed_batch_graph("mandelbox", s)
         else:
             g = mixed_batch_graph("menger", int(rng.integers(3, 8)))
         dist = float(rng.uniform(2.5, 4.0))

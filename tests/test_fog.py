@@ -232,3 +232,116 @@ def test_fog_jobs_in_a_batch_equal_their_sessions(renderer):
         scale = max(1.0, float(np.abs(ref.accum[..., :3]).max()))
         assert np.abs(got.accum[..., :3] - ref.accum[..., :3]).max() <= 1e-4 * scale, i
     b.close()
+
+
+def test_oracle_volume_planes(oracle_mod):
+    """The oracle's film planes (pathtrace.wgsl:1243-1266): volume + surface = radiance,
+    moments >= 0, counts = samples; a clear scene has no volume part."""
+    scene = fog_bulb_scene()
+    cfg = RenderConfig(96, 64, 8, max_bounces=3, max_steps=256)
+    pix = np.stack([np.arange(0, 96, 3), np.full(32, 30)], 1).astype(np.uint32)
+    r = oracle_mod.OracleGraph(scene.graph).render(scene.desc(96, 64), cfg.desc(), pix, 0, 8, precision=32,
+                                                    planes=True)
+    np.testing.assert_allclose(r["volume"][:, :3] + r["surface"][:, :3], r["accum"], rtol=1e-5, atol=1e-6)
+    assert (r["volume"][:, 3] == 8).all() and (r["moments"][:, 3] == 8).all() and (r["surface"][:, 3] == 8).all()
+    assert (r["moments"][:, :3] >= 0).all() and r["volume"][:, :3].sum() > 0
+    clear = fog_bulb_scene()
+    clear.fog = None
+    c = oracle_mod.OracleGraph(clear.graph).render(clear.desc(96, 64), cfg.desc(), pix, 0, 8, precision=32,
+                                                    planes=True)
+    assert (c["volume"][:, :3] == 0).all() and (c["moments"][:, :3] == 0).all()
+    np.testing.assert_array_equal(c["surface"][:, :3], c["accum"])
+
+
+def _session_planes(renderer, scene, cfg):
+    from syfrack_gb300 import RenderSession
+
+    s = RenderSession(renderer, scene, cfg)
+    while not s.step(0):
+        pass
+    planes = s.film_planes()
+    s.close()
+    return planes
+
+
+@pytest.mark.gpu
+def test_fog_volume_planes_against_the_oracle(renderer, oracle_mod):
+    """The film's volume layer split on the device: both integrators keep it, it adds
+    up to the radiance, and it follows the f32 oracle's planes."""
+    scene = fog_bulb_scene()
+    out = {}
+    for integ in ("wavefront", "megakernel"):
+        cfg = RenderConfig(96, 64, 8, max_bounces=3, max_steps=256, pixel_tolerance=1.0, tile_size=64,
+                           samples_per_dispatch=4, integrator=integ)
+        out[integ] = _session_planes(renderer, scene, cfg)
+    wf, mk = out["wavefront"], out["megakernel"]
+    for k in ("volume", "moments", "surface"):
+        assert (wf[k][..., 3] == 8).all(), k
+        np.testing.assert_allclose(wf[k], mk[k], rtol=1e-4, atol=1e-5, err_msg=k)
+    np.testing.assert_allclose(wf["volume"][..., :3] + wf["surface"][..., :3], wf["accum"][..., :3], rtol=1e-5,
+                               atol=1e-5)
+    assert (wf["moments"][..., :3] >= 0).all()
+    assert wf["volume"][..., :3].mean() > 1e-3  # the fog's light reaches the camera
+    rng = np.random.default_rng(23)
+    pix = np.stack([rng.integers(0, 96, 128), rng.integers(0, 64, 128)], 1).astype(np.uint32)
+    ref = oracle_mod.OracleGraph(scene.graph).render(scene.desc(96, 64), cfg.desc(), pix, 0, 8, precision=32,
+                                                      planes=True)
+    for k in ("volume", "surface"):
+        mine = wf[k][pix[:, 1], pix[:, 0], :3] / 8
+        rmse = float(np.sqrt(np.mean((mine - ref[k][:, :3] / 8) ** 2)))
+        assert rmse <= 2e-2, (k, rmse)
+
+
+@pytest.mark.gpu
+def test_clear_scene_has_no_volume_part(renderer):
+    from syfrack_gb300 import workloads
+
+    cfg = workloads.mandelbox_pathtrace_config(width=64, height=36, spp=4, samples_per_dispatch=4)
+    p = _session_planes(renderer, workloads.mandelbox_scene(), cfg)
+    assert (p["volume"][..., :3] == 0).all() and (p["volume"][..., 3] == 4).all()
+    np.testing.assert_array_equal(p["surface"], p["accum"])
+
+
+@pytest.mark.gpu
+def test_fog_volume_planes_survive_a_checkpoint(renderer, tmp_path):
+    """A fog session saved after its first dispatch and resumed ends with the planes of
+    the uninterrupted render, bit for bit."""
+    from syfrack_gb300 import RenderSession
+
+    scene = fog_bulb_scene()
+    cfg = RenderConfig(64, 48, 8, max_bounces=3, max_steps=256, pixel_tolerance=1.0, tile_size=64,
+                       samples_per_dispatch=4, integrator="wavefront")
+    whole = _session_planes(renderer, scene, cfg)
+    s = RenderSession(renderer, scene, cfg)
+    s.step(0)
+    s.save(str(tmp_path / "ck"))
+    s.close()
+    r = RenderSession.resume(renderer, scene, cfg, str(tmp_path / "ck"))
+    while not r.step(0):
+        pass
+    got = r.film_planes()
+    r.close()
+    for k in ("accum", "volume", "moments", "surface"):
+        np.testing.assert_array_equal(got[k], whole[k], err_msg=k)
+
+
+@pytest.mark.gpu
+def test_fog_job_volume_planes_in_a_batch(renderer):
+    """A batched fog job keeps the volume layer split of its session."""
+    from syfrack_gb300 import Batch
+
+    cfg = RenderConfig(48, 32, 4, max_bounces=3, max_steps=256, pixel_tolerance=1.0, tile_size=48,
+                       samples_per_dispatch=4, integrator="wavefront")
+    fog = fog_bulb_scene()
+    clear = fog_bulb_scene()
+    clear.fog = None
+    clear.lights = clear.lights[:1]
+    b = Batch(renderer, [(clear, cfg), (fog, cfg)])
+    b.run(1, use_graph=False)
+    assert b.sync() == 0
+    got = b.film_planes(1)
+    b.close()
+    ref = _session_planes(renderer, fog, cfg)
+    for k in ("volume", "moments", "surface"):
+        np.testing.assert_allclose(got[k], ref[k], rtol=1e-4, atol=1e-4 * max(1.0, float(np.abs(ref[k]).max())),
+                                   err_msg=k)

@@ -159,7 +159,8 @@ def _c3_extent(kind, value):
 
 
 C3_FORMS = ([("mandelbulb", float(p)) for p in range(2, 13)] +
-            [("mandelbox", s) for s in (-2.5, -2.0, -1.5, -1.05, -0.8, -0.3, 0.0, 0.4, 0.9, 1.05, 1.5, 2.0, 2.5)] +
+            [("mandelbox", s) for s in (-2.5, -2.0, -1.5, -1.05, -0.8, -0.3, -0.01, 0.01, 0.4, 0.9, 1.05, 1.5, 2.0,
+                                        2.5)] +
             [("menger", lv) for lv in range(3, 8)])
 
 
@@ -189,3 +190,17 @@ def test_mixed_batch_forms_against_oracle(renderer, oracle_mod, kind, value):
     rel = np.abs(gpu["distance"] - ref32["distance"]) / np.maximum(np.abs(ref32["distance"]), 1.0)
     assert np.quantile(rel, 0.99) < 1e-5, np.quantile(rel, 0.99)
     assert (gpu["iterations"] == ref32["iterations"]).mean() >= 0.995
+
+
+def test_mixed_batch_scale_band_the_reference_rejects(renderer):
+    """Scale factors below 1e-3 in magnitude fail validation (validate.rs:187-196), so
+    the uneven batch draws its Mandelbox scales from -2.5..2.5 without that band."""
+    from syfrack_gb300 import workloads
+
+    with pytest.raises(SyfrackError) as e:
+        renderer.compile(workloads.mixed_batch_graph("mandelbox", 0.0))
+    assert e.value.status == 2
+    jobs = workloads.mixed_batch(seed=7, jobs=64)
+    scales = [n.kind.fields["factor"] for sc, _ in jobs for n in sc.graph.nodes if n.kind.name == "Scale"]
+    assert len(scales) >= 20 and min(abs(x) for x in scales) >= 1e-3
+    assert min(scales) < -1.0 and max(scales) > 1.0 and any(abs(x) < 1.05 for x in scales)

@@ -86,3 +86,29 @@ def test_uncommitted_tiles_keep_cleared_planes(renderer):
     assert (counts == 3.0).sum() == 16 * 16
     assert np.all(p["depth"][counts == 0] == -1.0)
     s.close()
+
+
+def test_fog_export_keeps_the_volume_planes(renderer, tmp_path):
+    """A fog scene exported tile by tile (with a checkpoint taken mid-export) equals the
+    resident session on every plane, the volume layer split included."""
+    from test_fog import fog_bulb_scene
+
+    scene = fog_bulb_scene()
+    c = cfg(w=70, h=45, spp=4, tile=16, spd=2)
+    ref = RenderSession(renderer, scene, c)
+    finish(ref)
+    expected = ref.film_planes()
+    ref.close()
+    assert expected["volume"][..., :3].max() > 0
+    ex = ExportSession(renderer, scene, c)
+    while ex.progress()["samples_max"] == 0:
+        ex.step(0)
+    d = str(tmp_path / "fog.state")
+    ex.save(d)
+    ex.close()
+    ex = ExportSession.resume(renderer, scene, c, d)
+    finish(ex)
+    got = ex.film_planes()
+    ex.close()
+    for k in ("accum", "depth", "aux", "volume", "moments", "surface"):
+        np.testing.assert_array_equal(got[k], expected[k], err_msg=k)
