@@ -282,6 +282,18 @@ __device__ __forceinline__ float2 mul2(float ax, float ay, float bx, float by) {
     return r;
 }
 
+// (a.x + b.x, a.y + b.y) as one packed add (add.rn.f32x2): each lane rounds as a
+// binary32 add.
+__device__ __forceinline__ float2 add2(float ax, float ay, float bx, float by) {
+    unsigned long long ra, rb, rd;
+    asm("mov.b64 %0, {%1, %2};" : "=l"(ra) : "f"(ax), "f"(ay));
+    asm("mov.b64 %0, {%1, %2};" : "=l"(rb) : "f"(bx), "f"(by));
+    asm("add.rn.f32x2 %0, %1, %2;" : "=l"(rd) : "l"(ra), "l"(rb));
+    float2 r;
+    asm("mov.b64 {%0, %1}, %2;" : "=f"(r.x), "=f"(r.y) : "l"(rd));
+    return r;
+}
+
 // Mandelbox: Iterate{BoxFold, Trap, SphereFold, Scale, AddOrigin} -> NormFence.
 // NORM_MIN0: the bundled trap (slot 0, Norm, Minimum) kept as min |p|^2.
 // The sphere fold's fr^2 / r^2 uses the fast reciprocal division (<= 2 ulp, the

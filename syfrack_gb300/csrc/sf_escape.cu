@@ -383,8 +383,12 @@ static __device__ __forceinline__ bool esc_chunk(const EscParams& p, EscOrbit& o
 }
 
 // The common tile: z^2 without twist (Julia, Mandelbrot or, SHIP, Burning Ship), the
-// default 12 stripes. The budget is checked once per chunk instead of per iteration;
-// the arithmetic is esc_step's, so the results are the same bit for bit.
+// default 12 stripes. The budget is checked once per chunk instead of per iteration.
+// The orbit's arithmetic rounds as esc_step's, bit for bit, with fewer instructions:
+// the squares x*x, y*y of |z|^2 serve the new real part (|x|*|x| = x*x exactly), the
+// imaginary part is fl(x*y) doubled (fl(x*y) + fl(y*x) = 2 fl(x*y), and
+// fl(|x|*|y|) = |fl(x*y)|), and the paired products and the sum with c are packed
+// f32x2 operations, each lane rounded as a binary32 multiply or add.
 template <bool TRAPS, bool SHIP>
 static __device__ __forceinline__ bool esc_chunk_z2(const EscParams& p, EscOrbit& o) {
     const uint32_t left = p.iterations - o.count;  // count <= iterations
@@ -394,7 +398,8 @@ static __device__ __forceinline__ bool esc_chunk_z2(const EscParams& p, EscOrbit
     int j = 0;
     bool escaped = false;
     for (; j < n; ++j) {
-        const float r2 = FA(FM(zx, zx), FM(zy, zy));
+        const float2 sq = mul2(zx, zy, zx, zy);  // (x*x, y*y)
+        const float r2 = FA(sq.x, sq.y);
         if (r2 > bt) {
             escaped = true;
             break;
@@ -402,13 +407,16 @@ static __device__ __forceinline__ bool esc_chunk_z2(const EscParams& p, EscOrbit
         if (TRAPS) {
             const float rinv = rsqrtf(r2);
             ring = fminf(ring, fabsf((r2 > 0.0f ? r2 * rinv : 0.0f) - tr));
-            if (r2 > 0.0f) stripe += sin_12(zx * rinv, zy * rinv);
+            if (r2 > 0.0f) {
+                const float2 u = mul2(zx, zy, rinv, rinv);  // z / |z|
+                stripe += sin_12(u.x, u.y);
+            }
         }
-        const float bx = SHIP ? fabsf(zx) : zx, by = SHIP ? fabsf(zy) : zy;
-        float nx, ny;
-        cmul_rn(bx, by, bx, by, nx, ny);
-        zx = FA(nx, cx);
-        zy = FA(ny, cy);
+        const float m = FM(zx, zy);
+        const float mm = SHIP ? fabsf(m) : m;
+        const float2 z = add2(FS(sq.x, sq.y), FA(mm, mm), cx, cy);
+        zx = z.x;
+        zy = z.y;
     }
     o.zx = zx;
     o.zy = zy;

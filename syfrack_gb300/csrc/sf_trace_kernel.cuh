@@ -120,67 +120,69 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
 
     const uint32_t regen = tl.regen ? tl.regen : 1u;
     while (true) {
-        // Idle lanes take new segments together once `regen` of them are idle (or no
-        // lane is marching): the segment set-up then runs for many lanes at once
-        // instead of for one or two lanes in most iterations.
+        // Two votes per DE call decide the warp's next move: all lanes done ends the
+        // loop; idle lanes take new segments together once `regen` of them are idle (or
+        // no lane is marching), so the segment set-up runs for many lanes at once and
+        // the fetch (a vote and one atomic) only runs when the warp refills.
         const uint32_t idle = __ballot_sync(FULL_MASK, state == TL_IDLE);
-        const uint32_t active = __ballot_sync(FULL_MASK, state == TL_MARCH || state == TL_CAND || state == TL_NORMAL);
-        const bool refill = idle && ((uint32_t)__popc(idle) >= regen || active == 0);
-        uint32_t w = warp_fetch(tl.work_counter, refill && state == TL_IDLE);
-        if constexpr (LANE_STATS) {
-            if (t_dry == 0 && __any_sync(FULL_MASK, refill && state == TL_IDLE && w >= total)) t_dry = clock64();
-        }
-        if (refill && state == TL_IDLE) {
-            if (w >= total) {
-                state = TL_DONE;
-            } else {
-                if (first) {
-                    shadow = w >= n_cont;
-                    item = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
+        const uint32_t done = __ballot_sync(FULL_MASK, state == TL_DONE);
+        if (done == FULL_MASK) break;
+        if (idle && ((uint32_t)__popc(idle) >= regen || (idle | done) == FULL_MASK)) {  // warp-uniform
+            const uint32_t w = warp_fetch(tl.work_counter, state == TL_IDLE);
+            if constexpr (LANE_STATS) {
+                if (t_dry == 0 && __any_sync(FULL_MASK, state == TL_IDLE && w >= total)) t_dry = clock64();
+            }
+            if (state == TL_IDLE) {
+                if (w >= total) {
+                    state = TL_DONE;
                 } else {
-                    const uint32_t it = tl.resume[w];
-                    item = it & 0x7fffffffu;
-                    shadow = (it >> 31) != 0;
-                }
-                path = shadow ? item % cap : item;
-                if constexpr (MULTI) {
-                    const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
-                    Pl = job.prog;
-                    Sl = job.scene;
-                    cone = Sl->pixel_cone;
-                    tol = Sl->pixel_tolerance;
-                    accept = hit_accept(*Sl);
-                    absolute = hit_absolute(*Sl);
-                    safety = Sl->step_scale;
-                    max_steps = Sl->max_steps;
-                }
-                float4 o = shadow ? soa.sh_o[item] : soa.o[path];
-                float4 d = shadow ? soa.sh_d[item] : soa.d[path];
-                // the march state: set by the stage that made the ray, or saved by the
-                // previous launch at its step quantum
-                const uint32_t row = shadow ? cap + item : item;
-                const float4 a = soa.m0[row], b = soa.m1[row];
-                m.ro = mk3(o.x, o.y, o.z);
-                m.rd = mk3(d.x, d.y, d.z);
-                m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
-                m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
-                li = soa.m2[row];
-                if (first) {
-                    if (shadow) n_shseg++;
-                    else n_seg++;
-                }
-                budget = quantum;
-                state = TL_MARCH;
-                int r = march_check(m, max_steps, accept);
-                if (r == MARCH_HIT) {
-                    if (shadow) finish(MARCH_HIT);
-                    else { m.t = m.cand_t; state = TL_CAND; }
-                } else if (r != MARCH_CONTINUE) {
-                    finish(r);
+                    if (first) {
+                        shadow = w >= n_cont;
+                        item = shadow ? tl.q.shadow[w - n_cont] : (tl.q.cont ? tl.q.cont[w] : w);
+                    } else {
+                        const uint32_t it = tl.resume[w];
+                        item = it & 0x7fffffffu;
+                        shadow = (it >> 31) != 0;
+                    }
+                    path = shadow ? item % cap : item;
+                    if constexpr (MULTI) {
+                        const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
+                        Pl = job.prog;
+                        Sl = job.scene;
+                        cone = Sl->pixel_cone;
+                        tol = Sl->pixel_tolerance;
+                        accept = hit_accept(*Sl);
+                        absolute = hit_absolute(*Sl);
+                        safety = Sl->step_scale;
+                        max_steps = Sl->max_steps;
+                    }
+                    float4 o = shadow ? soa.sh_o[item] : soa.o[path];
+                    float4 d = shadow ? soa.sh_d[item] : soa.d[path];
+                    // the march state: set by the stage that made the ray, or saved by the
+                    // previous launch at its step quantum
+                    const uint32_t row = shadow ? cap + item : item;
+                    const float4 a = soa.m0[row], b = soa.m1[row];
+                    m.ro = mk3(o.x, o.y, o.z);
+                    m.rd = mk3(d.x, d.y, d.z);
+                    m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
+                    m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
+                    li = soa.m2[row];
+                    if (first) {
+                        if (shadow) n_shseg++;
+                        else n_seg++;
+                    }
+                    budget = quantum;
+                    state = TL_MARCH;
+                    int r = march_check(m, max_steps, accept);
+                    if (r == MARCH_HIT) {
+                        if (shadow) finish(MARCH_HIT);
+                        else { m.t = m.cand_t; state = TL_CAND; }
+                    } else if (r != MARCH_CONTINUE) {
+                        finish(r);
+                    }
                 }
             }
         }
-        if (__all_sync(FULL_MASK, state == TL_DONE)) break;
         if (state == TL_MARCH || state == TL_CAND || state == TL_NORMAL) {
             float3 q = m.ro + m.rd * m.t;
             if (state == TL_NORMAL) q = q + tetra_offset(tap) * hstep;
