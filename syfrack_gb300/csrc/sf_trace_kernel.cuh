@@ -69,27 +69,40 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     const uint32_t quantum = tl.quantum ? tl.quantum : 0xffffffffu;
     const DeProgram* Pl = &P;
     const DevScene* Sl = &S;
-    float accept = 0.f, safety = 0.f, cone = 0.f, tol = 0.f;
-    uint32_t max_steps = 0;
-    bool absolute = false;
-    if constexpr (!MULTI) {
-        accept = hit_accept(S);
-        absolute = hit_absolute(S);
-        safety = S.step_scale;
-        max_steps = S.max_steps;
-        cone = S.pixel_cone;
-        tol = S.pixel_tolerance;
-    }
+    // a batch lane's job constants (registers); the single-job kernel reads the staged
+    // scene (shared memory) at each use instead, which keeps them out of registers
+    float accept_j = 0.f, safety_j = 0.f, cone_j = 0.f, tol_j = 0.f;
+    uint32_t max_steps_j = 0;
+    bool absolute_j = false;
+#define TR_ACCEPT (MULTI ? accept_j : hit_accept(S))
+#define TR_ABSOLUTE (MULTI ? absolute_j : hit_absolute(S))
+#define TR_SAFETY (MULTI ? safety_j : S.step_scale)
+#define TR_MAX_STEPS (MULTI ? max_steps_j : S.max_steps)
+#define TR_CONE (MULTI ? cone_j : S.pixel_cone)
+#define TR_TOL (MULTI ? tol_j : S.pixel_tolerance)
     const uint32_t cap = soa.capacity;
 
     // item: the continuation path, or the shadow row (k * cap + path) of a shadow segment
-    uint32_t state = TL_IDLE, path = 0, item = 0, li = SF_NO_LIGHT, tap = 0, budget = 0;
+    uint32_t state = TL_IDLE, path = 0, item = 0, li = SF_NO_LIGHT, budget = 0;
     bool shadow = false;
     March m{};  // set by each refill before use
-    float3 grad = mk3(0.f, 0.f, 0.f);
-    float hstep = 0.f;
-    uint32_t hit_w = 0;  // iterations | material << 16 of the surface hit whose normal is being tapped
-    uint32_t n_eval = 0, n_iter = 0, n_seg = 0, n_shseg = 0, n_wcall = 0;
+    // The normal taps of a surface hit overlay march fields that are dead once the hit
+    // is recorded: the gradient (omega, previous radius, step length), the tap step
+    // (candidate error), the hit word iterations | material << 16 (steps) and the tap
+    // index (the quantum budget).
+    float& gx = m.omega;
+    float& gy = m.prev_radius;
+    float& gz = m.step_len;
+    float& hstep = m.cand_err;
+    uint32_t& hit_w = m.i;
+    uint32_t& tap = budget;
+    uint32_t n_eval = 0, n_iter = 0, n_wcall = 0;
+    // every item of a round's first launch is one segment: the queue counts are the
+    // segment statistics (one thread adds them)
+    if (first && blockIdx.x == 0 && threadIdx.x == 0) {
+        atomicAdd(&stats[SF_STAT_SEGMENTS], (unsigned long long)total);
+        atomicAdd(&stats[SF_STAT_SHADOW_SEGMENTS], (unsigned long long)(total - n_cont));
+    }
     unsigned long long n_slots = 0;
     // LANE_STATS: the warp's cycles, and those after its first failed fetch (the tail,
     // when the launch's work is exhausted and lanes idle beside the last segments)
@@ -112,8 +125,8 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         soa.hit[path] = make_uint4(__float_as_uint(m.t), m.i, SF_NO_LIGHT, SF_HF_HIT);
         soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
         hit_w = smp.iter | (smp.material << 16);  // stored with the normal after the last tap
-        hstep = fmaxf(m.t * cone * 0.5f, 1e-4f) * tol;
-        grad = mk3(0.f, 0.f, 0.f);
+        hstep = fmaxf(m.t * TR_CONE * 0.5f, 1e-4f) * TR_TOL;
+        gx = gy = gz = 0.f;
         tap = 0;
         state = TL_NORMAL;
     };
@@ -149,12 +162,12 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                         const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
                         Pl = job.prog;
                         Sl = job.scene;
-                        cone = Sl->pixel_cone;
-                        tol = Sl->pixel_tolerance;
-                        accept = hit_accept(*Sl);
-                        absolute = hit_absolute(*Sl);
-                        safety = Sl->step_scale;
-                        max_steps = Sl->max_steps;
+                        cone_j = Sl->pixel_cone;
+                        tol_j = Sl->pixel_tolerance;
+                        accept_j = hit_accept(*Sl);
+                        absolute_j = hit_absolute(*Sl);
+                        safety_j = Sl->step_scale;
+                        max_steps_j = Sl->max_steps;
                     }
                     float4 o = shadow ? soa.sh_o[item] : soa.o[path];
                     float4 d = shadow ? soa.sh_d[item] : soa.d[path];
@@ -167,13 +180,9 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
                     m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
                     li = soa.m2[row];
-                    if (first) {
-                        if (shadow) n_shseg++;
-                        else n_seg++;
-                    }
                     budget = quantum;
                     state = TL_MARCH;
-                    int r = march_check(m, max_steps, accept);
+                    int r = march_check(m, TR_MAX_STEPS, TR_ACCEPT);
                     if (r == MARCH_HIT) {
                         if (shadow) finish(MARCH_HIT);
                         else { m.t = m.cand_t; state = TL_CAND; }
@@ -194,7 +203,7 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             n_iter += s.iter;
             if constexpr (FORM == SF_FORM_ANY) {
                 // a flagged march or candidate sample near acceptance: the exact sample
-                if (state != TL_NORMAL && needs_exact(s, m.t, safety, accept, absolute)) {
+                if (state != TL_NORMAL && needs_exact(s, m.t, TR_SAFETY, TR_ACCEPT, TR_ABSOLUTE)) {
                     if constexpr (MULTI) s = de_raw_exact(*Pl, q);
                     else s = de_raw_exact(P, q);
                     n_eval++;
@@ -212,24 +221,27 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                 }
             }
             if (state == TL_NORMAL) {
-                grad = grad + tetra_offset(tap) * s.d;
+                const float3 off = tetra_offset(tap);
+                gx = fmaf(off.x, s.d, gx);
+                gy = fmaf(off.y, s.d, gy);
+                gz = fmaf(off.z, s.d, gz);
                 if (++tap == 4) {
                     // the taps of a hit end in the launch that found it (no quantum applies)
-                    const float3 n = wnormalize(grad);
+                    const float3 n = wnormalize(mk3(gx, gy, gz));
                     soa.hit_n[path] = make_float4(n.x, n.y, n.z, __uint_as_float(hit_w));
                     state = TL_IDLE;
                 }
             } else if (state == TL_CAND) {
                 surface_hit(s);
             } else {
-                int r = march_update(m, s.d, s.flags, safety, accept, absolute);
+                int r = march_update(m, s.d, s.flags, TR_SAFETY, TR_ACCEPT, TR_ABSOLUTE);
                 if (r == MARCH_HIT) {
                     if (shadow) finish(MARCH_HIT);
                     else surface_hit(s);
                 } else if (r != MARCH_CONTINUE) {
                     finish(r);
                 } else {
-                    r = march_check(m, max_steps, accept);
+                    r = march_check(m, TR_MAX_STEPS, TR_ACCEPT);
                     if (r == MARCH_HIT) {  // candidate accepted at the step budget
                         if (shadow) finish(MARCH_HIT);
                         else { m.t = m.cand_t; state = TL_CAND; }
@@ -250,8 +262,6 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
     }
     warp_stat(&stats[SF_STAT_DE_EVALS], n_eval);
     warp_stat(&stats[SF_STAT_DE_ITERS], n_iter);
-    warp_stat(&stats[SF_STAT_SEGMENTS], n_seg + n_shseg);
-    warp_stat(&stats[SF_STAT_SHADOW_SEGMENTS], n_shseg);
     if constexpr (LANE_STATS) {
         warp_stat(&stats[SF_STAT_WARP_DE_CALLS], n_wcall);
         warp_stat(&stats[SF_STAT_ITER_SLOTS], n_slots);
@@ -261,6 +271,12 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
             atomicAdd(&stats[SF_STAT_TAIL_CYCLES], (unsigned long long)(t_dry ? t_end - t_dry : 0));
         }
     }
+#undef TR_ACCEPT
+#undef TR_ABSOLUTE
+#undef TR_SAFETY
+#undef TR_MAX_STEPS
+#undef TR_CONE
+#undef TR_TOL
 }
 
 template <int FORM>
