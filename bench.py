@@ -174,6 +174,7 @@ def reduce_ranks(dist, elapsed, work, device):
 
 
 def run_ours(args):
+    spp_step = args.spp_per_step
     import ctypes as C
 
     n_ranks, rank, local_rank = dist_env()
@@ -191,9 +192,9 @@ def run_ours(args):
     ctx = GpuContext(device=local_rank if n_ranks > 1 else 0)
     renderer = Renderer(ctx)
     scene = workloads.mandelbox_scene()
-    spp_total = SPP_PER_STEP * (args.warmup + args.steps)
+    spp_total = spp_step * (args.warmup + args.steps)
     cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=spp_total,
-                                               samples_per_dispatch=SPP_PER_STEP)
+                                               samples_per_dispatch=spp_step)
     sess = RenderSession(renderer, scene, cfg)
     sess.set_launch(args.min_blocks, args.quantum, args.regen)
     tile = (0, 0, cfg.width, cfg.height)
@@ -201,7 +202,7 @@ def run_ours(args):
     check(ctx.lib.sf_device_fp32_peak(ctx.h, C.byref(peak)))
 
     def step(k):
-        sess.dispatch((*tile, k * SPP_PER_STEP), SPP_PER_STEP)
+        sess.dispatch((*tile, k * spp_step), spp_step)
 
     for k in range(args.warmup):
         step(k)
@@ -242,11 +243,11 @@ def run_ours(args):
     # warp-level DE calls and iteration slots (lane use), on a separate session
     ctx.set_profiling(True, lane_stats=True)
     ctx.reset_stats()
-    lane_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=SPP_PER_STEP,
-                                                    samples_per_dispatch=SPP_PER_STEP)
+    lane_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=spp_step,
+                                                    samples_per_dispatch=spp_step)
     lane_sess = RenderSession(renderer, scene, lane_cfg)
     lane_sess.set_launch(args.min_blocks, args.quantum, args.regen)
-    lane_sess.dispatch(tile + (0,), SPP_PER_STEP)
+    lane_sess.dispatch(tile + (0,), spp_step)
     lane_sess.sync(600000)
     lst = ctx.stats()
     lane_sess.close()
@@ -256,7 +257,7 @@ def run_ours(args):
     # end to end through the public API: one full 64-spp frame (8 dispatches of 8 spp)
     # rendered from host descriptions, film read back
     e2e_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=64,
-                                                   samples_per_dispatch=SPP_PER_STEP)
+                                                   samples_per_dispatch=spp_step)
     ctx.reset_stats()
     if dist:
         dist.barrier()
@@ -270,7 +271,7 @@ def run_ours(args):
         e2e_s, e2e_segs = reduce_ranks(dist, e2e_s, e2e_segs, "cuda")
     e2e = e2e_segs / e2e_s / 1e6
     px = e2e_cfg.width * e2e_cfg.height
-    e2e_steps = e2e_cfg.samples_per_pixel // SPP_PER_STEP
+    e2e_steps = max(1, e2e_cfg.samples_per_pixel // spp_step)
     d2h = px * (16 + 4 + 16)
     h2d = C.sizeof(__import__("syfrack_gb300").abi.sf_scene_desc) + 4096
     cone = None
@@ -288,15 +289,16 @@ def run_ours(args):
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Mandelbox scene; no dataset)",
             "config": {"workload": WORKLOAD if (cfg.width, cfg.height) == (1280, 720) else f"profiling case {cfg.width}x{cfg.height}",
-                       "width": cfg.width, "height": cfg.height, "spp_per_step": SPP_PER_STEP,
+                       "width": cfg.width, "height": cfg.height, "spp_per_step": spp_step,
                        "hit_rule": f"fixed epsilon {cfg.hit_epsilon:g} (radius <= epsilon)",
-                       "paths_per_step": cfg.width * cfg.height * SPP_PER_STEP, "max_bounces": cfg.max_bounces,
+                       "paths_per_step": cfg.width * cfg.height * spp_step, "max_bounces": cfg.max_bounces,
                        "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
                        "launch": {"min_blocks_per_sm": args.min_blocks, "quantum": args.quantum,
                                   "regen": args.regen},
-                       "l2": "inputs larger than L2 (path state 1.9 GB per step)",
+                       "l2": f"inputs larger than L2 (path state {cfg.width * cfg.height * spp_step * 260 / 1e9:.1f} GB "
+                             f"per step)",
                        "segments_per_step": segs_all / args.steps,
-                       "pixel_samples_per_s": cfg.width * cfg.height * SPP_PER_STEP * args.steps * n_ranks
+                       "pixel_samples_per_s": cfg.width * cfg.height * spp_step * args.steps * n_ranks
                        / (ms_max * 1e-3)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                     "d2h_bytes_per_step": d2h // e2e_steps,
@@ -339,15 +341,16 @@ def run_ours(args):
 def pathtrace_variant(renderer, ctx, scene, args, rule, steps=5, warmup=2):
     """The headline frame with another hit rule ("cone": the reference's
     cone-relative test at pixel tolerance 1), device-timed like the headline."""
+    spp_step = args.spp_per_step
     from syfrack_gb300 import RenderSession, workloads
 
     cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height,
-                                               spp=SPP_PER_STEP * (steps + warmup),
-                                               samples_per_dispatch=SPP_PER_STEP, rule=rule)
+                                               spp=spp_step * (steps + warmup),
+                                               samples_per_dispatch=spp_step, rule=rule)
     sess = RenderSession(renderer, scene, cfg)
     sess.set_launch(args.min_blocks, args.quantum, args.regen)
     for k in range(warmup):
-        sess.dispatch((0, 0, cfg.width, cfg.height, k * SPP_PER_STEP), SPP_PER_STEP)
+        sess.dispatch((0, 0, cfg.width, cfg.height, k * spp_step), spp_step)
     sess.sync(600000)
     ctx.reset_stats()
     import torch
@@ -356,7 +359,7 @@ def pathtrace_variant(renderer, ctx, scene, args, rule, steps=5, warmup=2):
     ev0, ev1 = torch.cuda.Event(enable_timing=True), torch.cuda.Event(enable_timing=True)
     ev0.record(stream)
     for k in range(warmup, warmup + steps):
-        sess.dispatch((0, 0, cfg.width, cfg.height, k * SPP_PER_STEP), SPP_PER_STEP)
+        sess.dispatch((0, 0, cfg.width, cfg.height, k * spp_step), spp_step)
     ev1.record(stream)
     ev1.synchronize()
     ms = ev0.elapsed_time(ev1)
@@ -890,6 +893,8 @@ def main():
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
+    ap.add_argument("--spp-per-step", type=int, default=8,
+                    help="samples per pixel of the frame rendered by one step (one dispatch)")
     ap.add_argument("--no-extras", action="store_true",
                     help="the headline only (without the other configurations' summaries)")
     ap.add_argument("--workload", default="pathtrace",

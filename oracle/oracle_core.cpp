@@ -675,7 +675,9 @@ static DistState<R> eval_instances(const Graph& g, const sf_node& n, V3<R> p, bo
         if (skip && bound > margin) {
             d = DistState<R>{bound, 0, 0, {INF, INF, INF, INF}, 1};
         } else {
-            d = eval_raw(g, child, q, fast, depth + 1);
+            // the template of a search that may not skip runs exactly (graph_wgsl.rs:
+            // the `_exact` variant), so fast mode passes into it only from a skipping one
+            d = eval_raw(g, child, q, skip, depth + 1);
             d.d = r_max(d.d * smin, bound);
         }
         if (d.d < best.d || (d.d == best.d && index < chosen)) {

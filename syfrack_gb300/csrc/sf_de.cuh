@@ -305,35 +305,44 @@ __device__ __forceinline__ float2 add2(float ax, float ay, float bx, float by) {
 template <bool NORM_MIN0, bool CLAMPED>
 __device__ __forceinline__ DeRaw de_box_t(const FormParams& f, float3 p) {
     DeRaw s = raw_empty();
-    const float3 c = p;
     float dr = 1.0f;
     const uint32_t n = f.iterations;
     const float l = f.limit, bt = f.bailout_t, mr2 = f.min_radius2, fr2 = f.fixed_radius2, kmin = f.fold_k_min;
     const float sc = f.scale, asc = f.abs_scale;
     const bool sq = f.trap_squared != 0;
     float t0 = SF_INF;
+    // The loop carries w = -p: the box fold 2 clamp(p) - p is then fma(clamp(w), -2, w)
+    // (clamp(-p) = -clamp(p) exactly), one packed FMA for x and y, and the next -p is
+    // fold * (-k scale) + (-c). Every result is the exact negation of the same
+    // operation on p, so the iteration rounds as it does on p.
+    const float ncx = -p.x, ncy = -p.y, ncz = -p.z;
+    float wx = ncx, wy = ncy, wz = ncz;
     uint32_t i = 0;
 #pragma unroll 2
     for (; i < n; ++i) {
-        if (dot3(p, p) > bt) break;
-        p = clamp3(p, -l, l) * 2.0f - p;
-        float r2 = dot3(p, p);
+        if (fmaf(wz, wz, fmaf(wx, wx, wy * wy)) > bt) break;  // dot3(p, p)
+        const float2 fxy = fma2_scalar(fminf(fmaxf(wx, -l), l), fminf(fmaxf(wy, -l), l), -2.0f, wx, wy);
+        const float fz = fmaf(fminf(fmaxf(wz, -l), l), -2.0f, wz);
+        const float3 q = mk3(fxy.x, fxy.y, fz);  // the folded point
+        float r2 = dot3(q, q);
         if (NORM_MIN0) {
             t0 = fminf(t0, r2);
         } else {
-            float v = sq ? r2 : trap_measure(f.trap_measure, p);
+            float v = sq ? r2 : trap_measure(f.trap_measure, q);
             trap_update(s, f.trap_slot, f.trap_mode, v);
         }
-        const float q = fr2 * rcp_approx(r2);
-        const float k = CLAMPED ? fminf(kmin, fmaxf(q, 1.0f)) : (r2 < mr2 ? kmin : fmaxf(q, 1.0f));
+        const float qk = fr2 * rcp_approx(r2);
+        const float k = CLAMPED ? fminf(kmin, fmaxf(qk, 1.0f)) : (r2 < mr2 ? kmin : fmaxf(qk, 1.0f));
         // sphere fold, Scale and AddOrigin as one multiply-add per component
-        const float2 kk = mul2(k, k, sc, asc);  // (k * scale, k * |scale|)
-        const float2 pxy = fma2_scalar(p.x, p.y, kk.x, c.x, c.y);
-        p = mk3(pxy.x, pxy.y, fmaf(p.z, kk.x, c.z));
+        const float2 kk = mul2(k, k, -sc, asc);  // (-k * scale, k * |scale|)
+        const float2 wxy = fma2_scalar(q.x, q.y, kk.x, ncx, ncy);
+        wx = wxy.x;
+        wy = wxy.y;
+        wz = fmaf(q.z, kk.x, ncz);
         dr = fmaf(dr, kk.y, 1.0f);
     }
     s.iter = i;
-    s.d = (sqrt_fast(dot3(p, p)) - f.fence[0]) * rcp_approx(fabsf(dr));
+    s.d = (sqrt_fast(fmaf(wz, wz, fmaf(wx, wx, wy * wy))) - f.fence[0]) * rcp_approx(fabsf(dr));
     s.material = f.material;
     if (NORM_MIN0) s.t0 = sqrt_fast(t0);
     else if (sq) trap_sqrt(s, f.trap_slot);
@@ -680,7 +689,10 @@ __device__ __forceinline__ bool inst_next(InstFrame& F) {
 // reference's de_sample (skippable Bounded branches skipped outside their margin,
 // the sample flagged); exact = true is de_sample_exact (every branch evaluated).
 static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bool exact) {
-    InstFrame F;  // the copy search in flight (one level: templates hold no Instances)
+    // the copy searches in flight, one per nesting level (eval.rs:808 recurses into the
+    // template of each copy; here the template's ops run between INST_BEGIN and INST_END)
+    InstFrame frames[SF_MAX_INST_DEPTH];
+    int fd = -1;
     PState s;
     s.p = c; s.dr = 1.0f; s.iter = 0; s.t0 = s.t1 = s.t2 = s.t3 = SF_INF;
     uint32_t loop_count[SF_MAX_LOOP_DEPTH];
@@ -748,7 +760,8 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
             break;
         }
         case SF_OP_INST_BEGIN: {
-            if (sp >= SF_MAX_DIST_STACK) { pc = op.b; break; }
+            if (sp >= SF_MAX_DIST_STACK || fd + 1 >= SF_MAX_INST_DEPTH) { pc = op.b; break; }
+            InstFrame& F = frames[++fd];
             const float* base = reinterpret_cast<const float*>(P.inst_data) + op.c;
             F.rows = base;
             F.bvh = base + size_t(op.a) * 12u;
@@ -766,6 +779,7 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
                     e.flags = 1;
                     stack[sp++] = e;
                     pc = op.b;
+                    fd--;
                     break;
                 }
             }
@@ -785,16 +799,19 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
             if (inst_next(F)) { c = F.q; break; }  // the template follows with the copy's point
             stack[sp++] = F.best;
             pc = op.b;
+            fd--;
             break;
         }
         case SF_OP_INST_END: {
-            if (sp < 1) break;
+            if (sp < 1 || fd < 0) break;
+            InstFrame& F = frames[fd];
             DeRaw d = stack[--sp];
             d.d = fmaxf(d.d * F.w, F.fence);
             if (d.d < F.best.d || (d.d == F.best.d && F.j < F.chosen)) { F.best = d; F.chosen = F.j; }
             if (inst_next(F)) { c = F.q; pc = op.a; break; }  // next copy: the template again
-            c = F.c;
+            c = F.c;  // the point the search ran at (an outer copy's local point, nested)
             stack[sp++] = F.best;
+            fd--;
             break;
         }
         case SF_OP_BOUND_END:

@@ -367,7 +367,12 @@ struct Lowerer {
     std::vector<float>* inst = nullptr;
     std::string err;
     int stack_depth = 0, max_stack = 0;
-    bool in_template = false;
+    // Instances templates being lowered (at most SF_MAX_INST_DEPTH nested), and whether
+    // the innermost runs exactly: the template of a copy search that may not skip is
+    // the reference's `_exact` variant (graph_wgsl.rs:744-790), so no Bounded or
+    // Instances node inside it skips either
+    int template_depth = 0;
+    bool template_exact = false;
 
     bool push(const DeOp& op) {
         if (P.n_ops >= SF_MAX_OPS) { err = "graph too large for the device program"; return false; }
@@ -452,7 +457,7 @@ struct Lowerer {
             return push(o);
         }
         if (n.kind == SF_NODE_BOUNDED) {
-            if (n.enabled && !unsafe_bounds.count(src)) {
+            if (n.enabled && !unsafe_bounds.count(src) && !template_exact) {
                 // skippable bound (graph_wgsl.rs:800-814): bound first, detail only near it
                 if (!chain(ha, a)) return false;
                 const uint32_t at = P.n_ops;
@@ -477,7 +482,7 @@ struct Lowerer {
         }
         if (n.kind == SF_NODE_INSTANCES) {
             if (!n.enabled) return dist(ha, a, guard + 1);  // passes its template through (eval.rs:816)
-            if (in_template) { err = "Instances nested in an Instances template are not supported on the device"; return false; }
+            if (template_depth >= SF_MAX_INST_DEPTH) { err = "Instances nested deeper than 3 levels"; return false; }
             if (!ha) {  // no template: the copies are empty (eval.rs:752-755)
                 stack_depth++;
                 max_stack = std::max(max_stack, stack_depth);
@@ -488,12 +493,16 @@ struct Lowerer {
             o.a = n.u[1];
             o.c = uint32_t(inst->size());
             std::memcpy(o.f, n.f, 4 * sizeof(float));
-            o.f[4] = unsafe_bounds.count(src) ? 0.f : 1.f;
+            const bool skippable = !unsafe_bounds.count(src) && !template_exact;
+            o.f[4] = skippable ? 1.f : 0.f;
             pack_instances(g.placements.data() + n.u[0], n.u[1], n.f, *inst);
             if (!push(o)) return false;
-            in_template = true;
+            const bool outer_exact = template_exact;
+            template_depth++;
+            template_exact = !skippable;
             const bool ok = dist(ha, a, guard + 1);
-            in_template = false;
+            template_depth--;
+            template_exact = outer_exact;
             if (!ok) return false;
             DeOp e = mk(SF_OP_INST_END);
             e.a = at;

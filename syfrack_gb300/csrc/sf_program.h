@@ -17,6 +17,7 @@
 #define SF_MAX_OPS 96
 #define SF_MAX_LOOP_DEPTH 4
 #define SF_MAX_DIST_STACK 6
+#define SF_MAX_INST_DEPTH 3  // nested Instances levels (MAX_DEPTH, graph/mod.rs:41)
 
 // Opcodes of the generic interpreter. Point and fence operations use the node
 // kind (enum sf_node_kind) as their code; control codes start at 100.
@@ -41,7 +42,8 @@ enum {
     // c = offset of the node's block in inst_data (12 floats of inverse affine rows per
     // placement, then 8 floats per hierarchy node: centre, half, escape, placement or -1),
     // f0..2 = half, f3 = margin, f4 = 1 when the copies may be skipped (fast). The ops
-    // between INST_BEGIN and INST_END evaluate the template at a copy's local point.
+    // between INST_BEGIN and INST_END evaluate the template at a copy's local point;
+    // they may hold further Instances, nested up to SF_MAX_INST_DEPTH levels.
     SF_OP_INST_BEGIN = 111,
     SF_OP_INST_END = 112    // a = index of the matching INST_BEGIN
 };

@@ -100,7 +100,51 @@ def brute_force_torus(points, placements):
     return best
 
 
+def nested_copies():
+    """Three nested Instances levels over a unit sphere: the innermost holds two
+    rotated, scaled copies; the middle one three; the outer two (12 spheres)."""
+    levels = [
+        [((0.9, 0.0, 0.1), (10.0, 0.0, 25.0), (0.5, 0.6, 0.55)), ((-0.8, 0.3, 0.0), (0.0, 35.0, 0.0), (0.45, 0.5, 0.5))],
+        [((0.0, 0.0, 0.0), (0.0, 0.0, 0.0), (1.0, 1.0, 1.0)), ((0.2, 1.8, 0.0), (0.0, 0.0, 90.0), (0.8, 0.8, 0.9)),
+         ((-0.3, -1.7, 0.4), (20.0, 0.0, -30.0), (0.9, 1.0, 0.8))],
+        [((-1.6, 0.0, 0.0), (0.0, 15.0, 0.0), (1.0, 0.9, 1.0)), ((1.7, 0.2, 0.5), (-25.0, 0.0, 10.0), (0.85, 0.85, 0.85))],
+    ]
+    halves = [1.6, 3.2, 4.5]
+    g = minimal()
+    last = 1
+    for placements, half in zip(levels, halves):
+        last = add(g, Kind("Instances", placements=placements, half=[half] * 3, margin=0.1), [last])
+    return to_output(g, last), list(zip(levels, halves))
+
+
+def brute_force_nested(points, levels):
+    """eval.rs:749-814 unrolled: each level's copy is max(template(q) * min scale,
+    its Box fence), the nearest copy wins; the innermost template is the unit sphere."""
+    def level(p, k):
+        if k < 0:
+            return np.linalg.norm(p, axis=1) - 1.0
+        placements, half = levels[k]
+        best = np.full(len(p), np.inf)
+        for pl in placements:
+            q, sc = local_points(p, pl)
+            best = np.minimum(best, np.maximum(level(q, k - 1) * sc.min(), box_fence(q, half, sc)))
+        return best
+    return level(np.asarray(points, np.float64), len(levels) - 1)
+
+
 # ---------------------------------------------------------------- CPU: oracle and host
+
+def test_nested_copies_match_the_composed_union(oracle_mod):
+    """Copies of copies of copies (eval.rs:808 recurses into each copy's template, up
+    to three levels) equal the brute-force composition of the levels."""
+    g, levels = nested_copies()
+    pts = grid_points() * 1.6
+    og = oracle_mod.OracleGraph(g)
+    np.testing.assert_allclose(og.de(pts, precision=64)["distance"], brute_force_nested(pts, levels), atol=1e-9,
+                               rtol=0)
+    np.testing.assert_allclose(og.de(pts, precision=32)["distance"], brute_force_nested(pts, levels), atol=2e-5,
+                               rtol=0)
+
 
 def test_hierarchy_matches_brute_force_union(oracle_mod):
     g, placements = big_hierarchy()
@@ -149,9 +193,7 @@ def test_validation():
         g.validate()
     assert e.value.status == 2  # SF_ERR_GRAPH
     g.node(last).enabled = False
-    with pytest.raises(SyfrackError) as e:  # three levels are valid, but the device runs one
-        g.validate()
-    assert e.value.status == 3  # SF_ERR_UNSUPPORTED
+    assert g.validate()["form"] == "generic"  # three levels are valid, and the device runs them
     for bad in ([((0, 0, 0), (0, 0, 0), (0.0, 1, 1))], [], [((2000.0, 0, 0), (0, 0, 0), (1, 1, 1))],
                 [((0, 0, 0), (200.0, 0, 0), (1, 1, 1))]):
         g = minimal()
@@ -224,15 +266,30 @@ def test_device_copies_march_and_film(renderer, oracle_mod):
 
 
 @pytest.mark.gpu
-def test_nested_copies_are_refused(renderer):
-    g = minimal()
-    inner = add(g, Kind("Instances", placements=[((0, 0, 0), (0, 0, 0), (1, 1, 1))], half=[2.0] * 3, margin=0.1), [1])
-    outer = add(g, Kind("Instances", placements=[((1, 0, 0), (0, 0, 0), (1, 1, 1))], half=[3.0] * 3, margin=0.1),
-                [inner])
-    to_output(g, outer)
-    with pytest.raises(SyfrackError) as e:
-        renderer.compile(g)
-    assert e.value.status == 3
+def test_device_nested_copies_against_brute_force_and_oracle(renderer, oracle_mod):
+    """Three nested levels on the device: the interpreter keeps one copy search per
+    level; it follows the composed brute force and the oracle, and its march with the
+    GPU's skips follows the oracle's."""
+    from test_gpu_de import gpu_de_rule
+
+    g, levels = nested_copies()
+    pts = grid_points() * 1.6
+    r = renderer.compile(g).probe(pts)
+    np.testing.assert_allclose(r["distance"], brute_force_nested(pts, levels), atol=2e-4, rtol=0)
+    lcg = lcg_points(4096, 5.0, 31)
+    assert gpu_de_rule(renderer.compile(g).probe(lcg), oracle_mod.OracleGraph(g).de(lcg, precision=32)) <= 0.005
+    cam_pos, target = (2.0, 3.5, -7.0), (0.0, 0.0, 0.0)
+    from syfrack_gb300.scene import Camera, Scene
+
+    cam = Camera.look_at(cam_pos, target, 55.0)
+    w = h = 64
+    gpu = renderer.primary(g, cam, w, h, max_steps=256, rule="cone", eps=1e-4, t_far=40.0, normal="central")
+    sd = Scene(graph=None, camera=cam).desc(w, h)
+    ref = oracle_mod.OracleGraph(g).primary(sd.camera, w, h, 256, 0, 1e-4, 40.0, 1.0, 0, precision=32)
+    hit_g, hit_r = gpu["t"] >= 0, ref["t"] >= 0
+    assert (hit_g == hit_r).mean() >= 0.99 and hit_g.mean() > 0.1
+    ds = np.abs(gpu["steps"].astype(np.int64) - ref["steps"].astype(np.int64))
+    assert (ds == 0).mean() >= 0.95
 
 
 def test_fence_hierarchy_contains_every_copy_once(oracle_mod):
