@@ -3,11 +3,12 @@ wavefront path trace (1280x720, 64 spp, 4 bounces, 512 steps, hit epsilon 1e-4).
 
   python bench.py [--gpus N] [--steps K] [--warmup W] [--impl ours|reference]
 
-A step is one progressive pass of 8 samples per pixel over the whole frame
-(7,372,800 paths). `value` is device-timed (CUDA events on the library stream,
-max over ranks); `e2e` is the same metric through the public API with host
-buffers: one full 64-spp frame via Renderer.render (scene and graph uploaded
-from the host, film read back). With N > 1 (torchrun) every rank renders its
+A step is one whole 64-spp frame rendered as one dispatch (58,982,400 paths,
+15.3 GB of path state in HBM; --spp-per-step chooses a smaller progressive
+pass). `value` is device-timed (CUDA events on the library stream, max over
+ranks); `e2e` is the same metric through the public API with host buffers: one
+full 64-spp frame via Renderer.render (scene and graph uploaded from the host,
+dispatches of the step's size, film read back). With N > 1 (torchrun) every rank renders its
 own replica (the path has no exchange step).
 
 At N = 1 the same line also carries the other configurations, measured in the
@@ -139,6 +140,20 @@ def cpu_port_rate(seconds_target: float = 12.0):
     return total_seg / total_t / 1e6, threads, f"{used} random pixels x {SPP_PER_STEP} spp of the frame, FP32"
 
 
+def workload_config(args, n_ranks):
+    """The workload's description, the same in both arms."""
+    from syfrack_gb300 import workloads
+
+    cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=64,
+                                               samples_per_dispatch=args.spp_per_step)
+    paths = cfg.width * cfg.height * args.spp_per_step
+    return {"workload": WORKLOAD if (cfg.width, cfg.height) == (1280, 720) else f"profiling case {cfg.width}x{cfg.height}",
+            "width": cfg.width, "height": cfg.height, "spp_per_step": args.spp_per_step,
+            "hit_rule": f"fixed epsilon {cfg.hit_epsilon:g} (radius <= epsilon)", "paths_per_step": paths,
+            "max_bounces": cfg.max_bounces, "max_steps": cfg.max_steps, "parallelism": f"replicas{n_ranks}",
+            "l2": f"inputs larger than L2 (path state {paths * 260 / 1e9:.1f} GB per step)"}
+
+
 def run_reference(args):
     n, rank, _ = dist_env()
     if rank != 0:
@@ -152,8 +167,9 @@ def run_reference(args):
     value = statistics.median(rates)
     line = {"impl": "reference", "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": n,
             "steps": args.steps, "warmup": args.warmup, "higher_is_better": True, "scaling": "weak",
-            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Mandelbox scene)",
-            "config": {"workload": WORKLOAD, "host_threads": threads},
+            "vs_baseline": None, "dtype": "f32", "data": "synthetic (seeded Mandelbox scene; no dataset)",
+            "config": workload_config(args, n),
+            "host_threads": threads,
             "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
                              "sample": sample + " (the reference is Rust/WGSL and cannot be built here; "
                                                 "timed: its C++ restatement in oracle/)"},
@@ -254,8 +270,8 @@ def run_ours(args):
     ctx.set_profiling(False)
     sess.close()
 
-    # end to end through the public API: one full 64-spp frame (8 dispatches of 8 spp)
-    # rendered from host descriptions, film read back
+    # end to end through the public API: one full 64-spp frame in dispatches of the
+    # step's size, rendered from host descriptions, film read back
     e2e_cfg = workloads.mandelbox_pathtrace_config(width=args.width, height=args.height, spp=64,
                                                    samples_per_dispatch=spp_step)
     ctx.reset_stats()
@@ -288,22 +304,16 @@ def run_ours(args):
             "warmup": args.warmup, "ms_per_step": ms_max / args.steps, "higher_is_better": True,
             "scaling": "weak", "vs_baseline": None, "dtype": "f32",
             "data": "synthetic (seeded Mandelbox scene; no dataset)",
-            "config": {"workload": WORKLOAD if (cfg.width, cfg.height) == (1280, 720) else f"profiling case {cfg.width}x{cfg.height}",
-                       "width": cfg.width, "height": cfg.height, "spp_per_step": spp_step,
-                       "hit_rule": f"fixed epsilon {cfg.hit_epsilon:g} (radius <= epsilon)",
-                       "paths_per_step": cfg.width * cfg.height * spp_step, "max_bounces": cfg.max_bounces,
-                       "max_steps": cfg.max_steps, "integrator": "wavefront", "parallelism": f"replicas{n_ranks}",
-                       "launch": {"min_blocks_per_sm": args.min_blocks, "quantum": args.quantum,
-                                  "regen": args.regen},
-                       "l2": f"inputs larger than L2 (path state {cfg.width * cfg.height * spp_step * 260 / 1e9:.1f} GB "
-                             f"per step)",
-                       "segments_per_step": segs_all / args.steps,
-                       "pixel_samples_per_s": cfg.width * cfg.height * spp_step * args.steps * n_ranks
-                       / (ms_max * 1e-3)},
+            "config": workload_config(args, n_ranks),
+            "run": {"integrator": "wavefront",
+                    "launch": {"min_blocks_per_sm": args.min_blocks, "quantum": args.quantum, "regen": args.regen},
+                    "segments_per_step": segs_all / args.steps,
+                    "pixel_samples_per_s": cfg.width * cfg.height * spp_step * args.steps * n_ranks
+                    / (ms_max * 1e-3)},
             "e2e": {"value": e2e, "unit": UNIT, "h2d_bytes_per_step": h2d // e2e_steps,
                     "d2h_bytes_per_step": d2h // e2e_steps,
-                    "call": "Renderer.render: one full 64-spp frame (8 dispatches of 8 spp), film read back; "
-                            "bytes per 8-spp step"},
+                    "call": f"Renderer.render: one full 64-spp frame ({e2e_steps} dispatch(es) of {spp_step} spp), "
+                            f"film read back; bytes per {spp_step}-spp step"},
             "roofline": {"bound": "fp32", "kernel": "k_trace", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
                          "traffic": profiled_traffic() if (cfg.width, cfg.height) == (1280, 720) else None,
@@ -315,7 +325,7 @@ def run_ours(args):
                          "simt_lane_efficiency": lst["de_evals"] / max(32 * lst["warp_de_calls"], 1),
                          "iterate_lane_efficiency": lst["de_iterations"] / max(lst["iteration_slots"], 1),
                          "launch_tail_fraction": lst["tail_cycles"] / max(lst["warp_cycles"], 1),
-                         "lane_efficiency_source": "one further 8-spp step on the diagnostic trace kernel"},
+                         "lane_efficiency_source": f"one further {spp_step}-spp step on the diagnostic trace kernel"},
             "gpu_launches": st["launches"],
             "status_word": status,
             "clocks": clocks.summary(),
@@ -893,7 +903,7 @@ def main():
     ap.add_argument("--width", type=int, default=1280)
     ap.add_argument("--height", type=int, default=720)
     ap.add_argument("--no-e2e", action="store_true")
-    ap.add_argument("--spp-per-step", type=int, default=8,
+    ap.add_argument("--spp-per-step", type=int, default=64,
                     help="samples per pixel of the frame rendered by one step (one dispatch)")
     ap.add_argument("--no-extras", action="store_true",
                     help="the headline only (without the other configurations' summaries)")
