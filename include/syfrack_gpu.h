@@ -229,7 +229,8 @@ typedef sf_area_light sf_light;
 #define SF_MAX_RAMP_STOPS 16
 /* Material.coloring (material.rs:100-130) as GpuColoring (uniforms.rs:193-215): the
  * ramp (palette.rs:74-100) multiplies the albedo by its value at the sample's trap
- * slot (0..3), iteration fraction (4) or n.y * 0.5 + 0.5 (5); 0xffff = none. */
+ * slot (0..3), iteration fraction (4), n.y * 0.5 + 0.5 (5) or the orbit mix of
+ * sf_scene_desc.coloring_orbit (6, ABI 1.3); 0xffff = none. */
 typedef struct sf_coloring {
     uint32_t slot;
     uint32_t stop_count;              /* 0: white */
@@ -246,6 +247,58 @@ typedef struct sf_fog {
     float density, height, falloff, anisotropy;
     float color[3];
 } sf_fog;
+/* FinishDetail (material.rs:200-212) as GpuFinish.detail_* (uniforms.rs:797-815): a
+ * world-space pattern (finish_detail.wgsl) that tints the albedo, shifts roughness and
+ * bends the shading normal. pattern: 0 = none, else FinishPattern's order from 1
+ * (VeinedStone, Patina, BrushedMetal, Basalt, Ripples, Rosettes, CoastalRock, Sand,
+ * Dust, Concrete, WeatheredConcrete) to 12 (WetConcrete). Concrete kinds (10-12) add
+ * the Oren-Nayar rough diffuse lobe. */
+typedef struct sf_finish_detail {
+    uint32_t pattern, seed;
+    float scale, strength, bump, roughness_delta;
+    float tint[3];
+} sf_finish_detail;
+/* OrbitColoring (material.rs:18-56): a signed mix of the four traps, the iteration
+ * fraction and n.y * 0.5 + 0.5, optionally log-remapped (logarithmic > 0). */
+typedef struct sf_orbit_coloring {
+    float traps[4];
+    float iterations, normal, logarithmic;
+} sf_orbit_coloring;
+/* Optics (optics.rs:7-21) as GpuOptics (uniforms.rs:95-122): stochastic coverage
+ * (opacity), a rough dielectric interface (transmission probability, ior, thin-walled
+ * sheet) and a homogeneous interior medium (Beer-Lambert absorption reaching
+ * absorption_color after absorption_distance; subsurface scattering of the given
+ * albedo with mean free path subsurface_radius / subsurface). enabled 0 = opaque. */
+typedef struct sf_optics {
+    uint32_t enabled;
+    float opacity, transmission, ior;
+    uint32_t thin_walled;
+    float absorption_color[3], absorption_distance;
+    float subsurface, subsurface_color[3], subsurface_radius;
+} sf_optics;
+/* FractalTexture (texture.rs:62-100) as GpuTexture (uniforms.rs:316-380): a volumetric
+ * texture evaluated by a second compiled graph (texture.wgsl, pattern.wgsl:2-49) on
+ * surfaces without a MaterialTag. channel: 0-3 trap, 4 iteration fraction, 6 signed
+ * distance, 7 orbit mix (orbit). The ramp colours the value (its slot is unused). The
+ * graph must outlive the sessions that render with it. */
+typedef struct sf_texture {
+    sf_graph* graph;
+    uint32_t channel;
+    sf_orbit_coloring orbit;
+    float scale, offset[3], rotation[3];  /* rotation: Euler XYZ in degrees */
+    uint32_t octaves;                     /* 1..4 */
+    float contrast;
+    sf_coloring ramp;
+    float strength, roughness, bump;      /* albedo, roughness and relief effects */
+    float parallax;                       /* depth in texture units, 0 = none */
+    uint32_t parallax_steps;              /* 4..32 */
+    uint32_t fan;                         /* FanMapping: staggered fans on world XZ */
+    float fan_period[2];
+    uint32_t fan_rays;
+    uint32_t mask;                        /* TextureMask: only where trap `mask_slot` is near mask_value */
+    uint32_t mask_slot;
+    float mask_value, mask_width;
+} sf_texture;
 typedef struct sf_scene_desc {
     sf_camera camera;
     sf_material material;                 /* index 0: the global surface */
@@ -260,6 +313,13 @@ typedef struct sf_scene_desc {
     uint64_t seed;                        /* Scene.seed; the device uses lo ^ hi */
     sf_coloring coloring;                 /* slot 0xffff (or no stops): no colouring */
     sf_fog fog;
+    /* ABI 1.3: the rest of make_surface (pathtrace.wgsl:271-386) and the optics of
+     * radiance (:833-1105). Zeroed fields keep the 1.2 behaviour. */
+    sf_finish_detail details[SF_MAX_FINISHES]; /* FinishDetail of finish i (MaterialTag i+1) */
+    float dune_wind;                      /* Dunes.wind_direction in degrees (Sand detail) */
+    sf_orbit_coloring coloring_orbit;     /* channels of coloring.slot 6 (Coloring::Orbit) */
+    sf_optics optics[SF_MAX_FINISHES + 1];/* 0: Material.optics; i: finish i's optics */
+    sf_texture texture;                   /* Material.texture; graph NULL = none */
 } sf_scene_desc;
 
 /* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138).

@@ -48,7 +48,9 @@ sf_status cuda_fail(cudaError_t e, const char* what) {
 constexpr uint32_t MAX_DEPTH = 3;          // graph/mod.rs:41
 constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
 constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
-constexpr uint32_t ABI_VERSION = (1u << 16) | 2u;  // 1.1: sf_film_planes.color; 1.2: sf_render_config.hit_epsilon
+// 1.1: sf_film_planes.color; 1.2: sf_render_config.hit_epsilon; 1.3: finish details, orbit
+// colouring, optics and textures in sf_scene_desc
+constexpr uint32_t ABI_VERSION = (1u << 16) | 3u;
 
 // ------------------------------------------------------------------ graph preparation
 
@@ -884,9 +886,38 @@ sf_status scene_check(const sf_scene_desc& d) {
         if (d.lights[i].kind == SF_LIGHT_HDRI && !d.lights[i].environment)
             return fail(SF_ERR_INVALID, "an HDRI light needs a panorama (sf_environment_create)");
     }
-    if (d.coloring.slot == 6 && d.coloring.stop_count)
-        return fail(SF_ERR_UNSUPPORTED, "orbit colouring is not built on the device");
     if (d.coloring.stop_count > SF_MAX_RAMP_STOPS) return fail(SF_ERR_INVALID, "more than 16 ramp stops");
+    for (uint32_t i = 0; i < d.finish_count; ++i) {
+        const sf_finish_detail& f = d.details[i];
+        if (f.pattern > 12) return fail(SF_ERR_INVALID, "finish detail pattern out of range (0..12)");
+        if (f.pattern && !(f.scale >= 0.01f && f.scale <= 200.0f))  // FinishDetail bounds (material.rs:226-231)
+            return fail(SF_ERR_INVALID, "finish detail scale must lie in [0.01, 200]");
+    }
+    for (uint32_t i = 0; i <= SF_MAX_FINISHES; ++i) {
+        const sf_optics& o = d.optics[i];
+        if (!o.enabled) continue;
+        // Optics bounds (optics.rs:40-72)
+        if (!(o.ior >= 1.0f && o.ior <= 3.0f) || !(o.opacity >= 0.0f && o.opacity <= 1.0f) ||
+            !(o.transmission >= 0.0f && o.transmission <= 1.0f) ||
+            !(o.absorption_distance >= 0.001f && o.absorption_distance <= 1000.0f) ||
+            !(o.subsurface_radius >= 0.001f && o.subsurface_radius <= 1000.0f) ||
+            !(o.subsurface >= 0.0f && o.subsurface <= 1.0f))
+            return fail(SF_ERR_INVALID, "optics parameter out of range");
+    }
+    const sf_texture& t = d.texture;
+    if (t.graph) {
+        // FractalTexture bounds (texture.rs:196-215)
+        if (t.octaves < 1 || t.octaves > 4) return fail(SF_ERR_INVALID, "texture octaves must lie in 1..4");
+        if (t.parallax_steps < 4 || t.parallax_steps > 32)
+            return fail(SF_ERR_INVALID, "texture parallax steps must lie in 4..32");
+        if (!(t.channel <= 4 || t.channel == 6 || t.channel == 7)) return fail(SF_ERR_INVALID, "texture channel");
+        if (t.mask && t.mask_slot > 3) return fail(SF_ERR_INVALID, "texture mask slot must lie in 0..3");
+        if (t.fan && !(t.fan_period[0] > 0.0f && t.fan_period[1] > 0.0f))
+            return fail(SF_ERR_INVALID, "texture fan periods must be positive");
+        if (!(t.scale > 0.0f)) return fail(SF_ERR_INVALID, "texture scale must be positive");
+        if (t.ramp.stop_count == 0 || t.ramp.stop_count > SF_MAX_RAMP_STOPS)
+            return fail(SF_ERR_INVALID, "the texture ramp needs 1..16 stops");
+    }
     if (!(d.fog.density >= 0.0f) || !(std::fabs(d.fog.anisotropy) < 1.0f))
         return fail(SF_ERR_INVALID, "fog density must be >= 0 and anisotropy in (-1, 1)");
     if (shadow_slots_of(d) > 8)
@@ -957,6 +988,17 @@ void material_dev(const sf_material& m, DevMaterial& o) {
     o.specular = m.specular;
     std::memcpy(o.emission, m.emission, 12);
 }
+// GpuRamp::from_ramp (uniforms.rs) of a colouring or texture ramp.
+static void ramp_dev(const sf_coloring& c, DevRamp& r) {
+    r.n = std::min<uint32_t>(c.stop_count, SF_MAX_RAMP);
+    r.cyclic = c.cyclic;
+    r.smooth = c.smooth;
+    r.positioned = c.positioned;
+    r.map[0] = c.frequency;
+    r.map[1] = c.phase;
+    r.map[2] = c.gamma;
+    std::memcpy(r.stops, c.stops, sizeof r.stops);
+}
 // Uniforms::from_scene (uniforms.rs:748-830) for the DE path.
 void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph_info& gi, DevScene& S) {
     std::memset(&S, 0, sizeof S);
@@ -1001,16 +1043,83 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     S.fog[2] = d.fog.falloff;
     S.fog[3] = d.fog.anisotropy;
     std::memcpy(S.fog_color, d.fog.color, 12);
-    const sf_coloring& col = d.coloring;
-    S.col_slot = col.slot;
-    S.col_n = std::min<uint32_t>(col.stop_count, SF_MAX_RAMP);
-    S.col_cyclic = col.cyclic;
-    S.col_smooth = col.smooth;
-    S.col_positioned = col.positioned;
-    S.col_map[0] = col.frequency;
-    S.col_map[1] = col.phase;
-    S.col_map[2] = col.gamma;
-    std::memcpy(S.col_stops, col.stops, sizeof S.col_stops);
+    S.col_slot = d.coloring.slot;
+    ramp_dev(d.coloring, S.col);
+    std::memcpy(S.col_weights, d.coloring_orbit.traps, 16);
+    S.col_extra[0] = d.coloring_orbit.iterations;
+    S.col_extra[1] = d.coloring_orbit.normal;
+    S.col_extra[2] = d.coloring_orbit.logarithmic;
+    // finish details (GpuFinish.detail_*, uniforms.rs:797-815)
+    S.dune_wind = d.dune_wind * (3.14159265f / 180.0f);
+    for (uint32_t i = 0; i < S.finish_count; ++i) {
+        const sf_finish_detail& f = d.details[i];
+        DevDetail& o = S.details[i];
+        o.kind = f.pattern;
+        o.seed = f.seed;
+        o.mapping[0] = f.scale;
+        o.mapping[1] = f.strength;
+        o.mapping[2] = f.bump;
+        o.mapping[3] = f.roughness_delta;
+        std::memcpy(o.tint, f.tint, 12);
+        if (f.pattern) S.rich |= SF_RICH_DETAIL;
+        if (f.pattern >= 10) S.rich |= SF_RICH_ROUGH_DIFFUSE;
+    }
+    // GpuOptics::from_optics (uniforms.rs:103-122); slots past the finish count stay opaque
+    for (uint32_t i = 0; i <= S.finish_count; ++i) {
+        const sf_optics& o = d.optics[i];
+        if (!o.enabled) continue;
+        DevOptics& g = S.optics[i];
+        g.surface[0] = o.opacity;
+        g.surface[1] = o.transmission;
+        g.surface[2] = o.ior;
+        g.surface[3] = o.thin_walled ? 1.0f : 0.0f;
+        for (int k = 0; k < 3; ++k)
+            g.absorption[k] = -logf(std::max(o.absorption_color[k], 0.0001f)) / o.absorption_distance;
+        g.absorption[3] = o.absorption_distance;
+        std::memcpy(g.subsurface, o.subsurface_color, 12);
+        g.subsurface[3] = o.subsurface / o.subsurface_radius;
+        S.rich |= SF_RICH_OPTICS;
+    }
+    // GpuTexture::from_texture (uniforms.rs:340-379)
+    const sf_texture& t = d.texture;
+    if (t.graph) {
+        DevTexture& x = S.tex;
+        x.channel = t.channel;
+        x.octaves = t.octaves;
+        x.budget = t.graph->info.iteration_product;  // FractalTexture::iteration_budget
+        x.enabled = 1;
+        std::memcpy(x.mapping, t.offset, 12);
+        x.mapping[3] = t.scale;
+        for (int k = 0; k < 3; ++k) x.rotation[k] = t.rotation[k] * (3.14159265f / 180.0f);
+        x.rotation[3] = t.contrast;
+        x.effects[0] = t.strength;
+        x.effects[1] = t.roughness;
+        x.effects[2] = t.bump;
+        x.effects[3] = 1.0f;
+        if (t.channel == 7) {
+            std::memcpy(x.weights, t.orbit.traps, 16);
+            x.extra[0] = t.orbit.iterations;
+            x.extra[1] = t.orbit.normal;
+            x.extra[2] = t.orbit.logarithmic;
+        }
+        x.parallax[0] = t.parallax;
+        x.parallax[1] = float(t.parallax_steps);
+        if (t.fan) {
+            x.fan[0] = t.fan_period[0];
+            x.fan[1] = t.fan_period[1];
+            x.fan[2] = float(t.fan_rays);
+            x.fan[3] = 1.0f;
+        }
+        if (t.mask) {
+            x.mask[0] = float(t.mask_slot);
+            x.mask[1] = t.mask_value;
+            x.mask[2] = t.mask_width;
+            x.mask[3] = 1.0f;
+        }
+        x.prog = reinterpret_cast<uint64_t>(t.graph->d_prog);
+        ramp_dev(t.ramp, x.ramp);
+        S.rich |= SF_RICH_TEXTURE;
+    }
 }
 
 }  // namespace sfh

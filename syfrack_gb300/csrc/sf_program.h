@@ -110,6 +110,39 @@ struct DevLight {
 struct DevMaterial {
     float albedo[3], roughness, metallic, specular, emission[3];
 };
+// A ramp (GpuRamp, palette_sample of common.wgsl:331-362): stops (rgb, position).
+struct DevRamp {
+    uint32_t n, cyclic, smooth, positioned;
+    float map[3];  // frequency, phase, gamma
+    float stops[SF_MAX_RAMP][4];
+};
+// GpuFinish.detail_* (uniforms.rs:797-815): kind (FinishPattern 1..12, 0 = none), seed,
+// mapping = scale, strength, bump, roughness delta; tint.
+struct DevDetail {
+    uint32_t kind, seed;
+    float mapping[4];
+    float tint[3];
+};
+// GpuOptics (uniforms.rs:95-122): surface = opacity, transmission, ior, thin sheet;
+// absorption = sigma_a rgb, distance (> 0: optics enabled); subsurface = albedo rgb,
+// collision rate.
+struct DevOptics {
+    float surface[4], absorption[4], subsurface[4];
+};
+// GpuTexture (uniforms.rs:316-380) with the texture graph's lowered program.
+struct DevTexture {
+    uint32_t channel, octaves, budget;  // kind.x, kind.y, kind.z (iteration budget)
+    uint32_t enabled;
+    float mapping[4];   // offset xyz, scale
+    float rotation[4];  // Euler radians xyz, contrast
+    float effects[4];   // colour, roughness, bump strength, enabled
+    float weights[4], extra[4];  // orbit channel mix
+    float parallax[2];  // depth, layer budget
+    float fan[4];       // period xz, rays, enabled
+    float mask[4];      // trap slot, value, width, enabled
+    uint64_t prog;      // device address of the texture graph's DeProgram
+    DevRamp ramp;
+};
 
 // Scene constants of one render (the Uniforms subset of common.wgsl:163-191
 // that the DE path reads).
@@ -127,14 +160,23 @@ struct DevScene {
     float pixel_cone;                           // tan_half * 2 / width
     float hit_eps;                              // > 0: fixed-epsilon hit test; 0: cone-relative
     uint32_t iteration_product;
-    // Material.coloring: slot (0..3 trap, 4 iterations, 5 normal, else none) and ramp
-    uint32_t col_slot, col_n, col_cyclic, col_smooth, col_positioned;
-    float col_map[3];                 // frequency, phase, gamma
-    float col_stops[SF_MAX_RAMP][4];  // rgb, position
+    // Material.coloring: slot (0..3 trap, 4 iterations, 5 normal, 6 orbit mix, else none)
+    // and ramp; col_weights / col_extra = the orbit mix (GpuColoring.weights, .extra)
+    uint32_t col_slot;
+    float col_weights[4], col_extra[3];
+    DevRamp col;
     uint32_t shadow_slots;            // shadow requests a bounce can make (shadow_slots_of)
     float fog[4];                     // density, height, falloff, anisotropy (atmosphere.a)
     float fog_color[3];               // scattering albedo (atmosphere.b.xyz)
     DevMaterial material;
     DevMaterial finishes[8];
     DevLight lights[8];
+    // make_surface's detail and texture and radiance's optics. rich: SF_RICH_* bits of
+    // what the scene uses (0 keeps every path of the plain surface).
+    uint32_t rich;
+    float dune_wind;  // radians
+    DevDetail details[8];
+    DevOptics optics[9];
+    DevTexture tex;
 };
+enum { SF_RICH_DETAIL = 1, SF_RICH_TEXTURE = 2, SF_RICH_OPTICS = 4, SF_RICH_ROUGH_DIFFUSE = 8 };

@@ -2,15 +2,15 @@
 //
 // Device twins of pathtrace.wgsl (PCG :20-37, march_segment :78-145, BRDF
 // :195-463, direct_light :471-558, camera_ray :781-800, radiance :802-1201)
-// and lights.wgsl (:150-356), restricted to area emitters with fog, optics,
-// ocean, portals, guiding, textures, sun and environment off. The bounce body
+// and lights.wgsl (:150-356), with ocean, portals, guiding, nature phenomena and
+// spectral dispersion off (each is an identity when off). The bounce body
 // is one function (bounce_body) used by both the per-pixel megakernel and the
 // wavefront shade stage, so both integrators perform identical arithmetic.
 #pragma once
 #include "sf_de.cuh"
+#include "sf_surface.cuh"
 
 #define SF_NO_LIGHT 0xffffffffu
-#define SF_PI 3.14159265358979f  // common.wgsl:6
 
 // ------------------------------------------------------------------ RNG
 __device__ __forceinline__ uint32_t pcg(uint32_t v) {
@@ -201,6 +201,7 @@ __device__ __forceinline__ float nearest_emitter(const DevScene& S, float3 ro, f
 struct Surface {
     float3 n, diffuse, f0, emission;
     float alpha;
+    float diffuse_sigma;  // > 0: Oren-Nayar rough diffuse (concrete finish details)
 };
 __device__ __forceinline__ float luminance(float3 c) { return fmaf(c.z, 0.0722f, fmaf(c.x, 0.2126f, c.y * 0.7152f)); }
 __device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt) {
@@ -276,6 +277,17 @@ static __device__ float3 brdf_eval(const Surface& s, float3 v, float3 l) {
     float a2 = s.alpha * s.alpha;
     float3 f = fresnel(s.f0, vh);
     float3 spec = f * wdiv(ggx_d(nh, a2) * smith_g1(nv, a2) * smith_g1(nl, a2), fmaxf(4.0f * nv * nl, 1e-4f));
+    if (s.diffuse_sigma > 0.0f) {
+        // Oren-Nayar reflectance (pathtrace.wgsl:408-419); the lobe stays cosine-sampled
+        const float sigma2 = s.diffuse_sigma * s.diffuse_sigma;
+        const float a = 1.0f - wdiv(sigma2, 2.0f * (sigma2 + 0.33f));
+        const float b = wdiv(0.45f * sigma2, sigma2 + 0.09f);
+        const float sin_l = wsqrt(fmaxf(0.0f, 1.0f - nl * nl));
+        const float sin_v = wsqrt(fmaxf(0.0f, 1.0f - nv * nv));
+        const float cos_phi = fmaxf(0.0f, wdiv(dot3(l - s.n * nl, v - s.n * nv), fmaxf(sin_l * sin_v, 1e-8f)));
+        const float factor = a + wdiv(b * cos_phi * sin_l * sin_v, fmaxf(fmaxf(nl, nv), 1e-5f));
+        return s.diffuse * (mk3(1.f, 1.f, 1.f) - f) * (factor * (1.0f / SF_PI)) + spec;
+    }
     return s.diffuse * (mk3(1.f, 1.f, 1.f) - f) * (1.0f / SF_PI) + spec;
 }
 __device__ __forceinline__ float spec_probability(const Surface& s, float nv) {
@@ -292,49 +304,26 @@ static __device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_s
     float pdf_spec = wdiv(ggx_d(nh, a2) * smith_g1(nv, a2), 4.0f * nv);
     return fmaf(p_spec, pdf_spec, (1.0f - p_spec) * nl * (1.0f / SF_PI));
 }
-// palette_sample (common.wgsl:331-362) of the colouring ramp.
-static __device__ float3 ramp_sample(const DevScene& S, float value) {
-    const uint32_t n = S.col_n;
-    if (n == 0) return mk3(1.f, 1.f, 1.f);
-    if (n == 1) return ld3(S.col_stops[0]);
-    auto mixs = [&](uint32_t a, uint32_t b, float amount) {
-        float f = fminf(fmaxf(amount, 0.0f), 1.0f);
-        if (S.col_smooth) f = f * f * (3.0f - 2.0f * f);
-        return lerp3(ld3(S.col_stops[a]), ld3(S.col_stops[b]), f);
-    };
-    float t = value * S.col_map[0] + S.col_map[1];
-    if (S.col_cyclic) t = t - floorf(t);
-    else t = fminf(fmaxf(t, 0.0f), 1.0f);
-    if (S.col_map[2] != 1.0f) t = powf(t, S.col_map[2]);
-    if (!S.col_positioned && !S.col_cyclic) {
-        const float x = t * float(n - 1);
-        const uint32_t i = min(uint32_t(floorf(x)), n - 2);
-        return mixs(i, i + 1, x - float(i));
-    }
-    const float first = S.col_stops[0][3], last = S.col_stops[n - 1][3];
-    if (S.col_cyclic && (t < first || t >= last)) {
-        const float x = t < first ? t + 1.0f : t;
-        return mixs(n - 1, 0, wdiv(x - last, fmaxf(1.0f + first - last, 1e-8f)));
-    }
-    if (t <= first) return ld3(S.col_stops[0]);
-    if (t >= last) return ld3(S.col_stops[n - 1]);
-    for (uint32_t i = 0; i + 1 < n; ++i)
-        if (t < S.col_stops[i + 1][3])
-            return mixs(i, i + 1, wdiv(t - S.col_stops[i][3], S.col_stops[i + 1][3] - S.col_stops[i][3]));
-    return ld3(S.col_stops[n - 1]);
-}
-
-// make_surface (pathtrace.wgsl:271-386) without texture, detail and phenomena.
-static __device__ Surface make_surface(const DevScene& S, float3 n, const DeSampleF& smp) {
+// make_surface (pathtrace.wgsl:271-386): the colouring ramp or orbit mix, the finish
+// of a MaterialTag, surface variation, the finish's world-space detail and, on
+// untagged surfaces, the volumetric texture (TEX: kernels built with the texture
+// interpreter). p is the hit point, n the shading-side normal, v toward the eye and
+// footprint the path's transported texture width.
+template <bool TEX = false>
+static __device__ Surface make_surface(const DevScene& S, float3 p, float3 n, float3 v, const DeSampleF& smp,
+                                       float footprint) {
     const DevMaterial* m = &S.material;
-    bool assigned = smp.material > 0 && smp.material <= S.finish_count;
+    const bool assigned = smp.material > 0 && smp.material <= S.finish_count;
     if (assigned) m = &S.finishes[smp.material - 1];
     float3 albedo = ld3(m->albedo);
-    if (!assigned && S.col_n) {  // the colouring ramp (pathtrace.wgsl:275-288)
+    if (!assigned && S.col.n) {  // the colouring ramp (pathtrace.wgsl:275-288)
         const uint32_t slot = S.col_slot;
-        if (slot < 4) albedo = albedo * ramp_sample(S, smp.traps[slot]);
-        else if (slot == 5) albedo = albedo * ramp_sample(S, n.y * 0.5f + 0.5f);
-        else if (slot == 4) albedo = albedo * ramp_sample(S, float(smp.iter) / fmaxf(float(S.iteration_product), 1.0f));
+        const float iter_frac = float(smp.iter) / fmaxf(float(S.iteration_product), 1.0f);
+        if (slot == 6) albedo = albedo * ramp_sample(S.col, orbit_mix(S.col_weights, S.col_extra, smp.traps, iter_frac,
+                                                                      n.y * 0.5f + 0.5f));
+        else if (slot < 4) albedo = albedo * ramp_sample(S.col, smp.traps[slot]);
+        else if (slot == 5) albedo = albedo * ramp_sample(S.col, n.y * 0.5f + 0.5f);
+        else if (slot == 4) albedo = albedo * ramp_sample(S.col, iter_frac);
     }
     float rough = m->roughness, metallic = m->metallic, spec = m->specular;
     float3 emission = assigned ? ld3(m->emission) : mk3(0.f, 0.f, 0.f);
@@ -346,13 +335,56 @@ static __device__ Surface make_surface(const DevScene& S, float3 n, const DeSamp
         rough = S.var_rough[0] + (S.var_rough[1] - S.var_rough[0]) * t;
         metallic = S.var_metal[0] + (S.var_metal[1] - S.var_metal[0]) * t;
     }
+    float3 shading_n = n;
+    float diffuse_sigma = 0.0f;
+    if (assigned && (S.rich & SF_RICH_DETAIL) && S.details[smp.material - 1].kind != 0u) {
+        const DevDetail& f = S.details[smp.material - 1];
+        float4 detail = finish_eval(f, p, footprint, S.dune_wind);
+        if (f.kind == 9u) detail = scale4(detail, sstep(0.10f, 0.80f, n.y));  // powder settles on tops
+        if (f.kind == 12u) detail.w *= sstep(0.45f, 0.95f, n.y);
+        const float value = detail.w;
+        const float amount = f.mapping[1] * value;
+        albedo = mk3(mixf(albedo.x, f.tint[0], amount), mixf(albedo.y, f.tint[1], amount),
+                     mixf(albedo.z, f.tint[2], amount));
+        if (f.kind == 9u) {
+            rough += fmaxf(f.mapping[3], 0.0f) * amount;
+            metallic *= 1.0f - amount;
+            spec = mixf(spec, 0.025f, amount);
+        } else if (f.kind == 12u) {
+            rough = mixf(rough, fminf(fmaxf(rough + f.mapping[3], 0.025f), 1.0f), amount);
+            spec = mixf(spec, 0.0204f, amount);
+            metallic *= 1.0f - amount;
+        } else {
+            rough += f.mapping[3] * (2.0f * value - 1.0f);
+        }
+        if (f.kind == 2u) metallic *= 1.0f - 0.75f * amount;
+        if (fabsf(f.mapping[2]) > 0.0f) shading_n = finish_normal(f.mapping[2], n, xyz(detail));
+        if (f.kind >= 10u) diffuse_sigma = 1.0f;  // times the final roughness below
+    }
+    if constexpr (TEX) {
+        const DevTexture& T = S.tex;
+        const float amount = texture_mask(T, smp.traps);
+        if (!assigned && T.effects[3] > 0.0f && amount > 0.0f) {
+            const float3 tex_p = texture_parallax(T, p, n, v, footprint);
+            const float value = texture_filtered_value(T, tex_p, footprint);
+            const float3 c = ramp_sample(T.ramp, value);
+            const float k = T.effects[0] * amount;
+            albedo = albedo * mk3(mixf(1.0f, c.x, k), mixf(1.0f, c.y, k), mixf(1.0f, c.z, k));
+            rough = mixf(rough, value, T.effects[1] * amount);
+            if (T.effects[2] > 0.0f) {
+                const float3 tn = texture_normal(T, tex_p, n, footprint);
+                shading_n = safe_normalize3(mk3(mixf(n.x, tn.x, amount), mixf(n.y, tn.y, amount), mixf(n.z, tn.z, amount)));
+            }
+        }
+    }
     rough = fminf(fmaxf(rough, 0.02f), 1.0f);
     Surface s;
-    s.n = n;
+    s.n = shading_n;
     s.diffuse = albedo * (1.0f - metallic);
     s.f0 = mk3(spec, spec, spec) * (1.0f - metallic) + albedo * metallic;
     s.alpha = rough * rough;
     s.emission = emission;
+    s.diffuse_sigma = diffuse_sigma * rough * 0.45f;
     return s;
 }
 
@@ -365,6 +397,12 @@ struct PathState {
     bool prev_from_bsdf;
     bool prev_from_volume;  // the segment left a fog scattering point (its emitters were estimated there)
     bool volume_path;       // the camera segment scattered in the fog (pathtrace.wgsl:822)
+    // rich surfaces (DevScene.rich != 0): the transported texture footprint
+    // (pathtrace.wgsl:811-814) and the optics state (:830-840): inside a solid
+    // dielectric medium of finish slot medium_slot, coverage null events taken.
+    float tex_width, tex_spread;
+    bool solid_medium;
+    uint32_t medium_slot, null_surfaces;
 };
 // The sample's volume part for the film's volume planes (pathtrace.wgsl:1198).
 __device__ __forceinline__ float3 path_volume(const PathState& ps) { return ps.volume_path ? ps.L : ps.pv; }
@@ -399,7 +437,46 @@ __device__ __forceinline__ void path_begin(const DevScene& S, PathState& ps, uin
     ps.pv = mk3(0.f, 0.f, 0.f);
     ps.volume_path = false;
     ps.bounce = 0;
+    ps.tex_width = 0.0f;
+    ps.tex_spread = S.pixel_cone * 0.5f;
+    ps.solid_medium = false;
+    ps.medium_slot = 0;
+    ps.null_surfaces = 0;
 }
+
+// ------------------------------------------------------------------ optics (optics.wgsl)
+// material_optics (optics.wgsl:1-3): finish slots beyond the finish count read slot 0.
+__device__ __forceinline__ const DevOptics& material_optics(const DevScene& S, uint32_t index) {
+    return S.optics[index <= S.finish_count ? index : 0u];
+}
+__device__ __forceinline__ bool optics_enabled(const DevOptics& o) { return o.absorption[3] > 0.0f; }
+// The medium a path starts in (pathtrace.wgsl:833-840): inside a transmissive solid
+// (not a thin sheet) with optics when the exact sample at the ray origin is negative.
+__device__ __forceinline__ void optics_initial_medium(const DevScene& S, PathState& ps, float d, uint32_t material) {
+    const DevOptics& o = material_optics(S, material);
+    ps.solid_medium = d < 0.0f && optics_enabled(o) && o.surface[1] > 0.0f && o.surface[3] == 0.0f;
+    ps.medium_slot = material;
+}
+// ocean_fresnel (ocean.wgsl:151-159): unpolarised dielectric reflectance.
+__device__ __forceinline__ float dielectric_fresnel(float cosine, float eta) {
+    const float ci = fminf(fmaxf(fabsf(cosine), 0.0f), 1.0f);
+    const float st2 = eta * eta * (1.0f - ci * ci);
+    if (st2 >= 1.0f) return 1.0f;
+    const float ct = wsqrt(fmaxf(0.0f, 1.0f - st2));
+    const float rs = wdiv(eta * ci - ct, fmaxf(eta * ci + ct, 1e-6f));
+    const float rp = wdiv(ci - eta * ct, fmaxf(ci + eta * ct, 1e-6f));
+    return 0.5f * (rs * rs + rp * rp);
+}
+// WGSL refract(e1, e2, eta): zero on total internal reflection.
+__device__ __forceinline__ float3 refract3(float3 i, float3 n, float eta) {
+    const float ni = dot3(n, i);
+    const float k = 1.0f - eta * eta * (1.0f - ni * ni);
+    if (k < 0.0f) return mk3(0.f, 0.f, 0.f);
+    return i * eta - n * (eta * ni + wsqrt(k));
+}
+__device__ __forceinline__ float3 reflect3(float3 i, float3 n) { return i - n * (2.0f * dot3(n, i)); }
+__device__ __forceinline__ float3 exp3(float3 a) { return mk3(expf(a.x), expf(a.y), expf(a.z)); }
+
 // point_stream of radiance (pathtrace.wgsl:823): the pixel's rotation of the
 // radical-inverse points.
 __device__ __forceinline__ uint32_t point_stream_of(const DevScene& S, uint32_t px, uint32_t py) {
