@@ -135,6 +135,8 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
         sf_status st = validate_config(jobs[i].cfg);
         if (st != SF_OK) return st;
         if (const sf_status sc = scene_check(jobs[i].scene); sc != SF_OK) return sc;
+        if (rich_of(jobs[i].scene))
+            return fail(SF_ERR_UNSUPPORTED, "finish details, textures and optics render through sessions, not batches");
         const sf_render_config& cf = jobs[i].cfg;
         uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
                                                    cf.samples_per_pixel), 1);

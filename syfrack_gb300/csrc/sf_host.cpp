@@ -1440,7 +1440,6 @@ extern "C" sf_status sf_primary_trace(sf_graph* g, const sf_primary_desc* d, flo
 
 namespace sfh {
 
-uint32_t rounds_of(const sf_render_config& c) { return c.max_bounces + 2; }
 
 void tile_grid(sf_session* s) {
     s->tiles.clear();
@@ -1485,7 +1484,7 @@ sf_status session_alloc(sf_session* s) {
     const uint32_t fw = s->window ? tw : cfg.width, fh = s->window ? th : cfg.height;
     const size_t px = size_t(fw) * fh;
     const bool wf = cfg.integrator == SF_INTEGRATOR_WAVEFRONT;
-    const uint32_t R = rounds_of(cfg);
+    const uint32_t R = rounds_of(cfg, s->scene);
     // layout
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
@@ -1495,6 +1494,9 @@ sf_status session_alloc(sf_session* s) {
     // fog scenes keep the film's volume layer split: a per-path volume row and three planes
     const bool split = has_fog(s->scene);
     size_t o_pv = split ? take(N * 16) : 0, o_vol = split ? take(px * 48) : 0;
+    // scenes with finish details, a texture or optics keep a per-path footprint and medium row
+    const bool rich = wf && rich_of(s->scene) != 0u;
+    size_t o_ex = rich ? take(N * 16) : 0;
     size_t o_soa = 0, o_lists = 0, o_march = 0, o_resume = 0;
     const uint32_t K = shadow_slots_of(s->scene);  // shadow segments one bounce may issue
     s->shadow_slots = K;
@@ -1526,6 +1528,7 @@ sf_status session_alloc(sf_session* s) {
         s->resume = reinterpret_cast<uint32_t*>(base + o_resume);
     }
     s->soa.Ls = reinterpret_cast<float4*>(base + o_Ls);
+    if (rich) s->soa.ex = reinterpret_cast<float4*>(base + o_ex);
     if (split) {
         s->soa.pv = reinterpret_cast<float4*>(base + o_pv);
         s->film.vol = reinterpret_cast<float4*>(base + o_vol);
@@ -1609,14 +1612,15 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
     if (s->cfg.integrator == SF_INTEGRATOR_MEGAKERNEL) {
         {
             LaunchTimer t(c, true);
-            CU(sf_launch_megakernel(s->graph->d_prog, s->d_scene, s->soa, g, s->film, c->d_stats, st));
+            CU(sf_launch_megakernel(s->graph->d_prog, s->d_scene, rich_of(s->scene), s->soa, g, s->film, c->d_stats,
+                                    st));
         }
         LaunchTimer t2(c, false);
         CU(sf_launch_commit(s->soa, g, s->film, st));
         s->dispatches++;
         return SF_OK;
     }
-    const uint32_t R = rounds_of(s->cfg);
+    const uint32_t R = rounds_of(s->cfg, s->scene);
     const size_t N = s->capacity;
     // launches per round: the first, then one per step quantum a segment may still need
     const uint32_t Q = s->quantum ? std::min<uint32_t>((s->cfg.max_steps + s->quantum - 1) / s->quantum + 1, 64) : 1;
@@ -1626,7 +1630,9 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
         LaunchTimer t(c, false);
         CU(sf_launch_generate(s->d_scene, s->soa, g, s->counts, st));
     }
-    const int blocks = int(s->min_blocks) * c->sm_count;
+    const uint32_t rich = rich_of(s->scene);
+    // the optics trace kernel holds more state per lane: two blocks per SM
+    const int blocks = int((rich & SF_RICH_OPTICS) ? 2u : s->min_blocks) * c->sm_count;
     const uint32_t K = s->shadow_slots;
     for (uint32_t r = 0; r < R; ++r) {
         RoundQueues q;
@@ -1643,12 +1649,13 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
             tl.quantum = j + 1 == Q ? 0u : s->quantum;  // the last launch runs segments to completion
             tl.regen = s->regen;
             tl.lane_stats = c->lane_stats ? 1u : 0u;
+            tl.optics = (rich & SF_RICH_OPTICS) ? 1u : 0u;
             LaunchTimer t(c, true);
             CU(sf_launch_trace(s->graph->prog.form, s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks,
                                int(s->min_blocks), st));
         }
         LaunchTimer t(c, false);
-        CU(sf_launch_shade(s->d_scene, s->soa, q, g, s->film, s->status, r + 1 == R ? 1 : 0, st));
+        CU(sf_launch_shade(s->d_scene, rich, s->soa, q, g, s->film, s->status, r + 1 == R ? 1 : 0, st));
     }
     LaunchTimer t(c, false);
     CU(sf_launch_commit(s->soa, g, s->film, st));

@@ -151,6 +151,23 @@ sf_status planar_check(const sf_planar_desc* f);
 cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);
 // Fog scenes keep the film's volume layer split (volume, moments and surface planes).
 inline bool has_fog(const sf_scene_desc& d) { return d.fog.density > 0.0f; }
+// DevScene.rich of a scene: finish details, a texture, optics (SF_RICH_* bits).
+inline uint32_t rich_of(const sf_scene_desc& d) {
+    uint32_t r = 0;
+    const uint32_t nf = d.finish_count < SF_MAX_FINISHES ? d.finish_count : SF_MAX_FINISHES;
+    for (uint32_t i = 0; i < nf; ++i)
+        if (d.details[i].pattern) r |= SF_RICH_DETAIL | (d.details[i].pattern >= 10 ? SF_RICH_ROUGH_DIFFUSE : 0u);
+    for (uint32_t i = 0; i <= nf; ++i)
+        if (d.optics[i].enabled) r |= SF_RICH_OPTICS;
+    if (d.texture.graph) r |= SF_RICH_TEXTURE;
+    return r;
+}
+// Wavefront rounds of a dispatch: every bounce, one round to resolve the last shadow
+// segments and, with optics, the 32 coverage null events a path may take without a
+// bounce (the reference sizes its wavefront the same way, session.rs:397-405).
+inline uint32_t rounds_of(const sf_render_config& c, const sf_scene_desc& d) {
+    return c.max_bounces + 2 + ((rich_of(d) & SF_RICH_OPTICS) ? 33u : 0u);
+}
 
 // Wavefront path state for N paths with K shadow slots (a bounce issues at most K
 // shadow segments): eight path planes, K sets of shadow planes and visibility words,

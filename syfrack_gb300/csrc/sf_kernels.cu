@@ -172,6 +172,8 @@ __global__ void __launch_bounds__(256) k_generate(const DevScene* __restrict__ s
 
 // Shade, then compact the surviving paths into the next round's queues with one
 // atomic per warp and list.
+// FEAT: the surface features the kernel is built with (SF_FEAT_*; 0 for plain scenes).
+template <int FEAT>
 __global__ void __launch_bounds__(256) k_shade(const DevScene* __restrict__ scene_g, PathSoA soa, RoundQueues q,
                                                DispatchGeom g, FilmPlanes film, uint32_t* status, int final_round) {
     __shared__ DevScene S;
@@ -180,7 +182,7 @@ __global__ void __launch_bounds__(256) k_shade(const DevScene* __restrict__ scen
     const uint32_t n = q.counts[0];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         uint32_t path = q.active ? q.active[j] : j;
-        uint32_t nf = shade_path(S, soa, g, film, path, path, status, final_round);
+        uint32_t nf = shade_path<FEAT>(S, soa, g, film, path, path, status, final_round);
         if (!final_round) enqueue_next(q, soa, nf, path);
     }
 }
@@ -245,6 +247,30 @@ static __device__ int march_full(const DeProgram& P, March& m, uint32_t max_step
     return r;
 }
 
+// optical_refine_hit (optics.wgsl:7-23): up to eight Newton steps along the ray on the
+// exact field from the hit at t, with a central difference of step eps (from the hit).
+static __device__ float optical_refine(const DeProgram& P, float3 ro, float3 rd, float t, unsigned long long& evals,
+                                       unsigned long long& iters) {
+    const float eps = fmaxf(1e-5f, fminf(1e-3f, t * 1e-5f));
+    for (uint32_t i = 0; i < 8u; ++i) {
+        const float3 p = ro + rd * t;
+        const DeRaw a = de_raw_exact(P, p);
+        evals++;
+        iters += a.iter;
+        if (fabsf(a.d) < 1e-5f) break;
+        const DeRaw b = de_raw_exact(P, p + rd * eps);
+        const DeRaw c = de_raw_exact(P, p + rd * (-eps));
+        evals += 2;
+        iters += b.iter + c.iter;
+        const float derivative = (b.d - c.d) / (2.0f * eps);
+        if (fabsf(derivative) < 1e-5f) break;
+        t = fmaxf(0.0f, t - fminf(fmaxf(a.d / derivative, -0.5f), 0.5f));
+    }
+    return t;
+}
+
+// FEAT: the surface features the kernel is built with (SF_FEAT_*; 0 for plain scenes).
+template <int FEAT>
 __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__ prog_g,
                                                    const DevScene* __restrict__ scene_g, PathSoA soa, DispatchGeom g,
                                                    FilmPlanes film, unsigned long long* stats) {
@@ -261,10 +287,17 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
     const bool absolute = hit_absolute(S);
     unsigned long long evals = 0, iters = 0, segs = 0;
     const uint32_t stream = point_stream_of(S, px, py);
+    const bool optics = (FEAT & SF_FEAT_RICH) && (S.rich & SF_RICH_OPTICS) != 0u;
     for (uint32_t s = 0; s < g.samples; ++s) {
         uint32_t sample = g.sample_start + s;
         PathState ps;
         path_begin(S, ps, px, py, sample);
+        if (optics) {  // the medium the camera ray starts in
+            const DeRaw r0 = de_raw_exact(P, ps.o);
+            evals++;
+            iters += r0.iter;
+            optics_initial_medium(S, ps, r0.d, r0.material);
+        }
         float* fd = nullptr;
         float4* fa = nullptr;
         for (;;) {
@@ -284,12 +317,20 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
             if (r == MARCH_HIT) {
                 h.hit = true;
                 h.t = m.cand_t;
+                bool optical = false;
+                if (optics && optics_enabled(material_optics(S, hs.material))) {
+                    h.t = optical_refine(P, ps.o, ps.d, h.t, evals, iters);
+                    hs = de_raw_exact(P, ps.o + ps.d * h.t);
+                    evals++;
+                    iters += hs.iter;
+                    optical = optics_enabled(material_optics(S, hs.material));
+                }
                 h.sample = de_finalize(P, hs);
                 float3 hp = ps.o + ps.d * h.t;
-                float hs = fmaxf(h.t * S.pixel_cone * 0.5f, 1e-4f) * S.pixel_tolerance;
+                const float tap_h = optical ? 1e-4f : fmaxf(h.t * S.pixel_cone * 0.5f, 1e-4f) * S.pixel_tolerance;
                 float3 grad = mk3(0.f, 0.f, 0.f);
                 for (uint32_t k = 0; k < 4; ++k) {
-                    DeRaw d = de_raw(P, hp + tetra_offset(k) * hs);
+                    DeRaw d = de_raw(P, hp + tetra_offset(k) * tap_h);
                     evals++;
                     iters += d.iter;
                     grad = grad + tetra_offset(k) * d.d;
@@ -310,19 +351,65 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
             // each shadow segment is traced as it is issued; its radiance lands in the
             // order the wavefront adds it (issue order, after the bounce's own terms)
             auto emit = [&](const ShadowReq& sh) {
-                uint32_t sli;
-                March sm;
-                float st_end = nearest_emitter(S, sh.o, sh.dir, sh.t_end, sli);
-                march_begin(sm, sh.o, sh.dir, st_end);
-                DeRaw shs;
-                int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, absolute, shs, evals, iters);
-                segs++;
-                if (sr == MARCH_MISS && sli == SF_NO_LIGHT) {
-                    ps.L = add_rn(ps.L, sh.contrib);
-                    if (sh.volume) ps.pv = add_rn(ps.pv, sh.contrib);
+                if (!optics) {
+                    uint32_t sli;
+                    March sm;
+                    float st_end = nearest_emitter(S, sh.o, sh.dir, sh.t_end, sli);
+                    march_begin(sm, sh.o, sh.dir, st_end);
+                    DeRaw shs;
+                    int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, absolute, shs, evals, iters);
+                    segs++;
+                    if (sr == MARCH_MISS && sli == SF_NO_LIGHT) {
+                        ps.L = add_rn(ps.L, sh.contrib);
+                        if (sh.volume) ps.pv = add_rn(ps.pv, sh.contrib);
+                    }
+                    return;
+                }
+                // geometry_visibility_weight (lights.wgsl:263-283): dielectric surfaces pass
+                // the segment weighted by 1 - opacity, up to 32 segments
+                float vis = 1.0f;
+                float3 origin = sh.o;
+                float remaining = sh.t_end;
+                bool clear = false;
+                for (uint32_t i = 0; i < 32u; ++i) {
+                    uint32_t sli;
+                    March sm;
+                    const float st_end = nearest_emitter(S, origin, sh.dir, remaining, sli);
+                    march_begin(sm, origin, sh.dir, st_end);
+                    DeRaw shs;
+                    const int sr = march_full(P, sm, S.max_steps, S.step_scale, accept, absolute, shs, evals, iters);
+                    segs++;
+                    if (sr == MARCH_EXHAUSTED) break;
+                    if (sr == MARCH_MISS) {
+                        clear = sli == SF_NO_LIGHT;
+                        break;
+                    }
+                    float t = sm.cand_t;
+                    if (optics_enabled(material_optics(S, shs.material))) {
+                        t = optical_refine(P, origin, sh.dir, t, evals, iters);
+                        shs = de_raw_exact(P, origin + sh.dir * t);
+                        evals++;
+                        iters += shs.iter;
+                    }
+                    const DevOptics& o = material_optics(S, shs.material);
+                    if (!optics_enabled(o)) break;
+                    vis *= 1.0f - o.surface[0];
+                    if (vis < 1e-6f) break;
+                    const float distance = t + 1e-4f;
+                    origin = origin + sh.dir * distance;
+                    remaining = remaining - distance;
+                    if (remaining <= 0.0f) {
+                        clear = true;
+                        break;
+                    }
+                }
+                if (clear) {
+                    const float3 c = sh.contrib * vis;
+                    ps.L = add_rn(ps.L, c);
+                    if (sh.volume) ps.pv = add_rn(ps.pv, c);
                 }
             };
-            int cont = bounce_body(S, ps, h, emit, fd, fa, sample, stream);
+            int cont = bounce_body<FEAT>(S, ps, h, emit, fd, fa, sample, stream);
             if (cont != PATH_CONTINUE) break;
         }
         soa.Ls[(size_t)s * tile_px + local] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
@@ -614,9 +701,12 @@ cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene
     default: return sf_launch_trace_any(prog, scene, soa, tl, stats, blocks, min_blocks, st);
     }
 }
-cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
-                            uint32_t* status, int final_round, cudaStream_t st) {
-    k_shade<<<grid_for(g.paths, 256, 16), 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
+cudaError_t sf_launch_shade(const DevScene* scene, uint32_t rich, PathSoA soa, RoundQueues q, DispatchGeom g,
+                            FilmPlanes film, uint32_t* status, int final_round, cudaStream_t st) {
+    const dim3 grid = grid_for(g.paths, 256, 16);
+    if (rich & SF_RICH_TEXTURE) k_shade<3><<<grid, 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
+    else if (rich) k_shade<1><<<grid, 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
+    else k_shade<0><<<grid, 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st) {
@@ -624,10 +714,12 @@ cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaS
     k_commit<<<(n + 255) / 256, 256, 0, st>>>(soa, g, film);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, PathSoA soa, DispatchGeom g,
-                                 FilmPlanes film, unsigned long long* stats, cudaStream_t st) {
+cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, uint32_t rich, PathSoA soa,
+                                 DispatchGeom g, FilmPlanes film, unsigned long long* stats, cudaStream_t st) {
     dim3 grid((g.tile_w + 7) / 8, (g.tile_h + 7) / 8);
-    k_megakernel<<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
+    if (rich & SF_RICH_TEXTURE) k_megakernel<3><<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
+    else if (rich) k_megakernel<1><<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
+    else k_megakernel<0><<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,

@@ -7,6 +7,8 @@
 
 // Path flags kept in the path state.
 enum { SF_PF_CONT = 1u, SF_PF_SHADOW = 2u, SF_PF_FROM_BSDF = 4u, SF_PF_FROM_VOLUME = 8u };
+// PathSoA.ex.z bits above the medium slot.
+enum { SF_EX_SOLID = 1u << 8, SF_EX_INIT = 1u << 9 };
 #define SF_PF_SHADOW_SHIFT 8  // bits 8..15 of the flags: which shadow slots hold a segment
 // Hit record flags.
 enum { SF_HF_HIT = 1u, SF_HF_EXHAUSTED = 2u };
@@ -44,6 +46,10 @@ struct PathSoA {
     // pending shadow slots | the camera segment scattered << 8); the sample's volume
     // part once the path ends
     float4* pv;
+    // scenes with finish details, a texture or optics only (null otherwise): x = the
+    // transported texture width, y = its spread, z = bits(medium slot | inside a solid
+    // medium << 8 | initial medium pending << 9), w = bits(coverage null events taken)
+    float4* ex;
     uint32_t capacity;
     uint32_t shadow_slots;  // K: sh_o/sh_d/sh_c/vis have K * capacity rows (row = k * capacity + path)
 };
@@ -76,6 +82,7 @@ struct TraceLaunch {
     uint32_t quantum;             // march steps per segment per launch (0 = unbounded)
     uint32_t regen;               // idle lanes a warp waits for before it takes new segments (1..32)
     uint32_t lane_stats;          // 1: count warp-level DE calls and iteration slots (diagnostic kernel)
+    uint32_t optics;              // 1: the scene has dielectric materials (the optics trace kernel)
 };
 
 struct FilmPlanes {
@@ -166,7 +173,7 @@ cudaError_t sf_launch_shade_batch(BatchTable bt, PathSoA soa, RoundQueues q, uin
                                   cudaStream_t st);
 cudaError_t sf_launch_commit_batch(BatchTable bt, PathSoA soa, cudaStream_t st);
 cudaError_t sf_launch_advance_batch(BatchTable bt, cudaStream_t st);
-cudaError_t sf_launch_shade(const DevScene* scene, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
+cudaError_t sf_launch_shade(const DevScene* scene, uint32_t rich, PathSoA soa, RoundQueues q, DispatchGeom g, FilmPlanes film,
                             uint32_t* status, int final_round, cudaStream_t st);
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st);
 
@@ -186,7 +193,7 @@ struct PreviewOut {
 cudaError_t sf_launch_preview(const DeProgram* prog, const DevScene* scene, uint32_t pixels, PreviewState st,
                               PreviewOut out, uint32_t quantum, uint32_t init, uint32_t* status, cudaStream_t s);
 cudaError_t sf_launch_film_clear(FilmPlanes film, cudaStream_t st);
-cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, PathSoA soa, DispatchGeom g,
+cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, uint32_t rich, PathSoA soa, DispatchGeom g,
                                  FilmPlanes film, unsigned long long* stats, cudaStream_t st);
 cudaError_t sf_launch_planar(const PlanarDev* f, const float* x, const float* y, size_t n, float* dist, float* traps,
                              uint32_t* iters, cudaStream_t st);

@@ -602,6 +602,8 @@ extern "C" sf_status sf_serve_submit(sf_server* s, const sf_request* q, uint64_t
         sf_status st = validate_config(q->cfg);
         if (st != SF_OK) return st;
         if (const sf_status sc = scene_check(q->scene); sc != SF_OK) return sc;
+        if (rich_of(q->scene))
+            return fail(SF_ERR_UNSUPPORTED, "finish details, textures and optics render through sessions, not the server");
         if (has_hdri(q->scene)) return fail(SF_ERR_UNSUPPORTED, "HDRI panoramas are rendered by sessions, not served");
         if (shadow_slots_of(q->scene) > kServeShadowSlots)
             return fail(SF_ERR_UNSUPPORTED, "the server's arenas hold 3 shadow segments per bounce");

@@ -14,6 +14,7 @@ static __device__ __forceinline__ void path_pixel(const DispatchGeom& g, uint32_
     py = g.tile_y + local / g.tile_w;
 }
 
+template <int FEAT = 0>
 static __device__ __forceinline__ void store_path(PathSoA& soa, uint32_t path, const PathState& ps, uint32_t flags) {
     soa.o[path] = make_float4(ps.o.x, ps.o.y, ps.o.z, ps.prev_pdf);
     soa.d[path] = make_float4(ps.d.x, ps.d.y, ps.d.z, ps.prev_area_total);
@@ -21,7 +22,15 @@ static __device__ __forceinline__ void store_path(PathSoA& soa, uint32_t path, c
     uint32_t f = flags | (ps.prev_from_bsdf ? SF_PF_FROM_BSDF : 0u) | (ps.prev_from_volume ? SF_PF_FROM_VOLUME : 0u);
     soa.L[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, __uint_as_float(ps.bounce | (f << 16)));
     soa.pn[path] = make_float4(ps.prev_normal.x, ps.prev_normal.y, ps.prev_normal.z, 0.f);
+    if ((FEAT & SF_FEAT_RICH) && soa.ex) {
+        const float4 e = soa.ex[path];  // keeps a pending initial-medium flag (set by generate)
+        const uint32_t keep = __float_as_uint(e.z) & SF_EX_INIT;
+        soa.ex[path] = make_float4(ps.tex_width, ps.tex_spread,
+                                   __uint_as_float(ps.medium_slot | (ps.solid_medium ? SF_EX_SOLID : 0u) | keep),
+                                   __uint_as_float(ps.null_surfaces));
+    }
 }
+template <int FEAT = 0>
 static __device__ __forceinline__ uint32_t load_path(const PathSoA& soa, uint32_t path, PathState& ps) {
     float4 o = soa.o[path], d = soa.d[path], tp = soa.tp[path], L = soa.L[path], pn = soa.pn[path];
     ps.o = mk3(o.x, o.y, o.z);
@@ -37,6 +46,20 @@ static __device__ __forceinline__ uint32_t load_path(const PathSoA& soa, uint32_
     ps.prev_from_bsdf = (flags & SF_PF_FROM_BSDF) != 0;
     ps.prev_from_volume = (flags & SF_PF_FROM_VOLUME) != 0;
     ps.prev_normal = mk3(pn.x, pn.y, pn.z);
+    ps.tex_width = 0.0f;
+    ps.tex_spread = 0.0f;
+    ps.solid_medium = false;
+    ps.medium_slot = 0;
+    ps.null_surfaces = 0;
+    if ((FEAT & SF_FEAT_RICH) && soa.ex) {
+        const float4 e = soa.ex[path];
+        ps.tex_width = e.x;
+        ps.tex_spread = e.y;
+        const uint32_t m = __float_as_uint(e.z);
+        ps.medium_slot = m & 0xffu;
+        ps.solid_medium = (m & SF_EX_SOLID) != 0u;
+        ps.null_surfaces = __float_as_uint(e.w);
+    }
     return flags;
 }
 
@@ -61,6 +84,8 @@ static __device__ __forceinline__ void generate_path(const DevScene& S, PathSoA&
     path_pixel(g, local, px, py, sample);
     PathState ps;
     path_begin(S, ps, px, py, sample);
+    if (soa.ex)  // the trace kernel samples the initial medium of optics scenes first
+        soa.ex[path] = make_float4(0.f, 0.f, __uint_as_float((S.rich & SF_RICH_OPTICS) ? SF_EX_INIT : 0u), 0.f);
     store_path(soa, path, ps, SF_PF_CONT);
     if (soa.pv) soa.pv[path] = make_float4(0.f, 0.f, 0.f, 0.f);
     begin_segment(S, soa, path, ps.o, ps.d, S.extent);
@@ -68,11 +93,12 @@ static __device__ __forceinline__ void generate_path(const DevScene& S, PathSoA&
 
 // wf_shade + wf_compact (wavefront.wgsl:196-223) for one path: resolve last round's
 // shadow segment, run the bounce body on this round's hit, return the next flags.
+template <int FEAT = 0>
 static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA& soa, const DispatchGeom& g,
                                                       const FilmPlanes& film, uint32_t local, uint32_t path,
                                                       uint32_t* status, int final_round) {
     PathState ps;
-    uint32_t flags = load_path(soa, path, ps);
+    uint32_t flags = load_path<FEAT>(soa, path, ps);
     const size_t cap = soa.capacity;
     // the volume layer split (fog scenes): the camera segment's in-scattered light and
     // the volume tags of last round's shadow slots
@@ -90,9 +116,12 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
         for (uint32_t k = 0; k < soa.shadow_slots; ++k) {
             const size_t row = k * cap + path;
             if (((mask >> k) & 1u) && soa.vis[row]) {
-                const float4 c = soa.sh_c[row];
-                ps.L = add_rn(ps.L, mk3(c.x, c.y, c.z));
-                if ((vbits >> k) & 1u) ps.pv = add_rn(ps.pv, mk3(c.x, c.y, c.z));
+                const float4 c4 = soa.sh_c[row];
+                float3 c = mk3(c4.x, c4.y, c4.z);
+                if ((FEAT & SF_FEAT_RICH) && (S.rich & SF_RICH_OPTICS))
+                    c = c * soa.sh_d[row].w;  // the coverage of crossed surfaces
+                ps.L = add_rn(ps.L, c);
+                if ((vbits >> k) & 1u) ps.pv = add_rn(ps.pv, c);
             }
         }
     }
@@ -132,14 +161,14 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
             }
             const size_t row = n_sh * cap + path;
             soa.sh_o[row] = make_float4(sh.o.x, sh.o.y, sh.o.z, sh.t_end);
-            soa.sh_d[row] = make_float4(sh.dir.x, sh.dir.y, sh.dir.z, 0.f);
+            soa.sh_d[row] = make_float4(sh.dir.x, sh.dir.y, sh.dir.z, 1.f);  // w: visibility weight
             soa.sh_c[row] = make_float4(sh.contrib.x, sh.contrib.y, sh.contrib.z, 0.f);
             begin_segment(S, soa, uint32_t(cap + row), sh.o, sh.dir, sh.t_end);
             sh_mask |= 1u << n_sh;
             if (sh.volume) vmask |= 1u << n_sh;
             n_sh++;
         };
-        int r = bounce_body(S, ps, h, emit, fd, fa, sample, point_stream_of(S, px, py));
+        int r = bounce_body<FEAT>(S, ps, h, emit, fd, fa, sample, point_stream_of(S, px, py));
         if (sh_mask) nf |= SF_PF_SHADOW | (sh_mask << SF_PF_SHADOW_SHIFT);
         if (r == PATH_CONTINUE) nf |= SF_PF_CONT;
     }
@@ -147,7 +176,7 @@ static __device__ __forceinline__ uint32_t shade_path(const DevScene& S, PathSoA
         atomicOr(status, SF_WF_ALIVE_AT_COMMIT);
         nf = 0;
     }
-    store_path(soa, path, ps, nf);
+    store_path<FEAT>(soa, path, ps, nf);
     if (nf & SF_PF_CONT) begin_segment(S, soa, path, ps.o, ps.d, S.extent);
     if (!nf) soa.Ls[path] = make_float4(ps.L.x, ps.L.y, ps.L.z, 1.0f);
     if (soa.pv) {

@@ -11,6 +11,10 @@
 #include "sf_surface.cuh"
 
 #define SF_NO_LIGHT 0xffffffffu
+// What a shading kernel is built with (a template argument of make_surface, bounce_body
+// and the kernels that inline them): finish details, optics and the transported
+// footprint; the volumetric texture's interpreter.
+enum { SF_FEAT_RICH = 1, SF_FEAT_TEX = 2 };
 
 // ------------------------------------------------------------------ RNG
 __device__ __forceinline__ uint32_t pcg(uint32_t v) {
@@ -306,10 +310,11 @@ static __device__ float bsdf_pdf(const Surface& s, float3 v, float3 l, float p_s
 }
 // make_surface (pathtrace.wgsl:271-386): the colouring ramp or orbit mix, the finish
 // of a MaterialTag, surface variation, the finish's world-space detail and, on
-// untagged surfaces, the volumetric texture (TEX: kernels built with the texture
-// interpreter). p is the hit point, n the shading-side normal, v toward the eye and
-// footprint the path's transported texture width.
-template <bool TEX = false>
+// untagged surfaces, the volumetric texture. FEAT selects what the calling kernel is
+// built with: SF_FEAT_RICH (finish details, optics, the footprint), SF_FEAT_TEX (the
+// texture's interpreter); 0 is the plain surface. p is the hit point, n the
+// shading-side normal, v toward the eye and footprint the path's texture width.
+template <int FEAT = 0>
 static __device__ Surface make_surface(const DevScene& S, float3 p, float3 n, float3 v, const DeSampleF& smp,
                                        float footprint) {
     const DevMaterial* m = &S.material;
@@ -337,7 +342,7 @@ static __device__ Surface make_surface(const DevScene& S, float3 p, float3 n, fl
     }
     float3 shading_n = n;
     float diffuse_sigma = 0.0f;
-    if (assigned && (S.rich & SF_RICH_DETAIL) && S.details[smp.material - 1].kind != 0u) {
+    if ((FEAT & SF_FEAT_RICH) && assigned && (S.rich & SF_RICH_DETAIL) && S.details[smp.material - 1].kind != 0u) {
         const DevDetail& f = S.details[smp.material - 1];
         float4 detail = finish_eval(f, p, footprint, S.dune_wind);
         if (f.kind == 9u) detail = scale4(detail, sstep(0.10f, 0.80f, n.y));  // powder settles on tops
@@ -361,7 +366,7 @@ static __device__ Surface make_surface(const DevScene& S, float3 p, float3 n, fl
         if (fabsf(f.mapping[2]) > 0.0f) shading_n = finish_normal(f.mapping[2], n, xyz(detail));
         if (f.kind >= 10u) diffuse_sigma = 1.0f;  // times the final roughness below
     }
-    if constexpr (TEX) {
+    if constexpr ((FEAT & SF_FEAT_TEX) != 0) {
         const DevTexture& T = S.tex;
         const float amount = texture_mask(T, smp.traps);
         if (!assigned && T.effects[3] > 0.0f && amount > 0.0f) {
@@ -384,7 +389,7 @@ static __device__ Surface make_surface(const DevScene& S, float3 p, float3 n, fl
     s.f0 = mk3(spec, spec, spec) * (1.0f - metallic) + albedo * metallic;
     s.alpha = rough * rough;
     s.emission = emission;
-    s.diffuse_sigma = diffuse_sigma * rough * 0.45f;
+    s.diffuse_sigma = (FEAT & SF_FEAT_RICH) ? diffuse_sigma * rough * 0.45f : 0.0f;
     return s;
 }
 
@@ -725,8 +730,6 @@ __device__ __forceinline__ float volume_light_probability(float weight, float to
     if (total <= 0.0f) return 0.0f;
     return fminf(1.0f, wdiv(3.0f * weight, total));
 }
-__device__ __forceinline__ float mixf(float x, float y, float a) { return fmaf(x, 1.0f - a, y * a); }
-
 // fog_segment_direct (pathtrace.wgsl:635-715): in-scattered emitter light along the
 // segment [0, end] of the current ray as a line integral. Each area light passes an
 // independent roulette; the point on the segment mixes equiangular sampling about a
@@ -883,21 +886,118 @@ static __device__ void fog_direct_light(const DevScene& S, float3 tpc, float3 p,
 // drawn along it may scatter the path (next events for the sky lights, phase-sampled
 // continuation) before the hit is reached. `point_index` is the sample index and
 // `point_stream` the pixel's rotation (point_stream_of) of the primary segment's points.
-template <class Emit>
+// optical_bounce (optics.wgsl:30-64) without dispersion or thin-film coating: the
+// dielectric's VNDF reflection or transmission (a thin sheet passes straight through
+// with its absorption tint), drawn as its own mixture component.
+struct OpticalBounce {
+    float3 direction, weight;
+    bool transmitted, valid;
+};
+static __device__ OpticalBounce optical_bounce(const DevOptics& o, float3 n, float3 rd, float alpha, bool entering,
+                                               uint32_t& rng) {
+    OpticalBounce b;
+    const float index = o.surface[2];
+    const bool thin = o.surface[3] > 0.0f;
+    const float3 tint = exp3(mk3(-o.absorption[0] * o.absorption[3], -o.absorption[1] * o.absorption[3],
+                                 -o.absorption[2] * o.absorption[3]));
+    if (index <= 1.0001f) {
+        b.direction = rd;
+        b.weight = thin ? tint : mk3(1.f, 1.f, 1.f);
+        b.transmitted = true;
+        b.valid = true;
+        return b;
+    }
+    const float eta = (entering || thin) ? wdiv(1.0f, index) : index;
+    const float r1 = rnd(rng);
+    const float r2 = rnd(rng);
+    const float3 h = sample_ggx_h(n, -rd, alpha, r1, r2);
+    float f = dielectric_fresnel(fmaxf(0.0f, dot3(-rd, h)), eta);
+    if (thin) f = wdiv(2.0f * f, 1.0f + f);
+    float3 color = mk3(f, f, f);
+    float probability = f;
+    const float3 transmitted = refract3(rd, h, eta);
+    if (!thin && dot3(transmitted, transmitted) < 0.5f) {  // total internal reflection
+        color = mk3(1.f, 1.f, 1.f);
+        probability = 1.0f;
+    }
+    const float a2 = alpha * alpha;
+    if (rnd(rng) < probability) {
+        b.direction = reflect3(rd, h);
+        const float cosine = dot3(n, b.direction);
+        b.weight = color * wdiv(smith_g1(fmaxf(cosine, 1e-6f), a2), fmaxf(probability, 1e-20f));
+        b.transmitted = false;
+        b.valid = cosine > 0.0f;
+        return b;
+    }
+    b.direction = thin ? rd : transmitted;
+    const float cosine = -dot3(n, b.direction);
+    const float3 w = thin ? tint : mk3(1.f, 1.f, 1.f) * (smith_g1(fmaxf(cosine, 1e-6f), a2) * eta * eta);
+    b.weight = w * (mk3(1.f, 1.f, 1.f) - color) * wdiv(1.0f, fmaxf(1.0f - probability, 1e-20f));
+    b.transmitted = true;
+    b.valid = cosine > 0.0f && dot3(b.direction, b.direction) > 0.5f;
+    return b;
+}
+
+// One bounce of `radiance` (pathtrace.wgsl:841-1196) after its trace: the interior
+// medium of a dielectric (absorption, subsurface scattering), hit classification, sky
+// and emitter emission with MIS, the optics of the hit (coverage null events, the
+// dielectric lobe), surface, next-event sampling (direct_light, pathtrace.wgsl:471-558:
+// every environment and sun, and the one selected area light, in scene order; each
+// visibility test is handed to `emit`, which adds its radiance if the segment is
+// clear) and BSDF continuation with Russian roulette. Writes first-hit depth/aux at
+// bounce 0. In fog (pathtrace.wgsl:980-1011) the segment first adds its in-scattered
+// emitter light, then a collision drawn along it may scatter the path (next events
+// for the sky lights, phase-sampled continuation) before the hit is reached.
+// `point_index` is the sample index and `point_stream` the pixel's rotation
+// (point_stream_of) of the primary segment's points. A surface hit on a material with
+// optics carries the refined hit and the normal of optical_refine_hit (optics.wgsl:
+// 7-23) and normal_at(p, 1e-4), made by the trace. FEAT: as make_surface's (the
+// optics and the footprint transport need SF_FEAT_RICH).
+template <int FEAT = 0, class Emit>
 static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInfo& h, Emit&& emit, float* first_depth,
                                   float4* first_aux, uint32_t point_index, uint32_t point_stream) {
+    constexpr bool RICH = (FEAT & SF_FEAT_RICH) != 0;
+    const bool optics = RICH && (S.rich & SF_RICH_OPTICS) != 0u;
+    if (optics && ps.solid_medium) {  // inside a dielectric solid (pathtrace.wgsl:857-875)
+        const DevOptics& medium = material_optics(S, ps.medium_slot);
+        float distance = h.t;
+        if (medium.subsurface[3] > 0.0f)
+            distance = fminf(h.t, wdiv(-logf(fmaxf(1e-7f, 1.0f - rnd(ps.rng))), medium.subsurface[3]));
+        ps.tp = ps.tp * exp3(mk3(-medium.absorption[0] * distance, -medium.absorption[1] * distance,
+                                 -medium.absorption[2] * distance));
+        if (distance < h.t) {
+            if (ps.bounce == S.max_bounces) return PATH_DONE;
+            ps.tp = ps.tp * ld3(medium.subsurface);
+            const float r1 = rnd(ps.rng);
+            const float r2 = rnd(ps.rng);
+            ps.o = ps.o + ps.d * distance;
+            ps.d = hg_sample(ps.d, 0.0f, r1, r2);
+            // no MIS after a subsurface collision: emitters reached next count in full
+            ps.prev_from_bsdf = false;
+            ps.prev_from_volume = false;
+            ps.prev_pdf = 0.0f;
+            ps.tex_spread = fmaxf(ps.tex_spread, 0.25f);
+            ps.bounce += 1;
+            return PATH_CONTINUE;
+        }
+    }
     if (h.hit && ps.bounce == 0 && first_depth) {
         *first_depth = h.t;
         const float3 en = h.light_index != SF_NO_LIGHT ? ld3(S.lights[h.light_index].n) : h.n;
         *first_aux = make_float4(en.x, en.y, en.z, float(h.steps));
     }
-    const bool fog = S.fog[0] > 0.0f;
+    const bool fog = S.fog[0] > 0.0f && !(RICH && ps.solid_medium);
     if (fog) {
         const float t_end = h.hit ? h.t : S.extent;
-        fog_segment_direct(S, ps.tp, ps.o, ps.d, t_end, ps.rng, point_index, point_stream, ps.bounce == 0, emit);
+        fog_segment_direct(S, ps.tp, ps.o, ps.d, t_end, ps.rng, point_index, point_stream,
+                           ps.bounce == 0 && (!RICH || ps.null_surfaces == 0), emit);
         const float t_s = fog_free_flight(S, ps.o, ps.d, t_end, ps.rng);
         if (t_s < t_end) {
             if (ps.bounce == 0) ps.volume_path = true;
+            if (RICH) {
+                ps.tex_width += t_s * ps.tex_spread;
+                ps.tex_spread = fmaxf(ps.tex_spread, 0.25f);
+            }
             if (ps.bounce == 0 && !h.hit && first_depth) *first_depth = t_s;
             const float3 p_s = ps.o + ps.d * t_s;
             const float volume_area_total = area_total_weight(S, p_s, mk3(0.f, 0.f, 0.f));
@@ -938,14 +1038,56 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
         return PATH_DONE;
     }
     float3 n = h.n;
+    bool optical = false, entering = true;
+    if (optics) {  // pathtrace.wgsl:1053-1066
+        const DevOptics& o = material_optics(S, h.sample.material);
+        optical = optics_enabled(o);
+        entering = dot3(ps.d, h.n) < 0.0f;
+        if (optical && !entering) n = -n;
+        if (optical && o.surface[0] < 1.0f && rnd(ps.rng) >= o.surface[0]) {
+            // a coverage null event: the path passes the surface within the same bounce
+            ps.null_surfaces += 1;
+            if (ps.null_surfaces > 32u) return PATH_DONE;
+            ps.o = p + ps.d * fmaxf(h.t * S.pixel_cone * 0.15f * S.pixel_tolerance, 1e-4f);
+            if (ps.bounce == 0 && first_depth) {
+                *first_depth = -1.0f;
+                *first_aux = make_float4(0.f, 0.f, 0.f, -1.0f);
+            }
+            return PATH_CONTINUE;
+        }
+        if (optical && ps.bounce == 0 && first_depth) *first_aux = make_float4(n.x, n.y, n.z, float(h.steps));
+    }
     if (ps.bounce == 0) {
         float x = fminf(fmaxf(float(h.steps) / 96.0f, 0.0f), 1.0f);
         ps.tp = ps.tp * (1.0f - S.cavity * (x * x * (3.0f - 2.0f * x)));
     }
     float3 v = -ps.d;
-    Surface s = make_surface(S, n, h.sample);
+    if (RICH) ps.tex_width += h.t * ps.tex_spread;
+    Surface s = make_surface<FEAT>(S, p, n, v, h.sample, fmaxf(ps.tex_width, 1e-4f));
     ps.L = ps.L + ps.tp * s.emission;
     float offset = fmaxf(h.t * S.pixel_cone * 2.0f, 1e-3f) * S.pixel_tolerance;
+    if (optical) {
+        const DevOptics& o = material_optics(S, h.sample.material);
+        if (o.surface[1] > 0.0f && rnd(ps.rng) < o.surface[1]) {  // the dielectric lobe (:1088-1107)
+            if (ps.bounce == S.max_bounces) return PATH_DONE;
+            const OpticalBounce b = optical_bounce(o, n, ps.d, s.alpha, entering, ps.rng);
+            if (!b.valid) return PATH_DONE;
+            ps.tp = ps.tp * b.weight;
+            const float bias = fmaxf(1e-4f, fminf(offset, 0.001f));
+            ps.o = p + b.direction * bias;
+            ps.d = b.direction;
+            if (b.transmitted && o.surface[3] == 0.0f) {
+                ps.solid_medium = entering;
+                ps.medium_slot = h.sample.material;
+            }
+            ps.prev_from_bsdf = false;
+            ps.prev_from_volume = false;
+            ps.prev_pdf = 0.0f;
+            ps.tex_spread = fmaxf(ps.tex_spread, s.alpha * 0.1f);
+            ps.bounce += 1;
+            return PATH_CONTINUE;
+        }
+    }
     float3 p_off = p + n * offset;
     float nv = fmaxf(dot3(s.n, v), 1e-4f);
     float p_spec = spec_probability(s, nv);
@@ -1077,6 +1219,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     }
     ps.o = p_off;
     ps.d = ldir;
+    if (RICH) ps.tex_spread = fmaxf(ps.tex_spread, s.alpha * 0.25f);
     ps.bounce += 1;
     return PATH_CONTINUE;
 }

@@ -15,7 +15,7 @@
 #include "sf_trace.cuh"
 #include "sf_warp.cuh"
 
-enum { TL_IDLE = 0, TL_MARCH = 1, TL_CAND = 2, TL_NORMAL = 3, TL_DONE = 4 };
+enum { TL_IDLE = 0, TL_MARCH = 1, TL_CAND = 2, TL_NORMAL = 3, TL_DONE = 4, TL_INIT = 5, TL_REFINE = 6, TL_FINAL = 7 };
 #define SF_FORM_ANY 99u
 #define SF_FORM_MIXED 98u  // any of the three iterated forms, chosen per lane
 
@@ -48,7 +48,14 @@ static __device__ __forceinline__ uint32_t find_job(const uint32_t* begins, uint
 // program and scene (L1-cached global memory) when it takes an item.
 // LANE_STATS: also count warp-level DE calls and, per call, the warp's longest
 // iteration count times its active lanes (a diagnostic of SIMT lane use).
-template <int FORM, int MIN_BLOCKS, bool MULTI = false, bool LANE_STATS = false>
+// OPTICS (single job, scenes with dielectric materials): a path's first segment
+// samples the field at its origin for the medium it starts in (pathtrace.wgsl:833-840);
+// a hit on a material with optics is refined by Newton steps on the exact field
+// (optical_refine_hit, optics.wgsl:7-23) and, for a continuation, its normal taken at
+// 1e-4; a shadow segment crosses such surfaces, its weight (PathSoA.sh_d.w) times
+// 1 - opacity at each, and marches on from just past them, up to 32 crossings
+// (geometry_visibility_weight, lights.wgsl:263-283).
+template <int FORM, int MIN_BLOCKS, bool MULTI = false, bool LANE_STATS = false, bool OPTICS = false>
 __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __restrict__ prog_g,
                                                            const DevScene* __restrict__ scene_g, PathSoA soa,
                                                            TraceLaunch tl, unsigned long long* stats,
@@ -131,6 +138,31 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
         state = TL_NORMAL;
     };
 
+    // OPTICS: a march that found a surface with sample s (at m.t): refine it when its
+    // material has optics, else end a shadow segment or record a continuation's hit.
+    auto on_hit = [&](const DeRaw& s) {
+        if (OPTICS && optics_enabled(material_optics(S, s.material))) {
+            hstep = fmaxf(1e-5f, fminf(1e-3f, m.t * 1e-5f));  // the Newton step's difference
+            tap = 0;                                           // iteration * 3 + tap of the step
+            state = TL_REFINE;
+        } else if (shadow) {
+            finish(MARCH_HIT);
+        } else {
+            surface_hit(s);
+        }
+    };
+    // OPTICS: the march of a fresh segment from its loaded state.
+    auto start = [&]() {
+        state = TL_MARCH;
+        int r = march_check(m, TR_MAX_STEPS, TR_ACCEPT);
+        if (r == MARCH_HIT) {
+            if (shadow && !OPTICS) finish(MARCH_HIT);
+            else { m.t = m.cand_t; state = TL_CAND; }
+        } else if (r != MARCH_CONTINUE) {
+            finish(r);
+        }
+    };
+
     const uint32_t regen = tl.regen ? tl.regen : 1u;
     while (true) {
         // Two votes per DE call decide the warp's next move: all lanes done ends the
@@ -181,29 +213,27 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
                     li = soa.m2[row];
                     budget = quantum;
-                    state = TL_MARCH;
-                    int r = march_check(m, TR_MAX_STEPS, TR_ACCEPT);
-                    if (r == MARCH_HIT) {
-                        if (shadow) finish(MARCH_HIT);
-                        else { m.t = m.cand_t; state = TL_CAND; }
-                    } else if (r != MARCH_CONTINUE) {
-                        finish(r);
-                    }
+                    if (OPTICS && !shadow && first &&
+                        (__float_as_uint(soa.ex[path].z) & SF_EX_INIT) != 0u) state = TL_INIT;
+                    else start();
                 }
             }
         }
-        if (state == TL_MARCH || state == TL_CAND || state == TL_NORMAL) {
+        if (state != TL_IDLE && state != TL_DONE) {
             float3 q = m.ro + m.rd * m.t;
             if (state == TL_NORMAL) q = q + tetra_offset(tap) * hstep;
+            if (OPTICS && state == TL_REFINE && tap % 3u != 0u) q = q + m.rd * (tap % 3u == 1u ? hstep : -hstep);
             // the single-job kernel reads the program from shared memory by name (LDS)
             DeRaw s;
+            const bool exact_state = OPTICS && (state == TL_INIT || state == TL_REFINE || state == TL_FINAL);
             if constexpr (MULTI) s = de_form<FORM>(*Pl, q);
+            else if constexpr (FORM == SF_FORM_ANY && OPTICS) s = exact_state ? de_raw_exact(P, q) : de_form<FORM>(P, q);
             else s = de_form<FORM>(P, q);
             n_eval++;
             n_iter += s.iter;
             if constexpr (FORM == SF_FORM_ANY) {
                 // a flagged march or candidate sample near acceptance: the exact sample
-                if (state != TL_NORMAL && needs_exact(s, m.t, TR_SAFETY, TR_ACCEPT, TR_ABSOLUTE)) {
+                if (state != TL_NORMAL && !exact_state && needs_exact(s, m.t, TR_SAFETY, TR_ACCEPT, TR_ABSOLUTE)) {
                     if constexpr (MULTI) s = de_raw_exact(*Pl, q);
                     else s = de_raw_exact(P, q);
                     n_eval++;
@@ -232,18 +262,88 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
                     state = TL_IDLE;
                 }
             } else if (state == TL_CAND) {
-                surface_hit(s);
+                if constexpr (OPTICS) on_hit(s);
+                else surface_hit(s);
+            } else if (OPTICS && state == TL_INIT) {
+                // the medium the path starts in, then its first march
+                const DevOptics& o = material_optics(S, s.material);
+                const bool solid = s.d < 0.0f && optics_enabled(o) && o.surface[1] > 0.0f && o.surface[3] == 0.0f;
+                soa.ex[path].z = __uint_as_float(s.material | (solid ? SF_EX_SOLID : 0u));
+                start();
+            } else if (OPTICS && state == TL_REFINE) {
+                const uint32_t k = tap % 3u;
+                if (k == 0u) {
+                    gx = s.d;
+                    if (fabsf(s.d) < 1e-5f) state = TL_FINAL;
+                    else tap++;
+                } else if (k == 1u) {
+                    gy = s.d;
+                    tap++;
+                } else {
+                    const float derivative = (gy - s.d) / (2.0f * hstep);
+                    if (fabsf(derivative) < 1e-5f) {
+                        state = TL_FINAL;
+                    } else {
+                        m.t = fmaxf(0.0f, m.t - fminf(fmaxf(gx / derivative, -0.5f), 0.5f));
+                        tap++;
+                        if (tap == 24u) state = TL_FINAL;  // eight Newton steps
+                    }
+                }
+            } else if (OPTICS && state == TL_FINAL) {
+                const DevOptics& o = material_optics(S, s.material);
+                if (!shadow) {
+                    // the refined hit, its sample and the normal taps (1e-4 on a dielectric)
+                    const DeSampleF smp = de_finalize(P, s);
+                    soa.hit[path] = make_uint4(__float_as_uint(m.t), m.i, SF_NO_LIGHT, SF_HF_HIT);
+                    soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
+                    hit_w = smp.iter | (smp.material << 16);
+                    hstep = optics_enabled(o) ? 1e-4f : fmaxf(m.t * TR_CONE * 0.5f, 1e-4f) * TR_TOL;
+                    gx = gy = gz = 0.f;
+                    tap = 0;
+                    state = TL_NORMAL;
+                } else if (!optics_enabled(o)) {
+                    finish(MARCH_HIT);
+                } else {
+                    // cross the surface: its coverage weighs the segment, which marches on
+                    float4 so = soa.sh_o[item];
+                    float4 sd = soa.sh_d[item];
+                    float4 sc = soa.sh_c[item];
+                    sd.w *= 1.0f - o.surface[0];
+                    sc.w += 1.0f;
+                    const float distance = m.t + 1e-4f;
+                    const float3 origin = m.ro + m.rd * distance;
+                    const float remaining = so.w - distance;
+                    if (sd.w < 1e-6f) {
+                        soa.vis[item] = 0u;
+                        state = TL_IDLE;
+                    } else if (remaining <= 0.0f) {
+                        soa.sh_d[item] = sd;
+                        soa.vis[item] = 1u;
+                        state = TL_IDLE;
+                    } else if (sc.w >= 32.0f) {  // the 32 segments of the visibility loop spent
+                        soa.vis[item] = 0u;
+                        state = TL_IDLE;
+                    } else {
+                        soa.sh_o[item] = make_float4(origin.x, origin.y, origin.z, remaining);
+                        soa.sh_d[item] = sd;
+                        soa.sh_c[item] = sc;
+                        const float te = nearest_emitter(S, origin, m.rd, remaining, li);
+                        march_begin(m, origin, m.rd, te);
+                        start();
+                    }
+                }
             } else {
                 int r = march_update(m, s.d, s.flags, TR_SAFETY, TR_ACCEPT, TR_ABSOLUTE);
                 if (r == MARCH_HIT) {
-                    if (shadow) finish(MARCH_HIT);
+                    if constexpr (OPTICS) on_hit(s);
+                    else if (shadow) finish(MARCH_HIT);
                     else surface_hit(s);
                 } else if (r != MARCH_CONTINUE) {
                     finish(r);
                 } else {
                     r = march_check(m, TR_MAX_STEPS, TR_ACCEPT);
                     if (r == MARCH_HIT) {  // candidate accepted at the step budget
-                        if (shadow) finish(MARCH_HIT);
+                        if (shadow && !OPTICS) finish(MARCH_HIT);
                         else { m.t = m.cand_t; state = TL_CAND; }
                     } else if (r != MARCH_CONTINUE) {
                         finish(r);
@@ -282,6 +382,10 @@ __global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __re
 template <int FORM>
 static cudaError_t launch_trace_form(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
                                      unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
+    if (tl.optics) {
+        k_trace<FORM, 2, false, false, true><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats);
+        return cudaGetLastError();
+    }
     if (tl.lane_stats && min_blocks == 3) {
         k_trace<FORM, 3, false, true><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats);
         return cudaGetLastError();
