@@ -846,6 +846,88 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
         s.coloring.stops[i] = V3<R>(R(col.stops[i][0]), R(col.stops[i][1]), R(col.stops[i][2]));
         s.coloring.pos[i] = R(col.stops[i][3]);
     }
+    for (int k = 0; k < 4; ++k) s.col_weights[k] = R(d.coloring_orbit.traps[k]);
+    s.col_extra[0] = R(d.coloring_orbit.iterations);
+    s.col_extra[1] = R(d.coloring_orbit.normal);
+    s.col_extra[2] = R(d.coloring_orbit.logarithmic);
+    // finish details and optics (uniforms.rs:797-815, :103-122)
+    s.dune_wind = R(d.dune_wind * (3.14159265f / 180.0f));
+    for (uint32_t i = 0; i < s.finish_count; ++i) {
+        const sf_finish_detail& f = d.details[i];
+        Detail<R>& o = s.details[i];
+        o.kind = f.pattern;
+        o.seed = f.seed;
+        o.scale = R(f.scale);
+        o.strength = R(f.strength);
+        o.bump = R(f.bump);
+        o.rough_delta = R(f.roughness_delta);
+        o.tint = v3<R>(f.tint);
+    }
+    for (uint32_t i = 0; i <= s.finish_count; ++i) {
+        const sf_optics& o = d.optics[i];
+        if (!o.enabled) continue;
+        Optics<R>& q = s.optics[i];
+        q.surface[0] = R(o.opacity);
+        q.surface[1] = R(o.transmission);
+        q.surface[2] = R(o.ior);
+        q.surface[3] = R(o.thin_walled ? 1 : 0);
+        // sigma = -ln(max(c, 1e-4)) / distance in binary32, as GpuOptics packs it
+        for (int k = 0; k < 3; ++k)
+            q.absorption[k] = R(-std::log(std::max(o.absorption_color[k], 0.0001f)) / o.absorption_distance);
+        q.absorption[3] = R(o.absorption_distance);
+        for (int k = 0; k < 3; ++k) q.subsurface[k] = R(o.subsurface_color[k]);
+        q.subsurface[3] = R(o.subsurface / o.subsurface_radius);
+        s.has_optics = true;
+    }
+    // the texture: on the oracle side sf_texture.graph carries an oracle graph handle
+    const sf_texture& t = d.texture;
+    if (t.graph) {
+        Texture<R>& x = s.tex;
+        x.graph = reinterpret_cast<const Graph*>(t.graph);
+        x.channel = t.channel;
+        x.octaves = t.octaves;
+        x.budget = x.graph->iteration_product;
+        for (int k = 0; k < 3; ++k) x.mapping[k] = R(t.offset[k]);
+        x.mapping[3] = R(t.scale);
+        for (int k = 0; k < 3; ++k) x.rotation[k] = R(t.rotation[k] * (3.14159265f / 180.0f));
+        x.rotation[3] = R(t.contrast);
+        x.effects[0] = R(t.strength);
+        x.effects[1] = R(t.roughness);
+        x.effects[2] = R(t.bump);
+        x.effects[3] = R(1);
+        if (t.channel == 7) {
+            for (int k = 0; k < 4; ++k) x.weights[k] = R(t.orbit.traps[k]);
+            x.extra[0] = R(t.orbit.iterations);
+            x.extra[1] = R(t.orbit.normal);
+            x.extra[2] = R(t.orbit.logarithmic);
+        }
+        x.parallax[0] = R(t.parallax);
+        x.parallax[1] = R(float(t.parallax_steps));
+        if (t.fan) {
+            x.fan[0] = R(t.fan_period[0]);
+            x.fan[1] = R(t.fan_period[1]);
+            x.fan[2] = R(float(t.fan_rays));
+            x.fan[3] = R(1);
+        }
+        if (t.mask) {
+            x.mask[0] = R(float(t.mask_slot));
+            x.mask[1] = R(t.mask_value);
+            x.mask[2] = R(t.mask_width);
+            x.mask[3] = R(1);
+        }
+        const sf_coloring& rc = t.ramp;
+        x.ramp.n = std::min<uint32_t>(rc.stop_count, SF_MAX_RAMP_STOPS);
+        x.ramp.cyclic = rc.cyclic != 0;
+        x.ramp.smooth = rc.smooth != 0;
+        x.ramp.positioned = rc.positioned != 0;
+        x.ramp.frequency = R(rc.frequency);
+        x.ramp.phase = R(rc.phase);
+        x.ramp.gamma = R(rc.gamma);
+        for (uint32_t i = 0; i < x.ramp.n; ++i) {
+            x.ramp.stops[i] = V3<R>(R(rc.stops[i][0]), R(rc.stops[i][1]), R(rc.stops[i][2]));
+            x.ramp.pos[i] = R(rc.stops[i][3]);
+        }
+    }
     s.variation_slot = d.variation_slot;
     s.variation_enabled = d.variation_enabled;
     s.var_rough[0] = R(d.variation_roughness[0]);
@@ -1001,7 +1083,7 @@ template <class R> static V3<R> area_emission(const Scene<R>& sc, V3<R> ro, V3<R
 }
 
 // BRDF (pathtrace.wgsl:195-249, :394-463).
-template <class R> struct Surface { V3<R> n, diffuse, f0; R alpha; V3<R> emission; };
+template <class R> struct Surface { V3<R> n, diffuse, f0; R alpha; V3<R> emission; R diffuse_sigma = 0; };
 static const double PI_W = 3.14159265358979;  // common.wgsl:6
 template <class R> static void tangent_frame(V3<R> n, V3<R>* t, V3<R>* bt) {
     R s = n.z >= R(0) ? R(1) : R(-1);
@@ -1047,7 +1129,17 @@ template <class R> static V3<R> brdf_eval(const Surface<R>& s, V3<R> v, V3<R> l)
     R a2 = s.alpha * s.alpha;
     V3<R> f = fresnel(s.f0, vh);
     V3<R> spec = f * (ggx_d(nh, a2) * smith_g1(nv, a2) * smith_g1(nl, a2)) / r_max(R(4) * nv * nl, R(1e-4));
-    return s.diffuse * (V3<R>::splat(1) - f) * R(1) / R(PI_W) + spec;
+    R diffuse_factor = 1;
+    if (s.diffuse_sigma > R(0)) {  // Oren-Nayar rough diffuse (pathtrace.wgsl:408-419)
+        R sigma2 = s.diffuse_sigma * s.diffuse_sigma;
+        R a = R(1) - sigma2 / (R(2) * (sigma2 + R(0.33)));
+        R b = R(0.45) * sigma2 / (sigma2 + R(0.09));
+        R sin_l = r_sqrt(r_max(R(0), R(1) - nl * nl));
+        R sin_v = r_sqrt(r_max(R(0), R(1) - nv * nv));
+        R cos_phi = r_max(R(0), (l - s.n * nl).dot(v - s.n * nv) / r_max(sin_l * sin_v, R(1e-8)));
+        diffuse_factor = a + b * cos_phi * sin_l * sin_v / r_max(r_max(nl, nv), R(1e-5));
+    }
+    return s.diffuse * (V3<R>::splat(1) - f) * diffuse_factor / R(PI_W) + spec;
 }
 template <class R> static R spec_probability(const Surface<R>& s, R nv) {
     V3<R> f = fresnel(s.f0, nv);
@@ -1096,15 +1188,308 @@ template <class R> static V3<R> ramp_sample(const Coloring<R>& c, R value) {
     return c.stops[n - 1];
 }
 
-template <class R> static Surface<R> make_surface(const Scene<R>& sc, V3<R> n, const Sample<R>& smp) {
+// ---------------------------------------------------------------- surface detail
+// finish_detail.wgsl (:1-160): value noise with analytic gradients, footprint-filtered.
+template <class R> static R smoothstep_r(R e0, R e1, R x) {
+    R t = r_clamp((x - e0) / (e1 - e0), R(0), R(1));
+    return t * t * (R(3) - R(2) * t);
+}
+template <class R> static R fract_r(R x) { return x - r_floor(x); }
+template <class R> static R sign_r(R x) { return x > R(0) ? R(1) : (x < R(0) ? R(-1) : R(0)); }
+template <class R> struct V4 { V3<R> g; R w; };
+template <class R> static V4<R> v4add(V4<R> a, V4<R> b) { return {a.g + b.g, a.w + b.w}; }
+template <class R> static V4<R> v4mul(V4<R> a, R s) { return {a.g * s, a.w * s}; }
+static float finish_hash(int32_t cx, int32_t cy, int32_t cz, uint32_t seed) {  // :3-7
+    uint32_t h = pcg(uint32_t(cx) ^ pcg(uint32_t(cy) + 0x9e3779b9u) ^ pcg(uint32_t(cz) + seed));
+    return float(h >> 8u) / 16777216.0f;
+}
+static int32_t floor_i(double x) {  // WGSL vec3i(floor(p)): saturating conversion
+    if (!(x == x)) return 0;
+    if (x >= 2147483647.0) return 2147483647;
+    if (x <= -2147483648.0) return -2147483647 - 1;
+    return int32_t(x);
+}
+template <class R> static V4<R> finish_noise(V3<R> p, uint32_t seed) {  // :8-21
+    V3<R> fl(r_floor(p.x), r_floor(p.y), r_floor(p.z));
+    int32_t x = floor_i(double(fl.x)), y = floor_i(double(fl.y)), z = floor_i(double(fl.z));
+    V3<R> f = p - fl;
+    V3<R> t = f * f * (V3<R>::splat(3) - f * R(2));
+    V3<R> dt = f * (V3<R>::splat(1) - f) * R(6);
+    R a0 = R(finish_hash(x, y, z, seed)), a1 = R(finish_hash(x + 1, y, z, seed));
+    R b0 = R(finish_hash(x, y + 1, z, seed)), b1 = R(finish_hash(x + 1, y + 1, z, seed));
+    R c0 = R(finish_hash(x, y, z + 1, seed)), c1 = R(finish_hash(x + 1, y, z + 1, seed));
+    R d0 = R(finish_hash(x, y + 1, z + 1, seed)), d1 = R(finish_hash(x + 1, y + 1, z + 1, seed));
+    R a = mixs(a0, a1, t.x), b = mixs(b0, b1, t.x), c = mixs(c0, c1, t.x), d = mixs(d0, d1, t.x);
+    R e = mixs(a, b, t.y), g = mixs(c, d, t.y);
+    R dx = mixs(mixs(a1 - a0, b1 - b0, t.y), mixs(c1 - c0, d1 - d0, t.y), t.z);
+    return {V3<R>(dx, mixs(b - a, d - c, t.z), g - e) * dt, mixs(e, g, t.z)};
+}
+template <class R> static V4<R> finish_fbm(V3<R> p, R width, uint32_t seed) {  // :22-33
+    R frequency = 1, weight = R(0.5);
+    V4<R> result{V3<R>(0, 0, 0), 0};
+    for (uint32_t i = 0; i < 3u; ++i) {
+        R visible = R(1) - smoothstep_r(R(0.35), R(0.85), width * frequency);
+        if (visible > R(0)) {
+            V4<R> n = finish_noise(p * frequency, seed + i * 97u);
+            result = v4add(result, v4mul(V4<R>{n.g * frequency * visible, mixs(R(0.5), n.w, visible)}, weight));
+        } else {
+            result.w += weight * R(0.5);
+        }
+        frequency *= R(2.13);
+        weight *= R(0.5);
+    }
+    return v4mul(result, R(1) / R(0.875));
+}
+template <class R> static R finish_smooth_derivative(R a, R b, R x) {
+    R t = r_clamp((x - a) / (b - a), R(0), R(1));
+    return R(6) * t * (R(1) - t) / (b - a);
+}
+template <class R> static V2<R> rot2(V2<R> v, R a) {
+    R s = r_sin(a), c = r_cos(a);
+    return V2<R>(c * v.x - s * v.y, s * v.x + c * v.y);
+}
+// finish_eval (:37-154); the coastal rock's wet band needs an ocean (not on this path).
+template <class R> static V4<R> finish_eval(const Detail<R>& f, V3<R> p, R footprint, R wind) {
+    const R scale = f.scale;
+    const V3<R> q = p * scale;
+    const R width = footprint * scale;
+    const uint32_t seed = f.seed, kind = f.kind;
+    const R PI = R(PI_W);
+    if (kind == 12u) {
+        V4<R> basin = finish_fbm(q * V3<R>(R(0.31), R(0.31), R(0.22)), width * R(0.31), seed + 911u);
+        R wet = smoothstep_r(R(0.47), R(0.59), basin.w);
+        V4<R> grit = finish_fbm(q * R(16), width * R(16), seed + 113u);
+        R visible = R(1) - smoothstep_r(R(0.15), R(0.6), width * R(3));
+        R phase = q.dot(V3<R>(R(2.8), R(0), R(4.1)));
+        V3<R> ripple = V3<R>(R(2.8), R(0), R(4.1)) * r_cos(phase) * R(0.018) * visible;
+        return {mixv(grit.g * R(16), ripple, wet) * scale, wet};
+    }
+    if (kind == 10u || kind == 11u) {
+        V4<R> stains = finish_fbm(q * R(0.14), width * R(0.14), seed + 17u);
+        V4<R> aggregate = finish_fbm(q * R(7), width * R(7), seed + 113u);
+        V4<R> pore = finish_noise(q * R(23), seed + 307u);
+        R visible = R(1) - smoothstep_r(R(0.25), R(0.75), width * R(23));
+        R pit = R(1) - smoothstep_r(R(0.24), R(0.43), pore.w);
+        V3<R> pit_gradient = pore.g * (-finish_smooth_derivative(R(0.24), R(0.43), pore.w) * R(23)) * visible;
+        R phase = fract_r(q.y / R(1.25) + R(0.5)) - R(0.5);
+        R board_visible = R(1) - smoothstep_r(R(0.03), R(0.15), width);
+        R joint = (R(1) - smoothstep_r(R(0.006), R(0.027), r_abs(phase))) * board_visible;
+        R joint_gradient = -finish_smooth_derivative(R(0.006), R(0.027), r_abs(phase)) * sign_r(phase) / R(1.25) *
+                           board_visible;
+        R height = R(0.18) * stains.w + R(0.65) * aggregate.w - R(0.14) * mixs(R(0.2), pit, visible) - R(0.09) * joint;
+        V3<R> gradient = (stains.g * (R(0.18) * R(0.14)) + aggregate.g * (R(0.65) * R(7)) - pit_gradient * R(0.14) -
+                          V3<R>(0, R(0.09) * joint_gradient, 0)) * scale;
+        if (kind == 11u) {
+            V3<R> axes(R(1.9), R(0.055), R(1.9));
+            V4<R> rain = finish_fbm(q * axes, width * R(1.9), seed + 601u);
+            R deposit = smoothstep_r(R(0.33), R(0.68), rain.w);
+            V3<R> rain_gradient = rain.g * axes * scale * finish_smooth_derivative(R(0.33), R(0.68), rain.w);
+            return {gradient + rain_gradient * R(0.12), r_clamp(R(0.72) * deposit + R(0.28) * stains.w, R(0), R(1))};
+        }
+        return {gradient, r_clamp(height + R(0.12), R(0), R(1))};
+    }
+    if (kind == 9u) {
+        V4<R> wa = finish_fbm(q * R(0.17), width * R(0.17), seed + 17u);
+        V4<R> wb = finish_fbm(q * R(0.17), width * R(0.17), seed + 53u);
+        V3<R> warped = q + V3<R>(wa.w - R(0.5), R(0), wb.w - R(0.5)) * R(2.8);
+        V4<R> cloud = finish_fbm(warped * R(0.16), width * R(0.48), seed + 211u);
+        V3<R> axes(R(0.65), R(0.18), R(0.09));
+        V4<R> streak = finish_fbm(warped * axes, width * R(1.95), seed + 397u);
+        R density = R(0.78) * cloud.w + R(0.22) * streak.w;
+        V3<R> g = cloud.g * (R(0.78) * R(0.16)) + axes * streak.g * R(0.22);
+        V3<R> density_gradient = (g + (wa.g * g.x + wb.g * g.z) * (R(2.8) * R(0.17))) * scale;
+        R deposit = smoothstep_r(R(0.36), R(0.64), density);
+        V3<R> deposit_gradient = density_gradient * finish_smooth_derivative(R(0.36), R(0.64), density);
+        V4<R> grain = finish_fbm(p * R(48), footprint * R(48), seed + 739u);
+        R powder = R(0.85) + R(0.15) * grain.w;
+        return {deposit_gradient * powder + grain.g * (deposit * R(0.15) * R(48)), deposit * powder};
+    }
+    if (kind == 8u) {
+        V2<R> xz = rot2(V2<R>(p.x, p.z), wind) * scale;
+        V4<R> warp = finish_noise(V3<R>(xz.x * R(0.045), R(0), xz.y * R(0.045)), seed);
+        R phase = R(2) * PI * (xz.x + R(1.7) * warp.w + R(0.12) * r_sin(xz.y * R(0.22)));
+        R w3 = width * R(3);
+        R visible = r_exp(-(w3 * w3));
+        R ripple = R(0.5) + R(0.36) * r_sin(phase) + R(0.10) * r_sin(R(2) * phase);
+        R amp = R(2) * PI * (R(0.36) * r_cos(phase) + R(0.20) * r_cos(R(2) * phase));
+        V2<R> gradient = V2<R>(R(1) + R(0.0765) * warp.g.x, R(0.0264) * r_cos(xz.y * R(0.22)) + R(0.0765) * warp.g.z) *
+                         (amp * scale * visible);
+        V4<R> grain = finish_fbm(p * R(90), footprint * R(90), seed + 139u);
+        V2<R> grad = rot2(gradient, -wind);
+        return {V3<R>(grad.x, R(0), grad.y) + grain.g * R(2.5), R(0.70) * mixs(R(0.5), ripple, visible) + R(0.30) * grain.w};
+    }
+    if (kind == 6u) {
+        R tx = fract_r(q.x + R(0.5)) - R(0.5), ty = fract_r(q.z + R(0.5)) - R(0.5);
+        R r = r_max(r_sqrt(tx * tx + ty * ty), R(1e-5));
+        R angle = r_atan2(ty, tx);
+        R flower = r - R(0.25) - R(0.07) * r_cos(angle * R(8));
+        R ring = r - R(0.45);
+        R ax = -ty / (r * r), ay = tx / (r * r);
+        R sf = sign_r(flower), k8 = R(0.56) * r_sin(angle * R(8));
+        R gx = sf * (tx / r + k8 * ax), gy = sf * (ty / r + k8 * ay);
+        R distance = r_abs(flower);
+        if (r_abs(ring) < distance) {
+            distance = r_abs(ring);
+            gx = sign_r(ring) * tx / r;
+            gy = sign_r(ring) * ty / r;
+        }
+        R visible = R(1) - smoothstep_r(R(0.10), R(0.40), width);
+        R carving = R(1) - smoothstep_r(R(0.012), R(0.045), distance);
+        R k = -finish_smooth_derivative(R(0.012), R(0.045), distance) * visible * scale;
+        return {V3<R>(gx * k, R(0), gy * k), mixs(R(0.2), carving, visible)};
+    }
+    if (kind == 3u) {
+        V3<R> axes(R(18), R(0.45), R(3));
+        V4<R> n = finish_fbm(q * axes, width * R(18), seed);
+        return {n.g * axes * scale, n.w};
+    }
+    V4<R> n = finish_fbm(q, width, seed);
+    V4<R> result = n;
+    if (kind == 1u) {
+        V3<R> axis(R(0.16), R(0.11), R(0.08));
+        R phase = (q.dot(axis) + n.w * R(2.8)) * PI * R(2);
+        R wave = r_sin(phase);
+        R veins = R(1) - smoothstep_r(R(0.035), R(0.19), r_abs(wave));
+        V3<R> gradient = (axis + n.g * R(2.8)) *
+                         (-finish_smooth_derivative(R(0.035), R(0.19), r_abs(wave)) * sign_r(wave) * r_cos(phase) * PI * R(2));
+        R visible = R(1) - smoothstep_r(R(0.18), R(0.45), width);
+        V4<R> mixed = v4add(v4mul(n, R(0.65)), v4mul(V4<R>{gradient, veins}, R(0.35)));
+        result = {mixv(n.g, mixed.g, visible), mixs(n.w, mixed.w, visible)};
+    } else if (kind == 2u) {
+        result = {n.g * finish_smooth_derivative(R(0.35), R(0.67), n.w), smoothstep_r(R(0.35), R(0.67), n.w)};
+    } else if (kind == 4u || kind == 7u) {
+        V4<R> grain = finish_fbm(q * R(3.7), width * R(3.7), seed + 53u);
+        result = v4add(v4mul(n, R(0.8)), v4mul(V4<R>{grain.g * R(3.7), grain.w}, R(0.2)));
+    } else if (kind == 5u) {
+        R a = q.x + R(0.75) * n.w;
+        R b = q.z * R(1.37) + q.x * R(0.4);
+        R visible = R(1) - smoothstep_r(R(0.35), R(1), width);
+        V3<R> gradient = ((V3<R>(1, 0, 0) + n.g * R(0.75)) * (R(0.32) * r_cos(a)) +
+                          V3<R>(R(0.4), R(0), R(1.37)) * (R(0.18) * r_cos(b))) * visible;
+        result = {gradient, R(0.5) + (R(0.32) * r_sin(a) + R(0.18) * r_sin(b)) * visible};
+    }
+    return {result.g * scale, result.w};
+}
+template <class R> static V3<R> finish_normal(R bump, V3<R> n, V3<R> gradient) {  // :155-159
+    V3<R> slope = gradient - n * gradient.dot(n);
+    R limit = R(0.75) / r_max(slope.length(), R(1e-5));
+    return safe_normalize(n - slope * r_clamp(bump, -limit, limit));
+}
+// OrbitColoring::value (material.rs:39-55).
+template <class R> static R orbit_mix(const R* w, const R* extra, const R* traps, R iter_frac, R normal_term) {
+    R v = w[0] * traps[0] + w[1] * traps[1] + w[2] * traps[2] + w[3] * traps[3] + extra[0] * iter_frac +
+          extra[1] * normal_term;
+    if (extra[2] > R(0)) v = sign_r(v) * r_log(R(1) + extra[2] * r_abs(v)) / r_log(R(1) + extra[2]);
+    return v;
+}
+// glam Quat::from_euler(XYZ) * p (common.wgsl:263-271): Z, then Y, then X.
+template <class R> static V3<R> rotate_xyz(V3<R> p, const R* a) {
+    V3<R> q = p;
+    q = V3<R>(r_cos(a[2]) * q.x - r_sin(a[2]) * q.y, r_sin(a[2]) * q.x + r_cos(a[2]) * q.y, q.z);
+    q = V3<R>(r_cos(a[1]) * q.x + r_sin(a[1]) * q.z, q.y, -r_sin(a[1]) * q.x + r_cos(a[1]) * q.z);
+    q = V3<R>(q.x, r_cos(a[0]) * q.y - r_sin(a[0]) * q.z, r_sin(a[0]) * q.y + r_cos(a[0]) * q.z);
+    return q;
+}
+template <class R> static R modf_euclid_r(R x, R m) { return x - m * r_floor(x / m); }
+// pattern_value (pattern.wgsl:2-49) of the scene's texture.
+template <class R> static R texture_value(const Texture<R>& T, V3<R> p) {
+    V3<R> off(T.mapping[0], T.mapping[1], T.mapping[2]);
+    const R scale = T.mapping[3];
+    V3<R> q = rotate_xyz(p * scale, T.rotation) + off;
+    R fan_angle = 0, fan_radius = 0;
+    if (T.fan[3] > R(0)) {
+        q = rotate_xyz(p, T.rotation) + off;
+        R row = r_floor(q.z / T.fan[1]);
+        R x = modf_euclid_r(q.x + modf_euclid_r(row, R(2)) * T.fan[0] * R(0.5), T.fan[0]) - T.fan[0] * R(0.5);
+        R z = modf_euclid_r(q.z, T.fan[1]) + R(0.03);
+        fan_angle = r_atan2(x, z);
+        fan_radius = r_sqrt(x * x + z * z);
+        q = V3<R>(fan_angle * T.fan[2] / R(PI_W), q.y, fan_radius) * scale;
+    }
+    const bool orbit = T.channel == 7u;
+    const R budget = r_max(R(float(T.budget)), R(1));
+    R total = 0, weights = 0, weight = 1;
+    for (uint32_t o = 0; o < T.octaves; ++o) {
+        Sample<R> smp = evaluate<R>(*T.graph, q);
+        R value;
+        if (orbit) value = orbit_mix(T.weights, T.extra, smp.traps, R(float(smp.iterations)) / budget, R(0.5));
+        else if (T.channel < 4u) value = smp.traps[T.channel];
+        else if (T.channel == 4u) value = R(float(smp.iterations)) / budget;
+        else value = R(0.5) + R(0.5) * smp.distance / (R(1) + r_abs(smp.distance));
+        if (!(value >= -R(3.4028235e38) && value <= R(3.4028235e38))) value = R(0.5);
+        total += (orbit ? value : r_clamp(value, R(0), R(1))) * weight;
+        weights += weight;
+        q = q * R(2) + V3<R>(R(0.73), R(1.17), R(0.91));
+        weight *= R(0.5);
+    }
+    R fractal = total / r_max(weights, R(1e-6));
+    R value = fractal;
+    if (T.fan[3] > R(0)) {
+        R spoke = r_pow(R(1) - r_abs(r_sin(fan_angle * T.fan[2] + R(0.16) * (fractal - R(0.5)))), R(4));
+        R arc = r_pow(R(1) - r_abs(r_sin(fan_radius * scale * R(PI_W) + R(0.35) * fractal)), R(6));
+        value = R(0.16) + R(0.28) * fractal + R(0.42) * spoke + R(0.22) * arc;
+    }
+    R result = (value - R(0.5)) * T.rotation[3] + R(0.5);
+    return orbit ? result : r_clamp(result, R(0), R(1));
+}
+template <class R> static R texture_mask(const Texture<R>& T, const R* traps) {  // texture.wgsl:17-21
+    if (T.mask[3] == R(0)) return 1;
+    return R(1) - smoothstep_r(T.mask[2] * R(0.5), T.mask[2], r_abs(traps[uint32_t(T.mask[0]) & 3u] - T.mask[1]));
+}
+template <class R> static R texture_filtered_value(const Texture<R>& T, V3<R> p, R footprint) {  // :27-31
+    R fade = smoothstep_r(R(0.25), R(0.75), footprint * T.mapping[3]);
+    if (fade >= R(1)) return R(0.5);
+    return mixs(texture_value(T, p), R(0.5), fade);
+}
+template <class R> static V3<R> texture_parallax(const Texture<R>& T, V3<R> p, V3<R> n, V3<R> v, R footprint) {  // :35-55
+    R depth = T.parallax[0] / T.mapping[3];
+    if (depth <= R(0) || depth < footprint * R(0.25)) return p;
+    R nv = r_max(n.dot(v), R(0.15));
+    V3<R> direction = (v - n * n.dot(v)) / nv + n;
+    uint32_t layers = uint32_t(mixs(R(4), T.parallax[1], R(1) - r_clamp(nv, R(0), R(1))));
+    uint32_t count = std::max(layers, 4u);
+    R step = R(1) / R(float(count));
+    R previous = texture_value(T, p) - R(1);
+    R layer = 0;
+    for (uint32_t i = 0; i < count; ++i) {
+        layer += step;
+        V3<R> q = p - direction * depth * layer;
+        R crossing = layer + texture_value(T, q) - R(1);
+        if (crossing >= R(0)) {
+            R fraction = r_clamp(-previous / r_max(crossing - previous, R(1e-6)), R(0), R(1));
+            return p - direction * depth * (layer - step + step * fraction);
+        }
+        previous = crossing;
+    }
+    return p - direction * depth;
+}
+template <class R> static V3<R> texture_normal(const Texture<R>& T, V3<R> p, V3<R> n, R footprint) {  // :57-72
+    R fade = smoothstep_r(R(0.25), R(0.75), footprint * T.mapping[3]);
+    if (fade >= R(1)) return n;
+    R h = r_max(footprint, R(0.005) / T.mapping[3]);
+    V3<R> a(1, -1, -1), b(-1, -1, 1), c(-1, 1, -1), d(1, 1, 1);
+    V3<R> gradient = (a * texture_value(T, p + a * h) + b * texture_value(T, p + b * h) + c * texture_value(T, p + c * h) +
+                      d * texture_value(T, p + d * h)) / (R(4) * h);
+    V3<R> tangent = (gradient - n * n.dot(gradient)) * T.effects[2] * (R(1) - fade) / T.mapping[3];
+    tangent = tangent / r_max(R(1), tangent.length());
+    return safe_normalize(n - tangent);
+}
+
+// make_surface (pathtrace.wgsl:271-386) without the nature phenomena: colouring ramp or
+// orbit mix, finish, variation, the finish's detail, the texture on untagged surfaces.
+template <class R>
+static Surface<R> make_surface(const Scene<R>& sc, V3<R> p, V3<R> n, V3<R> v, const Sample<R>& smp, R footprint) {
     V3<R> albedo = sc.material.albedo;
     bool assigned = smp.material > 0 && smp.material <= sc.finish_count;
     if (!assigned && sc.coloring.n) {  // pathtrace.wgsl:275-288
         const uint32_t slot = sc.coloring.slot;
-        if (slot < 4) albedo = albedo * ramp_sample(sc.coloring, smp.traps[slot]);
+        const R iter_frac = R(float(smp.iterations)) / r_max(R(float(sc.iteration_product)), R(1));
+        if (slot == 6)
+            albedo = albedo * ramp_sample(sc.coloring, orbit_mix(sc.col_weights, sc.col_extra, smp.traps, iter_frac,
+                                                                 n.y * R(0.5) + R(0.5)));
+        else if (slot < 4) albedo = albedo * ramp_sample(sc.coloring, smp.traps[slot]);
         else if (slot == 5) albedo = albedo * ramp_sample(sc.coloring, n.y * R(0.5) + R(0.5));
-        else if (slot == 4)
-            albedo = albedo * ramp_sample(sc.coloring, R(float(smp.iterations)) / r_max(R(float(sc.iteration_product)), R(1)));
+        else if (slot == 4) albedo = albedo * ramp_sample(sc.coloring, iter_frac);
     }
     R rough = sc.material.roughness, metallic = sc.material.metallic, spec = sc.material.specular;
     V3<R> emission(0, 0, 0);
@@ -1126,9 +1511,46 @@ template <class R> static Surface<R> make_surface(const Scene<R>& sc, V3<R> n, c
         rough = sc.var_rough[0] + (sc.var_rough[1] - sc.var_rough[0]) * t;
         metallic = sc.var_metal[0] + (sc.var_metal[1] - sc.var_metal[0]) * t;
     }
+    V3<R> shading_n = n;
+    bool rough_diffuse = false;
+    if (assigned && sc.details[smp.material - 1].kind != 0u) {  // pathtrace.wgsl:303-340
+        const Detail<R>& f = sc.details[smp.material - 1];
+        V4<R> detail = finish_eval(f, p, footprint, sc.dune_wind);
+        if (f.kind == 9u) detail = v4mul(detail, smoothstep_r(R(0.10), R(0.80), n.y));
+        if (f.kind == 12u) detail.w *= smoothstep_r(R(0.45), R(0.95), n.y);
+        R value = detail.w;
+        R amount = f.strength * value;
+        albedo = mixv(albedo, f.tint, amount);
+        if (f.kind == 9u) {
+            rough += r_max(f.rough_delta, R(0)) * amount;
+            metallic *= R(1) - amount;
+            spec = mixs(spec, R(0.025), amount);
+        } else if (f.kind == 12u) {
+            rough = mixs(rough, r_clamp(rough + f.rough_delta, R(0.025), R(1)), amount);
+            spec = mixs(spec, R(0.0204), amount);
+            metallic *= R(1) - amount;
+        } else {
+            rough += f.rough_delta * (R(2) * value - R(1));
+        }
+        if (f.kind == 2u) metallic *= R(1) - R(0.75) * amount;
+        if (r_abs(f.bump) > R(0)) shading_n = finish_normal(f.bump, n, detail.g);
+        rough_diffuse = f.kind >= 10u;
+    }
+    const Texture<R>& T = sc.tex;
+    if (T.graph) {  // pathtrace.wgsl:345-355
+        R amount = texture_mask(T, smp.traps);
+        if (!assigned && T.effects[3] > R(0) && amount > R(0)) {
+            V3<R> tex_p = texture_parallax(T, p, n, v, footprint);
+            R value = texture_filtered_value(T, tex_p, footprint);
+            albedo = albedo * mixv(V3<R>::splat(1), ramp_sample(T.ramp, value), T.effects[0] * amount);
+            rough = mixs(rough, value, T.effects[1] * amount);
+            if (T.effects[2] > R(0)) shading_n = safe_normalize(mixv(n, texture_normal(T, tex_p, n, footprint), amount));
+        }
+    }
     rough = r_clamp(rough, R(0.02), R(1));
     Surface<R> s;
-    s.n = n;
+    s.n = shading_n;
+    s.diffuse_sigma = rough_diffuse ? rough * R(0.45) : R(0);
     s.diffuse = albedo * (R(1) - metallic);
     s.f0 = mixv(V3<R>::splat(spec), albedo, metallic);
     s.alpha = rough * rough;
@@ -1535,8 +1957,9 @@ static V3<R> fog_segment_direct(const Scene<R>& sc, V3<R> ro, V3<R> rd, R end, u
         const V3<R> wi = to_light / distance;
         const R cosine = area_normal(l).dot(-wi);
         if (cosine <= R(0)) continue;
-        if (!visible(p, wi, r_max(R(0), distance - r_max(R(1e-5), distance * R(1e-6))))) continue;
-        const R tr = transmittance * r_exp(-fog_optical_depth(sc, p, wi, distance));
+        const R vw = visible(p, wi, r_max(R(0), distance - r_max(R(1e-5), distance * R(1e-6))));
+        if (!(vw > R(0))) continue;
+        const R tr = vw * transmittance * r_exp(-fog_optical_depth(sc, p, wi, distance));
         result = result + l.color * (sigma * tr * hg_phase(rd.dot(wi), g) /
                                      (probability * distance_pdf * area_direction_pdf(l, distance2, cosine)));
     }
@@ -1560,8 +1983,9 @@ static V3<R> fog_direct_light(const Scene<R>& sc, V3<R> p, V3<R> rd, R area_tota
             const R phi = R(2) * R(PI_W) * rnd<R>(rng);
             const R radius = r_sqrt(r_max(R(0), R(1) - z * z));
             const V3<R> dir(radius * r_cos(phi), z, radius * r_sin(phi));
-            if (!visible(p, dir, extent)) continue;
-            const R tr = fog_transmittance(sc, p, dir, extent);
+            const R vw = visible(p, dir, extent);
+            if (!(vw > R(0))) continue;
+            const R tr = vw * fog_transmittance(sc, p, dir, extent);
             const R ph = hg_phase(rd.dot(dir), g);
             const R pl = probability / (R(4) * R(PI_W));
             L = L + environment_value(l, dir) * ph * tr * (last ? R(1) : mis_power(pl, ph)) / pl;
@@ -1571,8 +1995,9 @@ static V3<R> fog_direct_light(const Scene<R>& sc, V3<R> p, V3<R> rd, R area_tota
             const R r1 = rnd<R>(rng);
             const R r2 = rnd<R>(rng);
             const V3<R> dir = hdri_sample(l, r0, r1, r2);
-            if (!visible(p, dir, extent)) continue;
-            const R tr = fog_transmittance(sc, p, dir, extent);
+            const R vw = visible(p, dir, extent);
+            if (!(vw > R(0))) continue;
+            const R tr = vw * fog_transmittance(sc, p, dir, extent);
             const R ph = hg_phase(rd.dot(dir), g);
             const R pl = hdri_pdf(l, dir);
             L = L + hdri_lookup(l, dir) * ph * tr * (last ? R(1) : mis_power(pl, ph)) / pl;
@@ -1580,8 +2005,9 @@ static V3<R> fog_direct_light(const Scene<R>& sc, V3<R> p, V3<R> rd, R area_tota
             const R r1 = rnd<R>(rng);
             const R r2 = rnd<R>(rng);
             const V3<R> dir = cone_sample(l.a, l.cos_max, r1, r2);
-            if (!visible(p, dir, extent)) continue;
-            const R tr = fog_transmittance(sc, p, dir, extent);
+            const R vw = visible(p, dir, extent);
+            if (!(vw > R(0))) continue;
+            const R tr = vw * fog_transmittance(sc, p, dir, extent);
             const R ph = hg_phase(rd.dot(dir), g);
             const R pl = sun_pdf(l.cos_max);
             L = L + l.color * ph * tr * (last ? R(1) : mis_power(pl, ph));
@@ -1590,8 +2016,81 @@ static V3<R> fog_direct_light(const Scene<R>& sc, V3<R> p, V3<R> rd, R area_tota
     return L;
 }
 
-// radiance (pathtrace.wgsl:802-1201) with the height fog, and with optics, ocean,
-// portals, nebulae, guiding and textures disabled (those branches are identities when off),
+// ---------------------------------------------------------------- optics (optics.wgsl)
+template <class R> static const Optics<R>& material_optics(const Scene<R>& sc, uint32_t index) {  // :1-3
+    return sc.optics[index <= sc.finish_count ? index : 0u];
+}
+template <class R> static bool optics_on(const Optics<R>& o) { return o.absorption[3] > R(0); }
+// optical_refine_hit (:7-23): Newton steps along the ray on the exact field.
+template <class R> static R optical_refine(const Graph& g, V3<R> ro, V3<R> rd, R t, uint64_t* evals) {
+    const R eps = r_max(R(1e-5), r_min(R(1e-3), t * R(1e-5)));
+    for (uint32_t i = 0; i < 8u; ++i) {
+        V3<R> p = ro + rd * t;
+        R d = evaluate<R>(g, p).distance;
+        *evals += 1;
+        if (r_abs(d) < R(1e-5)) break;
+        R derivative = (evaluate<R>(g, p + rd * eps).distance - evaluate<R>(g, p - rd * eps).distance) / (R(2) * eps);
+        *evals += 2;
+        if (r_abs(derivative) < R(1e-5)) break;
+        t = r_max(R(0), t - r_clamp(d / derivative, R(-0.5), R(0.5)));
+    }
+    return t;
+}
+// ocean_fresnel (ocean.wgsl:151-159).
+template <class R> static R dielectric_fresnel(R cosine, R eta) {
+    R ci = r_clamp(r_abs(cosine), R(0), R(1));
+    R st2 = eta * eta * (R(1) - ci * ci);
+    if (st2 >= R(1)) return 1;
+    R ct = r_sqrt(r_max(R(0), R(1) - st2));
+    R rs = (eta * ci - ct) / r_max(eta * ci + ct, R(1e-6));
+    R rp = (ci - eta * ct) / r_max(ci + eta * ct, R(1e-6));
+    return R(0.5) * (rs * rs + rp * rp);
+}
+template <class R> static V3<R> refract_w(V3<R> i, V3<R> n, R eta) {  // WGSL refract
+    R ni = n.dot(i);
+    R k = R(1) - eta * eta * (R(1) - ni * ni);
+    if (k < R(0)) return V3<R>(0, 0, 0);
+    return i * eta - n * (eta * ni + r_sqrt(k));
+}
+template <class R> static V3<R> reflect_w(V3<R> i, V3<R> n) { return i - n * (R(2) * n.dot(i)); }
+template <class R> static V3<R> exp_v(V3<R> a) { return V3<R>(r_exp(a.x), r_exp(a.y), r_exp(a.z)); }
+template <class R> struct OpticalBounce { V3<R> direction, weight; bool transmitted, valid; };
+// optical_bounce (:30-64) without dispersion or thin-film coating.
+template <class R>
+static OpticalBounce<R> optical_bounce(const Optics<R>& o, V3<R> n, V3<R> rd, R alpha, bool entering, uint32_t* rng) {
+    const R index = o.surface[2];
+    const bool thin = o.surface[3] > R(0);
+    const V3<R> tint = exp_v(V3<R>(-o.absorption[0], -o.absorption[1], -o.absorption[2]) * o.absorption[3]);
+    if (index <= R(1.0001)) return {rd, thin ? tint : V3<R>::splat(1), true, true};
+    const R eta = (entering || thin) ? R(1) / index : index;
+    const R r1 = rnd<R>(rng);
+    const R r2 = rnd<R>(rng);
+    const V3<R> h = sample_ggx_h(n, -rd, alpha, r1, r2);
+    R f = dielectric_fresnel(r_max(R(0), (-rd).dot(h)), eta);
+    if (thin) f = R(2) * f / (R(1) + f);
+    V3<R> color = V3<R>::splat(f);
+    R probability = f;
+    const V3<R> transmitted = refract_w(rd, h, eta);
+    if (!thin && transmitted.dot(transmitted) < R(0.5)) {
+        color = V3<R>::splat(1);
+        probability = 1;
+    }
+    const R a2 = alpha * alpha;
+    if (rnd<R>(rng) < probability) {
+        V3<R> direction = reflect_w(rd, h);
+        R cosine = n.dot(direction);
+        return {direction, color / r_max(probability, R(1e-20)) * smith_g1(r_max(cosine, R(1e-6)), a2), false,
+                cosine > R(0)};
+    }
+    V3<R> direction = thin ? rd : transmitted;
+    R cosine = -n.dot(direction);
+    V3<R> weight = thin ? tint : V3<R>::splat(smith_g1(r_max(cosine, R(1e-6)), a2) * eta * eta);
+    weight = weight * (V3<R>::splat(1) - color) / r_max(R(1) - probability, R(1e-20));
+    return {direction, weight, true, cosine > R(0) && direction.dot(direction) > R(0.5)};
+}
+
+// radiance (pathtrace.wgsl:802-1201) with the height fog, finish details, textures and optics, and with ocean,
+// portals, nebulae, guiding and the nature phenomena disabled (those branches are identities when off),
 // camera_ray (:781-800) and the per-sample film terms of main (:1203-1276).
 template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint32_t px, uint32_t py, uint32_t sample) {
     PixelResult res{};
@@ -1621,11 +2120,50 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
     V3<R> prev_normal(0, 0, 0);
     bool prev_from_volume = false;  // prev_volume_nee is the same flag without ocean and nebulae
     const uint32_t point_stream = pcg(pcg(px ^ sc.seed) ^ pcg(py ^ 0x27d4eb2du));
+    // the transported texture footprint (pathtrace.wgsl:811-814) and the optics state
+    R tex_width = 0, tex_spread = pixel_cone * R(0.5);
+    bool solid_medium = false;
+    uint32_t medium_slot = 0, null_surfaces = 0;
     const bool in_fog = sc.fog[0] > R(0);
-    auto visible_from = [&](V3<R> o, V3<R> dir, R t_end) {
-        Hit<R> sh = trace_scene(g, sc, o, dir, pixel_cone, t_end, &res.de_evals);
-        res.segments++;
-        return !sh.hit && !sh.exhausted;
+    const bool optics = sc.has_optics;
+    if (optics) {  // the medium the camera ray starts in (:833-840)
+        const Sample<R> init = evaluate<R>(g, ro);
+        res.de_evals++;
+        const Optics<R>& o = material_optics(sc, init.material);
+        solid_medium = init.distance < R(0) && optics_on(o) && o.surface[1] > R(0) && o.surface[3] == R(0);
+        medium_slot = init.material;
+    }
+    // scene_visibility_weight (lights.wgsl:260-283): with optics, surfaces of dielectric
+    // materials pass the segment weighted by 1 - opacity, up to 32 segments
+    auto visible_from = [&](V3<R> o, V3<R> dir, R t_end) -> R {
+        if (!optics) {
+            Hit<R> sh = trace_scene(g, sc, o, dir, pixel_cone, t_end, &res.de_evals);
+            res.segments++;
+            return (!sh.hit && !sh.exhausted) ? R(1) : R(0);
+        }
+        V3<R> origin = o;
+        R remaining = t_end, visibility = 1;
+        for (uint32_t i = 0; i < 32u; ++i) {
+            Hit<R> sh = trace_scene(g, sc, origin, dir, pixel_cone, remaining, &res.de_evals);
+            res.segments++;
+            if (sh.hit && sh.light_index == 0xffffffffu && optics_on(material_optics(sc, sh.sample.material))) {
+                sh.t = optical_refine(g, origin, dir, sh.t, &res.de_evals);
+                sh.sample = evaluate<R>(g, origin + dir * sh.t);
+                res.de_evals++;
+            }
+            if (sh.exhausted) return 0;
+            if (!sh.hit) return visibility;
+            if (sh.light_index != 0xffffffffu) return 0;
+            const Optics<R>& oo = material_optics(sc, sh.sample.material);
+            if (!optics_on(oo)) return 0;
+            visibility *= R(1) - oo.surface[0];
+            if (visibility < R(1e-6)) return 0;
+            const R distance = sh.t + R(1e-4);
+            origin = origin + dir * distance;
+            remaining -= distance;
+            if (remaining <= R(0)) return visibility;
+        }
+        return 0;
     };
     R first_depth = -1;
     R aux[4] = {0, 0, 0, -1};
@@ -1633,24 +2171,57 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
     for (uint32_t bounce = 0; bounce <= sc.max_bounces;) {
         Hit<R> h = trace_scene(g, sc, ro, rd, pixel_cone, extent, &res.de_evals);
         res.segments++;
+        bool refined = false;  // a hit on a dielectric material: optical_refine_hit (optics.wgsl:7-23)
+        if (optics && h.hit && h.light_index == 0xffffffffu && optics_on(material_optics(sc, h.sample.material))) {
+            h.t = optical_refine(g, ro, rd, h.t, &res.de_evals);
+            h.sample = evaluate<R>(g, ro + rd * h.t);
+            res.de_evals++;
+            refined = true;
+        }
+        if (optics && solid_medium) {  // inside a dielectric solid (pathtrace.wgsl:857-875)
+            const Optics<R>& medium = material_optics(sc, medium_slot);
+            R distance = h.t;
+            if (medium.subsurface[3] > R(0))
+                distance = r_min(h.t, -r_log(r_max(R(1e-7), R(1) - rnd<R>(&rng))) / medium.subsurface[3]);
+            throughput = throughput * exp_v(V3<R>(-medium.absorption[0], -medium.absorption[1], -medium.absorption[2]) *
+                                            distance);
+            if (distance < h.t) {
+                if (bounce == sc.max_bounces) break;
+                throughput = throughput * V3<R>(medium.subsurface[0], medium.subsurface[1], medium.subsurface[2]);
+                const R r1 = rnd<R>(&rng);
+                const R r2 = rnd<R>(&rng);
+                ro = ro + rd * distance;
+                rd = hg_sample(rd, R(0), r1, r2);
+                prev_from_bsdf = false;
+                prev_from_volume = false;
+                prev_pdf = 0;
+                tex_spread = r_max(tex_spread, R(0.25));
+                bounce++;
+                continue;
+            }
+        }
         V3<R> gn(0, 0, 0);
         if (h.hit) {
             if (h.light_index != 0xffffffffu) gn = area_normal(sc.lights[h.light_index]);
             else {
-                gn = normal_tetra(g, ro + rd * h.t, r_max(h.t * pixel_cone * R(0.5), R(1e-4)) * sc.pixel_tolerance);
+                const bool optical = refined && optics_on(material_optics(sc, h.sample.material));
+                gn = normal_tetra(g, ro + rd * h.t,
+                                  optical ? R(1e-4) : r_max(h.t * pixel_cone * R(0.5), R(1e-4)) * sc.pixel_tolerance);
                 res.de_evals += 4;
             }
             if (bounce == 0) { first_depth = h.t; aux[0] = gn.x; aux[1] = gn.y; aux[2] = gn.z; aux[3] = R(h.steps); }
         }
-        if (in_fog) {  // pathtrace.wgsl:980-1011
+        if (in_fog && !solid_medium) {  // pathtrace.wgsl:980-1011
             const R t_end = h.hit ? h.t : extent;
             const V3<R> direct_volume = throughput * fog_segment_direct(sc, ro, rd, t_end, &rng, sample, point_stream,
-                                                                        bounce == 0, visible_from);
+                                                                        bounce == 0 && null_surfaces == 0, visible_from);
             L = L + direct_volume;
             if (bounce == 0) primary_volume = primary_volume + direct_volume;
             const R t_s = fog_free_flight(sc, ro, rd, t_end, &rng);
             if (t_s < t_end) {
                 if (bounce == 0) volume_path = true;
+                tex_width += t_s * tex_spread;
+                tex_spread = r_max(tex_spread, R(0.25));
                 if (bounce == 0 && !h.hit) first_depth = t_s;
                 const V3<R> p_s = ro + rd * t_s;
                 const R volume_area_total = area_total_weight(sc, p_s, V3<R>(0, 0, 0));
@@ -1696,6 +2267,18 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
             break;
         }
         V3<R> n = gn;
+        const Optics<R>& hit_optics = material_optics(sc, h.sample.material);
+        const bool optical = optics && optics_on(hit_optics);
+        const bool entering = rd.dot(gn) < R(0);
+        if (optical && !entering) n = -n;
+        if (optical && hit_optics.surface[0] < R(1) && rnd<R>(&rng) >= hit_optics.surface[0]) {
+            // a coverage null event (pathtrace.wgsl:1058-1065): the same bounce continues past it
+            null_surfaces++;
+            if (null_surfaces > 32u) break;
+            ro = p + rd * r_max(h.t * pixel_cone * R(0.15) * sc.pixel_tolerance, R(1e-4));
+            if (bounce == 0) { first_depth = -1; aux[0] = aux[1] = aux[2] = 0; aux[3] = -1; }
+            continue;
+        }
         if (bounce == 0) {
             first_depth = h.t;
             aux[0] = n.x; aux[1] = n.y; aux[2] = n.z; aux[3] = R(h.steps);
@@ -1703,9 +2286,30 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
             throughput = throughput * (R(1) - sc.cavity * (x * x * (R(3) - R(2) * x)));
         }
         V3<R> v = -rd;
-        Surface<R> s = make_surface(sc, n, h.sample);
+        tex_width += h.t * tex_spread;
+        Surface<R> s = make_surface(sc, p, n, v, h.sample, r_max(tex_width, R(1e-4)));
         L = L + throughput * s.emission;
         R offset = r_max(h.t * pixel_cone * R(2), R(1e-3)) * sc.pixel_tolerance;
+        if (optical && hit_optics.surface[1] > R(0) && rnd<R>(&rng) < hit_optics.surface[1]) {
+            // the dielectric lobe (pathtrace.wgsl:1088-1107)
+            if (bounce == sc.max_bounces) break;
+            const OpticalBounce<R> b = optical_bounce(hit_optics, n, rd, s.alpha, entering, &rng);
+            if (!b.valid) break;
+            throughput = throughput * b.weight;
+            const R bias = r_max(R(1e-4), r_min(offset, R(0.001)));
+            ro = p + b.direction * bias;
+            rd = b.direction;
+            if (b.transmitted && hit_optics.surface[3] == R(0)) {
+                solid_medium = entering;
+                medium_slot = h.sample.material;
+            }
+            prev_from_bsdf = false;
+            prev_from_volume = false;
+            prev_pdf = 0;
+            tex_spread = r_max(tex_spread, s.alpha * R(0.1));
+            bounce++;
+            continue;
+        }
         V3<R> p_off = p + n * offset;
         R nv = r_max(s.n.dot(v), R(1e-4));
         R p_spec = spec_probability(s, nv);
@@ -1732,7 +2336,9 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
             }
             auto visible = [&](V3<R> dir, R t_end) { return visible_from(p_off, dir, t_end); };
             // direct_light's fog transmittance toward each light (pathtrace.wgsl:501-549)
-            auto fog_tr = [&](V3<R> dir, R dist) { return in_fog ? fog_transmittance(sc, p_off, dir, dist) : R(1); };
+            auto fog_tr = [&](V3<R> dir, R dist) {
+                return (in_fog && !solid_medium) ? fog_transmittance(sc, p_off, dir, dist) : R(1);
+            };
             for (uint32_t i = 0; i < sc.light_count; ++i) {
                 const Light<R>& l = sc.lights[i];
                 if (l.kind == SF_LIGHT_ENVIRONMENT) {
@@ -1744,12 +2350,13 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     V3<R> ldir = cosine_sample(s.n, r1, r2);
                     R nl = r_max(s.n.dot(ldir), R(0));
                     if (n.dot(ldir) <= R(0) || nl <= R(0)) continue;
-                    if (!visible(ldir, extent)) continue;
+                    const R vw = visible(ldir, extent);
+                    if (!(vw > R(0))) continue;
                     R pl = probability * nl / R(PI_W);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
                     L = L + throughput * (brdf_eval(s, v, ldir) * nl * environment_value(l, ldir) *
-                                          fog_tr(ldir, extent) * w / pl);
+                                          (vw * fog_tr(ldir, extent)) * w / pl);
                 } else if (l.kind == SF_LIGHT_HDRI) {
                     if (l.color.x <= R(0)) continue;
                     R r0 = rnd<R>(&rng);
@@ -1758,23 +2365,25 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     V3<R> ldir = hdri_sample(l, r0, r1, r2);
                     R nl = s.n.dot(ldir);
                     if (nl <= R(0) || n.dot(ldir) <= R(0)) continue;
-                    if (!visible(ldir, extent)) continue;
+                    const R vw = visible(ldir, extent);
+                    if (!(vw > R(0))) continue;
                     R pl = hdri_pdf(l, ldir);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) * fog_tr(ldir, extent) *
-                                          w / pl);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * hdri_lookup(l, ldir) *
+                                          (vw * fog_tr(ldir, extent)) * w / pl);
                 } else if (l.kind == SF_LIGHT_SUN) {
                     R r1 = rnd<R>(&rng);
                     R r2 = rnd<R>(&rng);
                     V3<R> ldir = cone_sample(l.a, l.cos_max, r1, r2);
                     R nl = s.n.dot(ldir);
                     if (nl <= R(0) || n.dot(ldir) <= R(0)) continue;
-                    if (!visible(ldir, extent)) continue;
+                    const R vw = visible(ldir, extent);
+                    if (!(vw > R(0))) continue;
                     R pl = sun_pdf(l.cos_max);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * w * fog_tr(ldir, extent));
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * w * (vw * fog_tr(ldir, extent)));
                 } else if (i == selected) {
                     R u1 = rnd<R>(&rng);
                     R u2 = rnd<R>(&rng);
@@ -1789,11 +2398,12 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R cos_l = ln.dot(-ldir);
                     if (nl <= R(0) || cos_l <= R(0) || n.dot(ldir) <= R(0)) continue;
                     R endpoint = r_max(R(0), dist - r_max(R(1e-5), dist * R(1e-6)));
-                    if (!visible(ldir, endpoint)) continue;
+                    const R vw = visible(ldir, endpoint);
+                    if (!(vw > R(0))) continue;
                     R pl = (selected_weight / area_total) * area_direction_pdf(l, dist2, cos_l);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * fog_tr(ldir, dist) * w / pl);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * (vw * fog_tr(ldir, dist)) * w / pl);
                 }
             }
         }
@@ -1822,6 +2432,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
         }
         ro = p_off;
         rd = ldir;
+        tex_spread = r_max(tex_spread, s.alpha * R(0.25));
         bounce++;
     }
     bool ok = L.x == L.x && L.y == L.y && L.z == L.z && r_abs(L.x) < R(1e30) && r_abs(L.y) < R(1e30) &&

@@ -217,6 +217,19 @@ template <class R> struct Coloring {
     R pos[SF_MAX_RAMP_STOPS];
 };
 template <class R> struct Mat { V3<R> albedo; R roughness, metallic, specular; V3<R> emission; };
+// FinishDetail (GpuFinish.detail_*, uniforms.rs:797-815): kind 0 = none.
+template <class R> struct Detail { uint32_t kind = 0, seed = 0; R scale = 1, strength = 0, bump = 0, rough_delta = 0; V3<R> tint; };
+// GpuOptics (uniforms.rs:103-122): enabled when absorption.w > 0.
+template <class R> struct Optics { R surface[4] = {0, 0, 0, 0}, absorption[4] = {0, 0, 0, 0}, subsurface[4] = {0, 0, 0, 0}; };
+// GpuTexture (uniforms.rs:340-379) with the texture's own graph.
+template <class R> struct Texture {
+    const Graph* graph = nullptr;
+    uint32_t channel = 0, octaves = 1, budget = 1;
+    R mapping[4] = {0, 0, 0, 1}, rotation[4] = {0, 0, 0, 1}, effects[4] = {0, 0, 0, 0};
+    R weights[4] = {0, 0, 0, 0}, extra[3] = {0, 0, 0};
+    R parallax[2] = {0, 8}, fan[4] = {0, 0, 0, 0}, mask[4] = {0, 0, 0, 0};
+    Coloring<R> ramp;
+};
 template <class R> struct Scene {
     Camera<R> cam;
     Mat<R> material;
@@ -225,6 +238,12 @@ template <class R> struct Scene {
     Light<R> lights[SF_MAX_LIGHTS];
     uint32_t light_count = 0;
     Coloring<R> coloring;
+    R col_weights[4] = {0, 0, 0, 0}, col_extra[3] = {0, 0, 0};  // the orbit mix of coloring slot 6
+    Detail<R> details[SF_MAX_FINISHES];
+    R dune_wind = 0;  // radians
+    Optics<R> optics[SF_MAX_FINISHES + 1];
+    bool has_optics = false;
+    Texture<R> tex;
     uint32_t variation_slot = 0, variation_enabled = 0;
     R var_rough[2] = {0, 0}, var_metal[2] = {0, 0};
     R cavity = 0;

@@ -100,6 +100,33 @@ class sf_fog(C.Structure):
                 ("anisotropy", C.c_float), ("color", C.c_float * 3)]
 
 
+class sf_finish_detail(C.Structure):
+    _fields_ = [("pattern", C.c_uint32), ("seed", C.c_uint32), ("scale", C.c_float), ("strength", C.c_float),
+                ("bump", C.c_float), ("roughness_delta", C.c_float), ("tint", C.c_float * 3)]
+
+
+class sf_orbit_coloring(C.Structure):
+    _fields_ = [("traps", C.c_float * 4), ("iterations", C.c_float), ("normal", C.c_float),
+                ("logarithmic", C.c_float)]
+
+
+class sf_optics(C.Structure):
+    _fields_ = [("enabled", C.c_uint32), ("opacity", C.c_float), ("transmission", C.c_float), ("ior", C.c_float),
+                ("thin_walled", C.c_uint32), ("absorption_color", C.c_float * 3),
+                ("absorption_distance", C.c_float), ("subsurface", C.c_float),
+                ("subsurface_color", C.c_float * 3), ("subsurface_radius", C.c_float)]
+
+
+class sf_texture(C.Structure):
+    _fields_ = [("graph", C.c_void_p), ("channel", C.c_uint32), ("orbit", sf_orbit_coloring),
+                ("scale", C.c_float), ("offset", C.c_float * 3), ("rotation", C.c_float * 3),
+                ("octaves", C.c_uint32), ("contrast", C.c_float), ("ramp", sf_coloring),
+                ("strength", C.c_float), ("roughness", C.c_float), ("bump", C.c_float), ("parallax", C.c_float),
+                ("parallax_steps", C.c_uint32), ("fan", C.c_uint32), ("fan_period", C.c_float * 2),
+                ("fan_rays", C.c_uint32), ("mask", C.c_uint32), ("mask_slot", C.c_uint32),
+                ("mask_value", C.c_float), ("mask_width", C.c_float)]
+
+
 class sf_scene_desc(C.Structure):
     _fields_ = [("camera", sf_camera), ("material", sf_material),
                 ("finishes", sf_material * SF_MAX_FINISHES), ("finish_count", C.c_uint32),
@@ -107,7 +134,11 @@ class sf_scene_desc(C.Structure):
                 ("variation_slot", C.c_uint32), ("variation_enabled", C.c_uint32),
                 ("variation_roughness", C.c_float * 2), ("variation_metallic", C.c_float * 2),
                 ("cavity_darkness", C.c_float), ("seed", C.c_uint64), ("coloring", sf_coloring),
-                ("fog", sf_fog)]
+                ("fog", sf_fog),
+                # ABI 1.3
+                ("details", sf_finish_detail * SF_MAX_FINISHES), ("dune_wind", C.c_float),
+                ("coloring_orbit", sf_orbit_coloring), ("optics", sf_optics * (SF_MAX_FINISHES + 1)),
+                ("texture", sf_texture)]
 
 
 class sf_render_config(C.Structure):

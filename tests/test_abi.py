@@ -78,7 +78,7 @@ def test_render_config_struct_matches_the_header(lib):
     """sf_render_config at ABI 1.2: the hit epsilon follows samples_per_dispatch."""
     from syfrack_gb300 import abi
 
-    assert lib.sf_abi_version() == (1 << 16) | 2
+    assert lib.sf_abi_version() == (1 << 16) | 3
     assert [f[0] for f in abi.sf_render_config._fields_][-1] == "hit_epsilon"
     assert C.sizeof(abi.sf_render_config) == 10 * 4
     header = open(os.path.join(ROOT, "include", "syfrack_gpu.h")).read()
@@ -96,3 +96,33 @@ def test_deep_zoom_frames_beyond_2_31_pixels_are_refused(lib):
     dummy = C.c_void_p(16)  # never dereferenced: the size check comes first
     assert lib.sf_deep_zoom_noalloc(C.byref(d), dummy, dummy, None) == 1  # SF_ERR_INVALID
     assert b"2^31" in lib.sf_last_error()
+
+
+def test_scene_descriptor_layout_matches_the_header(tmp_path):
+    """ABI 1.3 appends finish details, orbit colouring, optics and the texture to
+    sf_scene_desc: the ctypes mirror has the C compiler's sizes and offsets."""
+    import subprocess
+
+    from syfrack_gb300 import abi
+
+    src = tmp_path / "layout.c"
+    src.write_text("""
+#include <stdio.h>
+#include <stddef.h>
+#include "syfrack_gpu.h"
+int main(void) {
+    printf("%zu %zu %zu %zu %zu %zu %zu %zu %zu %zu\\n", sizeof(sf_scene_desc), offsetof(sf_scene_desc, fog),
+           offsetof(sf_scene_desc, details), offsetof(sf_scene_desc, dune_wind),
+           offsetof(sf_scene_desc, coloring_orbit), offsetof(sf_scene_desc, optics),
+           offsetof(sf_scene_desc, texture), sizeof(sf_texture), offsetof(sf_texture, ramp), sizeof(sf_optics));
+    return 0;
+}
+""")
+    exe = tmp_path / "layout"
+    subprocess.run(["gcc", "-I", os.path.join(ROOT, "include"), str(src), "-o", str(exe)], check=True)
+    got = [int(x) for x in subprocess.run([str(exe)], capture_output=True, text=True, check=True).stdout.split()]
+    S = abi.sf_scene_desc
+    want = [C.sizeof(S), S.fog.offset, S.details.offset, S.dune_wind.offset, S.coloring_orbit.offset,
+            S.optics.offset, S.texture.offset, C.sizeof(abi.sf_texture), abi.sf_texture.ramp.offset,
+            C.sizeof(abi.sf_optics)]
+    assert got == want
