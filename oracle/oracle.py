@@ -84,6 +84,7 @@ def lib():
         L.or_mandel_escapes.restype = C.c_int
         L.or_mandel_escapes.argtypes = [C.c_int, C.c_double, C.c_double, C.c_double, C.c_double,
                                         C.c_uint32]
+        L.or_texture_values.argtypes = [C.POINTER(abi.sf_scene_desc), C.c_int, dp, C.c_size_t, dp]
         _lib = L
     return _lib
 
@@ -233,3 +234,13 @@ def mandel_orbit(c_ref, max_iter, bailout=2.0, precision=128):
     n = lib().or_mandel_orbit(precision, float(c_ref[0]), float(c_ref[1]), max_iter, bailout,
                               out.ctypes.data_as(C.POINTER(C.c_float)))
     return out[:n].copy()
+
+
+def texture_values(scene_desc, texture_graph, points, precision=32):
+    """pattern_value (pattern.wgsl:2-49) of the descriptor's texture at points[n, 3]; the
+    texture's graph is given as an OracleGraph."""
+    pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+    scene_desc.texture.graph = texture_graph.h
+    out = np.zeros(len(pts))
+    lib().or_texture_values(C.byref(scene_desc), precision, _dp(pts), len(pts), _dp(out))
+    return out

@@ -348,4 +348,20 @@ int or_mandel_escapes(int precision, double cx_hi, double cx_lo, double cy_hi, d
     return it < max_iter ? 1 : 0;
 }
 
+// The scene's texture value (pattern_value) at n points; sf_texture.graph carries an
+// oracle graph handle.
+void or_texture_values(const sf_scene_desc* scene, int precision, const double* xyz, size_t n, double* out) {
+    sf_render_config cfg{};
+    cfg.width = cfg.height = 1;
+    const Graph& tg = *reinterpret_cast<const Graph*>(scene->texture.graph);
+    if (precision == 32) {
+        const Scene<float> s = make_scene<float>(tg, *scene, cfg);
+        for (size_t i = 0; i < n; ++i)
+            out[i] = texture_value_at<float>(s, V3<float>(float(xyz[3 * i]), float(xyz[3 * i + 1]), float(xyz[3 * i + 2])));
+    } else {
+        const Scene<double> s = make_scene<double>(tg, *scene, cfg);
+        for (size_t i = 0; i < n; ++i) out[i] = texture_value_at<double>(s, V3<double>(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]));
+    }
+}
+
 }  // extern "C"

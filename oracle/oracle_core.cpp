@@ -2534,6 +2534,9 @@ template <class R> Sample<R> planar_sample(const PlanarParams& f, V2<R> input) {
 // explicit instantiations
 template Sample<float> evaluate<float>(const Graph&, V3<float>, bool);
 template Sample<double> evaluate<double>(const Graph&, V3<double>, bool);
+template <class R> R texture_value_at(const Scene<R>& sc, V3<R> p) { return texture_value(sc.tex, p); }
+template float texture_value_at<float>(const Scene<float>&, V3<float>);
+template double texture_value_at<double>(const Scene<double>&, V3<double>);
 template Scene<float> make_scene<float>(const Graph&, const sf_scene_desc&, const sf_render_config&);
 template Scene<double> make_scene<double>(const Graph&, const sf_scene_desc&, const sf_render_config&);
 template PixelResult radiance<float>(const Graph&, const Scene<float>&, uint32_t, uint32_t, uint32_t);

@@ -257,6 +257,8 @@ template <class R> struct Scene {
     uint32_t width = 1, height = 1, max_bounces = 4, max_steps = 256;
 };
 template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, const sf_render_config& c);
+// pattern_value (pattern.wgsl:2-49) of the scene's texture at p.
+template <class R> R texture_value_at(const Scene<R>& sc, V3<R> p);
 
 // L: the sample's radiance; V: its volume part (pathtrace.wgsl:1197-1198: all of L when
 // the camera segment scattered in fog, else that segment's in-scattered emitter light);

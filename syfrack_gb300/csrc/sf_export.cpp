@@ -271,6 +271,8 @@ extern "C" sf_status sf_export_readback(sf_export* e, sf_film_planes* out) {
 extern "C" sf_status sf_export_save(sf_export* e, const char* dir) {
     if (!e || !dir || !*dir) return fail(SF_ERR_INVALID, "null argument");
     if (has_hdri(e->win->scene)) return fail(SF_ERR_UNSUPPORTED, "scenes with an HDRI panorama are not checkpointed");
+    if (e->win->scene.texture.graph)  // the texture's graph is a caller object, like a panorama
+        return fail(SF_ERR_UNSUPPORTED, "textured scenes are not checkpointed");
     cudaSetDevice(e->ctx->device);
     sf_status st = flush(e);
     if (st != SF_OK) return st;

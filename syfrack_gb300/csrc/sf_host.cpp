@@ -1906,6 +1906,8 @@ bool has_hdri(const sf_scene_desc& d) {
 extern "C" sf_status sf_session_save(sf_session* s, const char* dir) {
     if (!s || !dir || !*dir) return fail(SF_ERR_INVALID, "null argument");
     if (has_hdri(s->scene)) return fail(SF_ERR_UNSUPPORTED, "scenes with an HDRI panorama are not checkpointed");
+    if (s->scene.texture.graph)  // the texture's graph is a caller object, like a panorama
+        return fail(SF_ERR_UNSUPPORTED, "textured scenes are not checkpointed");
     sf_context* c = s->ctx;
     cudaSetDevice(c->device);
     CU(cudaStreamSynchronize(c->stream));

@@ -223,11 +223,14 @@ class RenderSession:
         self.scene = scene
         self.cfg = cfg
         self.graph = renderer.compile(scene.graph)
+        tex = scene.material.texture
+        # the texture's graph is compiled like the form's and kept alive with the session
+        self.tex_graph = renderer.compile(tex.graph) if tex is not None else None
         self.t0 = time.perf_counter()
         if _handle is not None:
             self.h = _handle
             return
-        sd = scene.desc(cfg.width, cfg.height)
+        sd = scene.desc(cfg.width, cfg.height, self.tex_graph.h.value if self.tex_graph else None)
         rc = cfg.desc()
         h = C.c_void_p()
         check(self.ctx.lib.sf_session_create(self.ctx.h, self.graph.h, C.byref(sd), C.byref(rc), C.byref(h)))
@@ -391,11 +394,14 @@ class ExportSession:
         self.scene = scene
         self.cfg = cfg
         self.graph = renderer.compile(scene.graph)
+        tex = scene.material.texture
+        # the texture's graph is compiled like the form's and kept alive with the session
+        self.tex_graph = renderer.compile(tex.graph) if tex is not None else None
         self.t0 = time.perf_counter()
         if _handle is not None:
             self.h = _handle
             return
-        sd = scene.desc(cfg.width, cfg.height)
+        sd = scene.desc(cfg.width, cfg.height, self.tex_graph.h.value if self.tex_graph else None)
         rc = cfg.desc()
         h = C.c_void_p()
         check(self.ctx.lib.sf_export_create(self.ctx.h, self.graph.h, C.byref(sd), C.byref(rc), C.byref(h)))

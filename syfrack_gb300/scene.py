@@ -259,10 +259,130 @@ class Ramp:
 
 
 @dataclass
+class OrbitColoring:
+    """OrbitColoring (material.rs:18-56): weights of the four traps, the iteration
+    fraction and n.y * 0.5 + 0.5, optional signed log remapping."""
+    traps: tuple = (1.0, 0.0, 0.0, 0.0)
+    iterations: float = 0.0
+    normal: float = 0.0
+    logarithmic: float = 0.0
+
+    def pack(self, out: abi.sf_orbit_coloring):
+        out.traps[:] = [float(x) for x in self.traps]
+        out.iterations, out.normal, out.logarithmic = self.iterations, self.normal, self.logarithmic
+
+
+@dataclass
 class Coloring:
-    """Coloring::Trap{slot, ramp} (material.rs:100-130); slot 4 = iterations, 5 = normal."""
+    """Coloring::Trap{slot, ramp} (material.rs:100-130); slot 4 = iterations, 5 = normal;
+    with `orbit` set, Coloring::Orbit{channels, ramp} (slot 6)."""
     slot: int = 0
     ramp: Ramp = field(default_factory=Ramp)
+    orbit: OrbitColoring | None = None
+
+
+FINISH_PATTERNS = ["VeinedStone", "Patina", "BrushedMetal", "Basalt", "Ripples", "Rosettes", "CoastalRock", "Sand",
+                   "Dust", "Concrete", "WeatheredConcrete", "WetConcrete"]
+
+
+@dataclass
+class FinishDetail:
+    """FinishDetail (material.rs:200-224): a world-space pattern on a finish."""
+    pattern: str = "VeinedStone"
+    seed: int = 7
+    scale: float = 2.0
+    strength: float = 0.25
+    bump: float = 0.004
+    roughness_delta: float = 0.15
+    tint: tuple = (0.3, 0.27, 0.2)
+
+    def pack(self, out: abi.sf_finish_detail):
+        out.pattern = FINISH_PATTERNS.index(self.pattern) + 1
+        out.seed = self.seed
+        out.scale, out.strength, out.bump, out.roughness_delta = self.scale, self.strength, self.bump, self.roughness_delta
+        out.tint[:] = [float(x) for x in self.tint]
+
+
+@dataclass
+class Optics:
+    """Optics (optics.rs:7-38): coverage, a rough dielectric interface and an interior medium."""
+    opacity: float = 1.0
+    transmission: float = 1.0
+    ior: float = 1.5
+    thin_walled: bool = False
+    absorption_color: tuple = (1.0, 1.0, 1.0)
+    absorption_distance: float = 1.0
+    subsurface: float = 0.0
+    subsurface_color: tuple = (0.9, 0.9, 0.9)
+    subsurface_radius: float = 0.5
+
+    def pack(self, out: abi.sf_optics):
+        out.enabled = 1
+        out.opacity, out.transmission, out.ior = self.opacity, self.transmission, self.ior
+        out.thin_walled = int(self.thin_walled)
+        out.absorption_color[:] = [float(x) for x in self.absorption_color]
+        out.absorption_distance = self.absorption_distance
+        out.subsurface = self.subsurface
+        out.subsurface_color[:] = [float(x) for x in self.subsurface_color]
+        out.subsurface_radius = self.subsurface_radius
+
+
+@dataclass
+class FractalTexture:
+    """FractalTexture (texture.rs:62-136): a volumetric texture from a second graph.
+    channel: ("trap", slot), ("iterations",), ("distance",) or ("orbit", OrbitColoring)."""
+    graph: Graph = None
+    channel: tuple = ("trap", 0)
+    scale: float = 3.0
+    offset: tuple = (0.37, 0.19, 0.53)
+    rotation: tuple = (0.0, 0.0, 0.0)
+    octaves: int = 2
+    contrast: float = 2.0
+    ramp: Ramp = field(default_factory=lambda: Ramp(stops=[(0.12, 0.22, 0.27), (0.86, 0.6, 0.22)]))
+    strength: float = 1.0
+    roughness: float = 0.35
+    bump: float = 0.15
+    parallax: float = 0.0
+    parallax_steps: int = 8
+    fan: tuple | None = None   # (period_x, period_z, rays)
+    mask: tuple | None = None  # (trap slot, value, width)
+
+    def pack(self, out: abi.sf_texture, graph_handle):
+        kind = self.channel[0]
+        out.graph = graph_handle
+        out.channel = {"trap": None, "iterations": 4, "distance": 6, "orbit": 7}[kind] if kind != "trap" else int(self.channel[1])
+        if kind == "orbit":
+            self.channel[1].pack(out.orbit)
+        out.scale = self.scale
+        out.offset[:] = [float(x) for x in self.offset]
+        out.rotation[:] = [float(x) for x in self.rotation]
+        out.octaves, out.contrast = self.octaves, self.contrast
+        _pack_ramp(self.ramp, out.ramp)
+        out.strength, out.roughness, out.bump = self.strength, self.roughness, self.bump
+        out.parallax, out.parallax_steps = self.parallax, self.parallax_steps
+        if self.fan is not None:
+            out.fan = 1
+            out.fan_period[:] = [float(self.fan[0]), float(self.fan[1])]
+            out.fan_rays = int(self.fan[2])
+        if self.mask is not None:
+            out.mask = 1
+            out.mask_slot, out.mask_value, out.mask_width = int(self.mask[0]), float(self.mask[1]), float(self.mask[2])
+
+
+def _pack_ramp(r: Ramp, out: abi.sf_coloring):
+    """GpuRamp::from_ramp: stops with their positions (palette.rs:106-115)."""
+    if len(r.stops) > abi.SF_MAX_RAMP_STOPS:
+        raise ValueError("at most 16 ramp stops")
+    n = len(r.stops)
+    out.stop_count = n
+    for i, c in enumerate(r.stops):
+        # Ramp::position: given, else i / (n or n - 1)
+        pos = r.positions[i] if r.positions else float(f32(i) / f32(n if r.cyclic else max(n - 1, 1)))
+        out.stops[i][:] = [float(c[0]), float(c[1]), float(c[2]), float(pos)]
+    out.cyclic = int(r.cyclic)
+    out.smooth = int(r.smooth)
+    out.positioned = int(bool(r.positions))
+    out.frequency, out.phase, out.gamma = r.frequency, r.phase, r.gamma
 
 
 @dataclass
@@ -272,6 +392,8 @@ class Finish:
     metallic: float = 0.0
     specular: float = 0.04
     emission: tuple = (0.0, 0.0, 0.0)
+    detail: FinishDetail | None = None
+    optics: Optics | None = None
 
     def packed(self) -> abi.sf_material:
         m = abi.sf_material()
@@ -294,6 +416,7 @@ class Material(Finish):
     finishes: list = field(default_factory=list)
     surface: SurfaceVariation | None = None
     coloring: Coloring | None = None
+    texture: FractalTexture | None = None
 
 
 @dataclass
@@ -317,9 +440,11 @@ class Scene:
     seed: int = 0
     cavity_darkness: float = 0.0
     fog: Fog | None = None
+    dune_wind: float = 0.0  # Dunes.wind_direction (degrees): the Sand detail's wind
 
-    def desc(self, width: int, height: int) -> abi.sf_scene_desc:
-        """The scene half of Uniforms::from_scene (uniforms.rs:748-830)."""
+    def desc(self, width: int, height: int, texture_graph=None) -> abi.sf_scene_desc:
+        """The scene half of Uniforms::from_scene (uniforms.rs:748-830). texture_graph:
+        the handle of the compiled texture graph when the material has a texture."""
         b = self.camera.basis()
         d = abi.sf_scene_desc()
         cam = d.camera
@@ -359,20 +484,23 @@ class Scene:
         col = self.material.coloring
         d.coloring.slot = 0xFFFF
         if col is not None:
-            r = col.ramp
-            if len(r.stops) > abi.SF_MAX_RAMP_STOPS:
-                raise ValueError("at most 16 ramp stops")
-            d.coloring.slot = col.slot
-            d.coloring.stop_count = len(r.stops)
-            n = len(r.stops)
-            for i, c in enumerate(r.stops):
-                # Ramp::position (palette.rs:106-115): given, else i / (n or n - 1)
-                pos = r.positions[i] if r.positions else float(f32(i) / f32(n if r.cyclic else max(n - 1, 1)))
-                d.coloring.stops[i][:] = [float(c[0]), float(c[1]), float(c[2]), float(pos)]
-            d.coloring.cyclic = int(r.cyclic)
-            d.coloring.smooth = int(r.smooth)
-            d.coloring.positioned = int(bool(r.positions))
-            d.coloring.frequency, d.coloring.phase, d.coloring.gamma = r.frequency, r.phase, r.gamma
+            _pack_ramp(col.ramp, d.coloring)
+            d.coloring.slot = 6 if col.orbit is not None else col.slot
+            if col.orbit is not None:
+                col.orbit.pack(d.coloring_orbit)
+        # ABI 1.3: finish details, optics, the texture
+        d.dune_wind = self.dune_wind
+        for i, f in enumerate(self.material.finishes):
+            if f.detail is not None:
+                f.detail.pack(d.details[i])
+            if f.optics is not None:
+                f.optics.pack(d.optics[i + 1])
+        if self.material.optics is not None:
+            self.material.optics.pack(d.optics[0])
+        if self.material.texture is not None:
+            if texture_graph is None:
+                raise ValueError("a textured scene needs its compiled texture graph")
+            self.material.texture.pack(d.texture, texture_graph)
         return d
 
 
