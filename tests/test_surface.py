@@ -308,7 +308,11 @@ def test_texture_changes_colour_roughness_and_relief_without_changing_geometry(r
     base_scene.material.texture = None
     base = render(renderer, base_scene, cfg)
     neutral = render(renderer, textured_scene(strength=0.0, roughness=0.0, bump=0.0), cfg)
-    np.testing.assert_array_equal(neutral.accum, base.accum)
+    # the textured scene runs the kernel built with the texture interpreter, whose fused
+    # operations elsewhere may round differently: equal to float rounding (the
+    # reference's bound is a mean difference below 1e-6)
+    np.testing.assert_allclose(neutral.accum, base.accum, rtol=1e-6, atol=1e-7)
+    assert np.abs(neutral.color - base.color).mean() < 1e-6
     for effect in ("strength", "roughness", "bump"):
         kw = dict(strength=0.0, roughness=0.0, bump=0.0)
         kw[effect] = 0.8
@@ -334,7 +338,7 @@ def test_parallax_and_mask(renderer):
     base_scene.material.texture = None
     base = render(renderer, base_scene, cfg)
     masked = render(renderer, textured_scene(fan=(2.6, 2.0, 18), mask=(3, 0.0, 0.05)), cfg)  # trap 3 unwritten
-    np.testing.assert_array_equal(masked.accum, base.accum)
+    np.testing.assert_allclose(masked.accum, base.accum, rtol=1e-6, atol=1e-7)  # the textured kernel's rounding
     shown = render(renderer, textured_scene(fan=(2.6, 2.0, 18), mask=(3, 1.0, 0.05)), cfg)
     assert not np.array_equal(shown.accum, base.accum)
     np.testing.assert_array_equal(shown.depth, base.depth)
