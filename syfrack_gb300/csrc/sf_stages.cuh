@@ -84,8 +84,9 @@ static __device__ __forceinline__ void generate_path(const DevScene& S, PathSoA&
     path_pixel(g, local, px, py, sample);
     PathState ps;
     path_begin(S, ps, px, py, sample);
-    if (soa.ex)  // the trace kernel samples the initial medium of optics scenes first
-        soa.ex[path] = make_float4(0.f, 0.f, __uint_as_float((S.rich & SF_RICH_OPTICS) ? SF_EX_INIT : 0u), 0.f);
+    if (soa.ex)  // the camera's footprint; the trace kernel samples the initial medium of optics scenes first
+        soa.ex[path] = make_float4(ps.tex_width, ps.tex_spread,
+                                   __uint_as_float((S.rich & SF_RICH_OPTICS) ? SF_EX_INIT : 0u), 0.f);
     store_path(soa, path, ps, SF_PF_CONT);
     if (soa.pv) soa.pv[path] = make_float4(0.f, 0.f, 0.f, 0.f);
     begin_segment(S, soa, path, ps.o, ps.d, S.extent);

@@ -244,24 +244,64 @@ def glass_bulb_scene():
                          SunLight(direction=(0.3, 0.9, -0.2), intensity=2.0), EnvironmentLight()], seed=9)
 
 
+def glass_sphere_scene():
+    """A frosted, tinted, scattering glass sphere and a thin tinted sheet finish on a
+    tagged half, under a softbox, a sun and the sky."""
+    g = Graph([Node(0, Kind("Input")), Node(1, Kind("Sphere", radius=1.0)),
+               Node(2, Kind("Box", half=[0.8, 0.02, 0.8])), Node(3, Kind("Translate", offset=[0.0, 1.3, 0.0])),
+               Node(4, Kind("MaterialTag", index=1)), Node(5, Kind("Union")), Node(6, Kind("Output"))],
+              [Link((0, 0), (1, 0)), Link((0, 0), (3, 0)), Link((3, 0), (2, 0)), Link((2, 0), (4, 0)),
+               Link((1, 0), (5, 0)), Link((4, 0), (5, 1)), Link((5, 0), (6, 0))], safety=1.0, bounding_radius_hint=2.0)
+    mat = Material(albedo=(0.8, 0.75, 0.7), roughness=0.15)
+    mat.optics = Optics(ior=1.5, absorption_color=(0.7, 0.85, 0.6), absorption_distance=1.2, opacity=0.9,
+                        transmission=0.95, subsurface=0.4, subsurface_radius=0.6)
+    sheet = Finish(albedo=(0.9, 0.9, 0.9), roughness=0.1, metallic=0.0, specular=0.04,
+                   optics=Optics(thin_walled=True, absorption_color=(0.9, 0.5, 0.4), opacity=0.7))
+    mat.finishes = [sheet]
+    return Scene(graph=g, camera=Camera((0.4, 0.9, 3.2), (0.0, 0.2, 0.0), 0.0, 40.0, 0.0, 3.0), material=mat,
+                 lights=[AreaLight(position=(1.5, 3.0, 1.5), normal=(-0.4, -0.8, -0.4), size=(1.5, 1.5), intensity=8.0),
+                         SunLight(direction=(0.3, 0.9, -0.2), intensity=2.0), EnvironmentLight()], seed=4)
+
+
 @pytest.mark.gpu
 def test_device_optics_follow_the_oracle(renderer, oracle_mod):
-    """A glass Mandelbulb (coverage, refraction, absorption, subsurface, shadows through
-    coverage): both integrators within a rounding of each other, and the f32 oracle's
-    image within the film tolerance on 128 seeded pixels."""
-    scene = glass_bulb_scene()
-    out, cfg = both(renderer, scene, 96, 64, 8, max_bounces=4, max_steps=256)
+    """A glass sphere under a tinted sheet (coverage, refraction, absorption, subsurface,
+    thin walls, shadows through coverage, all three light kinds): both integrators agree
+    and follow the f32 oracle within the film tolerance on 128 seeded pixels."""
+    scene = glass_sphere_scene()
+    out, cfg = both(renderer, scene, 96, 64, 16, max_bounces=6, max_steps=256)
     wf, mk = out["wavefront"], out["megakernel"]
     assert np.all(np.isfinite(wf.accum)) and np.all(np.isfinite(mk.accum))
-    diff = np.abs(wf.color[..., :3] - mk.color[..., :3])
-    assert float(np.sqrt(np.mean(diff ** 2))) < 2e-2
+    assert float(np.sqrt(np.mean((wf.color[..., :3] - mk.color[..., :3]) ** 2))) < 1e-2
     rng = np.random.default_rng(5)
     pix = np.stack([rng.integers(0, 96, 128), rng.integers(0, 64, 128)], 1).astype(np.uint32)
     ref, _ = oracle_color(oracle_mod, scene, cfg, pixels=pix)
     mine = wf.color[pix[:, 1], pix[:, 0], :3]
     rmse = float(np.sqrt(np.mean((mine - ref) ** 2)))
     assert rmse <= 2e-2, rmse
-    assert mine.mean() > 0.02
+    assert mine.mean() > 0.05
+
+
+@pytest.mark.gpu
+def test_glass_mandelbulb_at_the_binary32_floor(renderer, oracle_mod):
+    """A glass Mandelbulb: the Newton refinement on a fractal field (steps clamped to 0.5)
+    and the refractions make paths chaotic, so the f32 oracle itself differs from FP64
+    by branch flips. The device is held to that floor: its image error against the f32
+    oracle at most 1.5 times the f32 oracle's against FP64, its mean within 2%."""
+    scene = glass_bulb_scene()
+    out, cfg = both(renderer, scene, 96, 64, 32, max_bounces=4, max_steps=256)
+    wf, mk = out["wavefront"], out["megakernel"]
+    assert np.all(np.isfinite(wf.accum)) and np.all(np.isfinite(mk.accum))
+    rng = np.random.default_rng(5)
+    pix = np.stack([rng.integers(0, 96, 128), rng.integers(0, 64, 128)], 1).astype(np.uint32)
+    ref32, _ = oracle_color(oracle_mod, scene, cfg, pixels=pix)
+    ref64, _ = oracle_color(oracle_mod, scene, cfg, pixels=pix, precision=64)
+    floor = float(np.sqrt(np.mean((ref32 - ref64) ** 2)))
+    for film in (wf, mk):
+        mine = film.color[pix[:, 1], pix[:, 0], :3]
+        rmse = float(np.sqrt(np.mean((mine - ref32) ** 2)))
+        assert rmse <= 1.5 * floor + 2e-3, (rmse, floor)
+        assert abs(mine.mean() - ref64.mean()) <= 0.02 * ref64.mean(), (mine.mean(), ref64.mean())
 
 
 @pytest.mark.gpu
