@@ -554,10 +554,11 @@ def serve_replay(renderer, ctx, events, args):
             "admission_waits": st["admission_waits"], "hbm_peak_gb": st["hbm_peak"] / (1 << 30)}
 
 
-def plain_replay(renderer, ctx, events, cap_s):
+def plain_replay(renderer, ctx, events, cap_s, integrator="wavefront"):
     """The same stream through the plain drop-in calls, one request at a time in
     arrival order: RenderSession + dispatch(1 spp) + readback per preview, a further
-    dispatch(8) + readback on that session per refinement, sf_escape2d per tile."""
+    dispatch(8) + readback on that session per refinement, sf_escape2d per tile.
+    integrator: the sessions' ("megakernel" is the reference's per-pixel loop)."""
     from syfrack_gb300 import RenderSession, escape2d
     from syfrack_gb300.workloads import SERVE_REFINE_WINDOW
 
@@ -579,7 +580,8 @@ def plain_replay(renderer, ctx, events, cap_s):
         elif kind == "preview":
             sc, cfg = payload
             # a session sized for its refinements: 8 samples per dispatch, open-ended target
-            cfg = type(cfg)(**{**cfg.__dict__, "samples_per_pixel": 1 << 16, "samples_per_dispatch": 8})
+            cfg = type(cfg)(**{**cfg.__dict__, "samples_per_pixel": 1 << 16, "samples_per_dispatch": 8,
+                               "integrator": integrator})
             s = RenderSession(renderer, sc, cfg)
             n = payload[1].samples_per_pixel
             s.dispatch((0, 0, cfg.width, cfg.height, 0), n)
@@ -630,10 +632,16 @@ def measure_serve(args):
     burst = [(0.0, k, pl) for _, k, pl in events[:args.burst]]
     cap_served = serve_replay(r, ctx, burst, args)
     cap_plain = plain_replay(r, ctx, burst, cap_s=600.0)
+    # the plain drop-in proper: previews and refinements through the per-pixel megakernel
+    cap_plain_mk = plain_replay(r, ctx, burst, cap_s=600.0, integrator="megakernel")
     capacity = {"requests": len(burst), "served_rps": cap_served["throughput_rps"],
                 "plain_rps": cap_plain["throughput_rps"],
                 "ratio": cap_served["throughput_rps"] / cap_plain["throughput_rps"],
                 "served_mrays_per_s": cap_served["mrays_per_s"], "plain_mrays_per_s": cap_plain["mrays_per_s"],
+                "plain_megakernel_rps": cap_plain_mk["throughput_rps"],
+                "plain_megakernel_mrays_per_s": cap_plain_mk["mrays_per_s"],
+                "ratio_vs_plain_megakernel": cap_served["throughput_rps"] / cap_plain_mk["throughput_rps"],
+                "mrays_ratio_vs_plain_megakernel": cap_served["mrays_per_s"] / cap_plain_mk["mrays_per_s"],
                 "served_batches": cap_served["batches"],
                 "served_mean_batch_requests": cap_served["mean_batch_requests"]}
     line = {"metric": "served p99 latency", "unit": "ms", "value": served["latency"]["all"].get("p99_ms"),
