@@ -316,9 +316,10 @@ def run_ours(args):
                             f"film read back; bytes per {spp_step}-spp step"},
             "roofline": {"bound": "fp32", "kernel": "k_trace", "achieved": achieved, "peak": peak.value,
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
-                         "traffic": profiled_traffic() if (cfg.width, cfg.height) == (1280, 720) else None,
-                         "traffic_source": "dram__bytes_read+write per k_trace launch, ncu capture at 640x360 x4 "
-                                           "(profiles/k_trace_mandelbox_640x360_ncu.md)", "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
+                         "traffic": profiled_traffic() if ((cfg.width, cfg.height) == (1280, 720)
+                                                           and spp_step == 64) else None,
+                         "traffic_source": "dram__bytes_read+write per k_trace launch, ncu capture at 640x360 x 64 "
+                                           "spp scaled x4 (profiles/k_trace_mandelbox_640x360_ncu.md)", "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
                          "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
                          "de_evals_per_step": st["de_evals"] / args.steps,
                          "de_iterations_per_step": st["de_iterations"] / args.steps,

@@ -223,7 +223,7 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
 
 extern "C" sf_status sf_batch_set_launch(sf_batch* b, uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
     if (!b) return fail(SF_ERR_INVALID, "null batch");
-    sf_status st = check_launch(min_blocks, quantum, regen);
+    sf_status st = check_launch(min_blocks, quantum, regen, false);
     if (st != SF_OK) return st;
     if (b->a.min_blocks != min_blocks || b->a.quantum != quantum || b->a.regen != regen) batch_drop_graph(b);
     b->a.min_blocks = min_blocks;

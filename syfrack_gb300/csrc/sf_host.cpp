@@ -1576,8 +1576,10 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
 }
 
 namespace sfh {
-sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
-    if (min_blocks < 2 || min_blocks > 4) return fail(SF_ERR_INVALID, "trace launch: 2..4 resident blocks per SM");
+sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen, bool small_blocks) {
+    // 2..4 blocks of 256 threads per SM; a single job may also take 6 or 7 of 128
+    const bool ok = (min_blocks >= 2 && min_blocks <= 4) || (small_blocks && (min_blocks == 6 || min_blocks == 7));
+    if (!ok) return fail(SF_ERR_INVALID, "trace launch: 2..4 resident blocks per SM (6 or 7 of 128 threads for a session)");
     if (quantum != 0 && quantum < 8) return fail(SF_ERR_INVALID, "step quantum below 8");
     if (regen < 1 || regen > 32) return fail(SF_ERR_INVALID, "regeneration threshold outside 1..32 lanes");
     return SF_OK;
@@ -1587,7 +1589,7 @@ sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen) {
 extern "C" sf_status sf_session_set_launch(sf_session* s, uint32_t min_blocks_per_sm, uint32_t quantum,
                                            uint32_t regen) {
     if (!s) return fail(SF_ERR_INVALID, "null session");
-    sf_status st = check_launch(min_blocks_per_sm, quantum, regen);
+    sf_status st = check_launch(min_blocks_per_sm, quantum, regen, true);
     if (st != SF_OK) return st;
     s->min_blocks = min_blocks_per_sm;
     s->quantum = quantum;

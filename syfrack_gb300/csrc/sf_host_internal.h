@@ -145,7 +145,7 @@ sf_status environment_tables(const float* rgb, uint32_t width, uint32_t height, 
                              uint32_t& ow, uint32_t& oh, bool& uniform);
 void environment_dev(const sf_environment* e, DevLight& o);
 bool has_hdri(const sf_scene_desc& d);
-sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen);
+sf_status check_launch(uint32_t min_blocks, uint32_t quantum, uint32_t regen, bool small_blocks);
 void planar_dev(const sf_planar_desc& f, PlanarDev& o);
 sf_status planar_check(const sf_planar_desc* f);
 cudaError_t film_readback(sf_context* c, const FilmPlanes& f, const sf_film_planes& out, cudaStream_t st);

@@ -692,7 +692,7 @@ cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom 
 }
 cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
                             unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
-    if (min_blocks < 2 || min_blocks > 4) min_blocks = 2;
+    if (min_blocks < 2 || min_blocks > 7 || min_blocks == 5) min_blocks = 2;
     if (blocks <= 0) blocks = sf_device_sm_count() * min_blocks;
     switch (form) {
     case SF_FORM_BULB: return sf_launch_trace_bulb(prog, scene, soa, tl, stats, blocks, min_blocks, st);

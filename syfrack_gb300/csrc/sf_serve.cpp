@@ -550,7 +550,7 @@ extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg
     if (k.slots > kServeMaxSlots) return fail(SF_ERR_INVALID, "1..8 slots");
     if (k.max_jobs > SF_BATCH_MAX_JOBS) return fail(SF_ERR_INVALID, "a batch holds 1 to 1024 requests");
     if (k.path_capacity > 0x7fffffffu) return fail(SF_ERR_INVALID, "path capacity above 2^31");
-    sf_status ls = check_launch(k.min_blocks, k.quantum, k.regen);
+    sf_status ls = check_launch(k.min_blocks, k.quantum, k.regen, false);
     if (ls != SF_OK) return ls;
     cudaSetDevice(c->device);
     auto* s = new sf_server();

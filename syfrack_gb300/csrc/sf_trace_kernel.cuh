@@ -55,8 +55,10 @@ static __device__ __forceinline__ uint32_t find_job(const uint32_t* begins, uint
 // 1e-4; a shadow segment crosses such surfaces, its weight (PathSoA.sh_d.w) times
 // 1 - opacity at each, and marches on from just past them, up to 32 crossings
 // (geometry_visibility_weight, lights.wgsl:263-283).
-template <int FORM, int MIN_BLOCKS, bool MULTI = false, bool LANE_STATS = false, bool OPTICS = false>
-__global__ void __launch_bounds__(256, MIN_BLOCKS) k_trace(const DeProgram* __restrict__ prog_g,
+// THREADS: 256, or 128 for the shapes that fit more warps per SM at the same registers.
+template <int FORM, int MIN_BLOCKS, bool MULTI = false, bool LANE_STATS = false, bool OPTICS = false,
+          int THREADS = 256>
+__global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* __restrict__ prog_g,
                                                            const DevScene* __restrict__ scene_g, PathSoA soa,
                                                            TraceLaunch tl, unsigned long long* stats,
                                                            BatchTable bt = BatchTable{}) {
@@ -393,6 +395,9 @@ static cudaError_t launch_trace_form(const DeProgram* prog, const DevScene* scen
     switch (min_blocks) {
     case 3: k_trace<FORM, 3><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
     case 4: k_trace<FORM, 4><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
+    // 128-thread blocks: 6 or 7 per SM (24 or 28 warps at up to 85 or 73 registers)
+    case 6: k_trace<FORM, 6, false, false, false, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats); break;
+    case 7: k_trace<FORM, 7, false, false, false, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats); break;
     default: k_trace<FORM, 2><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
     }
     return cudaGetLastError();
