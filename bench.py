@@ -904,7 +904,8 @@ def main():
     ap.add_argument("--steps", type=int, default=8)
     ap.add_argument("--warmup", type=int, default=3)
     ap.add_argument("--impl", default="ours", choices=["ours", "reference"])
-    ap.add_argument("--min-blocks", type=int, default=3)
+    ap.add_argument("--min-blocks", type=int, default=7,
+                    help="trace blocks per SM: 2-4 of 256 threads or 6-7 of 128 (batches take 2-4)")
     ap.add_argument("--quantum", type=int, default=0)
     ap.add_argument("--regen", type=int, default=4)
     ap.add_argument("--no-cpu-baseline", action="store_true")

@@ -636,6 +636,18 @@ sf_status ctx_alloc(sf_context* c, size_t bytes, void** p, bool trim) {
     *p = nullptr;
     if (bytes == 0) return SF_OK;
     std::unique_lock<std::mutex> lk(c->alloc_mu);
+    for (size_t i = 0; i < c->cached.size(); ++i) {  // an idle arena of this exact size
+        if (c->cached[i].second == bytes) {
+            *p = c->cached[i].first;
+            c->cached.erase(c->cached.begin() + long(i));
+            return SF_OK;
+        }
+    }
+    while (!c->cached.empty() && c->used + bytes > c->budget) {  // idle arenas give way first
+        cudaFree(c->cached.front().first);
+        c->used -= std::min<uint64_t>(c->used, c->cached.front().second);
+        c->cached.erase(c->cached.begin());
+    }
     if (trim && c->used + bytes > c->budget) {
         // The cached scratch of primary and escape-time calls gives way to an admission.
         // Its owner (stage_mu) may be in a readback: then wait for it, taking the locks in
@@ -671,6 +683,16 @@ void ctx_free(sf_context* c, void* p, size_t bytes) {
     cudaFree(p);
     c->used -= std::min<uint64_t>(c->used, bytes);
 }
+void ctx_free_cached(sf_context* c, void* p, size_t bytes) {
+    if (!p) return;
+    std::lock_guard<std::mutex> lk(c->alloc_mu);
+    c->cached.emplace_back(p, bytes);
+    if (c->cached.size() > 4) {
+        cudaFree(c->cached.front().first);
+        c->used -= std::min<uint64_t>(c->used, c->cached.front().second);
+        c->cached.erase(c->cached.begin());
+    }
+}
 
 void ctx_retain(sf_context* c) {
     std::lock_guard<std::mutex> lk(c->mu);
@@ -687,6 +709,8 @@ void ctx_release(sf_context* c) {
     collect_timing(c);
     for (auto e : c->spare) cudaEventDestroy(e);
     ctx_free(c, c->d_stats, SF_STAT_COUNT * sizeof(unsigned long long) + 64 * sizeof(uint32_t));
+    for (auto& b : c->cached) cudaFree(b.first);
+    c->cached.clear();
     if (c->stage) cudaFreeHost(c->stage);
     ctx_free(c, c->scratch, c->scratch_bytes);
     cudaStreamDestroy(c->stream);
@@ -1633,8 +1657,8 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
         CU(sf_launch_generate(s->d_scene, s->soa, g, s->counts, st));
     }
     const uint32_t rich = rich_of(s->scene);
-    // the optics trace kernel holds more state per lane: two blocks per SM
-    const int blocks = int((rich & SF_RICH_OPTICS) ? 2u : s->min_blocks) * c->sm_count;
+    // the optics trace kernel runs 6 blocks of 128 threads per SM
+    const int blocks = int((rich & SF_RICH_OPTICS) ? 6u : s->min_blocks) * c->sm_count;
     const uint32_t K = s->shadow_slots;
     for (uint32_t r = 0; r < R; ++r) {
         RoundQueues q;
@@ -1823,7 +1847,7 @@ extern "C" sf_status sf_session_destroy(sf_session* s) {
     sf_context* c = s->ctx;
     cudaSetDevice(c->device);
     cudaStreamSynchronize(c->stream);
-    ctx_free(c, s->mem, s->mem_bytes);
+    ctx_free_cached(c, s->mem, s->mem_bytes);  // idle now: kept for the next session of its size
     sf_graph* g = s->graph;
     delete s;
     sf_graph_destroy(g);  // drops the session's reference

@@ -81,6 +81,10 @@ struct sf_context {
     size_t stage_bytes = 0;
     void* scratch = nullptr;
     size_t scratch_bytes = 0;
+    // arenas of destroyed sessions (idle: their stream was synchronised), kept for the
+    // next session of the same size; counted in `used`, released first when an
+    // admission needs the room (alloc_mu guards them)
+    std::vector<std::pair<void*, size_t>> cached;
     std::mutex stage_mu;
 };
 
@@ -103,6 +107,8 @@ namespace sfh {
 // primary and escape-time calls be released first (callers holding stage_mu pass false).
 sf_status ctx_alloc(sf_context* c, size_t bytes, void** p, bool trim = true);
 void ctx_free(sf_context* c, void* p, size_t bytes);
+// Frees an idle block into the context's cache of session arenas (at most four).
+void ctx_free_cached(sf_context* c, void* p, size_t bytes);
 void ctx_retain(sf_context* c);
 void ctx_release(sf_context* c);
 void graph_retain(sf_graph* g);
@@ -259,7 +265,7 @@ struct sf_session {
     size_t mem_bytes = 0;
     std::vector<sf_tile> tiles;
     uint32_t tile_size = 0, dispatches = 0;
-    uint32_t min_blocks = 3, quantum = 0, regen = 4;
+    uint32_t min_blocks = 7, quantum = 0, regen = 4;  // 7 blocks of 128 threads per SM
     uint32_t status_host = 0;
     double ms_per_path = 0.0;  // measured device cost of a path, for step() pacing
     bool window = false;       // tiled export: a tile-sized film whose origin the export sets

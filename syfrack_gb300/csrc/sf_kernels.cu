@@ -174,7 +174,7 @@ __global__ void __launch_bounds__(256) k_generate(const DevScene* __restrict__ s
 // atomic per warp and list.
 // FEAT: the surface features the kernel is built with (SF_FEAT_*; 0 for plain scenes).
 template <int FEAT>
-__global__ void __launch_bounds__(256) k_shade(const DevScene* __restrict__ scene_g, PathSoA soa, RoundQueues q,
+__global__ void __launch_bounds__(128, 5) k_shade(const DevScene* __restrict__ scene_g, PathSoA soa, RoundQueues q,
                                                DispatchGeom g, FilmPlanes film, uint32_t* status, int final_round) {
     __shared__ DevScene S;
     stage_pod(S, scene_g);
@@ -703,10 +703,10 @@ cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene
 }
 cudaError_t sf_launch_shade(const DevScene* scene, uint32_t rich, PathSoA soa, RoundQueues q, DispatchGeom g,
                             FilmPlanes film, uint32_t* status, int final_round, cudaStream_t st) {
-    const dim3 grid = grid_for(g.paths, 256, 16);
-    if (rich & SF_RICH_TEXTURE) k_shade<3><<<grid, 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
-    else if (rich) k_shade<1><<<grid, 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
-    else k_shade<0><<<grid, 256, 0, st>>>(scene, soa, q, g, film, status, final_round);
+    const dim3 grid = grid_for(g.paths, 128, 32);
+    if (rich & SF_RICH_TEXTURE) k_shade<3><<<grid, 128, 0, st>>>(scene, soa, q, g, film, status, final_round);
+    else if (rich) k_shade<1><<<grid, 128, 0, st>>>(scene, soa, q, g, film, status, final_round);
+    else k_shade<0><<<grid, 128, 0, st>>>(scene, soa, q, g, film, status, final_round);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st) {

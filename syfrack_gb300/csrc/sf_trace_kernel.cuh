@@ -384,12 +384,16 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
 template <int FORM>
 static cudaError_t launch_trace_form(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
                                      unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
-    if (tl.optics) {
-        k_trace<FORM, 2, false, false, true><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats);
+    if (tl.optics) {  // 6 blocks of 128 threads per SM (the host sizes the grid)
+        k_trace<FORM, 6, false, false, true, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats);
         return cudaGetLastError();
     }
     if (tl.lane_stats && min_blocks == 3) {
         k_trace<FORM, 3, false, true><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats);
+        return cudaGetLastError();
+    }
+    if (tl.lane_stats && min_blocks == 7) {
+        k_trace<FORM, 7, false, true, false, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats);
         return cudaGetLastError();
     }
     switch (min_blocks) {

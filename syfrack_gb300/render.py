@@ -247,9 +247,10 @@ class RenderSession:
         except Exception:
             pass
 
-    def set_launch(self, min_blocks_per_sm: int = 3, quantum: int = 0, regen: int = 4):
-        """Trace-kernel shape: resident blocks per SM (register budget), step quantum,
-        regeneration threshold (idle lanes a warp waits for before taking new segments)."""
+    def set_launch(self, min_blocks_per_sm: int = 7, quantum: int = 0, regen: int = 4):
+        """Trace-kernel shape: resident blocks per SM (2-4 of 256 threads, or 6-7 of 128),
+        step quantum, regeneration threshold (idle lanes a warp waits for before taking
+        new segments)."""
         check(self.ctx.lib.sf_session_set_launch(self.h, min_blocks_per_sm, quantum, regen))
 
     def dispatch(self, tile, samples: int):

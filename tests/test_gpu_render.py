@@ -45,7 +45,7 @@ def test_wavefront_equals_megakernel(renderer):
     assert a.color[..., :3].mean() > 0.01  # the light reaches the form
 
 
-@pytest.mark.parametrize("shape", [(2, 16, 1), (4, 64, 8), (3, 256, 32)])
+@pytest.mark.parametrize("shape", [(2, 16, 1), (4, 64, 8), (3, 256, 32), (7, 0, 4), (6, 128, 8)])
 def test_launch_shapes_give_the_same_film(renderer, shape):
     # march state saved at a step quantum and resumed by the next launch, any
     # regeneration threshold and any register budget: the same film bit for bit
