@@ -25,6 +25,8 @@ __global__ void __launch_bounds__(256) k_generate_batch(BatchTable bt, PathSoA s
     generate_path(*job.scene, soa, job.geom, path - job.path_begin, path);
 }
 
+// FEAT: the surface features the kernel is built with (SF_FEAT_*; 0 when no job has any).
+template <int FEAT>
 __global__ void __launch_bounds__(256) k_shade_batch(BatchTable bt, PathSoA soa, RoundQueues q, uint32_t* status,
                                                      int final_round) {
     __shared__ uint32_t begins[SF_BATCH_MAX_JOBS];
@@ -33,8 +35,8 @@ __global__ void __launch_bounds__(256) k_shade_batch(BatchTable bt, PathSoA soa,
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
         uint32_t path = q.active ? q.active[j] : j;
         const BatchJob& job = bt.jobs[find_job(begins, bt.n_jobs, path)];
-        uint32_t nf = shade_path(*job.scene, soa, job.geom, job.film, path - job.path_begin, path, status,
-                                 final_round);
+        uint32_t nf = shade_path<FEAT>(*job.scene, soa, job.geom, job.film, path - job.path_begin, path, status,
+                                       final_round);
         if (!final_round) enqueue_next(q, soa, nf, path);
     }
 }
@@ -60,11 +62,14 @@ cudaError_t sf_launch_generate_batch(BatchTable bt, PathSoA soa, uint32_t* count
     k_generate_batch<<<blocks_for(bt.total_paths), 256, 0, st>>>(bt, soa, counts);
     return cudaGetLastError();
 }
-cudaError_t sf_launch_shade_batch(BatchTable bt, PathSoA soa, RoundQueues q, uint32_t* status, int final_round,
-                                  cudaStream_t st) {
+cudaError_t sf_launch_shade_batch(BatchTable bt, uint32_t rich, PathSoA soa, RoundQueues q, uint32_t* status,
+                                  int final_round, cudaStream_t st) {
     unsigned cap = (unsigned)sf_device_sm_count() * 16u;
     unsigned b = blocks_for(bt.total_paths);
-    k_shade_batch<<<b < cap ? b : cap, 256, 0, st>>>(bt, soa, q, status, final_round);
+    b = b < cap ? b : cap;
+    if (rich & SF_RICH_TEXTURE) k_shade_batch<3><<<b, 256, 0, st>>>(bt, soa, q, status, final_round);
+    else if (rich) k_shade_batch<1><<<b, 256, 0, st>>>(bt, soa, q, status, final_round);
+    else k_shade_batch<0><<<b, 256, 0, st>>>(bt, soa, q, status, final_round);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_commit_batch(BatchTable bt, PathSoA soa, cudaStream_t st) {
@@ -79,6 +84,10 @@ cudaError_t sf_launch_advance_batch(BatchTable bt, cudaStream_t st) {
 template <int FORM>
 static cudaError_t launch_trace_batch_form(BatchTable bt, PathSoA soa, TraceLaunch tl, unsigned long long* stats,
                                            int blocks, int min_blocks, cudaStream_t st) {
+    if (tl.optics) {  // a job with dielectric materials: the optics instantiation, 2 blocks per SM
+        k_trace<FORM, 2, true, false, true><<<blocks, 256, 0, st>>>(nullptr, nullptr, soa, tl, stats, bt);
+        return cudaGetLastError();
+    }
     switch (min_blocks) {
     case 3: k_trace<FORM, 3, true><<<blocks, 256, 0, st>>>(nullptr, nullptr, soa, tl, stats, bt); break;
     case 4: k_trace<FORM, 4, true><<<blocks, 256, 0, st>>>(nullptr, nullptr, soa, tl, stats, bt); break;

@@ -84,10 +84,13 @@ sf_status wave_record_pass(sf_context* c, const WaveArena& a, cudaStream_t st, b
             tl.quantum = j + 1 == Q ? 0u : a.quantum;
             tl.regen = a.regen;
             LaunchTimer t(c, true, timed, st);
-            CU(sf_launch_trace_batch(a.bt, a.soa, tl, c->d_stats, blocks, int(a.min_blocks), a.any_generic ? 1 : 0, st));
+            tl.optics = (a.rich & SF_RICH_OPTICS) ? 1u : 0u;
+            // the optics trace kernel runs two blocks of 256 threads per SM
+            CU(sf_launch_trace_batch(a.bt, a.soa, tl, c->d_stats, tl.optics ? 2 * c->sm_count : blocks,
+                                     int(a.min_blocks), a.any_generic ? 1 : 0, st));
         }
         LaunchTimer t(c, false, timed, st);
-        CU(sf_launch_shade_batch(a.bt, a.soa, q, a.status, r + 1 == R ? 1 : 0, st));
+        CU(sf_launch_shade_batch(a.bt, a.rich, a.soa, q, a.status, r + 1 == R ? 1 : 0, st));
     }
     {
         LaunchTimer t(c, false, timed, st);
@@ -135,8 +138,7 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
         sf_status st = validate_config(jobs[i].cfg);
         if (st != SF_OK) return st;
         if (const sf_status sc = scene_check(jobs[i].scene); sc != SF_OK) return sc;
-        if (rich_of(jobs[i].scene))
-            return fail(SF_ERR_UNSUPPORTED, "finish details, textures and optics render through sessions, not batches");
+
         const sf_render_config& cf = jobs[i].cfg;
         uint32_t spd = std::max<uint32_t>(std::min(cf.samples_per_dispatch ? cf.samples_per_dispatch : cf.samples_per_pixel,
                                                    cf.samples_per_pixel), 1);
@@ -144,7 +146,7 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
         pixels += uint64_t(cf.width) * cf.height;
         // accum | aux | depth, and for fog scenes volume | moments | surface
         film_bytes += ((uint64_t(cf.width) * cf.height * (has_fog(jobs[i].scene) ? 84 : 36) + 255) & ~uint64_t(255));
-        rounds = std::max(rounds, cf.max_bounces + 2);
+        rounds = std::max(rounds, rounds_of(cf, jobs[i].scene));
         max_steps = std::max(max_steps, cf.max_steps);
         generic |= jobs[i].graph->prog.form == SF_FORM_GENERIC;
     }
@@ -157,13 +159,18 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     size_t extra = 0;
     uint32_t K = 1;  // the most shadow segments one bounce of any job issues
     bool any_fog = false;
+    uint32_t rich = 0;
     for (uint32_t i = 0; i < n; ++i) {
         K = std::max(K, shadow_slots_of(jobs[i].scene));
         any_fog |= has_fog(jobs[i].scene);
+        rich |= rich_of(jobs[i].scene);
     }
-    // a fog job keeps the volume layer split: every path gets a volume row
+    // a fog job keeps the volume layer split: every path gets a volume row; finish
+    // details, textures and optics keep the footprint and medium row
     const size_t pv_bytes = any_fog ? size_t(paths) * 16 : 0;
-    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, K, scene_bytes + pv_bytes + film_bytes, &extra);
+    const size_t ex_bytes = rich ? size_t(paths) * 16 : 0;
+    sf_status st = arena_alloc(c, b->a, uint32_t(paths), n, rounds, K,
+                               scene_bytes + pv_bytes + ex_bytes + film_bytes, &extra);
     if (st != SF_OK) { delete b; return st; }
     b->a.max_steps = max_steps;
     b->a.any_generic = generic;
@@ -174,7 +181,9 @@ extern "C" sf_status sf_batch_create(sf_context* c, const sf_batch_job* jobs, ui
     DevScene* d_scenes = reinterpret_cast<DevScene*>(base);
     std::vector<DevScene> scenes(n);
     if (any_fog) b->a.soa.pv = reinterpret_cast<float4*>(base + scene_bytes);
-    char* film = base + scene_bytes + pv_bytes;
+    if (rich) b->a.soa.ex = reinterpret_cast<float4*>(base + scene_bytes + pv_bytes);
+    b->a.rich = rich;
+    char* film = base + scene_bytes + pv_bytes + ex_bytes;
     uint32_t pbeg = 0, xbeg = 0;
     for (uint32_t i = 0; i < n; ++i) {
         const sf_render_config& cf = jobs[i].cfg;

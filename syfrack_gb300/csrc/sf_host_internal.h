@@ -237,6 +237,7 @@ struct WaveArena {
     void* mem = nullptr;
     size_t mem_bytes = 0;
     bool any_generic = false;
+    uint32_t rich = 0;  // SF_RICH_* of any job: the shading and trace kernels' features
     uint32_t min_blocks = 3, quantum = 128, regen = 4;
 };
 

@@ -169,7 +169,7 @@ cudaError_t sf_launch_trace_any(const DeProgram*, const DevScene*, PathSoA, Trac
 cudaError_t sf_launch_generate_batch(BatchTable bt, PathSoA soa, uint32_t* counts, cudaStream_t st);
 cudaError_t sf_launch_trace_batch(BatchTable bt, PathSoA soa, TraceLaunch tl, unsigned long long* stats, int blocks,
                                   int min_blocks, int any_generic, cudaStream_t st);
-cudaError_t sf_launch_shade_batch(BatchTable bt, PathSoA soa, RoundQueues q, uint32_t* status, int final_round,
+cudaError_t sf_launch_shade_batch(BatchTable bt, uint32_t rich, PathSoA soa, RoundQueues q, uint32_t* status, int final_round,
                                   cudaStream_t st);
 cudaError_t sf_launch_commit_batch(BatchTable bt, PathSoA soa, cudaStream_t st);
 cudaError_t sf_launch_advance_batch(BatchTable bt, cudaStream_t st);

@@ -48,7 +48,7 @@ static __device__ __forceinline__ uint32_t find_job(const uint32_t* begins, uint
 // program and scene (L1-cached global memory) when it takes an item.
 // LANE_STATS: also count warp-level DE calls and, per call, the warp's longest
 // iteration count times its active lanes (a diagnostic of SIMT lane use).
-// OPTICS (single job, scenes with dielectric materials): a path's first segment
+// OPTICS (scenes with dielectric materials): a path's first segment
 // samples the field at its origin for the medium it starts in (pathtrace.wgsl:833-840);
 // a hit on a material with optics is refined by Newton steps on the exact field
 // (optical_refine_hit, optics.wgsl:7-23) and, for a continuation, its normal taken at
@@ -143,7 +143,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
     // OPTICS: a march that found a surface with sample s (at m.t): refine it when its
     // material has optics, else end a shadow segment or record a continuation's hit.
     auto on_hit = [&](const DeRaw& s) {
-        if (OPTICS && optics_enabled(material_optics(S, s.material))) {
+        if (OPTICS && optics_enabled(material_optics(*Sl, s.material))) {
             hstep = fmaxf(1e-5f, fminf(1e-3f, m.t * 1e-5f));  // the Newton step's difference
             tap = 0;                                           // iteration * 3 + tap of the step
             state = TL_REFINE;
@@ -228,7 +228,9 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
             // the single-job kernel reads the program from shared memory by name (LDS)
             DeRaw s;
             const bool exact_state = OPTICS && (state == TL_INIT || state == TL_REFINE || state == TL_FINAL);
-            if constexpr (MULTI) s = de_form<FORM>(*Pl, q);
+            if constexpr (MULTI && FORM == SF_FORM_ANY && OPTICS)
+                s = exact_state ? de_raw_exact(*Pl, q) : de_form<FORM>(*Pl, q);
+            else if constexpr (MULTI) s = de_form<FORM>(*Pl, q);
             else if constexpr (FORM == SF_FORM_ANY && OPTICS) s = exact_state ? de_raw_exact(P, q) : de_form<FORM>(P, q);
             else s = de_form<FORM>(P, q);
             n_eval++;
@@ -268,7 +270,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
                 else surface_hit(s);
             } else if (OPTICS && state == TL_INIT) {
                 // the medium the path starts in, then its first march
-                const DevOptics& o = material_optics(S, s.material);
+                const DevOptics& o = material_optics(*Sl, s.material);
                 const bool solid = s.d < 0.0f && optics_enabled(o) && o.surface[1] > 0.0f && o.surface[3] == 0.0f;
                 soa.ex[path].z = __uint_as_float(s.material | (solid ? SF_EX_SOLID : 0u));
                 start();
@@ -292,10 +294,10 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
                     }
                 }
             } else if (OPTICS && state == TL_FINAL) {
-                const DevOptics& o = material_optics(S, s.material);
+                const DevOptics& o = material_optics(*Sl, s.material);
                 if (!shadow) {
                     // the refined hit, its sample and the normal taps (1e-4 on a dielectric)
-                    const DeSampleF smp = de_finalize(P, s);
+                    const DeSampleF smp = de_finalize(*Pl, s);
                     soa.hit[path] = make_uint4(__float_as_uint(m.t), m.i, SF_NO_LIGHT, SF_HF_HIT);
                     soa.hit_tr[path] = make_float4(smp.traps[0], smp.traps[1], smp.traps[2], smp.traps[3]);
                     hit_w = smp.iter | (smp.material << 16);
@@ -329,7 +331,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
                         soa.sh_o[item] = make_float4(origin.x, origin.y, origin.z, remaining);
                         soa.sh_d[item] = sd;
                         soa.sh_c[item] = sc;
-                        const float te = nearest_emitter(S, origin, m.rd, remaining, li);
+                        const float te = nearest_emitter(*Sl, origin, m.rd, remaining, li);
                         march_begin(m, origin, m.rd, te);
                         start();
                     }

@@ -474,10 +474,13 @@ class Batch:
         self.ctx = renderer.ctx
         self.jobs = list(jobs)
         self._graphs = [renderer.compile(sc.graph) for sc, _ in self.jobs]
+        # textured jobs: their texture graphs, compiled and kept alive with the batch
+        self._tex = [renderer.compile(sc.material.texture.graph) if sc.material.texture else None
+                     for sc, _ in self.jobs]
         arr = (sf_batch_job * len(self.jobs))()
         for i, (sc, cfg) in enumerate(self.jobs):
             arr[i].graph = self._graphs[i].h
-            arr[i].scene = sc.desc(cfg.width, cfg.height)
+            arr[i].scene = sc.desc(cfg.width, cfg.height, self._tex[i].h.value if self._tex[i] else None)
             arr[i].cfg = cfg.desc()
         h = C.c_void_p()
         check(self.ctx.lib.sf_batch_create(self.ctx.h, arr, len(self.jobs), C.byref(h)))
