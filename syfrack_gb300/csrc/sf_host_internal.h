@@ -181,7 +181,7 @@ inline uint32_t rounds_of(const sf_render_config& c, const sf_scene_desc& d) {
 // round lists (active, continuation, K*N shadow rows) in two parities, and two
 // resume lists of (1 + K) * N items.
 inline size_t wave_soa_bytes(size_t N, uint32_t K) { return N * 16 * 8 + size_t(K) * N * (16 * 3 + 4); }
-inline size_t wave_march_bytes(size_t N, uint32_t K) { return (1 + size_t(K)) * N * (16 + 16 + 4 + 4); }
+inline size_t wave_march_bytes(size_t N, uint32_t K) { return (1 + size_t(K)) * N * (16 + 16 + 4); }
 inline size_t wave_lists_bytes(size_t N, uint32_t K) { return 2 * (2 + size_t(K)) * N * 4; }
 inline size_t wave_resume_bytes(size_t N, uint32_t K) { return 2 * (1 + size_t(K)) * N * 4; }
 inline void wave_bind(PathSoA& soa, void* soa_mem, void* march_mem, uint32_t N, uint32_t K) {
@@ -203,7 +203,6 @@ inline void wave_bind(PathSoA& soa, void* soa_mem, void* march_mem, uint32_t N, 
     soa.m0 = m;
     soa.m1 = m + rows;
     soa.m2 = reinterpret_cast<uint32_t*>(m + 2 * rows);
-    soa.te = reinterpret_cast<float*>(soa.m2 + rows);
     soa.capacity = N;
     soa.shadow_slots = K;
 }

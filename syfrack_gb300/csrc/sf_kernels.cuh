@@ -37,13 +37,11 @@ struct PathSoA {
     float4* hit_n;   // normal, w = bits(iterations | material << 16)
     uint32_t* vis;   // shadow visibility (1 = clear)
     float4* Ls;      // per-path final radiance (committed in ascending sample order)
-    // march state by row: continuation rows [0, capacity), shadow rows capacity +
-    // [0, K * capacity). A fresh segment is its end and the light ahead of it (te, m2);
-    // a segment cut at the step quantum also saves the rest of its march (m0, m1).
+    // resumable march state of a segment cut at the step quantum: continuation rows
+    // [0, capacity), shadow rows capacity + [0, K * capacity)
     float4* m0;      // t, omega, prev_radius, step_len
     float4* m1;      // t_end, cand_t, cand_err, bits(steps)
     uint32_t* m2;    // light index ahead of the segment
-    float* te;       // a fresh segment's end (the nearest emitter's distance or its t_end)
     // fog scenes only (null otherwise): primary volume xyz, w = bits(volume tags of the
     // pending shadow slots | the camera segment scattered << 8); the sample's volume
     // part once the path ends

@@ -63,14 +63,16 @@ static __device__ __forceinline__ uint32_t load_path(const PathSoA& soa, uint32_
     return flags;
 }
 
-// A segment's start: the nearest emitter on the ray (lights.wgsl:183-209) bounds it;
-// its end and that light's index are written to the path's continuation row (row =
-// path) or shadow row (row = path + capacity) by the stage that creates the ray, and
-// the trace kernel starts the march from them (march_begin's other fields are constants).
+// A segment's march state at its start -- the nearest emitter on the ray
+// (lights.wgsl:183-209) bounds it, then march_begin's fields -- written to the path's
+// continuation row (row = path) or shadow row (row = path + capacity) by the stage
+// that creates the ray, so the trace kernel only loads it.
 static __device__ __forceinline__ void begin_segment(const DevScene& S, PathSoA& soa, uint32_t row, float3 ro,
                                                      float3 rd, float t_end) {
     uint32_t li;
-    soa.te[row] = nearest_emitter(S, ro, rd, t_end, li);
+    const float te = nearest_emitter(S, ro, rd, t_end, li);
+    soa.m0[row] = make_float4(0.0f, 1.2f, 0.0f, 0.0f);    // t, omega, previous radius, step
+    soa.m1[row] = make_float4(te, 0.0f, 1e30f, 0.0f);     // t_end, candidate t, candidate error, steps (0)
     soa.m2[row] = li;
 }
 

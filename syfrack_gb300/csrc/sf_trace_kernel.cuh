@@ -205,18 +205,14 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
                     }
                     float4 o = shadow ? soa.sh_o[item] : soa.o[path];
                     float4 d = shadow ? soa.sh_d[item] : soa.d[path];
-                    // the march state: a fresh segment's end from the stage that made the
-                    // ray, or the whole state saved by the previous launch at its quantum
+                    // the march state: set by the stage that made the ray, or saved by the
+                    // previous launch at its step quantum
                     const uint32_t row = shadow ? cap + item : item;
-                    if (first) {
-                        march_begin(m, mk3(o.x, o.y, o.z), mk3(d.x, d.y, d.z), soa.te[row]);
-                    } else {
-                        const float4 a = soa.m0[row], b = soa.m1[row];
-                        m.ro = mk3(o.x, o.y, o.z);
-                        m.rd = mk3(d.x, d.y, d.z);
-                        m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
-                        m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
-                    }
+                    const float4 a = soa.m0[row], b = soa.m1[row];
+                    m.ro = mk3(o.x, o.y, o.z);
+                    m.rd = mk3(d.x, d.y, d.z);
+                    m.t = a.x; m.omega = a.y; m.prev_radius = a.z; m.step_len = a.w;
+                    m.t_end = b.x; m.cand_t = b.y; m.cand_err = b.z; m.i = __float_as_uint(b.w);
                     li = soa.m2[row];
                     budget = quantum;
                     if (OPTICS && !shadow && first &&
