@@ -138,6 +138,8 @@ struct ServeFilm {
     sf_graph* graph = nullptr;
     uint32_t samples = 0;  // samples once every scheduled pass has finished
     uint32_t max_bounces = 0, max_steps = 0;
+    uint32_t rounds = 0;   // wavefront rounds of a pass (rounds_of)
+    uint32_t rich = 0;     // SF_RICH_* of the scene: finish details, a texture, optics
     bool busy = false;     // written by a batch in flight
     int refs = 0;          // the preview until released, plus each refinement until it ends
 };
@@ -316,7 +318,7 @@ sf_status launch_wave(sf_server* s, ServeSlot& sl) {
     WaveArena& a = sl.arena;
     BatchJob* hj = reinterpret_cast<BatchJob*>(sl.stage + stage_jobs_off(s));
     DevScene* hs = reinterpret_cast<DevScene*>(sl.stage + stage_scenes_off(s));
-    uint32_t paths = 0, pixels = 0, rounds = 0, steps = 0, n_scenes = 0;
+    uint32_t paths = 0, pixels = 0, rounds = 0, steps = 0, n_scenes = 0, rich = 0;
     for (size_t i = 0; i < sl.reqs.size(); ++i) {
         ServeReq* r = sl.reqs[i];
         ServeFilm* f = r->film;
@@ -332,8 +334,9 @@ sf_status launch_wave(sf_server* s, ServeSlot& sl) {
         hj[i] = j;
         paths += px * r->samples;
         pixels += px;
-        rounds = std::max(rounds, f->max_bounces + 2);
+        rounds = std::max(rounds, f->rounds);
         steps = std::max(steps, f->max_steps);
+        rich |= f->rich;
         if (r->kind == SF_REQ_PREVIEW) {
             hs[n_scenes] = r->scene;
             CU(cudaMemcpyAsync(f->scene, hs + n_scenes, sizeof(DevScene), cudaMemcpyHostToDevice, st));
@@ -353,6 +356,10 @@ sf_status launch_wave(sf_server* s, ServeSlot& sl) {
     // rounds vary per batch; the arena's queue counters are sized for its largest
     WaveArena pass = a;
     pass.rounds = rounds;
+    // scenes with finish details, a texture or optics: the feature-built kernels and the
+    // footprint and medium rows (kept by the slot, unused by plain batches)
+    pass.rich = rich;
+    if (!rich) pass.soa.ex = nullptr;
     uint64_t before = s->ctx->launches;
     sf_status rs = wave_record_pass(s->ctx, pass, st, false);
     s->stats.launches += s->ctx->launches - before;
@@ -427,7 +434,7 @@ bool serve_admit(sf_server* s, ServeSlot& sl) {
             r->film->samples += r->samples;
             r->film->busy = true;
             paths += px * r->samples;
-            rounds = std::max(rounds, r->film->max_bounces + 2);
+            rounds = std::max(rounds, r->film->rounds);
             r->work = px * r->samples;
         } else {
             r->work = px;
@@ -571,7 +578,8 @@ extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg
     int lo_prio = 0, hi_prio = 0;
     cudaDeviceGetStreamPriorityRange(&lo_prio, &hi_prio);
     s->slots.resize(k.slots);
-    const uint32_t max_rounds = 32 + 2;  // bounces <= 32 (validate_config)
+    // bounces <= 32 (validate_config), and the 33 rounds of an optics scene's null events
+    const uint32_t max_rounds = 32 + 2 + 33;
     for (auto& sl : s->slots) {
         sl.stage_bytes = stage_status_off(s) + 256;
         e = cudaStreamCreateWithPriority(&sl.hi, cudaStreamNonBlocking, hi_prio);
@@ -580,8 +588,11 @@ extern "C" sf_status sf_server_create(sf_context* c, const sf_server_config* cfg
         if (e == cudaSuccess)
             e = cudaHostAlloc(reinterpret_cast<void**>(&sl.stage), sl.stage_bytes, cudaHostAllocDefault);
         if (e != cudaSuccess) return bail(cuda_fail(e, "server slot"));
-        sf_status st = arena_alloc(c, sl.arena, k.path_capacity, k.max_jobs, max_rounds, kServeShadowSlots, 0, nullptr);
+        size_t ex_off = 0;
+        sf_status st = arena_alloc(c, sl.arena, k.path_capacity, k.max_jobs, max_rounds, kServeShadowSlots,
+                                   size_t(k.path_capacity) * 16, &ex_off);
         if (st != SF_OK) return bail(st);
+        sl.arena.soa.ex = reinterpret_cast<float4*>(static_cast<char*>(sl.arena.mem) + ex_off);
         sl.arena.min_blocks = k.min_blocks;
         sl.arena.quantum = k.quantum;
         sl.arena.regen = k.regen;
@@ -602,8 +613,6 @@ extern "C" sf_status sf_serve_submit(sf_server* s, const sf_request* q, uint64_t
         sf_status st = validate_config(q->cfg);
         if (st != SF_OK) return st;
         if (const sf_status sc = scene_check(q->scene); sc != SF_OK) return sc;
-        if (rich_of(q->scene))
-            return fail(SF_ERR_UNSUPPORTED, "finish details, textures and optics render through sessions, not the server");
         if (has_hdri(q->scene)) return fail(SF_ERR_UNSUPPORTED, "HDRI panoramas are rendered by sessions, not served");
         if (shadow_slots_of(q->scene) > kServeShadowSlots)
             return fail(SF_ERR_UNSUPPORTED, "the server's arenas hold 3 shadow segments per bounce");
@@ -671,6 +680,8 @@ extern "C" sf_status sf_serve_submit(sf_server* s, const sf_request* q, uint64_t
         graph_retain(q->graph);
         f->max_bounces = q->cfg.max_bounces;
         f->max_steps = q->cfg.max_steps;
+        f->rounds = rounds_of(q->cfg, q->scene);
+        f->rich = rich_of(q->scene);
         f->refs = 1;
         r->film = f;
     }

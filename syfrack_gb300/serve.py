@@ -87,9 +87,11 @@ class Server:
         """Queues the first pass of a view: cfg.samples_per_pixel samples into a new
         device film. Returns the ticket."""
         g = self.renderer.compile(scene.graph)  # the film holds its own reference
+        # a textured scene's texture graph: compiled and kept by the renderer's cache
+        tex = self.renderer.compile(scene.material.texture.graph) if scene.material.texture else None
         r = sf_request(kind=PREVIEW)
         r.graph = g.h
-        r.scene = scene.desc(cfg.width, cfg.height)
+        r.scene = scene.desc(cfg.width, cfg.height, tex.h.value if tex else None)
         r.cfg = cfg.desc()
         return self._submit(r)
 

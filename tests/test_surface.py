@@ -434,16 +434,42 @@ def test_surface_feature_jobs_in_a_batch_equal_their_sessions(renderer):
 
 
 @pytest.mark.gpu
-def test_surface_features_stay_out_of_the_server_and_checkpoints(renderer, tmp_path):
-    """The server renders the plain surfaces; textured scenes are not checkpointed
-    (their texture graph is a caller object)."""
-    from syfrack_gb300 import RenderSession, Server
+def test_surface_feature_previews_served_equal_their_sessions(renderer):
+    """A detailed, a textured and a glass preview, each with a refinement, served
+    together: every film equals the same samples rendered by a session (the server's
+    batched kernels, the session's per-form ones)."""
+    from syfrack_gb300 import Server
+    from syfrack_gb300.serve import DONE
+
+    scenes = [detail_scene("Sand"), textured_scene(bump=0.3), glass_sphere_scene()]
+    cfg = RenderConfig(48, 32, 2, max_bounces=3, max_steps=256, pixel_tolerance=1.0, tile_size=48,
+                       samples_per_dispatch=2, integrator="wavefront")
+    srv = Server(renderer, hbm_budget=1 << 30, path_capacity=1 << 16)
+    previews = [srv.preview(sc, cfg) for sc in scenes]
+    refines = [srv.refine(t, 2) for t in previews]
+    for t in previews:
+        assert srv.wait(t).state == DONE
+    results = [srv.wait(t) for t in refines]
+    for i, (sc, r) in enumerate(zip(scenes, results)):
+        assert r.state == DONE and r.status == 0, i
+        ref = render(renderer, sc, RenderConfig(**{**cfg.__dict__, "samples_per_pixel": 4}))
+        if i == 2:  # the glass refractions amplify last-ulp differences between the kernels
+            got = r.accum[..., :3] / np.maximum(r.accum[..., 3:], 1)
+            assert float(np.sqrt(np.mean((got - ref.color[..., :3]) ** 2))) < 1e-2
+        else:
+            scale = max(1.0, float(np.abs(ref.accum[..., :3]).max()))
+            assert np.abs(r.accum[..., :3] - ref.accum[..., :3]).max() <= 1e-4 * scale, i
+    for t in previews + refines:
+        srv.release(t)
+    srv.close()
+
+
+@pytest.mark.gpu
+def test_textured_scenes_are_not_checkpointed(renderer, tmp_path):
+    """The texture graph is a caller object (like a panorama): no checkpoint."""
+    from syfrack_gb300 import RenderSession
 
     cfg = RenderConfig(32, 32, 4, max_bounces=1, integrator="wavefront")
-    srv = Server(renderer, hbm_budget=1 << 30, slots=1)
-    with pytest.raises(SyfrackError, match="SF_ERR_UNSUPPORTED"):
-        srv.preview(detail_scene("Patina"), RenderConfig(32, 32, 1, max_bounces=1, integrator="wavefront"))
-    srv.close()
     s = RenderSession(renderer, textured_scene(), cfg)
     s.step(0)
     with pytest.raises(SyfrackError, match="SF_ERR_UNSUPPORTED"):
