@@ -139,6 +139,11 @@ typedef struct sf_graph_info {
     uint32_t form;               /* SF_FORM_*: specialised device code path */
     uint32_t op_count;           /* length of the lowered device program */
     float bounding_radius_hint;
+    /* ABI 1.4: the leaves of the exact union branch-and-bound (graph_wgsl.rs:1112-1154)
+     * when the Output's input is a union over 2 to 32 leaves and the graph has a
+     * skippable Bounded or Instances node, else 0. sf_de_probe and the preview search
+     * unions of three or more leaves; every kernel's sample is the whole program's. */
+    uint32_t exact_union_leaves;
 } sf_graph_info;
 enum { SF_FORM_GENERIC = 0, SF_FORM_BULB = 1, SF_FORM_BOX = 2, SF_FORM_MENGER = 3 };
 

@@ -61,7 +61,9 @@ class sf_de_sample(C.Structure):
 class sf_graph_info(C.Structure):
     _fields_ = [("step_scale", C.c_float), ("lipschitz", C.c_float), ("trap_scales", C.c_float * 4),
                 ("iteration_product", C.c_uint32), ("form", C.c_uint32), ("op_count", C.c_uint32),
-                ("bounding_radius_hint", C.c_float)]
+                ("bounding_radius_hint", C.c_float),
+                # ABI 1.4
+                ("exact_union_leaves", C.c_uint32)]
 
 
 class sf_camera(C.Structure):

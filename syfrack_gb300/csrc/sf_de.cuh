@@ -685,10 +685,21 @@ __device__ __forceinline__ bool inst_next(InstFrame& F) {
     return false;
 }
 
-// Postfix interpreter over DeProgram.ops (generic graphs). exact = false is the
-// reference's de_sample (skippable Bounded branches skipped outside their margin,
-// the sample flagged); exact = true is de_sample_exact (every branch evaluated).
-static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bool exact) {
+// Evaluation modes of the generic interpreter.
+enum : uint32_t {
+    SF_EVAL_FAST = 0,   // de_sample: skippable branches skipped outside their margin, the sample flagged
+    SF_EVAL_EXACT = 1,  // de_sample_exact: every branch evaluated
+    // the union probe (graph_wgsl.rs:1124-1136, bounds_only): every skippable Bounded
+    // pushes its bound and every skippable Instances its root fence, flagged, whatever
+    // the margin; a sample without the flag took no skip and is exact
+    SF_EVAL_PROBE = 2
+};
+
+// Postfix interpreter over the ops [pc0, pc1) of DeProgram.ops (generic graphs) in
+// one of the SF_EVAL_* modes; the whole program is [0, n_ops). Inlined into the two
+// entry points below, so the whole-program one keeps its constant range and modes.
+__device__ __forceinline__ DeRaw de_run(const DeProgram& P, float3 c, uint32_t mode, uint32_t pc0, uint32_t pc1) {
+    const bool exact = mode == SF_EVAL_EXACT, probe = mode == SF_EVAL_PROBE;
     // the copy searches in flight, one per nesting level (eval.rs:808 recurses into the
     // template of each copy; here the template's ops run between INST_BEGIN and INST_END)
     InstFrame frames[SF_MAX_INST_DEPTH];
@@ -703,8 +714,7 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
     int sp = 0;
     float3 seed_p = c;
     float seed_dr = 1.0f;
-    const uint32_t n = P.n_ops;
-    for (uint32_t pc = 0; pc < n; ++pc) {
+    for (uint32_t pc = pc0; pc < pc1; ++pc) {
         const DeOp& op = P.ops[pc];
         switch (op.code) {
         case SF_OP_BEGIN:
@@ -750,7 +760,7 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
             if (sp >= SF_MAX_DIST_STACK) break;
             DeRaw b = raw_empty();
             b.d = box_fence(s.p, ld3(op.f), s.dr);
-            if (!exact && b.d > op.f[3]) {
+            if (!exact && (probe || b.d > op.f[3])) {
                 b.flags = 1;
                 stack[sp++] = b;
                 pc = op.b;  // past BOUND_END
@@ -773,7 +783,7 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
             if (F.skip) {
                 // empty space needs only the root fence (graph_wgsl.rs:769-771)
                 const float env = cluster_bound(F.bvh, c);
-                if (env > F.margin) {
+                if (probe || env > F.margin) {
                     DeRaw e = raw_empty();
                     e.d = env;
                     e.flags = 1;
@@ -838,6 +848,56 @@ static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bo
     }
     return sp > 0 ? stack[sp - 1] : raw_empty();
 }
+// The whole program: exact = false is the reference's de_sample (skippable Bounded
+// branches skipped outside their margin, the sample flagged); exact = true is
+// de_sample_exact (every branch evaluated).
+static __device__ __noinline__ DeRaw de_generic(const DeProgram& P, float3 c, bool exact) {
+    return de_run(P, c, exact ? SF_EVAL_EXACT : SF_EVAL_FAST, 0, P.n_ops);
+}
+// One union leaf's op range, probed or exact.
+static __device__ __noinline__ DeRaw de_generic_leaf(const DeProgram& P, float3 c, uint32_t mode, uint32_t leaf) {
+    return de_run(P, c, mode, P.leaf_begin[leaf], P.leaf_end[leaf]);
+}
+
+// The exact sample of a wide union by branch and bound (graph_wgsl.rs:1112-1154): every
+// leaf is probed for its conservative distance (a probe that took no skip is the
+// leaf's exact sample), then the unsettled leaf with the lowest bound is evaluated
+// exactly, lowest index first on ties, until no bound can reach the best. Skippable
+// bounds are lower bounds (a bound reached through a Subtraction's second input is
+// never skippable), so every leaf left out is strictly farther than the winner and the
+// result is the union's own: the nearest leaf, the first in depth-first order on ties
+// (a Union keeps its first input when a.d <= b.d). The search starts from the empty
+// state rather than the WGSL's 1e30 sentinel, so a union of empty leaves stays +inf
+// as the union itself does.
+static __device__ __noinline__ DeRaw de_union_exact(const DeProgram& P, float3 c) {
+    const uint32_t k = P.union_leaves;
+    float lower[SF_MAX_UNION_LEAVES];
+    uint32_t settled = 0;  // bit i: leaf i's exact sample is known
+    DeRaw best = raw_empty();
+    uint32_t winner = k;
+    for (uint32_t i = 0; i < k; ++i) {
+        const DeRaw s = de_generic_leaf(P, c, SF_EVAL_PROBE, i);
+        lower[i] = s.d;
+        if (s.flags == 0) {
+            settled |= 1u << i;
+            if (s.d < best.d || (s.d == best.d && i < winner)) { best = s; winner = i; }
+        }
+    }
+    for (uint32_t step = 0; step < k; ++step) {
+        uint32_t chosen = k;
+        float bound = SF_INF;
+        for (uint32_t i = 0; i < k; ++i)
+            if (!((settled >> i) & 1u) && (lower[i] < bound || (lower[i] == bound && i < chosen))) {
+                chosen = i;
+                bound = lower[i];
+            }
+        if (chosen == k || bound > best.d) break;
+        settled |= 1u << chosen;
+        const DeRaw s = de_generic_leaf(P, c, SF_EVAL_EXACT, chosen);
+        if (s.d < best.d || (s.d == best.d && chosen < winner)) { best = s; winner = chosen; }
+    }
+    return best;
+}
 
 // Entry point: raw DE at p for the program's form.
 __device__ __forceinline__ DeRaw de_raw(const DeProgram& P, float3 p) {
@@ -849,9 +909,23 @@ __device__ __forceinline__ DeRaw de_raw(const DeProgram& P, float3 p) {
     }
 }
 // de_sample_exact: the generic program with every Bounded branch evaluated; the
-// specialised forms have no bounds.
+// specialised forms have no bounds. The path tracers take this whole-program form:
+// their exact samples (normals, acceptance, refinement) are a small share of their
+// work, and the search's call would raise their register allocation.
 __device__ __forceinline__ DeRaw de_raw_exact(const DeProgram& P, float3 p) {
     if (P.form != SF_FORM_GENERIC) return de_raw(P, p);
+    return de_generic(P, p, true);
+}
+// The same sample, with a union of SF_UNION_SEARCH_MIN or more leaves searched by
+// branch and bound: for the kernels whose work is exact samples (the batched probe,
+// the preview's march on the exact field), where each one would otherwise evaluate
+// every leaf's detail. Two leaves are left to the whole program: their search saves at
+// most one leaf for two probes (a bounded Mandelbulb beside a sphere previews 25%
+// slower searched, while a nine-leaf union previews 28% faster).
+#define SF_UNION_SEARCH_MIN 3
+__device__ __forceinline__ DeRaw de_raw_exact_search(const DeProgram& P, float3 p) {
+    if (P.form != SF_FORM_GENERIC) return de_raw(P, p);
+    if (P.union_leaves >= SF_UNION_SEARCH_MIN) return de_union_exact(P, p);
     return de_generic(P, p, true);
 }
 // The march's sample (pathtrace.wgsl:100-106, lights.wgsl:234): a flagged sample

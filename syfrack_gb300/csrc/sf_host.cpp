@@ -50,7 +50,7 @@ constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
 constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
 // 1.1: sf_film_planes.color; 1.2: sf_render_config.hit_epsilon; 1.3: finish details, orbit
 // colouring, optics and textures in sf_scene_desc
-constexpr uint32_t ABI_VERSION = (1u << 16) | 3u;
+constexpr uint32_t ABI_VERSION = (1u << 16) | 4u;
 
 // ------------------------------------------------------------------ graph preparation
 
@@ -525,6 +525,34 @@ struct Lowerer {
         err = "point value wired into a distance port";
         return false;
     }
+    // The Output's input lowered as dist() lowers it, recording the op range of each
+    // leaf below its enabled Unions (union_leaves, graph_wgsl.rs:18-26: depth-first,
+    // first input first, a leaf reached twice kept once).
+    struct Leaf {
+        bool has;
+        uint32_t id, begin, end;
+    };
+    std::vector<Leaf> leaves;
+    bool union_tree(bool has_src, uint32_t src, int guard = 0) {
+        if (guard > 256) { err = "distance tree too deep"; return false; }
+        const sf_node* n = has_src ? g.node(src) : nullptr;
+        if (n && n->enabled && n->kind == SF_NODE_UNION) {
+            uint32_t a = 0, b = 0;
+            const bool ha = g.input_of(src, 0, &a), hb = g.input_of(src, 1, &b);
+            if (!union_tree(ha, a, guard + 1) || !union_tree(hb, b, guard + 1)) return false;
+            DeOp o = mk(SF_OP_COMBINE);
+            o.a = n->kind;
+            o.f[0] = n->f[0];
+            stack_depth--;
+            return push(o);
+        }
+        const uint32_t begin = P.n_ops;
+        if (!dist(has_src, src, guard)) return false;
+        const bool known = n && std::any_of(leaves.begin(), leaves.end(),
+                                            [&](const Leaf& l) { return l.has && l.id == src; });
+        if (!known) leaves.push_back({n != nullptr, src, begin, P.n_ops});
+        return true;
+    }
 };
 
 // Largest float x with sqrtf(x) <= b. sqrtf is correctly rounded and monotonic,
@@ -886,9 +914,23 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     }
     uint32_t src = 0;
     bool has = g.input_of(out->id, 0, &src);
-    if (!L.dist(has, src)) return fail(L.err.find("not supported") != std::string::npos ? SF_ERR_UNSUPPORTED : SF_ERR_GRAPH, L.err);
+    if (!L.union_tree(has, src)) return fail(L.err.find("not supported") != std::string::npos ? SF_ERR_UNSUPPORTED : SF_ERR_GRAPH, L.err);
     if (L.max_stack > SF_MAX_DIST_STACK) return fail(SF_ERR_UNSUPPORTED, "distance tree wider than the device stack");
     P.max_stack = L.max_stack;
+    // The branch-and-bound needs a skippable node anywhere in the graph (the `fast` set
+    // of graph_wgsl.rs:1021-1033: enabled Bounded or Instances not reached negatively).
+    // Past SF_MAX_UNION_LEAVES leaves the plain exact program runs: the same sample.
+    const bool any_fast = std::any_of(g.nodes.begin(), g.nodes.end(), [&](const sf_node& n) {
+        return n.enabled && (n.kind == SF_NODE_BOUNDED || n.kind == SF_NODE_INSTANCES) &&
+               !L.unsafe_bounds.count(n.id);
+    });
+    if (any_fast && L.leaves.size() > 1 && L.leaves.size() <= SF_MAX_UNION_LEAVES) {
+        P.union_leaves = uint32_t(L.leaves.size());
+        for (size_t i = 0; i < L.leaves.size(); ++i) {
+            P.leaf_begin[i] = uint8_t(L.leaves[i].begin);
+            P.leaf_end[i] = uint8_t(L.leaves[i].end);
+        }
+    }
     P.inst_floats = uint32_t(inst.size());
     detect_form(g, P);
     std::memset(&info, 0, sizeof info);
@@ -899,6 +941,7 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     info.form = P.form;
     info.op_count = P.n_ops;
     info.bounding_radius_hint = g.hint;
+    info.exact_union_leaves = P.form == SF_FORM_GENERIC ? P.union_leaves : 0;
     return SF_OK;
 }
 

@@ -20,7 +20,7 @@ __global__ void __launch_bounds__(256) k_de_probe(const DeProgram* __restrict__ 
     stage_program(P, prog_g);
     __syncthreads();
     for (size_t i = blockIdx.x * (size_t)blockDim.x + threadIdx.x; i < n; i += (size_t)gridDim.x * blockDim.x) {
-        DeSampleF s = de_finalize(P, de_raw_exact(P, mk3(x[i], y[i], z[i])));
+        DeSampleF s = de_finalize(P, de_raw_exact_search(P, mk3(x[i], y[i], z[i])));
         dist[i] = s.d;
         traps[i] = s.traps[0];
         traps[n + i] = s.traps[1];

@@ -51,7 +51,7 @@ __global__ void __launch_bounds__(256) k_preview(const DeProgram* __restrict__ p
         for (uint32_t q = 0; q < quantum && tag.x < PV_DONE; ++q) {
             float3 p = org + rd * m.x;
             if (tag.x >= PV_TAP0) p = p + tetra_offset(tag.x - PV_TAP0) * g.w;
-            const float d = de_raw_exact(P, p).d;
+            const float d = de_raw_exact_search(P, p).d;
             if (!(fabsf(d) <= 3.4028235e38f)) {  // an undefined distance is an evaluation error
                 tag.x = PV_ERROR;
                 atomicAdd(&status[2], 1u);

@@ -18,6 +18,7 @@
 #define SF_MAX_LOOP_DEPTH 4
 #define SF_MAX_DIST_STACK 6
 #define SF_MAX_INST_DEPTH 3  // nested Instances levels (MAX_DEPTH, graph/mod.rs:41)
+#define SF_MAX_UNION_LEAVES 32  // leaves of the exact union branch-and-bound
 
 // Opcodes of the generic interpreter. Point and fence operations use the node
 // kind (enum sf_node_kind) as their code; control codes start at 100.
@@ -84,7 +85,16 @@ struct DeProgram {
     float trap_scales[4];
     FormParams fp;
     DeOp ops[SF_MAX_OPS];
+    // The exact union branch-and-bound (graph_wgsl.rs:1112-1154): when the graph has a
+    // skippable Bounded or Instances node and the Output's input is a tree of enabled
+    // Unions over 2..SF_MAX_UNION_LEAVES distinct leaves, leaf i (in depth-first order,
+    // first occurrence) is the self-contained op range [leaf_begin[i], leaf_end[i]),
+    // which pushes one distance state. 0 = exact samples run the whole program. Kept
+    // after the ops, whose offset in shared memory stays that of the plain program.
+    uint32_t union_leaves;
+    uint8_t leaf_begin[SF_MAX_UNION_LEAVES], leaf_end[SF_MAX_UNION_LEAVES];
 };
+static_assert(SF_MAX_OPS <= 255, "leaf ranges are stored as bytes");
 
 // One area light in device form (GpuLight of uniforms.rs:671-713 with the
 // derived quantities the shading code needs every bounce).

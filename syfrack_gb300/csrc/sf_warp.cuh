@@ -51,6 +51,9 @@ static __device__ void stage_program(DeProgram& dst, const DeProgram* src) {
     const uint32_t* s = reinterpret_cast<const uint32_t*>(src);
     uint32_t* d = reinterpret_cast<uint32_t*>(&dst);
     for (size_t i = threadIdx.x; i < bytes / 4; i += blockDim.x) d[i] = __ldg(s + i);
+    // the union leaf table after the ops
+    constexpr size_t tail = offsetof(DeProgram, union_leaves) / 4, end = sizeof(DeProgram) / 4;
+    for (size_t i = tail + threadIdx.x; i < end; i += blockDim.x) d[i] = __ldg(s + i);
 }
 template <class T> static __device__ void stage_pod(T& dst, const T* src) {
     const uint32_t* s = reinterpret_cast<const uint32_t*>(src);

@@ -203,7 +203,8 @@ class Graph:
         check(load().sf_graph_validate(C.byref(desc), C.byref(info)))
         return {"step_scale": info.step_scale, "lipschitz": info.lipschitz,
                 "trap_scales": list(info.trap_scales), "iteration_product": info.iteration_product,
-                "form": abi.FORMS.get(info.form, info.form), "op_count": info.op_count}
+                "form": abi.FORMS.get(info.form, info.form), "op_count": info.op_count,
+                "exact_union_leaves": info.exact_union_leaves}
 
     # -- C ABI packing -----------------------------------------------------------
     def to_desc(self):

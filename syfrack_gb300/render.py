@@ -108,7 +108,8 @@ class CompiledGraph:
         check(self.ctx.lib.sf_graph_info_get(self.h, C.byref(i)))
         return {"step_scale": i.step_scale, "lipschitz": i.lipschitz, "trap_scales": list(i.trap_scales),
                 "iteration_product": i.iteration_product, "form": abi.FORMS.get(i.form, i.form),
-                "op_count": i.op_count, "bounding_radius_hint": i.bounding_radius_hint}
+                "op_count": i.op_count, "bounding_radius_hint": i.bounding_radius_hint,
+                "exact_union_leaves": i.exact_union_leaves}
 
     def update(self, graph: Graph):
         desc, keep = graph.to_desc()
