@@ -47,7 +47,7 @@ FLOPS_PER_EVAL = 29
 
 def profiled_traffic():
     """DRAM bytes per trace launch at 1280x720 from the committed ncu summary (or None)."""
-    path = os.path.join(ROOT, "profiles", "k_trace_mandelbox_640x360_ncu.md")
+    path = os.path.join(ROOT, "profiles", "k_trace_mandelbox_ncu.md")
     try:
         for line in open(path):
             if line.startswith("traffic_bytes_per_launch_1280x720:"):
@@ -318,8 +318,9 @@ def run_ours(args):
                          "unit": "TFLOP/s", "frac": achieved / peak.value if peak.value else None,
                          "traffic": profiled_traffic() if ((cfg.width, cfg.height) == (1280, 720)
                                                            and spp_step == 64) else None,
-                         "traffic_source": "dram__bytes_read+write per k_trace launch, ncu capture at 640x360 x 64 "
-                                           "spp scaled x4 (profiles/k_trace_mandelbox_640x360_ncu.md)", "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
+                         "traffic_source": "dram__bytes_read+write per k_trace launch, one-pass ncu capture of the "
+                                           "1280x720 x 64-spp dispatch (profiles/k_trace_mandelbox_ncu.md)",
+                         "peak_source": "measured FFMA probe (sf_device_fp32_peak)",
                          "flops_per_launch": per_launch_flops, "launch_ms": avg_launch_s * 1e3,
                          "de_evals_per_step": st["de_evals"] / args.steps,
                          "de_iterations_per_step": st["de_iterations"] / args.steps,
