@@ -167,14 +167,15 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
 
     const uint32_t regen = tl.regen ? tl.regen : 1u;
     while (true) {
-        // Two votes per DE call decide the warp's next move: all lanes done ends the
-        // loop; idle lanes take new segments together once `regen` of them are idle (or
-        // no lane is marching), so the segment set-up runs for many lanes at once and
-        // the fetch (a vote and one atomic) only runs when the warp refills.
-        const uint32_t idle = __ballot_sync(FULL_MASK, state == TL_IDLE);
-        const uint32_t done = __ballot_sync(FULL_MASK, state == TL_DONE);
-        if (done == FULL_MASK) break;
-        if (idle && ((uint32_t)__popc(idle) >= regen || (idle | done) == FULL_MASK)) {  // warp-uniform
+        // One vote per DE call while every lane marches; when some lane is idle or done,
+        // a second vote decides the warp's next move: all lanes done ends the loop; idle
+        // lanes take new segments together once `regen` of them are idle (or no lane is
+        // marching), so the segment set-up runs for many lanes at once and the fetch (a
+        // vote and one atomic) only runs when the warp refills.
+        const uint32_t quiet = __ballot_sync(FULL_MASK, state == TL_IDLE || state == TL_DONE);
+        const uint32_t idle = quiet ? __ballot_sync(FULL_MASK, state == TL_IDLE) : 0u;  // warp-uniform
+        if (quiet == FULL_MASK && idle == 0u) break;  // every lane done
+        if (idle && ((uint32_t)__popc(idle) >= regen || quiet == FULL_MASK)) {  // warp-uniform
             const uint32_t w = warp_fetch(tl.work_counter, state == TL_IDLE);
             if constexpr (LANE_STATS) {
                 if (t_dry == 0 && __any_sync(FULL_MASK, state == TL_IDLE && w >= total)) t_dry = clock64();
