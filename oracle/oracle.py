@@ -62,6 +62,9 @@ def lib():
         up = C.POINTER(C.c_uint32)
         L.or_de_eval.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, dp, up, up, C.c_int]
         L.or_de_eval_fast.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, up, C.c_int]
+        L.or_de_eval_search.argtypes = [C.c_void_p, C.c_int, dp, C.c_size_t, dp, dp, up, up, up, C.c_int]
+        L.or_union_leaves.argtypes = [C.c_void_p, up]
+        L.or_union_leaves.restype = C.c_uint32
         L.or_panorama.argtypes = [C.c_uint64, C.POINTER(C.c_float), C.c_uint32, C.c_uint32, C.POINTER(C.c_float),
                                   up, up]
         L.or_panorama.restype = C.c_int
@@ -161,6 +164,28 @@ class OracleGraph:
         lib().or_de_eval(self.h, precision, _dp(pts), n, _dp(dist), _dp(traps), _up(iters), _up(mats),
                          threads or default_threads())
         return {"distance": dist, "traps": traps, "iterations": iters, "material": mats}
+
+    def de_search(self, points, precision=64, threads=None):
+        """The exact sample through the union search (graph_wgsl.rs:1112-1154): the
+        leaves probed for their bounds, then evaluated exactly while a bound can beat
+        the best; the same fields as de(), and per point the leaves evaluated exactly
+        after the probes."""
+        pts = np.ascontiguousarray(points, dtype=np.float64).reshape(-1, 3)
+        n = len(pts)
+        dist = np.zeros(n)
+        traps = np.zeros((n, 4))
+        iters = np.zeros(n, dtype=np.uint32)
+        mats = np.zeros(n, dtype=np.uint32)
+        exact = np.zeros(n, dtype=np.uint32)
+        lib().or_de_eval_search(self.h, precision, _dp(pts), n, _dp(dist), _dp(traps), _up(iters), _up(mats),
+                                _up(exact), threads or default_threads())
+        return {"distance": dist, "traps": traps, "iterations": iters, "material": mats, "exact_leaves": exact}
+
+    def union_leaves(self):
+        """(leaves of the union search, whether the graph has a skippable node)."""
+        fast = C.c_uint32()
+        n = lib().or_union_leaves(self.h, C.byref(fast))
+        return int(n), bool(fast.value)
 
     def de_fast(self, points, precision=64, threads=None):
         """The GPU's march sample: skippable Bounded branches outside their margin

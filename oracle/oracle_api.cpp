@@ -168,6 +168,38 @@ void or_de_eval(void* gp, int precision, const double* xyz, size_t n, double* di
     });
 }
 
+// The exact sample through the union search (graph_wgsl.rs:1112-1154), as or_de_eval.
+// exact_leaves[i]: the leaves point i evaluated exactly after the probes.
+void or_de_eval_search(void* gp, int precision, const double* xyz, size_t n, double* dist, double* traps,
+                       uint32_t* iters, uint32_t* mats, uint32_t* exact_leaves, int threads) {
+    const Graph& g = *static_cast<Graph*>(gp);
+    parallel_for(n, threads, [&](size_t i) {
+        exact_leaves[i] = 0;
+        if (precision == 32) {
+            auto s = evaluate_union_search<float>(
+                g, V3<float>(float(xyz[3 * i]), float(xyz[3 * i + 1]), float(xyz[3 * i + 2])), &exact_leaves[i]);
+            dist[i] = s.distance;
+            for (int k = 0; k < 4; ++k) traps[4 * i + k] = s.traps[k];
+            iters[i] = s.iterations;
+            mats[i] = s.material;
+        } else {
+            auto s = evaluate_union_search<double>(g, V3<double>(xyz[3 * i], xyz[3 * i + 1], xyz[3 * i + 2]),
+                                                   &exact_leaves[i]);
+            dist[i] = s.distance;
+            for (int k = 0; k < 4; ++k) traps[4 * i + k] = s.traps[k];
+            iters[i] = s.iterations;
+            mats[i] = s.material;
+        }
+    });
+}
+// The union search's leaves (union_leaves, graph_wgsl.rs:18-26) and whether the graph
+// has a skippable Bounded or Instances node.
+uint32_t or_union_leaves(void* gp, uint32_t* any_fast) {
+    const Graph& g = *static_cast<Graph*>(gp);
+    *any_fast = g.fast_bounds.empty() ? 0u : 1u;
+    return uint32_t(g.union_leaves.size());
+}
+
 // The GPU's fast sample (de_sample, graph_wgsl.rs:800-814): distance and flags.
 void or_de_eval_fast(void* gp, int precision, const double* xyz, size_t n, double* dist, uint32_t* flags,
                      int threads) {

@@ -2,6 +2,7 @@
 #include "oracle_core.hpp"
 
 #include <algorithm>
+#include <functional>
 #include <map>
 #include <set>
 #include <unordered_map>
@@ -232,6 +233,33 @@ bool prepare(Graph& g) {
             for (uint32_t id : g.order) if (sub.count(id)) plan.push_back(id);
             g.plans[child] = plan;
         }
+    }
+    g.union_leaves.clear();
+    {
+        std::function<void(bool, uint32_t)> leaves = [&](bool has, uint32_t id) {
+            const sf_node* n = has ? g.node(id) : nullptr;
+            if (n && n->enabled && n->kind == SF_NODE_UNION) {
+                for (uint32_t port = 0; port < 2; ++port) {
+                    uint32_t from = 0;
+                    const bool h = g.input_of(id, port, &from);
+                    leaves(h, from);
+                }
+                return;
+            }
+            if (!n) { g.union_leaves.push_back(UINT32_MAX); return; }
+            if (std::find(g.union_leaves.begin(), g.union_leaves.end(), id) != g.union_leaves.end()) return;
+            g.union_leaves.push_back(id);
+            if (!g.plans.count(id)) {
+                std::set<uint32_t> sub;
+                needed(g, id, sub);
+                std::vector<uint32_t> plan;
+                for (uint32_t o : g.order) if (sub.count(o)) plan.push_back(o);
+                g.plans[id] = plan;
+            }
+        };
+        uint32_t root = 0;
+        const bool has = g.input_of(g.output, 0, &root);
+        leaves(has, root);
     }
     for (int i = 0; i < 4; ++i) g.trap_scales[i] = 1.f;
     for (uint32_t id : g.order) trap_walk(g, id, 0, g.trap_scales);
@@ -619,13 +647,16 @@ template <class R> static DistState<R> combine(const sf_node& n, DistState<R> a,
     return r;
 }
 
-template <class R> static DistState<R> eval_raw(const Graph& g, uint32_t target, V3<R> p, bool fast, int depth);
+template <class R>
+static DistState<R> eval_raw(const Graph& g, uint32_t target, V3<R> p, bool fast, int depth, bool probe = false);
 
 // Instances (eval.rs:749-814): the nearest copy found by the seeded stackless walk
 // over the fence hierarchy; with fast, the GPU's skips (graph_wgsl.rs:760-790): the
-// root fence beyond the margin, and copies whose fence is beyond it.
+// root fence beyond the margin, and copies whose fence is beyond it. probe (the union
+// search's bounds-only sample, graph_wgsl.rs:766-767): the root fence whatever the margin.
 template <class R>
-static DistState<R> eval_instances(const Graph& g, const sf_node& n, V3<R> p, bool fast, int depth) {
+static DistState<R> eval_instances(const Graph& g, const sf_node& n, V3<R> p, bool fast, int depth,
+                                   bool probe = false) {
     const R INF = std::numeric_limits<R>::infinity();
     DistState<R> best{INF, 0, 0, {INF, INF, INF, INF}};
     uint32_t child;
@@ -637,7 +668,7 @@ static DistState<R> eval_instances(const Graph& g, const sf_node& n, V3<R> p, bo
     if (skip) {
         best.d = R(1e30);
         R env = inst_bound(nodes[0], p);
-        if (env > margin) return DistState<R>{env, 0, 0, {INF, INF, INF, INF}, 1};
+        if (probe || env > margin) return DistState<R>{env, 0, 0, {INF, INF, INF, INF}, 1};
     }
     size_t chosen = SIZE_MAX, seed = 0;
     while (nodes[seed].placement < 0) {
@@ -689,8 +720,11 @@ static DistState<R> eval_instances(const Graph& g, const sf_node& n, V3<R> p, bo
 }
 
 // evaluate_raw (eval.rs:671-826) + PreparedGraph::evaluate (eval.rs:98-114); with
-// fast, the GPU's skippable bounds (graph_wgsl.rs:800-814).
-template <class R> static DistState<R> eval_raw(const Graph& g, uint32_t target, V3<R> p, bool fast, int depth) {
+// fast, the GPU's skippable bounds (graph_wgsl.rs:800-814); with probe as well, the
+// union search's bounds-only sample (graph_wgsl.rs:808-812): every skippable bound
+// whatever the margin.
+template <class R>
+static DistState<R> eval_raw(const Graph& g, uint32_t target, V3<R> p, bool fast, int depth, bool probe) {
     const R INF = std::numeric_limits<R>::infinity();
     DistState<R> empty{INF, 0, 0, {INF, INF, INF, INF}};
     PointState<R> start{p, R(1), 0, {INF, INF, INF, INF}};
@@ -744,14 +778,14 @@ template <class R> static DistState<R> eval_raw(const Graph& g, uint32_t target,
                 sf_node box = n;
                 box.kind = SF_NODE_BOX;
                 const R bound = fence(box, get_point(id, 0));
-                if (fast && g.fast_bounds.count(id) && bound > R(n.f[3]))
+                if (fast && g.fast_bounds.count(id) && (probe || bound > R(n.f[3])))
                     v.ds = DistState<R>{bound, 0, 0, {INF, INF, INF, INF}, 1};
                 else
                     v.ds.d = r_max(v.ds.d, bound);
             }
         } else if (k == SF_NODE_INSTANCES && n.enabled) {
             v.point = false;
-            v.ds = eval_instances(g, n, p, fast, depth);
+            v.ds = eval_instances(g, n, p, fast, depth, probe);
         } else if (!n.enabled) {
             v.point = false;
             v.ds = get_dist(id, 0);
@@ -764,6 +798,56 @@ template <class R> static DistState<R> eval_raw(const Graph& g, uint32_t target,
     auto it = values.find(target);
     if (it != values.end() && !it->second.point) return it->second.ds;
     return empty;
+}
+
+template <class R> static Sample<R> sample_of(const Graph& g, const DistState<R>& r) {
+    Sample<R> out;
+    out.distance = r.d;
+    out.material = r.material;
+    for (int i = 0; i < 4; ++i)
+        out.traps[i] = r_finite(r.traps[i]) ? r_min(r.traps[i] / R(g.trap_scales[i]), R(1)) : R(1);
+    out.iterations = std::min(r.iter, g.iteration_product);
+    out.flags = r.flags;
+    return out;
+}
+
+// The union search (graph_wgsl.rs:1112-1154, its `_exact` function): each leaf's probe
+// (a probe that took no skip is the leaf's exact sample), then the unsettled leaf with
+// the lowest bound, ties to the lower index, evaluated exactly until no bound can
+// reach the best; the best starts empty (+inf) where the WGSL starts from a 1e30
+// sentinel, so an all-empty union keeps the plain union's +inf.
+template <class R> Sample<R> evaluate_union_search(const Graph& g, V3<R> p, uint32_t* exact_leaves) {
+    const size_t k = g.union_leaves.size();
+    if (k < 2 || k > 128 || g.fast_bounds.empty()) return evaluate(g, p, false);
+    const R INF = std::numeric_limits<R>::infinity();
+    const DistState<R> empty{INF, 0, 0, {INF, INF, INF, INF}};
+    auto leaf = [&](size_t i, bool probe) {
+        return g.union_leaves[i] == UINT32_MAX ? empty : eval_raw(g, g.union_leaves[i], p, probe, 0, probe);
+    };
+    std::vector<R> lower(k);
+    std::vector<char> settled(k, 0);
+    DistState<R> best = empty;
+    size_t winner = k;
+    for (size_t i = 0; i < k; ++i) {
+        const DistState<R> s = leaf(i, true);
+        lower[i] = s.d;
+        if (s.flags == 0) {
+            settled[i] = 1;
+            if (s.d < best.d || (s.d == best.d && i < winner)) { best = s; winner = i; }
+        }
+    }
+    for (size_t step = 0; step < k; ++step) {
+        size_t chosen = k;
+        R bound = INF;
+        for (size_t i = 0; i < k; ++i)
+            if (!settled[i] && (lower[i] < bound || (lower[i] == bound && i < chosen))) { chosen = i; bound = lower[i]; }
+        if (chosen == k || bound > best.d) break;
+        settled[chosen] = 1;
+        if (exact_leaves) ++*exact_leaves;
+        const DistState<R> s = leaf(chosen, false);
+        if (s.d < best.d || (s.d == best.d && chosen < winner)) { best = s; winner = chosen; }
+    }
+    return sample_of(g, best);
 }
 
 template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast) {
@@ -2534,6 +2618,8 @@ template <class R> Sample<R> planar_sample(const PlanarParams& f, V2<R> input) {
 // explicit instantiations
 template Sample<float> evaluate<float>(const Graph&, V3<float>, bool);
 template Sample<double> evaluate<double>(const Graph&, V3<double>, bool);
+template Sample<float> evaluate_union_search<float>(const Graph&, V3<float>, uint32_t*);
+template Sample<double> evaluate_union_search<double>(const Graph&, V3<double>, uint32_t*);
 template <class R> R texture_value_at(const Scene<R>& sc, V3<R> p) { return texture_value(sc.tex, p); }
 template float texture_value_at<float>(const Scene<float>&, V3<float>);
 template double texture_value_at<double>(const Scene<double>&, V3<double>);

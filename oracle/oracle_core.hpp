@@ -134,6 +134,11 @@ struct Graph {
     struct InstBounds { float center[3], half[3]; size_t escape; int64_t placement; };
     std::map<uint32_t, std::vector<InstBounds>> instances;
     std::map<uint32_t, std::vector<uint32_t>> plans;
+    // The exact union search (graph_wgsl.rs:1112-1154): the leaves below the Output's
+    // enabled Unions, depth-first, first input first, a leaf reached twice kept once
+    // (union_leaves, :18-26); an unconnected port is a leaf of its own (UINT32_MAX:
+    // the empty state). Each leaf has a plan.
+    std::vector<uint32_t> union_leaves;
 
     const sf_node* node(uint32_t id) const {
         for (auto& n : nodes) if (n.id == id) return &n;
@@ -192,6 +197,12 @@ template <class R> struct Sample { R distance; R traps[4]; uint32_t iterations; 
 // fast = true: the GPU's de_sample (graph_wgsl.rs:800-814): a skippable Bounded
 // branch outside its margin gives its bound, flagged (flags = 1).
 template <class R> Sample<R> evaluate(const Graph& g, V3<R> p, bool fast = false);
+// The reference's exact sample with the union search (graph_wgsl.rs:1112-1154): every
+// leaf probed for its bound, then the leaves whose bound can beat the best evaluated
+// exactly, lowest bound first; when the search does not apply (fewer than two leaves,
+// more than 128, or no skippable node) the plain exact sample.
+// exact_leaves (optional): adds the number of leaves evaluated exactly after the probes.
+template <class R> Sample<R> evaluate_union_search(const Graph& g, V3<R> p, uint32_t* exact_leaves = nullptr);
 
 // ---------------------------------------------------------------- transport
 template <class R> struct Camera { V3<R> origin, forward, right, up; R tan_half, aspect, lens_radius, focus_distance; };

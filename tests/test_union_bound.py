@@ -135,6 +135,31 @@ def test_a_leaf_reached_twice_counts_once():
     assert b.graph(root).validate()["exact_union_leaves"] == 2
 
 
+def test_oracle_search_is_the_union(oracle_mod):
+    """The oracle's restatement of the search (probe every leaf, then the exact leaves
+    whose bound can beat the best) returns the union's own sample: equal in every field
+    to the plain evaluation, in binary32 and in FP64, on points about every leaf; the
+    leaves it walks are the host lowering's."""
+    og = oracle_mod.OracleGraph(union_world())
+    assert og.union_leaves() == (UNION_WORLD_LEAVES, True)
+    assert oracle_mod.OracleGraph(union_world(hidden=True)).union_leaves()[0] == 1
+    assert oracle_mod.OracleGraph(bounded_bulb(subtract=True)).union_leaves()[1] is False
+    pts = union_points()
+    for prec in (32, 64):
+        a, b = og.de_search(pts, precision=prec), og.de(pts, precision=prec)
+        for k in ("distance", "traps", "iterations", "material"):
+            np.testing.assert_array_equal(a[k], b[k], err_msg=f"{k} at {prec} bits")
+        # six of the nine leaves have skippable bounds (their probes are bounds); the
+        # search evaluates few of them exactly
+        assert a["exact_leaves"].max() <= 6 and a["exact_leaves"].mean() < 2.5, a["exact_leaves"].mean()
+    # far from the world every probe of a bounded leaf loses to an exact probe (the
+    # sphere, the cut, the disabled union's leaf) or to another bound: still the union
+    far = lcg_points(512, 12.0, 5)
+    a, b = og.de_search(far, precision=64), og.de(far, precision=64)
+    np.testing.assert_array_equal(a["distance"], b["distance"])
+    np.testing.assert_array_equal(a["material"], b["material"])
+
+
 def test_the_world_is_within_the_device_program():
     info = union_world().validate()
     hidden = union_world(hidden=True).validate()
