@@ -106,6 +106,24 @@ def kitchen_sink():
     return Graph(n, links, safety=0.8, bounding_radius_hint=3.0)
 
 
+def test_spherical_power_vectors_on_the_device(renderer):
+    """eval.rs:180-222 on the device's Power node (the binary-power branch for n outside
+    {6, 8}, the repeated squaring for 6 and 8): the powered point of n = 1..16 against
+    FP64 trigonometry on the reference's points, within the reference's bounds (5e-6
+    r^n on the point, 4e-6 on the derivative), and the filament (1e-6, 0, 1)^8."""
+    from test_oracle import power_component_graph, spherical_power_error, spherical_power_points
+
+    pts = spherical_power_points()
+    worst = {}
+    for n in range(1, 17):
+        d = [renderer.compile(power_component_graph(n, a)).probe(pts)["distance"].astype(np.float64) for a in range(3)]
+        worst[n] = spherical_power_error(d, pts, n)
+    print({n: round(w, 3) for n, w in worst.items()})
+    assert max(worst.values()) <= 1.0, worst
+    x = renderer.compile(power_component_graph(8, 0)).probe(np.array([[1e-6, 0.0, 1.0]], np.float32))["distance"][0]
+    assert abs(float(x) * 8.0 - 8e-6) < 1e-10
+
+
 def test_generic_node_kinds_against_oracle(renderer, oracle_mod):
     g = kitchen_sink()
     pts = lcg_points(4096, 2.5, 17)

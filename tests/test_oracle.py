@@ -74,6 +74,59 @@ def test_integer_spherical_powers_match_trig(oracle_mod):
         assert np.all(np.isfinite(theta)) and np.all(np.isfinite(phi))
 
 
+def power_component_graph(n, axis):
+    """Input -> Power(n) -> Plane(normal = axis, offset 0): the distance is the powered
+    point's component on the axis over the power's derivative, p_n[axis] / (n r^(n-1))."""
+    normal = [0.0, 0.0, 0.0]
+    normal[axis] = 1.0
+    nodes = [Node(0, Kind("Input")), Node(1, Kind("Power", power=float(n))),
+             Node(2, Kind("Plane", normal=normal, offset=0.0)), Node(3, Kind("Output"))]
+    return Graph(nodes, [Link((0, 0), (1, 0)), Link((1, 0), (2, 0)), Link((2, 0), (3, 0))])
+
+
+def spherical_power_points():
+    """The points of eval.rs:180-222: the axes, two near-pole filaments, and 1,000 LCG
+    points in [-1.5, 1.5]^3 (seed 12341)."""
+    special = np.array([[1, 0, 0], [0, 1, 0], [0, 0, 1], [0, 0, -1], [1e-6, 0, 1], [-1e-6, 2e-6, -1]], np.float32)
+    return np.concatenate([special, lcg_points(1000, 1.5, 12341)])
+
+
+def spherical_power_expected(pts, n):
+    """FP64 trigonometry (eval.rs:200-210): the powered point and its derivative."""
+    q = pts.astype(np.float64)
+    r = np.linalg.norm(q, axis=1)
+    theta = np.arccos(np.clip(q[:, 2] / r, -1, 1)) * n
+    phi = np.arctan2(q[:, 1], q[:, 0]) * n
+    e = np.stack([np.sin(theta) * np.cos(phi), np.sin(theta) * np.sin(phi), np.cos(theta)], 1) * (r ** n)[:, None]
+    return e, n * r ** (n - 1), r
+
+
+def spherical_power_error(dist_by_axis, pts, n):
+    """Each component's error against FP64 trigonometry, in units of the reference's
+    bounds: the point within 5e-6 r^n and the derivative within 4e-6 of itself
+    (eval.rs:212-217), both carried by p_n[axis] / dr."""
+    e, dr, r = spherical_power_expected(pts, n)
+    worst = 0.0
+    for axis in range(3):
+        got = dist_by_axis[axis] * dr  # the component, through the expected derivative
+        bound = 5e-6 * np.maximum(r ** n, 1e-20) + 4e-6 * np.abs(e[:, axis])
+        worst = max(worst, float((np.abs(got - e[:, axis]) / bound).max()))
+    return worst
+
+
+def test_spherical_power_vectors_match_trig(oracle_mod):
+    # eval.rs:180-222 componentwise: the powered point of n = 1..16 against FP64
+    # trigonometry on the reference's own points, and the filament (1e-6, 0, 1)^8,
+    # whose rounded cosine is exactly 1: x = 8e-6 within 1e-10
+    pts = spherical_power_points()
+    for n in range(1, 17):
+        d = [oracle_mod.OracleGraph(power_component_graph(n, a)).de(pts, precision=32)["distance"] for a in range(3)]
+        assert spherical_power_error(d, pts, n) <= 1.0, n
+    x = oracle_mod.OracleGraph(power_component_graph(8, 0)).de(np.array([[1e-6, 0.0, 1.0]], np.float32),
+                                                               precision=32)["distance"][0]
+    assert abs(x * 8.0 - 8e-6) < 1e-10
+
+
 def test_bulb_symmetry_and_inside_outside(oracle_mod):
     # fractal.rs:103-178: inside/far points, 2pi/7 symmetry about z, not pi/4
     og = oracle_mod.OracleGraph(Graph.bundled("mandelbulb"))
