@@ -215,8 +215,17 @@ typedef struct sf_material {
  *   Sun: direction toward the sun, angular_size = full angular diameter in degrees,
  *     radiance = irradiance (color * intensity);
  *   Environment: zenith, horizon and ground radiance (colors * intensity);
- *   Hdri: an equirectangular panorama (below), intensity in radiance[0], rotation. */
-enum { SF_LIGHT_AREA = 0, SF_LIGHT_SUN = 1, SF_LIGHT_ENVIRONMENT = 2, SF_LIGHT_HDRI = 3 };
+ *   Hdri: an equirectangular panorama (below), intensity in radiance[0], rotation;
+ *   Projector (ABI 1.5; Light::Projector, uniforms.rs:671-716): an Area light (centre,
+ *     edges, radiance) whose emission about its normal is full within direction[0]
+ *     degrees (the inner angle), none beyond direction[1] degrees (the outer angle,
+ *     0 < outer < 90, inner <= outer) and blended between (lights.wgsl:11-16);
+ *   Tube (ABI 1.5; Light::Tube, uniforms.rs:717-729): a capsule from center (the
+ *     start) to edge_u (the end point), radius edge_v[0], radiance = color * intensity. */
+enum {
+    SF_LIGHT_AREA = 0, SF_LIGHT_SUN = 1, SF_LIGHT_ENVIRONMENT = 2, SF_LIGHT_HDRI = 3,
+    SF_LIGHT_PROJECTOR = 4, SF_LIGHT_TUBE = 5
+};
 typedef struct sf_area_light {
     float center[3], edge_u[3], edge_v[3], radiance[3];
     uint32_t kind;

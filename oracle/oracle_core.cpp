@@ -911,10 +911,25 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
             R peak = 0;
             for (int k = 0; k < 3; ++k) peak = r_max(peak, r_max(R(l.zenith[k]), r_max(R(l.horizon[k]), R(l.ground[k]))));
             o.peak = peak;
+        } else if (l.kind == SF_LIGHT_TUBE) {
+            // GpuLight::from_light (uniforms.rs:717-729): start, end, radius, length
+            o.a = v3<R>(l.center);
+            o.b = v3<R>(l.edge_u);
+            o.radius = R(l.edge_v[0]);
+            o.length = (o.b - o.a).length();
         } else {
+            // an area light; a projector adds its beam (uniforms.rs:690-715), in binary32
+            o.kind = SF_LIGHT_AREA;
             o.a = v3<R>(l.center);
             o.b = v3<R>(l.edge_u);
             o.c = v3<R>(l.edge_v);
+            if (l.kind == SF_LIGHT_PROJECTOR) {
+                const float deg = 3.14159265f / 180.0f;
+                o.projector = true;
+                o.beam[0] = R(std::cos(l.direction[0] * deg));
+                o.beam[1] = R(std::cos(l.direction[1] * deg));
+                o.beam[2] = R(std::tan(l.direction[1] * deg));
+            }
         }
     }
     const sf_coloring& col = d.coloring;
@@ -1104,9 +1119,88 @@ template <class R> V3<R> normal_central(const Graph& g, V3<R> p, R h) {
     return normalize(grad);
 }
 
-// Lights (lights.wgsl:150-356), area emitters only.
+static const double PI_W = 3.14159265358979;  // common.wgsl:6
+// Lights (lights.wgsl:5-356): rectangles, projectors (a rectangle with a beam) and
+// tubes (capsules) are the emitters.
 template <class R> static V3<R> area_normal(const Light<R>& l) { return safe_normalize(l.b.cross(l.c)); }
 template <class R> static R luminance(V3<R> c) { return c.x * R(0.2126) + c.y * R(0.7152) + c.z * R(0.0722); }
+template <class R> static bool is_emitter(const Light<R>& l) { return l.kind == SF_LIGHT_AREA || l.kind == SF_LIGHT_TUBE; }
+// beam_profile (lights.wgsl:11-16)
+template <class R> static R beam_profile(const Light<R>& l, V3<R> direction) {
+    if (!l.projector) return 1;
+    const R cosine = area_normal(l).dot(direction);
+    const R t = r_clamp((cosine - l.beam[1]) / r_max(l.beam[0] - l.beam[1], R(1e-7)), R(0), R(1));
+    return t * t * t * (R(10) + t * (R(-15) + R(6) * t));
+}
+template <class R> static V3<R> emitter_radiance(const Light<R>& l, V3<R> direction) {
+    return l.color * beam_profile(l, direction);
+}
+// cone_segment (lights.wgsl:23-68); an empty interval is (1, 0)
+template <class R>
+static void cone_segment(V3<R> ro, V3<R> rd, R end, V3<R> apex, V3<R> axis, R cosine, R* lo, R* hi) {
+    R ix = 0, iy = end;
+    const V3<R> delta = ro - apex;
+    const R axial = delta.dot(axis), slope = rd.dot(axis);
+    auto empty = [&]() { *lo = 1; *hi = 0; };
+    if (r_abs(slope) < R(1e-8)) {
+        if (axial < R(0)) return empty();
+    } else {
+        const R crossing = -axial / slope;
+        if (slope > R(0)) ix = r_max(ix, crossing);
+        else iy = r_min(iy, crossing);
+    }
+    if (iy <= ix) return empty();
+    const R c2 = cosine * cosine;
+    const R s2 = (R(1) - cosine) * (R(1) + cosine);
+    const V3<R> radial = delta - axis * axial;
+    const V3<R> radial_slope = rd - axis * slope;
+    const R a = s2 * slope * slope - c2 * radial_slope.dot(radial_slope);
+    const R b = R(2) * (s2 * axial * slope - c2 * radial.dot(radial_slope));
+    const R c = s2 * axial * axial - c2 * radial.dot(radial);
+    if (r_abs(a) < R(1e-12)) {
+        if (r_abs(b) < R(1e-12)) {
+            if (c < R(0)) return empty();
+        } else if (b > R(0)) {
+            ix = r_max(ix, -c / b);
+        } else {
+            iy = r_min(iy, -c / b);
+        }
+        *lo = ix; *hi = iy;
+        return;
+    }
+    const R discriminant = b * b - R(4) * a * c;
+    if (discriminant <= R(0)) {
+        const R middle = (ix + iy) * R(0.5);
+        if ((a * middle + b) * middle + c < R(0)) return empty();
+        *lo = ix; *hi = iy;
+        return;
+    }
+    const R root = r_sqrt(discriminant);
+    const R q = R(-0.5) * (b + (b >= R(0) ? root : -root));
+    const R r0 = q / a, r1 = c / q;
+    const R low = r_min(r0, r1), high = r_max(r0, r1);
+    if (a < R(0)) { *lo = r_max(ix, low); *hi = r_min(iy, high); return; }
+    if (r_min(iy, low) > ix) { *lo = ix; *hi = r_min(iy, low); return; }
+    *lo = r_max(ix, high);
+    *hi = iy;
+}
+// projector_bound_apex (lights.wgsl:72-75)
+template <class R> static V3<R> projector_bound_apex(const Light<R>& l) {
+    const R radius = R(0.5) * (l.b + l.c).length();
+    return l.a - area_normal(l) * (radius / l.beam[2]);
+}
+// emitter_area (lights.wgsl:77-85)
+template <class R> static R emitter_area(const Light<R>& l) {
+    if (l.kind == SF_LIGHT_TUBE) return R(2) * R(PI_W) * l.radius * (l.length + R(2) * l.radius);
+    return l.b.cross(l.c).length();
+}
+// emitter_normal (lights.wgsl:87-94)
+template <class R> static V3<R> emitter_normal(const Light<R>& l, V3<R> point) {
+    if (l.kind != SF_LIGHT_TUBE) return area_normal(l);
+    const V3<R> axis = l.b - l.a;
+    const R t = r_clamp((point - l.a).dot(axis) / axis.dot(axis), R(0), R(1));
+    return safe_normalize(point - l.a - axis * t);
+}
 template <class R> static R area_intersection(V3<R> ro, V3<R> rd, const Light<R>& l) {
     V3<R> n = area_normal(l);
     R den = n.dot(rd);
@@ -1119,19 +1213,94 @@ template <class R> static R area_intersection(V3<R> ro, V3<R> rd, const Light<R>
     if (r_abs(x) > R(0.5) || r_abs(y) > R(0.5)) return R(1e30);
     return t;
 }
-template <class R> static R emitter_area(const Light<R>& l) { return l.b.cross(l.c).length(); }
+// tube_intersection (lights.wgsl:97-129)
+template <class R> static R tube_intersection(V3<R> ro, V3<R> rd, const Light<R>& l) {
+    const R r = l.radius, len = l.length;
+    const V3<R> axis = (l.b - l.a) / len;
+    const V3<R> oa = ro - l.a;
+    const R axial_ray = axis.dot(rd), axial_origin = axis.dot(oa);
+    const V3<R> side = axis.cross(rd);
+    const R a = side.dot(side);
+    R nearest = R(1e30);
+    if (a > R(1e-10)) {
+        const R perpendicular = oa.dot(side) / r_sqrt(a);
+        const R h = r * r - perpendicular * perpendicular;
+        if (h < R(0)) return nearest;
+        const R middle = -(rd.dot(oa) - axial_origin * axial_ray) / a;
+        const R root = r_sqrt(r_max(R(0), h) / a);
+        for (int i = 0; i < 2; ++i) {
+            const R t = middle + (i == 1 ? root : -root);
+            const R y = axial_origin + t * axial_ray;
+            if (t > R(1e-6) && y >= R(0) && y <= len) nearest = r_min(nearest, t);
+        }
+    } else {
+        const V3<R> radial = oa - axis * axial_origin;
+        if (radial.dot(radial) > r * r) return nearest;
+    }
+    for (int cap = 0; cap < 2; ++cap) {
+        const V3<R> oc = ro - (cap == 1 ? l.b : l.a);
+        const R projection = oc.dot(rd);
+        const V3<R> closest = oc - rd * projection;
+        const R h = r * r - closest.dot(closest);
+        if (h < R(0)) continue;
+        const R sh = r_sqrt(h);
+        for (int i = 0; i < 2; ++i) {
+            const R t = -projection + (i == 1 ? sh : -sh);
+            const R y = (ro + rd * t - l.a).dot(axis);
+            const bool on_cap = cap == 1 ? y >= len : y <= R(0);
+            if (t > R(1e-6) && on_cap) nearest = r_min(nearest, t);
+        }
+    }
+    return nearest;
+}
+template <class R> static R emitter_intersection(V3<R> ro, V3<R> rd, const Light<R>& l) {
+    return l.kind == SF_LIGHT_TUBE ? tube_intersection(ro, rd, l) : area_intersection(ro, rd, l);
+}
+template <class R> static void tangent_frame(V3<R> n, V3<R>* t, V3<R>* bt);
+// sample_emitter_point (lights.wgsl:143-160)
+template <class R> static void sample_emitter_point(const Light<R>& l, R u, R v, R w, V3<R>* position, V3<R>* normal) {
+    if (l.kind != SF_LIGHT_TUBE) {
+        *position = l.a + l.b * (u - R(0.5)) + l.c * (v - R(0.5));
+        *normal = area_normal(l);
+        return;
+    }
+    const V3<R> axis = (l.b - l.a) / l.length;
+    V3<R> t, bt;
+    tangent_frame(axis, &t, &bt);
+    const R phi = R(2) * R(PI_W) * w;
+    const V3<R> radial = t * r_cos(phi) + bt * r_sin(phi);
+    const R cylinder_fraction = l.length / (l.length + R(2) * l.radius);
+    if (u < cylinder_fraction) {
+        *position = (l.a * (R(1) - v) + l.b * v) + radial * l.radius;
+        *normal = radial;
+        return;
+    }
+    const bool top = (u - cylinder_fraction) / (R(1) - cylinder_fraction) >= R(0.5);
+    const V3<R> n = radial * r_sqrt(r_max(R(0), R(1) - v * v)) + axis * (v * (top ? R(1) : R(-1)));
+    *position = (top ? l.b : l.a) + n * l.radius;
+    *normal = n;
+}
+// area_weight (lights.wgsl:285-302)
 template <class R> static R area_weight(V3<R> p, V3<R> n, const Light<R>& l) {
+    const bool tube = l.kind == SF_LIGHT_TUBE;
     R area = emitter_area(l);
-    V3<R> to_light = l.a - p;
+    const V3<R> center = tube ? (l.a + l.b) * R(0.5) : l.a;
+    V3<R> to_light = center - p;
     R dist2 = r_max(to_light.dot(to_light), R(1e-6));
     V3<R> dir = to_light / r_sqrt(dist2);
-    R facing = r_max(area_normal(l).dot(-dir), R(0));
+    R facing = tube ? R(0.25) : r_max(area_normal(l).dot(-dir), R(0));
+    if (l.projector) {
+        const V3<R> delta = p - projector_bound_apex(l);
+        const R axial = delta.dot(area_normal(l));
+        if (axial < R(0) || axial * axial < l.beam[1] * l.beam[1] * delta.dot(delta)) return 0;
+        facing = facing * r_max(R(0.025), beam_profile(l, -dir));
+    }
     return luminance(l.color) * area * facing * r_max(n.dot(dir), R(0.15)) / dist2;
 }
 template <class R> static R area_total_weight(const Scene<R>& sc, V3<R> p, V3<R> n) {
     R total = 0;
     for (uint32_t i = 0; i < sc.light_count; ++i)
-        if (sc.lights[i].kind == SF_LIGHT_AREA) total += area_weight(p, n, sc.lights[i]);
+        if (is_emitter(sc.lights[i])) total += area_weight(p, n, sc.lights[i]);
     return total;
 }
 template <class R> static R area_direction_pdf(const Light<R>& l, R dist2, R cos_l) {
@@ -1148,10 +1317,10 @@ template <class R> static V3<R> area_emission(const Scene<R>& sc, V3<R> ro, V3<R
     V3<R> L(0, 0, 0);
     for (uint32_t i = 0; i < sc.light_count; ++i) {
         const Light<R>& l = sc.lights[i];
-        if (l.kind != SF_LIGHT_AREA) continue;
-        R cos_l = area_normal(l).dot(-rd);
+        if (!is_emitter(l)) continue;
+        R cos_l = emitter_normal(l, ro + rd * distance).dot(-rd);
         if (cos_l <= R(0)) continue;
-        R t = area_intersection(ro, rd, l);
+        R t = emitter_intersection(ro, rd, l);
         if (r_abs(t - distance) > r_max(R(1e-6), distance * R(1e-6))) continue;
         R w = 1;
         if (use_mis) {
@@ -1161,14 +1330,13 @@ template <class R> static V3<R> area_emission(const Scene<R>& sc, V3<R> ro, V3<R
             pl = pl * selection;
             w = mis_power(prev_pdf, pl);
         }
-        L = L + l.color * w;
+        L = L + emitter_radiance(l, -rd) * w;
     }
     return L;
 }
 
 // BRDF (pathtrace.wgsl:195-249, :394-463).
 template <class R> struct Surface { V3<R> n, diffuse, f0; R alpha; V3<R> emission; R diffuse_sigma = 0; };
-static const double PI_W = 3.14159265358979;  // common.wgsl:6
 template <class R> static void tangent_frame(V3<R> n, V3<R>* t, V3<R>* bt) {
     R s = n.z >= R(0) ? R(1) : R(-1);
     R a = R(-1) / (s + n.z);
@@ -1932,10 +2100,16 @@ static float volume_coordinate(uint32_t sample_index, uint32_t dimension, uint32
     return v - std::floor(v);
 }
 // fog_segment_weight (pathtrace.wgsl:621-633) and volume_light_probability
-// (lights.wgsl:319-323) for rectangles.
+// (lights.wgsl:319-323).
 template <class R> static R fog_segment_weight(V3<R> ro, V3<R> rd, R end, const Light<R>& l) {
-    const R along = r_clamp((l.a - ro).dot(rd), R(0), end);
-    const V3<R> delta = l.a - (ro + rd * along);
+    const V3<R> center = l.kind == SF_LIGHT_TUBE ? (l.a + l.b) * R(0.5) : l.a;
+    R lo = 0, hi = end;
+    if (l.projector) {
+        cone_segment(ro, rd, end, projector_bound_apex(l), area_normal(l), l.beam[1], &lo, &hi);
+        if (hi <= lo) return 0;
+    }
+    const R along = r_clamp((center - ro).dot(rd), lo, hi);
+    const V3<R> delta = center - (ro + rd * along);
     const R area = emitter_area(l);
     return r_max(r_max(l.color.x, l.color.y), l.color.z) * area / (delta.dot(delta) + area);
 }
@@ -1950,8 +2124,8 @@ static Hit<R> trace_scene(const Graph& g, const Scene<R>& sc, V3<R> ro, V3<R> rd
     R nearest = t_end;
     uint32_t light_index = 0xffffffffu;
     for (uint32_t i = 0; i < sc.light_count; ++i) {
-        if (sc.lights[i].kind != SF_LIGHT_AREA) continue;
-        R t = area_intersection(ro, rd, sc.lights[i]);
+        if (!is_emitter(sc.lights[i])) continue;
+        R t = emitter_intersection(ro, rd, sc.lights[i]);
         if (t < nearest) { nearest = t; light_index = i; }
     }
     // the reference's cone-relative test, or a fixed epsilon when the render states one
@@ -1978,25 +2152,34 @@ static V3<R> fog_segment_direct(const Scene<R>& sc, V3<R> ro, V3<R> rd, R end, u
     if (tau_end <= R(0)) return result;
     R total = 0;
     for (uint32_t i = 0; i < sc.light_count; ++i)
-        if (sc.lights[i].kind == SF_LIGHT_AREA) total += fog_segment_weight(ro, rd, end, sc.lights[i]);
+        if (is_emitter(sc.lights[i])) total += fog_segment_weight(ro, rd, end, sc.lights[i]);
     const R g = sc.fog[3];
     for (uint32_t i = 0; i < sc.light_count; ++i) {
         const Light<R>& l = sc.lights[i];
-        if (l.kind != SF_LIGHT_AREA) continue;
+        if (!is_emitter(l)) continue;
         const R probability = volume_light_probability(fog_segment_weight(ro, rd, end, l), total);
         const uint32_t stream = pcg(point_stream ^ (i * 0x85ebca6bu));
         R selection = rnd<R>(rng);
         if (primary) selection = R(volume_coordinate(point_index, 5, stream));
         if (probability <= R(0) || selection >= probability) continue;
+        // sample_emitter draws two numbers for a rectangle, three for a tube
         R u1 = rnd<R>(rng);
         R u2 = rnd<R>(rng);
+        R u3 = l.kind == SF_LIGHT_TUBE ? rnd<R>(rng) : R(0);
         if (primary) {
             u1 = R(volume_coordinate(point_index, 0, stream));
             u2 = R(volume_coordinate(point_index, 1, stream));
+            u3 = R(volume_coordinate(point_index, 2, stream));
         }
-        const V3<R> q = l.a + l.b * (u1 - R(0.5)) + l.c * (u2 - R(0.5));
-        const R tau_begin = fog_optical_depth(sc, ro, rd, R(0));
-        const R tau_finish = fog_optical_depth(sc, ro, rd, end);
+        V3<R> q, qn;
+        sample_emitter_point(l, u1, u2, u3, &q, &qn);
+        R lo = 0, hi = end;
+        if (l.projector) {
+            cone_segment(ro, rd, end, q, area_normal(l), l.beam[1], &lo, &hi);
+            if (hi <= lo) continue;
+        }
+        const R tau_begin = fog_optical_depth(sc, ro, rd, lo);
+        const R tau_finish = fog_optical_depth(sc, ro, rd, hi);
         const R tau_span = r_max(R(0), tau_finish - tau_begin);
         if (tau_span <= R(0)) continue;
         R conditional_mass = R(1) - r_exp(-tau_span);
@@ -2006,8 +2189,8 @@ static V3<R> fog_segment_direct(const Scene<R>& sc, V3<R> ro, V3<R> rd, R end, u
         const V3<R> delta = q - ro;
         const R projection = delta.dot(rd);
         const R perpendicular = (delta - rd * projection).length();
-        const R theta_a = r_atan2(R(0) - projection, r_max(perpendicular, R(1e-6)));
-        const R theta_b = r_atan2(end - projection, r_max(perpendicular, R(1e-6)));
+        const R theta_a = r_atan2(lo - projection, r_max(perpendicular, R(1e-6)));
+        const R theta_b = r_atan2(hi - projection, r_max(perpendicular, R(1e-6)));
         const R span = theta_b - theta_a;
         const bool regular = perpendicular > R(1e-4) && span > R(1e-5);
         R xi = rnd<R>(rng);
@@ -2016,21 +2199,21 @@ static V3<R> fog_segment_direct(const Scene<R>& sc, V3<R> ro, V3<R> rd, R end, u
             xi = R(volume_coordinate(point_index, 3, stream));
             technique = R(volume_coordinate(point_index, 4, stream));
         }
-        R t = end * xi;  // mix(0, end, xi)
+        R t = lo * (R(1) - xi) + hi * xi;  // mix(lo, hi, xi)
         if (technique < R(0.5)) {
             if (regular)
-                t = r_clamp(projection + perpendicular * r_tan(theta_a * (R(1) - xi) + theta_b * xi), R(0), end);
+                t = r_clamp(projection + perpendicular * r_tan(theta_a * (R(1) - xi) + theta_b * xi), lo, hi);
         } else {
             const R tau = tau_begin - r_log(r_max(R(1) - xi * conditional_mass, R(1e-7)));
-            const R split = fog_split(sc, ro, rd, end);
+            const R split = fog_split(sc, ro, rd, hi);
             const R first = fog_segment_tau(sc, ro, rd, R(0), split);
             t = tau < first ? fog_invert_segment(sc, ro, rd, R(0), split, tau)
-                            : fog_invert_segment(sc, ro, rd, split, end, tau - first);
+                            : fog_invert_segment(sc, ro, rd, split, hi, tau - first);
         }
         const V3<R> p = ro + rd * t;
         const R transmittance = r_exp(-fog_optical_depth(sc, ro, rd, t));
         const R sigma = fog_sigma(sc, p);
-        R angular_pdf = R(1) / end;
+        R angular_pdf = R(1) / (hi - lo);
         if (regular)
             angular_pdf = perpendicular / (span * (perpendicular * perpendicular + (t - projection) * (t - projection)));
         const R distance_pdf = R(0.5) * (angular_pdf + sigma * transmittance / interval_mass);
@@ -2039,12 +2222,12 @@ static V3<R> fog_segment_direct(const Scene<R>& sc, V3<R> ro, V3<R> rd, R end, u
         if (distance2 < R(1e-8)) continue;
         const R distance = r_sqrt(distance2);
         const V3<R> wi = to_light / distance;
-        const R cosine = area_normal(l).dot(-wi);
+        const R cosine = qn.dot(-wi);
         if (cosine <= R(0)) continue;
         const R vw = visible(p, wi, r_max(R(0), distance - r_max(R(1e-5), distance * R(1e-6))));
         if (!(vw > R(0))) continue;
         const R tr = vw * transmittance * r_exp(-fog_optical_depth(sc, p, wi, distance));
-        result = result + l.color * (sigma * tr * hg_phase(rd.dot(wi), g) /
+        result = result + emitter_radiance(l, -wi) * (sigma * tr * hg_phase(rd.dot(wi), g) /
                                      (probability * distance_pdf * area_direction_pdf(l, distance2, cosine)));
     }
     return result * sc.fog_color;
@@ -2286,7 +2469,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
         }
         V3<R> gn(0, 0, 0);
         if (h.hit) {
-            if (h.light_index != 0xffffffffu) gn = area_normal(sc.lights[h.light_index]);
+            if (h.light_index != 0xffffffffu) gn = emitter_normal(sc.lights[h.light_index], ro + rd * h.t);
             else {
                 const bool optical = refined && optics_on(material_optics(sc, h.sample.material));
                 gn = normal_tetra(g, ro + rd * h.t,
@@ -2341,7 +2524,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
         if (h.light_index != 0xffffffffu) {
             if (bounce == 0) {
                 first_depth = h.t;
-                V3<R> en = area_normal(sc.lights[h.light_index]);
+                V3<R> en = emitter_normal(sc.lights[h.light_index], ro + rd * h.t);
                 aux[0] = en.x; aux[1] = en.y; aux[2] = en.z; aux[3] = R(h.steps);
             }
             // after a fog scattering point its segment estimate already holds the emitters
@@ -2408,7 +2591,7 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                 R threshold = rnd<R>(&rng) * area_total;
                 R sum = 0;
                 for (uint32_t i = 0; i < sc.light_count; ++i) {
-                    if (sc.lights[i].kind != SF_LIGHT_AREA) continue;
+                    if (!is_emitter(sc.lights[i])) continue;
                     R w = area_weight(p_off, s.n, sc.lights[i]);
                     sum += w;
                     if (w > R(0)) {
@@ -2469,10 +2652,12 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R w = last ? R(1) : mis_power(pl, pb);
                     L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * w * (vw * fog_tr(ldir, extent)));
                 } else if (i == selected) {
+                    // sample_emitter: two numbers for a rectangle, three for a tube
                     R u1 = rnd<R>(&rng);
                     R u2 = rnd<R>(&rng);
-                    V3<R> q = l.a + l.b * (u1 - R(0.5)) + l.c * (u2 - R(0.5));
-                    V3<R> ln = area_normal(l);
+                    R u3 = l.kind == SF_LIGHT_TUBE ? rnd<R>(&rng) : R(0);
+                    V3<R> q, ln;
+                    sample_emitter_point(l, u1, u2, u3, &q, &ln);
                     V3<R> to_q = q - p_off;
                     R dist2 = to_q.dot(to_q);
                     if (dist2 < R(1e-8)) continue;
@@ -2487,7 +2672,8 @@ template <class R> PixelResult radiance(const Graph& g, const Scene<R>& sc, uint
                     R pl = (selected_weight / area_total) * area_direction_pdf(l, dist2, cos_l);
                     R pb = last ? R(0) : bsdf_pdf(s, v, ldir, p_spec);
                     R w = last ? R(1) : mis_power(pl, pb);
-                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * l.color * (vw * fog_tr(ldir, dist)) * w / pl);
+                    L = L + throughput * (brdf_eval(s, v, ldir) * nl * emitter_radiance(l, -ldir) * (vw * fog_tr(ldir, dist)) *
+                                          w / pl);
                 }
             }
         }

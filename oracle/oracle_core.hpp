@@ -219,6 +219,11 @@ template <class R> struct Light {
     uint32_t kind = 0;
     R cos_max = 1, energy = 0, peak = 0;
     const Panorama* pano = nullptr;  // HDRI: a = (cos, sin of the rotation, uniform), color.x = intensity
+    // a projector is an area light with its beam (cos inner, cos outer, tan outer);
+    // a tube (SF_LIGHT_TUBE): a = start, b = end, radius and length
+    bool projector = false;
+    R beam[3] = {0, 0, 0};
+    R radius = 0, length = 0;
 };
 template <class R> struct Coloring {
     uint32_t slot = 0xffff, n = 0;

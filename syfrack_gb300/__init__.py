@@ -8,7 +8,7 @@ from .graph import Graph, Kind, Link, Node
 from .render import (Batch, Canvas, CompiledGraph, DeSample, ExportSession, GpuContext, PlanarFractal, PreviewSession,
                      RenderOutput, Renderer, RenderSession, deep_zoom, escape2d)
 from .serve import ServeResult, Server
-from .scene import AreaLight, Camera, Finish, Material, RenderConfig, Scene, SurfaceVariation
+from .scene import AreaLight, Camera, Finish, Material, ProjectorLight, RenderConfig, Scene, SurfaceVariation, TubeLight
 from ._lib import SyfrackError
 
 __all__ = ["abi", "ron", "Batch", "Graph", "Kind", "Link", "Node", "Canvas", "CompiledGraph", "DeSample", "ExportSession",

@@ -77,7 +77,7 @@ class sf_material(C.Structure):
                 ("specular", C.c_float), ("emission", C.c_float * 3)]
 
 
-SF_LIGHT_AREA, SF_LIGHT_SUN, SF_LIGHT_ENVIRONMENT, SF_LIGHT_HDRI = 0, 1, 2, 3
+SF_LIGHT_AREA, SF_LIGHT_SUN, SF_LIGHT_ENVIRONMENT, SF_LIGHT_HDRI, SF_LIGHT_PROJECTOR, SF_LIGHT_TUBE = 0, 1, 2, 3, 4, 5
 SF_MAX_RAMP_STOPS = 16
 
 

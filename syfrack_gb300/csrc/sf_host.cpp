@@ -949,7 +949,18 @@ sf_status scene_check(const sf_scene_desc& d) {
     if (d.light_count > SF_MAX_LIGHTS || d.finish_count > SF_MAX_FINISHES)
         return fail(SF_ERR_INVALID, "too many lights or finishes");
     for (uint32_t i = 0; i < d.light_count; ++i) {
-        if (d.lights[i].kind > SF_LIGHT_HDRI) return fail(SF_ERR_UNSUPPORTED, "light kind not built on the device");
+        const sf_area_light& l = d.lights[i];
+        if (l.kind > SF_LIGHT_TUBE) return fail(SF_ERR_UNSUPPORTED, "light kind not built on the device");
+        // Light::visit_params bounds (light.rs:162-226)
+        if (l.kind == SF_LIGHT_PROJECTOR &&
+            !(l.direction[0] >= 0.1f && l.direction[1] <= 89.0f && l.direction[0] <= l.direction[1] - 0.01f))
+            return fail(SF_ERR_INVALID, "projector angles: inner in [0.1, outer - 0.01], outer at most 89 degrees");
+        if (l.kind == SF_LIGHT_TUBE) {
+            const float dx = l.edge_u[0] - l.center[0], dy = l.edge_u[1] - l.center[1], dz = l.edge_u[2] - l.center[2];
+            if (!(l.edge_v[0] >= 0.001f && l.edge_v[0] <= 1000.0f))
+                return fail(SF_ERR_INVALID, "tube radius must lie in [0.001, 1000]");
+            if (!(dx * dx + dy * dy + dz * dz > 0.0f)) return fail(SF_ERR_INVALID, "a tube needs distinct ends");
+        }
         if (d.lights[i].kind == SF_LIGHT_HDRI && !d.lights[i].environment)
             return fail(SF_ERR_INVALID, "an HDRI light needs a panorama (sf_environment_create)");
     }
@@ -997,7 +1008,10 @@ sf_status scene_check(const sf_scene_desc& d) {
 uint32_t shadow_slots_of(const sf_scene_desc& d) {
     uint32_t area = 0, sky = 0;
     for (uint32_t i = 0; i < std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS); ++i)
-        (d.lights[i].kind == SF_LIGHT_AREA ? area : sky)++;
+        (d.lights[i].kind == SF_LIGHT_AREA || d.lights[i].kind == SF_LIGHT_PROJECTOR ||
+                 d.lights[i].kind == SF_LIGHT_TUBE
+             ? area
+             : sky)++;
     return 1 + sky + (d.fog.density > 0.0f ? area : 0);
 }
 void light_dev(const sf_area_light& l, DevLight& o) {
@@ -1029,6 +1043,28 @@ void light_dev(const sf_area_light& l, DevLight& o) {
         for (int k = 0; k < 3; ++k) peak = std::max({peak, l.zenith[k], l.horizon[k], l.ground[k]});
         o.peak = peak;
         return;
+    }
+    if (l.kind == SF_LIGHT_TUBE) {
+        // GpuLight::from_light (uniforms.rs:717-729): start, end, radius, length
+        std::memcpy(o.a, l.center, 12);
+        std::memcpy(o.b, l.edge_u, 12);
+        std::memcpy(o.color, l.radiance, 12);
+        const float dx = l.edge_u[0] - l.center[0], dy = l.edge_u[1] - l.center[1], dz = l.edge_u[2] - l.center[2];
+        o.radius = l.edge_v[0];
+        o.length = sqrtf(dx * dx + dy * dy + dz * dz);
+        o.area = 2.0f * 3.14159265f * o.radius * (o.length + 2.0f * o.radius);  // emitter_area, lights.wgsl:80-85
+        o.n[1] = 1.0f;
+        o.lum = lum(l.radiance);
+        return;
+    }
+    // a projector is an area light with its beam (kind.y = 1, uniforms.rs:690-715)
+    o.kind = SF_LIGHT_AREA;
+    if (l.kind == SF_LIGHT_PROJECTOR) {
+        const float deg = 3.14159265f / 180.0f;
+        o.projector = 1;
+        o.beam[0] = cosf(l.direction[0] * deg);
+        o.beam[1] = cosf(l.direction[1] * deg);
+        o.beam[2] = tanf(l.direction[1] * deg);
     }
     std::memcpy(o.a, l.center, 12);
     std::memcpy(o.b, l.edge_u, 12);

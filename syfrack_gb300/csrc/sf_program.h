@@ -104,16 +104,22 @@ static_assert(SF_MAX_OPS <= 255, "leaf ranges are stored as bytes");
 // luminance, peak = their largest component.
 // SF_LIGHT_HDRI: a.x/a.y = cos/sin of the rotation, a.z = 1 for uniform sampling,
 // color.x = intensity, texels = the panorama's (rgb, cdf) rows of tw x th texels.
+// SF_LIGHT_AREA with projector = 1: a projector (GpuLight kind.y, uniforms.rs:671-716),
+// whose emission follows beam = (cos inner, cos outer, tan outer angle);
+// SF_LIGHT_TUBE (uniforms.rs:717-729): a capsule, a = start, b = end, radius, length.
 struct DevLight {
     float a[3], b[3], c[3], color[3];
     float n[3];          // safe_normalize(cross(b, c))
-    float area;          // |cross(b, c)|
+    float area;          // emitter_area: |cross(b, c)|, a tube's 2 pi r (length + 2 r)
     float inv_bb, inv_cc;// 1 / dot(b,b), 1 / dot(c,c)
     float lum;           // luminance(color)
     uint32_t kind;
     float cos_max, energy, peak;
     uint32_t tw, th;
     uint64_t texels;     // device address of float4 texels (HDRI)
+    uint32_t projector;
+    float beam[3];
+    float radius, length;
 };
 #define SF_MAX_RAMP 16
 

@@ -147,17 +147,195 @@ __device__ __forceinline__ float area_intersection(float3 ro, float3 rd, const D
     if (fabsf(x) > 0.5f || fabsf(y) > 0.5f) return 1e30f;
     return t;
 }
+// Emitters (lights.wgsl:5-168): rectangles, projectors (a rectangle with a beam) and
+// tubes (capsules) are hit by rays and sampled for next events. Their arithmetic is
+// rounded operation by operation (e_add .. e_mul, explicit fmaf), so the kernels that
+// inline it round it alike and the two integrators stay equal bit for bit.
+__device__ __forceinline__ float3 e_add(float3 a, float3 b) {
+    return mk3(__fadd_rn(a.x, b.x), __fadd_rn(a.y, b.y), __fadd_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 e_sub(float3 a, float3 b) {
+    return mk3(__fsub_rn(a.x, b.x), __fsub_rn(a.y, b.y), __fsub_rn(a.z, b.z));
+}
+__device__ __forceinline__ float3 e_mul(float3 a, float s) {
+    return mk3(__fmul_rn(a.x, s), __fmul_rn(a.y, s), __fmul_rn(a.z, s));
+}
+__device__ __forceinline__ bool is_emitter(const DevLight& l) {
+    return l.kind == SF_LIGHT_AREA || l.kind == SF_LIGHT_TUBE;
+}
+// beam_profile (lights.wgsl:11-16): the projector's smootherstep from its outer cone
+// to its inner one; 1 for the other emitters.
+__device__ __forceinline__ float beam_profile(const DevLight& l, float3 direction) {
+    if (!l.projector) return 1.0f;
+    const float cosine = dot3(ld3(l.n), direction);
+    const float t = fminf(
+        fmaxf(wdiv(__fsub_rn(cosine, l.beam[1]), fmaxf(__fsub_rn(l.beam[0], l.beam[1]), 1e-7f)), 0.0f), 1.0f);
+    return __fmul_rn(__fmul_rn(__fmul_rn(t, t), t), fmaf(t, fmaf(6.0f, t, -15.0f), 10.0f));
+}
+__device__ __forceinline__ float3 emitter_radiance(const DevLight& l, float3 direction) {
+    return e_mul(ld3(l.color), beam_profile(l, direction));
+}
+// cone_segment (lights.wgsl:23-68): the part of [0, end] of a ray inside the positive
+// cone of apex, axis and cosine; empty as (1, 0).
+static __device__ float2 cone_segment(float3 ro, float3 rd, float end, float3 apex, float3 axis, float cosine) {
+    float2 interval = make_float2(0.0f, end);
+    const float3 delta = e_sub(ro, apex);
+    const float axial = dot3(delta, axis), slope = dot3(rd, axis);
+    if (fabsf(slope) < 1e-8f) {
+        if (axial < 0.0f) return make_float2(1.0f, 0.0f);
+    } else {
+        const float crossing = wdiv(-axial, slope);
+        if (slope > 0.0f) interval.x = fmaxf(interval.x, crossing);
+        else interval.y = fminf(interval.y, crossing);
+    }
+    if (interval.y <= interval.x) return make_float2(1.0f, 0.0f);
+    const float c2 = __fmul_rn(cosine, cosine);
+    const float s2 = __fmul_rn(__fsub_rn(1.0f, cosine), __fadd_rn(1.0f, cosine));
+    const float3 radial = e_sub(delta, e_mul(axis, axial));
+    const float3 radial_slope = e_sub(rd, e_mul(axis, slope));
+    const float a = __fsub_rn(__fmul_rn(__fmul_rn(s2, slope), slope), __fmul_rn(c2, dot3(radial_slope, radial_slope)));
+    const float b = __fmul_rn(2.0f, __fsub_rn(__fmul_rn(__fmul_rn(s2, axial), slope),
+                                              __fmul_rn(c2, dot3(radial, radial_slope))));
+    const float c = __fsub_rn(__fmul_rn(__fmul_rn(s2, axial), axial), __fmul_rn(c2, dot3(radial, radial)));
+    if (fabsf(a) < 1e-12f) {
+        if (fabsf(b) < 1e-12f) {
+            if (c < 0.0f) return make_float2(1.0f, 0.0f);
+        } else if (b > 0.0f) {
+            interval.x = fmaxf(interval.x, wdiv(-c, b));
+        } else {
+            interval.y = fminf(interval.y, wdiv(-c, b));
+        }
+        return interval;
+    }
+    const float discriminant = __fsub_rn(__fmul_rn(b, b), __fmul_rn(__fmul_rn(4.0f, a), c));
+    if (discriminant <= 0.0f) {
+        const float middle = __fmul_rn(__fadd_rn(interval.x, interval.y), 0.5f);
+        if (__fadd_rn(__fmul_rn(__fadd_rn(__fmul_rn(a, middle), b), middle), c) < 0.0f) return make_float2(1.0f, 0.0f);
+        return interval;
+    }
+    const float root = wsqrt(discriminant);
+    const float q = __fmul_rn(-0.5f, __fadd_rn(b, b >= 0.0f ? root : -root));
+    const float r0 = wdiv(q, a), r1 = wdiv(c, q);
+    const float low = fminf(r0, r1), high = fmaxf(r0, r1);
+    if (a < 0.0f) return make_float2(fmaxf(interval.x, low), fminf(interval.y, high));
+    if (fminf(interval.y, low) > interval.x) return make_float2(interval.x, fminf(interval.y, low));
+    return make_float2(fmaxf(interval.x, high), interval.y);
+}
+// projector_bound_apex (lights.wgsl:72-75): the apex of a cone bounding the whole
+// rectangle's beam, moved back by its half diagonal over tan(outer).
+__device__ __forceinline__ float3 projector_bound_apex(const DevLight& l) {
+    const float3 d = e_add(ld3(l.b), ld3(l.c));
+    const float radius = __fmul_rn(0.5f, wsqrt(dot3(d, d)));
+    return e_sub(ld3(l.a), e_mul(ld3(l.n), wdiv(radius, l.beam[2])));
+}
+// emitter_normal (lights.wgsl:87-94): a tube's normal is radial from its axis.
+__device__ __forceinline__ float3 emitter_normal(const DevLight& l, float3 point) {
+    if (l.kind != SF_LIGHT_TUBE) return ld3(l.n);
+    const float3 axis = e_sub(ld3(l.b), ld3(l.a));
+    const float3 pa = e_sub(point, ld3(l.a));
+    const float t = fminf(fmaxf(wdiv(dot3(pa, axis), dot3(axis, axis)), 0.0f), 1.0f);
+    return wsafe_normalize(e_sub(pa, e_mul(axis, t)));
+}
+// tube_intersection (lights.wgsl:97-129): the closest hit of the cylinder and its two
+// spherical caps.
+static __device__ float tube_intersection(float3 ro, float3 rd, const DevLight& l) {
+    const float3 A = ld3(l.a), B = ld3(l.b);
+    const float r = l.radius, len = l.length;
+    const float r2 = __fmul_rn(r, r);
+    const float3 axis = e_mul(e_sub(B, A), wdiv(1.0f, len));
+    const float3 oa = e_sub(ro, A);
+    const float axial_ray = dot3(axis, rd), axial_origin = dot3(axis, oa);
+    const float3 side = cross3(axis, rd);
+    const float a = dot3(side, side);
+    float nearest = 1e30f;
+    if (a > 1e-10f) {
+        const float perpendicular = wdiv(dot3(oa, side), wsqrt(a));
+        const float h = __fsub_rn(r2, __fmul_rn(perpendicular, perpendicular));
+        if (h < 0.0f) return nearest;
+        const float middle = wdiv(-__fsub_rn(dot3(rd, oa), __fmul_rn(axial_origin, axial_ray)), a);
+        const float root = wsqrt(wdiv(fmaxf(0.0f, h), a));
+        for (int i = 0; i < 2; ++i) {
+            const float t = __fadd_rn(middle, i == 1 ? root : -root);
+            const float y = __fadd_rn(axial_origin, __fmul_rn(t, axial_ray));
+            if (t > 1e-6f && y >= 0.0f && y <= len) nearest = fminf(nearest, t);
+        }
+    } else {
+        const float3 radial = e_sub(oa, e_mul(axis, axial_origin));
+        if (dot3(radial, radial) > r2) return nearest;
+    }
+    for (int cap = 0; cap < 2; ++cap) {
+        const float3 oc = e_sub(ro, cap == 1 ? B : A);
+        const float projection = dot3(oc, rd);
+        const float3 closest = e_sub(oc, e_mul(rd, projection));
+        const float h = __fsub_rn(r2, dot3(closest, closest));
+        if (h < 0.0f) continue;
+        const float sh = wsqrt(h);
+        for (int i = 0; i < 2; ++i) {
+            const float t = __fadd_rn(-projection, i == 1 ? sh : -sh);
+            const float y = dot3(e_sub(e_add(ro, e_mul(rd, t)), A), axis);
+            const bool on_cap = cap == 1 ? y >= len : y <= 0.0f;
+            if (t > 1e-6f && on_cap) nearest = fminf(nearest, t);
+        }
+    }
+    return nearest;
+}
+__device__ __forceinline__ float emitter_intersection(float3 ro, float3 rd, const DevLight& l) {
+    return l.kind == SF_LIGHT_TUBE ? tube_intersection(ro, rd, l) : area_intersection(ro, rd, l);
+}
+// sample_emitter_point (lights.wgsl:143-160): a rectangle's point from (u, v); a
+// tube's from (choice, polar, phi): its cylinder by area, else one of its caps.
+struct EmitterPoint {
+    float3 position, normal;
+};
+__device__ __forceinline__ void tangent_frame(float3 n, float3& t, float3& bt);
+static __device__ EmitterPoint sample_emitter_point(const DevLight& l, float u, float v, float w) {
+    EmitterPoint e;
+    if (l.kind != SF_LIGHT_TUBE) {
+        e.position = e_add(e_add(ld3(l.a), e_mul(ld3(l.b), __fsub_rn(u, 0.5f))), e_mul(ld3(l.c), __fsub_rn(v, 0.5f)));
+        e.normal = ld3(l.n);
+        return e;
+    }
+    const float3 A = ld3(l.a), B = ld3(l.b);
+    const float3 axis = e_mul(e_sub(B, A), wdiv(1.0f, l.length));
+    float3 t, bt;
+    tangent_frame(axis, t, bt);
+    float sp, cp;
+    sincosf(__fmul_rn(2.0f * SF_PI, w), &sp, &cp);
+    const float3 radial = e_add(e_mul(t, cp), e_mul(bt, sp));
+    const float cylinder_fraction = wdiv(l.length, __fadd_rn(l.length, __fmul_rn(2.0f, l.radius)));
+    if (u < cylinder_fraction) {
+        const float g = __fsub_rn(1.0f, v);  // mix(a, b, polar)
+        e.position = e_add(e_add(e_mul(A, g), e_mul(B, v)), e_mul(radial, l.radius));
+        e.normal = radial;
+        return e;
+    }
+    const bool top = wdiv(__fsub_rn(u, cylinder_fraction), __fsub_rn(1.0f, cylinder_fraction)) >= 0.5f;
+    const float3 n = e_add(e_mul(radial, wsqrt(fmaxf(0.0f, __fsub_rn(1.0f, __fmul_rn(v, v))))),
+                           e_mul(axis, top ? v : -v));
+    e.position = e_add(top ? B : A, e_mul(n, l.radius));
+    e.normal = n;
+    return e;
+}
+// area_weight (lights.wgsl:285-302): the selection weight of an emitter at p.
 __device__ __forceinline__ float area_weight(float3 p, float3 n, const DevLight& l) {
-    float3 to_light = ld3(l.a) - p;
+    const bool tube = l.kind == SF_LIGHT_TUBE;
+    const float3 center = tube ? (ld3(l.a) + ld3(l.b)) * 0.5f : ld3(l.a);
+    float3 to_light = center - p;
     float dist2 = fmaxf(dot3(to_light, to_light), 1e-6f);
     float3 dir = to_light * rsqrtf(dist2);
-    float facing = fmaxf(dot3(ld3(l.n), -dir), 0.0f);
+    float facing = tube ? 0.25f : fmaxf(dot3(ld3(l.n), -dir), 0.0f);
+    if (l.projector) {
+        const float3 delta = p - projector_bound_apex(l);
+        const float axial = dot3(delta, ld3(l.n));
+        if (axial < 0.0f || axial * axial < l.beam[1] * l.beam[1] * dot3(delta, delta)) return 0.0f;
+        facing *= fmaxf(0.025f, beam_profile(l, -dir));
+    }
     return wdiv(l.lum * l.area * facing * fmaxf(dot3(n, dir), 0.15f), dist2);
 }
 __device__ __forceinline__ float area_total_weight(const DevScene& S, float3 p, float3 n) {
     float total = 0.0f;
     for (uint32_t i = 0; i < S.light_count; ++i)
-        if (S.lights[i].kind == SF_LIGHT_AREA) total += area_weight(p, n, S.lights[i]);
+        if (is_emitter(S.lights[i])) total += area_weight(p, n, S.lights[i]);
     return total;
 }
 __device__ __forceinline__ float mis_power(float a, float b) {
@@ -172,10 +350,10 @@ static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, 
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
         const DevLight& l = S.lights[i];
-        if (l.kind != SF_LIGHT_AREA) continue;
-        float cos_l = dot3(ld3(l.n), -rd);
+        if (!is_emitter(l)) continue;
+        float cos_l = dot3(emitter_normal(l, e_add(ro, e_mul(rd, distance))), -rd);
         if (cos_l <= 0.0f) continue;
-        float t = area_intersection(ro, rd, l);
+        float t = emitter_intersection(ro, rd, l);
         if (fabsf(t - distance) > fmaxf(1e-6f, distance * 1e-6f)) continue;
         float w = 1.0f;
         if (use_mis) {
@@ -185,7 +363,7 @@ static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, 
             pl = pl * selection;
             w = mis_power(prev_pdf, pl);
         }
-        L = L + ld3(l.color) * w;
+        L = L + emitter_radiance(l, -rd) * w;
     }
     return L;
 }
@@ -194,8 +372,8 @@ __device__ __forceinline__ float nearest_emitter(const DevScene& S, float3 ro, f
     float nearest = t_end;
     li = SF_NO_LIGHT;
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        if (S.lights[i].kind != SF_LIGHT_AREA) continue;
-        float t = area_intersection(ro, rd, S.lights[i]);
+        if (!is_emitter(S.lights[i])) continue;
+        float t = emitter_intersection(ro, rd, S.lights[i]);
         if (t < nearest) { nearest = t; li = i; }
     }
     return nearest;
@@ -717,11 +895,17 @@ __device__ __forceinline__ float volume_coordinate(uint32_t sample_index, uint32
     const float v = value + shift;
     return v - floorf(v);
 }
-// fog_segment_weight (pathtrace.wgsl:621-633) for a rectangle: max-channel power over
-// the distance from the segment's closest point to the light's centre.
-__device__ __forceinline__ float fog_segment_weight(float3 ro, float3 rd, float end, const DevLight& l) {
-    const float3 center = ld3(l.a);
-    const float along = fminf(fmaxf(dot3(center - ro, rd), 0.0f), end);
+// fog_segment_weight (pathtrace.wgsl:621-633): max-channel power over the distance
+// from the segment's closest point to the emitter's centre (a tube's midpoint), on the
+// part of the segment inside a projector's bounding cone.
+static __device__ float fog_segment_weight(float3 ro, float3 rd, float end, const DevLight& l) {
+    const float3 center = l.kind == SF_LIGHT_TUBE ? (ld3(l.a) + ld3(l.b)) * 0.5f : ld3(l.a);
+    float2 interval = make_float2(0.0f, end);
+    if (l.projector) {
+        interval = cone_segment(ro, rd, end, projector_bound_apex(l), ld3(l.n), l.beam[1]);
+        if (interval.y <= interval.x) return 0.0f;
+    }
+    const float along = fminf(fmaxf(dot3(center - ro, rd), interval.x), interval.y);
     const float3 delta = center - (ro + rd * along);
     return wdiv(fmaxf(fmaxf(l.color[0], l.color[1]), l.color[2]) * l.area, dot3(delta, delta) + l.area);
 }
@@ -746,25 +930,34 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
     if (tau_end <= 0.0f) return;
     float total = 0.0f;
     for (uint32_t i = 0; i < S.light_count; ++i)
-        if (S.lights[i].kind == SF_LIGHT_AREA) total += fog_segment_weight(ro, rd, end, S.lights[i]);
+        if (is_emitter(S.lights[i])) total += fog_segment_weight(ro, rd, end, S.lights[i]);
     const float g = S.fog[3];
     for (uint32_t i = 0; i < S.light_count; ++i) {
         const DevLight& l = S.lights[i];
-        if (l.kind != SF_LIGHT_AREA) continue;
+        if (!is_emitter(l)) continue;
         const float probability = volume_light_probability(fog_segment_weight(ro, rd, end, l), total);
         const uint32_t stream = pcg(point_stream ^ (i * 0x85ebca6bu));
         float selection = rnd(rng);
         if (primary) selection = volume_coordinate(point_index, 5u, stream);
         if (probability <= 0.0f || selection >= probability) continue;
+        // sample_emitter draws two numbers for a rectangle, three for a tube
         float u1 = rnd(rng);
         float u2 = rnd(rng);
+        float u3 = l.kind == SF_LIGHT_TUBE ? rnd(rng) : 0.0f;
         if (primary) {
             u1 = volume_coordinate(point_index, 0u, stream);
             u2 = volume_coordinate(point_index, 1u, stream);
+            u3 = volume_coordinate(point_index, 2u, stream);
         }
-        const float3 q = ld3(l.a) + ld3(l.b) * (u1 - 0.5f) + ld3(l.c) * (u2 - 0.5f);
-        const float tau_begin = fog_optical_depth(S, ro, rd, 0.0f);
-        const float tau_finish = fog_optical_depth(S, ro, rd, end);
+        const EmitterPoint emitter = sample_emitter_point(l, u1, u2, u3);
+        const float3 q = emitter.position;
+        float2 interval = make_float2(0.0f, end);
+        if (l.projector) {
+            interval = cone_segment(ro, rd, end, q, ld3(l.n), l.beam[1]);
+            if (interval.y <= interval.x) continue;
+        }
+        const float tau_begin = fog_optical_depth(S, ro, rd, interval.x);
+        const float tau_finish = fog_optical_depth(S, ro, rd, interval.y);
         const float tau_span = fmaxf(0.0f, tau_finish - tau_begin);
         if (tau_span <= 0.0f) continue;
         float conditional_mass = 1.0f - expf(-tau_span);
@@ -775,8 +968,8 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
         const float projection = dot3(delta, rd);
         const float3 perp_v = delta - rd * projection;
         const float perpendicular = wsqrt(dot3(perp_v, perp_v));
-        const float theta_a = atan2f(0.0f - projection, fmaxf(perpendicular, 1e-6f));
-        const float theta_b = atan2f(end - projection, fmaxf(perpendicular, 1e-6f));
+        const float theta_a = atan2f(interval.x - projection, fmaxf(perpendicular, 1e-6f));
+        const float theta_b = atan2f(interval.y - projection, fmaxf(perpendicular, 1e-6f));
         const float span = theta_b - theta_a;
         const bool regular = perpendicular > 1e-4f && span > 1e-5f;
         float xi = rnd(rng);
@@ -785,20 +978,21 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
             xi = volume_coordinate(point_index, 3u, stream);
             technique = volume_coordinate(point_index, 4u, stream);
         }
-        float t = mixf(0.0f, end, xi);
+        float t = mixf(interval.x, interval.y, xi);
         if (technique < 0.5f) {
-            if (regular) t = fminf(fmaxf(projection + perpendicular * tanf(mixf(theta_a, theta_b, xi)), 0.0f), end);
+            if (regular)
+                t = fminf(fmaxf(projection + perpendicular * tanf(mixf(theta_a, theta_b, xi)), interval.x), interval.y);
         } else {
             const float tau = tau_begin - logf(fmaxf(1.0f - xi * conditional_mass, 1e-7f));
-            const float split = fog_split(S, ro, rd, end);
+            const float split = fog_split(S, ro, rd, interval.y);
             const float first = fog_segment_tau(S, ro, rd, 0.0f, split);
             t = tau < first ? fog_invert_segment(S, ro, rd, 0.0f, split, tau)
-                            : fog_invert_segment(S, ro, rd, split, end, tau - first);
+                            : fog_invert_segment(S, ro, rd, split, interval.y, tau - first);
         }
         const float3 p = ro + rd * t;
         const float transmittance = expf(-fog_optical_depth(S, ro, rd, t));
         const float sigma = fog_sigma(S, p);
-        float angular_pdf = wdiv(1.0f, end - 0.0f);
+        float angular_pdf = wdiv(1.0f, interval.y - interval.x);
         if (regular) {
             const float dt = t - projection;
             angular_pdf = wdiv(perpendicular, span * (perpendicular * perpendicular + dt * dt));
@@ -809,7 +1003,7 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
         if (distance2 < 1e-8f) continue;
         const float distance = wsqrt(distance2);
         const float3 wi = to_light * wdiv(1.0f, distance);
-        const float cosine = dot3(ld3(l.n), -wi);
+        const float cosine = dot3(emitter.normal, -wi);
         if (cosine <= 0.0f) continue;
         const float tr = transmittance * expf(-fog_optical_depth(S, p, wi, distance));
         const float light_pdf = wdiv(distance2, fmaxf(l.area * cosine, 1e-20f));
@@ -818,7 +1012,7 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
         sh.o = p;
         sh.dir = wi;
         sh.t_end = fmaxf(0.0f, distance - fmaxf(1e-5f, distance * 1e-6f));
-        sh.contrib = tp * ((ld3(l.color) * scale) * color);
+        sh.contrib = tp * ((emitter_radiance(l, -wi) * scale) * color);
         sh.volume = primary;  // pathtrace.wgsl:985: bounce 0's direct volume
         emit(sh);
     }
@@ -983,7 +1177,9 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     }
     if (h.hit && ps.bounce == 0 && first_depth) {
         *first_depth = h.t;
-        const float3 en = h.light_index != SF_NO_LIGHT ? ld3(S.lights[h.light_index].n) : h.n;
+        const float3 en = h.light_index != SF_NO_LIGHT
+                              ? emitter_normal(S.lights[h.light_index], e_add(ps.o, e_mul(ps.d, h.t)))
+                              : h.n;
         *first_aux = make_float4(en.x, en.y, en.z, float(h.steps));
     }
     const bool fog = S.fog[0] > 0.0f && !(RICH && ps.solid_medium);
@@ -1100,7 +1296,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
         float threshold = rnd(ps.rng) * area_total;
         float sum = 0.0f;
         for (uint32_t i = 0; i < S.light_count; ++i) {
-            if (S.lights[i].kind != SF_LIGHT_AREA) continue;
+            if (!is_emitter(S.lights[i])) continue;
             float w = area_weight(p_off, s.n, S.lights[i]);
             sum += w;
             if (w > 0.0f) {
@@ -1166,10 +1362,13 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             sh.contrib = ps.tp * (brdf_eval(s, v, ldir) * nl * ld3(l.color) * w * tr);
             emit(sh);
         } else if (i == selected) {
+            // sample_emitter: two numbers for a rectangle, three for a tube
             float u1 = rnd(ps.rng);
             float u2 = rnd(ps.rng);
-            float3 q = ld3(l.a) + ld3(l.b) * (u1 - 0.5f) + ld3(l.c) * (u2 - 0.5f);
-            float3 ln = ld3(l.n);
+            float u3 = l.kind == SF_LIGHT_TUBE ? rnd(ps.rng) : 0.0f;
+            const EmitterPoint emitter = sample_emitter_point(l, u1, u2, u3);
+            float3 q = emitter.position;
+            float3 ln = emitter.normal;
             float3 to_q = q - p_off;
             float dist2 = dot3(to_q, to_q);
             if (dist2 < 1e-8f) continue;
@@ -1183,7 +1382,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
             float pb = last ? 0.0f : bsdf_pdf(s, v, ldir, p_spec);
             float w = last ? 1.0f : mis_power(pl, pb);
             const float tr = fog ? fog_transmittance(S, p_off, ldir, dist) : 1.0f;
-            float3 Ld = brdf_eval(s, v, ldir) * nl * ld3(l.color) * tr * wdiv(w, pl);
+            float3 Ld = brdf_eval(s, v, ldir) * nl * emitter_radiance(l, -ldir) * tr * wdiv(w, pl);
             ShadowReq sh;
             sh.o = p_off;
             sh.dir = ldir;

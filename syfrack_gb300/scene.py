@@ -110,6 +110,42 @@ class AreaLight:
         return out
 
 
+@dataclass
+class ProjectorLight(AreaLight):
+    """Light::Projector{position, normal, size, color, intensity, inner_angle, outer_angle}:
+    an area light whose emission about its normal is full within inner_angle degrees
+    and none beyond outer_angle (light.rs:88-97, lights.wgsl:11-16)."""
+    inner_angle: float = 10.0
+    outer_angle: float = 18.0
+
+    def packed(self) -> abi.sf_area_light:
+        out = super().packed()
+        out.kind = abi.SF_LIGHT_PROJECTOR
+        out.direction[0] = self.inner_angle
+        out.direction[1] = self.outer_angle
+        return out
+
+
+@dataclass
+class TubeLight:
+    """Light::Tube{start, end, radius, color, intensity}: a capsule emitter (light.rs:99-105,
+    GpuLight::from_light uniforms.rs:717-729)."""
+    start: tuple = (-0.5, 2.0, 0.0)
+    end: tuple = (0.5, 2.0, 0.0)
+    radius: float = 0.05
+    color: tuple = (1.0, 1.0, 1.0)
+    intensity: float = 10.0
+
+    def packed(self) -> abi.sf_area_light:
+        out = abi.sf_area_light()
+        out.kind = abi.SF_LIGHT_TUBE
+        out.center[:] = [float(x) for x in _v(self.start)]
+        out.edge_u[:] = [float(x) for x in _v(self.end)]
+        out.edge_v[0] = self.radius
+        out.radiance[:] = [float(f32(c) * f32(self.intensity)) for c in _color(self.color)]
+        return out
+
+
 def kelvin_to_linear(kelvin: float):
     """Color::Kelvin (light.rs:28-58): Tanner Helland's black-body approximation,
     sRGB to linear, normalised so the brightest channel is 1 (binary32)."""
@@ -544,7 +580,7 @@ def _rgb(c):
 
 def scene_from_ron_value(v) -> Scene:
     """Scene (crates/syfrack-core/src/scene/mod.rs) from a parsed scenes/*.ron value: the
-    graph fractal, Orbit/Free camera, Sun/Environment/Area lights, the material with its
+    graph fractal, Orbit/Free camera, Sun/Environment/Area/Projector/Tube lights, the material with its
     Trap/iteration/normal colouring, and the seed. Fog, ocean, textures, finishes with
     detail and HDRI are not on this path and raise ValueError when enabled."""
     from . import ron
@@ -577,6 +613,13 @@ def scene_from_ron_value(v) -> Scene:
         elif kind == "Area":
             lights.append(AreaLight(tuple(ron.vec(l["position"])), tuple(ron.vec(l["normal"])),
                                     tuple(ron.vec(l["size"])), _rgb(l["color"]), float(l["intensity"])))
+        elif kind == "Projector":
+            lights.append(ProjectorLight(tuple(ron.vec(l["position"])), tuple(ron.vec(l["normal"])),
+                                         tuple(ron.vec(l["size"])), _rgb(l["color"]), float(l["intensity"]),
+                                         float(l["inner_angle"]), float(l["outer_angle"])))
+        elif kind == "Tube":
+            lights.append(TubeLight(tuple(ron.vec(l["start"])), tuple(ron.vec(l["end"])), float(l["radius"]),
+                                    _rgb(l["color"]), float(l["intensity"])))
         else:
             raise ValueError(f"{kind} lights are not on this path")
     m = v["material"]
