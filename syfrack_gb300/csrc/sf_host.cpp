@@ -50,7 +50,7 @@ constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
 constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
 // 1.1: sf_film_planes.color; 1.2: sf_render_config.hit_epsilon; 1.3: finish details, orbit
 // colouring, optics and textures in sf_scene_desc
-constexpr uint32_t ABI_VERSION = (1u << 16) | 4u;
+constexpr uint32_t ABI_VERSION = (1u << 16) | 5u;
 
 // ------------------------------------------------------------------ graph preparation
 

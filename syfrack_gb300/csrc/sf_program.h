@@ -14,7 +14,7 @@
 #pragma once
 #include <stdint.h>
 
-#define SF_MAX_OPS 96
+#define SF_MAX_OPS 255
 #define SF_MAX_LOOP_DEPTH 4
 #define SF_MAX_DIST_STACK 6
 #define SF_MAX_INST_DEPTH 3  // nested Instances levels (MAX_DEPTH, graph/mod.rs:41)

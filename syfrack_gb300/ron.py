@@ -33,7 +33,8 @@ class Tuple:
 
 
 _NUM = re.compile(r"[+-]?(?:inf|NaN|(?:\d[\d_]*(?:\.[\d_]*)?|\.\d[\d_]*)(?:[eE][+-]?\d+)?)")
-_IDENT = re.compile(r"[A-Za-z_][A-Za-z0-9_]*")
+# an identifier, or a raw one (r#name: the name itself, never a keyword such as None)
+_IDENT = re.compile(r"(?:r#)?[A-Za-z_][A-Za-z0-9_]*")
 
 
 class _Parser:
@@ -118,6 +119,11 @@ class _Parser:
             raise RonError(f"unexpected {self.s[self.i:self.i + 20]!r} at {self.i}")
         name = m.group(0)
         self.i = m.end()
+        if name.startswith("r#"):
+            name = name[2:]
+            if self.i < len(self.s) and self.s[self.i] == "(":
+                return self.parens(name)
+            return Unit(name)
         if name == "true":
             return True
         if name == "false":
@@ -197,7 +203,7 @@ class _Parser:
                     raise RonError(f"expected field name at {self.i}")
                 self.i = m.end()
                 self.expect(":")
-                d[m.group(0)] = self.value()
+                d[m.group(0).removeprefix("r#")] = self.value()
         items = []
         while True:
             self.skip()

@@ -578,13 +578,126 @@ def _rgb(c):
     return tuple(ron.vec(c))
 
 
-def scene_from_ron_value(v) -> Scene:
-    """Scene (crates/syfrack-core/src/scene/mod.rs) from a parsed scenes/*.ron value: the
-    graph fractal, Orbit/Free camera, Sun/Environment/Area/Projector/Tube lights, the material with its
-    Trap/iteration/normal colouring, and the seed. Fog, ocean, textures, finishes with
-    detail and HDRI are not on this path and raise ValueError when enabled."""
+def _is_none(x):
     from . import ron
 
+    return x is None or (isinstance(x, ron.Unit) and x.name == "None")
+
+
+def _ramp_from_ron(r) -> Ramp:
+    """Ramp (palette.rs:74-100) with its serde defaults."""
+    from . import ron
+
+    if _is_none(r) or r is None:
+        return Ramp()
+    interp = r.get("interpolation")
+    return Ramp(stops=[tuple(ron.vec(x)) for x in r.get("stops", [])] or Ramp().stops,
+                positions=[float(x) for x in r.get("positions", [])], cyclic=bool(r.get("cyclic", False)),
+                frequency=float(r.get("frequency", 1.0)), phase=float(r.get("phase", 0.0)),
+                gamma=float(r.get("gamma", 1.0)), smooth=isinstance(interp, ron.Unit) and interp.name == "Smooth")
+
+
+def _orbit_from_ron(o) -> OrbitColoring:
+    """OrbitColoring (material.rs:18-40), serde(default)."""
+    from . import ron
+
+    return OrbitColoring(traps=tuple(float(x) for x in ron.vec(o.get("traps", (1.0, 0.0, 0.0, 0.0)))),
+                         iterations=float(o.get("iterations", 0.0)), normal=float(o.get("normal", 0.0)),
+                         logarithmic=float(o.get("logarithmic", 0.0)))
+
+
+def _coloring_from_ron(c):
+    """Coloring::{None, Trap{slot, ramp}, Orbit{channels, ramp}} (material.rs:12-16)."""
+    if _is_none(c):
+        return None
+    if isinstance(c, dict) and c.get("__name__") == "Trap":
+        return Coloring(int(c["slot"]), _ramp_from_ron(c.get("ramp")))
+    if isinstance(c, dict) and c.get("__name__") == "Orbit":
+        return Coloring(6, _ramp_from_ron(c.get("ramp")), orbit=_orbit_from_ron(c.get("channels", {})))
+    raise ValueError(f"colouring {c!r} is not on this path")
+
+
+def _optics_from_ron(o):
+    """Option<Optics> (optics.rs:7-38)."""
+    from . import ron
+
+    if _is_none(o):
+        return None
+    return Optics(opacity=float(o["opacity"]), transmission=float(o["transmission"]), ior=float(o["ior"]),
+                  thin_walled=bool(o["thin_walled"]), absorption_color=tuple(ron.vec(o["absorption_color"])),
+                  absorption_distance=float(o["absorption_distance"]), subsurface=float(o["subsurface"]),
+                  subsurface_color=tuple(ron.vec(o["subsurface_color"])),
+                  subsurface_radius=float(o["subsurface_radius"]))
+
+
+def _detail_from_ron(d):
+    """Option<FinishDetail> (material.rs:200-224)."""
+    from . import ron
+
+    if _is_none(d):
+        return None
+    pattern = d["pattern"].name if isinstance(d["pattern"], ron.Unit) else str(d["pattern"])
+    return FinishDetail(pattern=pattern, seed=int(d["seed"]), scale=float(d["scale"]), strength=float(d["strength"]),
+                        bump=float(d["bump"]), roughness_delta=float(d["roughness_delta"]),
+                        tint=tuple(ron.vec(d["tint"])))
+
+
+def _texture_from_ron(t):
+    """Option<FractalTexture> (texture.rs:62-136) with its serde defaults."""
+    from . import ron
+
+    if _is_none(t):
+        return None
+    if not _is_none(t.get("planar")):
+        raise ValueError("planar textures are not on this path")
+    ch = t["channel"]
+    if isinstance(ch, (ron.Unit, str)):
+        channel = {"Distance": ("distance",), "Iterations": ("iterations",)}[getattr(ch, "name", ch)]
+    elif ch.get("__name__") == "Trap":
+        channel = ("trap", int(ch["slot"]))
+    else:
+        channel = ("orbit", _orbit_from_ron(ch.get("channels", {})))
+    fan, mask = t.get("fan"), t.get("mask")
+    return FractalTexture(
+        graph=Graph.from_ron_value(t["graph"]), channel=channel, scale=float(t["scale"]),
+        offset=tuple(ron.vec(t["offset"])), rotation=tuple(ron.vec(t["rotation"])), octaves=int(t["octaves"]),
+        contrast=float(t["contrast"]), ramp=_ramp_from_ron(t.get("ramp")), strength=float(t["strength"]),
+        roughness=float(t["roughness"]), bump=float(t["bump"]), parallax=float(t.get("parallax", 0.0)),
+        parallax_steps=int(t.get("parallax_steps", 8)),
+        fan=None if _is_none(fan) else (*[float(x) for x in ron.vec(fan["period"])], int(fan["rays"])),
+        mask=None if _is_none(mask) else (int(mask["slot"]), float(mask["value"]), float(mask["width"])))
+
+
+def _material_from_ron(m) -> "Material":
+    """Material (material.rs:136-158): colouring, texture, surface variation, finishes
+    (Finish, material.rs:160-176) and optics."""
+    from . import ron
+
+    sv = m.get("surface")
+    surface = None if _is_none(sv) else SurfaceVariation(slot=int(sv["slot"]), roughness=tuple(ron.vec(sv["roughness"])),
+                                                        metallic=tuple(ron.vec(sv["metallic"])))
+    finishes = [Finish(albedo=tuple(ron.vec(f["albedo"])), roughness=float(f["roughness"]),
+                       metallic=float(f["metallic"]), specular=float(f["specular"]),
+                       emission=tuple(ron.vec(f.get("emission", (0.0, 0.0, 0.0)))),
+                       detail=_detail_from_ron(f.get("detail")), optics=_optics_from_ron(f.get("optics")))
+                for f in (m.get("finishes") or [])]
+    return Material(albedo=tuple(ron.vec(m["albedo"])), roughness=float(m["roughness"]),
+                    metallic=float(m["metallic"]), specular=float(m["specular"]),
+                    optics=_optics_from_ron(m.get("optics")), finishes=finishes, surface=surface,
+                    coloring=_coloring_from_ron(m.get("coloring")), texture=_texture_from_ron(m.get("texture")))
+
+
+def scene_from_ron_value(v) -> Scene:
+    """Scene (crates/syfrack-core/src/scene/mod.rs) from a parsed scenes/*.ron value: the
+    graph fractal, Orbit/Free camera, Sun/Environment/Area/Projector/Tube lights, the
+    material (colouring, surface variation, volumetric texture, finishes with their
+    details and optics, optics), the height fog, cavity darkness and the seed. Creation
+    scenes, planar textures and HDRI panoramas (files) are not read and raise
+    ValueError."""
+    from . import ron
+
+    if "fractal" not in v:
+        raise ValueError("creation scenes (a creation graph instead of a fractal) are not on this path")
     frac = v["fractal"]
     if not (isinstance(frac, ron.Tuple) and frac.name == "Graph"):
         raise ValueError("only graph fractals are on this path")
@@ -622,21 +735,7 @@ def scene_from_ron_value(v) -> Scene:
                                     _rgb(l["color"]), float(l["intensity"])))
         else:
             raise ValueError(f"{kind} lights are not on this path")
-    m = v["material"]
-    col = None
-    c = m.get("coloring")
-    if isinstance(c, dict) and c.get("__name__") == "Trap":
-        r = c.get("ramp", {})
-        ramp = Ramp(stops=[tuple(ron.vec(s)) for s in r.get("stops", [])] or Ramp().stops,
-                    positions=[float(x) for x in r.get("positions", [])], cyclic=bool(r.get("cyclic", False)),
-                    frequency=float(r.get("frequency", 1.0)), phase=float(r.get("phase", 0.0)),
-                    gamma=float(r.get("gamma", 1.0)),
-                    smooth=isinstance(r.get("interpolation"), ron.Unit) and r["interpolation"].name == "Smooth")
-        col = Coloring(int(c["slot"]), ramp)
-    elif c is not None and not (isinstance(c, ron.Unit) and c.name == "None"):
-        raise ValueError("only Trap colouring is on this path")
-    mat = Material(albedo=tuple(ron.vec(m["albedo"])), roughness=float(m["roughness"]),
-                   metallic=float(m["metallic"]), specular=float(m["specular"]), coloring=col)
+    mat = _material_from_ron(v["material"])
     atm = v.get("atmosphere", {})
     fog = None
     if float(atm.get("fog_density", 0.0)) > 0.0:

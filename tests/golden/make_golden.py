@@ -10,6 +10,9 @@ It reads, as data:
       -> graph_<name>.json      (nodes, links, safety, bounding_radius_hint)
   scenes/{mandelbox,menger,mandelbulb}.ron
       -> scene_<name>.json      (the scene file as JSON: graph, camera, lights, material)
+  scenes/{eclosion-brume,puits-des-eons}.ron
+      -> scene_<name>.json      (the same, for the reader's material, light and fog
+         fields: finishes with details, projectors and tubes, a texture graph)
   crates/syfrack-render/tests/fixtures/parity/{mandelbox,menger,mandelbulb}.exr
       -> film_<name>_blocks.json (the reference's own 640x360, 64-spp render of that
          scene, reduced to what the film gate reads: 8x8 block means of the 8-bit
@@ -48,6 +51,7 @@ def to_json(v):
 
 
 SCENES = ["mandelbox", "menger", "mandelbulb"]
+EXTRA_SCENES = ["eclosion-brume", "puits-des-eons"]  # scene files without a reference render
 
 
 def read_exr(path):
@@ -173,7 +177,11 @@ def main(root):
                        "blocks": [[round(float(x), 3) for x in row.reshape(-1)] for row in bm],
                        "mean_linear": [float(x) for x in rgb.reshape(-1, 3).mean(0)],
                        "mean_8bit": [float(x) for x in enc.reshape(-1, 3).mean(0)]}, f)
-    print("wrote", len(NAMES) * 2 + len(SCENES) * 2, "files")
+    for name in EXTRA_SCENES:
+        v = ron.load(os.path.join(root, "scenes", f"{name}.ron"))
+        with open(os.path.join(HERE, f"scene_{name}.json"), "w") as f:
+            json.dump({"source": f"scenes/{name}.ron", "scene": to_json(v)}, f, indent=0)
+    print("wrote", len(NAMES) * 2 + len(SCENES) * 2 + len(EXTRA_SCENES), "files")
 
 
 if __name__ == "__main__":

@@ -88,6 +88,8 @@ def golden_scene(name, atmosphere=None):
         d = json.load(f)
 
     def back(v):
+        if isinstance(v, dict) and "nodes" in v and "links" in v:  # a texture's graph
+            return _jsonish_to_ron(v)
         if isinstance(v, dict) and "__items__" in v:
             items = [back(x) for x in v["__items__"]]
             if v["__name__"] == "Graph":

@@ -44,3 +44,37 @@ def test_desc_packing():
     assert [d.body_ids[i] for i in range(it.body_offset, it.body_offset + it.body_len)] == [2, 3, 4, 5, 6]
     trap = d.nodes[3]
     assert trap.kind == abi.KIND_ID["Trap"] and list(trap.u) == [0, 0, 0] and trap.f[0] == 2.0
+
+
+def test_scene_reader_keeps_materials_lights_and_fog():
+    """The scene files' material (finishes with their details, surface variation, a
+    volumetric texture with its own graph), projector and tube lights, and fog reach
+    the scene (scenes/eclosion-brume.ron, scenes/puits-des-eons.ron)."""
+    from helpers import golden_scene
+    from syfrack_gb300.scene import ProjectorLight, TubeLight
+
+    s = golden_scene("eclosion-brume")
+    kinds = [type(l).__name__ for l in s.lights]
+    assert kinds == ["ProjectorLight", "ProjectorLight", "AreaLight", "AreaLight", "TubeLight", "TubeLight",
+                     "EnvironmentLight"]
+    p = s.lights[0]
+    assert isinstance(p, ProjectorLight) and p.inner_angle < p.outer_angle
+    assert isinstance(s.lights[4], TubeLight) and s.lights[4].radius > 0
+    assert len(s.material.finishes) == 8 and sum(f.detail is not None for f in s.material.finishes) == 4
+    assert s.material.finishes[0].detail.pattern == "BrushedMetal"
+    assert s.fog is not None and s.fog.density > 0 and s.cavity_darkness > 0
+    s = golden_scene("puits-des-eons")
+    t = s.material.texture
+    assert t is not None and t.channel == ("trap", 0) and len(t.graph.nodes) > 3
+    assert t.graph.validate()["op_count"] > 0
+    assert s.material.surface is not None and s.material.coloring is not None
+    d = golden_scene("eclosion-brume").desc(64, 36)
+    assert d.light_count == 7 and d.finish_count == 8 and sum(d.details[i].pattern > 0 for i in range(8)) == 4
+    assert [d.lights[i].kind for i in range(7)] == [4, 4, 0, 0, 5, 5, 2]
+
+
+def test_creation_scenes_are_refused():
+    from syfrack_gb300.scene import scene_from_ron_value
+
+    with pytest.raises(ValueError, match="creation"):
+        scene_from_ron_value({"creation": {}, "camera": {}, "lights": [], "material": {}})
