@@ -238,7 +238,8 @@ typedef struct sf_area_light {
     float rotation;
 } sf_area_light;
 typedef sf_area_light sf_light;
-#define SF_MAX_LIGHTS 8
+#define SF_MAX_LIGHTS 8          /* lights held inline in sf_scene_desc */
+#define SF_MAX_SCENE_LIGHTS 96   /* Scene::lights bound, MAX_LIGHTS (light.rs:7); ABI 1.6 */
 #define SF_MAX_FINISHES 8
 #define SF_MAX_RAMP_STOPS 16
 /* Material.coloring (material.rs:100-130) as GpuColoring (uniforms.rs:193-215): the
@@ -334,6 +335,15 @@ typedef struct sf_scene_desc {
     sf_orbit_coloring coloring_orbit;     /* channels of coloring.slot 6 (Coloring::Orbit) */
     sf_optics optics[SF_MAX_FINISHES + 1];/* 0: Material.optics; i: finish i's optics */
     sf_texture texture;                   /* Material.texture; graph NULL = none */
+    /* ABI 1.6: a scene of up to SF_MAX_SCENE_LIGHTS lights (Scene::validate,
+     * scene/mod.rs:512). A non-NULL light_list holds light_list_count lights and
+     * replaces lights/light_count; sessions copy it at creation. Sessions take up to
+     * 96 lights; batches, the server, previews and exports take SF_MAX_LIGHTS. The
+     * wavefront integrator stores at most 8 shadow segments per bounce (one per sky
+     * light plus the surface's, and one per emitter in fog); the megakernel traces
+     * them as they are issued and has no such bound. */
+    const sf_area_light* light_list;
+    uint32_t light_list_count;
 } sf_scene_desc;
 
 /* RenderConfig (renderer.rs:17-43), validated as RenderConfig::validate (:81-138).

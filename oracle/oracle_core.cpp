@@ -887,9 +887,11 @@ template <class R> Scene<R> make_scene(const Graph& g, const sf_scene_desc& d, c
     s.material = mat(d.material);
     s.finish_count = std::min<uint32_t>(d.finish_count, SF_MAX_FINISHES);
     for (uint32_t i = 0; i < s.finish_count; ++i) s.finishes[i] = mat(d.finishes[i]);
-    s.light_count = std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
+    // the scene's lights: light_list (up to 96) when set, else the inline array
+    s.light_count = d.light_list ? std::min<uint32_t>(d.light_list_count, SF_MAX_SCENE_LIGHTS)
+                                 : std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
     for (uint32_t i = 0; i < s.light_count; ++i) {
-        const sf_area_light& l = d.lights[i];
+        const sf_area_light& l = d.light_list ? d.light_list[i] : d.lights[i];
         Light<R>& o = s.lights[i];
         o.kind = l.kind;
         o.color = v3<R>(l.radiance);

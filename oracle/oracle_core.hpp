@@ -251,7 +251,7 @@ template <class R> struct Scene {
     Mat<R> material;
     Mat<R> finishes[SF_MAX_FINISHES];
     uint32_t finish_count = 0;
-    Light<R> lights[SF_MAX_LIGHTS];
+    Light<R> lights[SF_MAX_SCENE_LIGHTS];  // Scene::lights, at most MAX_LIGHTS (light.rs:7)
     uint32_t light_count = 0;
     Coloring<R> coloring;
     R col_weights[4] = {0, 0, 0, 0}, col_extra[3] = {0, 0, 0};  // the orbit mix of coloring slot 6

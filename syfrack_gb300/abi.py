@@ -24,7 +24,8 @@ MEASURES = ["Norm", "AxisX", "AxisY", "AxisZ", "PlaneY", "AngleXY", "AngleXZ", "
 TRAP_MODES = ["Minimum", "Maximum", "Last"]
 FORMS = {0: "generic", 1: "bulb", 2: "box", 3: "menger"}
 
-SF_MAX_LIGHTS = 8
+SF_MAX_LIGHTS = 8          # lights inline in sf_scene_desc
+SF_MAX_SCENE_LIGHTS = 96   # MAX_LIGHTS (light.rs:7): the rest through light_list (ABI 1.6)
 SF_MAX_FINISHES = 8
 INTEGRATOR_MEGAKERNEL = 0
 INTEGRATOR_WAVEFRONT = 1
@@ -140,7 +141,9 @@ class sf_scene_desc(C.Structure):
                 # ABI 1.3
                 ("details", sf_finish_detail * SF_MAX_FINISHES), ("dune_wind", C.c_float),
                 ("coloring_orbit", sf_orbit_coloring), ("optics", sf_optics * (SF_MAX_FINISHES + 1)),
-                ("texture", sf_texture)]
+                ("texture", sf_texture),
+                # ABI 1.6
+                ("light_list", C.POINTER(sf_area_light)), ("light_list_count", C.c_uint32)]
 
 
 class sf_render_config(C.Structure):

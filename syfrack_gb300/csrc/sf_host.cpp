@@ -50,7 +50,7 @@ constexpr uint32_t MAX_PLACEMENTS = 16384; // graph/mod.rs:18
 constexpr uint32_t MAX_INSTANCE_PRODUCT = 65536;  // graph/mod.rs:20
 // 1.1: sf_film_planes.color; 1.2: sf_render_config.hit_epsilon; 1.3: finish details, orbit
 // colouring, optics and textures in sf_scene_desc
-constexpr uint32_t ABI_VERSION = (1u << 16) | 5u;
+constexpr uint32_t ABI_VERSION = (1u << 16) | 6u;
 
 // ------------------------------------------------------------------ graph preparation
 
@@ -945,11 +945,19 @@ sf_status build_graph(const sf_graph_desc* d, HostGraph& g, DeProgram& P, sf_gra
     return SF_OK;
 }
 
-sf_status scene_check(const sf_scene_desc& d) {
-    if (d.light_count > SF_MAX_LIGHTS || d.finish_count > SF_MAX_FINISHES)
-        return fail(SF_ERR_INVALID, "too many lights or finishes");
-    for (uint32_t i = 0; i < d.light_count; ++i) {
-        const sf_area_light& l = d.lights[i];
+sf_status scene_check(const sf_scene_desc& d, uint32_t max_lights, bool inline_shadows) {
+    if (d.finish_count > SF_MAX_FINISHES) return fail(SF_ERR_INVALID, "more than 8 finishes");
+    if (!d.light_list && d.light_count > SF_MAX_LIGHTS)
+        return fail(SF_ERR_INVALID, "more than 8 inline lights (light_list holds up to 96)");
+    if (d.light_list && d.light_list_count > SF_MAX_SCENE_LIGHTS)
+        return fail(SF_ERR_INVALID, "a scene may have at most 96 lights");  // Scene::validate (scene/mod.rs:512)
+    const uint32_t n_lights = scene_light_count(d);
+    if (n_lights > max_lights)
+        return fail(SF_ERR_UNSUPPORTED, "more than 8 lights: batches, the server, previews and exports take 8, "
+                                        "sessions up to 96");
+    const sf_area_light* lights = scene_lights(d);
+    for (uint32_t i = 0; i < n_lights; ++i) {
+        const sf_area_light& l = lights[i];
         if (l.kind > SF_LIGHT_TUBE) return fail(SF_ERR_UNSUPPORTED, "light kind not built on the device");
         // Light::visit_params bounds (light.rs:162-226)
         if (l.kind == SF_LIGHT_PROJECTOR &&
@@ -961,7 +969,7 @@ sf_status scene_check(const sf_scene_desc& d) {
                 return fail(SF_ERR_INVALID, "tube radius must lie in [0.001, 1000]");
             if (!(dx * dx + dy * dy + dz * dz > 0.0f)) return fail(SF_ERR_INVALID, "a tube needs distinct ends");
         }
-        if (d.lights[i].kind == SF_LIGHT_HDRI && !d.lights[i].environment)
+        if (l.kind == SF_LIGHT_HDRI && !l.environment)
             return fail(SF_ERR_INVALID, "an HDRI light needs a panorama (sf_environment_create)");
     }
     if (d.coloring.stop_count > SF_MAX_RAMP_STOPS) return fail(SF_ERR_INVALID, "more than 16 ramp stops");
@@ -998,8 +1006,9 @@ sf_status scene_check(const sf_scene_desc& d) {
     }
     if (!(d.fog.density >= 0.0f) || !(std::fabs(d.fog.anisotropy) < 1.0f))
         return fail(SF_ERR_INVALID, "fog density must be >= 0 and anisotropy in (-1, 1)");
-    if (shadow_slots_of(d) > 8)
-        return fail(SF_ERR_UNSUPPORTED, "more than 8 shadow segments per bounce (too many lights)");
+    if (!inline_shadows && shadow_slots_of(d) > 8)
+        return fail(SF_ERR_UNSUPPORTED, "more than 8 shadow segments per bounce (sky lights, and emitters in fog): "
+                                        "the wavefront stores them; the megakernel integrator traces them inline");
     return SF_OK;
 }
 // Shadow segments one bounce can issue: the surface's next events (the selected area
@@ -1007,9 +1016,9 @@ sf_status scene_check(const sf_scene_desc& d) {
 // one per area light for the segment's line integral.
 uint32_t shadow_slots_of(const sf_scene_desc& d) {
     uint32_t area = 0, sky = 0;
-    for (uint32_t i = 0; i < std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS); ++i)
-        (d.lights[i].kind == SF_LIGHT_AREA || d.lights[i].kind == SF_LIGHT_PROJECTOR ||
-                 d.lights[i].kind == SF_LIGHT_TUBE
+    const sf_area_light* lights = scene_lights(d);
+    for (uint32_t i = 0; i < scene_light_count(d); ++i)
+        (lights[i].kind == SF_LIGHT_AREA || lights[i].kind == SF_LIGHT_PROJECTOR || lights[i].kind == SF_LIGHT_TUBE
              ? area
              : sky)++;
     return 1 + sky + (d.fog.density > 0.0f ? area : 0);
@@ -1102,6 +1111,11 @@ static void ramp_dev(const sf_coloring& c, DevRamp& r) {
     r.map[2] = c.gamma;
     std::memcpy(r.stops, c.stops, sizeof r.stops);
 }
+void scene_lights_dev(const sf_scene_desc& d, std::vector<DevLight>& more) {
+    const uint32_t n = scene_light_count(d);
+    more.assign(n > SF_SHARED_LIGHTS ? n - SF_SHARED_LIGHTS : 0, DevLight{});
+    for (uint32_t i = SF_SHARED_LIGHTS; i < n; ++i) light_dev(scene_lights(d)[i], more[i - SF_SHARED_LIGHTS]);
+}
 // Uniforms::from_scene (uniforms.rs:748-830) for the DE path.
 void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph_info& gi, DevScene& S) {
     std::memset(&S, 0, sizeof S);
@@ -1118,7 +1132,7 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     S.max_bounces = c.max_bounces;
     S.max_steps = c.max_steps;
     S.seed = uint32_t(d.seed) ^ uint32_t(d.seed >> 32);
-    S.light_count = std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
+    S.light_count = scene_light_count(d);  // lights past SF_SHARED_LIGHTS: the light table
     S.finish_count = std::min<uint32_t>(d.finish_count, SF_MAX_FINISHES);
     S.variation_slot = d.variation_slot;
     S.variation_enabled = d.variation_enabled;
@@ -1138,7 +1152,8 @@ void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph
     S.iteration_product = gi.iteration_product;
     material_dev(d.material, S.material);
     for (uint32_t i = 0; i < S.finish_count; ++i) material_dev(d.finishes[i], S.finishes[i]);
-    for (uint32_t i = 0; i < S.light_count; ++i) light_dev(d.lights[i], S.lights[i]);
+    for (uint32_t i = 0; i < std::min<uint32_t>(S.light_count, SF_SHARED_LIGHTS); ++i)
+        light_dev(scene_lights(d)[i], S.lights[i]);
     S.shadow_slots = shadow_slots_of(d);
     // GpuAtmosphere (uniforms.rs:217-227): fog in a, its colour in b
     S.fog[0] = d.fog.density;
@@ -1592,6 +1607,11 @@ sf_status session_alloc(sf_session* s) {
     size_t off = 0;
     auto take = [&](size_t bytes) { size_t o = off; off += (bytes + 255) & ~size_t(255); return o; };
     size_t o_scene = take(sizeof(DevScene));
+    std::vector<DevLight> more;  // lights past the staged ones: the light table, right after the scene
+    scene_lights_dev(s->scene, more);
+    size_t o_lights = more.empty() ? 0 : take(more.size() * sizeof(DevLight));
+    if (!more.empty() && o_lights != o_scene + SF_LIGHT_TABLE_OFFSET) return fail(SF_ERR_INVALID, "light table layout");
+    s->light_smem = uint32_t(more.size() * sizeof(DevLight));  // staged per block by the light-reading kernels
     size_t o_acc = take(px * 16), o_depth = take(px * 4), o_aux = take(px * 16);
     size_t o_Ls = take(N * 16);
     // fog scenes keep the film's volume layer split: a per-path volume row and three planes
@@ -1643,6 +1663,10 @@ sf_status session_alloc(sf_session* s) {
     s->status = reinterpret_cast<uint32_t*>(base + o_status);
     DevScene S;
     scene_dev(s->scene, cfg, s->graph->info, S);
+    if (!more.empty()) {
+        CU(cudaMemcpyAsync(base + o_lights, more.data(), more.size() * sizeof(DevLight), cudaMemcpyHostToDevice,
+                           c->stream));
+    }
     CU(cudaMemcpyAsync(s->d_scene, &S, sizeof S, cudaMemcpyHostToDevice, c->stream));
     // depth = -1 and aux = (0,0,0,-1) until sample 0 lands (RenderOutput conventions)
     CU(sf_launch_film_clear(s->film, c->stream));
@@ -1659,12 +1683,19 @@ extern "C" sf_status sf_session_create(sf_context* c, sf_graph* g, const sf_scen
     *out = nullptr;
     sf_status st = validate_config(*cfg);
     if (st != SF_OK) return st;
-    if (const sf_status sc = scene_check(*scene); sc != SF_OK) return sc;
+    if (const sf_status sc =
+            scene_check(*scene, SF_MAX_SCENE_LIGHTS, cfg->integrator == SF_INTEGRATOR_MEGAKERNEL);
+        sc != SF_OK)
+        return sc;
     cudaSetDevice(c->device);
     auto* s = new sf_session();
     s->ctx = c;
     s->graph = g;
     s->scene = *scene;
+    if (scene->light_list) {
+        s->light_store.assign(scene->light_list, scene->light_list + scene->light_list_count);
+        s->scene.light_list = s->light_store.data();
+    }
     s->cfg = *cfg;
     st = session_alloc(s);
     if (st != SF_OK) {
@@ -1712,7 +1743,7 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
     if (paths > s->capacity) return fail(SF_ERR_INVALID, "tile * samples exceeds the session capacity");
     sf_context* c = s->ctx;
     cudaSetDevice(c->device);
-    DispatchGeom g{tile.x, tile.y, tile.w, tile.h, tile.done, samples, uint32_t(paths)};
+    DispatchGeom g{tile.x, tile.y, tile.w, tile.h, tile.done, samples, uint32_t(paths), s->light_smem};
     cudaStream_t st = c->stream;
     if (s->cfg.integrator == SF_INTEGRATOR_MEGAKERNEL) {
         {
@@ -1757,7 +1788,7 @@ extern "C" sf_status sf_session_dispatch(sf_session* s, sf_tile tile, uint32_t s
             tl.optics = (rich & SF_RICH_OPTICS) ? 1u : 0u;
             LaunchTimer t(c, true);
             CU(sf_launch_trace(s->graph->prog.form, s->graph->d_prog, s->d_scene, s->soa, tl, c->d_stats, blocks,
-                               int(s->min_blocks), st));
+                               int(s->min_blocks), s->light_smem, st));
         }
         LaunchTimer t(c, false);
         CU(sf_launch_shade(s->d_scene, rich, s->soa, q, g, s->film, s->status, r + 1 == R ? 1 : 0, st));
@@ -2002,8 +2033,8 @@ sf_status install_checkpoint(const std::string& final_dir,
 
 namespace sfh {
 bool has_hdri(const sf_scene_desc& d) {
-    for (uint32_t i = 0; i < std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS); ++i)
-        if (d.lights[i].kind == SF_LIGHT_HDRI) return true;
+    for (uint32_t i = 0; i < scene_light_count(d); ++i)
+        if (scene_lights(d)[i].kind == SF_LIGHT_HDRI) return true;
     return false;
 }
 }  // namespace sfh

@@ -143,9 +143,18 @@ struct LaunchTimer {
 float sqrt_threshold(float b);
 void scene_dev(const sf_scene_desc& d, const sf_render_config& c, const sf_graph_info& gi, DevScene& S);
 sf_status validate_config(const sf_render_config& c);
-// Scene limits and the light kinds and colouring the device path supports.
-sf_status scene_check(const sf_scene_desc& d);
+// Scene limits and the light kinds and colouring the device path supports: at most
+// max_lights lights, and (unless the integrator traces shadow segments as it issues
+// them) at most 8 shadow segments per bounce.
+sf_status scene_check(const sf_scene_desc& d, uint32_t max_lights = SF_MAX_LIGHTS, bool inline_shadows = false);
 uint32_t shadow_slots_of(const sf_scene_desc& d);
+// The scene's lights: light_list when set, else the inline array.
+inline const sf_area_light* scene_lights(const sf_scene_desc& d) { return d.light_list ? d.light_list : d.lights; }
+inline uint32_t scene_light_count(const sf_scene_desc& d) {
+    return d.light_list ? d.light_list_count : std::min<uint32_t>(d.light_count, SF_MAX_LIGHTS);
+}
+// Lights SF_SHARED_LIGHTS.. of the scene, packed for the device light table.
+void scene_lights_dev(const sf_scene_desc& d, std::vector<DevLight>& more);
 // Panorama tables (sf_environment.cpp) and an HDRI light's device fields.
 sf_status environment_tables(const float* rgb, uint32_t width, uint32_t height, std::vector<float>& texels,
                              uint32_t& ow, uint32_t& oh, bool& uniform);
@@ -252,6 +261,8 @@ struct sf_session {
     sf_context* ctx = nullptr;
     sf_graph* graph = nullptr;
     sf_scene_desc scene;
+    std::vector<sf_area_light> light_store;  // the session's copy of scene.light_list
+    uint32_t light_smem = 0;                  // dynamic shared bytes of its lights past SF_SHARED_LIGHTS
     sf_render_config cfg;
     DevScene* d_scene = nullptr;
     FilmPlanes film{};

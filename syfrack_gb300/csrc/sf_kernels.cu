@@ -159,6 +159,7 @@ __global__ void __launch_bounds__(256) k_generate(const DevScene* __restrict__ s
                                                   uint32_t* counts) {
     __shared__ DevScene S;
     stage_pod(S, scene_g);
+    stage_more_lights(scene_g);
     __syncthreads();
     uint32_t path = blockIdx.x * blockDim.x + threadIdx.x;
     if (path == 0) {
@@ -178,6 +179,7 @@ __global__ void __launch_bounds__(128, 5) k_shade(const DevScene* __restrict__ s
                                                DispatchGeom g, FilmPlanes film, uint32_t* status, int final_round) {
     __shared__ DevScene S;
     stage_pod(S, scene_g);
+    stage_more_lights(scene_g);
     __syncthreads();
     const uint32_t n = q.counts[0];
     for (uint32_t j = blockIdx.x * blockDim.x + threadIdx.x; j < n; j += gridDim.x * blockDim.x) {
@@ -278,6 +280,7 @@ __global__ void __launch_bounds__(64) k_megakernel(const DeProgram* __restrict__
     __shared__ DevScene S;
     stage_program(P, prog_g);
     stage_pod(S, scene_g);
+    stage_more_lights(scene_g);
     __syncthreads();
     uint32_t lx = blockIdx.x * 8 + (threadIdx.x & 7), ly = blockIdx.y * 8 + (threadIdx.x >> 3);
     if (lx >= g.tile_w || ly >= g.tile_h) return;
@@ -687,26 +690,26 @@ cudaError_t sf_launch_primary(const DeProgram* prog, const DevScene* scene, uint
     return cudaGetLastError();
 }
 cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom g, uint32_t* counts, cudaStream_t st) {
-    k_generate<<<(g.paths + 255) / 256, 256, 0, st>>>(scene, soa, g, counts);
+    k_generate<<<(g.paths + 255) / 256, 256, g.light_smem, st>>>(scene, soa, g, counts);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
-                            unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
+                            unsigned long long* stats, int blocks, int min_blocks, uint32_t light_smem, cudaStream_t st) {
     if (min_blocks < 2 || min_blocks > 7 || min_blocks == 5) min_blocks = 2;
     if (blocks <= 0) blocks = sf_device_sm_count() * min_blocks;
     switch (form) {
-    case SF_FORM_BULB: return sf_launch_trace_bulb(prog, scene, soa, tl, stats, blocks, min_blocks, st);
-    case SF_FORM_BOX: return sf_launch_trace_box(prog, scene, soa, tl, stats, blocks, min_blocks, st);
-    case SF_FORM_MENGER: return sf_launch_trace_menger(prog, scene, soa, tl, stats, blocks, min_blocks, st);
-    default: return sf_launch_trace_any(prog, scene, soa, tl, stats, blocks, min_blocks, st);
+    case SF_FORM_BULB: return sf_launch_trace_bulb(prog, scene, soa, tl, stats, blocks, min_blocks, light_smem, st);
+    case SF_FORM_BOX: return sf_launch_trace_box(prog, scene, soa, tl, stats, blocks, min_blocks, light_smem, st);
+    case SF_FORM_MENGER: return sf_launch_trace_menger(prog, scene, soa, tl, stats, blocks, min_blocks, light_smem, st);
+    default: return sf_launch_trace_any(prog, scene, soa, tl, stats, blocks, min_blocks, light_smem, st);
     }
 }
 cudaError_t sf_launch_shade(const DevScene* scene, uint32_t rich, PathSoA soa, RoundQueues q, DispatchGeom g,
                             FilmPlanes film, uint32_t* status, int final_round, cudaStream_t st) {
     const dim3 grid = grid_for(g.paths, 128, 32);
-    if (rich & SF_RICH_TEXTURE) k_shade<3><<<grid, 128, 0, st>>>(scene, soa, q, g, film, status, final_round);
-    else if (rich) k_shade<1><<<grid, 128, 0, st>>>(scene, soa, q, g, film, status, final_round);
-    else k_shade<0><<<grid, 128, 0, st>>>(scene, soa, q, g, film, status, final_round);
+    if (rich & SF_RICH_TEXTURE) k_shade<3><<<grid, 128, g.light_smem, st>>>(scene, soa, q, g, film, status, final_round);
+    else if (rich) k_shade<1><<<grid, 128, g.light_smem, st>>>(scene, soa, q, g, film, status, final_round);
+    else k_shade<0><<<grid, 128, g.light_smem, st>>>(scene, soa, q, g, film, status, final_round);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaStream_t st) {
@@ -717,9 +720,9 @@ cudaError_t sf_launch_commit(PathSoA soa, DispatchGeom g, FilmPlanes film, cudaS
 cudaError_t sf_launch_megakernel(const DeProgram* prog, const DevScene* scene, uint32_t rich, PathSoA soa,
                                  DispatchGeom g, FilmPlanes film, unsigned long long* stats, cudaStream_t st) {
     dim3 grid((g.tile_w + 7) / 8, (g.tile_h + 7) / 8);
-    if (rich & SF_RICH_TEXTURE) k_megakernel<3><<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
-    else if (rich) k_megakernel<1><<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
-    else k_megakernel<0><<<grid, 64, 0, st>>>(prog, scene, soa, g, film, stats);
+    if (rich & SF_RICH_TEXTURE) k_megakernel<3><<<grid, 64, g.light_smem, st>>>(prog, scene, soa, g, film, stats);
+    else if (rich) k_megakernel<1><<<grid, 64, g.light_smem, st>>>(prog, scene, soa, g, film, stats);
+    else k_megakernel<0><<<grid, 64, g.light_smem, st>>>(prog, scene, soa, g, film, stats);
     return cudaGetLastError();
 }
 cudaError_t sf_launch_ref_orbit(double cx, double cy, uint32_t max_iter, double bailout, float2* orbit_lo,

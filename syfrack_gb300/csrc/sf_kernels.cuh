@@ -105,6 +105,7 @@ struct DispatchGeom {
     uint32_t tile_x, tile_y, tile_w, tile_h;
     uint32_t sample_start, samples;
     uint32_t paths;  // tile_w * tile_h * samples
+    uint32_t light_smem;  // dynamic shared bytes: the scene's lights past SF_SHARED_LIGHTS
 };
 
 // stripe_k: the stripe count as an integer (|k| <= 64), else SF_STRIPES_GENERAL;
@@ -156,14 +157,14 @@ cudaError_t sf_launch_primary(const DeProgram* prog, const DevScene* scene, uint
 cudaError_t sf_launch_generate(const DevScene* scene, PathSoA soa, DispatchGeom g, uint32_t* counts, cudaStream_t st);
 // Persistent trace kernel, one instantiation per form (sf_trace_<form>.cu).
 cudaError_t sf_launch_trace(uint32_t form, const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
-                            unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st);
-cudaError_t sf_launch_trace_bulb(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
+                            unsigned long long* stats, int blocks, int min_blocks, uint32_t light_smem, cudaStream_t st);
+cudaError_t sf_launch_trace_bulb(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int, uint32_t,
                                  cudaStream_t);
-cudaError_t sf_launch_trace_box(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
+cudaError_t sf_launch_trace_box(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int, uint32_t,
                                 cudaStream_t);
 cudaError_t sf_launch_trace_menger(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int,
-                                   int, cudaStream_t);
-cudaError_t sf_launch_trace_any(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int,
+                                   int, uint32_t, cudaStream_t);
+cudaError_t sf_launch_trace_any(const DeProgram*, const DevScene*, PathSoA, TraceLaunch, unsigned long long*, int, int, uint32_t,
                                 cudaStream_t);
 // Batched wavefront (sf_batch.cu): all jobs' paths in one set of launches.
 cudaError_t sf_launch_generate_batch(BatchTable bt, PathSoA soa, uint32_t* counts, cudaStream_t st);

@@ -122,6 +122,9 @@ struct DevLight {
     float radius, length;
 };
 #define SF_MAX_RAMP 16
+// Lights held in DevScene itself (staged into shared memory with it); a scene's further
+// lights, up to 96, follow its DevScene in device memory at SF_LIGHT_TABLE_OFFSET.
+#define SF_SHARED_LIGHTS 8
 
 struct DevMaterial {
     float albedo[3], roughness, metallic, specular, emission[3];
@@ -186,7 +189,7 @@ struct DevScene {
     float fog_color[3];               // scattering albedo (atmosphere.b.xyz)
     DevMaterial material;
     DevMaterial finishes[8];
-    DevLight lights[8];
+    DevLight lights[SF_SHARED_LIGHTS];
     // make_surface's detail and texture and radiance's optics. rich: SF_RICH_* bits of
     // what the scene uses (0 keeps every path of the plain surface).
     uint32_t rich;
@@ -195,4 +198,6 @@ struct DevScene {
     DevOptics optics[9];
     DevTexture tex;
 };
+// Byte offset from a DevScene in device memory to its lights past SF_SHARED_LIGHTS.
+#define SF_LIGHT_TABLE_OFFSET ((sizeof(DevScene) + 255) & ~size_t(255))
 enum { SF_RICH_DETAIL = 1, SF_RICH_TEXTURE = 2, SF_RICH_OPTICS = 4, SF_RICH_ROUGH_DIFFUSE = 8 };

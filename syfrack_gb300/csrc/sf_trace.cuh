@@ -135,6 +135,27 @@ __device__ __forceinline__ float3 wsafe_normalize(float3 v) {
 }
 
 // ------------------------------------------------------------------ lights (lights.wgsl)
+// A scene's lights past SF_SHARED_LIGHTS, staged from its light table (after the scene
+// in device memory, SF_LIGHT_TABLE_OFFSET) into dynamic
+// shared memory by the kernels that read lights (stage_more_lights); the launch gives
+// (light_count - SF_SHARED_LIGHTS) * sizeof(DevLight) bytes, none for up to 8 lights.
+extern __shared__ __align__(16) DevLight sf_more_lights[];
+__device__ __forceinline__ void stage_more_lights(const DevScene* scene_g) {
+    const uint32_t n = scene_g->light_count;
+    if (n <= SF_SHARED_LIGHTS) return;
+    uint32_t avail;
+    asm("mov.u32 %0, %%dynamic_smem_size;" : "=r"(avail));
+    const uint32_t words = min((n - SF_SHARED_LIGHTS) * uint32_t(sizeof(DevLight) / 4), avail / 4u);
+    const uint32_t* s = reinterpret_cast<const uint32_t*>(reinterpret_cast<const char*>(scene_g) + SF_LIGHT_TABLE_OFFSET);
+    uint32_t* d = reinterpret_cast<uint32_t*>(sf_more_lights);
+    for (uint32_t i = threadIdx.x; i < words; i += blockDim.x) d[i] = __ldg(s + i);
+}
+// Light i of the scene: the first SF_SHARED_LIGHTS staged with the scene, the rest
+// staged by stage_more_lights; both in shared memory.
+__device__ __forceinline__ const DevLight& light_of(const DevScene& S, uint32_t i) {
+    if (i < SF_SHARED_LIGHTS) return S.lights[i];
+    return sf_more_lights[i - SF_SHARED_LIGHTS];
+}
 __device__ __forceinline__ float area_intersection(float3 ro, float3 rd, const DevLight& l) {
     float3 n = ld3(l.n);
     float den = dot3(n, rd);
@@ -335,7 +356,7 @@ __device__ __forceinline__ float area_weight(float3 p, float3 n, const DevLight&
 __device__ __forceinline__ float area_total_weight(const DevScene& S, float3 p, float3 n) {
     float total = 0.0f;
     for (uint32_t i = 0; i < S.light_count; ++i)
-        if (is_emitter(S.lights[i])) total += area_weight(p, n, S.lights[i]);
+        if (is_emitter(light_of(S, i))) total += area_weight(p, n, light_of(S, i));
     return total;
 }
 __device__ __forceinline__ float mis_power(float a, float b) {
@@ -349,7 +370,7 @@ static __device__ float3 area_emission(const DevScene& S, float3 ro, float3 rd, 
                                 float3 prev_normal, float prev_total) {
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         if (!is_emitter(l)) continue;
         float cos_l = dot3(emitter_normal(l, e_add(ro, e_mul(rd, distance))), -rd);
         if (cos_l <= 0.0f) continue;
@@ -372,8 +393,8 @@ __device__ __forceinline__ float nearest_emitter(const DevScene& S, float3 ro, f
     float nearest = t_end;
     li = SF_NO_LIGHT;
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        if (!is_emitter(S.lights[i])) continue;
-        float t = emitter_intersection(ro, rd, S.lights[i]);
+        if (!is_emitter(light_of(S, i))) continue;
+        float t = emitter_intersection(ro, rd, light_of(S, i));
         if (t < nearest) { nearest = t; li = i; }
     }
     return nearest;
@@ -681,7 +702,7 @@ static __device__ float3 environment_emission(const DevScene& S, float3 dir, flo
                                               bool from_volume, float area_total) {
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         if (l.kind != SF_LIGHT_ENVIRONMENT) continue;
         float w = 1.0f;
         if (use_mis) {
@@ -697,7 +718,7 @@ __device__ __forceinline__ float sun_pdf(float cos_max) { return wdiv(1.0f, 2.0f
 static __device__ float3 sun_radiance(const DevScene& S, float3 dir, float pdf_bsdf, bool use_mis) {
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         if (l.kind != SF_LIGHT_SUN || dot3(dir, ld3(l.a)) < l.cos_max) continue;
         const float pl = sun_pdf(l.cos_max);
         const float w = use_mis ? mis_power(pdf_bsdf, pl) : 1.0f;
@@ -789,7 +810,7 @@ static __device__ float3 hdri_sample(const DevLight& l, float r0, float r1, floa
 static __device__ float3 hdri_emission(const DevScene& S, float3 dir, float previous_pdf, bool use_mis) {
     float3 L = mk3(0.f, 0.f, 0.f);
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         if (l.kind != SF_LIGHT_HDRI) continue;
         const float w = use_mis ? mis_power(previous_pdf, hdri_pdf(l, dir)) : 1.0f;
         L = L + hdri_lookup(l, dir) * w;
@@ -930,10 +951,10 @@ static __device__ void fog_segment_direct(const DevScene& S, float3 tp, float3 r
     if (tau_end <= 0.0f) return;
     float total = 0.0f;
     for (uint32_t i = 0; i < S.light_count; ++i)
-        if (is_emitter(S.lights[i])) total += fog_segment_weight(ro, rd, end, S.lights[i]);
+        if (is_emitter(light_of(S, i))) total += fog_segment_weight(ro, rd, end, light_of(S, i));
     const float g = S.fog[3];
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         if (!is_emitter(l)) continue;
         const float probability = volume_light_probability(fog_segment_weight(ro, rd, end, l), total);
         const uint32_t stream = pcg(point_stream ^ (i * 0x85ebca6bu));
@@ -1025,7 +1046,7 @@ static __device__ void fog_direct_light(const DevScene& S, float3 tpc, float3 p,
                                         uint32_t& rng, Emit&& emit) {
     const float g = S.fog[3];
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         float3 dir, value;
         float pl;
         if (l.kind == SF_LIGHT_ENVIRONMENT) {
@@ -1178,7 +1199,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
     if (h.hit && ps.bounce == 0 && first_depth) {
         *first_depth = h.t;
         const float3 en = h.light_index != SF_NO_LIGHT
-                              ? emitter_normal(S.lights[h.light_index], e_add(ps.o, e_mul(ps.d, h.t)))
+                              ? emitter_normal(light_of(S, h.light_index), e_add(ps.o, e_mul(ps.d, h.t)))
                               : h.n;
         *first_aux = make_float4(en.x, en.y, en.z, float(h.steps));
     }
@@ -1296,8 +1317,8 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
         float threshold = rnd(ps.rng) * area_total;
         float sum = 0.0f;
         for (uint32_t i = 0; i < S.light_count; ++i) {
-            if (!is_emitter(S.lights[i])) continue;
-            float w = area_weight(p_off, s.n, S.lights[i]);
+            if (!is_emitter(light_of(S, i))) continue;
+            float w = area_weight(p_off, s.n, light_of(S, i));
             sum += w;
             if (w > 0.0f) {
                 selected = i;
@@ -1307,7 +1328,7 @@ static __device__ int bounce_body(const DevScene& S, PathState& ps, const HitInf
         }
     }
     for (uint32_t i = 0; i < S.light_count; ++i) {
-        const DevLight& l = S.lights[i];
+        const DevLight& l = light_of(S, i);
         if (l.kind == SF_LIGHT_ENVIRONMENT) {
             if (l.peak <= 0.0f) continue;
             const float probability = environment_probability(l, area_total);

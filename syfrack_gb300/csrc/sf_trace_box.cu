@@ -2,6 +2,6 @@
 #include "sf_trace_kernel.cuh"
 
 cudaError_t sf_launch_trace_box(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
-                               unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
-    return launch_trace_form<SF_FORM_BOX>(prog, scene, soa, tl, stats, blocks, min_blocks, st);
+                               unsigned long long* stats, int blocks, int min_blocks, uint32_t light_smem, cudaStream_t st) {
+    return launch_trace_form<SF_FORM_BOX>(prog, scene, soa, tl, stats, blocks, min_blocks, light_smem, st);
 }

@@ -70,6 +70,7 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
     } else {
         stage_program(P, prog_g);
         stage_pod(S, scene_g);
+        stage_more_lights(scene_g);
     }
     __syncthreads();
     const bool first = tl.resume == nullptr;
@@ -386,26 +387,26 @@ __global__ void __launch_bounds__(THREADS, MIN_BLOCKS) k_trace(const DeProgram* 
 
 template <int FORM>
 static cudaError_t launch_trace_form(const DeProgram* prog, const DevScene* scene, PathSoA soa, TraceLaunch tl,
-                                     unsigned long long* stats, int blocks, int min_blocks, cudaStream_t st) {
+                                     unsigned long long* stats, int blocks, int min_blocks, uint32_t light_smem, cudaStream_t st) {
     if (tl.optics) {  // 6 blocks of 128 threads per SM (the host sizes the grid)
-        k_trace<FORM, 6, false, false, true, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats);
+        k_trace<FORM, 6, false, false, true, 128><<<blocks, 128, light_smem, st>>>(prog, scene, soa, tl, stats);
         return cudaGetLastError();
     }
     if (tl.lane_stats && min_blocks == 3) {
-        k_trace<FORM, 3, false, true><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats);
+        k_trace<FORM, 3, false, true><<<blocks, 256, light_smem, st>>>(prog, scene, soa, tl, stats);
         return cudaGetLastError();
     }
     if (tl.lane_stats && min_blocks == 7) {
-        k_trace<FORM, 7, false, true, false, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats);
+        k_trace<FORM, 7, false, true, false, 128><<<blocks, 128, light_smem, st>>>(prog, scene, soa, tl, stats);
         return cudaGetLastError();
     }
     switch (min_blocks) {
-    case 3: k_trace<FORM, 3><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
-    case 4: k_trace<FORM, 4><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
+    case 3: k_trace<FORM, 3><<<blocks, 256, light_smem, st>>>(prog, scene, soa, tl, stats); break;
+    case 4: k_trace<FORM, 4><<<blocks, 256, light_smem, st>>>(prog, scene, soa, tl, stats); break;
     // 128-thread blocks: 6 or 7 per SM (24 or 28 warps at up to 85 or 73 registers)
-    case 6: k_trace<FORM, 6, false, false, false, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats); break;
-    case 7: k_trace<FORM, 7, false, false, false, 128><<<blocks, 128, 0, st>>>(prog, scene, soa, tl, stats); break;
-    default: k_trace<FORM, 2><<<blocks, 256, 0, st>>>(prog, scene, soa, tl, stats); break;
+    case 6: k_trace<FORM, 6, false, false, false, 128><<<blocks, 128, light_smem, st>>>(prog, scene, soa, tl, stats); break;
+    case 7: k_trace<FORM, 7, false, false, false, 128><<<blocks, 128, light_smem, st>>>(prog, scene, soa, tl, stats); break;
+    default: k_trace<FORM, 2><<<blocks, 256, light_smem, st>>>(prog, scene, soa, tl, stats); break;
     }
     return cudaGetLastError();
 }

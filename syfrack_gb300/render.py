@@ -479,9 +479,12 @@ class Batch:
         self._tex = [renderer.compile(sc.material.texture.graph) if sc.material.texture else None
                      for sc, _ in self.jobs]
         arr = (sf_batch_job * len(self.jobs))()
+        # the descriptors stay alive with the batch: a light list is referenced, not copied
+        self._descs = [sc.desc(cfg.width, cfg.height, self._tex[i].h.value if self._tex[i] else None)
+                       for i, (sc, cfg) in enumerate(self.jobs)]
         for i, (sc, cfg) in enumerate(self.jobs):
             arr[i].graph = self._graphs[i].h
-            arr[i].scene = sc.desc(cfg.width, cfg.height, self._tex[i].h.value if self._tex[i] else None)
+            arr[i].scene = self._descs[i]
             arr[i].cfg = cfg.desc()
         h = C.c_void_p()
         check(self.ctx.lib.sf_batch_create(self.ctx.h, arr, len(self.jobs), C.byref(h)))

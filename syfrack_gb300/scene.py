@@ -6,6 +6,7 @@ Vector arithmetic is binary32 (numpy float32), like glam's Vec3.
 """
 from __future__ import annotations
 
+import ctypes as C
 import math
 from dataclasses import dataclass, field
 
@@ -498,11 +499,19 @@ class Scene:
         for i, f in enumerate(self.material.finishes):
             d.finishes[i] = f.packed()
         d.finish_count = len(self.material.finishes)
+        if len(self.lights) > abi.SF_MAX_SCENE_LIGHTS:
+            # Scene::validate (scene/mod.rs:512)
+            raise ValueError(f"a scene may have at most {abi.SF_MAX_SCENE_LIGHTS} lights, got {len(self.lights)}")
         if len(self.lights) > abi.SF_MAX_LIGHTS:
-            raise ValueError("at most 8 lights on the device path")
-        for i, l in enumerate(self.lights):
-            d.lights[i] = l.packed()
-        d.light_count = len(self.lights)
+            # more than the inline array holds: the list replaces it (kept alive with d)
+            table = (abi.sf_area_light * len(self.lights))(*[l.packed() for l in self.lights])
+            d._light_table = table
+            d.light_list = C.cast(table, C.POINTER(abi.sf_area_light))
+            d.light_list_count = len(self.lights)
+        else:
+            for i, l in enumerate(self.lights):
+                d.lights[i] = l.packed()
+            d.light_count = len(self.lights)
         sv = self.material.surface
         if sv is not None:
             d.variation_slot = sv.slot

@@ -10,9 +10,11 @@ It reads, as data:
       -> graph_<name>.json      (nodes, links, safety, bounding_radius_hint)
   scenes/{mandelbox,menger,mandelbulb}.ron
       -> scene_<name>.json      (the scene file as JSON: graph, camera, lights, material)
-  scenes/{eclosion-brume,puits-des-eons}.ron
+  scenes/{eclosion-brume,puits-des-eons}.ron, scenes/showcase/la-cathedrale-des-marees-neons.ron,
+  scenes/studies/cathedrale-des-marees-20261020/etude-neons.ron
       -> scene_<name>.json      (the same, for the reader's material, light and fog
-         fields: finishes with details, projectors and tubes, a texture graph)
+         fields: finishes with details, projectors and tubes, a texture graph; 14
+         and 82 lights, past the descriptor's inline eight)
   crates/syfrack-render/tests/fixtures/parity/{mandelbox,menger,mandelbulb}.exr
       -> film_<name>_blocks.json (the reference's own 640x360, 64-spp render of that
          scene, reduced to what the film gate reads: 8x8 block means of the 8-bit
@@ -51,7 +53,9 @@ def to_json(v):
 
 
 SCENES = ["mandelbox", "menger", "mandelbulb"]
-EXTRA_SCENES = ["eclosion-brume", "puits-des-eons"]  # scene files without a reference render
+# scene files without a reference render (paths under scenes/; fixtures named by the file)
+EXTRA_SCENES = ["eclosion-brume", "puits-des-eons", "showcase/la-cathedrale-des-marees-neons",
+                "studies/cathedrale-des-marees-20261020/etude-neons"]
 
 
 def read_exr(path):
@@ -179,7 +183,7 @@ def main(root):
                        "mean_8bit": [float(x) for x in enc.reshape(-1, 3).mean(0)]}, f)
     for name in EXTRA_SCENES:
         v = ron.load(os.path.join(root, "scenes", f"{name}.ron"))
-        with open(os.path.join(HERE, f"scene_{name}.json"), "w") as f:
+        with open(os.path.join(HERE, f"scene_{os.path.basename(name)}.json"), "w") as f:
             json.dump({"source": f"scenes/{name}.ron", "scene": to_json(v)}, f, indent=0)
     print("wrote", len(NAMES) * 2 + len(SCENES) * 2 + len(EXTRA_SCENES), "files")
 

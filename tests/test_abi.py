@@ -78,7 +78,7 @@ def test_render_config_struct_matches_the_header(lib):
     """sf_render_config at ABI 1.2: the hit epsilon follows samples_per_dispatch."""
     from syfrack_gb300 import abi
 
-    assert lib.sf_abi_version() == (1 << 16) | 5
+    assert lib.sf_abi_version() == (1 << 16) | 6
     assert [f[0] for f in abi.sf_render_config._fields_][-1] == "hit_epsilon"
     assert C.sizeof(abi.sf_render_config) == 10 * 4
     header = open(os.path.join(ROOT, "include", "syfrack_gpu.h")).read()

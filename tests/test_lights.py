@@ -8,7 +8,10 @@ the reference's independent area x line quadrature within 3%
 import numpy as np
 
 from syfrack_gb300.graph import Graph, Kind, Link, Node
-from syfrack_gb300.scene import Camera, Fog, Material, ProjectorLight, RenderConfig, Scene, TubeLight
+import pytest
+
+from syfrack_gb300 import workloads
+from syfrack_gb300.scene import AreaLight, Camera, Fog, Material, ProjectorLight, RenderConfig, Scene, SunLight, TubeLight
 
 
 def minimal(kind):
@@ -79,3 +82,46 @@ def test_projector_beams_in_fog_match_the_quadrature(oracle_mod):
         mean = c[:, ch].mean()
         assert abs(mean / PROJECTOR_QUADRATURE - 1.0) < 0.03, (ch, mean)
         assert c[:, ch].std() / mean < 0.16, (ch, c[:, ch].std() / mean)
+
+
+def compact_scene():
+    """The Mandelbox workload scene lit by an area light, a sun and a tube."""
+    scene = workloads.mandelbox_scene()
+    scene.lights = scene.lights + [SunLight(direction=(-0.4, 0.8, 0.3), intensity=3.0),
+                                   TubeLight(start=(-2.0, 3.0, -2.5), end=(2.0, 3.0, -2.5), radius=0.1, intensity=8.0)]
+    return scene
+
+
+def dark():
+    """An emitter of zero radiance far below the scene (beyond the ray extent): it is
+    never selected for next events (zero weight) and never met by a ray."""
+    return AreaLight(position=(0.0, -5000.0, 0.0), normal=(0.0, -1.0, 0.0), size=(0.1, 0.1), intensity=0.0)
+
+
+def padded_scene():
+    """compact_scene's lights at indices 4, 10 and 11 of twelve: the area light among
+    the eight the descriptor holds inline, the sun and the tube past them."""
+    scene = compact_scene()
+    area, sun, tube = scene.lights
+    scene.lights = [dark() for _ in range(4)] + [area] + [dark() for _ in range(5)] + [sun, tube]
+    return scene
+
+
+def test_a_scene_of_97_lights_is_refused():
+    # Scene::validate (scene/mod.rs:512-514), its test at :971-975
+    scene = workloads.mandelbox_scene()
+    scene.lights = [scene.lights[0]] * 97
+    with pytest.raises(ValueError, match="at most 96 lights"):
+        scene.desc(8, 8)
+    scene.lights = [scene.lights[0]] * 96
+    d = scene.desc(8, 8)
+    assert d.light_count == 0 and d.light_list_count == 96 and d.light_list[95].radiance[0] == 10.0
+
+
+def test_dark_lights_in_front_leave_the_film_unchanged(oracle_mod):
+    w, h, spp = 24, 16, 4
+    pix = [(x, y) for y in range(0, h, 2) for x in range(0, w, 2)]
+    a = oracle_pixels(oracle_mod, compact_scene(), w, h, spp, 3, pixels=pix)
+    b = oracle_pixels(oracle_mod, padded_scene(), w, h, spp, 3, pixels=pix)
+    np.testing.assert_array_equal(a, b)
+    assert a.mean() > 0.01
